@@ -1,0 +1,308 @@
+"""ctypes binding of the C ABI declared in include/eif.h.
+
+``Solver`` wraps one context. The same class binds any library that exports the
+eif.h entry points under a given symbol prefix; the product library uses the
+prefix ``eif_``.
+
+Array conventions follow the reference solver (include/arrays/fluid.h):
+``ux`` has shape (jtot+2, itot+1) and ``uy``, ``p``, ``psi`` have shape
+(jtot+2, itot+2), each row-major with x contiguous; row 0 and row jtot+1 are
+the periodic halo rows. Particle records have EIF_NFIELDS = 30 doubles in the
+order of the reference's ``particle_t`` (include/suspensions.h:8-31).
+"""
+import ctypes
+
+import numpy as np
+
+NFIELDS = 30
+PREC_FP64 = 0
+PREC_MIXED = 1
+
+ERRORS = {
+    -1: "invalid argument",
+    -2: "CUDA error",
+    -3: "iteration cap reached",
+    -4: "out of memory",
+    -5: "call out of order",
+    -6: "non-finite velocity",
+}
+
+# particle record fields (include/eif.h enum eif_particle_field)
+FIELDS = ("den a b x y az dx dy daz ux uy vz dux duy dvz fux fuy tvz "
+          "iux0 iux1 iuy0 iuy1 ivz0 ivz1 cfx0 cfx1 cfy0 cfy1 ctz0 ctz1").split()
+F = {name: k for k, name in enumerate(FIELDS)}
+
+
+class EifError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s (%d): %s" % (ERRORS.get(code, "error"), code, msg))
+        self.code = code
+
+
+class Config(ctypes.Structure):
+    """eif_config_t (include/eif.h)."""
+
+    _fields_ = [
+        ("itot", ctypes.c_int),
+        ("jtot", ctypes.c_int),
+        ("ly", ctypes.c_double),
+        ("Re", ctypes.c_double),
+        ("Fr", ctypes.c_double),
+        ("extfrcy", ctypes.c_double),
+        ("safefactors", ctypes.c_double * 3),
+        ("uy_wall", ctypes.c_double * 2),
+        ("precision", ctypes.c_int),
+        ("device", ctypes.c_int),
+    ]
+
+
+def make_config(itot, jtot, ly=1.0, Re=2334.0, Fr=np.finfo(np.float64).max, extfrcy=0.0,
+                safefactors=(0.75, 0.75, 0.95), uy_wall=(0.0, 0.0), precision=PREC_FP64, device=0):
+    cfg = Config()
+    cfg.itot, cfg.jtot, cfg.ly = itot, jtot, ly
+    cfg.Re, cfg.Fr, cfg.extfrcy = Re, Fr, extfrcy
+    for k in range(3):
+        cfg.safefactors[k] = safefactors[k]
+    cfg.uy_wall[0], cfg.uy_wall[1] = uy_wall
+    cfg.precision = precision
+    cfg.device = device
+    return cfg
+
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+_vp = ctypes.c_void_p
+
+
+def bind(lib, prefix):
+    """Declare argument types of every eif.h entry point present in ``lib``."""
+    sigs = {
+        "create": [ctypes.POINTER(Config), ctypes.POINTER(_vp)],
+        "destroy": [_vp],
+        "synchronize": [_vp],
+        "push_fluid": [_vp, _dp, _dp, _dp],
+        "pull_fluid": [_vp, _dp, _dp, _dp, _dp],
+        "push_particles": [_vp, ctypes.c_int, _dp],
+        "pull_particles": [_vp, ctypes.c_int, _dp],
+        "pull_src": [_vp, _dp, _dp, _dp, _dp],
+        "push_src": [_vp, _dp, _dp],
+        "pull_ibm_fields": [_vp, _dp, _dp],
+        "decide_dt": [_vp, _dp],
+        "set_dt": [_vp, ctypes.c_double],
+        "get_dt": [_vp, _dp],
+        "integrate": [_vp, _ip],
+        "advance": [_vp, ctypes.c_int],
+        "get_time": [_vp, _ip, _dp],
+        "set_time": [_vp, ctypes.c_int, ctypes.c_double],
+        "update_boundaries": [_vp],
+        "reset_particle_increments": [_vp],
+        "compute_inertia": [_vp, ctypes.c_int],
+        "update_velocity": [_vp, ctypes.c_int],
+        "exchange_momentum": [_vp],
+        "update_momentum_field": [_vp],
+        "compute_potential": [_vp, ctypes.c_int],
+        "correct_velocity": [_vp, ctypes.c_int],
+        "update_pressure": [_vp],
+        "compute_collision_force": [_vp, ctypes.c_int],
+        "increment_particles": [_vp, ctypes.c_int, _dp],
+        "update_particles": [_vp],
+        "divergence": [_vp, _dp, _dp],
+        "set_threads": [_vp, ctypes.c_int],
+    }
+    for name, args in sigs.items():
+        fn = getattr(lib, prefix + name, None)
+        if fn is not None:
+            fn.argtypes = args
+            fn.restype = ctypes.c_int
+    le = getattr(lib, prefix + "last_error")
+    le.argtypes = [_vp]
+    le.restype = ctypes.c_char_p
+    st = getattr(lib, prefix + "stream", None)
+    if st is not None:
+        st.argtypes = [_vp]
+        st.restype = _vp
+    return lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(_dp)
+
+
+class Solver:
+    """One solver context behind the eif.h C ABI."""
+
+    def __init__(self, lib, prefix, cfg):
+        self.lib, self.prefix, self.cfg = lib, prefix, cfg
+        self.itot, self.jtot = cfg.itot, cfg.jtot
+        self.n_particles = 0
+        self.ctx = _vp()
+        self._call("create", ctypes.byref(cfg), ctypes.byref(self.ctx))
+
+    # ---- plumbing ----
+    def _fn(self, name):
+        return getattr(self.lib, self.prefix + name)
+
+    def _call(self, name, *args):
+        rc = self._fn(name)(*args)
+        if rc != 0:
+            msg = self._fn("last_error")(self.ctx) if self.ctx else b""
+            raise EifError(rc, (msg or b"").decode(errors="replace"))
+        return rc
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            self._fn("destroy")(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # ---- shapes ----
+    def shapes(self):
+        return (self.jtot + 2, self.itot + 1), (self.jtot + 2, self.itot + 2)
+
+    # ---- state transfer ----
+    def push_fluid(self, ux, uy, p):
+        sx, sy = self.shapes()
+        ux = np.ascontiguousarray(ux, dtype=np.float64)
+        uy = np.ascontiguousarray(uy, dtype=np.float64)
+        p = np.ascontiguousarray(p, dtype=np.float64)
+        if ux.shape != sx or uy.shape != sy or p.shape != sy:
+            raise ValueError("field shapes must be %s and %s" % (sx, sy))
+        self._call("push_fluid", self.ctx, _ptr(ux), _ptr(uy), _ptr(p))
+
+    def pull_fluid(self):
+        sx, sy = self.shapes()
+        ux, uy, p, psi = np.empty(sx), np.empty(sy), np.empty(sy), np.empty(sy)
+        self._call("pull_fluid", self.ctx, _ptr(ux), _ptr(uy), _ptr(p), _ptr(psi))
+        return ux, uy, p, psi
+
+    def push_particles(self, records):
+        records = np.ascontiguousarray(records, dtype=np.float64).reshape(-1, NFIELDS)
+        self.n_particles = records.shape[0]
+        buf = records if records.size else np.zeros(NFIELDS)
+        self._call("push_particles", self.ctx, self.n_particles, _ptr(buf))
+
+    def pull_particles(self):
+        out = np.zeros((max(self.n_particles, 1), NFIELDS))
+        self._call("pull_particles", self.ctx, self.n_particles, _ptr(out))
+        return out[: self.n_particles]
+
+    def pull_src(self):
+        nx = (self.jtot, self.itot - 1)
+        ny = (self.jtot, self.itot)
+        arrs = [np.empty(nx), np.empty(nx), np.empty(ny), np.empty(ny)]
+        self._call("pull_src", self.ctx, *[_ptr(a) for a in arrs])
+        return arrs
+
+    def push_src(self, uxa, uya):
+        uxa = np.ascontiguousarray(uxa, dtype=np.float64)
+        uya = np.ascontiguousarray(uya, dtype=np.float64)
+        self._call("push_src", self.ctx, _ptr(uxa), _ptr(uya))
+
+    def pull_ibm_fields(self):
+        _, sy = self.shapes()
+        dux, duy = np.empty(sy), np.empty(sy)
+        self._call("pull_ibm_fields", self.ctx, _ptr(dux), _ptr(duy))
+        return dux, duy
+
+    # ---- stepping ----
+    def decide_dt(self):
+        v = ctypes.c_double()
+        self._call("decide_dt", self.ctx, ctypes.byref(v))
+        return v.value
+
+    @property
+    def dt(self):
+        v = ctypes.c_double()
+        self._call("get_dt", self.ctx, ctypes.byref(v))
+        return v.value
+
+    @dt.setter
+    def dt(self, value):
+        self._call("set_dt", self.ctx, float(value))
+
+    def integrate(self):
+        sub = (ctypes.c_int * 3)()
+        self._call("integrate", self.ctx, sub)
+        return list(sub)
+
+    def step(self):
+        """decide_dt + integrate + counters, returning the sub-iteration counts."""
+        self.decide_dt()
+        sub = self.integrate()
+        step, time = self.time_state()
+        self._call("set_time", self.ctx, step + 1, time + self.dt)
+        return sub
+
+    def advance(self, nsteps):
+        self._call("advance", self.ctx, int(nsteps))
+
+    def time_state(self):
+        s, t = ctypes.c_int(), ctypes.c_double()
+        self._call("get_time", self.ctx, ctypes.byref(s), ctypes.byref(t))
+        return s.value, t.value
+
+    def set_time(self, step, time):
+        self._call("set_time", self.ctx, int(step), float(time))
+
+    def synchronize(self):
+        fn = getattr(self.lib, self.prefix + "synchronize", None)
+        if fn is not None:
+            self._call("synchronize", self.ctx)
+
+    def set_threads(self, n):
+        self._call("set_threads", self.ctx, int(n))
+
+    def divergence(self):
+        mx, sm = ctypes.c_double(), ctypes.c_double()
+        self._call("divergence", self.ctx, ctypes.byref(mx), ctypes.byref(sm))
+        return mx.value, sm.value
+
+    # ---- stage-level entry points ----
+    def update_boundaries(self):
+        self._call("update_boundaries", self.ctx)
+
+    def reset_particle_increments(self):
+        self._call("reset_particle_increments", self.ctx)
+
+    def compute_inertia(self, cnstep):
+        self._call("compute_inertia", self.ctx, int(cnstep))
+
+    def update_velocity(self, rkstep):
+        self._call("update_velocity", self.ctx, int(rkstep))
+
+    def exchange_momentum(self):
+        self._call("exchange_momentum", self.ctx)
+
+    def update_momentum_field(self):
+        self._call("update_momentum_field", self.ctx)
+
+    def compute_potential(self, rkstep):
+        self._call("compute_potential", self.ctx, int(rkstep))
+
+    def correct_velocity(self, rkstep):
+        self._call("correct_velocity", self.ctx, int(rkstep))
+
+    def update_pressure(self):
+        self._call("update_pressure", self.ctx)
+
+    def compute_collision_force(self, cnstep):
+        self._call("compute_collision_force", self.ctx, int(cnstep))
+
+    def increment_particles(self, rkstep):
+        r = ctypes.c_double()
+        self._call("increment_particles", self.ctx, int(rkstep), ctypes.byref(r))
+        return r.value
+
+    def update_particles(self):
+        self._call("update_particles", self.ctx)

@@ -1,0 +1,140 @@
+/*
+ * EllipsesInFlows-GB300: C ABI of the time-step hot path.
+ *
+ * The reference solver (NaokiHori/EllipsesInFlows) advances its state with
+ *     param_decide_dt(param, parallel, fluid, suspensions);   src/param/decide_dt.c:11
+ *     integrate(param, parallel, fluid, suspensions);         src/main.c:13-55
+ * inside its main loop (src/main.c:69-101). This library replaces those two calls.
+ * The caller keeps its own host arrays in the reference's haloed layouts
+ * (include/arrays/fluid.h:13-43) and its particle_t records
+ * (include/suspensions.h:8-31); it pushes them once, steps on the GPU, and
+ * pulls them back before logging / saving / statistics.
+ *
+ * Every function returns EIF_OK (0) or a negative error code; eif_last_error()
+ * gives the message. A context owns one CUDA stream on one device and is not
+ * thread-safe. All functions that take host arrays are synchronous with respect
+ * to those arrays.
+ */
+#ifndef EIF_H
+#define EIF_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- error codes ---- */
+#define EIF_OK 0
+#define EIF_ERR_ARG (-1)      /* invalid argument (sizes, null pointers, stage index) */
+#define EIF_ERR_CUDA (-2)     /* a CUDA runtime call failed */
+#define EIF_ERR_NOCONV (-3)   /* an iteration cap was hit on the device (circle fit) */
+#define EIF_ERR_NOMEM (-4)    /* device or host allocation failed */
+#define EIF_ERR_STATE (-5)    /* call out of order (e.g. step before push) */
+#define EIF_ERR_NONFINITE (-6)/* a NaN/Inf was found in the velocity field */
+
+/* ---- arithmetic of the step ---- */
+#define EIF_PREC_FP64 0       /* every operation in double precision */
+#define EIF_PREC_MIXED 1      /* stencils / indicator / IBM forcing in float; storage,
+                                 Poisson tridiagonal solves and particle dynamics in double */
+
+/*
+ * Particle record: 30 doubles in the field order of the reference's particle_t
+ * (include/suspensions.h:8-31), so that a particle_t* can be passed as a double*.
+ */
+#define EIF_NFIELDS 30
+enum eif_particle_field {
+  EIF_P_DEN = 0, EIF_P_A = 1, EIF_P_B = 2,
+  EIF_P_X = 3, EIF_P_Y = 4, EIF_P_AZ = 5,
+  EIF_P_DX = 6, EIF_P_DY = 7, EIF_P_DAZ = 8,
+  EIF_P_UX = 9, EIF_P_UY = 10, EIF_P_VZ = 11,
+  EIF_P_DUX = 12, EIF_P_DUY = 13, EIF_P_DVZ = 14,
+  EIF_P_FUX = 15, EIF_P_FUY = 16, EIF_P_TVZ = 17,
+  EIF_P_IUX0 = 18, EIF_P_IUX1 = 19, EIF_P_IUY0 = 20, EIF_P_IUY1 = 21,
+  EIF_P_IVZ0 = 22, EIF_P_IVZ1 = 23,
+  EIF_P_CFX0 = 24, EIF_P_CFX1 = 25, EIF_P_CFY0 = 26, EIF_P_CFY1 = 27,
+  EIF_P_CTZ0 = 28, EIF_P_CTZ1 = 29
+};
+
+/*
+ * Run configuration. Mirrors the scalar members of the reference's param_t
+ * (include/param.h:24-48) that the step reads, as loaded from the environment
+ * by load_config (src/param/init.c:67-103). lx is fixed to 1 (include/param.h:14).
+ * uy_wall is new: the reference selects moving walls by swapping
+ * src/fluid/boundary_conditions.c for the Couette variant
+ * (docs/source/examples/case1/config/src_fluid_boundary_conditions.c:39-40).
+ */
+typedef struct {
+  int itot, jtot;            /* cells in x (wall-normal, walls at x=0,1) and y (periodic) */
+  double ly;                 /* domain length in y */
+  double Re, Fr;             /* Reynolds and Froude numbers (Fr = DBL_MAX: no buoyancy) */
+  double extfrcy;            /* uniform body force in y (pressure-gradient driving) */
+  double safefactors[3];     /* advective, diffusive, particle dt safety factors */
+  double uy_wall[2];         /* y-velocity of the walls at x=0 and x=1 */
+  int precision;             /* EIF_PREC_FP64 or EIF_PREC_MIXED */
+  int device;                /* CUDA device ordinal */
+} eif_config_t;
+
+typedef struct eif_ctx eif_ctx;
+
+/* ---- lifetime ---- */
+int eif_create(const eif_config_t *cfg, eif_ctx **ctx);
+int eif_destroy(eif_ctx *ctx);
+const char *eif_last_error(const eif_ctx *ctx);
+int eif_synchronize(eif_ctx *ctx);
+/* the context's CUDA stream (a cudaStream_t), for callers that enqueue around it */
+void *eif_stream(eif_ctx *ctx);
+
+/* ---- state transfer (host arrays in the reference layouts) ----
+ * ux:  (jtot+2) rows of (itot+1) doubles, UX(i,j) = ux[j*(itot+1)+(i-1)]
+ * uy, p, psi: (jtot+2) rows of (itot+2) doubles, UY(i,j) = uy[j*(itot+2)+i]
+ * Halo rows and wall columns are recomputed on push, as fluid_init does
+ * (src/fluid/init.c:51,69,83). */
+int eif_push_fluid(eif_ctx *ctx, const double *ux, const double *uy, const double *p);
+int eif_pull_fluid(eif_ctx *ctx, double *ux, double *uy, double *p, double *psi);
+/* records: n * EIF_NFIELDS doubles; n may change between pushes */
+int eif_push_particles(eif_ctx *ctx, int n, const double *records);
+int eif_pull_particles(eif_ctx *ctx, int n, double *records);
+/* RK source terms: explicit part of the current (a) and previous (b) stage,
+ * ux-like arrays of (itot-1)*jtot, uy-like of itot*jtot (include/arrays/fluid.h:53-103) */
+int eif_pull_src(eif_ctx *ctx, double *srcuxa, double *srcuxb, double *srcuya, double *srcuyb);
+int eif_push_src(eif_ctx *ctx, const double *srcuxa, const double *srcuya);
+/* IBM response fields dux, duy (include/arrays/suspensions.h:13-23), uy-like layout */
+int eif_pull_ibm_fields(eif_ctx *ctx, double *dux, double *duy);
+
+/* ---- time stepping ---- */
+/* param_decide_dt (src/param/decide_dt.c:11-81); the result stays on the device
+ * for the following integrate and is also returned in *dt (synchronising) if dt != NULL */
+int eif_decide_dt(eif_ctx *ctx, double *dt);
+int eif_set_dt(eif_ctx *ctx, double dt);
+int eif_get_dt(eif_ctx *ctx, double *dt);
+/* integrate (src/main.c:13-55): three RK stages with the particle fixed point;
+ * substeps[3] (may be NULL) receives the sub-iteration count of each stage */
+int eif_integrate(eif_ctx *ctx, int *substeps);
+/* nsteps times { decide_dt; integrate; step += 1; time += dt } without host
+ * synchronisation between steps (src/main.c:71-77) */
+int eif_advance(eif_ctx *ctx, int nsteps);
+/* step counter and simulated time accumulated by eif_advance */
+int eif_get_time(eif_ctx *ctx, int *step, double *time);
+int eif_set_time(eif_ctx *ctx, int step, double time);
+
+/* ---- stage-level entry points, one per reference function ---- */
+int eif_update_boundaries(eif_ctx *ctx);                              /* src/fluid/boundary_conditions.c:7-62 */
+int eif_reset_particle_increments(eif_ctx *ctx);                      /* src/suspensions/reset.c:7-18 */
+int eif_compute_inertia(eif_ctx *ctx, int cnstep);                    /* src/suspensions/inertia.c:96-102 */
+int eif_update_velocity(eif_ctx *ctx, int rkstep);                    /* src/fluid/update_velocity.c:229-237 */
+int eif_exchange_momentum(eif_ctx *ctx);                              /* src/suspensions/exchange.c:114-120 */
+int eif_update_momentum_field(eif_ctx *ctx);                          /* src/suspensions/update.c:36-59 */
+int eif_compute_potential(eif_ctx *ctx, int rkstep);                  /* src/fluid/compute_potential.c:48-138 */
+int eif_correct_velocity(eif_ctx *ctx, int rkstep);                   /* src/fluid/correct_velocity.c:6-42 */
+int eif_update_pressure(eif_ctx *ctx);                                /* src/fluid/update_pressure.c:7-24 */
+int eif_compute_collision_force(eif_ctx *ctx, int cnstep);            /* src/suspensions/collision.c:306-367 */
+int eif_increment_particles(eif_ctx *ctx, int rkstep, double *residual); /* src/suspensions/increment.c:66-72 */
+int eif_update_particles(eif_ctx *ctx);                               /* src/suspensions/update.c:61-65 */
+
+/* ---- diagnostics (src/logging.c:40-80) ---- */
+int eif_divergence(eif_ctx *ctx, double *divmax, double *divsum);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* EIF_H */
