@@ -1,0 +1,344 @@
+"""Benchmark: cell-steps/s of the EllipsesInFlows time step on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--precision fp64|mixed] [--workload NAME]
+
+One step is one full time step of the solver (dt decision + three RK stages
+with the immersed-boundary exchange, the pressure projection, collisions and
+the particle fixed point), i.e. src/main.c:71-77 of the reference. The metric
+is cells x steps / wall time of the timed steps. The default workload is the
+2048 x 4096 grid with 2048 ellipses (aspect ratio U[1,3], density ratio
+U[1,1.2], Re 400, seeded placement); inputs are synthetic.
+
+--impl ours        the CUDA library through its C ABI (value: device-timed
+                   steps with the state resident in HBM; e2e: the same steps
+                   with the state copied host->device before and device->host
+                   after every step through the public API).
+--impl reference   the CPU restatement of the reference algorithm
+                   (oracle/port, OpenMP over all host threads) on the same
+                   workload; reported as the reference arm.
+
+Under torchrun with N > 1 every rank advances an independent replica on its
+own GPU (the path has no data exchange between suspensions); value is the
+sum over ranks, timed as the maximum over ranks.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+MEASURED = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+
+# Algorithmic DRAM bytes per cell for one launch of each streaming kernel
+# (double precision storage; read + write of every field the kernel touches once).
+#   predictor: R ux uy p srcB_x srcB_y, W srcA_x srcA_y ux' uy'       9 words
+#   correct:   R ux uy dux duy psi p, W ux uy p                        9 words
+#   dct2:      R ux uy dux duy, W qhat                                 5 words
+#   tdm:       R qhat, W qhat                                          2 words
+#   dct3:      R qhat, W psi                                           2 words
+#   decide_dt: R ux uy                                                 2 words
+#   gather:    W dux duy                                               2 words
+HBM_WORDS = {"predictor": 9, "correct": 9, "poisson_dct2": 5, "poisson_tdm": 2, "poisson_dct3": 2,
+             "decide_dt": 2, "ibm_gather": 2}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--workload", default="mixed_target", choices=["mixed_target", "poiseuille", "couette_circle"])
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def make_case(name):
+    from ellipsesinflows_gb300 import cases
+    return cases.CONFIGS[name]()
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for k, name in enumerate(names):
+                if parts[5 + k].lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(MEASURED) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def dist_init(gpus):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if os.environ.get("EIF_BENCH_BACKEND", "nccl") == "nccl" else "gloo"
+        dist.init_process_group(backend=backend)
+        pg = dist
+    return world, rank, local, pg
+
+
+def barrier(pg, device=None):
+    if pg is not None:
+        if device is not None:
+            pg.barrier(device_ids=[device])
+        else:
+            pg.barrier()
+
+
+def max_over_ranks(pg, value, device):
+    if pg is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device="cuda:%d" % device if device is not None else "cpu")
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_ours(args, world, rank, local, pg):
+    import torch
+    from ellipsesinflows_gb300 import PREC_FP64, PREC_MIXED, Simulation, build
+    build.build()
+    torch.cuda.set_device(local)
+    case = make_case(args.workload)
+    prec = PREC_MIXED if args.precision == "mixed" else PREC_FP64
+    sim = Simulation.from_case(case, precision=prec, device=local)
+    stream = torch.cuda.ExternalStream(sim._fn("stream")(sim.ctx), device=local)
+    for _ in range(args.warmup):
+        sim.advance(1)
+    sim.synchronize()
+    # ---- device-timed region: state resident in HBM ----
+    sim._call("profile_reset", sim.ctx)
+    sim._call("profile_enable", sim.ctx, 1)
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier(pg, local)
+        torch.cuda.synchronize()
+        start.record(stream)
+        sim.advance(args.steps)
+        stop.record(stream)
+        torch.cuda.synchronize()
+        barrier(pg, local)
+    sim._call("profile_enable", sim.ctx, 0)
+    ms = start.elapsed_time(stop)
+    ms = max_over_ranks(pg, ms, local)
+    prof = profile_entries(sim)
+    # ---- end-to-end through the public API with host buffers ----
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(sim, case, args.steps, pg, local)
+    cells = case.cells
+    value = world * cells * args.steps / (ms / 1e3)
+    hbm, hbm_src = peaks()
+    roof = roofline(prof, cells, hbm, hbm_src)
+    launches = sum(e["launches"] for e in prof)
+    out = {
+        "metric": "cell-steps/s", "value": value, "unit": "cell-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if prec == PREC_FP64 else "f32+f64",
+        "data": "synthetic (seeded ellipse placement, fluid at rest)",
+        "config": {"workload": case.name, "itot": case.itot, "jtot": case.jtot, "n_particles": case.n_particles,
+                   "Re": case.Re, "precision": args.precision,
+                   "l2": "inputs larger than L2 (~1 GB of device state per step)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "e2e": e2e, "roofline": roof, "gpu_launches": launches,
+        "clocks": clk.summary(),
+        "kernels": {e["name"]: {"launches": e["launches"], "ms": round(e["ms"], 4)} for e in prof},
+    }
+    if rank == 0 and world == 1:
+        out["cpu_baseline"] = cpu_baseline(args, case)
+    return out, rank
+
+
+def profile_entries(sim):
+    import ctypes
+    n = ctypes.c_int()
+    sim._call("profile_count", sim.ctx, ctypes.byref(n))
+    fn = sim._fn("profile_get")
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_char_p, ctypes.c_int,
+                   ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_double)]
+    out = []
+    for k in range(n.value):
+        name = ctypes.create_string_buffer(64)
+        launches, ms = ctypes.c_longlong(), ctypes.c_double()
+        fn(sim.ctx, k, name, 64, ctypes.byref(launches), ctypes.byref(ms))
+        out.append({"name": name.value.decode(), "launches": launches.value, "ms": ms.value})
+    out.sort(key=lambda e: -e["ms"])
+    return out
+
+
+def roofline(prof, cells, hbm, hbm_src):
+    """Roofline of the dominant streaming kernel against the measured copy bandwidth."""
+    total = sum(e["ms"] for e in prof) or 1.0
+    stream = [e for e in prof if e["name"] in HBM_WORDS and e["launches"] > 0]
+    if not stream:
+        return None
+    top = stream[0]
+    per_launch_ms = top["ms"] / top["launches"]
+    bytes_per_launch = HBM_WORDS[top["name"]] * 8.0 * cells
+    achieved = bytes_per_launch / (per_launch_ms / 1e3) / 1e9
+    dominant = prof[0]
+    return {"bound": "hbm", "kernel": top["name"], "achieved": achieved, "peak": hbm, "unit": "GB/s",
+            "frac": achieved / hbm, "peak_source": hbm_src, "traffic": None,
+            "algorithmic_bytes_per_launch": bytes_per_launch, "share_of_step": top["ms"] / total,
+            "dominant_kernel": dominant["name"], "dominant_share": dominant["ms"] / total}
+
+
+def run_e2e(sim, case, steps, pg, device):
+    """Every step: host->device copy of the state, one step, device->host copy of the result."""
+    import torch
+    from ellipsesinflows_gb300.capi import NFIELDS
+    ux, uy, p, _ = sim.pull_fluid()
+    parts = sim.pull_particles()
+    pin = lambda a: torch.from_numpy(a).pin_memory().numpy()  # noqa: E731
+    hux, huy, hp, hpsi = pin(ux), pin(uy), pin(p), pin(np.zeros_like(p))
+    hpart = pin(parts)
+    h2d = hux.nbytes + huy.nbytes + hp.nbytes + hpart.nbytes
+    d2h = hux.nbytes + huy.nbytes + hp.nbytes + hpsi.nbytes + hpart.nbytes
+    barrier(pg, device)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        sim.push_fluid(hux, huy, hp)
+        sim.push_particles(hpart)
+        sim.advance(1)
+        r = sim.pull_fluid()
+        hux[...], huy[...], hp[...], hpsi[...] = r
+        hpart[...] = sim.pull_particles()
+    el = time.perf_counter() - t0
+    el = max_over_ranks(pg, el, device)
+    world = pg.get_world_size() if pg is not None else 1
+    return {"value": world * case.cells * steps / el, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": d2h, "n_particle_fields": NFIELDS}
+
+
+def cpu_baseline(args, case):
+    """The CPU restatement on the host cores, on a bounded sample: one time step of the workload."""
+    from oracle import port
+    threads = os.cpu_count() or 1
+    s = port.PortSolver(case.config(), threads=threads)
+    s.push_fluid(*case.fluid())
+    s.push_particles(case.particles)
+    t0 = time.perf_counter()
+    s.step()
+    el = time.perf_counter() - t0
+    return {"value": case.cells / el, "unit": "cell-steps/s", "cores": threads, "kind": "port",
+            "sample": "1 time step of the full %s workload from its initial state" % case.name}
+
+
+def run_reference(args, world, rank):
+    """Reference arm: the CPU restatement of the reference algorithm on all host threads."""
+    if rank != 0:
+        return None, rank
+    from oracle import port
+    case = make_case(args.workload)
+    threads = os.cpu_count() or 1
+    s = port.PortSolver(case.config(), threads=threads)
+    s.push_fluid(*case.fluid())
+    s.push_particles(case.particles)
+    # bounded sample: each timed step is one full time step of the workload
+    warm = min(args.warmup, 1)
+    steps = max(1, min(args.steps, 2))
+    for _ in range(warm):
+        s.step()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        s.step()
+    el = time.perf_counter() - t0
+    value = case.cells * steps / el
+    sample = "%d timed + %d warm-up full time steps of %s (cap of 2 timed steps keeps the CPU run bounded)" % (
+        steps, warm, case.name)
+    out = {"metric": "cell-steps/s", "value": value, "unit": "cell-steps/s", "n_gpus": world, "steps": steps,
+           "warmup": warm, "ms_per_step": 1e3 * el / steps, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded ellipse placement, fluid at rest)",
+           "config": {"workload": case.name, "itot": case.itot, "jtot": case.jtot, "n_particles": case.n_particles,
+                      "Re": case.Re, "precision": "fp64"},
+           "impl": "reference",
+           "cpu_baseline": {"value": value, "unit": "cell-steps/s", "cores": threads, "kind": "port",
+                            "sample": sample},
+           "e2e": {"value": value, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    return out, rank
+
+
+def main():
+    args = parse()
+    world, rank, local, pg = dist_init(args.gpus)
+    if args.impl == "reference":
+        out, rank = run_reference(args, world, rank)
+    else:
+        out, rank = run_ours(args, world, rank, local, pg)
+    if rank == 0 and out is not None:
+        print(json.dumps(out), flush=True)
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

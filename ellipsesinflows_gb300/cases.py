@@ -1,0 +1,174 @@
+"""Initial states of the benchmark configurations.
+
+A ``Case`` holds the run parameters (the environment variables of the
+reference's load_config, src/param/init.c:67-103, plus the wall velocities),
+the initial fluid fields in the reference's haloed layouts and the particle
+records. Particle placement is a seeded random sequential addition with the
+bounding-circle clearance test; the reference's own generator
+(initparticles/RandomGenerator/src/main.c) uses C rand() with hard-coded
+sizes, so seeds here do not reproduce its layouts.
+"""
+import math
+
+import numpy as np
+
+from .capi import F, NFIELDS, PREC_FP64, make_config
+
+DBL_MAX = float(np.finfo(np.float64).max)
+
+
+class Case:
+    def __init__(self, name, itot, jtot, ly, Re, extfrcy=0.0, Fr=DBL_MAX, safefactors=(0.75, 0.75, 0.95),
+                 uy_wall=(0.0, 0.0), particles=None, couette_init=False, steps=1):
+        self.name, self.itot, self.jtot, self.ly = name, itot, jtot, ly
+        self.Re, self.extfrcy, self.Fr = Re, extfrcy, Fr
+        self.safefactors, self.uy_wall = tuple(safefactors), tuple(uy_wall)
+        self.particles = np.zeros((0, NFIELDS)) if particles is None else np.asarray(particles, dtype=np.float64)
+        self.couette_init = couette_init
+        self.steps = steps
+
+    @property
+    def n_particles(self):
+        return self.particles.shape[0]
+
+    @property
+    def cells(self):
+        return self.itot * self.jtot
+
+    def config(self, precision=PREC_FP64, device=0):
+        return make_config(self.itot, self.jtot, ly=self.ly, Re=self.Re, Fr=self.Fr, extfrcy=self.extfrcy,
+                           safefactors=self.safefactors, uy_wall=self.uy_wall, precision=precision, device=device)
+
+    def xc(self):
+        """Cell-centre x coordinates XC(0..itot+1) as set_coordinate computes them."""
+        it = self.itot
+        dx = 1.0 / it
+        xf = np.array([1.0 * (i - 1) * dx for i in range(1, it + 2)])
+        xf[0], xf[it] = 0.0, 1.0
+        xc = np.empty(it + 2)
+        xc[0] = xf[0]
+        xc[1:it + 1] = 0.5 * (xf[:it] + xf[1:it + 1])
+        xc[it + 1] = xf[it]
+        return xc
+
+    def fluid(self):
+        """(ux, uy, p) initial fields, haloed reference layouts."""
+        it, jt = self.itot, self.jtot
+        ux = np.zeros((jt + 2, it + 1))
+        uy = np.zeros((jt + 2, it + 2))
+        p = np.zeros((jt + 2, it + 2))
+        if self.couette_init:
+            # docs/source/examples/case1/config/src_fluid_init.c:59-66
+            uy[:, 1:it + 1] = -0.5 + self.xc()[1:it + 1][None, :]
+        return ux, uy, p
+
+
+def particle_records(den, a, b, x, y, az, ux=None, uy=None, vz=None):
+    n = len(den)
+    rec = np.zeros((n, NFIELDS))
+    rec[:, F["den"]], rec[:, F["a"]], rec[:, F["b"]] = den, a, b
+    rec[:, F["x"]], rec[:, F["y"]], rec[:, F["az"]] = x, y, az
+    if ux is not None:
+        rec[:, F["ux"]] = ux
+    if uy is not None:
+        rec[:, F["uy"]] = uy
+    if vz is not None:
+        rec[:, F["vz"]] = vz
+    return rec
+
+
+def place(n, radius, ly, clearance, rng, xmargin, max_tries=2_000_000):
+    """Random sequential addition of n centres with pairwise distance >= r_i + r_j + clearance
+    (periodic in y, centres kept xmargin + r_i away from the walls)."""
+    radius = np.broadcast_to(np.asarray(radius, dtype=np.float64), (n,)).copy()
+    rmax = float(radius.max())
+    cell = 2 * rmax + clearance
+    ncy = max(1, int(ly // cell))
+    ncx = max(1, int(1.0 // cell))
+    grid = {}
+    xs, ys = np.empty(n), np.empty(n)
+    placed, tries = 0, 0
+    while placed < n:
+        tries += 1
+        if tries > max_tries:
+            raise RuntimeError("could not place %d particles (placed %d)" % (n, placed))
+        r = radius[placed]
+        x = rng.uniform(r + xmargin, 1.0 - r - xmargin)
+        y = rng.uniform(0.0, ly)
+        cx, cy = min(int(x / (1.0 / ncx)), ncx - 1), min(int(y / (ly / ncy)), ncy - 1)
+        ok = True
+        for dxc in (-1, 0, 1):
+            for dyc in (-1, 0, 1):
+                for k in grid.get((cx + dxc, (cy + dyc) % ncy), ()):
+                    ddy = abs(ys[k] - y)
+                    ddy = min(ddy, ly - ddy)
+                    if math.hypot(xs[k] - x, ddy) < r + radius[k] + clearance:
+                        ok = False
+                        break
+                if not ok:
+                    break
+            if not ok:
+                break
+        if ok:
+            xs[placed], ys[placed] = x, y
+            grid.setdefault((cx, cy), []).append(placed)
+            placed += 1
+    return xs, ys
+
+
+def couette_circle(itot=64, jtot=128, steps=200):
+    """Single neutrally buoyant circle in Couette flow (lateral migration, case1)."""
+    rec = particle_records([1.0], [0.125], [0.125], [0.3], [1.0], [0.0])
+    return Case("couette_circle_%dx%d" % (itot, jtot), itot, jtot, 2.0, 100.0, safefactors=(0.4, 0.4, 0.95),
+                uy_wall=(-0.5, 0.5), particles=rec, couette_init=True, steps=steps)
+
+
+def poiseuille(itot=512, jtot=1024, n=128, a=0.04, b=0.02, Re=200.0, seed=0, steps=1000):
+    """Plane Poiseuille suspension of identical ellipses, fluid at rest, extfrcy = 8/Re."""
+    rng = np.random.default_rng(seed)
+    dx = 1.0 / itot
+    xs, ys = place(n, a, 2.0, dx, rng, dx)
+    az = rng.uniform(0.0, math.pi, n)
+    rec = particle_records(np.ones(n), np.full(n, a), np.full(n, b), xs, ys, az)
+    return Case("poiseuille_%dx%d_n%d" % (itot, jtot, n), itot, jtot, 2.0, Re, extfrcy=8.0 / Re, particles=rec,
+                steps=steps)
+
+
+def mixed_target(itot=2048, jtot=4096, n=2048, a=0.012, Re=400.0, seed=1, steps=500):
+    """Dense suspension of ellipses with aspect ratio U[1,3] and density ratio U[1,1.2]."""
+    rng = np.random.default_rng(seed)
+    dx = 1.0 / itot
+    xs, ys = place(n, a, 2.0, dx, rng, dx)
+    ar = rng.uniform(1.0, 3.0, n)
+    den = rng.uniform(1.0, 1.2, n)
+    az = rng.uniform(0.0, math.pi, n)
+    rec = particle_records(den, np.full(n, a), a / ar, xs, ys, az)
+    return Case("suspension_%dx%d_n%d" % (itot, jtot, n), itot, jtot, 2.0, Re, extfrcy=8.0 / Re, particles=rec,
+                steps=steps)
+
+
+def contact_cluster(itot=64, jtot=128, seed=7):
+    """Small case with ellipses overlapping tip to tip, across the periodic
+    boundary and into a wall, so that every branch of the collision model is
+    exercised from the first step."""
+    rng = np.random.default_rng(seed)
+    den = [1.0, 1.1, 1.0, 1.05, 1.0, 1.0]
+    a = [0.10, 0.09, 0.08, 0.10, 0.07, 0.06]
+    b = [0.05, 0.06, 0.04, 0.10, 0.035, 0.03]
+    x = [0.30, 0.485, 0.60, 0.15, 0.935, 0.60]
+    y = [1.00, 1.01, 1.90, 1.50, 0.60, 0.02]
+    az = [0.05, 0.1, 0.5 * math.pi + 0.1, 0.0, 0.08, 0.5 * math.pi - 0.05]
+    ux = list(rng.uniform(-0.1, 0.1, 6))
+    uy = list(rng.uniform(-0.1, 0.1, 6))
+    vz = list(rng.uniform(-0.5, 0.5, 6))
+    rec = particle_records(den, a, b, x, y, az, ux, uy, vz)
+    return Case("contact_cluster_%dx%d" % (itot, jtot), itot, jtot, 2.0, 150.0, extfrcy=0.02, Fr=3.0, particles=rec,
+                steps=20)
+
+
+CONFIGS = {
+    "couette_circle": couette_circle,
+    "poiseuille": poiseuille,
+    "mixed_target": mixed_target,
+    "contact_cluster": contact_cluster,
+}

@@ -1,0 +1,545 @@
+// C ABI of include/eif.h: context lifetime, state transfer, stage entry points
+// and the time-step orchestration of integrate (src/main.c:13-55).
+#include "eif_internal.cuh"
+#include <cstdio>
+#include <cstdarg>
+#include <cstring>
+#include <cstdlib>
+#include <cmath>
+#include <new>
+#include <vector>
+
+namespace eif {
+
+int fail(eif_ctx *c, int code, const char *fmt, ...) {
+  if (c) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(c->err, sizeof(c->err), fmt, ap);
+    va_end(ap);
+  }
+  return code;
+}
+
+int check_cuda(eif_ctx *c, cudaError_t e, const char *what) {
+  return fail(c, EIF_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+}  // namespace eif
+
+using namespace eif;
+
+namespace {
+
+// grid metrics exactly as set_coordinate computes them (src/param/init.c:105-167)
+void host_metrics(eif_ctx *c) {
+  const int itot = c->itot, jtot = c->jtot;
+  c->h_xf = new double[itot + 2];
+  c->h_xc = new double[itot + 2];
+  c->h_dxf = new double[itot + 2];
+  c->h_dxc = new double[itot + 2];
+  c->h_yf = new double[jtot + 2];
+  c->h_yc = new double[jtot + 2];
+  // 0-based storage of XF(1..itot+1), XC(0..itot+1), DXF(1..itot), DXC(1..itot+1), YF(1..), YC(1..)
+  const double dx = c->lx / itot;
+  c->dx = dx;
+  for (int i = 1; i <= itot + 1; i++) c->h_xf[i - 1] = 1. * (i - 1) * dx;
+  c->h_xf[0] = 0.;
+  c->h_xf[itot] = c->lx;
+  for (int i = 1; i <= itot; i++) c->h_dxf[i - 1] = c->h_xf[i] - c->h_xf[i - 1];
+  c->h_xc[0] = c->h_xf[0];
+  for (int i = 1; i <= itot; i++) c->h_xc[i] = 0.5 * (c->h_xf[i - 1] + c->h_xf[i]);
+  c->h_xc[itot + 1] = c->h_xf[itot];
+  for (int i = 1; i <= itot + 1; i++) c->h_dxc[i - 1] = c->h_xc[i] - c->h_xc[i - 1];
+  const double dy = c->ly / jtot;
+  c->dy = dy;
+  for (int j = 1; j <= jtot + 1; j++) c->h_yf[j - 1] = 0. + 1. * (j - 1) * dy;
+  for (int j = 1; j <= jtot; j++) c->h_yc[j - 1] = 0. + 0.5 * (2 * j - 1) * dy;
+}
+
+int upload(eif_ctx *c, double **dst, const std::vector<double> &v) {
+  EIF_CK(c, cudaMalloc((void **)dst, sizeof(double) * v.size()));
+  EIF_CK(c, cudaMemcpy(*dst, v.data(), sizeof(double) * v.size(), cudaMemcpyHostToDevice));
+  return EIF_OK;
+}
+
+int device_metrics(eif_ctx *c) {
+  const int itot = c->itot, jtot = c->jtot;
+  auto DXF = [&](int i) { return c->h_dxf[i - 1]; };
+  auto DXC = [&](int i) { return c->h_dxc[i - 1]; };
+  std::vector<double> xc(itot + 2), yc(jtot + 2, 0.), rdxf(itot + 2, 0.), rdxc(itot + 2, 0.), dxc(itot + 2, 0.);
+  std::vector<double> cxm(itot + 2, 0.), cxp(itot + 2, 0.), cym(itot + 2, 0.), cyp(itot + 2, 0.);
+  for (int i = 0; i <= itot + 1; i++) xc[i] = c->h_xc[i];
+  for (int j = 1; j <= jtot; j++) yc[j] = c->h_yc[j - 1];
+  for (int i = 1; i <= itot; i++) rdxf[i] = 1. / DXF(i);
+  for (int i = 1; i <= itot + 1; i++) { rdxc[i] = 1. / DXC(i); dxc[i] = DXC(i); }
+  for (int i = 2; i <= itot; i++) {
+    // update_velocity.c:38-39
+    cxm[i] = DXF(i - 1) / (2. * DXC(i));
+    cxp[i] = DXF(i) / (2. * DXC(i));
+  }
+  for (int i = 1; i <= itot; i++) {
+    // update_velocity.c:121-122
+    cym[i] = DXC(i) / (2. * DXF(i));
+    cyp[i] = DXC(i + 1) / (2. * DXF(i));
+  }
+  int rc;
+  if ((rc = upload(c, &c->xc, xc))) return rc;
+  if ((rc = upload(c, &c->yc, yc))) return rc;
+  if ((rc = upload(c, &c->rdxf, rdxf))) return rc;
+  if ((rc = upload(c, &c->rdxc, rdxc))) return rc;
+  if ((rc = upload(c, &c->dxc, dxc))) return rc;
+  if ((rc = upload(c, &c->cxm, cxm))) return rc;
+  if ((rc = upload(c, &c->cxp, cxp))) return rc;
+  if ((rc = upload(c, &c->cym, cym))) return rc;
+  if ((rc = upload(c, &c->cyp, cyp))) return rc;
+  return EIF_OK;
+}
+
+int check_flags(eif_ctx *c) {
+  // called after a synchronisation; reports and clears kernel error flags
+  unsigned f = *c->h_flags;
+  if (f == 0u) return EIF_OK;
+  *c->h_flags = 0u;
+  EIF_CK(c, cudaMemsetAsync(c->d_flags, 0, sizeof(unsigned), c->stream));
+  if (f & EIF_FLAG_NONFINITE) return fail(c, EIF_ERR_NONFINITE, "non-finite velocity detected");
+  if (f & EIF_FLAG_NOCONV) return fail(c, EIF_ERR_NOCONV, "an iteration cap was reached on the device");
+  return EIF_OK;
+}
+
+// copy the scalars and flags to the host and wait
+int sync_scalars(eif_ctx *c) {
+  EIF_CK(c, cudaMemcpyAsync(c->h_scal, c->d_scal, sizeof(double) * 4, cudaMemcpyDeviceToHost, c->stream));
+  EIF_CK(c, cudaMemcpyAsync(c->h_flags, c->d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+  EIF_CK(c, cudaStreamSynchronize(c->stream));
+  c->dt_host = c->h_scal[0];
+  return check_flags(c);
+}
+
+int ensure_pcap(eif_ctx *c, int n) {
+  if (n <= c->pcap && c->P) return EIF_OK;
+  if (c->P) cudaFree(c->P);
+  c->P = nullptr;
+  const int cap = n > 0 ? n : 1;
+  EIF_CK(c, cudaMalloc((void **)&c->P, sizeof(double) * EIF_NFIELDS * (size_t)cap));
+  EIF_CK(c, cudaMemset(c->P, 0, sizeof(double) * EIF_NFIELDS * (size_t)cap));
+  c->pcap = cap;
+  return EIF_OK;
+}
+
+bool valid_rk(int rk) { return rk >= 0 && rk < 3; }
+
+// one RK stage of integrate (src/main.c:14-53); *sub receives the sub-iterations
+int rk_stage(eif_ctx *c, int rk, int *sub) {
+  int rc;
+  const bool ibm = c->np > 0;
+  if ((rc = launch_reset_increments(c))) return rc;
+  if ((rc = launch_inertia(c, 0))) return rc;
+  if ((rc = launch_predictor(c, rk))) return rc;
+  if (ibm && (rc = launch_exchange(c))) return rc;
+  if ((rc = launch_potential(c, rk, ibm))) return rc;
+  if ((rc = launch_correct(c, rk, ibm, true))) return rc;
+  if ((rc = launch_collision(c, 0))) return rc;
+  int s = 0;
+  for (s = 0;; s++) {
+    if ((rc = launch_inertia(c, 1))) return rc;
+    if ((rc = launch_collision(c, 1))) return rc;
+    if ((rc = launch_increment(c, rk))) return rc;
+    if ((rc = sync_scalars(c))) return rc;
+    if (c->h_scal[1] < 1.e-8) break;
+    if (s > 100) break;
+  }
+  if (sub) *sub = s + 1;
+  return launch_update_particles(c);
+}
+
+}  // namespace
+
+extern "C" {
+
+int eif_create(const eif_config_t *cfg, eif_ctx **out) {
+  if (!cfg || !out) return EIF_ERR_ARG;
+  *out = nullptr;
+  eif_ctx *c = new (std::nothrow) eif_ctx();
+  if (!c) return EIF_ERR_NOMEM;
+  c->cfg = *cfg;
+  if (cfg->itot < 4 || cfg->jtot < 3 || !(cfg->ly > 0.) || !(cfg->Re > 0.) ||
+      (cfg->precision != EIF_PREC_FP64 && cfg->precision != EIF_PREC_MIXED)) {
+    int rc = fail(c, EIF_ERR_ARG, "invalid configuration");
+    delete c;
+    return rc;
+  }
+  c->itot = cfg->itot;
+  c->jtot = cfg->jtot;
+  c->lx = 1.;
+  c->ly = cfg->ly;
+  c->ld = ((cfg->itot + 2) + 31) / 32 * 32;
+  c->nfield = (size_t)c->ld * (c->jtot + 2);
+  c->device = cfg->device;
+  *out = c;
+#define CK_CREATE(call) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) return check_cuda(c, e_, #call); } while (0)
+  CK_CREATE(cudaSetDevice(c->device));
+  int sms = 0;
+  CK_CREATE(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
+  c->sms = sms;
+  CK_CREATE(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  host_metrics(c);
+  int rc = device_metrics(c);
+  if (rc) return rc;
+  double **fields[] = {&c->ux[0], &c->ux[1], &c->uy[0], &c->uy[1], &c->p, &c->psi,
+                       &c->sxa[0], &c->sxa[1], &c->sya[0], &c->sya[1], &c->dux, &c->duy, &c->qhat};
+  for (double **f : fields) {
+    CK_CREATE(cudaMalloc((void **)f, sizeof(double) * c->nfield));
+    CK_CREATE(cudaMemset(*f, 0, sizeof(double) * c->nfield));
+  }
+  CK_CREATE(cudaMalloc((void **)&c->d_scal, sizeof(double) * 4));
+  CK_CREATE(cudaMemset(c->d_scal, 0, sizeof(double) * 4));
+  CK_CREATE(cudaMalloc((void **)&c->d_flags, sizeof(unsigned)));
+  CK_CREATE(cudaMemset(c->d_flags, 0, sizeof(unsigned)));
+  CK_CREATE(cudaMallocHost((void **)&c->h_scal, sizeof(double) * 4));
+  CK_CREATE(cudaMallocHost((void **)&c->h_flags, sizeof(unsigned)));
+  *c->h_flags = 0u;
+#undef CK_CREATE
+  rc = poisson_init(c);
+  if (rc) return rc;
+  rc = ensure_pcap(c, 1);
+  if (rc) return rc;
+  rc = launch_boundaries(c);
+  if (rc) return rc;
+  EIF_CK(c, cudaStreamSynchronize(c->stream));
+  return EIF_OK;
+}
+
+int eif_destroy(eif_ctx *c) {
+  if (!c) return EIF_OK;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  double *ptrs[] = {c->ux[0], c->ux[1], c->uy[0], c->uy[1], c->p, c->psi, c->sxa[0], c->sxa[1], c->sya[0],
+                    c->sya[1], c->dux, c->duy, c->qhat, c->xc, c->yc, c->rdxf, c->rdxc, c->cxm, c->cxp, c->cym,
+                    c->cyp, c->dxc, c->P, c->d_scal};
+  for (double *p : ptrs) if (p) cudaFree(p);
+  if (c->d_flags) cudaFree(c->d_flags);
+  if (c->h_scal) cudaFreeHost(c->h_scal);
+  if (c->h_flags) cudaFreeHost(c->h_flags);
+  poisson_free(c);
+  ibm_free(c);
+  profile_free(c);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete[] c->h_xf; delete[] c->h_xc; delete[] c->h_dxf; delete[] c->h_dxc; delete[] c->h_yf; delete[] c->h_yc;
+  delete c;
+  return EIF_OK;
+}
+
+const char *eif_last_error(const eif_ctx *c) { return c ? c->err : "null context"; }
+
+int eif_synchronize(eif_ctx *c) {
+  if (!c) return EIF_ERR_ARG;
+  EIF_CK(c, cudaStreamSynchronize(c->stream));
+  return EIF_OK;
+}
+
+void *eif_stream(eif_ctx *c) { return c ? (void *)c->stream : nullptr; }
+
+int eif_push_fluid(eif_ctx *c, const double *ux, const double *uy, const double *p) {
+  if (!c || !ux || !uy || !p) return EIF_ERR_ARG;
+  const size_t dp = sizeof(double) * c->ld;
+  const int rows = c->jtot + 2;
+  EIF_CK(c, cudaMemcpy2DAsync(c->ux[c->cur], dp, ux, sizeof(double) * (c->itot + 1), sizeof(double) * (c->itot + 1),
+                              rows, cudaMemcpyHostToDevice, c->stream));
+  EIF_CK(c, cudaMemcpy2DAsync(c->uy[c->cur], dp, uy, sizeof(double) * (c->itot + 2), sizeof(double) * (c->itot + 2),
+                              rows, cudaMemcpyHostToDevice, c->stream));
+  EIF_CK(c, cudaMemcpy2DAsync(c->p, dp, p, sizeof(double) * (c->itot + 2), sizeof(double) * (c->itot + 2), rows,
+                              cudaMemcpyHostToDevice, c->stream));
+  int rc = launch_boundaries(c);
+  if (rc) return rc;
+  EIF_CK(c, cudaStreamSynchronize(c->stream));
+  c->fluid_pushed = true;
+  return EIF_OK;
+}
+
+int eif_pull_fluid(eif_ctx *c, double *ux, double *uy, double *p, double *psi) {
+  if (!c) return EIF_ERR_ARG;
+  const size_t dp = sizeof(double) * c->ld;
+  const int rows = c->jtot + 2;
+  const size_t wx = sizeof(double) * (c->itot + 1), wy = sizeof(double) * (c->itot + 2);
+  if (ux) EIF_CK(c, cudaMemcpy2DAsync(ux, wx, c->ux[c->cur], dp, wx, rows, cudaMemcpyDeviceToHost, c->stream));
+  if (uy) EIF_CK(c, cudaMemcpy2DAsync(uy, wy, c->uy[c->cur], dp, wy, rows, cudaMemcpyDeviceToHost, c->stream));
+  if (p) EIF_CK(c, cudaMemcpy2DAsync(p, wy, c->p, dp, wy, rows, cudaMemcpyDeviceToHost, c->stream));
+  if (psi) EIF_CK(c, cudaMemcpy2DAsync(psi, wy, c->psi, dp, wy, rows, cudaMemcpyDeviceToHost, c->stream));
+  EIF_CK(c, cudaStreamSynchronize(c->stream));
+  return EIF_OK;
+}
+
+int eif_push_particles(eif_ctx *c, int n, const double *rec) {
+  if (!c || n < 0 || (n > 0 && !rec)) return EIF_ERR_ARG;
+  int rc = ensure_pcap(c, n);
+  if (rc) return rc;
+  std::vector<double> soa((size_t)EIF_NFIELDS * c->pcap, 0.);
+  for (int f = 0; f < EIF_NFIELDS; f++)
+    for (int k = 0; k < n; k++) soa[(size_t)f * c->pcap + k] = rec[(size_t)k * EIF_NFIELDS + f];
+  EIF_CK(c, cudaMemcpy(c->P, soa.data(), sizeof(double) * soa.size(), cudaMemcpyHostToDevice));
+  c->np = n;
+  return ibm_reserve(c);
+}
+
+int eif_pull_particles(eif_ctx *c, int n, double *rec) {
+  if (!c || n != c->np || (n > 0 && !rec)) return fail(c, EIF_ERR_ARG, "particle count mismatch (%d vs %d)", n, c ? c->np : 0);
+  if (n == 0) return EIF_OK;
+  std::vector<double> soa((size_t)EIF_NFIELDS * c->pcap);
+  EIF_CK(c, cudaStreamSynchronize(c->stream));
+  EIF_CK(c, cudaMemcpy(soa.data(), c->P, sizeof(double) * soa.size(), cudaMemcpyDeviceToHost));
+  for (int f = 0; f < EIF_NFIELDS; f++)
+    for (int k = 0; k < n; k++) rec[(size_t)k * EIF_NFIELDS + f] = soa[(size_t)f * c->pcap + k];
+  return EIF_OK;
+}
+
+// source arrays: SRCUXA(i,j) for i=2..itot at ux index, SRCUYA(i,j) for i=1..itot at uy index
+int eif_pull_src(eif_ctx *c, double *uxa, double *uxb, double *uya, double *uyb) {
+  if (!c) return EIF_ERR_ARG;
+  const size_t dp = sizeof(double) * c->ld;
+  const size_t wx = sizeof(double) * (c->itot - 1), wy = sizeof(double) * c->itot;
+  const int a = c->scur, b = 1 - c->scur;
+  // SRCUXA(2,1) sits at ux index (2,1) -> row 1, column 1
+  if (uxa) EIF_CK(c, cudaMemcpy2DAsync(uxa, wx, c->sxa[a] + c->ld + 1, dp, wx, c->jtot, cudaMemcpyDeviceToHost, c->stream));
+  if (uxb) EIF_CK(c, cudaMemcpy2DAsync(uxb, wx, c->sxa[b] + c->ld + 1, dp, wx, c->jtot, cudaMemcpyDeviceToHost, c->stream));
+  if (uya) EIF_CK(c, cudaMemcpy2DAsync(uya, wy, c->sya[a] + c->ld + 1, dp, wy, c->jtot, cudaMemcpyDeviceToHost, c->stream));
+  if (uyb) EIF_CK(c, cudaMemcpy2DAsync(uyb, wy, c->sya[b] + c->ld + 1, dp, wy, c->jtot, cudaMemcpyDeviceToHost, c->stream));
+  EIF_CK(c, cudaStreamSynchronize(c->stream));
+  return EIF_OK;
+}
+
+int eif_push_src(eif_ctx *c, const double *uxa, const double *uya) {
+  if (!c || !uxa || !uya) return EIF_ERR_ARG;
+  const size_t dp = sizeof(double) * c->ld;
+  const size_t wx = sizeof(double) * (c->itot - 1), wy = sizeof(double) * c->itot;
+  EIF_CK(c, cudaMemcpy2DAsync(c->sxa[c->scur] + c->ld + 1, dp, uxa, wx, wx, c->jtot, cudaMemcpyHostToDevice, c->stream));
+  EIF_CK(c, cudaMemcpy2DAsync(c->sya[c->scur] + c->ld + 1, dp, uya, wy, wy, c->jtot, cudaMemcpyHostToDevice, c->stream));
+  EIF_CK(c, cudaStreamSynchronize(c->stream));
+  return EIF_OK;
+}
+
+int eif_pull_ibm_fields(eif_ctx *c, double *dux, double *duy) {
+  if (!c || !dux || !duy) return EIF_ERR_ARG;
+  const size_t dp = sizeof(double) * c->ld, wy = sizeof(double) * (c->itot + 2);
+  EIF_CK(c, cudaMemcpy2DAsync(dux, wy, c->dux, dp, wy, c->jtot + 2, cudaMemcpyDeviceToHost, c->stream));
+  EIF_CK(c, cudaMemcpy2DAsync(duy, wy, c->duy, dp, wy, c->jtot + 2, cudaMemcpyDeviceToHost, c->stream));
+  EIF_CK(c, cudaStreamSynchronize(c->stream));
+  return EIF_OK;
+}
+
+int eif_decide_dt(eif_ctx *c, double *dt) {
+  if (!c) return EIF_ERR_ARG;
+  int rc = launch_decide_dt(c);
+  if (rc) return rc;
+  if (dt) {
+    if ((rc = sync_scalars(c))) return rc;
+    *dt = c->dt_host;
+  }
+  return EIF_OK;
+}
+
+int eif_set_dt(eif_ctx *c, double dt) {
+  if (!c || !(dt > 0.)) return EIF_ERR_ARG;
+  c->h_scal[0] = dt;
+  EIF_CK(c, cudaMemcpyAsync(c->d_scal, c->h_scal, sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  EIF_CK(c, cudaStreamSynchronize(c->stream));
+  c->dt_host = dt;
+  return EIF_OK;
+}
+
+int eif_get_dt(eif_ctx *c, double *dt) {
+  if (!c || !dt) return EIF_ERR_ARG;
+  int rc = sync_scalars(c);
+  if (rc) return rc;
+  *dt = c->dt_host;
+  return EIF_OK;
+}
+
+int eif_integrate(eif_ctx *c, int *substeps) {
+  if (!c) return EIF_ERR_ARG;
+  if (!c->fluid_pushed) return fail(c, EIF_ERR_STATE, "push the fluid state before integrating");
+  for (int rk = 0; rk < 3; rk++) {
+    int sub = 0;
+    int rc = rk_stage(c, rk, &sub);
+    if (rc) return rc;
+    if (substeps) substeps[rk] = sub;
+  }
+  return sync_scalars(c);
+}
+
+int eif_advance(eif_ctx *c, int nsteps) {
+  if (!c || nsteps < 0) return EIF_ERR_ARG;
+  if (!c->fluid_pushed) return fail(c, EIF_ERR_STATE, "push the fluid state before integrating");
+  for (int s = 0; s < nsteps; s++) {
+    int rc = launch_decide_dt(c);
+    if (rc) return rc;
+    rc = eif_integrate(c, nullptr);
+    if (rc) return rc;
+    c->step += 1;
+    c->time += c->dt_host;
+  }
+  return EIF_OK;
+}
+
+int eif_get_time(eif_ctx *c, int *step, double *time) {
+  if (!c || !step || !time) return EIF_ERR_ARG;
+  *step = c->step;
+  *time = c->time;
+  return EIF_OK;
+}
+
+int eif_set_time(eif_ctx *c, int step, double time) {
+  if (!c) return EIF_ERR_ARG;
+  c->step = step;
+  c->time = time;
+  return EIF_OK;
+}
+
+int eif_update_boundaries(eif_ctx *c) { return c ? launch_boundaries(c) : EIF_ERR_ARG; }
+int eif_reset_particle_increments(eif_ctx *c) { return c ? launch_reset_increments(c) : EIF_ERR_ARG; }
+
+int eif_compute_inertia(eif_ctx *c, int cn) {
+  if (!c || (cn != 0 && cn != 1)) return c ? fail(c, EIF_ERR_ARG, "cnstep must be 0 or 1") : EIF_ERR_ARG;
+  return launch_inertia(c, cn);
+}
+
+int eif_update_velocity(eif_ctx *c, int rk) {
+  if (!c || !valid_rk(rk)) return c ? fail(c, EIF_ERR_ARG, "rkstep must be 0, 1 or 2") : EIF_ERR_ARG;
+  return launch_predictor(c, rk);
+}
+
+int eif_exchange_momentum(eif_ctx *c) { return c ? launch_exchange(c) : EIF_ERR_ARG; }
+int eif_update_momentum_field(eif_ctx *c) { return c ? launch_update_momentum_field(c) : EIF_ERR_ARG; }
+
+int eif_compute_potential(eif_ctx *c, int rk) {
+  if (!c || !valid_rk(rk)) return c ? fail(c, EIF_ERR_ARG, "rkstep must be 0, 1 or 2") : EIF_ERR_ARG;
+  return launch_potential(c, rk, false);
+}
+
+int eif_correct_velocity(eif_ctx *c, int rk) {
+  if (!c || !valid_rk(rk)) return c ? fail(c, EIF_ERR_ARG, "rkstep must be 0, 1 or 2") : EIF_ERR_ARG;
+  return launch_correct(c, rk, false, false);
+}
+
+int eif_update_pressure(eif_ctx *c) { return c ? launch_update_pressure(c) : EIF_ERR_ARG; }
+
+int eif_compute_collision_force(eif_ctx *c, int cn) {
+  if (!c || (cn != 0 && cn != 1)) return c ? fail(c, EIF_ERR_ARG, "cnstep must be 0 or 1") : EIF_ERR_ARG;
+  int rc = launch_collision(c, cn);
+  if (rc) return rc;
+  return sync_scalars(c);
+}
+
+int eif_increment_particles(eif_ctx *c, int rk, double *residual) {
+  if (!c || !valid_rk(rk)) return c ? fail(c, EIF_ERR_ARG, "rkstep must be 0, 1 or 2") : EIF_ERR_ARG;
+  int rc = launch_increment(c, rk);
+  if (rc) return rc;
+  if ((rc = sync_scalars(c))) return rc;
+  if (residual) *residual = c->h_scal[1];
+  return EIF_OK;
+}
+
+int eif_update_particles(eif_ctx *c) { return c ? launch_update_particles(c) : EIF_ERR_ARG; }
+
+int eif_divergence(eif_ctx *c, double *divmax, double *divsum) {
+  if (!c || !divmax || !divsum) return EIF_ERR_ARG;
+  return launch_divergence(c, divmax, divsum);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// kernel timing
+namespace eif {
+
+static cudaEvent_t take_event(eif_ctx *c) {
+  if (!c->prof.pool.empty()) {
+    cudaEvent_t e = c->prof.pool.back();
+    c->prof.pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+ProfScope::ProfScope(eif_ctx *c_, const char *name, int kernels) : c(c_), entry(-1), stop(nullptr) {
+  if (!c->prof.enabled) return;
+  auto &es = c->prof.entries;
+  for (size_t k = 0; k < es.size(); k++) {
+    if (es[k].name == name) { entry = (int)k; break; }
+  }
+  if (entry < 0) {
+    es.push_back(Profiler::Entry{name, 0, 0.});
+    entry = (int)es.size() - 1;
+  }
+  es[entry].launches += kernels;
+  cudaEvent_t start = take_event(c);
+  stop = take_event(c);
+  cudaEventRecord(start, c->stream);
+  c->prof.pending.push_back(Profiler::Pending{entry, start, stop});
+}
+
+ProfScope::~ProfScope() {
+  if (entry >= 0) cudaEventRecord(stop, c->stream);
+}
+
+int profile_flush(eif_ctx *c) {
+  if (c->prof.pending.empty()) return EIF_OK;
+  EIF_CK(c, cudaStreamSynchronize(c->stream));
+  for (auto &p : c->prof.pending) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, p.start, p.stop) == cudaSuccess) c->prof.entries[p.entry].ms += ms;
+    c->prof.pool.push_back(p.start);
+    c->prof.pool.push_back(p.stop);
+  }
+  c->prof.pending.clear();
+  return EIF_OK;
+}
+
+void profile_free(eif_ctx *c) {
+  for (auto &p : c->prof.pending) { cudaEventDestroy(p.start); cudaEventDestroy(p.stop); }
+  for (auto e : c->prof.pool) cudaEventDestroy(e);
+  c->prof.pending.clear();
+  c->prof.pool.clear();
+}
+
+}  // namespace eif
+
+extern "C" {
+
+int eif_profile_enable(eif_ctx *c, int enable) {
+  if (!c) return EIF_ERR_ARG;
+  int rc = profile_flush(c);
+  c->prof.enabled = enable != 0;
+  return rc;
+}
+
+int eif_profile_reset(eif_ctx *c) {
+  if (!c) return EIF_ERR_ARG;
+  int rc = profile_flush(c);
+  c->prof.entries.clear();
+  return rc;
+}
+
+int eif_profile_count(eif_ctx *c, int *count) {
+  if (!c || !count) return EIF_ERR_ARG;
+  int rc = profile_flush(c);
+  *count = (int)c->prof.entries.size();
+  return rc;
+}
+
+int eif_profile_get(eif_ctx *c, int k, char *name, int name_len, long long *launches, double *ms) {
+  if (!c || k < 0 || k >= (int)c->prof.entries.size()) return EIF_ERR_ARG;
+  int rc = profile_flush(c);
+  const auto &e = c->prof.entries[k];
+  if (name && name_len > 0) {
+    strncpy(name, e.name.c_str(), (size_t)name_len - 1);
+    name[name_len - 1] = 0;
+  }
+  if (launches) *launches = e.launches;
+  if (ms) *ms = e.ms;
+  return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,203 @@
+// Internal declarations of the GB300 implementation of include/eif.h.
+//
+// Device data layout (one context = one suspension on one GPU):
+//  * Fields keep the reference's haloed index spaces (include/arrays/fluid.h)
+//    but rows are padded to a pitch `ld` (a multiple of 32 doubles, 256 B):
+//      UX(i,j) -> ux[j*ld + (i-1)]      i = 1..itot+1, j = 0..jtot+1
+//      UY(i,j) -> uy[j*ld + i]          i = 0..itot+1, j = 0..jtot+1 (also p, psi, dux, duy)
+//    Row 0 and row jtot+1 are the periodic halo rows; wall columns hold the
+//    boundary values. Every kernel that writes a field also writes the halo
+//    copies and wall/Neumann values it affects, so the device state is always
+//    boundary-consistent (the reference refreshes them with separate calls,
+//    src/fluid/boundary_conditions.c).
+//  * The explicit RK source terms use the same index spaces as the velocity
+//    they belong to (SRCUXA(i,j) at ux's index, SRCUYA(i,j) at uy's index).
+//  * ux/uy are double-buffered: the predictor reads one buffer and writes the
+//    other, which removes the read-after-write hazard of an in-place stencil.
+//  * Particles are structure-of-arrays: field f of particle n at P[f*pcap + n],
+//    f in the order of the reference's particle_t (EIF_P_* in eif.h).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstddef>
+#include "eif.h"
+
+#define EIF_WARP 32
+
+// error flags raised by kernels (bit mask in ctx->d_flags)
+#define EIF_FLAG_NOCONV 1u
+#define EIF_FLAG_NONFINITE 2u
+
+// cap of the equivalent-circle fixed point (the reference has none,
+// src/suspensions/collision.c:117-133,141-152)
+#define EIF_FIT_MAX_ITER 10000
+// cap of the normal-foot iteration (src/ellipse.c:57-59: stop after n > 100)
+#define EIF_NORMAL_MAX_ITER 101
+
+// Interior block length of the partitioned tridiagonal solver along y.
+#define EIF_TDM_M 16
+
+#include <vector>
+#include <string>
+
+namespace eif {
+
+// per-kernel event timing of one context
+struct Profiler {
+  bool enabled = false;
+  struct Entry { std::string name; long long launches = 0; double ms = 0.; };
+  std::vector<Entry> entries;
+  struct Pending { int entry; cudaEvent_t start, stop; };
+  std::vector<Pending> pending;
+  std::vector<cudaEvent_t> pool;
+};
+
+// Poisson solver tables, built once per context on the host in double precision.
+struct PoissonPlan {
+  int n;            // DCT length (itot), even
+  int m;            // complex FFT length n/2
+  int nfac;         // radix sequence of the m-point FFT
+  int fac[16];
+  double2 *tw;      // exp(-2 pi i k / m), k < m
+  double2 *rot;     // exp(-i pi k / 2n), k < n
+  double2 *wn;      // exp(-2 pi i k / n), k < n
+  // tridiagonal solver along y (jtot rows, one system per wavenumber)
+  int blk;          // interior rows per block + 1 (EIF_TDM_M), or 0: serial path
+  int nblk;         // blocks per column (jtot / blk)
+  double *tdm_inv;  // [k][i]  1/pivot of the interior Thomas sweep, i < blk-1
+  double *tdm_up;   // [k][i]  modified upper diagonal, i < blk-1
+  double *tdm_g;    // [k][i]  response of the interior block to its left neighbour
+  double *red_inv;  // [k][b]  reduced cyclic system: Thomas pivots (b < nblk-1)
+  double *red_up;   // [k][b]
+  double *red_q1;   // [k][b]  correction vector of the reduced cyclic system
+  double *red_coef; // [k][4]  A, B, den, pin flag
+  double *lam;      // [k]     eigenvalue of the DCT direction
+  double *ywork;    // nblk*itot: reduced right-hand sides / interface values
+};
+
+}  // namespace eif
+
+struct eif_ctx {
+  eif_config_t cfg;
+  int itot, jtot, ld;
+  size_t nfield;                // ld * (jtot+2)
+  double lx, ly, dx, dy;
+  int device;
+  cudaStream_t stream;
+  // fields
+  double *ux[2], *uy[2];
+  int cur;                      // index of the current velocity buffer
+  double *p, *psi;
+  double *sxa[2], *sya[2];      // RK explicit terms: [scur] current stage, [1-scur] previous
+  int scur;
+  double *dux, *duy;
+  double *qhat;                 // Poisson work field (wavenumber space)
+  // grid metrics (device, indexed like the reference arrays)
+  double *xc;                   // XC(0..itot+1)
+  double *yc;                   // YC(1..jtot) at [j]
+  double *rdxf, *rdxc;          // 1/DXF(i), 1/DXC(i) at [i]
+  double *cxm, *cxp, *cym, *cyp;// stencil interpolation weights at [i]
+  double *dxc;                  // DXC(i) at [i]
+  // host copies of the metrics
+  double *h_xf, *h_xc, *h_dxf, *h_dxc, *h_yf, *h_yc;
+  eif::PoissonPlan pp;
+  // particles
+  int np, pcap;
+  double *P;                    // EIF_NFIELDS * pcap
+  // immersed-boundary work
+  int *box;                     // per particle: 3 images x {imin,imax,jmin,jmax}
+  int *chunk_off;               // per particle: first chunk (exclusive scan), [np] = total
+  double *partial;              // per chunk: 3 partial sums
+  double *wbuf;                 // per box cell: dux, duy contribution
+  size_t wcap;                  // capacity of wbuf in cells
+  int chunk_cap;                // capacity of partial in chunks
+  // device scalars
+  double *d_scal;               // [0] dt, [1] residual, [2] scratch
+  unsigned *d_flags;
+  double *h_scal;               // pinned mirror
+  unsigned *h_flags;
+  int sms;
+  // host bookkeeping
+  int step;
+  double time;
+  double dt_host;
+  bool fluid_pushed;
+  eif::Profiler prof;
+  char err[512];
+};
+
+namespace eif {
+
+// ---- kernel timing: a scope records events around the launches inside it ----
+struct ProfScope {
+  eif_ctx *c;
+  int entry;
+  cudaEvent_t stop;
+  ProfScope(eif_ctx *c, const char *name, int kernels);
+  ~ProfScope();
+};
+#define EIF_PROF(c, name, kernels) eif::ProfScope eif_prof_scope_((c), (name), (kernels))
+int profile_flush(eif_ctx *c);
+void profile_free(eif_ctx *c);
+
+// ---- launch helpers ----
+int fail(eif_ctx *c, int code, const char *fmt, ...);
+int check_cuda(eif_ctx *c, cudaError_t e, const char *what);
+#define EIF_CK(c, call) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) return eif::check_cuda((c), e_, #call); } while (0)
+#define EIF_LAUNCH_CK(c) do { cudaError_t e_ = cudaGetLastError(); if (e_ != cudaSuccess) return eif::check_cuda((c), e_, "kernel launch"); } while (0)
+
+// ---- fluid (fluid.cu) ----
+int launch_boundaries(eif_ctx *c);
+int launch_bc_p_like(eif_ctx *c, double *a);
+int launch_predictor(eif_ctx *c, int rk);
+int launch_update_momentum_field(eif_ctx *c);
+int launch_correct(eif_ctx *c, int rk, bool with_ibm, bool with_pressure);
+int launch_update_pressure(eif_ctx *c);
+int launch_decide_dt(eif_ctx *c);
+int launch_divergence(eif_ctx *c, double *divmax, double *divsum);
+
+// ---- Poisson (poisson.cu) ----
+int poisson_init(eif_ctx *c);
+void poisson_free(eif_ctx *c);
+int launch_potential(eif_ctx *c, int rk, bool with_ibm);
+
+// ---- immersed boundary (ibm.cu) ----
+int ibm_reserve(eif_ctx *c);
+void ibm_free(eif_ctx *c);
+int launch_inertia(eif_ctx *c, int cn);
+int launch_exchange(eif_ctx *c);
+
+// ---- particles (particles.cu) ----
+int launch_collision(eif_ctx *c, int cn);
+int launch_reset_increments(eif_ctx *c);
+int launch_increment(eif_ctx *c, int rk);
+int launch_update_particles(eif_ctx *c);
+
+// RK3 coefficients (src/param/init.c:169-191)
+struct RK { double alpha, beta, gamma; };
+RK rk_coef(int rk);
+
+}  // namespace eif
+
+// ---- device helpers shared by the kernels ----
+#define EIF_HD __host__ __device__ __forceinline__
+
+namespace eifd {
+
+__device__ __forceinline__ int ux_idx(int i, int j, int ld) { return j * ld + (i - 1); }
+__device__ __forceinline__ int uy_idx(int i, int j, int ld) { return j * ld + i; }
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+}  // namespace eifd

@@ -1,0 +1,445 @@
+// Fluid kernels: boundary values, RK predictor, projection, pressure update,
+// time-step size and divergence diagnostics.
+//
+// Reference functions restated here (NaokiHori/EllipsesInFlows):
+//   fluid_update_boundaries_{ux,uy,p}   src/fluid/boundary_conditions.c:7-62
+//   compute_src_ux / compute_src_uy     src/fluid/update_velocity.c:9-173
+//   update_ux / update_uy               src/fluid/update_velocity.c:175-227
+//   suspensions_update_momentum_fleid   src/suspensions/update.c:36-59
+//   fluid_correct_velocity              src/fluid/correct_velocity.c:6-42
+//   fluid_update_pressure               src/fluid/update_pressure.c:7-24
+//   param_decide_dt                     src/param/decide_dt.c:11-81
+//   check_divergence                    src/logging.c:40-80
+#include "eif_internal.cuh"
+#include <cfloat>
+
+namespace {
+
+using eifd::ux_idx;
+using eifd::uy_idx;
+
+constexpr int TX = 32, TY = 8;
+
+// ---------------------------------------------------------------------------
+// boundary and halo values of one field kind
+// kind 0: ux-like (halo i=2..itot, walls i=1,itot+1 set to 0)
+// kind 1: uy-like (halo i=1..itot, walls i=0,itot+1 set to the wall velocity)
+// kind 2: p-like  (halo i=1..itot, Neumann copies at i=0,itot+1 incl. halo rows)
+__global__ void k_bc(double *__restrict__ a, int kind, int itot, int jtot, int ld, double w0, double w1) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  // halo rows
+  const int ilo = kind == 0 ? 2 : 1;
+  const int ihi = itot;
+  const int col = kind == 0 ? -1 : 0;  // ux stores UX(i) at i-1
+  if (t >= ilo && t <= ihi) {
+    a[0 * ld + t + col] = a[jtot * ld + t + col];
+    a[(jtot + 1) * ld + t + col] = a[1 * ld + t + col];
+  }
+  // wall columns, rows 0..jtot+1
+  if (t <= jtot + 1) {
+    const int j = t;
+    if (kind == 0) {
+      a[ux_idx(1, j, ld)] = 0.;
+      a[ux_idx(itot + 1, j, ld)] = 0.;
+    } else if (kind == 1) {
+      a[uy_idx(0, j, ld)] = w0;
+      a[uy_idx(itot + 1, j, ld)] = w1;
+    } else {
+      // source row of the (already periodic) value: halo rows mirror rows jtot and 1
+      const int js = j == 0 ? jtot : (j == jtot + 1 ? 1 : j);
+      a[uy_idx(0, j, ld)] = a[uy_idx(1, js, ld)];
+      a[uy_idx(itot + 1, j, ld)] = a[uy_idx(itot, js, ld)];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// RK predictor: explicit/implicit source terms and the velocity update fused,
+// reading (ux, uy, p) and writing the other velocity buffer
+// (src/fluid/update_velocity.c:9-237). Also writes the halo rows of the new
+// velocities; wall columns of both buffers are constant and set at creation.
+struct PredArgs {
+  const double *ux, *uy, *p;
+  const double *sxb, *syb;     // previous explicit terms (srcB)
+  double *sxa, *sya;           // new explicit terms (srcA)
+  double *uxn, *uyn;           // new velocities
+  const double *rdxf, *rdxc, *cxm, *cxp, *cym, *cyp;
+  const double *dt;
+  double alpha, beta, gamma, rRe, rdy, ext;
+  int itot, jtot, ld;
+};
+
+__global__ void __launch_bounds__(TX *TY) k_predictor(PredArgs a) {
+  const int i = 1 + blockIdx.x * TX + threadIdx.x;
+  const int j = 1 + blockIdx.y * TY + threadIdx.y;
+  if (i > a.itot || j > a.jtot) return;
+  const int ld = a.ld;
+  const double dt = __ldg(a.dt);
+  const double adt = a.alpha * dt, bdt = a.beta * dt, gdt = a.gamma * dt;
+  const double rdy = a.rdy;
+  // ---- ux at face i (2..itot) ----
+  if (i >= 2) {
+    const int c = ux_idx(i, j, ld);
+    const double u0 = __ldg(a.ux + c);
+    const double uw = __ldg(a.ux + c - 1), ue = __ldg(a.ux + c + 1);
+    const double us = __ldg(a.ux + c - ld), un = __ldg(a.ux + c + ld);
+    const double rdxf_m = __ldg(a.rdxf + i - 1), rdxf_p = __ldg(a.rdxf + i);
+    const double cxm = __ldg(a.cxm + i), cxp = __ldg(a.cxp + i);
+    const double duxdx_xm = (u0 - uw) * rdxf_m;
+    const double duxdx_xp = (ue - u0) * rdxf_p;
+    const double duxdy_ym = (u0 - us) * rdy;
+    const double duxdy_yp = (un - u0) * rdy;
+    const double ux_xm = 0.5 * uw + 0.5 * u0;
+    const double ux_xp = 0.5 * u0 + 0.5 * ue;
+    const double adv1 = -cxm * ux_xm * duxdx_xm - cxp * ux_xp * duxdx_xp;
+    const int cy = uy_idx(i, j, ld);
+    const double uy_ym = cxm * __ldg(a.uy + cy - 1) + cxp * __ldg(a.uy + cy);
+    const double uy_yp = cxm * __ldg(a.uy + cy - 1 + ld) + cxp * __ldg(a.uy + cy + ld);
+    const double adv2 = -0.5 * uy_ym * duxdy_ym - 0.5 * uy_yp * duxdy_yp;
+    const double rdxc = __ldg(a.rdxc + i);
+    const double dif1 = a.rRe * (duxdx_xp - duxdx_xm) * rdxc;
+    const double dif2 = a.rRe * (duxdy_yp - duxdy_ym) * rdy;
+    const double pre = -(__ldg(a.p + cy) - __ldg(a.p + cy - 1)) * rdxc;
+    const double A = (adv1 + adv2) + (dif1 + dif2);
+    const double B = __ldg(a.sxb + c);
+    a.sxa[c] = A;
+    const double un_ = u0 + (adt * A + bdt * B + gdt * pre);
+    a.uxn[c] = un_;
+    if (j == 1) a.uxn[c + a.jtot * ld] = un_;
+    if (j == a.jtot) a.uxn[c - a.jtot * ld] = un_;
+  }
+  // ---- uy at cell i (1..itot) ----
+  {
+    const int c = uy_idx(i, j, ld);
+    const double v0 = __ldg(a.uy + c);
+    const double vw = __ldg(a.uy + c - 1), ve = __ldg(a.uy + c + 1);
+    const double vs = __ldg(a.uy + c - ld), vn = __ldg(a.uy + c + ld);
+    const double rdxc_m = __ldg(a.rdxc + i), rdxc_p = __ldg(a.rdxc + i + 1);
+    const double duydx_xm = (v0 - vw) * rdxc_m;
+    const double duydx_xp = (ve - v0) * rdxc_p;
+    const double duydy_ym = (v0 - vs) * rdy;
+    const double duydy_yp = (vn - v0) * rdy;
+    const double cym = __ldg(a.cym + i), cyp = __ldg(a.cyp + i);
+    const int cx = ux_idx(i, j, ld);
+    const double ux_xm = 0.5 * __ldg(a.ux + cx - ld) + 0.5 * __ldg(a.ux + cx);
+    const double ux_xp = 0.5 * __ldg(a.ux + cx + 1 - ld) + 0.5 * __ldg(a.ux + cx + 1);
+    const double adv1 = -cym * ux_xm * duydx_xm - cyp * ux_xp * duydx_xp;
+    const double uy_ym = 0.5 * vs + 0.5 * v0;
+    const double uy_yp = 0.5 * v0 + 0.5 * vn;
+    const double adv2 = -0.5 * uy_ym * duydy_ym - 0.5 * uy_yp * duydy_yp;
+    const double dif1 = a.rRe * (duydx_xp - duydx_xm) * __ldg(a.rdxf + i);
+    const double dif2 = a.rRe * (duydy_yp - duydy_ym) * rdy;
+    const double pre = -(__ldg(a.p + c) - __ldg(a.p + c - ld)) * rdy;
+    const double A = (adv1 + adv2) + (dif1 + dif2) + a.ext;
+    const double B = __ldg(a.syb + c);
+    a.sya[c] = A;
+    const double vn_ = v0 + (adt * A + bdt * B + gdt * pre);
+    a.uyn[c] = vn_;
+    if (j == 1) a.uyn[c + a.jtot * ld] = vn_;
+    if (j == a.jtot) a.uyn[c - a.jtot * ld] = vn_;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Projection (src/fluid/correct_velocity.c:6-42), optionally preceded by the
+// IBM field response (src/suspensions/update.c:36-59) and followed by the
+// pressure update (src/fluid/update_pressure.c:7-24), in one pass. The IBM
+// response and the projection are applied as two separately rounded updates,
+// as the reference applies them in two functions.
+struct CorrArgs {
+  double *ux, *uy, *p;
+  const double *psi, *dux, *duy, *rdxc, *dt;
+  double gamma, rdy;
+  int itot, jtot, ld, with_ibm, with_proj, with_pressure;
+};
+
+__global__ void __launch_bounds__(TX *TY) k_correct(CorrArgs a) {
+  const int i = 1 + blockIdx.x * TX + threadIdx.x;
+  const int j = 1 + blockIdx.y * TY + threadIdx.y;
+  if (i > a.itot || j > a.jtot) return;
+  const int ld = a.ld, jtot = a.jtot, itot = a.itot;
+  const double gdt = a.with_proj ? a.gamma * __ldg(a.dt) : 0.;
+  const int cy = uy_idx(i, j, ld);
+  const double psi0 = (a.with_proj || a.with_pressure) ? __ldg(a.psi + cy) : 0.;
+  const bool vel = a.with_ibm || a.with_proj;
+  if (vel && i >= 2) {
+    const int c = ux_idx(i, j, ld);
+    double u = a.ux[c];
+    if (a.with_ibm) u = u + 0.5 * (__ldg(a.dux + cy - 1) + __ldg(a.dux + cy));
+    if (a.with_proj) u = u - gdt * (psi0 - __ldg(a.psi + cy - 1)) * __ldg(a.rdxc + i);
+    a.ux[c] = u;
+    if (j == 1) a.ux[c + jtot * ld] = u;
+    if (j == jtot) a.ux[c - jtot * ld] = u;
+  }
+  if (vel) {
+    double v = a.uy[cy];
+    if (a.with_ibm) v = v + 0.5 * (__ldg(a.duy + cy - ld) + __ldg(a.duy + cy));
+    if (a.with_proj) v = v - gdt * (psi0 - __ldg(a.psi + cy - ld)) * a.rdy;
+    a.uy[cy] = v;
+    if (j == 1) a.uy[cy + jtot * ld] = v;
+    if (j == jtot) a.uy[cy - jtot * ld] = v;
+  }
+  if (a.with_pressure) {
+    const double pv = a.p[cy] + psi0;
+    a.p[cy] = pv;
+    // periodic halo rows and Neumann wall copies (boundary_conditions.c:45-62)
+    if (j == 1) a.p[cy + jtot * ld] = pv;
+    if (j == jtot) a.p[cy - jtot * ld] = pv;
+    if (i == 1) {
+      a.p[cy - 1] = pv;
+      if (j == 1) a.p[cy - 1 + jtot * ld] = pv;
+      if (j == jtot) a.p[cy - 1 - jtot * ld] = pv;
+    }
+    if (i == itot) {
+      a.p[cy + 1] = pv;
+      if (j == 1) a.p[cy + 1 + jtot * ld] = pv;
+      if (j == jtot) a.p[cy + 1 - jtot * ld] = pv;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// dt: column maxima of |ux| and the global maximum of |uy| as order-preserving
+// integer maxima of the IEEE bit patterns (non-negative doubles order like
+// their bits), so the result is independent of the reduction order.
+__global__ void k_dt_colmax(const double *__restrict__ ux, const double *__restrict__ uy, int itot, int jtot, int ld,
+                            unsigned long long *__restrict__ colmax, unsigned long long *__restrict__ uymax,
+                            unsigned *__restrict__ flags) {
+  const int i = 1 + blockIdx.x * TX + threadIdx.x;
+  unsigned long long mx = 0ull, my = 0ull;
+  bool bad = false;
+  if (i <= itot) {
+    for (int j = 1 + blockIdx.y * TY + threadIdx.y; j <= jtot; j += TY * gridDim.y) {
+      if (i >= 2) {
+        const unsigned long long b = __double_as_longlong(__ldg(ux + ux_idx(i, j, ld))) & 0x7fffffffffffffffull;
+        bad |= b >= 0x7ff0000000000000ull;
+        mx = b > mx ? b : mx;
+      }
+      const unsigned long long b = __double_as_longlong(__ldg(uy + uy_idx(i, j, ld))) & 0x7fffffffffffffffull;
+      bad |= b >= 0x7ff0000000000000ull;
+      my = b > my ? b : my;
+    }
+  }
+  __shared__ unsigned long long sx[TY][TX];
+  sx[threadIdx.y][threadIdx.x] = mx;
+  // maximum of uy over the block: warp reduce then one atomic per warp
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long other = __shfl_xor_sync(0xffffffffu, my, o);
+    my = other > my ? other : my;
+  }
+  if (threadIdx.x == 0 && my) atomicMax(uymax, my);
+  if (bad) atomicOr(flags, EIF_FLAG_NONFINITE);
+  __syncthreads();
+  if (threadIdx.y == 0 && i <= itot && i >= 2) {
+    unsigned long long m = 0ull;
+    for (int r = 0; r < TY; r++) m = sx[r][threadIdx.x] > m ? sx[r][threadIdx.x] : m;
+    if (m) atomicMax(colmax + i, m);
+  }
+}
+
+// dt from the maxima (decide_dt.c:25-80): one block.
+__global__ void k_dt_final(const unsigned long long *__restrict__ colmax, const unsigned long long *__restrict__ uymax,
+                           const double *__restrict__ dxc, int itot, double dy, double Re, double lx, double dx_uniform,
+                           double sf_adv, double sf_dif, double sf_par, const double *__restrict__ P, int pcap, int np,
+                           double *__restrict__ dt_out) {
+  const double small = 1.e-8;
+  double dta = 5.e-2, dxmin = lx, dtp = DBL_MAX;
+  for (int i = 2 + threadIdx.x; i <= itot; i += blockDim.x) {
+    const double vel = fmax(__longlong_as_double((long long)colmax[i]), small);
+    dta = fmin(dta, dxc[i] / vel);
+    dxmin = fmin(dxmin, dxc[i]);
+  }
+  if (threadIdx.x == 0) {
+    const double vel = fmax(__longlong_as_double((long long)uymax[0]), small);
+    dta = fmin(dta, dy / vel);
+  }
+  const double delta = fmin(dx_uniform, dy);
+  for (int n = threadIdx.x; n < np; n += blockDim.x) {
+    const double a = P[EIF_P_A * pcap + n], b = P[EIF_P_B * pcap + n];
+    const double r = fmax(a, b);
+    const double vz = P[EIF_P_VZ * pcap + n];
+    const double pux = fmax(fabs(P[EIF_P_UX * pcap + n]) + fabs(r * vz), small);
+    const double puy = fmax(fabs(P[EIF_P_UY * pcap + n]) + fabs(r * vz), small);
+    dtp = fmin(dtp, delta / fmax(pux, puy));
+  }
+  __shared__ double s[3][32];
+  for (int o = 16; o > 0; o >>= 1) {
+    dta = fmin(dta, __shfl_xor_sync(0xffffffffu, dta, o));
+    dxmin = fmin(dxmin, __shfl_xor_sync(0xffffffffu, dxmin, o));
+    dtp = fmin(dtp, __shfl_xor_sync(0xffffffffu, dtp, o));
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) { s[0][w] = dta; s[1][w] = dxmin; s[2][w] = dtp; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int nw = blockDim.x >> 5;
+    for (int k = 1; k < nw; k++) { dta = fmin(dta, s[0][k]); dxmin = fmin(dxmin, s[1][k]); dtp = fmin(dtp, s[2][k]); }
+    dta *= sf_adv;
+    double difx = 0.25 * Re * (dxmin * dxmin);
+    double dify = 0.25 * Re * (dy * dy);
+    difx *= sf_dif;
+    dify *= sf_dif;
+    dtp *= sf_par;
+    *dt_out = fmin(fmin(dta, fmin(difx, dify)), dtp);
+  }
+}
+
+// ---------------------------------------------------------------------------
+__global__ void k_divergence(const double *__restrict__ ux, const double *__restrict__ uy, const double *__restrict__ rdxf,
+                             double rdy, int itot, int jtot, int ld, double *__restrict__ out /* per block: max, sum */) {
+  double mx = 0., sm = 0.;
+  const int n = itot * jtot;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const int i = 1 + t % itot, j = 1 + t / itot;
+    const double d = (ux[ux_idx(i + 1, j, ld)] - ux[ux_idx(i, j, ld)]) * rdxf[i] +
+                     (uy[uy_idx(i, j + 1, ld)] - uy[uy_idx(i, j, ld)]) * rdy;
+    mx = fmax(mx, fabs(d));
+    sm += d;
+  }
+  mx = eifd::warp_max(mx);
+  sm = eifd::warp_sum(sm);
+  __shared__ double s[2][32];
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) { s[0][w] = mx; s[1][w] = sm; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int k = 1; k < (int)(blockDim.x >> 5); k++) { mx = fmax(mx, s[0][k]); sm += s[1][k]; }
+    out[2 * blockIdx.x] = mx;
+    out[2 * blockIdx.x + 1] = sm;
+  }
+}
+
+}  // namespace
+
+namespace eif {
+
+RK rk_coef(int rk) {
+  // src/param/init.c:177-189
+  static const double al[3] = {32. / 60., 25. / 60., 45. / 60.};
+  static const double be[3] = {0. / 60., -17. / 60., -25. / 60.};
+  return RK{al[rk], be[rk], al[rk] + be[rk]};
+}
+
+static dim3 cell_grid(const eif_ctx *c) {
+  return dim3((c->itot + TX - 1) / TX, (c->jtot + TY - 1) / TY);
+}
+
+int launch_bc_p_like(eif_ctx *c, double *a) {
+  EIF_PROF(c, "boundaries", 1);
+  const int n = (c->itot > c->jtot ? c->itot : c->jtot) + 2;
+  k_bc<<<(n + 255) / 256, 256, 0, c->stream>>>(a, 2, c->itot, c->jtot, c->ld, 0., 0.);
+  EIF_LAUNCH_CK(c);
+  return EIF_OK;
+}
+
+int launch_boundaries(eif_ctx *c) {
+  EIF_PROF(c, "boundaries", 5);
+  const int n = (c->itot > c->jtot ? c->itot : c->jtot) + 2;
+  for (int b = 0; b < 2; b++) {
+    k_bc<<<(n + 255) / 256, 256, 0, c->stream>>>(c->ux[b], 0, c->itot, c->jtot, c->ld, 0., 0.);
+    k_bc<<<(n + 255) / 256, 256, 0, c->stream>>>(c->uy[b], 1, c->itot, c->jtot, c->ld, c->cfg.uy_wall[0],
+                                                 c->cfg.uy_wall[1]);
+  }
+  k_bc<<<(n + 255) / 256, 256, 0, c->stream>>>(c->p, 2, c->itot, c->jtot, c->ld, 0., 0.);
+  EIF_LAUNCH_CK(c);
+  return EIF_OK;
+}
+
+int launch_predictor(eif_ctx *c, int rk) {
+  const RK k = rk_coef(rk);
+  // the explicit term of the previous stage becomes srcB (update_velocity.c:26,110)
+  c->scur = 1 - c->scur;
+  PredArgs a;
+  a.ux = c->ux[c->cur];
+  a.uy = c->uy[c->cur];
+  a.p = c->p;
+  a.sxb = c->sxa[1 - c->scur];
+  a.syb = c->sya[1 - c->scur];
+  a.sxa = c->sxa[c->scur];
+  a.sya = c->sya[c->scur];
+  a.uxn = c->ux[1 - c->cur];
+  a.uyn = c->uy[1 - c->cur];
+  a.rdxf = c->rdxf; a.rdxc = c->rdxc;
+  a.cxm = c->cxm; a.cxp = c->cxp; a.cym = c->cym; a.cyp = c->cyp;
+  a.dt = c->d_scal;
+  a.alpha = k.alpha; a.beta = k.beta; a.gamma = k.gamma;
+  a.rRe = 1. / c->cfg.Re;
+  a.rdy = 1. / c->dy;
+  a.ext = c->cfg.extfrcy;
+  a.itot = c->itot; a.jtot = c->jtot; a.ld = c->ld;
+  EIF_PROF(c, "predictor", 1);
+  k_predictor<<<cell_grid(c), dim3(TX, TY), 0, c->stream>>>(a);
+  EIF_LAUNCH_CK(c);
+  c->cur = 1 - c->cur;
+  return EIF_OK;
+}
+
+static int launch_corr(eif_ctx *c, int rk, int with_ibm, int with_proj, int with_pressure) {
+  CorrArgs a;
+  a.ux = c->ux[c->cur];
+  a.uy = c->uy[c->cur];
+  a.p = c->p;
+  a.psi = c->psi;
+  a.dux = c->dux;
+  a.duy = c->duy;
+  a.rdxc = c->rdxc;
+  a.dt = c->d_scal;
+  a.gamma = rk >= 0 ? rk_coef(rk).gamma : 0.;
+  a.rdy = 1. / c->dy;
+  a.itot = c->itot; a.jtot = c->jtot; a.ld = c->ld;
+  a.with_ibm = with_ibm; a.with_proj = with_proj; a.with_pressure = with_pressure;
+  EIF_PROF(c, "correct", 1);
+  k_correct<<<cell_grid(c), dim3(TX, TY), 0, c->stream>>>(a);
+  EIF_LAUNCH_CK(c);
+  return EIF_OK;
+}
+
+int launch_update_momentum_field(eif_ctx *c) { return launch_corr(c, -1, 1, 0, 0); }
+int launch_correct(eif_ctx *c, int rk, bool with_ibm, bool with_pressure) {
+  return launch_corr(c, rk, with_ibm ? 1 : 0, 1, with_pressure ? 1 : 0);
+}
+int launch_update_pressure(eif_ctx *c) { return launch_corr(c, -1, 0, 0, 1); }
+
+int launch_decide_dt(eif_ctx *c) {
+  unsigned long long *colmax = reinterpret_cast<unsigned long long *>(c->qhat);  // scratch: itot+2 words
+  unsigned long long *uymax = colmax + c->itot + 2;
+  EIF_PROF(c, "decide_dt", 2);
+  EIF_CK(c, cudaMemsetAsync(colmax, 0, sizeof(unsigned long long) * (c->itot + 3), c->stream));
+  int gy = (c->jtot + TY - 1) / TY;
+  const int gx = (c->itot + TX - 1) / TX;
+  const int target = c->sms * 8;
+  if (gx * gy > target) gy = (target + gx - 1) / gx;
+  if (gy < 1) gy = 1;
+  k_dt_colmax<<<dim3(gx, gy), dim3(TX, TY), 0, c->stream>>>(c->ux[c->cur], c->uy[c->cur], c->itot, c->jtot, c->ld,
+                                                            colmax, uymax, c->d_flags);
+  EIF_LAUNCH_CK(c);
+  k_dt_final<<<1, 256, 0, c->stream>>>(colmax, uymax, c->dxc, c->itot, c->dy, c->cfg.Re, c->lx, c->dx,
+                                       c->cfg.safefactors[0], c->cfg.safefactors[1], c->cfg.safefactors[2], c->P,
+                                       c->pcap, c->np, c->d_scal);
+  EIF_LAUNCH_CK(c);
+  return EIF_OK;
+}
+
+int launch_divergence(eif_ctx *c, double *divmax, double *divsum) {
+  const int blocks = c->sms * 2;
+  double *part = c->qhat;  // scratch
+  EIF_PROF(c, "divergence", 1);
+  k_divergence<<<blocks, 256, 0, c->stream>>>(c->ux[c->cur], c->uy[c->cur], c->rdxf, 1. / c->dy, c->itot, c->jtot,
+                                               c->ld, part);
+  EIF_LAUNCH_CK(c);
+  double *h = new double[2 * blocks];
+  cudaError_t e = cudaMemcpyAsync(h, part, sizeof(double) * 2 * blocks, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) {
+    delete[] h;
+    return check_cuda(c, e, "divergence readback");
+  }
+  double mx = 0., sm = 0.;
+  for (int b = 0; b < blocks; b++) { mx = fmax(mx, h[2 * b]); sm += h[2 * b + 1]; }
+  delete[] h;
+  *divmax = mx;
+  *divsum = sm;
+  return EIF_OK;
+}
+
+}  // namespace eif

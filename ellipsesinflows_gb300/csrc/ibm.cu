@@ -1,0 +1,549 @@
+// Immersed-boundary kernels: smoothed indicator, momentum exchange and the
+// volume integrals of the particle interiors.
+//
+// Reference functions restated here (NaokiHori/EllipsesInFlows):
+//   suspensions_decide_loop_size   src/suspensions/auxiliary.c:11-17
+//   compute_signed_dist            src/suspensions/auxiliary.c:19-47
+//   suspensions_s_weight/v_weight  src/suspensions/auxiliary.c:51-59
+//   mass, moment of inertia        src/suspensions/auxiliary.c:63-75
+//   find_normal_t, compute_ex/ey   src/ellipse.c:7-65
+//   kernel_exchange_momentum       src/suspensions/exchange.c:13-88
+//   compute_inertia                src/suspensions/inertia.c:9-70
+//
+// Work decomposition. For every particle the reference visits, for the
+// periodic images -1, 0, +1, the cells of a clipped bounding box. Here those
+// cells are enumerated in the same (image, j, i) order and cut into chunks of
+// CHUNK cells. One warp evaluates one chunk (two cells per lane) inside a
+// persistent grid sized to the SM count, so particles of any size keep all
+// SMs busy. Per-particle sums are reduced per chunk with warp shuffles and
+// then per particle over its chunks in a fixed order: results are
+// deterministic. The momentum exchange also stores each box cell's field
+// contribution in a scratch buffer; a tile gather then adds, for every cell,
+// the contributions of all covering boxes in (particle, image) order, which
+// is the reference's accumulation order (exchange.c:71-72), without atomics.
+#include "eif_internal.cuh"
+#include <cfloat>
+#include <vector>
+#include <algorithm>
+#include <cmath>
+
+namespace {
+
+constexpr int CHUNK = 64;       // cells per warp task
+constexpr int NEXTRA = 3;       // auxiliary.c:8
+constexpr double BETA = 2.;     // auxiliary.c:49
+constexpr int GTX = 64, GTY = 8, GTHREADS = 256;  // gather tile and block
+constexpr int LMAX = 1024;      // list capacity of one gather tile
+
+// per-particle geometry needed by a box cell evaluation
+struct Ell {
+  double a, b, px, py, cz, sz;   // semi-axes, centre, cos(-az), sin(-az)
+  double kex, key, ab2;          // a(1-(b/a)^2), b(1-(a/b)^2), a*a+b*b
+};
+
+__device__ __forceinline__ Ell make_ell(double a, double b, double px, double py, double az) {
+  Ell e;
+  e.a = a; e.b = b; e.px = px; e.py = py;
+  sincos(-az, &e.sz, &e.cz);
+  e.kex = a * (1. - (b / a) * (b / a));
+  e.key = b * (1. - (a / b) * (a / b));
+  e.ab2 = a * a + b * b;
+  return e;
+}
+
+// ellipse.c:30-65 (x_, y_ in the body frame)
+__device__ __forceinline__ double normal_t(const Ell &e, double x_, double y_) {
+  const double px = fabs(x_), py = fabs(y_);
+  double t = 0.25 * M_PI;
+  for (int n = 0;; n++) {
+    double st, ct;
+    sincos(t, &st, &ct);
+    const double x = e.a * ct, y = e.b * st;
+    const double ex = e.kex * (ct * ct * ct);
+    const double ey = e.key * (st * st * st);
+    const double rx = x - ex, ry = y - ey;
+    const double qx = px - ex, qy = py - ey;
+    const double r = sqrt(ry * ry + rx * rx);
+    const double q = sqrt(qy * qy + qx * qx);
+    const double dc = r * asin((rx * qy - ry * qx) / (r * q));
+    const double dt = dc / sqrt(e.ab2 - x * x - y * y);
+    t += dt;
+    t = fmin(0.5 * M_PI, t);
+    t = fmax(0., t);
+    if (fabs(dt) < 1.e-8) break;
+    if (n > EIF_NORMAL_MAX_ITER - 1) break;
+  }
+  if (x_ < 0.) t = M_PI - t;
+  if (y_ < 0.) t = -t;
+  return t;
+}
+
+// auxiliary.c:19-47, in units of the grid size h (rh = 1/h)
+__device__ __forceinline__ double signed_dist(const Ell &e, double x, double y, double rh) {
+  const double ddx = x - e.px, ddy = y - e.py;
+  const double x_ = e.cz * ddx - e.sz * ddy;
+  const double y_ = e.sz * ddx + e.cz * ddy;
+  const double f0 = 1. - (x_ / e.a) * (x_ / e.a) - (y_ / e.b) * (y_ / e.b);
+  const double sign = f0 > 0. ? 1. : -1.;
+  const double t = normal_t(e, x_, y_);
+  double st, ct;
+  sincos(t, &st, &ct);
+  const double dxx = e.a * ct - x_, dyy = e.b * st - y_;
+  return sign * sqrt(dxx * dxx + dyy * dyy) * rh;
+}
+
+// auxiliary.c:11-17
+__device__ __forceinline__ void loop_size(int lb, int ub, double h, double r, double gc, int &mn, int &mx) {
+  mn = (int)(floor((gc - r) / h) - NEXTRA);
+  mx = (int)(ceil((gc + r) / h) + NEXTRA);
+  mn = mn < lb ? lb : mn;
+  mx = mx > ub ? ub : mx;
+}
+
+__device__ __forceinline__ double pmass(double den, double a, double b) { return den * (M_PI * a * b); }
+__device__ __forceinline__ double pmoi(double den, double a, double b) {
+  return 0.25 * pmass(den, a, b) * (a * a + b * b);
+}
+
+struct BoxArgs {
+  const double *P;
+  int pcap, np, itot, jtot, use_increment;
+  double dx, dy, ly, yf1;
+  int *box, *nchunk;
+};
+
+// per-particle boxes of the three periodic images and their chunk counts
+__global__ void k_boxes(BoxArgs a) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= a.np) return;
+  const double *P = a.P;
+  const int pc = a.pcap;
+  const double pa = P[EIF_P_A * pc + n], pb = P[EIF_P_B * pc + n];
+  double px = P[EIF_P_X * pc + n], py = P[EIF_P_Y * pc + n];
+  if (a.use_increment) {
+    px = px + P[EIF_P_DX * pc + n];
+    py = py + P[EIF_P_DY * pc + n];
+  }
+  const double r = fmax(pa, pb);
+  int cells = 0;
+  for (int per = -1; per <= 1; per++) {
+    int imin, imax, jmin, jmax;
+    loop_size(1, a.itot, a.dx, r, px, imin, imax);
+    loop_size(1, a.jtot, a.dy, r, py + a.ly * per - a.yf1, jmin, jmax);
+    int *bx = a.box + 12 * n + 4 * (per + 1);
+    bx[0] = imin; bx[1] = imax; bx[2] = jmin; bx[3] = jmax;
+    if (imax >= imin && jmax >= jmin) cells += (imax - imin + 1) * (jmax - jmin + 1);
+  }
+  a.nchunk[n] = (cells + CHUNK - 1) / CHUNK;
+}
+
+// exclusive scan of the chunk counts (one block); off[np] = total
+__global__ void k_scan(const int *__restrict__ cnt, int *__restrict__ off, int np) {
+  __shared__ int s[1024];
+  __shared__ int carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int base = 0; base < np; base += 1024) {
+    const int t = base + threadIdx.x;
+    const int v = t < np ? cnt[t] : 0;
+    s[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+      const int add = threadIdx.x >= o ? s[threadIdx.x - o] : 0;
+      __syncthreads();
+      s[threadIdx.x] += add;
+      __syncthreads();
+    }
+    if (t < np) off[t] = carry + s[threadIdx.x] - v;
+    __syncthreads();
+    if (threadIdx.x == 1023) carry += s[1023];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) off[np] = carry;
+}
+
+// locate a chunk's particle: largest n with off[n] <= c
+__device__ __forceinline__ int find_particle(const int *__restrict__ off, int np, int c) {
+  int lo = 0, hi = np - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(off + mid) <= c) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// map a particle-local cell index to (i, j, image) using its boxes
+__device__ __forceinline__ bool cell_of(const int *bx, int k, int &i, int &j, int &img) {
+  for (int m = 0; m < 3; m++) {
+    const int w = bx[4 * m + 1] - bx[4 * m + 0] + 1;
+    const int h = bx[4 * m + 3] - bx[4 * m + 2] + 1;
+    if (w <= 0 || h <= 0) continue;
+    const int cnt = w * h;
+    if (k < cnt) {
+      img = m - 1;
+      j = bx[4 * m + 2] + k / w;
+      i = bx[4 * m + 0] + k % w;
+      return true;
+    }
+    k -= cnt;
+  }
+  return false;
+}
+
+struct WorkArgs {
+  const double *P;
+  const double *ux, *uy, *xc, *yc, *dt;
+  const int *box, *off;
+  double *partial;   // 3 per chunk
+  double2 *wbuf;     // CHUNK per chunk (exchange only)
+  int pcap, np, ld, mode, cn;   // mode 0: inertia (cn), 1: exchange
+  double dx, dy, ly, h;
+};
+
+// one warp per chunk of box cells: indicator weights, partial sums, and (for
+// the exchange) per-cell field contributions
+__global__ void __launch_bounds__(256) k_ibm_work(WorkArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const int total = __ldg(a.off + a.np);
+  const double rh = 1. / a.h;
+  const double dxdy = a.dx * a.dy;
+  const double dtv = a.mode == 1 ? __ldg(a.dt) : 0.;
+  const int pc = a.pcap, ld = a.ld;
+  for (int c = warp; c < total; c += nwarps) {
+    const int n = find_particle(a.off, a.np, c);
+    const int local0 = (c - __ldg(a.off + n)) * CHUNK;
+    int bx[12];
+#pragma unroll
+    for (int q = 0; q < 12; q++) bx[q] = __ldg(a.box + 12 * n + q);
+    const double *P = a.P;
+    const double pden = __ldg(P + EIF_P_DEN * pc + n), pa = __ldg(P + EIF_P_A * pc + n), pb = __ldg(P + EIF_P_B * pc + n);
+    double px = __ldg(P + EIF_P_X * pc + n), py = __ldg(P + EIF_P_Y * pc + n), paz = __ldg(P + EIF_P_AZ * pc + n);
+    if (a.mode == 0) {
+      // inertia.c:29-31: positions at k + increment
+      px = px + __ldg(P + EIF_P_DX * pc + n);
+      py = py + __ldg(P + EIF_P_DY * pc + n);
+      paz = paz + __ldg(P + EIF_P_DAZ * pc + n);
+    }
+    const double pm = pmass(pden, pa, pb);
+    const double pim = pmoi(pden, pa, pb);
+    const double pux = __ldg(P + EIF_P_UX * pc + n), puy = __ldg(P + EIF_P_UY * pc + n), pvz = __ldg(P + EIF_P_VZ * pc + n);
+    Ell e0 = make_ell(pa, pb, px, py, paz);
+    double s0 = 0., s1 = 0., s2 = 0.;
+#pragma unroll
+    for (int half = 0; half < CHUNK / 32; half++) {
+      const int kk = local0 + half * 32 + lane;
+      int i, j, img;
+      double2 contrib = make_double2(0., 0.);
+      if (cell_of(bx, kk, i, j, img)) {
+        const double py_ = py + a.ly * img;
+        Ell e = e0;
+        e.py = py_;
+        const double x = __ldg(a.xc + i), y = __ldg(a.yc + j);
+        const double d = signed_dist(e, x, y, rh);
+        const double th = tanh(BETA * d);
+        const double uxf = 0.5 * (__ldg(a.ux + j * ld + (i - 1)) + __ldg(a.ux + j * ld + i));
+        const double uyf = 0.5 * (__ldg(a.uy + j * ld + i) + __ldg(a.uy + (j + 1) * ld + i));
+        if (a.mode == 0) {
+          // inertia.c:51-59
+          const double w = 0.5 * (1. + th);
+          const double valx = w * 0.5 * (2. * uxf) * dxdy;
+          const double valy = w * 0.5 * (2. * uyf) * dxdy;
+          s0 += valx / pm;
+          s1 += valy / pm;
+          s2 += (-(y - py_) * valx / pim) + ((x - px) * valy / pim);
+        } else {
+          // exchange.c:61-76
+          const double w = 0.5 * BETA * (1. - th * th);
+          const double uxp = pux - pvz * (y - py_);
+          const double uyp = puy + pvz * (x - px);
+          const double fx = w * (uxp - uxf) / dtv;
+          const double fy = w * (uyp - uyf) / dtv;
+          contrib = make_double2(fx * dtv, fy * dtv);
+          const double Fx = fx * a.dx * a.dy, Fy = fy * a.dx * a.dy;
+          s0 += -(Fx / pm);
+          s1 += -(Fy / pm);
+          s2 += ((y - py_) * Fx / pim) - ((x - px) * Fy / pim);
+        }
+      }
+      if (a.mode == 1) a.wbuf[(size_t)c * CHUNK + half * 32 + lane] = contrib;
+    }
+    s0 = eifd::warp_sum(s0);
+    s1 = eifd::warp_sum(s1);
+    s2 = eifd::warp_sum(s2);
+    if (lane == 0) {
+      a.partial[3 * (size_t)c + 0] = s0;
+      a.partial[3 * (size_t)c + 1] = s1;
+      a.partial[3 * (size_t)c + 2] = s2;
+    }
+  }
+}
+
+// per-particle sums over chunks in a fixed order (warp per particle)
+__global__ void k_chunk_reduce(const double *__restrict__ partial, const int *__restrict__ off, double *__restrict__ P,
+                               int pcap, int np, int f0, int f1, int f2) {
+  const int lane = threadIdx.x & 31;
+  const int n = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (n >= np) return;
+  const int c0 = off[n], c1 = off[n + 1];
+  double s0 = 0., s1 = 0., s2 = 0.;
+  for (int c = c0 + lane; c < c1; c += 32) {
+    s0 += partial[3 * (size_t)c + 0];
+    s1 += partial[3 * (size_t)c + 1];
+    s2 += partial[3 * (size_t)c + 2];
+  }
+  s0 = eifd::warp_sum(s0);
+  s1 = eifd::warp_sum(s1);
+  s2 = eifd::warp_sum(s2);
+  if (lane == 0) {
+    P[f0 * pcap + n] = s0;
+    P[f1 * pcap + n] = s1;
+    P[f2 * pcap + n] = s2;
+  }
+}
+
+struct GatherArgs {
+  const int *box, *off;
+  const double2 *wbuf;
+  double *dux, *duy;
+  unsigned *flags;
+  int np, itot, jtot, ld;
+};
+
+// field response dux/duy (exchange.c:71-72,80-81): per tile, the ordered list
+// of covering (particle, image) boxes, then per cell the sum in that order
+__global__ void __launch_bounds__(GTHREADS) k_gather(GatherArgs a) {
+  __shared__ int list[LMAX];
+  __shared__ int cnt[1024 / 32 + 1];
+  __shared__ int nlist;
+  const int i0 = 1 + blockIdx.x * GTX, j0 = 1 + blockIdx.y * GTY;
+  const int i1 = min(i0 + GTX - 1, a.itot), j1 = min(j0 + GTY - 1, a.jtot);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = GTHREADS / 32;
+  const int ngroups = (a.np + 31) / 32;
+  double acc_x[2] = {0., 0.}, acc_y[2] = {0., 0.};
+  // cells of this thread: (i0 + lx, j0 + ly) for two rows
+  const int lx = threadIdx.x % GTX, ly0 = threadIdx.x / GTX;  // GTHREADS / GTX = 4 rows per pass
+  for (int gbase = 0; gbase < ngroups; gbase += 32) {
+    // phase 1: count covering images per particle group
+    unsigned masks_dummy = 0;
+    (void)masks_dummy;
+    for (int g = gbase + warp; g < min(gbase + 32, ngroups); g += nw) {
+      const int n = g * 32 + lane;
+      int m = 0;
+      if (n < a.np) {
+        for (int q = 0; q < 3; q++) {
+          const int *bx = a.box + 12 * n + 4 * q;
+          if (bx[0] <= i1 && bx[1] >= i0 && bx[2] <= j1 && bx[3] >= j0 && bx[1] >= bx[0] && bx[3] >= bx[2]) m++;
+        }
+      }
+      // inclusive warp scan of m
+      int s = m;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, s, o);
+        if (lane >= o) s += v;
+      }
+      if (lane == 31) cnt[g - gbase] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int tot = 0;
+      for (int g = 0; g < min(32, ngroups - gbase); g++) {
+        const int v = cnt[g];
+        cnt[g] = tot;
+        tot += v;
+      }
+      nlist = tot;
+    }
+    __syncthreads();
+    const int L = nlist;
+    if (L > LMAX) {
+      if (threadIdx.x == 0) atomicOr(a.flags, EIF_FLAG_NOCONV);
+      return;
+    }
+    // phase 2: ordered fill
+    for (int g = gbase + warp; g < min(gbase + 32, ngroups); g += nw) {
+      const int n = g * 32 + lane;
+      int m = 0, bits = 0;
+      if (n < a.np) {
+        for (int q = 0; q < 3; q++) {
+          const int *bx = a.box + 12 * n + 4 * q;
+          if (bx[0] <= i1 && bx[1] >= i0 && bx[2] <= j1 && bx[3] >= j0 && bx[1] >= bx[0] && bx[3] >= bx[2]) {
+            bits |= 1 << q;
+            m++;
+          }
+        }
+      }
+      int s = m;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, s, o);
+        if (lane >= o) s += v;
+      }
+      int pos = cnt[g - gbase] + s - m;
+      for (int q = 0; q < 3; q++) {
+        if (bits & (1 << q)) list[pos++] = 3 * n + q;
+      }
+    }
+    __syncthreads();
+    // phase 3: accumulate in list order
+    for (int e = 0; e < L; e++) {
+      const int n = list[e] / 3, q = list[e] % 3;
+      const int *bx = a.box + 12 * n;
+      // offset of image q within the particle's enumeration
+      int base = 0;
+      for (int m = 0; m < q; m++) {
+        const int w = bx[4 * m + 1] - bx[4 * m] + 1, h = bx[4 * m + 3] - bx[4 * m + 2] + 1;
+        if (w > 0 && h > 0) base += w * h;
+      }
+      const int bi0 = bx[4 * q], bi1 = bx[4 * q + 1], bj0 = bx[4 * q + 2], bj1 = bx[4 * q + 3];
+      const int w = bi1 - bi0 + 1;
+      const size_t pbase = (size_t)__ldg(a.off + n) * CHUNK + base;
+#pragma unroll
+      for (int r = 0; r < 2; r++) {
+        const int i = i0 + lx, j = j0 + ly0 + 4 * r;
+        if (i >= bi0 && i <= bi1 && j >= bj0 && j <= bj1) {
+          const double2 v = a.wbuf[pbase + (size_t)(j - bj0) * w + (i - bi0)];
+          acc_x[r] += v.x;
+          acc_y[r] += v.y;
+        }
+      }
+    }
+    __syncthreads();
+  }
+  // write the tile (zero where no box covers), periodic halo rows and Neumann columns
+  const int ld = a.ld, jtot = a.jtot, itot = a.itot;
+#pragma unroll
+  for (int r = 0; r < 2; r++) {
+    const int i = i0 + lx, j = j0 + ly0 + 4 * r;
+    if (i > i1 || j > j1) continue;
+    const int cidx = j * ld + i;
+    const double vx = acc_x[r], vy = acc_y[r];
+    a.dux[cidx] = vx; a.duy[cidx] = vy;
+    if (j == 1) { a.dux[cidx + jtot * ld] = vx; a.duy[cidx + jtot * ld] = vy; }
+    if (j == jtot) { a.dux[cidx - jtot * ld] = vx; a.duy[cidx - jtot * ld] = vy; }
+    if (i == 1) {
+      a.dux[cidx - 1] = vx; a.duy[cidx - 1] = vy;
+      if (j == 1) { a.dux[cidx - 1 + jtot * ld] = vx; a.duy[cidx - 1 + jtot * ld] = vy; }
+      if (j == jtot) { a.dux[cidx - 1 - jtot * ld] = vx; a.duy[cidx - 1 - jtot * ld] = vy; }
+    }
+    if (i == itot) {
+      a.dux[cidx + 1] = vx; a.duy[cidx + 1] = vy;
+      if (j == 1) { a.dux[cidx + 1 + jtot * ld] = vx; a.duy[cidx + 1 + jtot * ld] = vy; }
+      if (j == jtot) { a.dux[cidx + 1 - jtot * ld] = vx; a.duy[cidx + 1 - jtot * ld] = vy; }
+    }
+  }
+}
+
+}  // namespace
+
+namespace eif {
+
+// Bound on the box cells of one particle over its three images. A box spans at
+// most 2r/h + 2 + 2*NEXTRA + 1 cells per direction before clipping; the three
+// images are shifted by exactly jtot rows, so their clipped row ranges together
+// never exceed the unclipped height.
+static size_t box_cells_bound(const eif_ctx *c, double r) {
+  const long w = (long)std::ceil(2. * r / c->dx) + 2 + 2 * NEXTRA + 2;
+  const long h = (long)std::ceil(2. * r / c->dy) + 2 + 2 * NEXTRA + 2;
+  const long wc = std::min<long>(w, c->itot);
+  const long hc = std::min<long>(h, 3L * c->jtot);
+  return (size_t)wc * (size_t)hc;
+}
+
+int ibm_reserve(eif_ctx *c) {
+  // called after a particle push: size the chunk and scratch buffers from the radii
+  ibm_free(c);
+  if (c->np == 0) return EIF_OK;
+  std::vector<double> a(c->np), b(c->np);
+  EIF_CK(c, cudaMemcpy(a.data(), c->P + EIF_P_A * c->pcap, sizeof(double) * c->np, cudaMemcpyDeviceToHost));
+  EIF_CK(c, cudaMemcpy(b.data(), c->P + EIF_P_B * c->pcap, sizeof(double) * c->np, cudaMemcpyDeviceToHost));
+  size_t chunks = 0;
+  for (int n = 0; n < c->np; n++) {
+    chunks += (box_cells_bound(c, std::max(a[n], b[n])) + CHUNK - 1) / CHUNK;
+  }
+  c->chunk_cap = (int)chunks;
+  c->wcap = chunks * CHUNK;
+  EIF_CK(c, cudaMalloc((void **)&c->box, sizeof(int) * 12 * c->np));
+  EIF_CK(c, cudaMalloc((void **)&c->chunk_off, sizeof(int) * 2 * (c->np + 1)));
+  EIF_CK(c, cudaMalloc((void **)&c->partial, sizeof(double) * 3 * chunks));
+  EIF_CK(c, cudaMalloc((void **)&c->wbuf, sizeof(double2) * c->wcap));
+  return EIF_OK;
+}
+
+void ibm_free(eif_ctx *c) {
+  if (c->box) cudaFree(c->box);
+  if (c->chunk_off) cudaFree(c->chunk_off);
+  if (c->partial) cudaFree(c->partial);
+  if (c->wbuf) cudaFree(c->wbuf);
+  c->box = nullptr; c->chunk_off = nullptr; c->partial = nullptr; c->wbuf = nullptr;
+  c->chunk_cap = 0; c->wcap = 0;
+}
+
+static int launch_boxes(eif_ctx *c, bool use_increment) {
+  BoxArgs b;
+  b.P = c->P; b.pcap = c->pcap; b.np = c->np; b.itot = c->itot; b.jtot = c->jtot;
+  b.use_increment = use_increment ? 1 : 0;
+  b.dx = c->dx; b.dy = c->dy; b.ly = c->ly; b.yf1 = c->h_yf[0];
+  b.box = c->box;
+  int *cnt = c->chunk_off + (c->np + 1);
+  b.nchunk = cnt;
+  EIF_PROF(c, "ibm_boxes", 2);
+  k_boxes<<<(c->np + 127) / 128, 128, 0, c->stream>>>(b);
+  EIF_LAUNCH_CK(c);
+  k_scan<<<1, 1024, 0, c->stream>>>(cnt, c->chunk_off, c->np);
+  EIF_LAUNCH_CK(c);
+  return EIF_OK;
+}
+
+static int launch_work(eif_ctx *c, int mode, int cn) {
+  WorkArgs w;
+  w.P = c->P; w.ux = c->ux[c->cur]; w.uy = c->uy[c->cur]; w.xc = c->xc; w.yc = c->yc; w.dt = c->d_scal;
+  w.box = c->box; w.off = c->chunk_off; w.partial = c->partial; w.wbuf = reinterpret_cast<double2 *>(c->wbuf);
+  w.pcap = c->pcap; w.np = c->np; w.ld = c->ld; w.mode = mode; w.cn = cn;
+  w.dx = c->dx; w.dy = c->dy; w.ly = c->ly; w.h = std::min(c->dx, c->dy);
+  const int blocks = std::max(1, std::min(c->sms * 8, (c->chunk_cap * 32 + 255) / 256));
+  {
+    EIF_PROF(c, mode == 0 ? "ibm_inertia" : "ibm_exchange", 1);
+    k_ibm_work<<<blocks, 256, 0, c->stream>>>(w);
+    EIF_LAUNCH_CK(c);
+  }
+  const int f0 = mode == 0 ? EIF_P_IUX0 + cn : EIF_P_FUX;
+  const int f1 = mode == 0 ? EIF_P_IUY0 + cn : EIF_P_FUY;
+  const int f2 = mode == 0 ? EIF_P_IVZ0 + cn : EIF_P_TVZ;
+  EIF_PROF(c, "ibm_reduce", 1);
+  k_chunk_reduce<<<(c->np * 32 + 255) / 256, 256, 0, c->stream>>>(c->partial, c->chunk_off, c->P, c->pcap, c->np, f0,
+                                                                    f1, f2);
+  EIF_LAUNCH_CK(c);
+  return EIF_OK;
+}
+
+int launch_inertia(eif_ctx *c, int cn) {
+  if (c->np == 0) return EIF_OK;
+  int rc = launch_boxes(c, true);
+  if (rc) return rc;
+  return launch_work(c, 0, cn);
+}
+
+int launch_exchange(eif_ctx *c) {
+  if (c->np == 0) {
+    EIF_PROF(c, "ibm_gather", 0);
+    EIF_CK(c, cudaMemsetAsync(c->dux, 0, sizeof(double) * c->nfield, c->stream));
+    EIF_CK(c, cudaMemsetAsync(c->duy, 0, sizeof(double) * c->nfield, c->stream));
+    return EIF_OK;
+  }
+  int rc = launch_boxes(c, false);
+  if (rc) return rc;
+  rc = launch_work(c, 1, 0);
+  if (rc) return rc;
+  GatherArgs g;
+  g.box = c->box; g.off = c->chunk_off; g.wbuf = reinterpret_cast<const double2 *>(c->wbuf);
+  g.dux = c->dux; g.duy = c->duy; g.flags = c->d_flags;
+  g.np = c->np; g.itot = c->itot; g.jtot = c->jtot; g.ld = c->ld;
+  dim3 grid((c->itot + GTX - 1) / GTX, (c->jtot + GTY - 1) / GTY);
+  EIF_PROF(c, "ibm_gather", 1);
+  k_gather<<<grid, GTHREADS, 0, c->stream>>>(g);
+  EIF_LAUNCH_CK(c);
+  return EIF_OK;
+}
+
+}  // namespace eif

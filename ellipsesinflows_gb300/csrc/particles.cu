@@ -1,0 +1,390 @@
+// Particle kernels: soft-sphere collisions between ellipses (via equivalent
+// circles), Crank-Nicolson increments, and the final velocity/position update.
+//
+// Reference functions restated here (NaokiHori/EllipsesInFlows):
+//   compute_evolute, find_equivalent_circle(s)   src/suspensions/collision.c:75-154
+//   compute_collision_force_p_p / _p_w           src/suspensions/collision.c:156-304
+//   suspensions_compute_collision_force          src/suspensions/collision.c:306-367
+//   compute_curvature                            src/ellipse.c:17-28
+//   suspensions_reset_particle_increments        src/suspensions/reset.c:7-18
+//   suspensions_increment_particles              src/suspensions/increment.c:10-72
+//   suspensions_update_particles                 src/suspensions/update.c:8-34,61-65
+//
+// Collision force on particle k accumulates, as in the reference, over the
+// pairs in the order of the pair matrix (partners m = 0..N-1, m != k) and
+// then the walls at x = 0 and x = lx. One warp owns one particle: lanes test
+// 32 partners at a time (a conservative single-precision distance test first,
+// then the exact double-precision bounding-circle test of collision.c:173-189);
+// partners that pass are evaluated one per lane and summed in partner order.
+#include "eif_internal.cuh"
+#include <cfloat>
+
+namespace {
+
+struct EllD { double a, b, x, y, angle; };
+
+__device__ __forceinline__ double pmass(double den, double a, double b) { return den * (M_PI * a * b); }
+__device__ __forceinline__ double pmoi(double den, double a, double b) {
+  return 0.25 * pmass(den, a, b) * (a * a + b * b);
+}
+
+// ellipse.c:30-65 with per-call evaluation of the evolute coefficients
+__device__ double normal_t_d(double a, double b, double x_, double y_) {
+  const double px = fabs(x_), py = fabs(y_);
+  const double kex = a * (1. - (b / a) * (b / a));
+  const double key = b * (1. - (a / b) * (a / b));
+  const double ab2 = a * a + b * b;
+  double t = 0.25 * M_PI;
+  for (int n = 0;; n++) {
+    double st, ct;
+    sincos(t, &st, &ct);
+    const double x = a * ct, y = b * st;
+    const double ex = kex * (ct * ct * ct), ey = key * (st * st * st);
+    const double rx = x - ex, ry = y - ey, qx = px - ex, qy = py - ey;
+    const double r = sqrt(ry * ry + rx * rx);
+    const double q = sqrt(qy * qy + qx * qx);
+    const double dc = r * asin((rx * qy - ry * qx) / (r * q));
+    const double dt = dc / sqrt(ab2 - x * x - y * y);
+    t += dt;
+    t = fmin(0.5 * M_PI, t);
+    t = fmax(0., t);
+    if (fabs(dt) < 1.e-8) break;
+    if (n > EIF_NORMAL_MAX_ITER - 1) break;
+  }
+  if (x_ < 0.) t = M_PI - t;
+  if (y_ < 0.) t = -t;
+  return t;
+}
+
+// ellipse.c:17-28
+__device__ __forceinline__ double curvature(double a, double b, double t) {
+  double st, ct;
+  sincos(t, &st, &ct);
+  const double ct2 = ct * ct, st2 = st * st;
+  return a * b * (ct2 + st2) / pow(a * a * st2 + b * b * ct2, 1.5);
+}
+
+// collision.c:75-109
+__device__ void evolute(const EllD &e, double x, double y, double &ex, double &ey, double &ix, double &iy, double &r) {
+  double sn, cs;
+  sincos(-e.angle, &sn, &cs);
+  const double x__ = x - e.x, y__ = y - e.y;
+  double x_ = cs * x__ - sn * y__;
+  double y_ = sn * x__ + cs * y__;
+  const double t = normal_t_d(e.a, e.b, x_, y_);
+  r = 1. / fmax(curvature(e.a, e.b, t), DBL_EPSILON);
+  double st, ct;
+  sincos(t, &st, &ct);
+  x_ = e.a * (1. - (e.b / e.a) * (e.b / e.a)) * (ct * ct * ct);
+  y_ = e.b * (1. - (e.a / e.b) * (e.a / e.b)) * (st * st * st);
+  double sp, cp;
+  sincos(e.angle, &sp, &cp);
+  ex = cp * x_ - sp * y_;
+  ey = sp * x_ + cp * y_;
+  ex = ex + e.x;
+  ey = ey + e.y;
+  x_ = e.a * ct;
+  y_ = e.b * st;
+  ix = cp * x_ - sp * y_;
+  iy = sp * x_ + cp * y_;
+}
+
+// collision.c:111-135; returns false when the iteration cap is reached
+__device__ bool fit_pair(const EllD &e0, const EllD &e1, double c0[3], double c1[3], double &ix0, double &iy0,
+                         double &ix1, double &iy1) {
+  c0[0] = e0.x; c0[1] = e0.y;
+  c1[0] = e1.x; c1[1] = e1.y;
+  for (int n = 0; n < EIF_FIT_MAX_ITER; n++) {
+    double c0x, c0y, c1x, c1y;
+    evolute(e0, c1[0], c1[1], c0x, c0y, ix0, iy0, c0[2]);
+    evolute(e1, c0[0], c0[1], c1x, c1y, ix1, iy1, c1[2]);
+    const double d0x = c0x - c0[0], d0y = c0y - c0[1];
+    const double d1x = c1x - c1[0], d1y = c1y - c1[1];
+    c0[0] += d0x; c0[1] += d0y;
+    c1[0] += d1x; c1[1] += d1y;
+    if (fmax(fmax(fabs(d0x), fabs(d0y)), fmax(fabs(d1x), fabs(d1y))) < 1.e-8) return true;
+  }
+  return false;
+}
+
+// collision.c:137-154
+__device__ bool fit_wall(const EllD &e, double wallx, double cc[3], double &ix, double &iy) {
+  cc[0] = e.x; cc[1] = e.y;
+  for (int n = 0; n < EIF_FIT_MAX_ITER; n++) {
+    double cx, cy;
+    evolute(e, 2. * wallx - cc[0], cc[1], cx, cy, ix, iy, cc[2]);
+    const double dcx = cx - cc[0], dcy = cy - cc[1];
+    cc[0] += dcx; cc[1] += dcy;
+    if (fmax(fabs(dcx), fabs(dcy)) < 1.e-8) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ double harmonic(double v0, double v1) { return 1. / (0.5 * (1. / v0 + 1. / v1)); }
+
+struct PV {  // particle view at the positions X^k + dX
+  double den, a, b, x, y, az;
+};
+
+__device__ __forceinline__ PV load_pv(const double *P, int pc, int n) {
+  PV v;
+  v.den = P[EIF_P_DEN * pc + n];
+  v.a = P[EIF_P_A * pc + n];
+  v.b = P[EIF_P_B * pc + n];
+  v.x = P[EIF_P_X * pc + n] + P[EIF_P_DX * pc + n];
+  v.y = P[EIF_P_Y * pc + n] + P[EIF_P_DY * pc + n];
+  v.az = P[EIF_P_AZ * pc + n];
+  return v;
+}
+
+// y-offset of the nearest periodic image of p1 seen from p0 (collision.c:158-171)
+__device__ __forceinline__ double image_offset(double p0y, double p1y, double ly) {
+  double yoff = 0., minval = DBL_MAX;
+  for (int per = -1; per <= 1; per++) {
+    const double v = fabs((p1y + ly * per) - p0y);
+    if (v < minval) { minval = v; yoff = ly * per; }
+  }
+  return yoff;
+}
+
+// exact early-out of collision.c:173-189: true when the bounding circles overlap
+__device__ __forceinline__ bool bounding_overlap(const PV &p0, const PV &p1, double ly) {
+  const double yoff = image_offset(p0.y, p1.y, ly);
+  const double nx = p1.x - p0.x, ny = (p1.y + yoff) - p0.y;
+  const double norm = fmax(hypot(nx, ny), DBL_EPSILON);
+  return !(fmax(p0.a, p0.b) + fmax(p1.a, p1.b) - norm < 0.);
+}
+
+// force/torque contribution of pair (n0 < n1) on particle `self` (collision.c:190-246)
+__device__ void pair_contribution(const PV &p0, const PV &p1, bool self_is_0, double ly, double out[3], bool &ok) {
+  out[0] = out[1] = out[2] = 0.;
+  const double yoff = image_offset(p0.y, p1.y, ly);
+  EllD e0{p0.a, p0.b, p0.x, p0.y, p0.az};
+  EllD e1{p1.a, p1.b, p1.x, p1.y + yoff, p1.az};
+  double c0[3], c1[3], ix0, iy0, ix1, iy1;
+  ok = fit_pair(e0, e1, c0, c1, ix0, iy0, ix1, iy1);
+  const double m0 = pmass(p0.den, p0.a, p0.b), m1 = pmass(p1.den, p1.a, p1.b);
+  const double i0 = pmoi(p0.den, p0.a, p0.b), i1 = pmoi(p1.den, p1.a, p1.b);
+  const double mass = harmonic(m0, m1);
+  const double reft = pow(harmonic(sqrt(p0.a * p0.b), sqrt(p1.a * p1.b)), 1.5);
+  const double k = mass * (M_PI * M_PI) / (reft * reft);
+  double nx = c1[0] - c0[0], ny = c1[1] - c0[1];
+  const double norm = fmax(hypot(nx, ny), DBL_EPSILON);
+  nx /= norm;
+  ny /= norm;
+  const double overlap = c0[2] + c1[2] - norm;
+  if (overlap > 0.) {
+    const double cfx = k * overlap * nx, cfy = k * overlap * ny;
+    if (self_is_0) {
+      out[0] = 1. / m0 * (-cfx);
+      out[1] = 1. / m0 * (-cfy);
+      out[2] = 1. / i0 * (ix0 * (-cfy) - iy0 * (-cfx));
+    } else {
+      out[0] = 1. / m1 * (+cfx);
+      out[1] = 1. / m1 * (+cfy);
+      out[2] = 1. / i1 * (ix1 * (+cfy) - iy1 * (+cfx));
+    }
+  }
+}
+
+// collision.c:249-304
+__device__ void wall_contribution(const PV &p, double wallx, double out[3], bool &ok) {
+  out[0] = out[1] = out[2] = 0.;
+  ok = true;
+  const double r = fmax(p.a, p.b);
+  if (r - fabs(wallx - p.x) < 0.) return;
+  EllD e{p.a, p.b, p.x, p.y, p.az};
+  double cc[3], ix, iy;
+  ok = fit_wall(e, wallx, cc, ix, iy);
+  const double pm = pmass(p.den, p.a, p.b), pim = pmoi(p.den, p.a, p.b);
+  const double reft = pow(sqrt(p.a * p.b), 1.5);
+  const double k = pm * (M_PI * M_PI) / (reft * reft);
+  double nx = wallx - cc[0];
+  const double norm = fabs(nx);
+  nx /= norm;
+  const double overlap = cc[2] - norm;
+  if (overlap > 0.) {
+    const double cfx = k * overlap * nx, cfy = 0.;
+    out[0] = 1. / pm * (-cfx);
+    out[1] = 1. / pm * (-cfy);
+    out[2] = 1. / pim * (ix * (-cfy) - iy * (-cfx));
+  }
+}
+
+constexpr int CWARPS = 4;
+
+__global__ void __launch_bounds__(CWARPS * 32) k_collision(double *__restrict__ P, int pcap, int np, int cn, double ly,
+                                                           double lx, unsigned *__restrict__ flags) {
+  __shared__ int cand[CWARPS][32];
+  __shared__ double cval[CWARPS][32][3];
+  const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+  const int k = blockIdx.x * CWARPS + wl;
+  if (k >= np) return;
+  const PV pk = load_pv(P, pcap, k);
+  const float rk = (float)fmax(pk.a, pk.b);
+  const float xk = (float)pk.x, yk = (float)pk.y, lyf = (float)ly;
+  double acc0 = 0., acc1 = 0., acc2 = 0.;
+  bool ok_all = true;
+  for (int base = 0; base < np; base += 32) {
+    const int m = base + lane;
+    bool hit = false;
+    if (m < np && m != k) {
+      const PV pm_ = load_pv(P, pcap, m);
+      // conservative single-precision test: skip only pairs clearly apart for every image
+      const float rs = rk + (float)fmax(pm_.a, pm_.b);
+      const float dxf = (float)pm_.x - xk;
+      const float lim = rs * rs * 1.001f + 1e-6f;
+      bool maybe = false;
+      for (int per = -1; per <= 1; per++) {
+        const float dyf = (float)pm_.y + lyf * per - yk;
+        maybe |= dxf * dxf + dyf * dyf <= lim;
+      }
+      if (maybe) {
+        // exact test with the canonical orientation of the pair
+        hit = m < k ? bounding_overlap(pm_, pk, ly) : bounding_overlap(pk, pm_, ly);
+      }
+    }
+    const unsigned ball = __ballot_sync(0xffffffffu, hit);
+    if (ball == 0u) continue;
+    const int ncand = __popc(ball);
+    const int pos = __popc(ball & ((1u << lane) - 1u));
+    if (hit) cand[wl][pos] = m;
+    __syncwarp();
+    if (lane < ncand) {
+      const int mm = cand[wl][lane];
+      const PV pmm = load_pv(P, pcap, mm);
+      double out[3];
+      bool ok;
+      if (mm < k) pair_contribution(pmm, pk, false, ly, out, ok);
+      else pair_contribution(pk, pmm, true, ly, out, ok);
+      ok_all &= ok;
+      cval[wl][lane][0] = out[0];
+      cval[wl][lane][1] = out[1];
+      cval[wl][lane][2] = out[2];
+    }
+    __syncwarp();
+    if (lane == 0) {
+      for (int q = 0; q < ncand; q++) {
+        acc0 += cval[wl][q][0];
+        acc1 += cval[wl][q][1];
+        acc2 += cval[wl][q][2];
+      }
+    }
+    __syncwarp();
+  }
+  const bool ok_warp = __all_sync(0xffffffffu, ok_all);
+  if (lane == 0) {
+    double out[3];
+    bool ok0, ok1;
+    wall_contribution(pk, 0., out, ok0);
+    acc0 += out[0]; acc1 += out[1]; acc2 += out[2];
+    wall_contribution(pk, lx, out, ok1);
+    acc0 += out[0]; acc1 += out[1]; acc2 += out[2];
+    P[(EIF_P_CFX0 + cn) * pcap + k] = acc0;
+    P[(EIF_P_CFY0 + cn) * pcap + k] = acc1;
+    P[(EIF_P_CTZ0 + cn) * pcap + k] = acc2;
+    if (!(ok_warp && ok0 && ok1)) atomicOr(flags, EIF_FLAG_NOCONV);
+  }
+}
+
+__global__ void k_reset(double *__restrict__ P, int pcap, int np) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= np) return;
+  P[EIF_P_DUX * pcap + n] = 0.; P[EIF_P_DUY * pcap + n] = 0.; P[EIF_P_DVZ * pcap + n] = 0.;
+  P[EIF_P_DX * pcap + n] = 0.; P[EIF_P_DY * pcap + n] = 0.; P[EIF_P_DAZ * pcap + n] = 0.;
+}
+
+// increment.c:10-72: one block; residual = max |change of the increments|
+__global__ void k_increment(double *__restrict__ P, int pcap, int np, double gamma, double Fr2,
+                            double *__restrict__ scal) {
+  const double dt = scal[0];
+  double res = 0.;
+  for (int n = threadIdx.x; n < np; n += blockDim.x) {
+    double *p = P;
+    const double den = p[EIF_P_DEN * pcap + n];
+    const double px = p[EIF_P_DUX * pcap + n], py = p[EIF_P_DUY * pcap + n], pz = p[EIF_P_DVZ * pcap + n];
+    const double hgd = 0.5 * gamma * dt;
+    const double dux = hgd * (p[EIF_P_CFX0 * pcap + n] + p[EIF_P_CFX1 * pcap + n]) + dt * p[EIF_P_FUX * pcap + n] +
+                       (p[EIF_P_IUX1 * pcap + n] - p[EIF_P_IUX0 * pcap + n]) + 1.0 * gamma * dt * (1. - den) / Fr2;
+    const double duy = hgd * (p[EIF_P_CFY0 * pcap + n] + p[EIF_P_CFY1 * pcap + n]) + dt * p[EIF_P_FUY * pcap + n] +
+                       (p[EIF_P_IUY1 * pcap + n] - p[EIF_P_IUY0 * pcap + n]);
+    const double dvz = hgd * (p[EIF_P_CTZ0 * pcap + n] + p[EIF_P_CTZ1 * pcap + n]) + dt * p[EIF_P_TVZ * pcap + n] +
+                       (p[EIF_P_IVZ1 * pcap + n] - p[EIF_P_IVZ0 * pcap + n]);
+    p[EIF_P_DUX * pcap + n] = dux;
+    p[EIF_P_DUY * pcap + n] = duy;
+    p[EIF_P_DVZ * pcap + n] = dvz;
+    res = fmax(res, fabs(dux - px));
+    res = fmax(res, fabs(duy - py));
+    res = fmax(res, fabs(dvz - pz));
+    const double ux0 = p[EIF_P_UX * pcap + n], uy0 = p[EIF_P_UY * pcap + n], vz0 = p[EIF_P_VZ * pcap + n];
+    p[EIF_P_DX * pcap + n] = hgd * (ux0 + (ux0 + dux));
+    p[EIF_P_DY * pcap + n] = hgd * (uy0 + (uy0 + duy));
+    p[EIF_P_DAZ * pcap + n] = hgd * (vz0 + (vz0 + dvz));
+  }
+  res = eifd::warp_max(res);
+  __shared__ double s[32];
+  if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = res;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); w++) res = fmax(res, s[w]);
+    scal[1] = res;
+  }
+}
+
+// update.c:8-34
+__global__ void k_update(double *__restrict__ P, int pcap, int np, double ly) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= np) return;
+  P[EIF_P_UX * pcap + n] += P[EIF_P_DUX * pcap + n];
+  P[EIF_P_UY * pcap + n] += P[EIF_P_DUY * pcap + n];
+  P[EIF_P_VZ * pcap + n] += P[EIF_P_DVZ * pcap + n];
+  double x = P[EIF_P_X * pcap + n] + P[EIF_P_DX * pcap + n];
+  double y = P[EIF_P_Y * pcap + n] + P[EIF_P_DY * pcap + n];
+  double az = P[EIF_P_AZ * pcap + n] + P[EIF_P_DAZ * pcap + n];
+  if (y < 0.) y += ly;
+  if (y > ly) y -= ly;
+  if (az < 0.) az += 2. * M_PI;
+  if (az > 2. * M_PI) az -= 2. * M_PI;
+  P[EIF_P_X * pcap + n] = x;
+  P[EIF_P_Y * pcap + n] = y;
+  P[EIF_P_AZ * pcap + n] = az;
+}
+
+}  // namespace
+
+namespace eif {
+
+int launch_collision(eif_ctx *c, int cn) {
+  if (c->np == 0) return EIF_OK;
+  EIF_PROF(c, "collision", 1);
+  k_collision<<<(c->np + CWARPS - 1) / CWARPS, CWARPS * 32, 0, c->stream>>>(c->P, c->pcap, c->np, cn, c->ly, c->lx,
+                                                                            c->d_flags);
+  EIF_LAUNCH_CK(c);
+  return EIF_OK;
+}
+
+int launch_reset_increments(eif_ctx *c) {
+  if (c->np == 0) return EIF_OK;
+  EIF_PROF(c, "particle_reset", 1);
+  k_reset<<<(c->np + 127) / 128, 128, 0, c->stream>>>(c->P, c->pcap, c->np);
+  EIF_LAUNCH_CK(c);
+  return EIF_OK;
+}
+
+int launch_increment(eif_ctx *c, int rk) {
+  const double Fr = c->cfg.Fr;
+  EIF_PROF(c, "particle_increment", 1);
+  k_increment<<<1, 1024, 0, c->stream>>>(c->P, c->pcap, c->np, rk_coef(rk).gamma, Fr * Fr, c->d_scal);
+  EIF_LAUNCH_CK(c);
+  return EIF_OK;
+}
+
+int launch_update_particles(eif_ctx *c) {
+  if (c->np == 0) return EIF_OK;
+  EIF_PROF(c, "particle_update", 1);
+  k_update<<<(c->np + 127) / 128, 128, 0, c->stream>>>(c->P, c->pcap, c->np, c->ly);
+  EIF_LAUNCH_CK(c);
+  return EIF_OK;
+}
+
+}  // namespace eif

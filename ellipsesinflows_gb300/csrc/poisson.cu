@@ -1,0 +1,539 @@
+// Pressure Poisson solve for the scalar potential psi
+// (src/fluid/compute_potential.c:48-138, src/tdm.c:37-131).
+//
+// The reference computes the right-hand side q = div(u)/(gamma dt), applies a
+// DCT-II (FFTW REDFT10) along x to each row, transposes, solves one periodic
+// tridiagonal system along y per x-wavenumber (tdm.c, Thomas on the leading
+// n-1 rows plus a correction vector and the last row), transposes back,
+// applies a DCT-III (REDFT01) and scales by 1/(2 itot).
+//
+// On the GPU no transpose is needed: rows stay x-contiguous, so a warp of
+// threads over consecutive wavenumbers walks a column with coalesced loads.
+//   1. k_dct2: one CTA per row. The right-hand side is formed in the load
+//      (including the IBM field response u** = u* + avg(dux), which is
+//      therefore never stored), then the DCT-II is computed as a length-n/2
+//      complex FFT (Makhoul's reordering + real-to-complex split) in shared
+//      memory with a mixed radix-4/2/3 Stockham autosort FFT.
+//   2. k_tdm_local: the column of each wavenumber is cut into blocks of
+//      EIF_TDM_M rows: EIF_TDM_M-1 interior rows and one interface row. Each
+//      thread solves the interior rows of one block in registers with
+//      pre-factored Thomas coefficients (the matrix is constant along y).
+//   3. k_tdm_reduced: one thread per wavenumber solves the cyclic system of
+//      the interface values, which again has constant coefficients and is
+//      solved with the reference's cyclic algorithm (tdm.c:64-108).
+//   4. k_dct3: one CTA per row; the interior values are reconstructed from
+//      the block solution and the two neighbouring interface values in the
+//      load, then DCT-III, scaling and the Neumann/halo values of psi
+//      (compute_potential.c:130-137).
+// The kx = 0 system is singular; the reference leaves its additive constant
+// to rounding noise (tdm.c:100-102, the guard does not fire). Here that
+// constant is fixed by pinning the last interface value of kx = 0 to zero.
+// The constant shifts psi (and p) uniformly and does not change velocities.
+#include "eif_internal.cuh"
+#include <cmath>
+#include <vector>
+#include <algorithm>
+
+namespace {
+
+using eifd::ux_idx;
+using eifd::uy_idx;
+
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ double2 conjd(double2 a) { return make_double2(a.x, -a.y); }
+// multiply by +i or -i
+__device__ __forceinline__ double2 mul_i(double2 a, int sign) {
+  return sign > 0 ? make_double2(-a.y, a.x) : make_double2(a.y, -a.x);
+}
+
+struct FftDesc {
+  int m, nfac;
+  int fac[16];
+};
+
+// Stockham autosort FFT of length d.m on shared memory buffers x and y;
+// returns the buffer holding the result. sign = -1 forward, +1 inverse
+// (unnormalised). tw[k] = exp(-2 pi i k / m).
+__device__ double2 *fft_smem(double2 *x, double2 *y, const FftDesc &d, const double2 *__restrict__ tw, int sign) {
+  const int m = d.m;
+  int L = 1;
+  for (int s = 0; s < d.nfac; s++) {
+    const int R = d.fac[s];
+    const int Ls = L * R;
+    const int nb = m / R;
+    const int tws = m / Ls;
+    for (int j = threadIdx.x; j < nb; j += blockDim.x) {
+      const int k = j % L;
+      const int blk = j / L;
+      double2 a[4];
+#pragma unroll
+      for (int r = 0; r < 4; r++) {
+        if (r < R) {
+          double2 v = x[j + r * nb];
+          if (r > 0 && k > 0) {
+            double2 w = __ldg(tw + r * k * tws);
+            if (sign > 0) w.y = -w.y;
+            v = cmul(v, w);
+          }
+          a[r] = v;
+        }
+      }
+      const int o = blk * Ls + k;
+      if (R == 4) {
+        const double2 s02 = cadd(a[0], a[2]), d02 = csub(a[0], a[2]);
+        const double2 s13 = cadd(a[1], a[3]), d13 = mul_i(csub(a[1], a[3]), sign);
+        y[o] = cadd(s02, s13);
+        y[o + L] = cadd(d02, d13);
+        y[o + 2 * L] = csub(s02, s13);
+        y[o + 3 * L] = csub(d02, d13);
+      } else if (R == 2) {
+        y[o] = cadd(a[0], a[1]);
+        y[o + L] = csub(a[0], a[1]);
+      } else {  // R == 3
+        const double c1 = -0.5;
+        const double s1 = sign * 0.86602540378443864676;  // sin(2 pi / 3)
+        const double2 t = cadd(a[1], a[2]);
+        const double2 u = csub(a[1], a[2]);
+        const double2 base = make_double2(a[0].x + c1 * t.x, a[0].y + c1 * t.y);
+        const double2 rot = make_double2(-s1 * u.y, s1 * u.x);
+        y[o] = cadd(a[0], t);
+        y[o + L] = cadd(base, rot);
+        y[o + 2 * L] = csub(base, rot);
+      }
+    }
+    __syncthreads();
+    double2 *t = x;
+    x = y;
+    y = t;
+    L = Ls;
+  }
+  return x;
+}
+
+struct Dct2Args {
+  const double *ux, *uy, *dux, *duy, *dt;
+  double *qhat;
+  const double2 *tw, *rot, *wn;
+  FftDesc fd;
+  double gamma, rdx, rdy;
+  int itot, jtot, ld, with_ibm;
+};
+
+// RHS + DCT-II of one row (compute_potential.c:70-92)
+__global__ void __launch_bounds__(256) k_dct2(Dct2Args a) {
+  extern __shared__ double2 sm[];
+  const int n = a.itot, m = n / 2, ld = a.ld;
+  double *q = reinterpret_cast<double *>(sm + 2 * m);
+  const int j = 1 + blockIdx.x;
+  const double inv = 1. / (a.gamma * __ldg(a.dt));
+  for (int i = 1 + threadIdx.x; i <= n; i += blockDim.x) {
+    // velocities after the IBM response, evaluated as the reference stores them
+    double uxm = __ldg(a.ux + ux_idx(i, j, ld)), uxp = __ldg(a.ux + ux_idx(i + 1, j, ld));
+    double uym = __ldg(a.uy + uy_idx(i, j, ld)), uyp = __ldg(a.uy + uy_idx(i, j + 1, ld));
+    if (a.with_ibm) {
+      const int c = uy_idx(i, j, ld);
+      const double dw = __ldg(a.dux + c - 1), d0 = __ldg(a.dux + c), de = __ldg(a.dux + c + 1);
+      if (i >= 2) uxm = uxm + 0.5 * (dw + d0);
+      if (i + 1 <= n) uxp = uxp + 0.5 * (d0 + de);
+      const double ds = __ldg(a.duy + c - ld), e0 = __ldg(a.duy + c), en = __ldg(a.duy + c + ld);
+      uym = uym + 0.5 * (ds + e0);
+      uyp = uyp + 0.5 * (e0 + en);
+    }
+    q[i - 1] = inv * ((uxp - uxm) * a.rdx + (uyp - uym) * a.rdy);
+  }
+  __syncthreads();
+  // Makhoul reordering v[t] = q[2t], v[n-1-t] = q[2t+1]; z[s] = v[2s] + i v[2s+1]
+  double2 *x = sm, *y = sm + m;
+  for (int s = threadIdx.x; s < m; s += blockDim.x) {
+    const int t0 = 2 * s, t1 = 2 * s + 1;
+    const double v0 = t0 < m ? q[2 * t0] : q[2 * (n - 1 - t0) + 1];
+    const double v1 = t1 < m ? q[2 * t1] : q[2 * (n - 1 - t1) + 1];
+    x[s] = make_double2(v0, v1);
+  }
+  __syncthreads();
+  const double2 *Z = fft_smem(x, y, a.fd, a.tw, -1);
+  double *out = a.qhat + (size_t)(j - 1) * ld;
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    const int kk = k <= m ? k : n - k;
+    const double2 zk = Z[kk % m];
+    const double2 zm = conjd(Z[(m - kk) % m]);
+    const double2 e = make_double2(0.5 * (zk.x + zm.x), 0.5 * (zk.y + zm.y));
+    const double2 df = csub(zk, zm);
+    const double2 o = make_double2(0.5 * df.y, -0.5 * df.x);  // (zk - zm) / 2i
+    double2 v = cadd(e, cmul(__ldg(a.wn + kk), o));
+    if (k > m) v.y = -v.y;
+    const double2 r = __ldg(a.rot + k);
+    out[k] = 2. * (r.x * v.x - r.y * v.y);
+  }
+}
+
+// interior Thomas solve of one block in registers
+template <int M>
+__global__ void __launch_bounds__(256) k_tdm_local(double *__restrict__ qhat, const double *__restrict__ inv,
+                                                  const double *__restrict__ up, double *__restrict__ iface_a,
+                                                  double *__restrict__ first, double l, int itot, int nblk, int ld) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int b = blockIdx.y;
+  if (k >= itot) return;
+  double v[M - 1];
+  const size_t base = (size_t)b * M * ld + k;
+#pragma unroll
+  for (int r = 0; r < M - 1; r++) v[r] = qhat[base + (size_t)r * ld];
+  const double rif = qhat[base + (size_t)(M - 1) * ld];
+  v[0] = v[0] * __ldg(inv + k);
+#pragma unroll
+  for (int r = 1; r < M - 1; r++) v[r] = (v[r] - l * v[r - 1]) * __ldg(inv + r * itot + k);
+#pragma unroll
+  for (int r = M - 3; r >= 0; r--) v[r] = v[r] - __ldg(up + r * itot + k) * v[r + 1];
+#pragma unroll
+  for (int r = 0; r < M - 1; r++) qhat[base + (size_t)r * ld] = v[r];
+  // interface equation: r_iface - l y[M-2] (this block) - l y[0] (next block)
+  iface_a[(size_t)b * itot + k] = rif - l * v[M - 2];
+  first[(size_t)b * itot + k] = v[0];
+}
+
+// cyclic system of the interface values of one wavenumber
+__global__ void k_tdm_reduced(double *__restrict__ iface, const double *__restrict__ first,
+                              const double *__restrict__ rinv, const double *__restrict__ rup,
+                              const double *__restrict__ rq1, const double *__restrict__ rcoef, double l, int itot,
+                              int nblk) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= itot) return;
+  const int P = nblk;
+  const double A = rcoef[4 * k + 0];
+  const double den = rcoef[4 * k + 2];
+  const bool pin = rcoef[4 * k + 3] != 0.;
+  // right-hand side R_b = (r_iface - l y_b[M-2]) - l y_{b+1}[0]
+  auto R = [&](int b) { return iface[(size_t)b * itot + k] - l * first[(size_t)((b + 1) % P) * itot + k]; };
+  // Thomas on the leading P-1 rows (in place in iface)
+  const double rP = R(P - 1);
+  double zprev = R(0) * rinv[k];
+  iface[k] = zprev;
+  for (int b = 1; b < P - 1; b++) {
+    const double z = (R(b) - A * zprev) * rinv[(size_t)b * itot + k];
+    iface[(size_t)b * itot + k] = z;
+    zprev = z;
+  }
+  for (int b = P - 3; b >= 0; b--) {
+    const double z = iface[(size_t)b * itot + k] - rup[(size_t)b * itot + k] * zprev;
+    iface[(size_t)b * itot + k] = z;
+    zprev = z;
+  }
+  const double z0 = iface[k], zl = iface[(size_t)(P - 2) * itot + k];
+  const double num = rP - A * z0 - A * zl;
+  const double last = pin ? 0. : num / den;
+  iface[(size_t)(P - 1) * itot + k] = last;
+  for (int b = 0; b < P - 1; b++) {
+    iface[(size_t)b * itot + k] = iface[(size_t)b * itot + k] + last * rq1[(size_t)b * itot + k];
+  }
+}
+
+// fallback for column lengths without a suitable block size: the reference's
+// sequential cyclic algorithm per wavenumber on global memory
+__global__ void k_tdm_serial(double *__restrict__ qhat, double *__restrict__ scratch, const double *__restrict__ lam,
+                             double l, int itot, int jtot, int ld) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= itot) return;
+  const int n = jtot;
+  const double c = -l - l + lam[k];
+  double *u0 = scratch + k;                     // [i*itot + k]
+  double *q1 = scratch + (size_t)n * itot + k;  // [i*itot + k]
+  auto Q = [&](int i) -> double & { return qhat[(size_t)i * ld + k]; };
+  auto U0 = [&](int i) -> double & { return u0[(size_t)i * itot]; };
+  auto Q1 = [&](int i) -> double & { return q1[(size_t)i * itot]; };
+  for (int i = 0; i < n - 1; i++) Q1(i) = i == 0 ? -l : (i == n - 2 ? -l : 0.);
+  // Thomas on rows 0..n-2 for q and q1 together (same factors)
+  U0(0) = l / c;
+  Q(0) = Q(0) / c;
+  Q1(0) = Q1(0) / c;
+  for (int i = 1; i <= n - 2; i++) {
+    double val = c - l * U0(i - 1);
+    if (fabs(val) < 2.220446049250313e-16) {
+      U0(i) = 0.; Q(i) = 0.; Q1(i) = 0.;
+    } else {
+      val = 1. / val;
+      U0(i) = val * l;
+      Q(i) = val * (Q(i) - l * Q(i - 1));
+      Q1(i) = val * (Q1(i) - l * Q1(i - 1));
+    }
+  }
+  for (int i = n - 3; i >= 0; i--) {
+    Q(i) -= U0(i) * Q(i + 1);
+    Q1(i) -= U0(i) * Q1(i + 1);
+  }
+  const double num = Q(n - 1) - l * Q(0) - l * Q(n - 2);
+  const double den = c + l * Q1(0) + l * Q1(n - 2);
+  const double last = (k == 0 || fabs(den) < 2.220446049250313e-16) ? 0. : num / den;
+  Q(n - 1) = last;
+  for (int i = 0; i <= n - 2; i++) Q(i) = Q(i) + last * Q1(i);
+}
+
+struct Dct3Args {
+  const double *qhat, *iface, *g;
+  double *psi;
+  const double2 *tw, *rot, *wn;
+  FftDesc fd;
+  int itot, jtot, ld, blk, nblk;
+};
+
+// block reconstruction + DCT-III + scaling of one row (compute_potential.c:118-137)
+__global__ void __launch_bounds__(256) k_dct3(Dct3Args a) {
+  extern __shared__ double2 sm[];
+  const int n = a.itot, m = n / 2, ld = a.ld;
+  double *xr = reinterpret_cast<double *>(sm + 2 * m);
+  const int j = 1 + blockIdx.x;
+  const int jr = j - 1;  // 0-based row in the tridiagonal systems
+  const double *row = a.qhat + (size_t)jr * ld;
+  if (a.blk > 0) {
+    const int M = a.blk;
+    const int b = jr / M, r = jr % M;
+    const int bm = (b + a.nblk - 1) % a.nblk;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+      double v;
+      if (r == M - 1) {
+        v = __ldg(a.iface + (size_t)b * n + k);
+      } else {
+        const double gl = __ldg(a.g + (size_t)r * n + k);
+        const double gr = __ldg(a.g + (size_t)(M - 2 - r) * n + k);
+        v = __ldg(row + k) + __ldg(a.iface + (size_t)bm * n + k) * gl + __ldg(a.iface + (size_t)b * n + k) * gr;
+      }
+      xr[k] = v;
+    }
+  } else {
+    for (int k = threadIdx.x; k < n; k += blockDim.x) xr[k] = __ldg(row + k);
+  }
+  __syncthreads();
+  double2 *x = sm, *y = sm + m;
+  // W[t] = exp(i pi t / 2n) (x[t] - i x[n-t]); Z[s] = (W[s] + W[s+m]) + i (W[s] - W[s+m]) exp(2 pi i s / n)
+  for (int s = threadIdx.x; s < m; s += blockDim.x) {
+    const int t0 = s, t1 = s + m;
+    const double2 r0 = conjd(__ldg(a.rot + t0)), r1 = conjd(__ldg(a.rot + t1));
+    const double2 w0 = cmul(r0, make_double2(xr[t0], t0 == 0 ? 0. : -xr[n - t0]));
+    const double2 w1 = cmul(r1, make_double2(xr[t1], -xr[n - t1]));
+    const double2 sum = cadd(w0, w1);
+    const double2 dif = cmul(csub(w0, w1), conjd(__ldg(a.wn + s)));
+    x[s] = make_double2(sum.x - dif.y, sum.y + dif.x);
+  }
+  __syncthreads();
+  const double2 *z = fft_smem(x, y, a.fd, a.tw, +1);
+  const double scale = 1. / (2. * n);
+  double *prow = a.psi + (size_t)j * ld;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    // y[2t] = w[t], y[2t+1] = w[n-1-t]; w[2s] = Re z[s], w[2s+1] = Im z[s]
+    const int t = (i & 1) ? n - 1 - (i >> 1) : (i >> 1);
+    const double w = (t & 1) ? z[t >> 1].y : z[t >> 1].x;
+    const double v = w * scale;
+    prow[i + 1] = v;
+    if (j == 1) a.psi[(size_t)(a.jtot + 1) * ld + i + 1] = v;
+    if (j == a.jtot) a.psi[i + 1] = v;
+    if (i == 0) {
+      prow[0] = v;
+      if (j == 1) a.psi[(size_t)(a.jtot + 1) * ld] = v;
+      if (j == a.jtot) a.psi[0] = v;
+    }
+    if (i == n - 1) {
+      prow[n + 1] = v;
+      if (j == 1) a.psi[(size_t)(a.jtot + 1) * ld + n + 1] = v;
+      if (j == a.jtot) a.psi[n + 1] = v;
+    }
+  }
+}
+
+bool factorize(int m, int *fac, int *nfac) {
+  int k = 0;
+  while (m % 4 == 0) { fac[k++] = 4; m /= 4; }
+  while (m % 2 == 0) { fac[k++] = 2; m /= 2; }
+  while (m % 3 == 0) { fac[k++] = 3; m /= 3; }
+  *nfac = k;
+  return m == 1 && k <= 16;
+}
+
+// Thomas factors of a constant-coefficient tridiagonal matrix of size n
+void thomas_factors(int n, double l, double c, double *inv, double *up) {
+  inv[0] = 1. / c;
+  up[0] = l * inv[0];
+  for (int i = 1; i < n; i++) {
+    inv[i] = 1. / (c - l * up[i - 1]);
+    up[i] = l * inv[i];
+  }
+}
+
+void thomas_apply(int n, double l, const double *inv, const double *up, double *q) {
+  q[0] = q[0] * inv[0];
+  for (int i = 1; i < n; i++) q[i] = (q[i] - l * q[i - 1]) * inv[i];
+  for (int i = n - 2; i >= 0; i--) q[i] = q[i] - up[i] * q[i + 1];
+}
+
+}  // namespace
+
+namespace eif {
+
+int poisson_init(eif_ctx *c) {
+  PoissonPlan &pp = c->pp;
+  const int n = c->itot, jt = c->jtot;
+  if (n % 2 != 0) return fail(c, EIF_ERR_ARG, "itot must be even (got %d)", n);
+  pp.n = n;
+  pp.m = n / 2;
+  if (!factorize(pp.m, pp.fac, &pp.nfac)) return fail(c, EIF_ERR_ARG, "itot/2 must be of the form 2^a 3^b (got %d)", pp.m);
+  const long double PI = 3.141592653589793238462643383279502884L;
+  std::vector<double2> tw(pp.m), rot(n), wn(n);
+  for (int k = 0; k < pp.m; k++) {
+    const long double t = -2.L * PI * k / pp.m;
+    tw[k] = make_double2((double)cosl(t), (double)sinl(t));
+  }
+  for (int k = 0; k < n; k++) {
+    const long double h = -PI * k / (2.L * n);
+    rot[k] = make_double2((double)cosl(h), (double)sinl(h));
+    const long double t = -2.L * PI * k / n;
+    wn[k] = make_double2((double)cosl(t), (double)sinl(t));
+  }
+  // tridiagonal coefficients (compute_potential.c:103-112)
+  const double dx = c->dx, dy = c->dy;
+  const double l = 1. / dy / dy;
+  std::vector<double> lam(n);
+  for (int k = 0; k < n; k++) {
+    const double s = sin(M_PI * k / (2. * n));
+    lam[k] = -4. / (dx * dx) * (s * s);
+  }
+  pp.blk = 0;
+  pp.nblk = 1;
+  const int cand[3] = {EIF_TDM_M, 8, 4};
+  for (int ci = 0; ci < 3; ci++) {
+    if (jt % cand[ci] == 0 && jt / cand[ci] >= 3) { pp.blk = cand[ci]; pp.nblk = jt / cand[ci]; break; }
+  }
+  auto up_load = [&](void **dst, const void *src, size_t bytes) -> cudaError_t {
+    cudaError_t e = cudaMalloc(dst, bytes);
+    if (e != cudaSuccess) return e;
+    return cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice);
+  };
+  EIF_CK(c, up_load((void **)&pp.tw, tw.data(), sizeof(double2) * pp.m));
+  EIF_CK(c, up_load((void **)&pp.rot, rot.data(), sizeof(double2) * n));
+  EIF_CK(c, up_load((void **)&pp.wn, wn.data(), sizeof(double2) * n));
+  EIF_CK(c, up_load((void **)&pp.lam, lam.data(), sizeof(double) * n));
+  if (pp.blk > 0) {
+    const int M = pp.blk, P = pp.nblk;
+    std::vector<double> inv((size_t)(M - 1) * n), up((size_t)(M - 1) * n), g((size_t)(M - 1) * n);
+    std::vector<double> rinv((size_t)P * n), rup((size_t)P * n), rq1((size_t)P * n), rcoef((size_t)4 * n);
+    std::vector<double> ti(M), tu(M), tg(M), ri(P), ru(P), rq(P);
+    for (int k = 0; k < n; k++) {
+      const double cc = -l - l + lam[k];
+      thomas_factors(M - 1, l, cc, ti.data(), tu.data());
+      for (int i = 0; i < M - 1; i++) tg[i] = 0.;
+      tg[0] = -l;
+      thomas_apply(M - 1, l, ti.data(), tu.data(), tg.data());
+      for (int i = 0; i < M - 1; i++) {
+        inv[(size_t)i * n + k] = ti[i];
+        up[(size_t)i * n + k] = tu[i];
+        g[(size_t)i * n + k] = tg[i];
+      }
+      // reduced cyclic system A s_{b-1} + B s_b + A s_{b+1} = R_b
+      const double A = l * tg[M - 2];
+      const double B = cc + 2. * l * tg[0];
+      thomas_factors(P - 1, A, B, ri.data(), ru.data());
+      for (int b = 0; b < P - 1; b++) rq[b] = 0.;
+      rq[0] = -A;
+      rq[P - 2] += -A;
+      thomas_apply(P - 1, A, ri.data(), ru.data(), rq.data());
+      for (int b = 0; b < P - 1; b++) {
+        rinv[(size_t)b * n + k] = ri[b];
+        rup[(size_t)b * n + k] = ru[b];
+        rq1[(size_t)b * n + k] = rq[b];
+      }
+      rcoef[4 * k + 0] = A;
+      rcoef[4 * k + 1] = B;
+      rcoef[4 * k + 2] = B + A * rq[0] + A * rq[P - 2];
+      rcoef[4 * k + 3] = k == 0 ? 1. : 0.;
+    }
+    EIF_CK(c, up_load((void **)&pp.tdm_inv, inv.data(), sizeof(double) * inv.size()));
+    EIF_CK(c, up_load((void **)&pp.tdm_up, up.data(), sizeof(double) * up.size()));
+    EIF_CK(c, up_load((void **)&pp.tdm_g, g.data(), sizeof(double) * g.size()));
+    EIF_CK(c, up_load((void **)&pp.red_inv, rinv.data(), sizeof(double) * rinv.size()));
+    EIF_CK(c, up_load((void **)&pp.red_up, rup.data(), sizeof(double) * rup.size()));
+    EIF_CK(c, up_load((void **)&pp.red_q1, rq1.data(), sizeof(double) * rq1.size()));
+    EIF_CK(c, up_load((void **)&pp.red_coef, rcoef.data(), sizeof(double) * rcoef.size()));
+    EIF_CK(c, cudaMalloc((void **)&pp.ywork, sizeof(double) * 2 * (size_t)P * n));
+  } else {
+    EIF_CK(c, cudaMalloc((void **)&pp.ywork, sizeof(double) * 2 * (size_t)jt * n));
+  }
+  const size_t smem = sizeof(double2) * 2 * pp.m + sizeof(double) * n;
+  if (smem > 48 * 1024) {
+    EIF_CK(c, cudaFuncSetAttribute(k_dct2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    EIF_CK(c, cudaFuncSetAttribute(k_dct3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  }
+  return EIF_OK;
+}
+
+void poisson_free(eif_ctx *c) {
+  PoissonPlan &pp = c->pp;
+  void *ptrs[] = {pp.tw, pp.rot, pp.wn, pp.lam, pp.tdm_inv, pp.tdm_up, pp.tdm_g,
+                  pp.red_inv, pp.red_up, pp.red_q1, pp.red_coef, pp.ywork};
+  for (void *p : ptrs) if (p) cudaFree(p);
+  pp = PoissonPlan{};
+}
+
+static int fft_threads(int m) { return m >= 512 ? 256 : (m >= 128 ? 128 : 64); }
+
+int launch_potential(eif_ctx *c, int rk, bool with_ibm) {
+  PoissonPlan &pp = c->pp;
+  const int n = c->itot, jt = c->jtot;
+  FftDesc fd;
+  fd.m = pp.m;
+  fd.nfac = pp.nfac;
+  for (int s = 0; s < 16; s++) fd.fac[s] = pp.fac[s];
+  const size_t smem = sizeof(double2) * 2 * pp.m + sizeof(double) * n;
+  const int thr = fft_threads(pp.m);
+  {
+    Dct2Args a;
+    a.ux = c->ux[c->cur]; a.uy = c->uy[c->cur];
+    a.dux = c->dux; a.duy = c->duy; a.dt = c->d_scal;
+    a.qhat = c->qhat;
+    a.tw = pp.tw; a.rot = pp.rot; a.wn = pp.wn;
+    a.fd = fd;
+    a.gamma = rk_coef(rk).gamma;
+    a.rdx = 1. / c->dx; a.rdy = 1. / c->dy;
+    a.itot = n; a.jtot = jt; a.ld = c->ld; a.with_ibm = with_ibm ? 1 : 0;
+    EIF_PROF(c, "poisson_dct2", 1);
+    k_dct2<<<jt, thr, smem, c->stream>>>(a);
+    EIF_LAUNCH_CK(c);
+  }
+  const double l = 1. / c->dy / c->dy;
+  double *iface = pp.ywork;
+  double *first = pp.ywork + (size_t)pp.nblk * n;
+  if (pp.blk > 0) {
+    EIF_PROF(c, "poisson_tdm", 2);
+    dim3 g((n + 127) / 128, pp.nblk);
+    if (pp.blk == 16) {
+      k_tdm_local<16><<<g, 128, 0, c->stream>>>(c->qhat, pp.tdm_inv, pp.tdm_up, iface, first, l, n, pp.nblk, c->ld);
+    } else if (pp.blk == 8) {
+      k_tdm_local<8><<<g, 128, 0, c->stream>>>(c->qhat, pp.tdm_inv, pp.tdm_up, iface, first, l, n, pp.nblk, c->ld);
+    } else {
+      k_tdm_local<4><<<g, 128, 0, c->stream>>>(c->qhat, pp.tdm_inv, pp.tdm_up, iface, first, l, n, pp.nblk, c->ld);
+    }
+    EIF_LAUNCH_CK(c);
+    k_tdm_reduced<<<(n + 63) / 64, 64, 0, c->stream>>>(iface, first, pp.red_inv, pp.red_up, pp.red_q1, pp.red_coef,
+                                                        l, n, pp.nblk);
+    EIF_LAUNCH_CK(c);
+  } else {
+    EIF_PROF(c, "poisson_tdm", 1);
+    k_tdm_serial<<<(n + 63) / 64, 64, 0, c->stream>>>(c->qhat, pp.ywork, pp.lam, l, n, jt, c->ld);
+    EIF_LAUNCH_CK(c);
+  }
+  {
+    Dct3Args a;
+    a.qhat = c->qhat; a.iface = iface; a.g = pp.tdm_g;
+    a.psi = c->psi;
+    a.tw = pp.tw; a.rot = pp.rot; a.wn = pp.wn;
+    a.fd = fd;
+    a.itot = n; a.jtot = jt; a.ld = c->ld; a.blk = pp.blk; a.nblk = pp.nblk;
+    EIF_PROF(c, "poisson_dct3", 1);
+    k_dct3<<<jt, thr, smem, c->stream>>>(a);
+    EIF_LAUNCH_CK(c);
+  }
+  return EIF_OK;
+}
+
+}  // namespace eif

@@ -133,6 +133,17 @@ int eif_update_particles(eif_ctx *ctx);                               /* src/sus
 /* ---- diagnostics (src/logging.c:40-80) ---- */
 int eif_divergence(eif_ctx *ctx, double *divmax, double *divsum);
 
+/* ---- kernel timing (no counterpart in the reference, which only times the
+ * whole run with MPI_Wtime, src/main.c:60-61,97-105) ----
+ * When enabled, every kernel launch of the context is bracketed by CUDA events
+ * on the context's stream and accumulated per kernel name. */
+int eif_profile_enable(eif_ctx *ctx, int enable);
+int eif_profile_reset(eif_ctx *ctx);
+/* number of kernel names recorded so far (synchronises the stream) */
+int eif_profile_count(eif_ctx *ctx, int *count);
+/* name, launch count and total device time (ms) of entry k */
+int eif_profile_get(eif_ctx *ctx, int k, char *name, int name_len, long long *launches, double *ms);
+
 #ifdef __cplusplus
 }
 #endif

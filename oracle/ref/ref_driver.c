@@ -25,6 +25,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <stdio.h>
+#include "ellipse.h"
 
 #define REF_NFIELDS 30
 
