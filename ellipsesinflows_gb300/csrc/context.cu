@@ -25,6 +25,28 @@ int check_cuda(eif_ctx *c, cudaError_t e, const char *what) {
   return fail(c, EIF_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
 }
 
+int launch_check(eif_ctx *c, const char *file, int line) {
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess && c->sync_debug) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return fail(c, EIF_ERR_CUDA, "kernel launched at %s:%d: %s", file, line, cudaGetErrorString(e));
+  if (c->sync_debug) {
+    int rc = check_records(c);
+    if (rc) return fail(c, rc, "%s (after the kernel launched at %s:%d)", c->err, file, line);
+  }
+  return EIF_OK;
+}
+
+// read the bounds-guard record (after a synchronisation) and report it
+int check_records(eif_ctx *c) {
+  if (!c->d_check) return EIF_OK;
+  EIF_CK(c, cudaMemcpyAsync(c->h_check, c->d_check, sizeof(unsigned long long) * 4, cudaMemcpyDeviceToHost, c->stream));
+  EIF_CK(c, cudaStreamSynchronize(c->stream));
+  if (c->h_check[0] == 0ull) return EIF_OK;
+  const unsigned long long tag = c->h_check[1], idx = c->h_check[2], bound = c->h_check[3];
+  EIF_CK(c, cudaMemsetAsync(c->d_check, 0, sizeof(unsigned long long) * 4, c->stream));
+  return fail(c, EIF_ERR_CUDA, "bounds guard %llu: index %llu outside [0, %llu)", tag, idx, bound);
+}
+
 }  // namespace eif
 
 using namespace eif;
@@ -113,6 +135,8 @@ int sync_scalars(eif_ctx *c) {
   EIF_CK(c, cudaMemcpyAsync(c->h_flags, c->d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
   EIF_CK(c, cudaStreamSynchronize(c->stream));
   c->dt_host = c->h_scal[0];
+  int rc = check_records(c);
+  if (rc) return rc;
   return check_flags(c);
 }
 
@@ -199,6 +223,10 @@ int eif_create(const eif_config_t *cfg, eif_ctx **out) {
   CK_CREATE(cudaMallocHost((void **)&c->h_scal, sizeof(double) * 4));
   CK_CREATE(cudaMallocHost((void **)&c->h_flags, sizeof(unsigned)));
   *c->h_flags = 0u;
+  CK_CREATE(cudaMallocHost((void **)&c->h_check, sizeof(unsigned long long) * 4));
+  CK_CREATE(cudaMalloc((void **)&c->d_check, sizeof(unsigned long long) * 4));
+  CK_CREATE(cudaMemset(c->d_check, 0, sizeof(unsigned long long) * 4));
+  c->sync_debug = getenv("EIF_SYNC_DEBUG") != nullptr;
 #undef CK_CREATE
   rc = poisson_init(c);
   if (rc) return rc;
@@ -219,6 +247,8 @@ int eif_destroy(eif_ctx *c) {
                     c->cyp, c->dxc, c->P, c->d_scal};
   for (double *p : ptrs) if (p) cudaFree(p);
   if (c->d_flags) cudaFree(c->d_flags);
+  if (c->d_check) cudaFree(c->d_check);
+  if (c->h_check) cudaFreeHost(c->h_check);
   if (c->h_scal) cudaFreeHost(c->h_scal);
   if (c->h_flags) cudaFreeHost(c->h_flags);
   poisson_free(c);
@@ -267,7 +297,7 @@ int eif_pull_fluid(eif_ctx *c, double *ux, double *uy, double *p, double *psi) {
   if (p) EIF_CK(c, cudaMemcpy2DAsync(p, wy, c->p, dp, wy, rows, cudaMemcpyDeviceToHost, c->stream));
   if (psi) EIF_CK(c, cudaMemcpy2DAsync(psi, wy, c->psi, dp, wy, rows, cudaMemcpyDeviceToHost, c->stream));
   EIF_CK(c, cudaStreamSynchronize(c->stream));
-  return EIF_OK;
+  return check_records(c);
 }
 
 int eif_push_particles(eif_ctx *c, int n, const double *rec) {
@@ -290,7 +320,7 @@ int eif_pull_particles(eif_ctx *c, int n, double *rec) {
   EIF_CK(c, cudaMemcpy(soa.data(), c->P, sizeof(double) * soa.size(), cudaMemcpyDeviceToHost));
   for (int f = 0; f < EIF_NFIELDS; f++)
     for (int k = 0; k < n; k++) rec[(size_t)k * EIF_NFIELDS + f] = soa[(size_t)f * c->pcap + k];
-  return EIF_OK;
+  return check_records(c);
 }
 
 // source arrays: SRCUXA(i,j) for i=2..itot at ux index, SRCUYA(i,j) for i=1..itot at uy index
@@ -305,7 +335,7 @@ int eif_pull_src(eif_ctx *c, double *uxa, double *uxb, double *uya, double *uyb)
   if (uya) EIF_CK(c, cudaMemcpy2DAsync(uya, wy, c->sya[a] + c->ld + 1, dp, wy, c->jtot, cudaMemcpyDeviceToHost, c->stream));
   if (uyb) EIF_CK(c, cudaMemcpy2DAsync(uyb, wy, c->sya[b] + c->ld + 1, dp, wy, c->jtot, cudaMemcpyDeviceToHost, c->stream));
   EIF_CK(c, cudaStreamSynchronize(c->stream));
-  return EIF_OK;
+  return check_records(c);
 }
 
 int eif_push_src(eif_ctx *c, const double *uxa, const double *uya) {
@@ -324,7 +354,7 @@ int eif_pull_ibm_fields(eif_ctx *c, double *dux, double *duy) {
   EIF_CK(c, cudaMemcpy2DAsync(dux, wy, c->dux, dp, wy, c->jtot + 2, cudaMemcpyDeviceToHost, c->stream));
   EIF_CK(c, cudaMemcpy2DAsync(duy, wy, c->duy, dp, wy, c->jtot + 2, cudaMemcpyDeviceToHost, c->stream));
   EIF_CK(c, cudaStreamSynchronize(c->stream));
-  return EIF_OK;
+  return check_records(c);
 }
 
 int eif_decide_dt(eif_ctx *c, double *dt) {

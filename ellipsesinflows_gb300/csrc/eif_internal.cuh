@@ -123,6 +123,9 @@ struct eif_ctx {
   double time;
   double dt_host;
   bool fluid_pushed;
+  bool sync_debug;
+  unsigned long long *d_check;  // bounds-guard record: flag, tag, index, bound
+  unsigned long long *h_check;  // pinned mirror
   eif::Profiler prof;
   char err[512];
 };
@@ -139,13 +142,17 @@ struct ProfScope {
 };
 #define EIF_PROF(c, name, kernels) eif::ProfScope eif_prof_scope_((c), (name), (kernels))
 int profile_flush(eif_ctx *c);
+int check_records(eif_ctx *c);
 void profile_free(eif_ctx *c);
 
 // ---- launch helpers ----
 int fail(eif_ctx *c, int code, const char *fmt, ...);
 int check_cuda(eif_ctx *c, cudaError_t e, const char *what);
 #define EIF_CK(c, call) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) return eif::check_cuda((c), e_, #call); } while (0)
-#define EIF_LAUNCH_CK(c) do { cudaError_t e_ = cudaGetLastError(); if (e_ != cudaSuccess) return eif::check_cuda((c), e_, "kernel launch"); } while (0)
+// After a launch: report launch errors; with EIF_SYNC_DEBUG set in the
+// environment, also wait for the kernel and name the launch site on failure.
+int launch_check(eif_ctx *c, const char *file, int line);
+#define EIF_LAUNCH_CK(c) do { int r_ = eif::launch_check((c), __FILE__, __LINE__); if (r_) return r_; } while (0)
 
 // ---- fluid (fluid.cu) ----
 int launch_boundaries(eif_ctx *c);
@@ -184,6 +191,25 @@ RK rk_coef(int rk);
 #define EIF_HD __host__ __device__ __forceinline__
 
 namespace eifd {
+
+// Bounds guards: an access outside its buffer is recorded (first one wins)
+// and skipped instead of performed; the host reports the record as an error at
+// its next synchronisation. The immersed-boundary kernels, whose indices come
+// from particle geometry, are always built with the guards (EIF_CHECK).
+#ifdef EIF_CHECK
+__device__ __forceinline__ bool chk(unsigned long long *rec, long long idx, long long bound, int tag) {
+  if (idx >= 0 && idx < bound) return true;
+  if (atomicCAS(rec, 0ull, 1ull) == 0ull) {
+    rec[1] = (unsigned long long)tag;
+    rec[2] = (unsigned long long)idx;
+    rec[3] = (unsigned long long)bound;
+  }
+  return false;
+}
+#define EIF_CHK(rec, idx, bound, tag) eifd::chk((rec), (long long)(idx), (long long)(bound), (tag))
+#else
+#define EIF_CHK(rec, idx, bound, tag) true
+#endif
 
 __device__ __forceinline__ int ux_idx(int i, int j, int ld) { return j * ld + (i - 1); }
 __device__ __forceinline__ int uy_idx(int i, int j, int ld) { return j * ld + i; }

@@ -21,6 +21,9 @@
 // contribution in a scratch buffer; a tile gather then adds, for every cell,
 // the contributions of all covering boxes in (particle, image) order, which
 // is the reference's accumulation order (exchange.c:71-72), without atomics.
+#ifndef EIF_CHECK
+#define EIF_CHECK 1
+#endif
 #include "eif_internal.cuh"
 #include <cfloat>
 #include <vector>
@@ -105,11 +108,19 @@ __device__ __forceinline__ double pmoi(double den, double a, double b) {
   return 0.25 * pmass(den, a, b) * (a * a + b * b);
 }
 
+// sizes of the buffers the IBM kernels touch (used by EIF_CHECK builds)
+struct Bounds {
+  long long P, box, off, partial, wbuf, field, xc, yc;
+  unsigned long long *rec;
+};
+
 struct BoxArgs {
   const double *P;
   int pcap, np, itot, jtot, use_increment;
   double dx, dy, ly, yf1;
   int *box, *nchunk;
+  const int *bd_off_base;   // start of the buffer nchunk points into
+  Bounds bd;
 };
 
 // per-particle boxes of the three periodic images and their chunk counts
@@ -118,6 +129,7 @@ __global__ void k_boxes(BoxArgs a) {
   if (n >= a.np) return;
   const double *P = a.P;
   const int pc = a.pcap;
+  if (!EIF_CHK(a.bd.rec, EIF_P_DY * pc + n, a.bd.P, 1)) return;
   const double pa = P[EIF_P_A * pc + n], pb = P[EIF_P_B * pc + n];
   double px = P[EIF_P_X * pc + n], py = P[EIF_P_Y * pc + n];
   if (a.use_increment) {
@@ -131,21 +143,23 @@ __global__ void k_boxes(BoxArgs a) {
     loop_size(1, a.itot, a.dx, r, px, imin, imax);
     loop_size(1, a.jtot, a.dy, r, py + a.ly * per - a.yf1, jmin, jmax);
     int *bx = a.box + 12 * n + 4 * (per + 1);
+    if (!EIF_CHK(a.bd.rec, 12 * n + 4 * (per + 1) + 3, a.bd.box, 2)) return;
     bx[0] = imin; bx[1] = imax; bx[2] = jmin; bx[3] = jmax;
     if (imax >= imin && jmax >= jmin) cells += (imax - imin + 1) * (jmax - jmin + 1);
   }
+  if (!EIF_CHK(a.bd.rec, (a.nchunk - a.bd_off_base) + n, a.bd.off, 3)) return;
   a.nchunk[n] = (cells + CHUNK - 1) / CHUNK;
 }
 
 // exclusive scan of the chunk counts (one block); off[np] = total
-__global__ void k_scan(const int *__restrict__ cnt, int *__restrict__ off, int np) {
+__global__ void k_scan(const int *__restrict__ cnt, int *__restrict__ off, int np, Bounds bd) {
   __shared__ int s[1024];
   __shared__ int carry;
   if (threadIdx.x == 0) carry = 0;
   __syncthreads();
   for (int base = 0; base < np; base += 1024) {
     const int t = base + threadIdx.x;
-    const int v = t < np ? cnt[t] : 0;
+    const int v = (t < np && EIF_CHK(bd.rec, (cnt - off) + t, bd.off, 4)) ? cnt[t] : 0;
     s[threadIdx.x] = v;
     __syncthreads();
     for (int o = 1; o < 1024; o <<= 1) {
@@ -154,12 +168,12 @@ __global__ void k_scan(const int *__restrict__ cnt, int *__restrict__ off, int n
       s[threadIdx.x] += add;
       __syncthreads();
     }
-    if (t < np) off[t] = carry + s[threadIdx.x] - v;
+    if (t < np && EIF_CHK(bd.rec, t, bd.off, 5)) off[t] = carry + s[threadIdx.x] - v;
     __syncthreads();
     if (threadIdx.x == 1023) carry += s[1023];
     __syncthreads();
   }
-  if (threadIdx.x == 0) off[np] = carry;
+  if (threadIdx.x == 0 && EIF_CHK(bd.rec, np, bd.off, 6)) off[np] = carry;
 }
 
 // locate a chunk's particle: largest n with off[n] <= c
@@ -198,6 +212,7 @@ struct WorkArgs {
   double2 *wbuf;     // CHUNK per chunk (exchange only)
   int pcap, np, ld, mode, cn;   // mode 0: inertia (cn), 1: exchange
   double dx, dy, ly, h;
+  Bounds bd;
 };
 
 // one warp per chunk of box cells: indicator weights, partial sums, and (for
@@ -206,13 +221,16 @@ __global__ void __launch_bounds__(256) k_ibm_work(WorkArgs a) {
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  const int total = __ldg(a.off + a.np);
+  const int total = EIF_CHK(a.bd.rec, a.np, a.bd.off, 10) ? __ldg(a.off + a.np) : 0;
   const double rh = 1. / a.h;
   const double dxdy = a.dx * a.dy;
   const double dtv = a.mode == 1 ? __ldg(a.dt) : 0.;
   const int pc = a.pcap, ld = a.ld;
   for (int c = warp; c < total; c += nwarps) {
     const int n = find_particle(a.off, a.np, c);
+    if (!EIF_CHK(a.bd.rec, n, a.np, 11)) continue;
+    if (!EIF_CHK(a.bd.rec, 12 * n + 11, a.bd.box, 12)) continue;
+    if (!EIF_CHK(a.bd.rec, EIF_P_VZ * pc + n, a.bd.P, 13)) continue;
     const int local0 = (c - __ldg(a.off + n)) * CHUNK;
     int bx[12];
 #pragma unroll
@@ -236,7 +254,13 @@ __global__ void __launch_bounds__(256) k_ibm_work(WorkArgs a) {
       const int kk = local0 + half * 32 + lane;
       int i, j, img;
       double2 contrib = make_double2(0., 0.);
-      if (cell_of(bx, kk, i, j, img)) {
+      bool in = cell_of(bx, kk, i, j, img);
+      if (in) {
+        in = EIF_CHK(a.bd.rec, i, a.bd.xc - 1, 14) && EIF_CHK(a.bd.rec, j, a.bd.yc - 1, 15) &&
+             EIF_CHK(a.bd.rec, j * ld + i, a.bd.field, 16) && EIF_CHK(a.bd.rec, (j + 1) * ld + i, a.bd.field, 17) &&
+             EIF_CHK(a.bd.rec, j * ld + (i - 1), a.bd.field, 18);
+      }
+      if (in) {
         const double py_ = py + a.ly * img;
         Ell e = e0;
         e.py = py_;
@@ -267,12 +291,13 @@ __global__ void __launch_bounds__(256) k_ibm_work(WorkArgs a) {
           s2 += ((y - py_) * Fx / pim) - ((x - px) * Fy / pim);
         }
       }
-      if (a.mode == 1) a.wbuf[(size_t)c * CHUNK + half * 32 + lane] = contrib;
+      if (a.mode == 1 && EIF_CHK(a.bd.rec, (long long)c * CHUNK + half * 32 + lane, a.bd.wbuf, 19))
+        a.wbuf[(size_t)c * CHUNK + half * 32 + lane] = contrib;
     }
     s0 = eifd::warp_sum(s0);
     s1 = eifd::warp_sum(s1);
     s2 = eifd::warp_sum(s2);
-    if (lane == 0) {
+    if (lane == 0 && EIF_CHK(a.bd.rec, 3LL * c + 2, a.bd.partial, 20)) {
       a.partial[3 * (size_t)c + 0] = s0;
       a.partial[3 * (size_t)c + 1] = s1;
       a.partial[3 * (size_t)c + 2] = s2;
@@ -282,13 +307,15 @@ __global__ void __launch_bounds__(256) k_ibm_work(WorkArgs a) {
 
 // per-particle sums over chunks in a fixed order (warp per particle)
 __global__ void k_chunk_reduce(const double *__restrict__ partial, const int *__restrict__ off, double *__restrict__ P,
-                               int pcap, int np, int f0, int f1, int f2) {
+                               int pcap, int np, int f0, int f1, int f2, Bounds bd) {
   const int lane = threadIdx.x & 31;
   const int n = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (n >= np) return;
+  if (!EIF_CHK(bd.rec, n + 1, bd.off, 30)) return;
   const int c0 = off[n], c1 = off[n + 1];
   double s0 = 0., s1 = 0., s2 = 0.;
   for (int c = c0 + lane; c < c1; c += 32) {
+    if (!EIF_CHK(bd.rec, 3LL * c + 2, bd.partial, 31)) break;
     s0 += partial[3 * (size_t)c + 0];
     s1 += partial[3 * (size_t)c + 1];
     s2 += partial[3 * (size_t)c + 2];
@@ -296,7 +323,7 @@ __global__ void k_chunk_reduce(const double *__restrict__ partial, const int *__
   s0 = eifd::warp_sum(s0);
   s1 = eifd::warp_sum(s1);
   s2 = eifd::warp_sum(s2);
-  if (lane == 0) {
+  if (lane == 0 && EIF_CHK(bd.rec, f2 * pcap + n, bd.P, 32)) {
     P[f0 * pcap + n] = s0;
     P[f1 * pcap + n] = s1;
     P[f2 * pcap + n] = s2;
@@ -309,6 +336,7 @@ struct GatherArgs {
   double *dux, *duy;
   unsigned *flags;
   int np, itot, jtot, ld;
+  Bounds bd;
 };
 
 // field response dux/duy (exchange.c:71-72,80-81): per tile, the ordered list
@@ -357,6 +385,7 @@ __global__ void __launch_bounds__(GTHREADS) k_gather(GatherArgs a) {
     }
     __syncthreads();
     const int L = nlist;
+    if (!EIF_CHK(a.bd.rec, L, LMAX + 1, 46)) return;
     if (L > LMAX) {
       if (threadIdx.x == 0) atomicOr(a.flags, EIF_FLAG_NOCONV);
       return;
@@ -381,13 +410,14 @@ __global__ void __launch_bounds__(GTHREADS) k_gather(GatherArgs a) {
       }
       int pos = cnt[g - gbase] + s - m;
       for (int q = 0; q < 3; q++) {
-        if (bits & (1 << q)) list[pos++] = 3 * n + q;
+        if ((bits & (1 << q)) && EIF_CHK(a.bd.rec, pos, LMAX, 40)) list[pos++] = 3 * n + q;
       }
     }
     __syncthreads();
     // phase 3: accumulate in list order
     for (int e = 0; e < L; e++) {
       const int n = list[e] / 3, q = list[e] % 3;
+      if (!EIF_CHK(a.bd.rec, n, a.np, 44) || !EIF_CHK(a.bd.rec, 12LL * n + 11, a.bd.box, 45)) continue;
       const int *bx = a.box + 12 * n;
       // offset of image q within the particle's enumeration
       int base = 0;
@@ -401,7 +431,8 @@ __global__ void __launch_bounds__(GTHREADS) k_gather(GatherArgs a) {
 #pragma unroll
       for (int r = 0; r < 2; r++) {
         const int i = i0 + lx, j = j0 + ly0 + 4 * r;
-        if (i >= bi0 && i <= bi1 && j >= bj0 && j <= bj1) {
+        if (i >= bi0 && i <= bi1 && j >= bj0 && j <= bj1 &&
+            EIF_CHK(a.bd.rec, (long long)(pbase + (size_t)(j - bj0) * w + (i - bi0)), a.bd.wbuf, 41)) {
           const double2 v = a.wbuf[pbase + (size_t)(j - bj0) * w + (i - bi0)];
           acc_x[r] += v.x;
           acc_y[r] += v.y;
@@ -417,6 +448,12 @@ __global__ void __launch_bounds__(GTHREADS) k_gather(GatherArgs a) {
     const int i = i0 + lx, j = j0 + ly0 + 4 * r;
     if (i > i1 || j > j1) continue;
     const int cidx = j * ld + i;
+    {
+      // every index written for this cell: the cell, its halo-row copy and its Neumann copies
+      const long long lo = cidx - (i == 1 ? 1 : 0) - (j == jtot ? (long long)jtot * ld : 0);
+      const long long hi = cidx + (i == itot ? 1 : 0) + (j == 1 ? (long long)jtot * ld : 0);
+      if (!EIF_CHK(a.bd.rec, lo, a.bd.field, 42) || !EIF_CHK(a.bd.rec, hi, a.bd.field, 43)) continue;
+    }
     const double vx = acc_x[r], vy = acc_y[r];
     a.dux[cidx] = vx; a.duy[cidx] = vy;
     if (j == 1) { a.dux[cidx + jtot * ld] = vx; a.duy[cidx + jtot * ld] = vy; }
@@ -479,8 +516,24 @@ void ibm_free(eif_ctx *c) {
   c->chunk_cap = 0; c->wcap = 0;
 }
 
+static Bounds bounds_of(const eif_ctx *c) {
+  Bounds b;
+  b.P = (long long)EIF_NFIELDS * c->pcap;
+  b.box = 12LL * c->np;
+  b.off = 2LL * (c->np + 1);
+  b.partial = 3LL * c->chunk_cap;
+  b.wbuf = (long long)c->wcap;
+  b.field = (long long)c->nfield;
+  b.xc = c->itot + 3;   // entries 0..itot+1 (EIF_CHK is given xc-1 as the bound of valid i)
+  b.yc = c->jtot + 3;
+  b.rec = c->d_check;
+  return b;
+}
+
 static int launch_boxes(eif_ctx *c, bool use_increment) {
   BoxArgs b;
+  b.bd = bounds_of(c);
+  b.bd_off_base = c->chunk_off;
   b.P = c->P; b.pcap = c->pcap; b.np = c->np; b.itot = c->itot; b.jtot = c->jtot;
   b.use_increment = use_increment ? 1 : 0;
   b.dx = c->dx; b.dy = c->dy; b.ly = c->ly; b.yf1 = c->h_yf[0];
@@ -490,7 +543,7 @@ static int launch_boxes(eif_ctx *c, bool use_increment) {
   EIF_PROF(c, "ibm_boxes", 2);
   k_boxes<<<(c->np + 127) / 128, 128, 0, c->stream>>>(b);
   EIF_LAUNCH_CK(c);
-  k_scan<<<1, 1024, 0, c->stream>>>(cnt, c->chunk_off, c->np);
+  k_scan<<<1, 1024, 0, c->stream>>>(cnt, c->chunk_off, c->np, bounds_of(c));
   EIF_LAUNCH_CK(c);
   return EIF_OK;
 }
@@ -501,6 +554,7 @@ static int launch_work(eif_ctx *c, int mode, int cn) {
   w.box = c->box; w.off = c->chunk_off; w.partial = c->partial; w.wbuf = reinterpret_cast<double2 *>(c->wbuf);
   w.pcap = c->pcap; w.np = c->np; w.ld = c->ld; w.mode = mode; w.cn = cn;
   w.dx = c->dx; w.dy = c->dy; w.ly = c->ly; w.h = std::min(c->dx, c->dy);
+  w.bd = bounds_of(c);
   const int blocks = std::max(1, std::min(c->sms * 8, (c->chunk_cap * 32 + 255) / 256));
   {
     EIF_PROF(c, mode == 0 ? "ibm_inertia" : "ibm_exchange", 1);
@@ -512,7 +566,7 @@ static int launch_work(eif_ctx *c, int mode, int cn) {
   const int f2 = mode == 0 ? EIF_P_IVZ0 + cn : EIF_P_TVZ;
   EIF_PROF(c, "ibm_reduce", 1);
   k_chunk_reduce<<<(c->np * 32 + 255) / 256, 256, 0, c->stream>>>(c->partial, c->chunk_off, c->P, c->pcap, c->np, f0,
-                                                                    f1, f2);
+                                                                    f1, f2, bounds_of(c));
   EIF_LAUNCH_CK(c);
   return EIF_OK;
 }
@@ -539,6 +593,7 @@ int launch_exchange(eif_ctx *c) {
   g.box = c->box; g.off = c->chunk_off; g.wbuf = reinterpret_cast<const double2 *>(c->wbuf);
   g.dux = c->dux; g.duy = c->duy; g.flags = c->d_flags;
   g.np = c->np; g.itot = c->itot; g.jtot = c->jtot; g.ld = c->ld;
+  g.bd = bounds_of(c);
   dim3 grid((c->itot + GTX - 1) / GTX, (c->jtot + GTY - 1) / GTY);
   EIF_PROF(c, "ibm_gather", 1);
   k_gather<<<grid, GTHREADS, 0, c->stream>>>(g);
