@@ -61,6 +61,7 @@ def parse():
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--workload", default="mixed_target", choices=["mixed_target", "poiseuille", "couette_circle"])
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
 
 
@@ -213,7 +214,7 @@ def run_ours(args, world, rank, local, pg):
         "clocks": clk.summary(),
         "kernels": {e["name"]: {"launches": e["launches"], "ms": round(e["ms"], 4)} for e in prof},
     }
-    if rank == 0 and world == 1:
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args, case)
     return out, rank
 
