@@ -30,6 +30,7 @@ extern "C" {
 #define EIF_ERR_NOMEM (-4)    /* device or host allocation failed */
 #define EIF_ERR_STATE (-5)    /* call out of order (e.g. step before push) */
 #define EIF_ERR_NONFINITE (-6)/* a NaN/Inf was found in the velocity field */
+#define EIF_ERR_TOO_LARGE (-7)/* size beyond the fixed scratch of eif_decide_dt_noalloc */
 
 /* ---- arithmetic of the step ---- */
 #define EIF_PREC_FP64 0       /* every operation in double precision */
@@ -129,6 +130,29 @@ int eif_update_pressure(eif_ctx *ctx);                                /* src/flu
 int eif_compute_collision_force(eif_ctx *ctx, int cnstep);            /* src/suspensions/collision.c:306-367 */
 int eif_increment_particles(eif_ctx *ctx, int rkstep, double *residual); /* src/suspensions/increment.c:66-72 */
 int eif_update_particles(eif_ctx *ctx);                               /* src/suspensions/update.c:61-65 */
+
+/* ---- time-step size without device allocation ----
+ * No counterpart in the reference. Computes the same dt as eif_decide_dt
+ * (param_decide_dt) directly from the caller's device arrays, for callers that
+ * cannot let a library allocate device memory: applications that own all
+ * device memory through their own pool, and time-critical loops in which a
+ * cudaMalloc/cudaFree would synchronise the device. It allocates nothing; its
+ * scratch is a fixed array in the library's static device memory (about
+ * 128 KiB per GPU, held until the process exits), which limits itot to
+ * EIF_NOALLOC_MAX_ITOT (larger grids return EIF_ERR_TOO_LARGE).
+ *   ux, uy:     device arrays in the reference layouts (rows 0..jtot+1) with row
+ *               pitches ux_pitch >= itot+1 and uy_pitch >= itot+2 (in doubles)
+ *   safefactors: host array of 3 (advective, diffusive, particle)
+ *   particles:  device array of n_particles * EIF_NFIELDS doubles (may be NULL if 0)
+ *   dt:         device pointer that receives the result, written on `stream`
+ *   stream:     a cudaStream_t (NULL: the legacy default stream)
+ * The first call on a device looks up the scratch address (do it before any
+ * stream capture). All calls share the scratch array: calls that overlap on
+ * the GPU race and must be serialised by the caller. */
+#define EIF_NOALLOC_MAX_ITOT 16384
+int eif_decide_dt_noalloc(const double *ux, int ux_pitch, const double *uy, int uy_pitch, int itot, int jtot,
+                          double ly, double Re, const double *safefactors, const double *particles,
+                          int n_particles, double *dt, void *stream);
 
 /* ---- diagnostics (src/logging.c:40-80) ---- */
 int eif_divergence(eif_ctx *ctx, double *divmax, double *divsum);
