@@ -305,6 +305,171 @@ __global__ void __launch_bounds__(256) k_ibm_work(WorkArgs a) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Single-precision indicator (EIF_PREC_MIXED). Cell offsets from the particle
+// centre are formed in grid units, (x - px)/dx = (i - i0) - g with the integer
+// i0 and the fraction g computed once per chunk in double precision, so the
+// per-cell arithmetic is single precision without cancellation. The normal
+// foot iteration is the reference's (ellipse.c:30-65) with a stopping threshold
+// suited to single precision.
+constexpr float NORMAL_TOL_F = 2.e-6f;
+constexpr int NORMAL_MAX_F = 24;
+
+struct EllF {
+  float a, b, cz, sz, kex, key;
+};
+
+__device__ __forceinline__ float normal_t_f(const EllF &e, float x_, float y_) {
+  const float px = fabsf(x_), py = fabsf(y_);
+  float t = 0.78539816339744831f;
+  for (int n = 0; n < NORMAL_MAX_F; n++) {
+    float st, ct;
+    sincosf(t, &st, &ct);
+    const float x = e.a * ct, y = e.b * st;
+    const float ex = e.kex * (ct * ct * ct), ey = e.key * (st * st * st);
+    const float rx = x - ex, ry = y - ey, qx = px - ex, qy = py - ey;
+    const float r = sqrtf(ry * ry + rx * rx);
+    const float q = sqrtf(qy * qy + qx * qx);
+    const float arg = fminf(fmaxf((rx * qy - ry * qx) / (r * q), -1.f), 1.f);
+    const float dc = r * asinf(arg);
+    // a^2 + b^2 - x^2 - y^2 written without cancellation
+    const float dt = dc / sqrtf(e.a * e.a * (st * st) + e.b * e.b * (ct * ct));
+    t += dt;
+    t = fminf(1.5707963267948966f, t);
+    t = fmaxf(0.f, t);
+    if (fabsf(dt) < NORMAL_TOL_F) break;
+  }
+  if (x_ < 0.f) t = 3.14159265358979323846f - t;
+  if (y_ < 0.f) t = -t;
+  return t;
+}
+
+// signed distance in grid units from the offset (X, Y) = (x - px, y - py)
+__device__ __forceinline__ float signed_dist_f(const EllF &e, float X, float Y, float rh) {
+  const float x_ = e.cz * X - e.sz * Y;
+  const float y_ = e.sz * X + e.cz * Y;
+  const float f0 = 1.f - (x_ / e.a) * (x_ / e.a) - (y_ / e.b) * (y_ / e.b);
+  const float sign = f0 > 0.f ? 1.f : -1.f;
+  const float t = normal_t_f(e, x_, y_);
+  float st, ct;
+  sincosf(t, &st, &ct);
+  const float dxx = e.a * ct - x_, dyy = e.b * st - y_;
+  return sign * sqrtf(dxx * dxx + dyy * dyy) * rh;
+}
+
+// one warp per chunk, single precision (see k_ibm_work for the decomposition)
+__global__ void __launch_bounds__(256) k_ibm_work_f(WorkArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const int total = EIF_CHK(a.bd.rec, a.np, a.bd.off, 50) ? __ldg(a.off + a.np) : 0;
+  const float rh = (float)(1. / a.h);
+  const float dxf = (float)a.dx, dyf = (float)a.dy;
+  const float dxdy = (float)(a.dx * a.dy);
+  const float dtv = a.mode == 1 ? (float)__ldg(a.dt) : 0.f;
+  const int pc = a.pcap, ld = a.ld;
+  float2 *wb = reinterpret_cast<float2 *>(a.wbuf);
+  for (int c = warp; c < total; c += nwarps) {
+    const int n = find_particle(a.off, a.np, c);
+    if (!EIF_CHK(a.bd.rec, n, a.np, 51)) continue;
+    if (!EIF_CHK(a.bd.rec, 12 * n + 11, a.bd.box, 52)) continue;
+    if (!EIF_CHK(a.bd.rec, EIF_P_VZ * pc + n, a.bd.P, 53)) continue;
+    const int local0 = (c - __ldg(a.off + n)) * CHUNK;
+    int bx[12];
+#pragma unroll
+    for (int q = 0; q < 12; q++) bx[q] = __ldg(a.box + 12 * n + q);
+    const double *P = a.P;
+    const double pden = __ldg(P + EIF_P_DEN * pc + n), pa = __ldg(P + EIF_P_A * pc + n), pb = __ldg(P + EIF_P_B * pc + n);
+    double px = __ldg(P + EIF_P_X * pc + n), py = __ldg(P + EIF_P_Y * pc + n), paz = __ldg(P + EIF_P_AZ * pc + n);
+    if (a.mode == 0) {
+      px = px + __ldg(P + EIF_P_DX * pc + n);
+      py = py + __ldg(P + EIF_P_DY * pc + n);
+      paz = paz + __ldg(P + EIF_P_DAZ * pc + n);
+    }
+    // per-chunk double-precision set-up (warp-uniform)
+    const float rpm = (float)(1. / pmass(pden, pa, pb));
+    const float rpim = (float)(1. / pmoi(pden, pa, pb));
+    const float pux = (float)__ldg(P + EIF_P_UX * pc + n), puy = (float)__ldg(P + EIF_P_UY * pc + n);
+    const float pvz = (float)__ldg(P + EIF_P_VZ * pc + n);
+    EllF e;
+    e.a = (float)pa; e.b = (float)pb;
+    {
+      double sz, cz;
+      sincos(-paz, &sz, &cz);
+      e.cz = (float)cz; e.sz = (float)sz;
+      e.kex = (float)(pa * (1. - (pb / pa) * (pb / pa)));
+      e.key = (float)(pb * (1. - (pa / pb) * (pa / pb)));
+    }
+    // XC(i) = (i - 1/2) dx: (x - px)/dx = (i - i0) - gx
+    const double sx = px / a.dx;
+    const int i0 = (int)floor(sx);
+    const float gx = (float)(sx - i0 + 0.5);
+    // YC(j) = (j - 1/2) dy for each periodic image -1, 0, +1
+    int j0s[3];
+    float gys[3];
+#pragma unroll
+    for (int m = 0; m < 3; m++) {
+      const double sy = (py + a.ly * (m - 1)) / a.dy;
+      j0s[m] = (int)floor(sy);
+      gys[m] = (float)(sy - j0s[m] + 0.5);
+    }
+    float sacc0 = 0.f, sacc1 = 0.f, sacc2 = 0.f;
+#pragma unroll
+    for (int half = 0; half < CHUNK / 32; half++) {
+      const int kk = local0 + half * 32 + lane;
+      int i, j, img;
+      float2 contrib = make_float2(0.f, 0.f);
+      bool in = cell_of(bx, kk, i, j, img);
+      if (in) {
+        in = EIF_CHK(a.bd.rec, j * ld + i, a.bd.field, 54) && EIF_CHK(a.bd.rec, (j + 1) * ld + i, a.bd.field, 55) &&
+             EIF_CHK(a.bd.rec, j * ld + (i - 1), a.bd.field, 56);
+      }
+      if (in) {
+        const int j0 = img < 0 ? j0s[0] : (img == 0 ? j0s[1] : j0s[2]);
+        const float gy = img < 0 ? gys[0] : (img == 0 ? gys[1] : gys[2]);
+        const float X = ((float)(i - i0) - gx) * dxf;
+        const float Y = ((float)(j - j0) - gy) * dyf;
+        const float d = signed_dist_f(e, X, Y, rh);
+        const float th = tanhf(2.f * d);
+        const float uxs = (float)__ldg(a.ux + j * ld + (i - 1)) + (float)__ldg(a.ux + j * ld + i);
+        const float uys = (float)__ldg(a.uy + j * ld + i) + (float)__ldg(a.uy + (j + 1) * ld + i);
+        if (a.mode == 0) {
+          const float w = 0.5f * (1.f + th);
+          const float valx = w * 0.5f * uxs * dxdy;
+          const float valy = w * 0.5f * uys * dxdy;
+          sacc0 += valx * rpm;
+          sacc1 += valy * rpm;
+          sacc2 += (-Y * valx + X * valy) * rpim;
+        } else {
+          const float w = 1.f - th * th;
+          const float uxp = pux - pvz * Y;
+          const float uyp = puy + pvz * X;
+          const float gxv = w * (uxp - 0.5f * uxs);   // fx * dt
+          const float gyv = w * (uyp - 0.5f * uys);   // fy * dt
+          contrib = make_float2(gxv, gyv);
+          const float Fx = gxv / dtv * dxdy, Fy = gyv / dtv * dxdy;
+          sacc0 -= Fx * rpm;
+          sacc1 -= Fy * rpm;
+          sacc2 += (Y * Fx - X * Fy) * rpim;
+        }
+      }
+      if (a.mode == 1 && EIF_CHK(a.bd.rec, (long long)c * CHUNK + half * 32 + lane, 2 * a.bd.wbuf, 57))
+        wb[(size_t)c * CHUNK + half * 32 + lane] = contrib;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      sacc0 += __shfl_xor_sync(0xffffffffu, sacc0, o);
+      sacc1 += __shfl_xor_sync(0xffffffffu, sacc1, o);
+      sacc2 += __shfl_xor_sync(0xffffffffu, sacc2, o);
+    }
+    if (lane == 0 && EIF_CHK(a.bd.rec, 3LL * c + 2, a.bd.partial, 58)) {
+      a.partial[3 * (size_t)c + 0] = sacc0;
+      a.partial[3 * (size_t)c + 1] = sacc1;
+      a.partial[3 * (size_t)c + 2] = sacc2;
+    }
+  }
+}
+
 // per-particle sums over chunks in a fixed order (warp per particle)
 __global__ void k_chunk_reduce(const double *__restrict__ partial, const int *__restrict__ off, double *__restrict__ P,
                                int pcap, int np, int f0, int f1, int f2, Bounds bd) {
@@ -332,7 +497,7 @@ __global__ void k_chunk_reduce(const double *__restrict__ partial, const int *__
 
 struct GatherArgs {
   const int *box, *off;
-  const double2 *wbuf;
+  const void *wbuf;
   double *dux, *duy;
   unsigned *flags;
   int np, itot, jtot, ld;
@@ -341,7 +506,9 @@ struct GatherArgs {
 
 // field response dux/duy (exchange.c:71-72,80-81): per tile, the ordered list
 // of covering (particle, image) boxes, then per cell the sum in that order
+template <typename V2, typename Acc>
 __global__ void __launch_bounds__(GTHREADS) k_gather(GatherArgs a) {
+  const V2 *wbuf = static_cast<const V2 *>(a.wbuf);
   __shared__ int list[LMAX];
   __shared__ int cnt[1024 / 32 + 1];
   __shared__ int nlist;
@@ -349,7 +516,7 @@ __global__ void __launch_bounds__(GTHREADS) k_gather(GatherArgs a) {
   const int i1 = min(i0 + GTX - 1, a.itot), j1 = min(j0 + GTY - 1, a.jtot);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = GTHREADS / 32;
   const int ngroups = (a.np + 31) / 32;
-  double acc_x[2] = {0., 0.}, acc_y[2] = {0., 0.};
+  Acc acc_x[2] = {0, 0}, acc_y[2] = {0, 0};
   // cells of this thread: (i0 + lx, j0 + ly) for two rows
   const int lx = threadIdx.x % GTX, ly0 = threadIdx.x / GTX;  // GTHREADS / GTX = 4 rows per pass
   for (int gbase = 0; gbase < ngroups; gbase += 32) {
@@ -432,8 +599,9 @@ __global__ void __launch_bounds__(GTHREADS) k_gather(GatherArgs a) {
       for (int r = 0; r < 2; r++) {
         const int i = i0 + lx, j = j0 + ly0 + 4 * r;
         if (i >= bi0 && i <= bi1 && j >= bj0 && j <= bj1 &&
-            EIF_CHK(a.bd.rec, (long long)(pbase + (size_t)(j - bj0) * w + (i - bi0)), a.bd.wbuf, 41)) {
-          const double2 v = a.wbuf[pbase + (size_t)(j - bj0) * w + (i - bi0)];
+            EIF_CHK(a.bd.rec, (long long)(pbase + (size_t)(j - bj0) * w + (i - bi0)),
+                    a.bd.wbuf * (long long)(sizeof(double2) / sizeof(V2)), 41)) {
+          const V2 v = wbuf[pbase + (size_t)(j - bj0) * w + (i - bi0)];
           acc_x[r] += v.x;
           acc_y[r] += v.y;
         }
@@ -454,7 +622,7 @@ __global__ void __launch_bounds__(GTHREADS) k_gather(GatherArgs a) {
       const long long hi = cidx + (i == itot ? 1 : 0) + (j == 1 ? (long long)jtot * ld : 0);
       if (!EIF_CHK(a.bd.rec, lo, a.bd.field, 42) || !EIF_CHK(a.bd.rec, hi, a.bd.field, 43)) continue;
     }
-    const double vx = acc_x[r], vy = acc_y[r];
+    const double vx = (double)acc_x[r], vy = (double)acc_y[r];
     a.dux[cidx] = vx; a.duy[cidx] = vy;
     if (j == 1) { a.dux[cidx + jtot * ld] = vx; a.duy[cidx + jtot * ld] = vy; }
     if (j == jtot) { a.dux[cidx - jtot * ld] = vx; a.duy[cidx - jtot * ld] = vy; }
@@ -558,7 +726,11 @@ static int launch_work(eif_ctx *c, int mode, int cn) {
   const int blocks = std::max(1, std::min(c->sms * 8, (c->chunk_cap * 32 + 255) / 256));
   {
     EIF_PROF(c, mode == 0 ? "ibm_inertia" : "ibm_exchange", 1);
-    k_ibm_work<<<blocks, 256, 0, c->stream>>>(w);
+    if (c->cfg.precision == EIF_PREC_MIXED) {
+      k_ibm_work_f<<<blocks, 256, 0, c->stream>>>(w);
+    } else {
+      k_ibm_work<<<blocks, 256, 0, c->stream>>>(w);
+    }
     EIF_LAUNCH_CK(c);
   }
   const int f0 = mode == 0 ? EIF_P_IUX0 + cn : EIF_P_FUX;
@@ -590,13 +762,17 @@ int launch_exchange(eif_ctx *c) {
   rc = launch_work(c, 1, 0);
   if (rc) return rc;
   GatherArgs g;
-  g.box = c->box; g.off = c->chunk_off; g.wbuf = reinterpret_cast<const double2 *>(c->wbuf);
+  g.box = c->box; g.off = c->chunk_off; g.wbuf = c->wbuf;
   g.dux = c->dux; g.duy = c->duy; g.flags = c->d_flags;
   g.np = c->np; g.itot = c->itot; g.jtot = c->jtot; g.ld = c->ld;
   g.bd = bounds_of(c);
   dim3 grid((c->itot + GTX - 1) / GTX, (c->jtot + GTY - 1) / GTY);
   EIF_PROF(c, "ibm_gather", 1);
-  k_gather<<<grid, GTHREADS, 0, c->stream>>>(g);
+  if (c->cfg.precision == EIF_PREC_MIXED) {
+    k_gather<float2, float><<<grid, GTHREADS, 0, c->stream>>>(g);
+  } else {
+    k_gather<double2, double><<<grid, GTHREADS, 0, c->stream>>>(g);
+  }
   EIF_LAUNCH_CK(c);
   return EIF_OK;
 }

@@ -1,0 +1,78 @@
+"""Mixed-precision form (EIF_PREC_MIXED) against the double-precision form.
+
+The double-precision form is pinned to the reference (test_gpu_parity.py).
+The mixed form computes the indicator, the immersed-boundary forcing and the
+predictor stencils in single precision while keeping storage, the Poisson
+solve, the projection and the particle dynamics in double precision. Its
+error bars are those of the target: velocity within 1e-4 relative to the
+double-precision run, maximum divergence below 1e-5.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_err
+from ellipsesinflows_gb300 import PREC_FP64, PREC_MIXED, Simulation, cases
+from ellipsesinflows_gb300.capi import F
+
+pytestmark = pytest.mark.gpu
+
+TOL_VEL = 1e-4
+TOL_DIV = 1e-5
+
+
+def pair(case):
+    a = Simulation.from_case(case, precision=PREC_FP64)
+    b = Simulation.from_case(case, precision=PREC_MIXED)
+    return a, b
+
+
+def vec_err(P, Q, fx, fy):
+    scale = max(np.max(np.abs(Q[:, F[fx]])), np.max(np.abs(Q[:, F[fy]])))
+    return max(np.max(np.abs(P[:, F[fx]] - Q[:, F[fx]])), np.max(np.abs(P[:, F[fy]] - Q[:, F[fy]]))) / scale
+
+
+@pytest.mark.parametrize("builder", [
+    lambda: cases.contact_cluster(),
+    lambda: cases.poiseuille(itot=256, jtot=512, n=24, a=0.04, b=0.02, seed=4),
+], ids=["contact_cluster", "poiseuille_256x512"])
+def test_mixed_ibm_stage_matches_fp64(builder, gpu_lib):
+    case = builder()
+    d, m = pair(case)
+    # drive a few steps in double precision so that the flow is not at rest
+    d.advance(2)
+    ux, uy, p, _ = d.pull_fluid()
+    parts = d.pull_particles()
+    m.push_fluid(ux, uy, p)
+    m.push_particles(parts)
+    for s in (d, m):
+        s.dt = 2.0e-4
+        s.reset_particle_increments()
+        s.compute_inertia(0)
+        s.exchange_momentum()
+    P, Q = m.pull_particles(), d.pull_particles()
+    assert vec_err(P, Q, "iux0", "iuy0") < 1e-5
+    assert vec_err(P, Q, "fux", "fuy") < 1e-4
+    for a, b in zip(m.pull_ibm_fields(), d.pull_ibm_fields()):
+        assert rel_err(a, b) < 1e-4
+
+
+@pytest.mark.parametrize("builder,steps", [
+    (lambda: cases.poiseuille(itot=256, jtot=512, n=24, a=0.04, b=0.02, seed=4), 20),
+    (lambda: cases.poiseuille(), 10),
+], ids=["poiseuille_256x512", "poiseuille_512x1024"])
+def test_mixed_steps_within_error_bars(builder, steps, gpu_lib):
+    case = builder()
+    d, m = pair(case)
+    for _ in range(steps):
+        d.advance(1)
+        m.advance(1)
+    du, dv, _, _ = d.pull_fluid()
+    mu, mv, _, _ = m.pull_fluid()
+    umag = max(np.abs(du).max(), np.abs(dv).max())
+    err = max(np.abs(mu - du).max(), np.abs(mv - dv).max()) / umag
+    assert err < TOL_VEL, err
+    divmax, _ = m.divergence()
+    assert divmax < TOL_DIV, divmax
+    P, Q = m.pull_particles(), d.pull_particles()
+    assert np.max(np.abs(P[:, F["x"]] - Q[:, F["x"]])) < 1e-6
+    assert np.max(np.abs(P[:, F["y"]] - Q[:, F["y"]])) < 1e-6
