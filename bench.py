@@ -58,7 +58,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
+    ap.add_argument("--no-fp64-leg", action="store_true")
     ap.add_argument("--workload", default="mixed_target", choices=["mixed_target", "poiseuille", "couette_circle"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -191,6 +192,10 @@ def run_ours(args, world, rank, local, pg):
     ms = start.elapsed_time(stop)
     ms = max_over_ranks(pg, ms, local)
     prof = profile_entries(sim)
+    accuracy = None
+    fp64 = None
+    if prec == PREC_MIXED and not args.no_fp64_leg:
+        fp64, accuracy = fp64_leg(args, case, sim, local, pg, world)
     # ---- end-to-end through the public API with host buffers ----
     e2e = None
     if not args.no_e2e:
@@ -211,12 +216,45 @@ def run_ours(args, world, rank, local, pg):
                    "l2": "inputs larger than L2 (~1 GB of device state per step)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "e2e": e2e, "roofline": roof, "gpu_launches": launches,
+        "fp64_form": fp64, "accuracy_vs_fp64": accuracy,
         "clocks": clk.summary(),
         "kernels": {e["name"]: {"launches": e["launches"], "ms": round(e["ms"], 4)} for e in prof},
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args, case)
     return out, rank
+
+
+def fp64_leg(args, case, mixed_sim, device, pg, world):
+    """The plain double-precision form on the same workload and step count, and the
+    error of the mixed-precision state against it after the same number of steps."""
+    import torch
+    from ellipsesinflows_gb300 import PREC_FP64, Simulation
+    sim = Simulation.from_case(case, precision=PREC_FP64, device=device)
+    stream = torch.cuda.ExternalStream(sim._fn("stream")(sim.ctx), device=device)
+    for _ in range(args.warmup):
+        sim.advance(1)
+    sim.synchronize()
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier(pg, device)
+    torch.cuda.synchronize()
+    start.record(stream)
+    sim.advance(args.steps)
+    stop.record(stream)
+    torch.cuda.synchronize()
+    ms = max_over_ranks(pg, start.elapsed_time(stop), device)
+    value = world * case.cells * args.steps / (ms / 1e3)
+    # both forms have now advanced warmup + steps steps from the same initial state
+    du, dv, _, _ = sim.pull_fluid()
+    mu, mv, _, _ = mixed_sim.pull_fluid()
+    umag = max(np.abs(du).max(), np.abs(dv).max())
+    err = max(np.abs(mu - du).max(), np.abs(mv - dv).max()) / umag
+    divmax, _ = mixed_sim.divergence()
+    divmax64, _ = sim.divergence()
+    sim.close()
+    return ({"value": value, "unit": "cell-steps/s", "ms_per_step": ms / args.steps},
+            {"steps_compared": args.warmup + args.steps, "velocity_rel_err": err, "max_divergence": divmax,
+             "max_divergence_fp64": divmax64})
 
 
 def profile_entries(sim):

@@ -106,6 +106,18 @@ int device_metrics(eif_ctx *c) {
     cyp[i] = DXC(i + 1) / (2. * DXF(i));
   }
   int rc;
+  auto upload_f = [&](float **dst, const std::vector<double> &v) -> int {
+    std::vector<float> f(v.begin(), v.end());
+    EIF_CK(c, cudaMalloc((void **)dst, sizeof(float) * f.size()));
+    EIF_CK(c, cudaMemcpy(*dst, f.data(), sizeof(float) * f.size(), cudaMemcpyHostToDevice));
+    return EIF_OK;
+  };
+  if ((rc = upload_f(&c->rdxf_f, rdxf))) return rc;
+  if ((rc = upload_f(&c->rdxc_f, rdxc))) return rc;
+  if ((rc = upload_f(&c->cxm_f, cxm))) return rc;
+  if ((rc = upload_f(&c->cxp_f, cxp))) return rc;
+  if ((rc = upload_f(&c->cym_f, cym))) return rc;
+  if ((rc = upload_f(&c->cyp_f, cyp))) return rc;
   if ((rc = upload(c, &c->xc, xc))) return rc;
   if ((rc = upload(c, &c->yc, yc))) return rc;
   if ((rc = upload(c, &c->rdxf, rdxf))) return rc;
@@ -216,6 +228,13 @@ int eif_create(const eif_config_t *cfg, eif_ctx **out) {
     CK_CREATE(cudaMalloc((void **)f, sizeof(double) * c->nfield));
     CK_CREATE(cudaMemset(*f, 0, sizeof(double) * c->nfield));
   }
+  if (cfg->precision == EIF_PREC_MIXED) {
+    float **ffields[] = {&c->sxf[0], &c->sxf[1], &c->syf[0], &c->syf[1]};
+    for (float **f : ffields) {
+      CK_CREATE(cudaMalloc((void **)f, sizeof(float) * c->nfield));
+      CK_CREATE(cudaMemset(*f, 0, sizeof(float) * c->nfield));
+    }
+  }
   CK_CREATE(cudaMalloc((void **)&c->d_scal, sizeof(double) * 4));
   CK_CREATE(cudaMemset(c->d_scal, 0, sizeof(double) * 4));
   CK_CREATE(cudaMalloc((void **)&c->d_flags, sizeof(unsigned)));
@@ -246,6 +265,9 @@ int eif_destroy(eif_ctx *c) {
                     c->sya[1], c->dux, c->duy, c->qhat, c->xc, c->yc, c->rdxf, c->rdxc, c->cxm, c->cxp, c->cym,
                     c->cyp, c->dxc, c->P, c->d_scal};
   for (double *p : ptrs) if (p) cudaFree(p);
+  float *fptrs[] = {c->rdxf_f, c->rdxc_f, c->cxm_f, c->cxp_f, c->cym_f, c->cyp_f, c->sxf[0], c->sxf[1], c->syf[0],
+                    c->syf[1]};
+  for (float *p : fptrs) if (p) cudaFree(p);
   if (c->d_flags) cudaFree(c->d_flags);
   if (c->d_check) cudaFree(c->d_check);
   if (c->h_check) cudaFreeHost(c->h_check);
@@ -329,6 +351,20 @@ int eif_pull_src(eif_ctx *c, double *uxa, double *uxb, double *uya, double *uyb)
   const size_t dp = sizeof(double) * c->ld;
   const size_t wx = sizeof(double) * (c->itot - 1), wy = sizeof(double) * c->itot;
   const int a = c->scur, b = 1 - c->scur;
+  if (c->cfg.precision == EIF_PREC_MIXED) {
+    // the mixed form keeps these terms in float: widen each through the scratch field
+    const float *srcs[4] = {c->sxf[a], c->sxf[b], c->syf[a], c->syf[b]};
+    double *dsts[4] = {uxa, uxb, uya, uyb};
+    for (int k = 0; k < 4; k++) {
+      if (!dsts[k]) continue;
+      int rc = launch_f2d_copy(c, srcs[k], c->qhat, c->nfield);
+      if (rc) return rc;
+      const size_t w = k < 2 ? wx : wy;
+      EIF_CK(c, cudaMemcpy2DAsync(dsts[k], w, c->qhat + c->ld + 1, dp, w, c->jtot, cudaMemcpyDeviceToHost, c->stream));
+      EIF_CK(c, cudaStreamSynchronize(c->stream));
+    }
+    return check_records(c);
+  }
   // SRCUXA(2,1) sits at ux index (2,1) -> row 1, column 1
   if (uxa) EIF_CK(c, cudaMemcpy2DAsync(uxa, wx, c->sxa[a] + c->ld + 1, dp, wx, c->jtot, cudaMemcpyDeviceToHost, c->stream));
   if (uxb) EIF_CK(c, cudaMemcpy2DAsync(uxb, wx, c->sxa[b] + c->ld + 1, dp, wx, c->jtot, cudaMemcpyDeviceToHost, c->stream));
@@ -342,6 +378,19 @@ int eif_push_src(eif_ctx *c, const double *uxa, const double *uya) {
   if (!c || !uxa || !uya) return EIF_ERR_ARG;
   const size_t dp = sizeof(double) * c->ld;
   const size_t wx = sizeof(double) * (c->itot - 1), wy = sizeof(double) * c->itot;
+  if (c->cfg.precision == EIF_PREC_MIXED) {
+    float *dsts[2] = {c->sxf[c->scur], c->syf[c->scur]};
+    const double *srcs[2] = {uxa, uya};
+    for (int k = 0; k < 2; k++) {
+      EIF_CK(c, cudaMemsetAsync(c->qhat, 0, sizeof(double) * c->nfield, c->stream));
+      const size_t w = k == 0 ? wx : wy;
+      EIF_CK(c, cudaMemcpy2DAsync(c->qhat + c->ld + 1, dp, srcs[k], w, w, c->jtot, cudaMemcpyHostToDevice, c->stream));
+      int rc = launch_d2f_copy(c, c->qhat, dsts[k], c->nfield);
+      if (rc) return rc;
+    }
+    EIF_CK(c, cudaStreamSynchronize(c->stream));
+    return EIF_OK;
+  }
   EIF_CK(c, cudaMemcpy2DAsync(c->sxa[c->scur] + c->ld + 1, dp, uxa, wx, wx, c->jtot, cudaMemcpyHostToDevice, c->stream));
   EIF_CK(c, cudaMemcpy2DAsync(c->sya[c->scur] + c->ld + 1, dp, uya, wy, wy, c->jtot, cudaMemcpyHostToDevice, c->stream));
   EIF_CK(c, cudaStreamSynchronize(c->stream));

@@ -99,6 +99,8 @@ struct eif_ctx {
   double *rdxf, *rdxc;          // 1/DXF(i), 1/DXC(i) at [i]
   double *cxm, *cxp, *cym, *cyp;// stencil interpolation weights at [i]
   double *dxc;                  // DXC(i) at [i]
+  float *rdxf_f, *rdxc_f, *cxm_f, *cxp_f, *cym_f, *cyp_f;  // single-precision copies
+  float *sxf[2], *syf[2];       // RK explicit terms of the mixed form
   // host copies of the metrics
   double *h_xf, *h_xc, *h_dxf, *h_dxc, *h_yf, *h_yc;
   eif::PoissonPlan pp;
@@ -163,6 +165,8 @@ int launch_correct(eif_ctx *c, int rk, bool with_ibm, bool with_pressure);
 int launch_update_pressure(eif_ctx *c);
 int launch_decide_dt(eif_ctx *c);
 int launch_divergence(eif_ctx *c, double *divmax, double *divsum);
+int launch_f2d_copy(eif_ctx *c, const float *in, double *out, size_t n);
+int launch_d2f_copy(eif_ctx *c, const double *in, float *out, size_t n);
 
 // ---- Poisson (poisson.cu) ----
 int poisson_init(eif_ctx *c);
@@ -213,6 +217,39 @@ __device__ __forceinline__ bool chk(unsigned long long *rec, long long idx, long
 
 __device__ __forceinline__ int ux_idx(int i, int j, int ld) { return j * ld + (i - 1); }
 __device__ __forceinline__ int uy_idx(int i, int j, int ld) { return j * ld + i; }
+
+// Conversions between double and float with integer operations on the IEEE-754
+// fields. On this GPU the hardware double->float conversion runs at a small
+// fraction of the FP64 rate, so the mixed-precision kernels use these instead.
+// d2f: exponent rebiased from 1023 to 127, mantissa cut to 23 bits and rounded
+// on the first discarded bit (ties away from zero); magnitudes below the
+// smallest normal float give a signed zero, above the largest float infinity.
+__device__ __forceinline__ float d2f(double x) {
+  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  const unsigned sign = hi & 0x80000000u, mag = hi & 0x7fffffffu;
+  unsigned f = (((mag - (896u << 20)) << 3) | (lo >> 29)) + ((lo >> 28) & 1u);
+  f = mag < (897u << 20) ? 0u : f;
+  f = mag >= (1151u << 20) ? 0x7f800000u : f;
+  return __uint_as_float(sign | f);
+}
+
+// f2d: exact for normal floats; zero and subnormal floats give a signed zero.
+__device__ __forceinline__ double f2d(float x) {
+  const unsigned u = __float_as_uint(x);
+  const unsigned sign = u & 0x80000000u, mag = u & 0x7fffffffu;
+  unsigned hi = sign | ((mag >> 3) + (896u << 20));
+  unsigned lo = mag << 29;
+  hi = mag < 0x00800000u ? sign : hi;
+  lo = mag < 0x00800000u ? 0u : lo;
+  hi = mag >= 0x7f800000u ? (sign | 0x7ff00000u | ((mag >> 3) & 0x000fffffu)) : hi;
+  return __hiloint2double((int)hi, (int)lo);
+}
+
+// a double as an unevaluated sum hi + lo of two floats (about 48 significant bits)
+__device__ __forceinline__ float2 d2ff(double x) {
+  const float hi = d2f(x);
+  return make_float2(hi, d2f(x - f2d(hi)));
+}
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll

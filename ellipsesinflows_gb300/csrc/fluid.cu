@@ -141,6 +141,111 @@ __global__ void __launch_bounds__(TX *TY) k_predictor(PredArgs a) {
 }
 
 // ---------------------------------------------------------------------------
+// Mixed-precision predictor: the same update with the source terms computed in
+// single precision. Each block stages a (TX+2) x (TY+2) tile of ux, uy and p in
+// shared memory as unevaluated float pairs hi + lo, so that differences of
+// neighbouring values keep their relative precision although the values
+// themselves are O(1); one double subtraction per staged value, instead of one
+// per stencil difference. The explicit terms are stored in float; the velocity
+// update u + (alpha A + beta B + gamma G) dt is added in double precision.
+struct PredArgsF {
+  const double *ux, *uy, *p;
+  const float *sxb, *syb;
+  float *sxa, *sya;
+  double *uxn, *uyn;
+  const float *rdxf, *rdxc, *cxm, *cxp, *cym, *cyp;
+  const double *dt;
+  double alpha, beta, gamma;
+  float rRe, rdy, ext;
+  int itot, jtot, ld;
+};
+
+constexpr int PX = TX + 2, PY = TY + 2;
+
+__device__ __forceinline__ float dif(float2 a, float2 b) { return (a.x - b.x) + (a.y - b.y); }
+__device__ __forceinline__ float val(float2 a) { return a.x + a.y; }
+
+__global__ void __launch_bounds__(TX *TY) k_predictor_mixed(PredArgsF a) {
+  __shared__ float2 tux[PY][PX], tuy[PY][PX], tp[PY][PX];
+  const int ld = a.ld, itot = a.itot, jtot = a.jtot;
+  const int ib = 1 + blockIdx.x * TX, jb = 1 + blockIdx.y * TY;
+  // stage the tile: tile (tx, ty) holds index (ib - 1 + tx, jb - 1 + ty)
+  for (int t = threadIdx.y * TX + threadIdx.x; t < PX * PY; t += TX * TY) {
+    const int tx = t % PX, ty = t / PX;
+    const int i = ib - 1 + tx, j = jb - 1 + ty;
+    float2 vux = make_float2(0.f, 0.f), vuy = vux, vp = vux;
+    if (j <= jtot + 1) {
+      if (i >= 1 && i <= itot + 1) vux = eifd::d2ff(__ldg(a.ux + j * ld + (i - 1)));
+      if (i <= itot + 1) {
+        vuy = eifd::d2ff(__ldg(a.uy + j * ld + i));
+        vp = eifd::d2ff(__ldg(a.p + j * ld + i));
+      }
+    }
+    tux[ty][tx] = vux;
+    tuy[ty][tx] = vuy;
+    tp[ty][tx] = vp;
+  }
+  __syncthreads();
+  const int i = ib + threadIdx.x, j = jb + threadIdx.y;
+  if (i > itot || j > jtot) return;
+  const int x = threadIdx.x + 1, y = threadIdx.y + 1;
+  const double dt = __ldg(a.dt);
+  const float adt = (float)(a.alpha * dt), bdt = (float)(a.beta * dt), gdt = (float)(a.gamma * dt);
+  const float rdy = a.rdy;
+  if (i >= 2) {
+    const float2 u0 = tux[y][x], uw = tux[y][x - 1], ue = tux[y][x + 1], us = tux[y - 1][x], un = tux[y + 1][x];
+    const float cxm = __ldg(a.cxm + i), cxp = __ldg(a.cxp + i);
+    const float duxdx_xm = dif(u0, uw) * __ldg(a.rdxf + i - 1);
+    const float duxdx_xp = dif(ue, u0) * __ldg(a.rdxf + i);
+    const float duxdy_ym = dif(u0, us) * rdy;
+    const float duxdy_yp = dif(un, u0) * rdy;
+    const float ux_xm = 0.5f * (val(uw) + val(u0));
+    const float ux_xp = 0.5f * (val(u0) + val(ue));
+    const float adv1 = -cxm * ux_xm * duxdx_xm - cxp * ux_xp * duxdx_xp;
+    const float uy_ym = cxm * val(tuy[y][x - 1]) + cxp * val(tuy[y][x]);
+    const float uy_yp = cxm * val(tuy[y + 1][x - 1]) + cxp * val(tuy[y + 1][x]);
+    const float adv2 = -0.5f * uy_ym * duxdy_ym - 0.5f * uy_yp * duxdy_yp;
+    const float rdxc = __ldg(a.rdxc + i);
+    const float dif_ = a.rRe * ((dif(ue, u0) * __ldg(a.rdxf + i) - dif(u0, uw) * __ldg(a.rdxf + i - 1)) * rdxc +
+                                (dif(un, u0) - dif(u0, us)) * rdy * rdy);
+    const float pre = -dif(tp[y][x], tp[y][x - 1]) * rdxc;
+    const float A = (adv1 + adv2) + dif_;
+    const int c = j * ld + (i - 1);
+    const float B = __ldg(a.sxb + c);
+    a.sxa[c] = A;
+    const double un_ = __ldg(a.ux + c) + eifd::f2d(adt * A + bdt * B + gdt * pre);
+    a.uxn[c] = un_;
+    if (j == 1) a.uxn[c + jtot * ld] = un_;
+    if (j == jtot) a.uxn[c - jtot * ld] = un_;
+  }
+  {
+    const float2 v0 = tuy[y][x], vw = tuy[y][x - 1], ve = tuy[y][x + 1], vs = tuy[y - 1][x], vn = tuy[y + 1][x];
+    const float rdxc_m = __ldg(a.rdxc + i), rdxc_p = __ldg(a.rdxc + i + 1);
+    const float duydx_xm = dif(v0, vw) * rdxc_m;
+    const float duydx_xp = dif(ve, v0) * rdxc_p;
+    const float duydy_ym = dif(v0, vs) * rdy;
+    const float duydy_yp = dif(vn, v0) * rdy;
+    const float cym = __ldg(a.cym + i), cyp = __ldg(a.cyp + i);
+    const float ux_xm = 0.5f * (val(tux[y - 1][x]) + val(tux[y][x]));
+    const float ux_xp = 0.5f * (val(tux[y - 1][x + 1]) + val(tux[y][x + 1]));
+    const float adv1 = -cym * ux_xm * duydx_xm - cyp * ux_xp * duydx_xp;
+    const float uy_ym = 0.5f * (val(vs) + val(v0));
+    const float uy_yp = 0.5f * (val(v0) + val(vn));
+    const float adv2 = -0.5f * uy_ym * duydy_ym - 0.5f * uy_yp * duydy_yp;
+    const float dif_ = a.rRe * ((duydx_xp - duydx_xm) * __ldg(a.rdxf + i) + (duydy_yp - duydy_ym) * rdy);
+    const float pre = -dif(tp[y][x], tp[y - 1][x]) * rdy;
+    const float A = (adv1 + adv2) + dif_ + a.ext;
+    const int c = j * ld + i;
+    const float B = __ldg(a.syb + c);
+    a.sya[c] = A;
+    const double vn_ = __ldg(a.uy + c) + eifd::f2d(adt * A + bdt * B + gdt * pre);
+    a.uyn[c] = vn_;
+    if (j == 1) a.uyn[c + jtot * ld] = vn_;
+    if (j == jtot) a.uyn[c - jtot * ld] = vn_;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Projection (src/fluid/correct_velocity.c:6-42), optionally preceded by the
 // IBM field response (src/suspensions/update.c:36-59) and followed by the
 // pressure update (src/fluid/update_pressure.c:7-24), in one pass. The IBM
@@ -345,10 +450,38 @@ int launch_boundaries(eif_ctx *c) {
   return EIF_OK;
 }
 
+static int launch_predictor_mixed(eif_ctx *c, int rk) {
+  const RK k = rk_coef(rk);
+  PredArgsF a;
+  a.ux = c->ux[c->cur];
+  a.uy = c->uy[c->cur];
+  a.p = c->p;
+  a.sxb = c->sxf[1 - c->scur];
+  a.syb = c->syf[1 - c->scur];
+  a.sxa = c->sxf[c->scur];
+  a.sya = c->syf[c->scur];
+  a.uxn = c->ux[1 - c->cur];
+  a.uyn = c->uy[1 - c->cur];
+  a.rdxf = c->rdxf_f; a.rdxc = c->rdxc_f;
+  a.cxm = c->cxm_f; a.cxp = c->cxp_f; a.cym = c->cym_f; a.cyp = c->cyp_f;
+  a.dt = c->d_scal;
+  a.alpha = k.alpha; a.beta = k.beta; a.gamma = k.gamma;
+  a.rRe = (float)(1. / c->cfg.Re);
+  a.rdy = (float)(1. / c->dy);
+  a.ext = (float)c->cfg.extfrcy;
+  a.itot = c->itot; a.jtot = c->jtot; a.ld = c->ld;
+  EIF_PROF(c, "predictor", 1);
+  k_predictor_mixed<<<cell_grid(c), dim3(TX, TY), 0, c->stream>>>(a);
+  EIF_LAUNCH_CK(c);
+  c->cur = 1 - c->cur;
+  return EIF_OK;
+}
+
 int launch_predictor(eif_ctx *c, int rk) {
   const RK k = rk_coef(rk);
   // the explicit term of the previous stage becomes srcB (update_velocity.c:26,110)
   c->scur = 1 - c->scur;
+  if (c->cfg.precision == EIF_PREC_MIXED) return launch_predictor_mixed(c, rk);
   PredArgs a;
   a.ux = c->ux[c->cur];
   a.uy = c->uy[c->cur];
@@ -442,4 +575,98 @@ int launch_divergence(eif_ctx *c, double *divmax, double *divsum) {
   return EIF_OK;
 }
 
+}  // namespace eif
+
+// ---------------------------------------------------------------------------
+// self-test of eifd::d2f / eifd::f2d against the hardware conversions
+namespace {
+
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+  z += 0x9e3779b97f4a7c15ull;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+
+__global__ void k_selftest_cvt(int n, unsigned long long *counts) {
+  unsigned long long bad_d2f = 0, bad_f2d = 0;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    // doubles whose exponents cover the float normal range and beyond
+    const unsigned long long r = mix64((unsigned long long)t);
+    const unsigned long long e = 850ull + (r >> 53) % 350ull;
+    const unsigned long long bits = (r & 0x800fffffffffffffull) | (e << 52);
+    double x = __longlong_as_double((long long)bits);
+    if (t == 0) x = 0.;
+    if (t == 1) x = -0.;
+    if (t == 2) x = 1.;
+    if (t == 3) x = 3.4028234663852886e38;  // FLT_MAX
+    if (t == 4) x = 1.1754943508222875e-38; // FLT_MIN
+    const float hw = __double2float_rn(x);
+    const float me = eifd::d2f(x);
+    const bool normal = fabs(x) >= 1.1754943508222875e-38 && fabs(x) <= 3.4028234663852886e38;
+    if (normal) {
+      const int diff = abs((int)__float_as_uint(hw) - (int)__float_as_uint(me));
+      if (diff > 1) bad_d2f++;
+      if (diff == 1) {
+        // allowed only on an exact tie (the discarded bits are exactly one half)
+        const unsigned lo = (unsigned)__double2loint(x);
+        if ((lo & 0x1fffffffu) != 0x10000000u) bad_d2f++;
+      }
+    }
+    // float -> double on the normal floats
+    const float xf = __uint_as_float((unsigned)(r & 0xffffffffu));
+    const unsigned mag = __float_as_uint(xf) & 0x7fffffffu;
+    if (mag >= 0x00800000u && mag < 0x7f800000u) {
+      if (__double_as_longlong(eifd::f2d(xf)) != __double_as_longlong((double)xf)) bad_f2d++;
+    }
+  }
+  atomicAdd(counts, bad_d2f);
+  atomicAdd(counts + 1, bad_f2d);
+}
+
+}  // namespace
+
+extern "C" int eif_selftest_conversions(int device, int n, long long *d2f_mismatch, long long *f2d_mismatch) {
+  if (n <= 0 || !d2f_mismatch || !f2d_mismatch) return EIF_ERR_ARG;
+  if (cudaSetDevice(device) != cudaSuccess) return EIF_ERR_CUDA;
+  unsigned long long *d = nullptr;
+  if (cudaMalloc((void **)&d, 2 * sizeof(unsigned long long)) != cudaSuccess) return EIF_ERR_NOMEM;
+  unsigned long long h[2] = {0, 0};
+  cudaError_t e = cudaMemset(d, 0, sizeof(h));
+  if (e == cudaSuccess) {
+    k_selftest_cvt<<<256, 256>>>(n, d);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return EIF_ERR_CUDA;
+  *d2f_mismatch = (long long)h[0];
+  *f2d_mismatch = (long long)h[1];
+  return EIF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// element-wise precision conversion of whole arrays (state transfer in the mixed form)
+namespace {
+__global__ void k_f2d_copy(const float *__restrict__ in, double *__restrict__ out, size_t n) {
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
+    out[t] = (double)in[t];
+}
+__global__ void k_d2f_copy(const double *__restrict__ in, float *__restrict__ out, size_t n) {
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
+    out[t] = __double2float_rn(in[t]);
+}
+}  // namespace
+
+namespace eif {
+int launch_f2d_copy(eif_ctx *c, const float *in, double *out, size_t n) {
+  k_f2d_copy<<<c->sms * 4, 256, 0, c->stream>>>(in, out, n);
+  EIF_LAUNCH_CK(c);
+  return EIF_OK;
+}
+int launch_d2f_copy(eif_ctx *c, const double *in, float *out, size_t n) {
+  k_d2f_copy<<<c->sms * 4, 256, 0, c->stream>>>(in, out, n);
+  EIF_LAUNCH_CK(c);
+  return EIF_OK;
+}
 }  // namespace eif

@@ -431,8 +431,8 @@ __global__ void __launch_bounds__(256) k_ibm_work_f(WorkArgs a) {
         const float Y = ((float)(j - j0) - gy) * dyf;
         const float d = signed_dist_f(e, X, Y, rh);
         const float th = tanhf(2.f * d);
-        const float uxs = (float)__ldg(a.ux + j * ld + (i - 1)) + (float)__ldg(a.ux + j * ld + i);
-        const float uys = (float)__ldg(a.uy + j * ld + i) + (float)__ldg(a.uy + (j + 1) * ld + i);
+        const float uxs = eifd::d2f(__ldg(a.ux + j * ld + (i - 1))) + eifd::d2f(__ldg(a.ux + j * ld + i));
+        const float uys = eifd::d2f(__ldg(a.uy + j * ld + i)) + eifd::d2f(__ldg(a.uy + (j + 1) * ld + i));
         if (a.mode == 0) {
           const float w = 0.5f * (1.f + th);
           const float valx = w * 0.5f * uxs * dxdy;
@@ -506,6 +506,9 @@ struct GatherArgs {
 
 // field response dux/duy (exchange.c:71-72,80-81): per tile, the ordered list
 // of covering (particle, image) boxes, then per cell the sum in that order
+__device__ __forceinline__ double to_double(double v) { return v; }
+__device__ __forceinline__ double to_double(float v) { return eifd::f2d(v); }
+
 template <typename V2, typename Acc>
 __global__ void __launch_bounds__(GTHREADS) k_gather(GatherArgs a) {
   const V2 *wbuf = static_cast<const V2 *>(a.wbuf);
@@ -622,7 +625,7 @@ __global__ void __launch_bounds__(GTHREADS) k_gather(GatherArgs a) {
       const long long hi = cidx + (i == itot ? 1 : 0) + (j == 1 ? (long long)jtot * ld : 0);
       if (!EIF_CHK(a.bd.rec, lo, a.bd.field, 42) || !EIF_CHK(a.bd.rec, hi, a.bd.field, 43)) continue;
     }
-    const double vx = (double)acc_x[r], vy = (double)acc_y[r];
+    const double vx = to_double(acc_x[r]), vy = to_double(acc_y[r]);
     a.dux[cidx] = vx; a.duy[cidx] = vy;
     if (j == 1) { a.dux[cidx + jtot * ld] = vx; a.duy[cidx + jtot * ld] = vy; }
     if (j == jtot) { a.dux[cidx - jtot * ld] = vx; a.duy[cidx - jtot * ld] = vy; }

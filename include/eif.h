@@ -154,6 +154,14 @@ int eif_decide_dt_noalloc(const double *ux, int ux_pitch, const double *uy, int 
                           double ly, double Re, const double *safefactors, const double *particles,
                           int n_particles, double *dt, void *stream);
 
+/* ---- self-test of the integer-pipe double<->float conversions used by the
+ * mixed-precision kernels (no counterpart in the reference) ----
+ * Converts n values spread over the normal range (plus zeros and the range
+ * limits) with both the library's conversions and the hardware ones and
+ * returns how many results differ by more than the rounding of a tie (d2f) or
+ * at all (f2d). */
+int eif_selftest_conversions(int device, int n, long long *d2f_mismatch, long long *f2d_mismatch);
+
 /* ---- diagnostics (src/logging.c:40-80) ---- */
 int eif_divergence(eif_ctx *ctx, double *divmax, double *divsum);
 

@@ -76,3 +76,35 @@ def test_mixed_steps_within_error_bars(builder, steps, gpu_lib):
     P, Q = m.pull_particles(), d.pull_particles()
     assert np.max(np.abs(P[:, F["x"]] - Q[:, F["x"]])) < 1e-6
     assert np.max(np.abs(P[:, F["y"]] - Q[:, F["y"]])) < 1e-6
+
+
+def test_integer_pipe_conversions_match_hardware(gpu_lib):
+    import ctypes
+    fn = gpu_lib.eif_selftest_conversions
+    fn.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)]
+    a, b = ctypes.c_longlong(-1), ctypes.c_longlong(-1)
+    assert fn(0, 1 << 24, ctypes.byref(a), ctypes.byref(b)) == 0
+    assert a.value == 0 and b.value == 0, (a.value, b.value)
+
+
+@pytest.mark.parametrize("builder", [
+    lambda: cases.couette_circle(),
+    lambda: cases.poiseuille(itot=256, jtot=512, n=24, a=0.04, b=0.02, seed=4),
+], ids=["couette_circle", "poiseuille_256x512"])
+def test_mixed_predictor_matches_fp64(builder, gpu_lib):
+    case = builder()
+    d, m = pair(case)
+    d.advance(3)
+    ux, uy, p, _ = d.pull_fluid()
+    m.push_fluid(ux, uy, p)
+    for s in (d, m):
+        s.dt = 1.0e-3
+        s.update_velocity(0)
+    ga, _, gya, _ = m.pull_src()
+    da, _, dya, _ = d.pull_src()
+    assert rel_err(ga, da) < 1e-5
+    assert rel_err(gya, dya) < 1e-5
+    mu, mv = m.pull_fluid()[:2]
+    du, dv = d.pull_fluid()[:2]
+    umag = max(np.abs(du).max(), np.abs(dv).max())
+    assert max(np.abs(mu - du).max(), np.abs(mv - dv).max()) / umag < 1e-9
