@@ -235,6 +235,8 @@ int eif_create(const eif_config_t *cfg, eif_ctx **out) {
       CK_CREATE(cudaMemset(*f, 0, sizeof(float) * c->nfield));
     }
   }
+  CK_CREATE(cudaMalloc((void **)&c->d_coef, sizeof(float) * 16));
+  CK_CREATE(cudaMemset(c->d_coef, 0, sizeof(float) * 16));
   CK_CREATE(cudaMalloc((void **)&c->d_scal, sizeof(double) * 4));
   CK_CREATE(cudaMemset(c->d_scal, 0, sizeof(double) * 4));
   CK_CREATE(cudaMalloc((void **)&c->d_flags, sizeof(unsigned)));
@@ -265,6 +267,7 @@ int eif_destroy(eif_ctx *c) {
                     c->sya[1], c->dux, c->duy, c->qhat, c->xc, c->yc, c->rdxf, c->rdxc, c->cxm, c->cxp, c->cym,
                     c->cyp, c->dxc, c->P, c->d_scal};
   for (double *p : ptrs) if (p) cudaFree(p);
+  if (c->d_coef) cudaFree(c->d_coef);
   float *fptrs[] = {c->rdxf_f, c->rdxc_f, c->cxm_f, c->cxp_f, c->cym_f, c->cyp_f, c->sxf[0], c->sxf[1], c->syf[0],
                     c->syf[1]};
   for (float *p : fptrs) if (p) cudaFree(p);
@@ -421,6 +424,8 @@ int eif_set_dt(eif_ctx *c, double dt) {
   if (!c || !(dt > 0.)) return EIF_ERR_ARG;
   c->h_scal[0] = dt;
   EIF_CK(c, cudaMemcpyAsync(c->d_scal, c->h_scal, sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  int rc = launch_coef(c);
+  if (rc) return rc;
   EIF_CK(c, cudaStreamSynchronize(c->stream));
   c->dt_host = dt;
   return EIF_OK;

@@ -114,8 +114,11 @@ struct eif_ctx {
   double *wbuf;                 // per box cell: dux, duy contribution
   size_t wcap;                  // capacity of wbuf in cells
   int chunk_cap;                // capacity of partial in chunks
+  float *pf;                    // per-particle single-precision parameters (mixed form)
+  int *owner;                   // owner particle of every chunk (mixed form)
   // device scalars
   double *d_scal;               // [0] dt, [1] residual, [2] scratch
+  float *d_coef;                // single-precision dt products: [3*rk+0..2] alpha/beta/gamma*dt, [9] 1/dt
   unsigned *d_flags;
   double *h_scal;               // pinned mirror
   unsigned *h_flags;
@@ -167,6 +170,7 @@ int launch_decide_dt(eif_ctx *c);
 int launch_divergence(eif_ctx *c, double *divmax, double *divsum);
 int launch_f2d_copy(eif_ctx *c, const float *in, double *out, size_t n);
 int launch_d2f_copy(eif_ctx *c, const double *in, float *out, size_t n);
+int launch_coef(eif_ctx *c);
 
 // ---- Poisson (poisson.cu) ----
 int poisson_init(eif_ctx *c);
@@ -245,10 +249,22 @@ __device__ __forceinline__ double f2d(float x) {
   return __hiloint2double((int)hi, (int)lo);
 }
 
-// a double as an unevaluated sum hi + lo of two floats (about 48 significant bits)
-__device__ __forceinline__ float2 d2ff(double x) {
-  const float hi = d2f(x);
-  return make_float2(hi, d2f(x - f2d(hi)));
+// a double as an unevaluated sum hi + lo of two floats, split with integer
+// operations only: hi keeps the leading 24 significant bits (truncated), lo is
+// the remaining 29 bits rounded to a float, so hi + lo carries about 48 bits.
+// Magnitudes below 2^-74 split into (x as a float, 0) precision-wise.
+__device__ __forceinline__ float2 split(double x) {
+  const unsigned hw = (unsigned)__double2hiint(x), lw = (unsigned)__double2loint(x);
+  const unsigned sign = hw & 0x80000000u, mag = hw & 0x7fffffffu;
+  const unsigned e = mag >> 20;                                   // biased double exponent
+  unsigned hb = ((mag - (896u << 20)) << 3) | (lw >> 29);         // truncated 24-bit significand
+  hb = mag < (897u << 20) ? 0u : hb;
+  // remaining bits: (lw & 0x1fffffff) * 2^(e - 1075)
+  const float rest = (float)(lw & 0x1fffffffu);
+  const int se = (int)e - 1075 + 127;
+  const float scale = se >= 1 ? __uint_as_float((unsigned)se << 23) : 0.f;
+  const float lo = mag < (897u << 20) ? 0.f : rest * scale;
+  return make_float2(__uint_as_float(sign | hb), sign ? -lo : lo);
 }
 
 __device__ __forceinline__ double warp_sum(double v) {

@@ -154,8 +154,7 @@ struct PredArgsF {
   float *sxa, *sya;
   double *uxn, *uyn;
   const float *rdxf, *rdxc, *cxm, *cxp, *cym, *cyp;
-  const double *dt;
-  double alpha, beta, gamma;
+  const float *coef;   // alpha dt, beta dt, gamma dt of this stage
   float rRe, rdy, ext;
   int itot, jtot, ld;
 };
@@ -175,10 +174,10 @@ __global__ void __launch_bounds__(TX *TY) k_predictor_mixed(PredArgsF a) {
     const int i = ib - 1 + tx, j = jb - 1 + ty;
     float2 vux = make_float2(0.f, 0.f), vuy = vux, vp = vux;
     if (j <= jtot + 1) {
-      if (i >= 1 && i <= itot + 1) vux = eifd::d2ff(__ldg(a.ux + j * ld + (i - 1)));
+      if (i >= 1 && i <= itot + 1) vux = eifd::split(__ldg(a.ux + j * ld + (i - 1)));
       if (i <= itot + 1) {
-        vuy = eifd::d2ff(__ldg(a.uy + j * ld + i));
-        vp = eifd::d2ff(__ldg(a.p + j * ld + i));
+        vuy = eifd::split(__ldg(a.uy + j * ld + i));
+        vp = eifd::split(__ldg(a.p + j * ld + i));
       }
     }
     tux[ty][tx] = vux;
@@ -189,8 +188,7 @@ __global__ void __launch_bounds__(TX *TY) k_predictor_mixed(PredArgsF a) {
   const int i = ib + threadIdx.x, j = jb + threadIdx.y;
   if (i > itot || j > jtot) return;
   const int x = threadIdx.x + 1, y = threadIdx.y + 1;
-  const double dt = __ldg(a.dt);
-  const float adt = (float)(a.alpha * dt), bdt = (float)(a.beta * dt), gdt = (float)(a.gamma * dt);
+  const float adt = __ldg(a.coef), bdt = __ldg(a.coef + 1), gdt = __ldg(a.coef + 2);
   const float rdy = a.rdy;
   if (i >= 2) {
     const float2 u0 = tux[y][x], uw = tux[y][x - 1], ue = tux[y][x + 1], us = tux[y - 1][x], un = tux[y + 1][x];
@@ -342,11 +340,24 @@ __global__ void k_dt_colmax(const double *__restrict__ ux, const double *__restr
   }
 }
 
+// single-precision products of dt used by the mixed-precision kernels, formed
+// once per time step instead of once per thread
+__device__ __forceinline__ void write_coef(double dt, float *coef) {
+  const double al[3] = {32. / 60., 25. / 60., 45. / 60.};
+  const double be[3] = {0. / 60., -17. / 60., -25. / 60.};
+  for (int rk = 0; rk < 3; rk++) {
+    coef[3 * rk + 0] = (float)(al[rk] * dt);
+    coef[3 * rk + 1] = (float)(be[rk] * dt);
+    coef[3 * rk + 2] = (float)((al[rk] + be[rk]) * dt);
+  }
+  coef[9] = (float)(1. / dt);
+}
+
 // dt from the maxima (decide_dt.c:25-80): one block.
 __global__ void k_dt_final(const unsigned long long *__restrict__ colmax, const unsigned long long *__restrict__ uymax,
                            const double *__restrict__ dxc, int itot, double dy, double Re, double lx, double dx_uniform,
                            double sf_adv, double sf_dif, double sf_par, const double *__restrict__ P, int pcap, int np,
-                           double *__restrict__ dt_out) {
+                           double *__restrict__ dt_out, float *__restrict__ coef) {
   const double small = 1.e-8;
   double dta = 5.e-2, dxmin = lx, dtp = DBL_MAX;
   for (int i = 2 + threadIdx.x; i <= itot; i += blockDim.x) {
@@ -385,9 +396,13 @@ __global__ void k_dt_final(const unsigned long long *__restrict__ colmax, const 
     difx *= sf_dif;
     dify *= sf_dif;
     dtp *= sf_par;
-    *dt_out = fmin(fmin(dta, fmin(difx, dify)), dtp);
+    const double dt = fmin(fmin(dta, fmin(difx, dify)), dtp);
+    *dt_out = dt;
+    write_coef(dt, coef);
   }
 }
+
+__global__ void k_coef(const double *__restrict__ dt, float *__restrict__ coef) { write_coef(*dt, coef); }
 
 // ---------------------------------------------------------------------------
 __global__ void k_divergence(const double *__restrict__ ux, const double *__restrict__ uy, const double *__restrict__ rdxf,
@@ -464,8 +479,8 @@ static int launch_predictor_mixed(eif_ctx *c, int rk) {
   a.uyn = c->uy[1 - c->cur];
   a.rdxf = c->rdxf_f; a.rdxc = c->rdxc_f;
   a.cxm = c->cxm_f; a.cxp = c->cxp_f; a.cym = c->cym_f; a.cyp = c->cyp_f;
-  a.dt = c->d_scal;
-  a.alpha = k.alpha; a.beta = k.beta; a.gamma = k.gamma;
+  (void)k;
+  a.coef = c->d_coef + 3 * rk;
   a.rRe = (float)(1. / c->cfg.Re);
   a.rdy = (float)(1. / c->dy);
   a.ext = (float)c->cfg.extfrcy;
@@ -548,7 +563,7 @@ int launch_decide_dt(eif_ctx *c) {
   EIF_LAUNCH_CK(c);
   k_dt_final<<<1, 256, 0, c->stream>>>(colmax, uymax, c->dxc, c->itot, c->dy, c->cfg.Re, c->lx, c->dx,
                                        c->cfg.safefactors[0], c->cfg.safefactors[1], c->cfg.safefactors[2], c->P,
-                                       c->pcap, c->np, c->d_scal);
+                                       c->pcap, c->np, c->d_scal, c->d_coef);
   EIF_LAUNCH_CK(c);
   return EIF_OK;
 }
@@ -666,6 +681,14 @@ int launch_f2d_copy(eif_ctx *c, const float *in, double *out, size_t n) {
 }
 int launch_d2f_copy(eif_ctx *c, const double *in, float *out, size_t n) {
   k_d2f_copy<<<c->sms * 4, 256, 0, c->stream>>>(in, out, n);
+  EIF_LAUNCH_CK(c);
+  return EIF_OK;
+}
+}  // namespace eif
+
+namespace eif {
+int launch_coef(eif_ctx *c) {
+  k_coef<<<1, 1, 0, c->stream>>>(c->d_scal, c->d_coef);
   EIF_LAUNCH_CK(c);
   return EIF_OK;
 }

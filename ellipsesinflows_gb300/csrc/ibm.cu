@@ -114,10 +114,17 @@ struct Bounds {
   unsigned long long *rec;
 };
 
+// Per-particle single-precision parameters of the mixed-precision indicator,
+// PF_WORDS words per particle (see k_boxes).
+constexpr int PF_WORDS = 24;
+enum { PF_A, PF_B, PF_CZ, PF_SZ, PF_KEX, PF_KEY, PF_RPM, PF_RPIM, PF_UX, PF_UY, PF_VZ, PF_GX, PF_I0,
+       PF_J0, PF_GY = PF_J0 + 3 };
+
 struct BoxArgs {
   const double *P;
   int pcap, np, itot, jtot, use_increment;
   double dx, dy, ly, yf1;
+  float *pf;                // PF_WORDS per particle, or null (double-precision form)
   int *box, *nchunk;
   const int *bd_off_base;   // start of the buffer nchunk points into
   Bounds bd;
@@ -137,6 +144,38 @@ __global__ void k_boxes(BoxArgs a) {
     py = py + P[EIF_P_DY * pc + n];
   }
   const double r = fmax(pa, pb);
+  if (a.pf) {
+    // everything the single-precision cell loop needs, formed once per particle in double
+    float *q = a.pf + (size_t)PF_WORDS * n;
+    const double den = P[EIF_P_DEN * pc + n];
+    double az = P[EIF_P_AZ * pc + n];
+    if (a.use_increment) az = az + P[EIF_P_DAZ * pc + n];
+    double sz, cz;
+    sincos(-az, &sz, &cz);
+    q[PF_A] = (float)pa;
+    q[PF_B] = (float)pb;
+    q[PF_CZ] = (float)cz;
+    q[PF_SZ] = (float)sz;
+    q[PF_KEX] = (float)(pa * (1. - (pb / pa) * (pb / pa)));
+    q[PF_KEY] = (float)(pb * (1. - (pa / pb) * (pa / pb)));
+    q[PF_RPM] = (float)(1. / pmass(den, pa, pb));
+    q[PF_RPIM] = (float)(1. / pmoi(den, pa, pb));
+    q[PF_UX] = (float)P[EIF_P_UX * pc + n];
+    q[PF_UY] = (float)P[EIF_P_UY * pc + n];
+    q[PF_VZ] = (float)P[EIF_P_VZ * pc + n];
+    // cell centres XC(i) = (i - 1/2) dx, YC(j) = (j - 1/2) dy: offsets in grid units are
+    // (i - i0) - gx and (j - j0[m]) - gy[m] for the periodic images m = -1, 0, +1
+    const double sx = px / a.dx;
+    const int i0 = (int)floor(sx);
+    q[PF_GX] = (float)(sx - i0 + 0.5);
+    q[PF_I0] = __int_as_float(i0);
+    for (int m = 0; m < 3; m++) {
+      const double sy = (py + a.ly * (m - 1)) / a.dy;
+      const int j0 = (int)floor(sy);
+      q[PF_J0 + m] = __int_as_float(j0);
+      q[PF_GY + m] = (float)(sy - j0 + 0.5);
+    }
+  }
   int cells = 0;
   for (int per = -1; per <= 1; per++) {
     int imin, imax, jmin, jmax;
@@ -176,6 +215,16 @@ __global__ void k_scan(const int *__restrict__ cnt, int *__restrict__ off, int n
   if (threadIdx.x == 0 && EIF_CHK(bd.rec, np, bd.off, 6)) off[np] = carry;
 }
 
+// owner particle of every chunk (replaces a search per chunk)
+__global__ void k_chunk_owner(const int *__restrict__ off, int *__restrict__ owner, int np, Bounds bd, int cap) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= np) return;
+  const int c0 = off[n], c1 = off[n + 1];
+  for (int c = c0; c < c1; c++) {
+    if (EIF_CHK(bd.rec, c, cap, 59)) owner[c] = n;
+  }
+}
+
 // locate a chunk's particle: largest n with off[n] <= c
 __device__ __forceinline__ int find_particle(const int *__restrict__ off, int np, int c) {
   int lo = 0, hi = np - 1;
@@ -212,6 +261,10 @@ struct WorkArgs {
   double2 *wbuf;     // CHUNK per chunk (exchange only)
   int pcap, np, ld, mode, cn;   // mode 0: inertia (cn), 1: exchange
   double dx, dy, ly, h;
+  const float *pf;       // per-particle single-precision parameters (mixed form)
+  const int *owner;      // owner particle of every chunk (mixed form)
+  const float *coef;     // single-precision dt products; [9] = 1/dt
+  float rh_f, dx_f, dy_f, dxdy_f;
   Bounds bd;
 };
 
@@ -363,56 +416,26 @@ __global__ void __launch_bounds__(256) k_ibm_work_f(WorkArgs a) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const int total = EIF_CHK(a.bd.rec, a.np, a.bd.off, 50) ? __ldg(a.off + a.np) : 0;
-  const float rh = (float)(1. / a.h);
-  const float dxf = (float)a.dx, dyf = (float)a.dy;
-  const float dxdy = (float)(a.dx * a.dy);
-  const float dtv = a.mode == 1 ? (float)__ldg(a.dt) : 0.f;
-  const int pc = a.pcap, ld = a.ld;
+  const float rh = a.rh_f, dxf = a.dx_f, dyf = a.dy_f, dxdy = a.dxdy_f;
+  const float rdtv = a.mode == 1 ? __ldg(a.coef + 9) : 0.f;
+  const int ld = a.ld;
   float2 *wb = reinterpret_cast<float2 *>(a.wbuf);
   for (int c = warp; c < total; c += nwarps) {
-    const int n = find_particle(a.off, a.np, c);
-    if (!EIF_CHK(a.bd.rec, n, a.np, 51)) continue;
-    if (!EIF_CHK(a.bd.rec, 12 * n + 11, a.bd.box, 52)) continue;
-    if (!EIF_CHK(a.bd.rec, EIF_P_VZ * pc + n, a.bd.P, 53)) continue;
+    if (!EIF_CHK(a.bd.rec, c, a.bd.partial / 3, 51)) continue;
+    const int n = __ldg(a.owner + c);
+    if (!EIF_CHK(a.bd.rec, n, a.np, 52) || !EIF_CHK(a.bd.rec, 12 * n + 11, a.bd.box, 53)) continue;
     const int local0 = (c - __ldg(a.off + n)) * CHUNK;
-    int bx[12];
-#pragma unroll
-    for (int q = 0; q < 12; q++) bx[q] = __ldg(a.box + 12 * n + q);
-    const double *P = a.P;
-    const double pden = __ldg(P + EIF_P_DEN * pc + n), pa = __ldg(P + EIF_P_A * pc + n), pb = __ldg(P + EIF_P_B * pc + n);
-    double px = __ldg(P + EIF_P_X * pc + n), py = __ldg(P + EIF_P_Y * pc + n), paz = __ldg(P + EIF_P_AZ * pc + n);
-    if (a.mode == 0) {
-      px = px + __ldg(P + EIF_P_DX * pc + n);
-      py = py + __ldg(P + EIF_P_DY * pc + n);
-      paz = paz + __ldg(P + EIF_P_DAZ * pc + n);
-    }
-    // per-chunk double-precision set-up (warp-uniform)
-    const float rpm = (float)(1. / pmass(pden, pa, pb));
-    const float rpim = (float)(1. / pmoi(pden, pa, pb));
-    const float pux = (float)__ldg(P + EIF_P_UX * pc + n), puy = (float)__ldg(P + EIF_P_UY * pc + n);
-    const float pvz = (float)__ldg(P + EIF_P_VZ * pc + n);
+    const int4 *b4 = reinterpret_cast<const int4 *>(a.box + 12 * n);
+    const int4 bA = __ldg(b4), bB = __ldg(b4 + 1), bC = __ldg(b4 + 2);
+    const int bx[12] = {bA.x, bA.y, bA.z, bA.w, bB.x, bB.y, bB.z, bB.w, bC.x, bC.y, bC.z, bC.w};
+    const float4 *q4 = reinterpret_cast<const float4 *>(a.pf + (size_t)PF_WORDS * n);
+    const float4 qA = __ldg(q4), qB = __ldg(q4 + 1), qC = __ldg(q4 + 2), qD = __ldg(q4 + 3), qE = __ldg(q4 + 4);
     EllF e;
-    e.a = (float)pa; e.b = (float)pb;
-    {
-      double sz, cz;
-      sincos(-paz, &sz, &cz);
-      e.cz = (float)cz; e.sz = (float)sz;
-      e.kex = (float)(pa * (1. - (pb / pa) * (pb / pa)));
-      e.key = (float)(pb * (1. - (pa / pb) * (pa / pb)));
-    }
-    // XC(i) = (i - 1/2) dx: (x - px)/dx = (i - i0) - gx
-    const double sx = px / a.dx;
-    const int i0 = (int)floor(sx);
-    const float gx = (float)(sx - i0 + 0.5);
-    // YC(j) = (j - 1/2) dy for each periodic image -1, 0, +1
-    int j0s[3];
-    float gys[3];
-#pragma unroll
-    for (int m = 0; m < 3; m++) {
-      const double sy = (py + a.ly * (m - 1)) / a.dy;
-      j0s[m] = (int)floor(sy);
-      gys[m] = (float)(sy - j0s[m] + 0.5);
-    }
+    e.a = qA.x; e.b = qA.y; e.cz = qA.z; e.sz = qA.w; e.kex = qB.x; e.key = qB.y;
+    const float rpm = qB.z, rpim = qB.w, pux = qC.x, puy = qC.y, pvz = qC.z, gx = qC.w;
+    const int i0 = __float_as_int(qD.x);
+    const int j0s[3] = {__float_as_int(qD.y), __float_as_int(qD.z), __float_as_int(qD.w)};
+    const float gys[3] = {qE.x, qE.y, qE.z};
     float sacc0 = 0.f, sacc1 = 0.f, sacc2 = 0.f;
 #pragma unroll
     for (int half = 0; half < CHUNK / 32; half++) {
@@ -425,10 +448,9 @@ __global__ void __launch_bounds__(256) k_ibm_work_f(WorkArgs a) {
              EIF_CHK(a.bd.rec, j * ld + (i - 1), a.bd.field, 56);
       }
       if (in) {
-        const int j0 = img < 0 ? j0s[0] : (img == 0 ? j0s[1] : j0s[2]);
-        const float gy = img < 0 ? gys[0] : (img == 0 ? gys[1] : gys[2]);
+        const int m = img + 1;
         const float X = ((float)(i - i0) - gx) * dxf;
-        const float Y = ((float)(j - j0) - gy) * dyf;
+        const float Y = ((float)(j - j0s[m]) - gys[m]) * dyf;
         const float d = signed_dist_f(e, X, Y, rh);
         const float th = tanhf(2.f * d);
         const float uxs = eifd::d2f(__ldg(a.ux + j * ld + (i - 1))) + eifd::d2f(__ldg(a.ux + j * ld + i));
@@ -447,7 +469,7 @@ __global__ void __launch_bounds__(256) k_ibm_work_f(WorkArgs a) {
           const float gxv = w * (uxp - 0.5f * uxs);   // fx * dt
           const float gyv = w * (uyp - 0.5f * uys);   // fy * dt
           contrib = make_float2(gxv, gyv);
-          const float Fx = gxv / dtv * dxdy, Fy = gyv / dtv * dxdy;
+          const float Fx = gxv * rdtv * dxdy, Fy = gyv * rdtv * dxdy;
           sacc0 -= Fx * rpm;
           sacc1 -= Fy * rpm;
           sacc2 += (Y * Fx - X * Fy) * rpim;
@@ -463,9 +485,9 @@ __global__ void __launch_bounds__(256) k_ibm_work_f(WorkArgs a) {
       sacc2 += __shfl_xor_sync(0xffffffffu, sacc2, o);
     }
     if (lane == 0 && EIF_CHK(a.bd.rec, 3LL * c + 2, a.bd.partial, 58)) {
-      a.partial[3 * (size_t)c + 0] = sacc0;
-      a.partial[3 * (size_t)c + 1] = sacc1;
-      a.partial[3 * (size_t)c + 2] = sacc2;
+      a.partial[3 * (size_t)c + 0] = eifd::f2d(sacc0);
+      a.partial[3 * (size_t)c + 1] = eifd::f2d(sacc1);
+      a.partial[3 * (size_t)c + 2] = eifd::f2d(sacc2);
     }
   }
 }
@@ -675,6 +697,8 @@ int ibm_reserve(eif_ctx *c) {
   EIF_CK(c, cudaMalloc((void **)&c->chunk_off, sizeof(int) * 2 * (c->np + 1)));
   EIF_CK(c, cudaMalloc((void **)&c->partial, sizeof(double) * 3 * chunks));
   EIF_CK(c, cudaMalloc((void **)&c->wbuf, sizeof(double2) * c->wcap));
+  EIF_CK(c, cudaMalloc((void **)&c->pf, sizeof(float) * PF_WORDS * c->np));
+  EIF_CK(c, cudaMalloc((void **)&c->owner, sizeof(int) * (size_t)chunks));
   return EIF_OK;
 }
 
@@ -683,7 +707,10 @@ void ibm_free(eif_ctx *c) {
   if (c->chunk_off) cudaFree(c->chunk_off);
   if (c->partial) cudaFree(c->partial);
   if (c->wbuf) cudaFree(c->wbuf);
+  if (c->pf) cudaFree(c->pf);
+  if (c->owner) cudaFree(c->owner);
   c->box = nullptr; c->chunk_off = nullptr; c->partial = nullptr; c->wbuf = nullptr;
+  c->pf = nullptr; c->owner = nullptr;
   c->chunk_cap = 0; c->wcap = 0;
 }
 
@@ -709,13 +736,19 @@ static int launch_boxes(eif_ctx *c, bool use_increment) {
   b.use_increment = use_increment ? 1 : 0;
   b.dx = c->dx; b.dy = c->dy; b.ly = c->ly; b.yf1 = c->h_yf[0];
   b.box = c->box;
+  b.pf = c->cfg.precision == EIF_PREC_MIXED ? c->pf : nullptr;
   int *cnt = c->chunk_off + (c->np + 1);
   b.nchunk = cnt;
-  EIF_PROF(c, "ibm_boxes", 2);
+  EIF_PROF(c, "ibm_boxes", c->cfg.precision == EIF_PREC_MIXED ? 3 : 2);
   k_boxes<<<(c->np + 127) / 128, 128, 0, c->stream>>>(b);
   EIF_LAUNCH_CK(c);
   k_scan<<<1, 1024, 0, c->stream>>>(cnt, c->chunk_off, c->np, bounds_of(c));
   EIF_LAUNCH_CK(c);
+  if (c->cfg.precision == EIF_PREC_MIXED) {
+    k_chunk_owner<<<(c->np + 127) / 128, 128, 0, c->stream>>>(c->chunk_off, c->owner, c->np, bounds_of(c),
+                                                               c->chunk_cap);
+    EIF_LAUNCH_CK(c);
+  }
   return EIF_OK;
 }
 
@@ -726,6 +759,13 @@ static int launch_work(eif_ctx *c, int mode, int cn) {
   w.pcap = c->pcap; w.np = c->np; w.ld = c->ld; w.mode = mode; w.cn = cn;
   w.dx = c->dx; w.dy = c->dy; w.ly = c->ly; w.h = std::min(c->dx, c->dy);
   w.bd = bounds_of(c);
+  w.pf = c->pf;
+  w.owner = c->owner;
+  w.coef = c->d_coef;
+  w.rh_f = (float)(1. / w.h);
+  w.dx_f = (float)c->dx;
+  w.dy_f = (float)c->dy;
+  w.dxdy_f = (float)(c->dx * c->dy);
   const int blocks = std::max(1, std::min(c->sms * 8, (c->chunk_cap * 32 + 255) / 256));
   {
     EIF_PROF(c, mode == 0 ? "ibm_inertia" : "ibm_exchange", 1);

@@ -104,7 +104,8 @@ def test_mixed_predictor_matches_fp64(builder, gpu_lib):
     da, _, dya, _ = d.pull_src()
     assert rel_err(ga, da) < 1e-5
     assert rel_err(gya, dya) < 1e-5
+    # the stage's velocity increment carries the single-precision error of its terms
     mu, mv = m.pull_fluid()[:2]
     du, dv = d.pull_fluid()[:2]
-    umag = max(np.abs(du).max(), np.abs(dv).max())
-    assert max(np.abs(mu - du).max(), np.abs(mv - dv).max()) / umag < 1e-9
+    inc = max(np.abs(du - ux).max(), np.abs(dv - uy).max())
+    assert max(np.abs(mu - du).max(), np.abs(mv - dv).max()) / inc < 1e-5
