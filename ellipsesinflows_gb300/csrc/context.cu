@@ -235,8 +235,8 @@ int eif_create(const eif_config_t *cfg, eif_ctx **out) {
       CK_CREATE(cudaMemset(*f, 0, sizeof(float) * c->nfield));
     }
   }
-  CK_CREATE(cudaMalloc((void **)&c->d_coef, sizeof(float) * 16));
-  CK_CREATE(cudaMemset(c->d_coef, 0, sizeof(float) * 16));
+  CK_CREATE(cudaMalloc((void **)&c->d_coef, sizeof(float) * 32));
+  CK_CREATE(cudaMemset(c->d_coef, 0, sizeof(float) * 32));
   CK_CREATE(cudaMalloc((void **)&c->d_scal, sizeof(double) * 4));
   CK_CREATE(cudaMemset(c->d_scal, 0, sizeof(double) * 4));
   CK_CREATE(cudaMalloc((void **)&c->d_flags, sizeof(unsigned)));

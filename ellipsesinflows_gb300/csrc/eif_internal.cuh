@@ -62,6 +62,7 @@ struct PoissonPlan {
   double2 *tw;      // exp(-2 pi i k / m), k < m
   double2 *rot;     // exp(-i pi k / 2n), k < n
   double2 *wn;      // exp(-2 pi i k / n), k < n
+  float4 *tw_f, *rot_f, *wn_f;  // the same tables as float pairs (re hi, re lo, im hi, im lo)
   // tridiagonal solver along y (jtot rows, one system per wavenumber)
   int blk;          // interior rows per block + 1 (EIF_TDM_M), or 0: serial path
   int nblk;         // blocks per column (jtot / blk)
@@ -118,7 +119,8 @@ struct eif_ctx {
   int *owner;                   // owner particle of every chunk (mixed form)
   // device scalars
   double *d_scal;               // [0] dt, [1] residual, [2] scratch
-  float *d_coef;                // single-precision dt products: [3*rk+0..2] alpha/beta/gamma*dt, [9] 1/dt
+  float *d_coef;                // single-precision dt products: [3*rk+0..2] alpha/beta/gamma*dt, [9] 1/dt,
+                                // [12+2*rk], [13+2*rk]: 1/(gamma dt) as a float pair
   unsigned *d_flags;
   double *h_scal;               // pinned mirror
   unsigned *h_flags;

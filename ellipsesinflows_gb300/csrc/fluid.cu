@@ -351,6 +351,12 @@ __device__ __forceinline__ void write_coef(double dt, float *coef) {
     coef[3 * rk + 2] = (float)((al[rk] + be[rk]) * dt);
   }
   coef[9] = (float)(1. / dt);
+  for (int rk = 0; rk < 3; rk++) {
+    const double inv = 1. / ((al[rk] + be[rk]) * dt);
+    const float hi = (float)inv;
+    coef[12 + 2 * rk] = hi;
+    coef[13 + 2 * rk] = (float)(inv - (double)hi);
+  }
 }
 
 // dt from the maxima (decide_dt.c:25-80): one block.

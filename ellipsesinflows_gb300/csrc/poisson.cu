@@ -343,6 +343,244 @@ __global__ void __launch_bounds__(256) k_dct3(Dct3Args a) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Double-float arithmetic for the mixed-precision form: a value is the
+// unevaluated sum hi + lo of two floats (about 48 significant bits), combined
+// with the error-free transformations of Knuth (TwoSum), Dekker (Fast2Sum) and
+// an FMA-based product (Ogita, Rump and Oishi, "Accurate sum and dot product",
+// SIAM J. Sci. Comput. 26, 2005). Only the FP32 pipe is used.
+struct DF { float hi, lo; };
+struct CDF { DF re, im; };
+
+__device__ __forceinline__ DF two_sum(float a, float b) {
+  const float s = a + b;
+  const float bb = s - a;
+  return DF{s, (a - (s - bb)) + (b - bb)};
+}
+__device__ __forceinline__ DF fast_sum(float a, float b) {  // requires |a| >= |b| or a == 0
+  const float s = a + b;
+  return DF{s, b - (s - a)};
+}
+__device__ __forceinline__ DF df_add(DF x, DF y) {
+  DF s = two_sum(x.hi, y.hi);
+  const DF t = two_sum(x.lo, y.lo);
+  s = fast_sum(s.hi, s.lo + t.hi);
+  return fast_sum(s.hi, s.lo + t.lo);
+}
+__device__ __forceinline__ DF df_neg(DF x) { return DF{-x.hi, -x.lo}; }
+__device__ __forceinline__ DF df_sub(DF x, DF y) { return df_add(x, df_neg(y)); }
+__device__ __forceinline__ DF df_mul(DF x, DF y) {
+  const float p = x.hi * y.hi;
+  float e = fmaf(x.hi, y.hi, -p);
+  e = fmaf(x.hi, y.lo, fmaf(x.lo, y.hi, e));
+  return fast_sum(p, e);
+}
+__device__ __forceinline__ DF df_scale(DF x, float pow2) { return DF{x.hi * pow2, x.lo * pow2}; }
+__device__ __forceinline__ DF df_of(double v) {
+  const float2 t = eifd::split(v);
+  return fast_sum(t.x, t.y);
+}
+__device__ __forceinline__ double df_to_double(DF x) { return eifd::f2d(x.hi) + eifd::f2d(x.lo); }
+
+__device__ __forceinline__ CDF cdf_add(CDF a, CDF b) { return CDF{df_add(a.re, b.re), df_add(a.im, b.im)}; }
+__device__ __forceinline__ CDF cdf_sub(CDF a, CDF b) { return CDF{df_sub(a.re, b.re), df_sub(a.im, b.im)}; }
+__device__ __forceinline__ CDF cdf_mul(CDF a, CDF b) {
+  return CDF{df_sub(df_mul(a.re, b.re), df_mul(a.im, b.im)), df_add(df_mul(a.re, b.im), df_mul(a.im, b.re))};
+}
+__device__ __forceinline__ CDF cdf_conj(CDF a) { return CDF{a.re, df_neg(a.im)}; }
+__device__ __forceinline__ CDF cdf_mul_i(CDF a, int sign) {
+  return sign > 0 ? CDF{df_neg(a.im), a.re} : CDF{a.im, df_neg(a.re)};
+}
+__device__ __forceinline__ CDF cdf_load(const float4 *t, int k) {
+  const float4 v = __ldg(t + k);
+  return CDF{DF{v.x, v.y}, DF{v.z, v.w}};
+}
+
+// double-float version of fft_smem (same Stockham radix-4/2/3 schedule)
+__device__ CDF *fft_smem_df(CDF *x, CDF *y, const FftDesc &d, const float4 *__restrict__ tw, int sign) {
+  const int m = d.m;
+  int L = 1;
+  for (int s = 0; s < d.nfac; s++) {
+    const int R = d.fac[s];
+    const int Ls = L * R;
+    const int nb = m / R;
+    const int tws = m / Ls;
+    for (int j = threadIdx.x; j < nb; j += blockDim.x) {
+      const int k = j % L;
+      const int blk = j / L;
+      CDF a[4];
+#pragma unroll
+      for (int r = 0; r < 4; r++) {
+        if (r < R) {
+          CDF v = x[j + r * nb];
+          if (r > 0 && k > 0) {
+            CDF w = cdf_load(tw, r * k * tws);
+            if (sign > 0) w = cdf_conj(w);
+            v = cdf_mul(v, w);
+          }
+          a[r] = v;
+        }
+      }
+      const int o = blk * Ls + k;
+      if (R == 4) {
+        const CDF s02 = cdf_add(a[0], a[2]), d02 = cdf_sub(a[0], a[2]);
+        const CDF s13 = cdf_add(a[1], a[3]), d13 = cdf_mul_i(cdf_sub(a[1], a[3]), sign);
+        y[o] = cdf_add(s02, s13);
+        y[o + L] = cdf_add(d02, d13);
+        y[o + 2 * L] = cdf_sub(s02, s13);
+        y[o + 3 * L] = cdf_sub(d02, d13);
+      } else if (R == 2) {
+        y[o] = cdf_add(a[0], a[1]);
+        y[o + L] = cdf_sub(a[0], a[1]);
+      } else {  // R == 3: w = -1/2 + i sign sqrt(3)/2
+        const CDF t = cdf_add(a[1], a[2]);
+        const CDF u = cdf_sub(a[1], a[2]);
+        const CDF base = cdf_sub(a[0], CDF{df_scale(t.re, 0.5f), df_scale(t.im, 0.5f)});
+        const DF s3 = DF{0.8660253882408142f, 1.5543625053737742e-08f};  // sqrt(3)/2 as a float pair
+        const DF ss = sign > 0 ? s3 : df_neg(s3);
+        const CDF rot = CDF{df_neg(df_mul(ss, u.im)), df_mul(ss, u.re)};
+        y[o] = cdf_add(a[0], t);
+        y[o + L] = cdf_add(base, rot);
+        y[o + 2 * L] = cdf_sub(base, rot);
+      }
+    }
+    __syncthreads();
+    CDF *t = x;
+    x = y;
+    y = t;
+    L = Ls;
+  }
+  return x;
+}
+
+struct Dct2ArgsDF {
+  const double *ux, *uy, *dux, *duy;
+  const float *coef;   // [12 + 2 rk] = hi, lo of 1/(gamma dt)
+  double *qhat;
+  const float4 *tw, *rot, *wn;
+  FftDesc fd;
+  DF rdx, rdy;
+  int itot, jtot, ld, with_ibm, rk;
+};
+
+// RHS + DCT-II of one row in double-float arithmetic (compute_potential.c:70-92)
+__global__ void __launch_bounds__(256) k_dct2_df(Dct2ArgsDF a) {
+  extern __shared__ CDF smd[];
+  const int n = a.itot, m = n / 2, ld = a.ld;
+  DF *q = reinterpret_cast<DF *>(smd + 2 * m);
+  const int j = 1 + blockIdx.x;
+  const DF inv = DF{__ldg(a.coef + 12 + 2 * a.rk), __ldg(a.coef + 13 + 2 * a.rk)};
+  for (int i = 1 + threadIdx.x; i <= n; i += blockDim.x) {
+    DF uxm = df_of(__ldg(a.ux + ux_idx(i, j, ld))), uxp = df_of(__ldg(a.ux + ux_idx(i + 1, j, ld)));
+    DF uym = df_of(__ldg(a.uy + uy_idx(i, j, ld))), uyp = df_of(__ldg(a.uy + uy_idx(i, j + 1, ld)));
+    if (a.with_ibm) {
+      const int c = uy_idx(i, j, ld);
+      const DF dw = df_of(__ldg(a.dux + c - 1)), d0 = df_of(__ldg(a.dux + c)), de = df_of(__ldg(a.dux + c + 1));
+      if (i >= 2) uxm = df_add(uxm, df_scale(df_add(dw, d0), 0.5f));
+      if (i + 1 <= n) uxp = df_add(uxp, df_scale(df_add(d0, de), 0.5f));
+      const DF ds = df_of(__ldg(a.duy + c - ld)), e0 = df_of(__ldg(a.duy + c)), en = df_of(__ldg(a.duy + c + ld));
+      uym = df_add(uym, df_scale(df_add(ds, e0), 0.5f));
+      uyp = df_add(uyp, df_scale(df_add(e0, en), 0.5f));
+    }
+    q[i - 1] = df_mul(inv, df_add(df_mul(df_sub(uxp, uxm), a.rdx), df_mul(df_sub(uyp, uym), a.rdy)));
+  }
+  __syncthreads();
+  CDF *x = smd, *y = smd + m;
+  for (int s = threadIdx.x; s < m; s += blockDim.x) {
+    const int t0 = 2 * s, t1 = 2 * s + 1;
+    const DF v0 = t0 < m ? q[2 * t0] : q[2 * (n - 1 - t0) + 1];
+    const DF v1 = t1 < m ? q[2 * t1] : q[2 * (n - 1 - t1) + 1];
+    x[s] = CDF{v0, v1};
+  }
+  __syncthreads();
+  const CDF *Z = fft_smem_df(x, y, a.fd, a.tw, -1);
+  double *out = a.qhat + (size_t)(j - 1) * ld;
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    const int kk = k <= m ? k : n - k;
+    const CDF zk = Z[kk % m];
+    const CDF zm = cdf_conj(Z[(m - kk) % m]);
+    const CDF sm = cdf_add(zk, zm), df = cdf_sub(zk, zm);
+    const CDF e = CDF{df_scale(sm.re, 0.5f), df_scale(sm.im, 0.5f)};
+    const CDF o = CDF{df_scale(df.im, 0.5f), df_scale(df_neg(df.re), 0.5f)};  // (zk - zm) / 2i
+    CDF v = cdf_add(e, cdf_mul(cdf_load(a.wn, kk), o));
+    if (k > m) v = cdf_conj(v);
+    const CDF r = cdf_load(a.rot, k);
+    const DF re = df_sub(df_mul(r.re, v.re), df_mul(r.im, v.im));
+    out[k] = df_to_double(df_scale(re, 2.f));
+  }
+}
+
+struct Dct3ArgsDF {
+  const double *qhat, *iface, *g;
+  double *psi;
+  const float4 *tw, *rot, *wn;
+  FftDesc fd;
+  DF scale;   // 1 / (2 itot)
+  int itot, jtot, ld, blk, nblk;
+};
+
+// block reconstruction + DCT-III + scaling of one row, double-float arithmetic
+__global__ void __launch_bounds__(256) k_dct3_df(Dct3ArgsDF a) {
+  extern __shared__ CDF smd[];
+  const int n = a.itot, m = n / 2, ld = a.ld;
+  DF *xr = reinterpret_cast<DF *>(smd + 2 * m);
+  const int j = 1 + blockIdx.x;
+  const int jr = j - 1;
+  const double *row = a.qhat + (size_t)jr * ld;
+  if (a.blk > 0) {
+    const int M = a.blk;
+    const int b = jr / M, r = jr % M;
+    const int bm = (b + a.nblk - 1) % a.nblk;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+      DF v;
+      if (r == M - 1) {
+        v = df_of(__ldg(a.iface + (size_t)b * n + k));
+      } else {
+        // y + s_left g + s_right h in double-float from the double-precision block solution
+        const DF gl = df_of(__ldg(a.g + (size_t)r * n + k));
+        const DF gr = df_of(__ldg(a.g + (size_t)(M - 2 - r) * n + k));
+        v = df_add(df_add(df_of(__ldg(row + k)), df_mul(df_of(__ldg(a.iface + (size_t)bm * n + k)), gl)),
+                   df_mul(df_of(__ldg(a.iface + (size_t)b * n + k)), gr));
+      }
+      xr[k] = v;
+    }
+  } else {
+    for (int k = threadIdx.x; k < n; k += blockDim.x) xr[k] = df_of(__ldg(row + k));
+  }
+  __syncthreads();
+  CDF *x = smd, *y = smd + m;
+  for (int s = threadIdx.x; s < m; s += blockDim.x) {
+    const int t0 = s, t1 = s + m;
+    const CDF r0 = cdf_conj(cdf_load(a.rot, t0)), r1 = cdf_conj(cdf_load(a.rot, t1));
+    const CDF w0 = cdf_mul(r0, CDF{xr[t0], t0 == 0 ? DF{0.f, 0.f} : df_neg(xr[n - t0])});
+    const CDF w1 = cdf_mul(r1, CDF{xr[t1], df_neg(xr[n - t1])});
+    const CDF sum = cdf_add(w0, w1);
+    const CDF dif = cdf_mul(cdf_sub(w0, w1), cdf_conj(cdf_load(a.wn, s)));
+    x[s] = CDF{df_sub(sum.re, dif.im), df_add(sum.im, dif.re)};
+  }
+  __syncthreads();
+  const CDF *z = fft_smem_df(x, y, a.fd, a.tw, +1);
+  double *prow = a.psi + (size_t)j * ld;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const int t = (i & 1) ? n - 1 - (i >> 1) : (i >> 1);
+    const DF w = (t & 1) ? z[t >> 1].im : z[t >> 1].re;
+    const double v = df_to_double(df_mul(w, a.scale));
+    prow[i + 1] = v;
+    if (j == 1) a.psi[(size_t)(a.jtot + 1) * ld + i + 1] = v;
+    if (j == a.jtot) a.psi[i + 1] = v;
+    if (i == 0) {
+      prow[0] = v;
+      if (j == 1) a.psi[(size_t)(a.jtot + 1) * ld] = v;
+      if (j == a.jtot) a.psi[0] = v;
+    }
+    if (i == n - 1) {
+      prow[n + 1] = v;
+      if (j == 1) a.psi[(size_t)(a.jtot + 1) * ld + n + 1] = v;
+      if (j == a.jtot) a.psi[n + 1] = v;
+    }
+  }
+}
+
 bool factorize(int m, int *fac, int *nfac) {
   int k = 0;
   while (m % 4 == 0) { fac[k++] = 4; m /= 4; }
@@ -411,6 +649,26 @@ int poisson_init(eif_ctx *c) {
     return cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice);
   };
   EIF_CK(c, up_load((void **)&pp.tw, tw.data(), sizeof(double2) * pp.m));
+  {
+    // the same twiddles as float pairs for the double-float (mixed-precision) transforms
+    auto pair = [&](long double t) {
+      const float hi = (float)t;
+      return std::make_pair(hi, (float)(t - (long double)hi));
+    };
+    auto df_table = [&](int len, long double step, float4 **dst) -> int {
+      std::vector<float4> v(len);
+      for (int k = 0; k < len; k++) {
+        const auto re = pair(cosl(step * k)), im = pair(sinl(step * k));
+        v[k] = make_float4(re.first, re.second, im.first, im.second);
+      }
+      EIF_CK(c, up_load((void **)dst, v.data(), sizeof(float4) * len));
+      return EIF_OK;
+    };
+    int rc;
+    if ((rc = df_table(pp.m, -2.L * PI / pp.m, &pp.tw_f))) return rc;
+    if ((rc = df_table(n, -PI / (2.L * n), &pp.rot_f))) return rc;
+    if ((rc = df_table(n, -2.L * PI / n, &pp.wn_f))) return rc;
+  }
   EIF_CK(c, up_load((void **)&pp.rot, rot.data(), sizeof(double2) * n));
   EIF_CK(c, up_load((void **)&pp.wn, wn.data(), sizeof(double2) * n));
   EIF_CK(c, up_load((void **)&pp.lam, lam.data(), sizeof(double) * n));
@@ -463,13 +721,15 @@ int poisson_init(eif_ctx *c) {
   if (smem > 48 * 1024) {
     EIF_CK(c, cudaFuncSetAttribute(k_dct2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     EIF_CK(c, cudaFuncSetAttribute(k_dct3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    EIF_CK(c, cudaFuncSetAttribute(k_dct2_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    EIF_CK(c, cudaFuncSetAttribute(k_dct3_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   }
   return EIF_OK;
 }
 
 void poisson_free(eif_ctx *c) {
   PoissonPlan &pp = c->pp;
-  void *ptrs[] = {pp.tw, pp.rot, pp.wn, pp.lam, pp.tdm_inv, pp.tdm_up, pp.tdm_g,
+  void *ptrs[] = {pp.tw, pp.rot, pp.wn, pp.tw_f, pp.rot_f, pp.wn_f, pp.lam, pp.tdm_inv, pp.tdm_up, pp.tdm_g,
                   pp.red_inv, pp.red_up, pp.red_q1, pp.red_coef, pp.ywork};
   for (void *p : ptrs) if (p) cudaFree(p);
   pp = PoissonPlan{};
@@ -486,7 +746,24 @@ int launch_potential(eif_ctx *c, int rk, bool with_ibm) {
   for (int s = 0; s < 16; s++) fd.fac[s] = pp.fac[s];
   const size_t smem = sizeof(double2) * 2 * pp.m + sizeof(double) * n;
   const int thr = fft_threads(pp.m);
-  {
+  const bool mixed = c->cfg.precision == EIF_PREC_MIXED;
+  auto dfpair = [](double v) {
+    const float hi = (float)v;
+    return DF{hi, (float)(v - (double)hi)};
+  };
+  if (mixed) {
+    Dct2ArgsDF a;
+    a.ux = c->ux[c->cur]; a.uy = c->uy[c->cur];
+    a.dux = c->dux; a.duy = c->duy; a.coef = c->d_coef;
+    a.qhat = c->qhat;
+    a.tw = pp.tw_f; a.rot = pp.rot_f; a.wn = pp.wn_f;
+    a.fd = fd;
+    a.rdx = dfpair(1. / c->dx); a.rdy = dfpair(1. / c->dy);
+    a.itot = n; a.jtot = jt; a.ld = c->ld; a.with_ibm = with_ibm ? 1 : 0; a.rk = rk;
+    EIF_PROF(c, "poisson_dct2", 1);
+    k_dct2_df<<<jt, thr, smem, c->stream>>>(a);
+    EIF_LAUNCH_CK(c);
+  } else {
     Dct2Args a;
     a.ux = c->ux[c->cur]; a.uy = c->uy[c->cur];
     a.dux = c->dux; a.duy = c->duy; a.dt = c->d_scal;
@@ -522,7 +799,18 @@ int launch_potential(eif_ctx *c, int rk, bool with_ibm) {
     k_tdm_serial<<<(n + 63) / 64, 64, 0, c->stream>>>(c->qhat, pp.ywork, pp.lam, l, n, jt, c->ld);
     EIF_LAUNCH_CK(c);
   }
-  {
+  if (mixed) {
+    Dct3ArgsDF a;
+    a.qhat = c->qhat; a.iface = iface; a.g = pp.tdm_g;
+    a.psi = c->psi;
+    a.tw = pp.tw_f; a.rot = pp.rot_f; a.wn = pp.wn_f;
+    a.fd = fd;
+    a.scale = dfpair(1. / (2. * n));
+    a.itot = n; a.jtot = jt; a.ld = c->ld; a.blk = pp.blk; a.nblk = pp.nblk;
+    EIF_PROF(c, "poisson_dct3", 1);
+    k_dct3_df<<<jt, thr, smem, c->stream>>>(a);
+    EIF_LAUNCH_CK(c);
+  } else {
     Dct3Args a;
     a.qhat = c->qhat; a.iface = iface; a.g = pp.tdm_g;
     a.psi = c->psi;
