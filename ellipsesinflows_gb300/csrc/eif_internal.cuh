@@ -117,6 +117,8 @@ struct eif_ctx {
   int chunk_cap;                // capacity of partial in chunks
   float *pf;                    // per-particle single-precision parameters (mixed form)
   int *owner;                   // owner particle of every chunk (mixed form)
+  int *band_lists, *band_counts;// ordered (particle, image) lists per band of gather rows
+  int band_cap;
   // device scalars
   double *d_scal;               // [0] dt, [1] residual, [2] scratch
   float *d_coef;                // single-precision dt products: [3*rk+0..2] alpha/beta/gamma*dt, [9] 1/dt,

@@ -36,7 +36,7 @@ constexpr int CHUNK = 64;       // cells per warp task
 constexpr int NEXTRA = 3;       // auxiliary.c:8
 constexpr double BETA = 2.;     // auxiliary.c:49
 constexpr int GTX = 64, GTY = 8, GTHREADS = 256;  // gather tile and block
-constexpr int LMAX = 1024;      // list capacity of one gather tile
+constexpr int LMAX = 256;       // gather entries staged in shared memory at a time
 
 // per-particle geometry needed by a box cell evaluation
 struct Ell {
@@ -94,6 +94,29 @@ __device__ __forceinline__ double signed_dist(const Ell &e, double x, double y, 
   const double dxx = e.a * ct - x_, dyy = e.b * st - y_;
   return sign * sqrt(dxx * dxx + dyy * dyy) * rh;
 }
+
+// Cells far from the interface. With rho = sqrt((x/a)^2 + (y/b)^2) (the gauge of
+// the ellipse, Lipschitz with constant 1/min(a,b)) the distance to the boundary is
+// at least min(a,b) |rho - 1|, and at least r - max(a,b) outside / min(a,b) - r
+// inside (r = |(x, y)|). When that bound times 2/h reaches the value at which
+// tanh rounds to +-1 in the working precision, the weights are exactly those of
+// the saturated tanh and the normal-foot iteration is not needed. Returns 0 for
+// a near cell, +1 for a far interior cell, -1 for a far exterior cell.
+__device__ __forceinline__ int far_side(double x_, double y_, double a, double b, double min_dist) {
+  const double mn = fmin(a, b), mx = fmax(a, b);
+  const double rho2 = (x_ / a) * (x_ / a) + (y_ / b) * (y_ / b);
+  const double rho = sqrt(rho2);
+  const double r = sqrt(x_ * x_ + y_ * y_);
+  if (rho > 1.) {
+    return fmax(mn * (rho - 1.), r - mx) >= min_dist ? -1 : 0;
+  }
+  return fmax(mn * (1. - rho), mn - r) >= min_dist ? 1 : 0;
+}
+
+// double-precision tanh(2d) equals +-1 exactly for |2d| >= 20 (the correction
+// 2/(exp(2|x|)+1) is below half an ulp of 1); with a margin for rounding of the bound
+constexpr double FAR_CELLS_D = 10.5;
+constexpr float FAR_CELLS_F = 5.f;
 
 // auxiliary.c:11-17
 __device__ __forceinline__ void loop_size(int lb, int ub, double h, double r, double gc, int &mn, int &mx) {
@@ -318,8 +341,19 @@ __global__ void __launch_bounds__(256) k_ibm_work(WorkArgs a) {
         Ell e = e0;
         e.py = py_;
         const double x = __ldg(a.xc + i), y = __ldg(a.yc + j);
-        const double d = signed_dist(e, x, y, rh);
-        const double th = tanh(BETA * d);
+        double th;
+        {
+          const double ddx = x - e.px, ddy = y - e.py;
+          const double x_ = e.cz * ddx - e.sz * ddy;
+          const double y_ = e.sz * ddx + e.cz * ddy;
+          const int side = far_side(x_, y_, e.a, e.b, FAR_CELLS_D * a.h);
+          if (side != 0) {
+            // reference sign convention: +1 inside (auxiliary.c:36-38); tanh saturated
+            th = (double)side;
+          } else {
+            th = tanh(BETA * signed_dist(e, x, y, rh));
+          }
+        }
         const double uxf = 0.5 * (__ldg(a.ux + j * ld + (i - 1)) + __ldg(a.ux + j * ld + i));
         const double uyf = 0.5 * (__ldg(a.uy + j * ld + i) + __ldg(a.uy + (j + 1) * ld + i));
         if (a.mode == 0) {
@@ -398,6 +432,14 @@ __device__ __forceinline__ float normal_t_f(const EllF &e, float x_, float y_) {
 }
 
 // signed distance in grid units from the offset (X, Y) = (x - px, y - py)
+__device__ __forceinline__ int far_side_f(float x_, float y_, float a, float b, float min_dist) {
+  const float mn = fminf(a, b), mx = fmaxf(a, b);
+  const float rho = sqrtf((x_ / a) * (x_ / a) + (y_ / b) * (y_ / b));
+  const float r = sqrtf(x_ * x_ + y_ * y_);
+  if (rho > 1.f) return fmaxf(mn * (rho - 1.f), r - mx) >= min_dist ? -1 : 0;
+  return fmaxf(mn * (1.f - rho), mn - r) >= min_dist ? 1 : 0;
+}
+
 __device__ __forceinline__ float signed_dist_f(const EllF &e, float X, float Y, float rh) {
   const float x_ = e.cz * X - e.sz * Y;
   const float y_ = e.sz * X + e.cz * Y;
@@ -451,8 +493,13 @@ __global__ void __launch_bounds__(256) k_ibm_work_f(WorkArgs a) {
         const int m = img + 1;
         const float X = ((float)(i - i0) - gx) * dxf;
         const float Y = ((float)(j - j0s[m]) - gys[m]) * dyf;
-        const float d = signed_dist_f(e, X, Y, rh);
-        const float th = tanhf(2.f * d);
+        float th;
+        {
+          const float x_ = e.cz * X - e.sz * Y;
+          const float y_ = e.sz * X + e.cz * Y;
+          const int side = far_side_f(x_, y_, e.a, e.b, FAR_CELLS_F / rh);
+          th = side != 0 ? (float)side : tanhf(2.f * signed_dist_f(e, X, Y, rh));
+        }
         const float uxs = eifd::d2f(__ldg(a.ux + j * ld + (i - 1))) + eifd::d2f(__ldg(a.ux + j * ld + i));
         const float uys = eifd::d2f(__ldg(a.uy + j * ld + i)) + eifd::d2f(__ldg(a.uy + (j + 1) * ld + i));
         if (a.mode == 0) {
@@ -517,8 +564,51 @@ __global__ void k_chunk_reduce(const double *__restrict__ partial, const int *__
   }
 }
 
+// Ordered lists of the (particle, image) boxes that reach each band of GTY rows,
+// built once per exchange; entry = 3 * particle + image index, in particle order.
+__global__ void k_band_lists(const int *__restrict__ box, int np, int jtot, int *__restrict__ lists,
+                             int *__restrict__ counts, int cap, unsigned *__restrict__ flags) {
+  const int lane = threadIdx.x & 31;
+  const int band = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nbands = (jtot + GTY - 1) / GTY;
+  if (band >= nbands) return;
+  const int j0 = 1 + band * GTY, j1 = min(j0 + GTY - 1, jtot);
+  int count = 0;
+  int *out = lists + (size_t)band * cap;
+  for (int base = 0; base < np; base += 32) {
+    const int n = base + lane;
+    int bits = 0;
+    if (n < np) {
+      for (int q = 0; q < 3; q++) {
+        const int *bx = box + 12 * n + 4 * q;
+        if (bx[1] >= bx[0] && bx[3] >= bx[2] && bx[2] <= j1 && bx[3] >= j0) bits |= 1 << q;
+      }
+    }
+    const int m = __popc(bits);
+    int sc = m;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, sc, o);
+      if (lane >= o) sc += v;
+    }
+    int pos = count + sc - m;
+    for (int q = 0; q < 3; q++) {
+      if (bits & (1 << q)) {
+        if (pos < cap) out[pos] = 3 * n + q;
+        pos++;
+      }
+    }
+    count += __shfl_sync(0xffffffffu, sc, 31);
+  }
+  if (lane == 0) {
+    counts[band] = count;
+    if (count > cap) atomicOr(flags, EIF_FLAG_NOCONV);
+  }
+}
+
 struct GatherArgs {
   const int *box, *off;
+  const int *lists, *counts;
+  int cap;
   const void *wbuf;
   double *dux, *duy;
   unsigned *flags;
@@ -534,92 +624,42 @@ __device__ __forceinline__ double to_double(float v) { return eifd::f2d(v); }
 template <typename V2, typename Acc>
 __global__ void __launch_bounds__(GTHREADS) k_gather(GatherArgs a) {
   const V2 *wbuf = static_cast<const V2 *>(a.wbuf);
-  __shared__ int list[LMAX];
-  __shared__ int cnt[1024 / 32 + 1];
-  __shared__ int nlist;
+  // per staged entry: columns, rows, row width and offset of the box in the scratch buffer
+  __shared__ int e_i0[LMAX], e_i1[LMAX], e_j0[LMAX], e_j1[LMAX], e_w[LMAX], e_base[LMAX];
   const int i0 = 1 + blockIdx.x * GTX, j0 = 1 + blockIdx.y * GTY;
   const int i1 = min(i0 + GTX - 1, a.itot), j1 = min(j0 + GTY - 1, a.jtot);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = GTHREADS / 32;
-  const int ngroups = (a.np + 31) / 32;
   Acc acc_x[2] = {0, 0}, acc_y[2] = {0, 0};
   // cells of this thread: (i0 + lx, j0 + ly) for two rows
   const int lx = threadIdx.x % GTX, ly0 = threadIdx.x / GTX;  // GTHREADS / GTX = 4 rows per pass
-  for (int gbase = 0; gbase < ngroups; gbase += 32) {
-    // phase 1: count covering images per particle group
-    unsigned masks_dummy = 0;
-    (void)masks_dummy;
-    for (int g = gbase + warp; g < min(gbase + 32, ngroups); g += nw) {
-      const int n = g * 32 + lane;
-      int m = 0;
-      if (n < a.np) {
-        for (int q = 0; q < 3; q++) {
-          const int *bx = a.box + 12 * n + 4 * q;
-          if (bx[0] <= i1 && bx[1] >= i0 && bx[2] <= j1 && bx[3] >= j0 && bx[1] >= bx[0] && bx[3] >= bx[2]) m++;
+  // the band's ordered list of boxes; keep those that also reach this tile's columns
+  const int band = blockIdx.y;
+  const int L = min(__ldg(a.counts + band), a.cap);
+  const int *blist = a.lists + (size_t)band * a.cap;
+  for (int base = 0; base < L; base += LMAX) {
+    const int cnt = min(LMAX, L - base);
+    for (int e = threadIdx.x; e < cnt; e += GTHREADS) {
+      const int ent = __ldg(blist + base + e);
+      const int n = ent / 3, q = ent % 3;
+      int bi0 = 1, bi1 = 0, bj0 = 1, bj1 = 0, off = 0;
+      if (EIF_CHK(a.bd.rec, n, a.np, 44) && EIF_CHK(a.bd.rec, 12LL * n + 11, a.bd.box, 45)) {
+        const int *bx = a.box + 12 * n;
+        int base_q = 0;
+        for (int m = 0; m < q; m++) {
+          const int w = bx[4 * m + 1] - bx[4 * m] + 1, h = bx[4 * m + 3] - bx[4 * m + 2] + 1;
+          if (w > 0 && h > 0) base_q += w * h;
         }
+        bi0 = bx[4 * q]; bi1 = bx[4 * q + 1]; bj0 = bx[4 * q + 2]; bj1 = bx[4 * q + 3];
+        off = __ldg(a.off + n) * CHUNK + base_q;
       }
-      // inclusive warp scan of m
-      int s = m;
-      for (int o = 1; o < 32; o <<= 1) {
-        const int v = __shfl_up_sync(0xffffffffu, s, o);
-        if (lane >= o) s += v;
-      }
-      if (lane == 31) cnt[g - gbase] = s;
+      // entries that miss this tile's columns are kept (as empty) to preserve the order
+      if (bi0 > i1 || bi1 < i0) { bi0 = 1; bi1 = 0; }
+      e_i0[e] = bi0; e_i1[e] = bi1; e_j0[e] = bj0; e_j1[e] = bj1; e_w[e] = bi1 - bi0 + 1; e_base[e] = off;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-      int tot = 0;
-      for (int g = 0; g < min(32, ngroups - gbase); g++) {
-        const int v = cnt[g];
-        cnt[g] = tot;
-        tot += v;
-      }
-      nlist = tot;
-    }
-    __syncthreads();
-    const int L = nlist;
-    if (!EIF_CHK(a.bd.rec, L, LMAX + 1, 46)) return;
-    if (L > LMAX) {
-      if (threadIdx.x == 0) atomicOr(a.flags, EIF_FLAG_NOCONV);
-      return;
-    }
-    // phase 2: ordered fill
-    for (int g = gbase + warp; g < min(gbase + 32, ngroups); g += nw) {
-      const int n = g * 32 + lane;
-      int m = 0, bits = 0;
-      if (n < a.np) {
-        for (int q = 0; q < 3; q++) {
-          const int *bx = a.box + 12 * n + 4 * q;
-          if (bx[0] <= i1 && bx[1] >= i0 && bx[2] <= j1 && bx[3] >= j0 && bx[1] >= bx[0] && bx[3] >= bx[2]) {
-            bits |= 1 << q;
-            m++;
-          }
-        }
-      }
-      int s = m;
-      for (int o = 1; o < 32; o <<= 1) {
-        const int v = __shfl_up_sync(0xffffffffu, s, o);
-        if (lane >= o) s += v;
-      }
-      int pos = cnt[g - gbase] + s - m;
-      for (int q = 0; q < 3; q++) {
-        if ((bits & (1 << q)) && EIF_CHK(a.bd.rec, pos, LMAX, 40)) list[pos++] = 3 * n + q;
-      }
-    }
-    __syncthreads();
-    // phase 3: accumulate in list order
-    for (int e = 0; e < L; e++) {
-      const int n = list[e] / 3, q = list[e] % 3;
-      if (!EIF_CHK(a.bd.rec, n, a.np, 44) || !EIF_CHK(a.bd.rec, 12LL * n + 11, a.bd.box, 45)) continue;
-      const int *bx = a.box + 12 * n;
-      // offset of image q within the particle's enumeration
-      int base = 0;
-      for (int m = 0; m < q; m++) {
-        const int w = bx[4 * m + 1] - bx[4 * m] + 1, h = bx[4 * m + 3] - bx[4 * m + 2] + 1;
-        if (w > 0 && h > 0) base += w * h;
-      }
-      const int bi0 = bx[4 * q], bi1 = bx[4 * q + 1], bj0 = bx[4 * q + 2], bj1 = bx[4 * q + 3];
-      const int w = bi1 - bi0 + 1;
-      const size_t pbase = (size_t)__ldg(a.off + n) * CHUNK + base;
+    for (int e = 0; e < cnt; e++) {
+      const int bi0 = e_i0[e], bi1 = e_i1[e], bj0 = e_j0[e], bj1 = e_j1[e], w = e_w[e];
+      if (bi1 < bi0) continue;
+      const size_t pbase = (size_t)e_base[e];
 #pragma unroll
       for (int r = 0; r < 2; r++) {
         const int i = i0 + lx, j = j0 + ly0 + 4 * r;
@@ -699,6 +739,10 @@ int ibm_reserve(eif_ctx *c) {
   EIF_CK(c, cudaMalloc((void **)&c->wbuf, sizeof(double2) * c->wcap));
   EIF_CK(c, cudaMalloc((void **)&c->pf, sizeof(float) * PF_WORDS * c->np));
   EIF_CK(c, cudaMalloc((void **)&c->owner, sizeof(int) * (size_t)chunks));
+  const int nbands = (c->jtot + GTY - 1) / GTY;
+  c->band_cap = 3 * c->np;
+  EIF_CK(c, cudaMalloc((void **)&c->band_lists, sizeof(int) * (size_t)nbands * c->band_cap));
+  EIF_CK(c, cudaMalloc((void **)&c->band_counts, sizeof(int) * (size_t)nbands));
   return EIF_OK;
 }
 
@@ -709,6 +753,9 @@ void ibm_free(eif_ctx *c) {
   if (c->wbuf) cudaFree(c->wbuf);
   if (c->pf) cudaFree(c->pf);
   if (c->owner) cudaFree(c->owner);
+  if (c->band_lists) cudaFree(c->band_lists);
+  if (c->band_counts) cudaFree(c->band_counts);
+  c->band_lists = nullptr; c->band_counts = nullptr;
   c->box = nullptr; c->chunk_off = nullptr; c->partial = nullptr; c->wbuf = nullptr;
   c->pf = nullptr; c->owner = nullptr;
   c->chunk_cap = 0; c->wcap = 0;
@@ -809,6 +856,14 @@ int launch_exchange(eif_ctx *c) {
   g.dux = c->dux; g.duy = c->duy; g.flags = c->d_flags;
   g.np = c->np; g.itot = c->itot; g.jtot = c->jtot; g.ld = c->ld;
   g.bd = bounds_of(c);
+  g.lists = c->band_lists; g.counts = c->band_counts; g.cap = c->band_cap;
+  {
+    const int nbands = (c->jtot + GTY - 1) / GTY;
+    EIF_PROF(c, "ibm_band_lists", 1);
+    k_band_lists<<<(nbands * 32 + 255) / 256, 256, 0, c->stream>>>(c->box, c->np, c->jtot, c->band_lists,
+                                                                     c->band_counts, c->band_cap, c->d_flags);
+    EIF_LAUNCH_CK(c);
+  }
   dim3 grid((c->itot + GTX - 1) / GTX, (c->jtot + GTY - 1) / GTY);
   EIF_PROF(c, "ibm_gather", 1);
   if (c->cfg.precision == EIF_PREC_MIXED) {

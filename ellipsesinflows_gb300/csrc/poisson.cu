@@ -196,39 +196,50 @@ __global__ void __launch_bounds__(256) k_tdm_local(double *__restrict__ qhat, co
   first[(size_t)b * itot + k] = v[0];
 }
 
-// cyclic system of the interface values of one wavenumber
-__global__ void k_tdm_reduced(double *__restrict__ iface, const double *__restrict__ first,
-                              const double *__restrict__ rinv, const double *__restrict__ rup,
-                              const double *__restrict__ rq1, const double *__restrict__ rcoef, double l, int itot,
-                              int nblk) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= itot) return;
+// cyclic system of the interface values of one wavenumber. One thread per
+// wavenumber, 32 wavenumbers per block; each thread keeps its column of right-
+// hand sides in shared memory, so the serial sweeps run at shared-memory
+// latency rather than one L2 round trip per step.
+constexpr int RED_COLS = 32;
+
+__global__ void __launch_bounds__(RED_COLS) k_tdm_reduced(double *__restrict__ iface, const double *__restrict__ first,
+                                                          const double *__restrict__ rinv, const double *__restrict__ rup,
+                                                          const double *__restrict__ rq1, const double *__restrict__ rcoef,
+                                                          double l, int itot, int nblk) {
+  extern __shared__ double zs[];  // [nblk][RED_COLS]
+  const int t = threadIdx.x;
+  const int k = blockIdx.x * RED_COLS + t;
+  const bool on = k < itot;
+  const int kk = on ? k : itot - 1;
   const int P = nblk;
-  const double A = rcoef[4 * k + 0];
-  const double den = rcoef[4 * k + 2];
-  const bool pin = rcoef[4 * k + 3] != 0.;
   // right-hand side R_b = (r_iface - l y_b[M-2]) - l y_{b+1}[0]
-  auto R = [&](int b) { return iface[(size_t)b * itot + k] - l * first[(size_t)((b + 1) % P) * itot + k]; };
-  // Thomas on the leading P-1 rows (in place in iface)
-  const double rP = R(P - 1);
-  double zprev = R(0) * rinv[k];
-  iface[k] = zprev;
+  for (int b = 0; b < P; b++) {
+    zs[b * RED_COLS + t] = iface[(size_t)b * itot + kk] - l * first[(size_t)((b + 1) % P) * itot + kk];
+  }
+  const double A = rcoef[4 * kk + 0];
+  const double den = rcoef[4 * kk + 2];
+  const bool pin = rcoef[4 * kk + 3] != 0.;
+  const double rP = zs[(P - 1) * RED_COLS + t];
+  // Thomas on the leading P-1 rows
+  double zprev = zs[t] * rinv[kk];
+  zs[t] = zprev;
+#pragma unroll 8
   for (int b = 1; b < P - 1; b++) {
-    const double z = (R(b) - A * zprev) * rinv[(size_t)b * itot + k];
-    iface[(size_t)b * itot + k] = z;
-    zprev = z;
+    zprev = (zs[b * RED_COLS + t] - A * zprev) * rinv[(size_t)b * itot + kk];
+    zs[b * RED_COLS + t] = zprev;
   }
+#pragma unroll 8
   for (int b = P - 3; b >= 0; b--) {
-    const double z = iface[(size_t)b * itot + k] - rup[(size_t)b * itot + k] * zprev;
-    iface[(size_t)b * itot + k] = z;
-    zprev = z;
+    zprev = zs[b * RED_COLS + t] - rup[(size_t)b * itot + kk] * zprev;
+    zs[b * RED_COLS + t] = zprev;
   }
-  const double z0 = iface[k], zl = iface[(size_t)(P - 2) * itot + k];
+  const double z0 = zs[t], zl = zs[(P - 2) * RED_COLS + t];
   const double num = rP - A * z0 - A * zl;
   const double last = pin ? 0. : num / den;
+  if (!on) return;
   iface[(size_t)(P - 1) * itot + k] = last;
   for (int b = 0; b < P - 1; b++) {
-    iface[(size_t)b * itot + k] = iface[(size_t)b * itot + k] + last * rq1[(size_t)b * itot + k];
+    iface[(size_t)b * itot + k] = zs[b * RED_COLS + t] + last * rq1[(size_t)b * itot + k];
   }
 }
 
@@ -717,6 +728,11 @@ int poisson_init(eif_ctx *c) {
   } else {
     EIF_CK(c, cudaMalloc((void **)&pp.ywork, sizeof(double) * 2 * (size_t)jt * n));
   }
+  const size_t red_smem = sizeof(double) * RED_COLS * (pp.blk > 0 ? pp.nblk : 1);
+  if (red_smem > 227 * 1024) return fail(c, EIF_ERR_ARG, "jtot %d needs too many tridiagonal blocks", jt);
+  if (red_smem > 48 * 1024) {
+    EIF_CK(c, cudaFuncSetAttribute(k_tdm_reduced, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)red_smem));
+  }
   const size_t smem = sizeof(double2) * 2 * pp.m + sizeof(double) * n;
   if (smem > 48 * 1024) {
     EIF_CK(c, cudaFuncSetAttribute(k_dct2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -791,8 +807,8 @@ int launch_potential(eif_ctx *c, int rk, bool with_ibm) {
       k_tdm_local<4><<<g, 128, 0, c->stream>>>(c->qhat, pp.tdm_inv, pp.tdm_up, iface, first, l, n, pp.nblk, c->ld);
     }
     EIF_LAUNCH_CK(c);
-    k_tdm_reduced<<<(n + 63) / 64, 64, 0, c->stream>>>(iface, first, pp.red_inv, pp.red_up, pp.red_q1, pp.red_coef,
-                                                        l, n, pp.nblk);
+    k_tdm_reduced<<<(n + RED_COLS - 1) / RED_COLS, RED_COLS, sizeof(double) * RED_COLS * pp.nblk, c->stream>>>(
+        iface, first, pp.red_inv, pp.red_up, pp.red_q1, pp.red_coef, l, n, pp.nblk);
     EIF_LAUNCH_CK(c);
   } else {
     EIF_PROF(c, "poisson_tdm", 1);
