@@ -114,6 +114,15 @@ int device_metrics(eif_ctx *c) {
   };
   if ((rc = upload_f(&c->rdxf_f, rdxf))) return rc;
   if ((rc = upload_f(&c->rdxc_f, rdxc))) return rc;
+  {
+    std::vector<float2> df(rdxc.size());
+    for (size_t q = 0; q < rdxc.size(); q++) {
+      const float hi = (float)rdxc[q];
+      df[q] = make_float2(hi, (float)(rdxc[q] - (double)hi));
+    }
+    EIF_CK(c, cudaMalloc((void **)&c->rdxc_df, sizeof(float2) * df.size()));
+    EIF_CK(c, cudaMemcpy(c->rdxc_df, df.data(), sizeof(float2) * df.size(), cudaMemcpyHostToDevice));
+  }
   if ((rc = upload_f(&c->cxm_f, cxm))) return rc;
   if ((rc = upload_f(&c->cxp_f, cxp))) return rc;
   if ((rc = upload_f(&c->cym_f, cym))) return rc;
@@ -155,10 +164,13 @@ int sync_scalars(eif_ctx *c) {
 int ensure_pcap(eif_ctx *c, int n) {
   if (n <= c->pcap && c->P) return EIF_OK;
   if (c->P) cudaFree(c->P);
+  if (c->cpf) cudaFree(c->cpf);
   c->P = nullptr;
+  c->cpf = nullptr;
   const int cap = n > 0 ? n : 1;
   EIF_CK(c, cudaMalloc((void **)&c->P, sizeof(double) * EIF_NFIELDS * (size_t)cap));
   EIF_CK(c, cudaMemset(c->P, 0, sizeof(double) * EIF_NFIELDS * (size_t)cap));
+  EIF_CK(c, cudaMalloc((void **)&c->cpf, sizeof(float4) * (size_t)cap));
   c->pcap = cap;
   return EIF_OK;
 }
@@ -268,6 +280,8 @@ int eif_destroy(eif_ctx *c) {
                     c->cyp, c->dxc, c->P, c->d_scal};
   for (double *p : ptrs) if (p) cudaFree(p);
   if (c->d_coef) cudaFree(c->d_coef);
+  if (c->cpf) cudaFree(c->cpf);
+  if (c->rdxc_df) cudaFree(c->rdxc_df);
   float *fptrs[] = {c->rdxf_f, c->rdxc_f, c->cxm_f, c->cxp_f, c->cym_f, c->cyp_f, c->sxf[0], c->sxf[1], c->syf[0],
                     c->syf[1]};
   for (float *p : fptrs) if (p) cudaFree(p);
@@ -403,6 +417,18 @@ int eif_push_src(eif_ctx *c, const double *uxa, const double *uya) {
 int eif_pull_ibm_fields(eif_ctx *c, double *dux, double *duy) {
   if (!c || !dux || !duy) return EIF_ERR_ARG;
   const size_t dp = sizeof(double) * c->ld, wy = sizeof(double) * (c->itot + 2);
+  if (c->cfg.precision == EIF_PREC_MIXED) {
+    // the mixed form keeps the field response in single precision: widen it in scratch
+    double *dst[2] = {dux, duy};
+    const float *src[2] = {reinterpret_cast<const float *>(c->dux), reinterpret_cast<const float *>(c->duy)};
+    for (int k = 0; k < 2; k++) {
+      int rc = launch_f2d_copy(c, src[k], c->qhat, c->nfield);
+      if (rc) return rc;
+      EIF_CK(c, cudaMemcpy2DAsync(dst[k], wy, c->qhat, dp, wy, c->jtot + 2, cudaMemcpyDeviceToHost, c->stream));
+      EIF_CK(c, cudaStreamSynchronize(c->stream));
+    }
+    return check_records(c);
+  }
   EIF_CK(c, cudaMemcpy2DAsync(dux, wy, c->dux, dp, wy, c->jtot + 2, cudaMemcpyDeviceToHost, c->stream));
   EIF_CK(c, cudaMemcpy2DAsync(duy, wy, c->duy, dp, wy, c->jtot + 2, cudaMemcpyDeviceToHost, c->stream));
   EIF_CK(c, cudaStreamSynchronize(c->stream));

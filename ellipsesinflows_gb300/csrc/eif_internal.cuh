@@ -69,6 +69,7 @@ struct PoissonPlan {
   double *tdm_inv;  // [k][i]  1/pivot of the interior Thomas sweep, i < blk-1
   double *tdm_up;   // [k][i]  modified upper diagonal, i < blk-1
   double *tdm_g;    // [k][i]  response of the interior block to its left neighbour
+  float2 *tdm_g_df = nullptr;  // the same as (hi, lo) float pairs (mixed form)
   double *red_inv;  // [k][b]  reduced cyclic system: Thomas pivots (b < nblk-1)
   double *red_up;   // [k][b]
   double *red_q1;   // [k][b]  correction vector of the reduced cyclic system
@@ -101,6 +102,7 @@ struct eif_ctx {
   double *cxm, *cxp, *cym, *cyp;// stencil interpolation weights at [i]
   double *dxc;                  // DXC(i) at [i]
   float *rdxf_f, *rdxc_f, *cxm_f, *cxp_f, *cym_f, *cyp_f;  // single-precision copies
+  float2 *rdxc_df = nullptr;    // 1/dxc as double-float pairs (hi, lo)
   float *sxf[2], *syf[2];       // RK explicit terms of the mixed form
   // host copies of the metrics
   double *h_xf, *h_xc, *h_dxf, *h_dxc, *h_yf, *h_yc;
@@ -108,6 +110,7 @@ struct eif_ctx {
   // particles
   int np, pcap;
   double *P;                    // EIF_NFIELDS * pcap
+  float4 *cpf = nullptr;        // pcap: single-precision x + dx, y + dy, max(a, b) for the collision prefilter
   // immersed-boundary work
   int *box;                     // per particle: 3 images x {imin,imax,jmin,jmax}
   int *chunk_off;               // per particle: first chunk (exclusive scan), [np] = total
@@ -123,6 +126,7 @@ struct eif_ctx {
   double *d_scal;               // [0] dt, [1] residual, [2] scratch
   float *d_coef;                // single-precision dt products: [3*rk+0..2] alpha/beta/gamma*dt, [9] 1/dt,
                                 // [12+2*rk], [13+2*rk]: 1/(gamma dt) as a float pair
+                                // [20+2*rk], [21+2*rk]: gamma dt as a float pair
   unsigned *d_flags;
   double *h_scal;               // pinned mirror
   unsigned *h_flags;

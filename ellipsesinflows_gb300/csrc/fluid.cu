@@ -11,6 +11,7 @@
 //   param_decide_dt                     src/param/decide_dt.c:11-81
 //   check_divergence                    src/logging.c:40-80
 #include "eif_internal.cuh"
+#include "eif_df.cuh"
 #include <cfloat>
 
 namespace {
@@ -301,6 +302,77 @@ __global__ void __launch_bounds__(TX *TY) k_correct(CorrArgs a) {
   }
 }
 
+// Mixed-precision projection. The FP64 pipe is used only where the result must
+// keep double precision: the differences of psi (exact for neighbouring values),
+// the rounding of the double-float increment to a double, and the final sums.
+// The products gamma dt (psi_i - psi_{i-1}) / dxc and the IBM response (single-
+// precision field values, summed exactly) are formed in double-float arithmetic.
+struct CorrArgsDF {
+  double *ux, *uy, *p;
+  const double *psi;
+  const float *dux, *duy;   // IBM field response in single precision
+  const float2 *rdxc;       // 1/dxc as (hi, lo)
+  const float *coef;        // [20 + 2 rk], [21 + 2 rk]: gamma dt
+  eifdf::DF rdy;
+  int rk, itot, jtot, ld, with_ibm, with_proj, with_pressure;
+};
+
+__global__ void __launch_bounds__(TX *TY) k_correct_df(CorrArgsDF a) {
+  using namespace eifdf;
+  const int i = 1 + blockIdx.x * TX + threadIdx.x;
+  const int j = 1 + blockIdx.y * TY + threadIdx.y;
+  if (i > a.itot || j > a.jtot) return;
+  const int ld = a.ld, jtot = a.jtot, itot = a.itot;
+  const DF gdt = a.with_proj ? DF{__ldg(a.coef + 20 + 2 * a.rk), __ldg(a.coef + 21 + 2 * a.rk)} : DF{0.f, 0.f};
+  const int cy = uy_idx(i, j, ld);
+  const double psi0 = (a.with_proj || a.with_pressure) ? __ldg(a.psi + cy) : 0.;
+  const bool vel = a.with_ibm || a.with_proj;
+  if (vel && i >= 2) {
+    const int c = ux_idx(i, j, ld);
+    DF inc{0.f, 0.f};
+    if (a.with_ibm) inc = two_sum(__ldg(a.dux + cy - 1), __ldg(a.dux + cy));
+    inc = df_scale(inc, 0.5f);
+    if (a.with_proj) {
+      const float2 r = __ldg(a.rdxc + i);
+      const DF g = df_mul(df_mul(gdt, df_of(psi0 - __ldg(a.psi + cy - 1))), DF{r.x, r.y});
+      inc = df_add_nw(inc, df_neg(g));
+    }
+    const double u = a.ux[c] + df_to_double(inc);
+    a.ux[c] = u;
+    if (j == 1) a.ux[c + jtot * ld] = u;
+    if (j == jtot) a.ux[c - jtot * ld] = u;
+  }
+  if (vel) {
+    DF inc{0.f, 0.f};
+    if (a.with_ibm) inc = two_sum(__ldg(a.duy + cy - ld), __ldg(a.duy + cy));
+    inc = df_scale(inc, 0.5f);
+    if (a.with_proj) {
+      const DF g = df_mul(df_mul(gdt, df_of(psi0 - __ldg(a.psi + cy - ld))), a.rdy);
+      inc = df_add_nw(inc, df_neg(g));
+    }
+    const double v = a.uy[cy] + df_to_double(inc);
+    a.uy[cy] = v;
+    if (j == 1) a.uy[cy + jtot * ld] = v;
+    if (j == jtot) a.uy[cy - jtot * ld] = v;
+  }
+  if (a.with_pressure) {
+    const double pv = a.p[cy] + psi0;
+    a.p[cy] = pv;
+    if (j == 1) a.p[cy + jtot * ld] = pv;
+    if (j == jtot) a.p[cy - jtot * ld] = pv;
+    if (i == 1) {
+      a.p[cy - 1] = pv;
+      if (j == 1) a.p[cy - 1 + jtot * ld] = pv;
+      if (j == jtot) a.p[cy - 1 - jtot * ld] = pv;
+    }
+    if (i == itot) {
+      a.p[cy + 1] = pv;
+      if (j == 1) a.p[cy + 1 + jtot * ld] = pv;
+      if (j == jtot) a.p[cy + 1 - jtot * ld] = pv;
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // dt: column maxima of |ux| and the global maximum of |uy| as order-preserving
 // integer maxima of the IEEE bit patterns (non-negative doubles order like
@@ -351,6 +423,12 @@ __device__ __forceinline__ void write_coef(double dt, float *coef) {
     coef[3 * rk + 2] = (float)((al[rk] + be[rk]) * dt);
   }
   coef[9] = (float)(1. / dt);
+  for (int rk = 0; rk < 3; rk++) {
+    const double gdt = (al[rk] + be[rk]) * dt;
+    const float hi = (float)gdt;
+    coef[20 + 2 * rk] = hi;
+    coef[21 + 2 * rk] = (float)(gdt - (double)hi);
+  }
   for (int rk = 0; rk < 3; rk++) {
     const double inv = 1. / ((al[rk] + be[rk]) * dt);
     const float hi = (float)inv;
@@ -529,6 +607,27 @@ int launch_predictor(eif_ctx *c, int rk) {
 }
 
 static int launch_corr(eif_ctx *c, int rk, int with_ibm, int with_proj, int with_pressure) {
+  if (c->cfg.precision == EIF_PREC_MIXED) {
+    CorrArgsDF a;
+    a.ux = c->ux[c->cur];
+    a.uy = c->uy[c->cur];
+    a.p = c->p;
+    a.psi = c->psi;
+    a.dux = reinterpret_cast<const float *>(c->dux);
+    a.duy = reinterpret_cast<const float *>(c->duy);
+    a.rdxc = c->rdxc_df;
+    a.coef = c->d_coef;
+    const double rdy = 1. / c->dy;
+    const float hi = (float)rdy;
+    a.rdy = eifdf::DF{hi, (float)(rdy - (double)hi)};
+    a.rk = rk >= 0 ? rk : 0;
+    a.itot = c->itot; a.jtot = c->jtot; a.ld = c->ld;
+    a.with_ibm = with_ibm; a.with_proj = with_proj; a.with_pressure = with_pressure;
+    EIF_PROF(c, "correct", 1);
+    k_correct_df<<<cell_grid(c), dim3(TX, TY), 0, c->stream>>>(a);
+    EIF_LAUNCH_CK(c);
+    return EIF_OK;
+  }
   CorrArgs a;
   a.ux = c->ux[c->cur];
   a.uy = c->uy[c->cur];

@@ -81,11 +81,9 @@ __device__ __forceinline__ double normal_t(const Ell &e, double x_, double y_) {
   return t;
 }
 
-// auxiliary.c:19-47, in units of the grid size h (rh = 1/h)
-__device__ __forceinline__ double signed_dist(const Ell &e, double x, double y, double rh) {
-  const double ddx = x - e.px, ddy = y - e.py;
-  const double x_ = e.cz * ddx - e.sz * ddy;
-  const double y_ = e.sz * ddx + e.cz * ddy;
+// auxiliary.c:19-47, in units of the grid size h (rh = 1/h), from the body-frame
+// offset (x_, y_) = R(-az) (x - px, y - py)
+__device__ __forceinline__ double signed_dist_body(const Ell &e, double x_, double y_, double rh) {
   const double f0 = 1. - (x_ / e.a) * (x_ / e.a) - (y_ / e.b) * (y_ / e.b);
   const double sign = f0 > 0. ? 1. : -1.;
   const double t = normal_t(e, x_, y_);
@@ -302,6 +300,9 @@ __global__ void __launch_bounds__(256) k_ibm_work(WorkArgs a) {
   const double dxdy = a.dx * a.dy;
   const double dtv = a.mode == 1 ? __ldg(a.dt) : 0.;
   const int pc = a.pcap, ld = a.ld;
+  // per warp: body-frame offsets of its near cells, overwritten by their weights
+  __shared__ double2 slot_buf[8][CHUNK];
+  double2 *slots = slot_buf[threadIdx.x >> 5];
   for (int c = warp; c < total; c += nwarps) {
     const int n = find_particle(a.off, a.np, c);
     if (!EIF_CHK(a.bd.rec, n, a.np, 11)) continue;
@@ -323,37 +324,61 @@ __global__ void __launch_bounds__(256) k_ibm_work(WorkArgs a) {
     const double pm = pmass(pden, pa, pb);
     const double pim = pmoi(pden, pa, pb);
     const double pux = __ldg(P + EIF_P_UX * pc + n), puy = __ldg(P + EIF_P_UY * pc + n), pvz = __ldg(P + EIF_P_VZ * pc + n);
-    Ell e0 = make_ell(pa, pb, px, py, paz);
-    double s0 = 0., s1 = 0., s2 = 0.;
+    const Ell e = make_ell(pa, pb, px, py, paz);
+    // pass 1: cells of the chunk, body-frame offsets, far cells settled
+    int ci[2], cj[2], cimg[2], rank[2];
+    bool cin[2];
+    double th2[2];
+    unsigned near_mask[2];
 #pragma unroll
     for (int half = 0; half < CHUNK / 32; half++) {
       const int kk = local0 + half * 32 + lane;
-      int i, j, img;
-      double2 contrib = make_double2(0., 0.);
-      bool in = cell_of(bx, kk, i, j, img);
+      bool in = cell_of(bx, kk, ci[half], cj[half], cimg[half]);
       if (in) {
+        const int i = ci[half], j = cj[half];
         in = EIF_CHK(a.bd.rec, i, a.bd.xc - 1, 14) && EIF_CHK(a.bd.rec, j, a.bd.yc - 1, 15) &&
              EIF_CHK(a.bd.rec, j * ld + i, a.bd.field, 16) && EIF_CHK(a.bd.rec, (j + 1) * ld + i, a.bd.field, 17) &&
              EIF_CHK(a.bd.rec, j * ld + (i - 1), a.bd.field, 18);
       }
+      cin[half] = in;
+      bool near = false;
+      double x_ = 0., y_ = 0.;
+      th2[half] = 0.;
       if (in) {
+        const double x = __ldg(a.xc + ci[half]), y = __ldg(a.yc + cj[half]);
+        const double ddx = x - e.px, ddy = y - (py + a.ly * cimg[half]);
+        x_ = e.cz * ddx - e.sz * ddy;
+        y_ = e.sz * ddx + e.cz * ddy;
+        const int side = far_side(x_, y_, e.a, e.b, FAR_CELLS_D * a.h);
+        // reference sign convention: +1 inside (auxiliary.c:36-38); tanh saturated
+        th2[half] = (double)side;
+        near = side == 0;
+      }
+      near_mask[half] = __ballot_sync(0xffffffffu, near);
+      rank[half] = (half ? __popc(near_mask[0]) : 0) + __popc(near_mask[half] & ((1u << lane) - 1u));
+      if (near) slots[rank[half]] = make_double2(x_, y_);
+    }
+    // pass 2: the near cells, packed onto consecutive lanes
+    const int nnear = __popc(near_mask[0]) + __popc(near_mask[1]);
+    __syncwarp();
+    for (int k = lane; k < nnear; k += 32) {
+      const double2 o = slots[k];
+      slots[k].x = tanh(BETA * signed_dist_body(e, o.x, o.y, rh));
+    }
+    __syncwarp();
+#pragma unroll
+    for (int half = 0; half < CHUNK / 32; half++)
+      if ((near_mask[half] >> lane) & 1u) th2[half] = slots[rank[half]].x;
+    __syncwarp();
+    double s0 = 0., s1 = 0., s2 = 0.;
+#pragma unroll
+    for (int half = 0; half < CHUNK / 32; half++) {
+      const int i = ci[half], j = cj[half], img = cimg[half];
+      double2 contrib = make_double2(0., 0.);
+      if (cin[half]) {
         const double py_ = py + a.ly * img;
-        Ell e = e0;
-        e.py = py_;
         const double x = __ldg(a.xc + i), y = __ldg(a.yc + j);
-        double th;
-        {
-          const double ddx = x - e.px, ddy = y - e.py;
-          const double x_ = e.cz * ddx - e.sz * ddy;
-          const double y_ = e.sz * ddx + e.cz * ddy;
-          const int side = far_side(x_, y_, e.a, e.b, FAR_CELLS_D * a.h);
-          if (side != 0) {
-            // reference sign convention: +1 inside (auxiliary.c:36-38); tanh saturated
-            th = (double)side;
-          } else {
-            th = tanh(BETA * signed_dist(e, x, y, rh));
-          }
-        }
+        const double th = th2[half];
         const double uxf = 0.5 * (__ldg(a.ux + j * ld + (i - 1)) + __ldg(a.ux + j * ld + i));
         const double uyf = 0.5 * (__ldg(a.uy + j * ld + i) + __ldg(a.uy + (j + 1) * ld + i));
         if (a.mode == 0) {
@@ -440,9 +465,7 @@ __device__ __forceinline__ int far_side_f(float x_, float y_, float a, float b, 
   return fmaxf(mn * (1.f - rho), mn - r) >= min_dist ? 1 : 0;
 }
 
-__device__ __forceinline__ float signed_dist_f(const EllF &e, float X, float Y, float rh) {
-  const float x_ = e.cz * X - e.sz * Y;
-  const float y_ = e.sz * X + e.cz * Y;
+__device__ __forceinline__ float signed_dist_body_f(const EllF &e, float x_, float y_, float rh) {
   const float f0 = 1.f - (x_ / e.a) * (x_ / e.a) - (y_ / e.b) * (y_ / e.b);
   const float sign = f0 > 0.f ? 1.f : -1.f;
   const float t = normal_t_f(e, x_, y_);
@@ -462,6 +485,9 @@ __global__ void __launch_bounds__(256) k_ibm_work_f(WorkArgs a) {
   const float rdtv = a.mode == 1 ? __ldg(a.coef + 9) : 0.f;
   const int ld = a.ld;
   float2 *wb = reinterpret_cast<float2 *>(a.wbuf);
+  // per warp: body-frame offsets of its near cells, overwritten by their weights
+  __shared__ float2 slot_buf[8][CHUNK];
+  float2 *slots = slot_buf[threadIdx.x >> 5];
   for (int c = warp; c < total; c += nwarps) {
     if (!EIF_CHK(a.bd.rec, c, a.bd.partial / 3, 51)) continue;
     const int n = __ldg(a.owner + c);
@@ -478,28 +504,59 @@ __global__ void __launch_bounds__(256) k_ibm_work_f(WorkArgs a) {
     const int i0 = __float_as_int(qD.x);
     const int j0s[3] = {__float_as_int(qD.y), __float_as_int(qD.z), __float_as_int(qD.w)};
     const float gys[3] = {qE.x, qE.y, qE.z};
-    float sacc0 = 0.f, sacc1 = 0.f, sacc2 = 0.f;
+    // pass 1: cells of the chunk, body-frame offsets, far cells settled
+    int ci[2], cj[2], rank[2];
+    float cX[2], cY[2], th2[2];
+    bool cin[2];
+    unsigned near_mask[2];
 #pragma unroll
     for (int half = 0; half < CHUNK / 32; half++) {
       const int kk = local0 + half * 32 + lane;
-      int i, j, img;
-      float2 contrib = make_float2(0.f, 0.f);
-      bool in = cell_of(bx, kk, i, j, img);
+      int img;
+      bool in = cell_of(bx, kk, ci[half], cj[half], img);
       if (in) {
+        const int i = ci[half], j = cj[half];
         in = EIF_CHK(a.bd.rec, j * ld + i, a.bd.field, 54) && EIF_CHK(a.bd.rec, (j + 1) * ld + i, a.bd.field, 55) &&
              EIF_CHK(a.bd.rec, j * ld + (i - 1), a.bd.field, 56);
       }
+      cin[half] = in;
+      bool near = false;
+      float x_ = 0.f, y_ = 0.f;
+      cX[half] = 0.f; cY[half] = 0.f; th2[half] = 0.f;
       if (in) {
         const int m = img + 1;
-        const float X = ((float)(i - i0) - gx) * dxf;
-        const float Y = ((float)(j - j0s[m]) - gys[m]) * dyf;
-        float th;
-        {
-          const float x_ = e.cz * X - e.sz * Y;
-          const float y_ = e.sz * X + e.cz * Y;
-          const int side = far_side_f(x_, y_, e.a, e.b, FAR_CELLS_F / rh);
-          th = side != 0 ? (float)side : tanhf(2.f * signed_dist_f(e, X, Y, rh));
-        }
+        const float X = ((float)(ci[half] - i0) - gx) * dxf;
+        const float Y = ((float)(cj[half] - j0s[m]) - gys[m]) * dyf;
+        cX[half] = X; cY[half] = Y;
+        x_ = e.cz * X - e.sz * Y;
+        y_ = e.sz * X + e.cz * Y;
+        const int side = far_side_f(x_, y_, e.a, e.b, FAR_CELLS_F / rh);
+        th2[half] = (float)side;
+        near = side == 0;
+      }
+      near_mask[half] = __ballot_sync(0xffffffffu, near);
+      rank[half] = (half ? __popc(near_mask[0]) : 0) + __popc(near_mask[half] & ((1u << lane) - 1u));
+      if (near) slots[rank[half]] = make_float2(x_, y_);
+    }
+    // pass 2: the near cells, packed onto consecutive lanes
+    const int nnear = __popc(near_mask[0]) + __popc(near_mask[1]);
+    __syncwarp();
+    for (int k = lane; k < nnear; k += 32) {
+      const float2 o = slots[k];
+      slots[k].x = tanhf(2.f * signed_dist_body_f(e, o.x, o.y, rh));
+    }
+    __syncwarp();
+#pragma unroll
+    for (int half = 0; half < CHUNK / 32; half++)
+      if ((near_mask[half] >> lane) & 1u) th2[half] = slots[rank[half]].x;
+    __syncwarp();
+    float sacc0 = 0.f, sacc1 = 0.f, sacc2 = 0.f;
+#pragma unroll
+    for (int half = 0; half < CHUNK / 32; half++) {
+      const int i = ci[half], j = cj[half];
+      float2 contrib = make_float2(0.f, 0.f);
+      if (cin[half]) {
+        const float X = cX[half], Y = cY[half], th = th2[half];
         const float uxs = eifd::d2f(__ldg(a.ux + j * ld + (i - 1))) + eifd::d2f(__ldg(a.ux + j * ld + i));
         const float uys = eifd::d2f(__ldg(a.uy + j * ld + i)) + eifd::d2f(__ldg(a.uy + (j + 1) * ld + i));
         if (a.mode == 0) {
@@ -610,7 +667,7 @@ struct GatherArgs {
   const int *lists, *counts;
   int cap;
   const void *wbuf;
-  double *dux, *duy;
+  void *dux, *duy;   // double (FP64 form) or float (mixed form) fields with the same pitch
   unsigned *flags;
   int np, itot, jtot, ld;
   Bounds bd;
@@ -618,9 +675,6 @@ struct GatherArgs {
 
 // field response dux/duy (exchange.c:71-72,80-81): per tile, the ordered list
 // of covering (particle, image) boxes, then per cell the sum in that order
-__device__ __forceinline__ double to_double(double v) { return v; }
-__device__ __forceinline__ double to_double(float v) { return eifd::f2d(v); }
-
 template <typename V2, typename Acc>
 __global__ void __launch_bounds__(GTHREADS) k_gather(GatherArgs a) {
   const V2 *wbuf = static_cast<const V2 *>(a.wbuf);
@@ -639,9 +693,11 @@ __global__ void __launch_bounds__(GTHREADS) k_gather(GatherArgs a) {
     const int cnt = min(LMAX, L - base);
     for (int e = threadIdx.x; e < cnt; e += GTHREADS) {
       const int ent = __ldg(blist + base + e);
-      const int n = ent / 3, q = ent % 3;
+      const int n = ent / 3, q = ent - 3 * n;
       int bi0 = 1, bi1 = 0, bj0 = 1, bj1 = 0, off = 0;
-      if (EIF_CHK(a.bd.rec, n, a.np, 44) && EIF_CHK(a.bd.rec, 12LL * n + 11, a.bd.box, 45)) {
+      // entry = 3 * particle + image with 0 <= image < 3; anything else is recorded and skipped
+      if (EIF_CHK(a.bd.rec, ent, 3LL * a.np, 46) && EIF_CHK(a.bd.rec, n, a.np, 44) &&
+          EIF_CHK(a.bd.rec, 12LL * n + 4 * q + 3, a.bd.box, 45)) {
         const int *bx = a.box + 12 * n;
         int base_q = 0;
         for (int m = 0; m < q; m++) {
@@ -674,34 +730,44 @@ __global__ void __launch_bounds__(GTHREADS) k_gather(GatherArgs a) {
     }
     __syncthreads();
   }
-  // write the tile (zero where no box covers), periodic halo rows and Neumann columns
-  const int ld = a.ld, jtot = a.jtot, itot = a.itot;
+  // write the tile's interior cells (zero where no box covers); the halo rows and
+  // ghost columns are filled afterwards by k_ibm_halo from these cells
+  const int ld = a.ld;
 #pragma unroll
   for (int r = 0; r < 2; r++) {
     const int i = i0 + lx, j = j0 + ly0 + 4 * r;
     if (i > i1 || j > j1) continue;
     const int cidx = j * ld + i;
-    {
-      // every index written for this cell: the cell, its halo-row copy and its Neumann copies
-      const long long lo = cidx - (i == 1 ? 1 : 0) - (j == jtot ? (long long)jtot * ld : 0);
-      const long long hi = cidx + (i == itot ? 1 : 0) + (j == 1 ? (long long)jtot * ld : 0);
-      if (!EIF_CHK(a.bd.rec, lo, a.bd.field, 42) || !EIF_CHK(a.bd.rec, hi, a.bd.field, 43)) continue;
-    }
-    const double vx = to_double(acc_x[r]), vy = to_double(acc_y[r]);
-    a.dux[cidx] = vx; a.duy[cidx] = vy;
-    if (j == 1) { a.dux[cidx + jtot * ld] = vx; a.duy[cidx + jtot * ld] = vy; }
-    if (j == jtot) { a.dux[cidx - jtot * ld] = vx; a.duy[cidx - jtot * ld] = vy; }
-    if (i == 1) {
-      a.dux[cidx - 1] = vx; a.duy[cidx - 1] = vy;
-      if (j == 1) { a.dux[cidx - 1 + jtot * ld] = vx; a.duy[cidx - 1 + jtot * ld] = vy; }
-      if (j == jtot) { a.dux[cidx - 1 - jtot * ld] = vx; a.duy[cidx - 1 - jtot * ld] = vy; }
-    }
-    if (i == itot) {
-      a.dux[cidx + 1] = vx; a.duy[cidx + 1] = vy;
-      if (j == 1) { a.dux[cidx + 1 + jtot * ld] = vx; a.duy[cidx + 1 + jtot * ld] = vy; }
-      if (j == jtot) { a.dux[cidx + 1 - jtot * ld] = vx; a.duy[cidx + 1 - jtot * ld] = vy; }
-    }
+    if (!EIF_CHK(a.bd.rec, cidx, a.bd.field, 42)) continue;
+    static_cast<Acc *>(a.dux)[cidx] = acc_x[r];
+    static_cast<Acc *>(a.duy)[cidx] = acc_y[r];
   }
+}
+
+// Periodic halo rows (j = 0 <- jtot, j = jtot+1 <- 1) and Neumann ghost columns
+// (i = 0 <- 1, i = itot+1 <- itot, corners included) of the IBM field response,
+// exchange.c:80-81 with the boundary update of the reference. Every thread reads
+// one interior cell and writes one halo cell.
+template <typename T>
+__global__ void k_ibm_halo(T *__restrict__ dux, T *__restrict__ duy, int itot, int jtot, int ld) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nrow = itot + 2;
+  int dst, src;
+  if (t < 2 * nrow) {
+    const int i = t % nrow, top = t / nrow;
+    const int ic = i < 1 ? 1 : (i > itot ? itot : i);
+    dst = (top ? jtot + 1 : 0) * ld + i;
+    src = (top ? 1 : jtot) * ld + ic;
+  } else if (t < 2 * nrow + 2 * jtot) {
+    const int u = t - 2 * nrow;
+    const int j = 1 + u % jtot, right = u / jtot;
+    dst = j * ld + (right ? itot + 1 : 0);
+    src = j * ld + (right ? itot : 1);
+  } else {
+    return;
+  }
+  dux[dst] = dux[src];
+  duy[dst] = duy[src];
 }
 
 }  // namespace
@@ -865,11 +931,18 @@ int launch_exchange(eif_ctx *c) {
     EIF_LAUNCH_CK(c);
   }
   dim3 grid((c->itot + GTX - 1) / GTX, (c->jtot + GTY - 1) / GTY);
-  EIF_PROF(c, "ibm_gather", 1);
+  EIF_PROF(c, "ibm_gather", 2);
+  const int nhalo = 2 * (c->itot + 2) + 2 * c->jtot;
   if (c->cfg.precision == EIF_PREC_MIXED) {
     k_gather<float2, float><<<grid, GTHREADS, 0, c->stream>>>(g);
+    EIF_LAUNCH_CK(c);
+    k_ibm_halo<float><<<(nhalo + 255) / 256, 256, 0, c->stream>>>(reinterpret_cast<float *>(c->dux),
+                                                                  reinterpret_cast<float *>(c->duy), c->itot,
+                                                                  c->jtot, c->ld);
   } else {
     k_gather<double2, double><<<grid, GTHREADS, 0, c->stream>>>(g);
+    EIF_LAUNCH_CK(c);
+    k_ibm_halo<double><<<(nhalo + 255) / 256, 256, 0, c->stream>>>(c->dux, c->duy, c->itot, c->jtot, c->ld);
   }
   EIF_LAUNCH_CK(c);
   return EIF_OK;

@@ -213,34 +213,44 @@ __device__ void wall_contribution(const PV &p, double wallx, double out[3], bool
 
 constexpr int CWARPS = 4;
 
-__global__ void __launch_bounds__(CWARPS * 32) k_collision(double *__restrict__ P, int pcap, int np, int cn, double ly,
-                                                           double lx, unsigned *__restrict__ flags) {
+// single-precision centre (at X^k + dX) and bounding radius of every particle
+__global__ void k_collision_prep(const double *__restrict__ P, int pcap, int np, float4 *__restrict__ cpf) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= np) return;
+  const PV v = load_pv(P, pcap, n);
+  cpf[n] = make_float4(eifd::d2f(v.x), eifd::d2f(v.y), eifd::d2f(fmax(v.a, v.b)), 0.f);
+}
+
+__global__ void __launch_bounds__(CWARPS * 32) k_collision(double *__restrict__ P, const float4 *__restrict__ cpf,
+                                                           int pcap, int np, int cn, double ly, double lx,
+                                                           unsigned *__restrict__ flags) {
   __shared__ int cand[CWARPS][32];
   __shared__ double cval[CWARPS][32][3];
   const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
   const int k = blockIdx.x * CWARPS + wl;
   if (k >= np) return;
   const PV pk = load_pv(P, pcap, k);
-  const float rk = (float)fmax(pk.a, pk.b);
-  const float xk = (float)pk.x, yk = (float)pk.y, lyf = (float)ly;
+  const float4 fk = __ldg(cpf + k);
+  const float rk = fk.z, xk = fk.x, yk = fk.y, lyf = eifd::d2f(ly);
   double acc0 = 0., acc1 = 0., acc2 = 0.;
   bool ok_all = true;
   for (int base = 0; base < np; base += 32) {
     const int m = base + lane;
     bool hit = false;
     if (m < np && m != k) {
-      const PV pm_ = load_pv(P, pcap, m);
+      const float4 fm = __ldg(cpf + m);
       // conservative single-precision test: skip only pairs clearly apart for every image
-      const float rs = rk + (float)fmax(pm_.a, pm_.b);
-      const float dxf = (float)pm_.x - xk;
+      const float rs = rk + fm.z;
+      const float dxf = fm.x - xk;
       const float lim = rs * rs * 1.001f + 1e-6f;
       bool maybe = false;
       for (int per = -1; per <= 1; per++) {
-        const float dyf = (float)pm_.y + lyf * per - yk;
+        const float dyf = fm.y + lyf * per - yk;
         maybe |= dxf * dxf + dyf * dyf <= lim;
       }
       if (maybe) {
         // exact test with the canonical orientation of the pair
+        const PV pm_ = load_pv(P, pcap, m);
         hit = m < k ? bounding_overlap(pm_, pk, ly) : bounding_overlap(pk, pm_, ly);
       }
     }
@@ -356,9 +366,11 @@ namespace eif {
 
 int launch_collision(eif_ctx *c, int cn) {
   if (c->np == 0) return EIF_OK;
-  EIF_PROF(c, "collision", 1);
-  k_collision<<<(c->np + CWARPS - 1) / CWARPS, CWARPS * 32, 0, c->stream>>>(c->P, c->pcap, c->np, cn, c->ly, c->lx,
-                                                                            c->d_flags);
+  EIF_PROF(c, "collision", 2);
+  k_collision_prep<<<(c->np + 127) / 128, 128, 0, c->stream>>>(c->P, c->pcap, c->np, c->cpf);
+  EIF_LAUNCH_CK(c);
+  k_collision<<<(c->np + CWARPS - 1) / CWARPS, CWARPS * 32, 0, c->stream>>>(c->P, c->cpf, c->pcap, c->np, cn, c->ly,
+                                                                            c->lx, c->d_flags);
   EIF_LAUNCH_CK(c);
   return EIF_OK;
 }

@@ -20,7 +20,8 @@
 //      pre-factored Thomas coefficients (the matrix is constant along y).
 //   3. k_tdm_reduced: one thread per wavenumber solves the cyclic system of
 //      the interface values, which again has constant coefficients and is
-//      solved with the reference's cyclic algorithm (tdm.c:64-108).
+//      solved with the reference's cyclic algorithm (tdm.c:64-108), on
+//      right-hand sides and factors staged in shared memory.
 //   4. k_dct3: one CTA per row; the interior values are reconstructed from
 //      the block solution and the two neighbouring interface values in the
 //      load, then DCT-III, scaling and the Neumann/halo values of psi
@@ -30,6 +31,7 @@
 // constant is fixed by pinning the last interface value of kx = 0 to zero.
 // The constant shifts psi (and p) uniformly and does not change velocities.
 #include "eif_internal.cuh"
+#include "eif_df.cuh"
 #include <cmath>
 #include <vector>
 #include <algorithm>
@@ -197,51 +199,71 @@ __global__ void __launch_bounds__(256) k_tdm_local(double *__restrict__ qhat, co
 }
 
 // cyclic system of the interface values of one wavenumber. One thread per
-// wavenumber, 32 wavenumbers per block; each thread keeps its column of right-
-// hand sides in shared memory, so the serial sweeps run at shared-memory
-// latency rather than one L2 round trip per step.
-constexpr int RED_COLS = 32;
+// wavenumber runs the serial sweeps; the block's other threads first stage the
+// right-hand sides and the elimination factors of its `cols` wavenumbers in
+// shared memory (many loads in flight), so that the sweeps run at shared-memory
+// latency, and afterwards write the results back.
+constexpr int RED_THREADS = 256;
 
-__global__ void __launch_bounds__(RED_COLS) k_tdm_reduced(double *__restrict__ iface, const double *__restrict__ first,
-                                                          const double *__restrict__ rinv, const double *__restrict__ rup,
-                                                          const double *__restrict__ rq1, const double *__restrict__ rcoef,
-                                                          double l, int itot, int nblk) {
-  extern __shared__ double zs[];  // [nblk][RED_COLS]
-  const int t = threadIdx.x;
-  const int k = blockIdx.x * RED_COLS + t;
-  const bool on = k < itot;
-  const int kk = on ? k : itot - 1;
+__global__ void __launch_bounds__(RED_THREADS) k_tdm_reduced(double *__restrict__ iface, const double *__restrict__ first,
+                                                             const double *__restrict__ rinv, const double *__restrict__ rup,
+                                                             const double *__restrict__ rq1, const double *__restrict__ rcoef,
+                                                             double l, int itot, int nblk, int cols) {
+  extern __shared__ double zs[];  // [nblk][cols] right-hand sides, then [nblk][cols] rinv, rup; [cols] last
   const int P = nblk;
-  // right-hand side R_b = (r_iface - l y_b[M-2]) - l y_{b+1}[0]
-  for (int b = 0; b < P; b++) {
-    zs[b * RED_COLS + t] = iface[(size_t)b * itot + kk] - l * first[(size_t)((b + 1) % P) * itot + kk];
+  double *fi = zs + (size_t)P * cols, *fu = fi + (size_t)P * cols, *lastv = fu + (size_t)P * cols;
+  const int k0 = blockIdx.x * cols;
+  // right-hand side R_b = (r_iface - l y_b[M-2]) - l y_{b+1}[0]; factors
+  for (int idx = threadIdx.x; idx < P * cols; idx += blockDim.x) {
+    const int b = idx / cols, t = idx - b * cols;
+    const int kk = min(k0 + t, itot - 1);
+    zs[idx] = iface[(size_t)b * itot + kk] - l * first[(size_t)((b + 1) % P) * itot + kk];
+    fi[idx] = rinv[(size_t)b * itot + kk];
+    fu[idx] = rup[(size_t)b * itot + kk];
   }
-  const double A = rcoef[4 * kk + 0];
-  const double den = rcoef[4 * kk + 2];
-  const bool pin = rcoef[4 * kk + 3] != 0.;
-  const double rP = zs[(P - 1) * RED_COLS + t];
-  // Thomas on the leading P-1 rows
-  double zprev = zs[t] * rinv[kk];
-  zs[t] = zprev;
+  __syncthreads();
+  const int t = threadIdx.x;
+  if (t < cols) {
+    const int kk = min(k0 + t, itot - 1);
+    const double A = rcoef[4 * kk + 0];
+    const double den = rcoef[4 * kk + 2];
+    const bool pin = rcoef[4 * kk + 3] != 0.;
+    const double rP = zs[(P - 1) * cols + t];
+    // Thomas on the leading P-1 rows
+    double zprev = zs[t] * fi[t];
+    zs[t] = zprev;
 #pragma unroll 8
-  for (int b = 1; b < P - 1; b++) {
-    zprev = (zs[b * RED_COLS + t] - A * zprev) * rinv[(size_t)b * itot + kk];
-    zs[b * RED_COLS + t] = zprev;
-  }
+    for (int b = 1; b < P - 1; b++) {
+      zprev = (zs[b * cols + t] - A * zprev) * fi[b * cols + t];
+      zs[b * cols + t] = zprev;
+    }
 #pragma unroll 8
-  for (int b = P - 3; b >= 0; b--) {
-    zprev = zs[b * RED_COLS + t] - rup[(size_t)b * itot + kk] * zprev;
-    zs[b * RED_COLS + t] = zprev;
+    for (int b = P - 3; b >= 0; b--) {
+      zprev = zs[b * cols + t] - fu[b * cols + t] * zprev;
+      zs[b * cols + t] = zprev;
+    }
+    const double z0 = zs[t], zl = zs[(P - 2) * cols + t];
+    const double num = rP - A * z0 - A * zl;
+    lastv[t] = pin ? 0. : num / den;
   }
-  const double z0 = zs[t], zl = zs[(P - 2) * RED_COLS + t];
-  const double num = rP - A * z0 - A * zl;
-  const double last = pin ? 0. : num / den;
-  if (!on) return;
-  iface[(size_t)(P - 1) * itot + k] = last;
-  for (int b = 0; b < P - 1; b++) {
-    iface[(size_t)b * itot + k] = zs[b * RED_COLS + t] + last * rq1[(size_t)b * itot + k];
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < P * cols; idx += blockDim.x) {
+    const int b = idx / cols, tt = idx - b * cols;
+    const int k = k0 + tt;
+    if (k >= itot) continue;
+    const double last = lastv[tt];
+    iface[(size_t)b * itot + k] = b == P - 1 ? last : zs[idx] + last * rq1[(size_t)b * itot + k];
   }
 }
+
+// columns per block of k_tdm_reduced that fit its shared memory
+static int red_cols(int nblk) {
+  for (int cols = 16; cols >= 1; cols /= 2) {
+    if (sizeof(double) * ((size_t)3 * nblk * cols + cols) <= 227 * 1024) return cols;
+  }
+  return 0;
+}
+static size_t red_smem_bytes(int nblk, int cols) { return sizeof(double) * ((size_t)3 * nblk * cols + cols); }
 
 // fallback for column lengths without a suitable block size: the reference's
 // sequential cyclic algorithm per wavenumber on global memory
@@ -355,48 +377,29 @@ __global__ void __launch_bounds__(256) k_dct3(Dct3Args a) {
 }
 
 // ---------------------------------------------------------------------------
-// Double-float arithmetic for the mixed-precision form: a value is the
-// unevaluated sum hi + lo of two floats (about 48 significant bits), combined
-// with the error-free transformations of Knuth (TwoSum), Dekker (Fast2Sum) and
-// an FMA-based product (Ogita, Rump and Oishi, "Accurate sum and dot product",
-// SIAM J. Sci. Comput. 26, 2005). Only the FP32 pipe is used.
-struct DF { float hi, lo; };
+// Complex double-float arithmetic (eif_df.cuh) for the mixed-precision form.
+using namespace eifdf;
 struct CDF { DF re, im; };
 
-__device__ __forceinline__ DF two_sum(float a, float b) {
-  const float s = a + b;
-  const float bb = s - a;
-  return DF{s, (a - (s - bb)) + (b - bb)};
+__device__ __forceinline__ CDF cdf_add(CDF a, CDF b) { return CDF{df_add_nw(a.re, b.re), df_add_nw(a.im, b.im)}; }
+__device__ __forceinline__ CDF cdf_sub(CDF a, CDF b) {
+  return CDF{df_add_nw(a.re, df_neg(b.re)), df_add_nw(a.im, df_neg(b.im))};
 }
-__device__ __forceinline__ DF fast_sum(float a, float b) {  // requires |a| >= |b| or a == 0
-  const float s = a + b;
-  return DF{s, b - (s - a)};
+// x.hi y.hi + s u.hi v.hi formed exactly (two products, one TwoSum), the
+// cross and trailing terms accumulated in single precision with FMAs
+__device__ __forceinline__ DF df_dot2(DF x, DF y, DF u, DF v, float sgn) {
+  const float p1 = x.hi * y.hi, p2 = sgn * (u.hi * v.hi);
+  const float e1 = fmaf(x.hi, y.hi, -p1), e2 = fmaf(sgn * u.hi, v.hi, -p2);
+  const DF s = two_sum(p1, p2);
+  float t = fmaf(x.hi, y.lo, e1);
+  t = fmaf(x.lo, y.hi, t);
+  t = fmaf(sgn * u.hi, v.lo, t);
+  t = fmaf(sgn * u.lo, v.hi, t);
+  t = t + e2 + s.lo;
+  return fast_sum(s.hi, t);
 }
-__device__ __forceinline__ DF df_add(DF x, DF y) {
-  DF s = two_sum(x.hi, y.hi);
-  const DF t = two_sum(x.lo, y.lo);
-  s = fast_sum(s.hi, s.lo + t.hi);
-  return fast_sum(s.hi, s.lo + t.lo);
-}
-__device__ __forceinline__ DF df_neg(DF x) { return DF{-x.hi, -x.lo}; }
-__device__ __forceinline__ DF df_sub(DF x, DF y) { return df_add(x, df_neg(y)); }
-__device__ __forceinline__ DF df_mul(DF x, DF y) {
-  const float p = x.hi * y.hi;
-  float e = fmaf(x.hi, y.hi, -p);
-  e = fmaf(x.hi, y.lo, fmaf(x.lo, y.hi, e));
-  return fast_sum(p, e);
-}
-__device__ __forceinline__ DF df_scale(DF x, float pow2) { return DF{x.hi * pow2, x.lo * pow2}; }
-__device__ __forceinline__ DF df_of(double v) {
-  const float2 t = eifd::split(v);
-  return fast_sum(t.x, t.y);
-}
-__device__ __forceinline__ double df_to_double(DF x) { return eifd::f2d(x.hi) + eifd::f2d(x.lo); }
-
-__device__ __forceinline__ CDF cdf_add(CDF a, CDF b) { return CDF{df_add(a.re, b.re), df_add(a.im, b.im)}; }
-__device__ __forceinline__ CDF cdf_sub(CDF a, CDF b) { return CDF{df_sub(a.re, b.re), df_sub(a.im, b.im)}; }
 __device__ __forceinline__ CDF cdf_mul(CDF a, CDF b) {
-  return CDF{df_sub(df_mul(a.re, b.re), df_mul(a.im, b.im)), df_add(df_mul(a.re, b.im), df_mul(a.im, b.re))};
+  return CDF{df_dot2(a.re, b.re, a.im, b.im, -1.f), df_dot2(a.re, b.im, a.im, b.re, 1.f)};
 }
 __device__ __forceinline__ CDF cdf_conj(CDF a) { return CDF{a.re, df_neg(a.im)}; }
 __device__ __forceinline__ CDF cdf_mul_i(CDF a, int sign) {
@@ -465,7 +468,8 @@ __device__ CDF *fft_smem_df(CDF *x, CDF *y, const FftDesc &d, const float4 *__re
 }
 
 struct Dct2ArgsDF {
-  const double *ux, *uy, *dux, *duy;
+  const double *ux, *uy;
+  const float *dux, *duy;   // IBM field response in single precision
   const float *coef;   // [12 + 2 rk] = hi, lo of 1/(gamma dt)
   double *qhat;
   const float4 *tw, *rot, *wn;
@@ -482,18 +486,19 @@ __global__ void __launch_bounds__(256) k_dct2_df(Dct2ArgsDF a) {
   const int j = 1 + blockIdx.x;
   const DF inv = DF{__ldg(a.coef + 12 + 2 * a.rk), __ldg(a.coef + 13 + 2 * a.rk)};
   for (int i = 1 + threadIdx.x; i <= n; i += blockDim.x) {
-    DF uxm = df_of(__ldg(a.ux + ux_idx(i, j, ld))), uxp = df_of(__ldg(a.ux + ux_idx(i + 1, j, ld)));
-    DF uym = df_of(__ldg(a.uy + uy_idx(i, j, ld))), uyp = df_of(__ldg(a.uy + uy_idx(i, j + 1, ld)));
+    // differences of neighbouring doubles (exact), then double-float
+    DF dux_ = df_of(__ldg(a.ux + ux_idx(i + 1, j, ld)) - __ldg(a.ux + ux_idx(i, j, ld)));
+    DF duy_ = df_of(__ldg(a.uy + uy_idx(i, j + 1, ld)) - __ldg(a.uy + uy_idx(i, j, ld)));
     if (a.with_ibm) {
+      // (u + (d0 + de)/2) - (u + (dw + d0)/2) with single-precision field values:
+      // the increments (de - dw)/2 and (en - ds)/2 as exact float sums
       const int c = uy_idx(i, j, ld);
-      const DF dw = df_of(__ldg(a.dux + c - 1)), d0 = df_of(__ldg(a.dux + c)), de = df_of(__ldg(a.dux + c + 1));
-      if (i >= 2) uxm = df_add(uxm, df_scale(df_add(dw, d0), 0.5f));
-      if (i + 1 <= n) uxp = df_add(uxp, df_scale(df_add(d0, de), 0.5f));
-      const DF ds = df_of(__ldg(a.duy + c - ld)), e0 = df_of(__ldg(a.duy + c)), en = df_of(__ldg(a.duy + c + ld));
-      uym = df_add(uym, df_scale(df_add(ds, e0), 0.5f));
-      uyp = df_add(uyp, df_scale(df_add(e0, en), 0.5f));
+      const float dw = (i >= 2) ? __ldg(a.dux + c - 1) : -__ldg(a.dux + c);
+      const float de = (i + 1 <= n) ? __ldg(a.dux + c + 1) : -__ldg(a.dux + c);
+      dux_ = df_add_nw(dux_, df_scale(two_sum(de, -dw), 0.5f));
+      duy_ = df_add_nw(duy_, df_scale(two_sum(__ldg(a.duy + c + ld), -__ldg(a.duy + c - ld)), 0.5f));
     }
-    q[i - 1] = df_mul(inv, df_add(df_mul(df_sub(uxp, uxm), a.rdx), df_mul(df_sub(uyp, uym), a.rdy)));
+    q[i - 1] = df_mul(inv, df_add_nw(df_mul(dux_, a.rdx), df_mul(duy_, a.rdy)));
   }
   __syncthreads();
   CDF *x = smd, *y = smd + m;
@@ -506,23 +511,29 @@ __global__ void __launch_bounds__(256) k_dct2_df(Dct2ArgsDF a) {
   __syncthreads();
   const CDF *Z = fft_smem_df(x, y, a.fd, a.tw, -1);
   double *out = a.qhat + (size_t)(j - 1) * ld;
-  for (int k = threadIdx.x; k < n; k += blockDim.x) {
-    const int kk = k <= m ? k : n - k;
+  // outputs k and n - k share the half-length spectrum values (conjugate pair)
+  for (int kk = threadIdx.x; kk <= m; kk += blockDim.x) {
     const CDF zk = Z[kk % m];
     const CDF zm = cdf_conj(Z[(m - kk) % m]);
     const CDF sm = cdf_add(zk, zm), df = cdf_sub(zk, zm);
     const CDF e = CDF{df_scale(sm.re, 0.5f), df_scale(sm.im, 0.5f)};
     const CDF o = CDF{df_scale(df.im, 0.5f), df_scale(df_neg(df.re), 0.5f)};  // (zk - zm) / 2i
-    CDF v = cdf_add(e, cdf_mul(cdf_load(a.wn, kk), o));
-    if (k > m) v = cdf_conj(v);
-    const CDF r = cdf_load(a.rot, k);
-    const DF re = df_sub(df_mul(r.re, v.re), df_mul(r.im, v.im));
-    out[k] = df_to_double(df_scale(re, 2.f));
+    const CDF v = cdf_add(e, cdf_mul(cdf_load(a.wn, kk), o));
+    {
+      const CDF r = cdf_load(a.rot, kk);
+      out[kk] = df_to_double(df_scale(df_dot2(r.re, v.re, r.im, v.im, -1.f), 2.f));
+    }
+    if (kk > 0 && kk < m) {
+      // v conjugated for k = n - kk
+      const CDF r = cdf_load(a.rot, n - kk);
+      out[n - kk] = df_to_double(df_scale(df_dot2(r.re, v.re, r.im, df_neg(v.im), -1.f), 2.f));
+    }
   }
 }
 
 struct Dct3ArgsDF {
-  const double *qhat, *iface, *g;
+  const double *qhat, *iface;
+  const float2 *g;   // tdm_g as (hi, lo)
   double *psi;
   const float4 *tw, *rot, *wn;
   FftDesc fd;
@@ -548,10 +559,10 @@ __global__ void __launch_bounds__(256) k_dct3_df(Dct3ArgsDF a) {
         v = df_of(__ldg(a.iface + (size_t)b * n + k));
       } else {
         // y + s_left g + s_right h in double-float from the double-precision block solution
-        const DF gl = df_of(__ldg(a.g + (size_t)r * n + k));
-        const DF gr = df_of(__ldg(a.g + (size_t)(M - 2 - r) * n + k));
-        v = df_add(df_add(df_of(__ldg(row + k)), df_mul(df_of(__ldg(a.iface + (size_t)bm * n + k)), gl)),
-                   df_mul(df_of(__ldg(a.iface + (size_t)b * n + k)), gr));
+        const float2 gl = __ldg(a.g + (size_t)r * n + k);
+        const float2 gr = __ldg(a.g + (size_t)(M - 2 - r) * n + k);
+        v = df_add_nw(df_add_nw(df_of(__ldg(row + k)), df_mul(df_of(__ldg(a.iface + (size_t)bm * n + k)), DF{gl.x, gl.y})),
+                      df_mul(df_of(__ldg(a.iface + (size_t)b * n + k)), DF{gr.x, gr.y}));
       }
       xr[k] = v;
     }
@@ -567,7 +578,7 @@ __global__ void __launch_bounds__(256) k_dct3_df(Dct3ArgsDF a) {
     const CDF w1 = cdf_mul(r1, CDF{xr[t1], df_neg(xr[n - t1])});
     const CDF sum = cdf_add(w0, w1);
     const CDF dif = cdf_mul(cdf_sub(w0, w1), cdf_conj(cdf_load(a.wn, s)));
-    x[s] = CDF{df_sub(sum.re, dif.im), df_add(sum.im, dif.re)};
+    x[s] = CDF{df_add_nw(sum.re, df_neg(dif.im)), df_add_nw(sum.im, dif.re)};
   }
   __syncthreads();
   const CDF *z = fft_smem_df(x, y, a.fd, a.tw, +1);
@@ -720,6 +731,14 @@ int poisson_init(eif_ctx *c) {
     EIF_CK(c, up_load((void **)&pp.tdm_inv, inv.data(), sizeof(double) * inv.size()));
     EIF_CK(c, up_load((void **)&pp.tdm_up, up.data(), sizeof(double) * up.size()));
     EIF_CK(c, up_load((void **)&pp.tdm_g, g.data(), sizeof(double) * g.size()));
+    {
+      std::vector<float2> gdf(g.size());
+      for (size_t q = 0; q < g.size(); q++) {
+        const float hi = (float)g[q];
+        gdf[q] = make_float2(hi, (float)(g[q] - (double)hi));
+      }
+      EIF_CK(c, up_load((void **)&pp.tdm_g_df, gdf.data(), sizeof(float2) * gdf.size()));
+    }
     EIF_CK(c, up_load((void **)&pp.red_inv, rinv.data(), sizeof(double) * rinv.size()));
     EIF_CK(c, up_load((void **)&pp.red_up, rup.data(), sizeof(double) * rup.size()));
     EIF_CK(c, up_load((void **)&pp.red_q1, rq1.data(), sizeof(double) * rq1.size()));
@@ -728,8 +747,9 @@ int poisson_init(eif_ctx *c) {
   } else {
     EIF_CK(c, cudaMalloc((void **)&pp.ywork, sizeof(double) * 2 * (size_t)jt * n));
   }
-  const size_t red_smem = sizeof(double) * RED_COLS * (pp.blk > 0 ? pp.nblk : 1);
-  if (red_smem > 227 * 1024) return fail(c, EIF_ERR_ARG, "jtot %d needs too many tridiagonal blocks", jt);
+  const int rcols = red_cols(pp.blk > 0 ? pp.nblk : 1);
+  if (rcols == 0) return fail(c, EIF_ERR_ARG, "jtot %d needs too many tridiagonal blocks", jt);
+  const size_t red_smem = red_smem_bytes(pp.blk > 0 ? pp.nblk : 1, rcols);
   if (red_smem > 48 * 1024) {
     EIF_CK(c, cudaFuncSetAttribute(k_tdm_reduced, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)red_smem));
   }
@@ -745,7 +765,7 @@ int poisson_init(eif_ctx *c) {
 
 void poisson_free(eif_ctx *c) {
   PoissonPlan &pp = c->pp;
-  void *ptrs[] = {pp.tw, pp.rot, pp.wn, pp.tw_f, pp.rot_f, pp.wn_f, pp.lam, pp.tdm_inv, pp.tdm_up, pp.tdm_g,
+  void *ptrs[] = {pp.tw, pp.rot, pp.wn, pp.tw_f, pp.rot_f, pp.wn_f, pp.lam, pp.tdm_inv, pp.tdm_up, pp.tdm_g, pp.tdm_g_df,
                   pp.red_inv, pp.red_up, pp.red_q1, pp.red_coef, pp.ywork};
   for (void *p : ptrs) if (p) cudaFree(p);
   pp = PoissonPlan{};
@@ -770,7 +790,8 @@ int launch_potential(eif_ctx *c, int rk, bool with_ibm) {
   if (mixed) {
     Dct2ArgsDF a;
     a.ux = c->ux[c->cur]; a.uy = c->uy[c->cur];
-    a.dux = c->dux; a.duy = c->duy; a.coef = c->d_coef;
+    a.dux = reinterpret_cast<const float *>(c->dux); a.duy = reinterpret_cast<const float *>(c->duy);
+    a.coef = c->d_coef;
     a.qhat = c->qhat;
     a.tw = pp.tw_f; a.rot = pp.rot_f; a.wn = pp.wn_f;
     a.fd = fd;
@@ -807,8 +828,9 @@ int launch_potential(eif_ctx *c, int rk, bool with_ibm) {
       k_tdm_local<4><<<g, 128, 0, c->stream>>>(c->qhat, pp.tdm_inv, pp.tdm_up, iface, first, l, n, pp.nblk, c->ld);
     }
     EIF_LAUNCH_CK(c);
-    k_tdm_reduced<<<(n + RED_COLS - 1) / RED_COLS, RED_COLS, sizeof(double) * RED_COLS * pp.nblk, c->stream>>>(
-        iface, first, pp.red_inv, pp.red_up, pp.red_q1, pp.red_coef, l, n, pp.nblk);
+    const int rcols = red_cols(pp.nblk);
+    k_tdm_reduced<<<(n + rcols - 1) / rcols, RED_THREADS, red_smem_bytes(pp.nblk, rcols), c->stream>>>(
+        iface, first, pp.red_inv, pp.red_up, pp.red_q1, pp.red_coef, l, n, pp.nblk, rcols);
     EIF_LAUNCH_CK(c);
   } else {
     EIF_PROF(c, "poisson_tdm", 1);
@@ -817,7 +839,7 @@ int launch_potential(eif_ctx *c, int rk, bool with_ibm) {
   }
   if (mixed) {
     Dct3ArgsDF a;
-    a.qhat = c->qhat; a.iface = iface; a.g = pp.tdm_g;
+    a.qhat = c->qhat; a.iface = iface; a.g = pp.tdm_g_df;
     a.psi = c->psi;
     a.tw = pp.tw_f; a.rot = pp.rot_f; a.wn = pp.wn_f;
     a.fd = fd;
