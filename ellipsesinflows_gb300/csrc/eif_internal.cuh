@@ -110,6 +110,7 @@ struct eif_ctx {
   // particles
   int np, pcap;
   double *P;                    // EIF_NFIELDS * pcap
+  int ibm_ctas_per_sm[2] = {0, 0};  // resident CTAs per SM of the IBM work kernels (FP64, mixed)
   float4 *cpf = nullptr;        // pcap: single-precision x + dx, y + dy, max(a, b) for the collision prefilter
   // immersed-boundary work
   int *box;                     // per particle: 3 images x {imin,imax,jmin,jmax}

@@ -137,9 +137,12 @@ struct Bounds {
 
 // Per-particle single-precision parameters of the mixed-precision indicator,
 // PF_WORDS words per particle (see k_boxes).
-constexpr int PF_WORDS = 24;
+constexpr int PF_WORDS = 28;
 enum { PF_A, PF_B, PF_CZ, PF_SZ, PF_KEX, PF_KEY, PF_RPM, PF_RPIM, PF_UX, PF_UY, PF_VZ, PF_GX, PF_I0,
-       PF_J0, PF_GY = PF_J0 + 3 };
+       PF_J0, PF_GY = PF_J0 + 3,
+       // 1/a, 1/b and the squared thresholds of the far-cell test (see far_side_f)
+       PF_IA = PF_GY + 3, PF_IB, PF_TRO, PF_TR2O, PF_TRI, PF_TR2I };
+static_assert(PF_TR2I < PF_WORDS && PF_WORDS % 4 == 0, "per-particle parameter block");
 
 struct BoxArgs {
   const double *P;
@@ -196,6 +199,16 @@ __global__ void k_boxes(BoxArgs a) {
       q[PF_J0 + m] = __int_as_float(j0);
       q[PF_GY + m] = (float)(sy - j0 + 0.5);
     }
+    // far-cell test in squared form: outside if rho >= 1 + md/mn or r >= mx + md,
+    // inside if rho <= 1 - md/mn or r <= mn - md (md = the far distance)
+    const double mn = fmin(pa, pb), mx = fmax(pa, pb);
+    const double md = FAR_CELLS_F * fmin(a.dx, a.dy);
+    q[PF_IA] = (float)(1. / pa);
+    q[PF_IB] = (float)(1. / pb);
+    q[PF_TRO] = (float)((1. + md / mn) * (1. + md / mn));
+    q[PF_TR2O] = (float)((mx + md) * (mx + md));
+    q[PF_TRI] = md < mn ? (float)((1. - md / mn) * (1. - md / mn)) : -1.f;
+    q[PF_TR2I] = md < mn ? (float)((mn - md) * (mn - md)) : -1.f;
   }
   int cells = 0;
   for (int per = -1; per <= 1; per++) {
@@ -258,6 +271,7 @@ __device__ __forceinline__ int find_particle(const int *__restrict__ off, int np
 
 // map a particle-local cell index to (i, j, image) using its boxes
 __device__ __forceinline__ bool cell_of(const int *bx, int k, int &i, int &j, int &img) {
+#pragma unroll
   for (int m = 0; m < 3; m++) {
     const int w = bx[4 * m + 1] - bx[4 * m + 0] + 1;
     const int h = bx[4 * m + 3] - bx[4 * m + 2] + 1;
@@ -375,10 +389,13 @@ __global__ void __launch_bounds__(256) k_ibm_work(WorkArgs a) {
     for (int half = 0; half < CHUNK / 32; half++) {
       const int i = ci[half], j = cj[half], img = cimg[half];
       double2 contrib = make_double2(0., 0.);
-      if (cin[half]) {
+      // cells of weight exactly zero (inertia: far outside; exchange: any far cell) are skipped
+      const double th_ = th2[half];
+      const bool live = a.mode == 0 ? th_ != -1. : fabs(th_) != 1.;
+      if (cin[half] && live) {
         const double py_ = py + a.ly * img;
         const double x = __ldg(a.xc + i), y = __ldg(a.yc + j);
-        const double th = th2[half];
+        const double th = th_;
         const double uxf = 0.5 * (__ldg(a.ux + j * ld + (i - 1)) + __ldg(a.ux + j * ld + i));
         const double uyf = 0.5 * (__ldg(a.uy + j * ld + i) + __ldg(a.uy + (j + 1) * ld + i));
         if (a.mode == 0) {
@@ -431,21 +448,25 @@ struct EllF {
   float a, b, cz, sz, kex, key;
 };
 
+// The reference's iteration (ellipse.c:30-65) in single precision. Its fixed point
+// is the normal foot whatever the accuracy of the intermediate sin/cos and square
+// roots, so the loop uses the hardware approximations (__sincosf, rsqrtf); the
+// distance at the converged angle is evaluated with the accurate sincosf, and the
+// distance is stationary in the angle.
 __device__ __forceinline__ float normal_t_f(const EllF &e, float x_, float y_) {
   const float px = fabsf(x_), py = fabsf(y_);
   float t = 0.78539816339744831f;
   for (int n = 0; n < NORMAL_MAX_F; n++) {
     float st, ct;
-    sincosf(t, &st, &ct);
+    __sincosf(t, &st, &ct);
     const float x = e.a * ct, y = e.b * st;
     const float ex = e.kex * (ct * ct * ct), ey = e.key * (st * st * st);
     const float rx = x - ex, ry = y - ey, qx = px - ex, qy = py - ey;
-    const float r = sqrtf(ry * ry + rx * rx);
-    const float q = sqrtf(qy * qy + qx * qx);
-    const float arg = fminf(fmaxf((rx * qy - ry * qx) / (r * q), -1.f), 1.f);
-    const float dc = r * asinf(arg);
+    const float r2 = ry * ry + rx * rx, q2 = qy * qy + qx * qx;
+    const float arg = fminf(fmaxf((rx * qy - ry * qx) * rsqrtf(r2 * q2), -1.f), 1.f);
+    const float dc = r2 * rsqrtf(r2) * asinf(arg);
     // a^2 + b^2 - x^2 - y^2 written without cancellation
-    const float dt = dc / sqrtf(e.a * e.a * (st * st) + e.b * e.b * (ct * ct));
+    const float dt = dc * rsqrtf(e.a * e.a * (st * st) + e.b * e.b * (ct * ct));
     t += dt;
     t = fminf(1.5707963267948966f, t);
     t = fmaxf(0.f, t);
@@ -456,27 +477,32 @@ __device__ __forceinline__ float normal_t_f(const EllF &e, float x_, float y_) {
   return t;
 }
 
-// signed distance in grid units from the offset (X, Y) = (x - px, y - py)
-__device__ __forceinline__ int far_side_f(float x_, float y_, float a, float b, float min_dist) {
-  const float mn = fminf(a, b), mx = fmaxf(a, b);
-  const float rho = sqrtf((x_ / a) * (x_ / a) + (y_ / b) * (y_ / b));
-  const float r = sqrtf(x_ * x_ + y_ * y_);
-  if (rho > 1.f) return fmaxf(mn * (rho - 1.f), r - mx) >= min_dist ? -1 : 0;
-  return fmaxf(mn * (1.f - rho), mn - r) >= min_dist ? 1 : 0;
+// Far cells from the squared gauge rho2 = (x/a)^2 + (y/b)^2 and r2 = x^2 + y^2
+// against per-particle thresholds (the bounds of far_side): -1 far outside,
+// +1 far inside, 0 near.
+__device__ __forceinline__ int far_side_f(float rho2, float r2, float tro, float tr2o, float tri, float tr2i) {
+  if (rho2 >= tro || r2 >= tr2o) return -1;
+  if (rho2 <= tri || r2 <= tr2i) return 1;
+  return 0;
 }
 
-__device__ __forceinline__ float signed_dist_body_f(const EllF &e, float x_, float y_, float rh) {
+// tanh(2 d / h) of the signed distance (positive inside), d from the body-frame
+// offset; tanh through one exponential, accurate to a few units of 1e-7 absolute
+__device__ __forceinline__ float indicator_f(const EllF &e, float x_, float y_, float rh) {
   const float f0 = 1.f - (x_ / e.a) * (x_ / e.a) - (y_ / e.b) * (y_ / e.b);
-  const float sign = f0 > 0.f ? 1.f : -1.f;
   const float t = normal_t_f(e, x_, y_);
   float st, ct;
   sincosf(t, &st, &ct);
   const float dxx = e.a * ct - x_, dyy = e.b * st - y_;
-  return sign * sqrtf(dxx * dxx + dyy * dyy) * rh;
+  // |2d/h|; tanh is 1 in single precision beyond 10, the clamp keeps exp finite
+  const float z = fminf(2.f * sqrtf(dxx * dxx + dyy * dyy) * rh, 20.f);
+  const float ez = __expf(2.f * z);
+  const float th = __fdividef(ez - 1.f, ez + 1.f);
+  return f0 > 0.f ? th : -th;
 }
 
 // one warp per chunk, single precision (see k_ibm_work for the decomposition)
-__global__ void __launch_bounds__(256) k_ibm_work_f(WorkArgs a) {
+__global__ void __launch_bounds__(256, 3) k_ibm_work_f(WorkArgs a) {
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -498,12 +524,13 @@ __global__ void __launch_bounds__(256) k_ibm_work_f(WorkArgs a) {
     const int bx[12] = {bA.x, bA.y, bA.z, bA.w, bB.x, bB.y, bB.z, bB.w, bC.x, bC.y, bC.z, bC.w};
     const float4 *q4 = reinterpret_cast<const float4 *>(a.pf + (size_t)PF_WORDS * n);
     const float4 qA = __ldg(q4), qB = __ldg(q4 + 1), qC = __ldg(q4 + 2), qD = __ldg(q4 + 3), qE = __ldg(q4 + 4);
+    const float4 qF = __ldg(q4 + 5), qG = __ldg(q4 + 6);
+    const float ia = qE.w, ib = qF.x, tro = qF.y, tr2o = qF.z, tri = qF.w, tr2i = qG.x;
     EllF e;
     e.a = qA.x; e.b = qA.y; e.cz = qA.z; e.sz = qA.w; e.kex = qB.x; e.key = qB.y;
     const float rpm = qB.z, rpim = qB.w, pux = qC.x, puy = qC.y, pvz = qC.z, gx = qC.w;
     const int i0 = __float_as_int(qD.x);
-    const int j0s[3] = {__float_as_int(qD.y), __float_as_int(qD.z), __float_as_int(qD.w)};
-    const float gys[3] = {qE.x, qE.y, qE.z};
+    const int j0m = __float_as_int(qD.y), j00 = __float_as_int(qD.z), j0p = __float_as_int(qD.w);
     // pass 1: cells of the chunk, body-frame offsets, far cells settled
     int ci[2], cj[2], rank[2];
     float cX[2], cY[2], th2[2];
@@ -526,11 +553,15 @@ __global__ void __launch_bounds__(256) k_ibm_work_f(WorkArgs a) {
       if (in) {
         const int m = img + 1;
         const float X = ((float)(ci[half] - i0) - gx) * dxf;
-        const float Y = ((float)(cj[half] - j0s[m]) - gys[m]) * dyf;
+        // image row origin and fraction selected without a local array
+        const int j0i = m == 0 ? j0m : (m == 1 ? j00 : j0p);
+        const float gyi = m == 0 ? qE.x : (m == 1 ? qE.y : qE.z);
+        const float Y = ((float)(cj[half] - j0i) - gyi) * dyf;
         cX[half] = X; cY[half] = Y;
         x_ = e.cz * X - e.sz * Y;
         y_ = e.sz * X + e.cz * Y;
-        const int side = far_side_f(x_, y_, e.a, e.b, FAR_CELLS_F / rh);
+        const float xa = x_ * ia, yb = y_ * ib;
+        const int side = far_side_f(xa * xa + yb * yb, x_ * x_ + y_ * y_, tro, tr2o, tri, tr2i);
         th2[half] = (float)side;
         near = side == 0;
       }
@@ -543,7 +574,7 @@ __global__ void __launch_bounds__(256) k_ibm_work_f(WorkArgs a) {
     __syncwarp();
     for (int k = lane; k < nnear; k += 32) {
       const float2 o = slots[k];
-      slots[k].x = tanhf(2.f * signed_dist_body_f(e, o.x, o.y, rh));
+      slots[k].x = indicator_f(e, o.x, o.y, rh);
     }
     __syncwarp();
 #pragma unroll
@@ -555,8 +586,11 @@ __global__ void __launch_bounds__(256) k_ibm_work_f(WorkArgs a) {
     for (int half = 0; half < CHUNK / 32; half++) {
       const int i = ci[half], j = cj[half];
       float2 contrib = make_float2(0.f, 0.f);
-      if (cin[half]) {
-        const float X = cX[half], Y = cY[half], th = th2[half];
+      // cells of weight exactly zero (inertia: far outside; exchange: any far cell) are skipped
+      const float th_ = th2[half];
+      const bool live = a.mode == 0 ? th_ != -1.f : fabsf(th_) != 1.f;
+      if (cin[half] && live) {
+        const float X = cX[half], Y = cY[half], th = th_;
         const float uxs = eifd::d2f(__ldg(a.ux + j * ld + (i - 1))) + eifd::d2f(__ldg(a.ux + j * ld + i));
         const float uys = eifd::d2f(__ldg(a.uy + j * ld + i)) + eifd::d2f(__ldg(a.uy + (j + 1) * ld + i));
         if (a.mode == 0) {
@@ -879,7 +913,19 @@ static int launch_work(eif_ctx *c, int mode, int cn) {
   w.dx_f = (float)c->dx;
   w.dy_f = (float)c->dy;
   w.dxdy_f = (float)(c->dx * c->dy);
-  const int blocks = std::max(1, std::min(c->sms * 8, (c->chunk_cap * 32 + 255) / 256));
+  // persistent grid: as many CTAs as are resident at once (queried once per context)
+  const bool mixed = c->cfg.precision == EIF_PREC_MIXED;
+  int &per_sm = c->ibm_ctas_per_sm[mixed ? 1 : 0];
+  if (per_sm == 0) {
+    int v = 0;
+    if (mixed) {
+      EIF_CK(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_ibm_work_f, 256, 0));
+    } else {
+      EIF_CK(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_ibm_work, 256, 0));
+    }
+    per_sm = std::max(1, v);
+  }
+  const int blocks = std::max(1, std::min(c->sms * per_sm, (c->chunk_cap * 32 + 255) / 256));
   {
     EIF_PROF(c, mode == 0 ? "ibm_inertia" : "ibm_exchange", 1);
     if (c->cfg.precision == EIF_PREC_MIXED) {
