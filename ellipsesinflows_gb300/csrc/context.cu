@@ -47,6 +47,19 @@ int check_records(eif_ctx *c) {
   return fail(c, EIF_ERR_CUDA, "bounds guard %llu: index %llu outside [0, %llu)", tag, idx, bound);
 }
 
+// the part of an RK stage before the particle sub-iterations (src/main.c:14-31)
+int rk_stage_front(eif_ctx *c, int rk) {
+  int rc;
+  const bool ibm = c->np > 0;
+  if ((rc = launch_reset_increments(c))) return rc;
+  if ((rc = launch_inertia(c, 0))) return rc;
+  if ((rc = launch_predictor(c, rk))) return rc;
+  if (ibm && (rc = launch_exchange(c))) return rc;
+  if ((rc = launch_potential(c, rk, ibm))) return rc;
+  if ((rc = launch_correct(c, rk, ibm, true))) return rc;
+  return launch_collision(c, 0);
+}
+
 }  // namespace eif
 
 using namespace eif;
@@ -180,14 +193,7 @@ bool valid_rk(int rk) { return rk >= 0 && rk < 3; }
 // one RK stage of integrate (src/main.c:14-53); *sub receives the sub-iterations
 int rk_stage(eif_ctx *c, int rk, int *sub) {
   int rc;
-  const bool ibm = c->np > 0;
-  if ((rc = launch_reset_increments(c))) return rc;
-  if ((rc = launch_inertia(c, 0))) return rc;
-  if ((rc = launch_predictor(c, rk))) return rc;
-  if (ibm && (rc = launch_exchange(c))) return rc;
-  if ((rc = launch_potential(c, rk, ibm))) return rc;
-  if ((rc = launch_correct(c, rk, ibm, true))) return rc;
-  if ((rc = launch_collision(c, 0))) return rc;
+  if ((rc = rk_stage_front(c, rk))) return rc;
   int s = 0;
   for (s = 0;; s++) {
     if ((rc = launch_inertia(c, 1))) return rc;
@@ -251,6 +257,8 @@ int eif_create(const eif_config_t *cfg, eif_ctx **out) {
   CK_CREATE(cudaMemset(c->d_coef, 0, sizeof(float) * 32));
   CK_CREATE(cudaMalloc((void **)&c->d_scal, sizeof(double) * 4));
   CK_CREATE(cudaMemset(c->d_scal, 0, sizeof(double) * 4));
+  CK_CREATE(cudaMalloc((void **)&c->d_inc, sizeof(unsigned long long) * 2));
+  CK_CREATE(cudaMemset(c->d_inc, 0, sizeof(unsigned long long) * 2));
   CK_CREATE(cudaMalloc((void **)&c->d_flags, sizeof(unsigned)));
   CK_CREATE(cudaMemset(c->d_flags, 0, sizeof(unsigned)));
   CK_CREATE(cudaMallocHost((void **)&c->h_scal, sizeof(double) * 4));
@@ -260,6 +268,7 @@ int eif_create(const eif_config_t *cfg, eif_ctx **out) {
   CK_CREATE(cudaMalloc((void **)&c->d_check, sizeof(unsigned long long) * 4));
   CK_CREATE(cudaMemset(c->d_check, 0, sizeof(unsigned long long) * 4));
   c->sync_debug = getenv("EIF_SYNC_DEBUG") != nullptr;
+  c->use_graphs = getenv("EIF_NO_GRAPHS") == nullptr;
 #undef CK_CREATE
   rc = poisson_init(c);
   if (rc) return rc;
@@ -282,6 +291,8 @@ int eif_destroy(eif_ctx *c) {
   if (c->d_coef) cudaFree(c->d_coef);
   if (c->cpf) cudaFree(c->cpf);
   if (c->rdxc_df) cudaFree(c->rdxc_df);
+  if (c->d_inc) cudaFree(c->d_inc);
+  graphs_free(c);
   float *fptrs[] = {c->rdxf_f, c->rdxc_f, c->cxm_f, c->cxp_f, c->cym_f, c->cyp_f, c->sxf[0], c->sxf[1], c->syf[0],
                     c->syf[1]};
   for (float *p : fptrs) if (p) cudaFree(p);
@@ -341,6 +352,8 @@ int eif_pull_fluid(eif_ctx *c, double *ux, double *uy, double *p, double *psi) {
 
 int eif_push_particles(eif_ctx *c, int n, const double *rec) {
   if (!c || n < 0 || (n > 0 && !rec)) return EIF_ERR_ARG;
+  // the step graphs hold the particle count and buffers: rebuild them on the next advance
+  graphs_free(c);
   int rc = ensure_pcap(c, n);
   if (rc) return rc;
   std::vector<double> soa((size_t)EIF_NFIELDS * c->pcap, 0.);
@@ -480,6 +493,18 @@ int eif_integrate(eif_ctx *c, int *substeps) {
 int eif_advance(eif_ctx *c, int nsteps) {
   if (!c || nsteps < 0) return EIF_ERR_ARG;
   if (!c->fluid_pushed) return fail(c, EIF_ERR_STATE, "push the fluid state before integrating");
+  if (c->use_graphs && !c->sync_debug && !c->prof.enabled) {
+    // one graph launch and one synchronisation per step (see graph.cu)
+    for (int s = 0; s < nsteps; s++) {
+      int rc = step_graph_launch(c);
+      if (rc) return rc;
+      rc = sync_scalars(c);
+      if (rc) return rc;
+      c->step += 1;
+      c->time += c->dt_host;
+    }
+    return EIF_OK;
+  }
   for (int s = 0; s < nsteps; s++) {
     int rc = launch_decide_dt(c);
     if (rc) return rc;

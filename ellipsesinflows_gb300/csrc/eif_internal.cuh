@@ -110,6 +110,17 @@ struct eif_ctx {
   // particles
   int np, pcap;
   double *P;                    // EIF_NFIELDS * pcap
+  // particle sub-iteration: [0] residual accumulator (IEEE bits), [1] loop counter (low word)
+  unsigned long long *d_inc = nullptr;
+  // step graphs (eif_advance): one per parity of the double-buffer indices at the step's start
+  struct StepGraph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int cur0 = -1, scur0 = -1, cur1 = 0, scur1 = 0;
+  } graphs[2];
+  bool use_graphs = true;
+  bool in_loop = false;                      // capturing the body of a sub-iteration loop
+  cudaGraphConditionalHandle loop_handle = 0;
   int ibm_ctas_per_sm[2] = {0, 0};  // resident CTAs per SM of the IBM work kernels (FP64, mixed)
   float4 *cpf = nullptr;        // pcap: single-precision x + dx, y + dy, max(a, b) for the collision prefilter
   // immersed-boundary work
@@ -157,6 +168,11 @@ struct ProfScope {
 #define EIF_PROF(c, name, kernels) eif::ProfScope eif_prof_scope_((c), (name), (kernels))
 int profile_flush(eif_ctx *c);
 int check_records(eif_ctx *c);
+// ---- step graphs (graph.cu) ----
+int step_graph_launch(eif_ctx *c);
+void graphs_free(eif_ctx *c);
+int rk_stage_front(eif_ctx *c, int rk);
+int ibm_prepare(eif_ctx *c);
 void profile_free(eif_ctx *c);
 
 // ---- launch helpers ----

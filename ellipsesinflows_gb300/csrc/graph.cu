@@ -1,0 +1,153 @@
+// Step graphs: one time step of eif_advance as a single CUDA graph.
+//
+// The graph holds, in launch order, the dt decision and for each RK stage the
+// stage kernels, a conditional WHILE node whose body is one particle
+// sub-iteration (inertia at the increment, collisions, increments), and the
+// particle update (src/main.c:13-53). k_increment_done sets the loop condition
+// on the device from the residual and the sub-iteration count, so a step needs
+// no host round trip; the host synchronises once per step to read dt and the
+// error flags. The kernels and their order are those of the host-driven path
+// (rk_stage), so both paths give bit-identical results.
+//
+// The stage kernels swap the double-buffered velocity and source arrays, so the
+// buffers a step touches depend on the buffer indices at its start; one graph
+// is kept per starting pair of indices (at most two occur). Graphs are rebuilt
+// after the particle buffers are reallocated.
+#include "eif_internal.cuh"
+#include <vector>
+
+namespace eif {
+
+namespace {
+
+int end_capture(eif_ctx *c, std::vector<cudaGraphNode_t> *sinks) {
+  if (sinks) {
+    cudaStreamCaptureStatus st;
+    const cudaGraphNode_t *deps = nullptr;
+    size_t n = 0;
+    cudaError_t e = cudaStreamGetCaptureInfo(c->stream, &st, nullptr, nullptr, &deps, nullptr, &n);
+    if (e == cudaSuccess) sinks->assign(deps, deps + n);
+    cudaGraph_t g = nullptr;
+    cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
+    if (e != cudaSuccess) return check_cuda(c, e, "cudaStreamGetCaptureInfo");
+    if (e2 != cudaSuccess) return check_cuda(c, e2, "cudaStreamEndCapture");
+    return EIF_OK;
+  }
+  cudaGraph_t g = nullptr;
+  EIF_CK(c, cudaStreamEndCapture(c->stream, &g));
+  return EIF_OK;
+}
+
+// abandon a capture after an error, leaving the stream usable
+void abort_capture(eif_ctx *c) {
+  cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(c->stream, &st) == cudaSuccess && st != cudaStreamCaptureStatusNone) {
+    cudaGraph_t g = nullptr;
+    cudaStreamEndCapture(c->stream, &g);
+  }
+  cudaGetLastError();
+  c->in_loop = false;
+}
+
+int build(eif_ctx *c, eif_ctx::StepGraph &sg) {
+  int rc = ibm_prepare(c);
+  if (rc) return rc;
+  const int cur0 = c->cur, scur0 = c->scur;
+  cudaGraph_t g = nullptr;
+  EIF_CK(c, cudaGraphCreate(&g, 0));
+  auto fail_out = [&](int code) {
+    abort_capture(c);
+    c->cur = cur0;
+    c->scur = scur0;
+    cudaGraphDestroy(g);
+    return code;
+  };
+  std::vector<cudaGraphNode_t> sinks;
+  cudaError_t e = cudaStreamBeginCaptureToGraph(c->stream, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return fail_out(check_cuda(c, e, "cudaStreamBeginCaptureToGraph"));
+  if ((rc = launch_decide_dt(c))) return fail_out(rc);
+  for (int rk = 0; rk < 3; rk++) {
+    if ((rc = rk_stage_front(c, rk))) return fail_out(rc);
+    // the sub-iteration counter starts at zero for every stage
+    e = cudaMemsetAsync(reinterpret_cast<unsigned *>(c->d_inc + 1), 0, sizeof(unsigned), c->stream);
+    if (e != cudaSuccess) return fail_out(check_cuda(c, e, "cudaMemsetAsync"));
+    if ((rc = end_capture(c, &sinks))) return fail_out(rc);
+    cudaGraphConditionalHandle h;
+    e = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault);
+    if (e != cudaSuccess) return fail_out(check_cuda(c, e, "cudaGraphConditionalHandleCreate"));
+    cudaGraphNodeParams p = {};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = h;
+    p.conditional.type = cudaGraphCondTypeWhile;
+    p.conditional.size = 1;
+    cudaGraphNode_t loop = nullptr;
+    e = cudaGraphAddNode(&loop, g, sinks.data(), nullptr, sinks.size(), &p);
+    if (e != cudaSuccess) return fail_out(check_cuda(c, e, "cudaGraphAddNode (while)"));
+    cudaGraph_t body = p.conditional.phGraph_out[0];
+    e = cudaStreamBeginCaptureToGraph(c->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return fail_out(check_cuda(c, e, "cudaStreamBeginCaptureToGraph (body)"));
+    c->in_loop = true;
+    c->loop_handle = h;
+    if ((rc = launch_inertia(c, 1))) return fail_out(rc);
+    if ((rc = launch_collision(c, 1))) return fail_out(rc);
+    if ((rc = launch_increment(c, rk))) return fail_out(rc);
+    c->in_loop = false;
+    if ((rc = end_capture(c, nullptr))) return fail_out(rc);
+    e = cudaStreamBeginCaptureToGraph(c->stream, g, &loop, nullptr, 1, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return fail_out(check_cuda(c, e, "cudaStreamBeginCaptureToGraph (after loop)"));
+    if ((rc = launch_update_particles(c))) return fail_out(rc);
+  }
+  if ((rc = end_capture(c, nullptr))) return fail_out(rc);
+  cudaGraphExec_t exec = nullptr;
+  e = cudaGraphInstantiate(&exec, g, 0);
+  if (e != cudaSuccess) {
+    c->cur = cur0;
+    c->scur = scur0;
+    cudaGraphDestroy(g);
+    return check_cuda(c, e, "cudaGraphInstantiate");
+  }
+  sg.graph = g;
+  sg.exec = exec;
+  sg.cur0 = cur0;
+  sg.scur0 = scur0;
+  sg.cur1 = c->cur;
+  sg.scur1 = c->scur;
+  // nothing has run yet: the step starts from the original buffers
+  c->cur = cur0;
+  c->scur = scur0;
+  return EIF_OK;
+}
+
+}  // namespace
+
+void graphs_free(eif_ctx *c) {
+  for (auto &sg : c->graphs) {
+    if (sg.exec) cudaGraphExecDestroy(sg.exec);
+    if (sg.graph) cudaGraphDestroy(sg.graph);
+    sg = eif_ctx::StepGraph{};
+  }
+}
+
+int step_graph_launch(eif_ctx *c) {
+  eif_ctx::StepGraph *sg = nullptr;
+  for (auto &g : c->graphs) {
+    if (g.exec && g.cur0 == c->cur && g.scur0 == c->scur) sg = &g;
+  }
+  if (!sg) {
+    for (auto &g : c->graphs) {
+      if (!g.exec) { sg = &g; break; }
+    }
+    if (!sg) {
+      graphs_free(c);
+      sg = &c->graphs[0];
+    }
+    int rc = build(c, *sg);
+    if (rc) return rc;
+  }
+  EIF_CK(c, cudaGraphLaunch(sg->exec, c->stream));
+  c->cur = sg->cur1;
+  c->scur = sg->scur1;
+  return EIF_OK;
+}
+
+}  // namespace eif

@@ -441,7 +441,10 @@ __global__ void __launch_bounds__(256) k_ibm_work(WorkArgs a) {
 // per-cell arithmetic is single precision without cancellation. The normal
 // foot iteration is the reference's (ellipse.c:30-65) with a stopping threshold
 // suited to single precision.
-constexpr float NORMAL_TOL_F = 2.e-6f;
+// The distance at the foot is stationary in t, so an angle error dt changes it by
+// O(a dt^2): stopping once the step is below 1e-3 leaves distance errors near 1e-9
+// cells (checked against fully converged iterations over the aspect ratios 1-3).
+constexpr float NORMAL_TOL_F = 1.e-3f;
 constexpr int NORMAL_MAX_F = 24;
 
 struct EllF {
@@ -820,6 +823,16 @@ static size_t box_cells_bound(const eif_ctx *c, double r) {
   return (size_t)wc * (size_t)hc;
 }
 
+// resident CTAs per SM of the IBM work kernels (a host query; done before any graph capture)
+int ibm_prepare(eif_ctx *c) {
+  int v = 0;
+  EIF_CK(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_ibm_work, 256, 0));
+  c->ibm_ctas_per_sm[0] = std::max(1, v);
+  EIF_CK(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_ibm_work_f, 256, 0));
+  c->ibm_ctas_per_sm[1] = std::max(1, v);
+  return EIF_OK;
+}
+
 int ibm_reserve(eif_ctx *c) {
   // called after a particle push: size the chunk and scratch buffers from the radii
   ibm_free(c);
@@ -914,17 +927,12 @@ static int launch_work(eif_ctx *c, int mode, int cn) {
   w.dy_f = (float)c->dy;
   w.dxdy_f = (float)(c->dx * c->dy);
   // persistent grid: as many CTAs as are resident at once (queried once per context)
-  const bool mixed = c->cfg.precision == EIF_PREC_MIXED;
-  int &per_sm = c->ibm_ctas_per_sm[mixed ? 1 : 0];
-  if (per_sm == 0) {
-    int v = 0;
-    if (mixed) {
-      EIF_CK(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_ibm_work_f, 256, 0));
-    } else {
-      EIF_CK(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_ibm_work, 256, 0));
-    }
-    per_sm = std::max(1, v);
+  const int per_sm_idx = c->cfg.precision == EIF_PREC_MIXED ? 1 : 0;
+  if (c->ibm_ctas_per_sm[per_sm_idx] == 0) {
+    int rc = ibm_prepare(c);
+    if (rc) return rc;
   }
+  const int per_sm = c->ibm_ctas_per_sm[per_sm_idx];
   const int blocks = std::max(1, std::min(c->sms * per_sm, (c->chunk_cap * 32 + 255) / 256));
   {
     EIF_PROF(c, mode == 0 ? "ibm_inertia" : "ibm_exchange", 1);

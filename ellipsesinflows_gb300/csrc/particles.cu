@@ -18,6 +18,7 @@
 // partners that pass are evaluated one per lane and summed in partner order.
 #include "eif_internal.cuh"
 #include <cfloat>
+#include <algorithm>
 
 namespace {
 
@@ -304,12 +305,15 @@ __global__ void k_reset(double *__restrict__ P, int pcap, int np) {
   P[EIF_P_DX * pcap + n] = 0.; P[EIF_P_DY * pcap + n] = 0.; P[EIF_P_DAZ * pcap + n] = 0.;
 }
 
-// increment.c:10-72: one block; residual = max |change of the increments|
+// increment.c:10-72; residual = max |change of the increments|, combined over
+// blocks as an integer max of the IEEE bits of non-negative doubles (independent
+// of the order). The FP64 work is spread over many SMs: one SM alone has only a
+// few FP64 lanes.
 __global__ void k_increment(double *__restrict__ P, int pcap, int np, double gamma, double Fr2,
-                            double *__restrict__ scal) {
+                            const double *__restrict__ scal, unsigned long long *__restrict__ res_bits) {
   const double dt = scal[0];
   double res = 0.;
-  for (int n = threadIdx.x; n < np; n += blockDim.x) {
+  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < np; n += gridDim.x * blockDim.x) {
     double *p = P;
     const double den = p[EIF_P_DEN * pcap + n];
     const double px = p[EIF_P_DUX * pcap + n], py = p[EIF_P_DUY * pcap + n], pz = p[EIF_P_DVZ * pcap + n];
@@ -337,7 +341,21 @@ __global__ void k_increment(double *__restrict__ P, int pcap, int np, double gam
   __syncthreads();
   if (threadIdx.x == 0) {
     for (int w = 1; w < (int)(blockDim.x >> 5); w++) res = fmax(res, s[w]);
-    scal[1] = res;
+    if (res > 0.) atomicMax(res_bits, (unsigned long long)__double_as_longlong(res));
+  }
+}
+
+// Publishes the residual, clears the accumulator, and, inside a step graph, sets
+// the condition of the sub-iteration loop: continue while the residual is not
+// below 1e-8 and at most 101 sub-iterations have run (main.c:32-49).
+__global__ void k_increment_done(unsigned long long *__restrict__ res_bits, double *__restrict__ scal,
+                                 unsigned *__restrict__ counter, cudaGraphConditionalHandle handle, int use_handle) {
+  const double res = __longlong_as_double((long long)*res_bits);
+  *res_bits = 0ull;
+  scal[1] = res;
+  if (use_handle) {
+    const unsigned count = ++*counter;
+    cudaGraphSetConditional(handle, (!(res < 1.e-8) && count <= 101u) ? 1u : 0u);
   }
 }
 
@@ -385,8 +403,13 @@ int launch_reset_increments(eif_ctx *c) {
 
 int launch_increment(eif_ctx *c, int rk) {
   const double Fr = c->cfg.Fr;
-  EIF_PROF(c, "particle_increment", 1);
-  k_increment<<<1, 1024, 0, c->stream>>>(c->P, c->pcap, c->np, rk_coef(rk).gamma, Fr * Fr, c->d_scal);
+  EIF_PROF(c, "particle_increment", 2);
+  const int blocks = std::max(1, std::min((c->np + 127) / 128, c->sms * 4));
+  k_increment<<<blocks, 128, 0, c->stream>>>(c->P, c->pcap, c->np, rk_coef(rk).gamma, Fr * Fr, c->d_scal,
+                                             c->d_inc);
+  EIF_LAUNCH_CK(c);
+  k_increment_done<<<1, 1, 0, c->stream>>>(c->d_inc, c->d_scal, reinterpret_cast<unsigned *>(c->d_inc + 1),
+                                           c->loop_handle, c->in_loop ? 1 : 0);
   EIF_LAUNCH_CK(c);
   return EIF_OK;
 }
