@@ -122,6 +122,7 @@ struct eif_ctx {
   bool in_loop = false;                      // capturing the body of a sub-iteration loop
   cudaGraphConditionalHandle loop_handle = 0;
   int ibm_ctas_per_sm[2] = {0, 0};  // resident CTAs per SM of the IBM work kernels (FP64, mixed)
+  unsigned *band_marks = nullptr;  // per band of 8 rows: bitmap over the 3*np (particle, image) boxes
   float4 *cpf = nullptr;        // pcap: single-precision x + dx, y + dy, max(a, b) for the collision prefilter
   // immersed-boundary work
   int *box;                     // per particle: 3 images x {imin,imax,jmin,jmax}

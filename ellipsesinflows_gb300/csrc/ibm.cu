@@ -11,11 +11,11 @@
 //   compute_inertia                src/suspensions/inertia.c:9-70
 //
 // Work decomposition. For every particle the reference visits, for the
-// periodic images -1, 0, +1, the cells of a clipped bounding box. Here those
-// cells are enumerated in the same (image, j, i) order and cut into chunks of
-// CHUNK cells. One warp evaluates one chunk (two cells per lane) inside a
-// persistent grid sized to the SM count, so particles of any size keep all
-// SMs busy. Per-particle sums are reduced per chunk with warp shuffles and
+// periodic images -1, 0, +1, the cells of a clipped bounding box. Here every
+// box row is one task (rows wider than CHUNK cells are cut into segments of
+// CHUNK cells); tasks are numbered in the reference's (image, j, i) order. One
+// warp evaluates one task (two cells per lane) inside a persistent grid sized
+// to the SM count, so particles of any size keep all SMs busy. Per-particle sums are reduced per chunk with warp shuffles and
 // then per particle over its chunks in a fixed order: results are
 // deterministic. The momentum exchange also stores each box cell's field
 // contribution in a scratch buffer; a tile gather then adds, for every cell,
@@ -32,7 +32,8 @@
 
 namespace {
 
-constexpr int CHUNK = 64;       // cells per warp task
+constexpr int CHUNK = 64;       // cells per warp task (a box row, or a segment of one)
+__device__ __host__ __forceinline__ int box_segs(int w) { return (w + CHUNK - 1) / CHUNK; }
 constexpr int NEXTRA = 3;       // auxiliary.c:8
 constexpr double BETA = 2.;     // auxiliary.c:49
 constexpr int GTX = 64, GTY = 8, GTHREADS = 256;  // gather tile and block
@@ -98,19 +99,9 @@ __device__ __forceinline__ double signed_dist_body(const Ell &e, double x_, doub
 // at least min(a,b) |rho - 1|, and at least r - max(a,b) outside / min(a,b) - r
 // inside (r = |(x, y)|). When that bound times 2/h reaches the value at which
 // tanh rounds to +-1 in the working precision, the weights are exactly those of
-// the saturated tanh and the normal-foot iteration is not needed. Returns 0 for
-// a near cell, +1 for a far interior cell, -1 for a far exterior cell.
-__device__ __forceinline__ int far_side(double x_, double y_, double a, double b, double min_dist) {
-  const double mn = fmin(a, b), mx = fmax(a, b);
-  const double rho2 = (x_ / a) * (x_ / a) + (y_ / b) * (y_ / b);
-  const double rho = sqrt(rho2);
-  const double r = sqrt(x_ * x_ + y_ * y_);
-  if (rho > 1.) {
-    return fmax(mn * (rho - 1.), r - mx) >= min_dist ? -1 : 0;
-  }
-  return fmax(mn * (1. - rho), mn - r) >= min_dist ? 1 : 0;
-}
-
+// the saturated tanh and the normal-foot iteration is not needed. row_chords
+// turns these bounds into column ranges of a box row.
+//
 // double-precision tanh(2d) equals +-1 exactly for |2d| >= 20 (the correction
 // 2/(exp(2|x|)+1) is below half an ulp of 1); with a margin for rounding of the bound
 constexpr double FAR_CELLS_D = 10.5;
@@ -140,9 +131,9 @@ struct Bounds {
 constexpr int PF_WORDS = 28;
 enum { PF_A, PF_B, PF_CZ, PF_SZ, PF_KEX, PF_KEY, PF_RPM, PF_RPIM, PF_UX, PF_UY, PF_VZ, PF_GX, PF_I0,
        PF_J0, PF_GY = PF_J0 + 3,
-       // 1/a, 1/b and the squared thresholds of the far-cell test (see far_side_f)
-       PF_IA = PF_GY + 3, PF_IB, PF_TRO, PF_TR2O, PF_TRI, PF_TR2I };
-static_assert(PF_TR2I < PF_WORDS && PF_WORDS % 4 == 0, "per-particle parameter block");
+       // quadratic form of the ellipse in the lab frame and the far-cell scales (row_chords)
+       PF_AL = PF_GY + 3, PF_KA, PF_DE, PF_SO2, PF_SI2, PF_RO2 };
+static_assert(PF_RO2 < PF_WORDS && PF_WORDS % 4 == 0, "per-particle parameter block");
 
 struct BoxArgs {
   const double *P;
@@ -199,18 +190,18 @@ __global__ void k_boxes(BoxArgs a) {
       q[PF_J0 + m] = __int_as_float(j0);
       q[PF_GY + m] = (float)(sy - j0 + 0.5);
     }
-    // far-cell test in squared form: outside if rho >= 1 + md/mn or r >= mx + md,
-    // inside if rho <= 1 - md/mn or r <= mn - md (md = the far distance)
+    // rho^2 = al X^2 + 2 ka X Y + de Y^2 for lab-frame offsets (X, Y); far-cell scales
     const double mn = fmin(pa, pb), mx = fmax(pa, pb);
     const double md = FAR_CELLS_F * fmin(a.dx, a.dy);
-    q[PF_IA] = (float)(1. / pa);
-    q[PF_IB] = (float)(1. / pb);
-    q[PF_TRO] = (float)((1. + md / mn) * (1. + md / mn));
-    q[PF_TR2O] = (float)((mx + md) * (mx + md));
-    q[PF_TRI] = md < mn ? (float)((1. - md / mn) * (1. - md / mn)) : -1.f;
-    q[PF_TR2I] = md < mn ? (float)((mn - md) * (mn - md)) : -1.f;
+    const double so = 1. + md / mn, si = 1. - md / mn;
+    q[PF_AL] = (float)(cz * cz / (pa * pa) + sz * sz / (pb * pb));
+    q[PF_KA] = (float)(cz * sz * (1. / (pb * pb) - 1. / (pa * pa)));
+    q[PF_DE] = (float)(sz * sz / (pa * pa) + cz * cz / (pb * pb));
+    q[PF_SO2] = (float)(so * so);
+    q[PF_SI2] = si > 0. ? (float)(si * si) : -1.f;
+    q[PF_RO2] = (float)((mx + md) * (mx + md));
   }
-  int cells = 0;
+  int tasks = 0;
   for (int per = -1; per <= 1; per++) {
     int imin, imax, jmin, jmax;
     loop_size(1, a.itot, a.dx, r, px, imin, imax);
@@ -218,10 +209,10 @@ __global__ void k_boxes(BoxArgs a) {
     int *bx = a.box + 12 * n + 4 * (per + 1);
     if (!EIF_CHK(a.bd.rec, 12 * n + 4 * (per + 1) + 3, a.bd.box, 2)) return;
     bx[0] = imin; bx[1] = imax; bx[2] = jmin; bx[3] = jmax;
-    if (imax >= imin && jmax >= jmin) cells += (imax - imin + 1) * (jmax - jmin + 1);
+    if (imax >= imin && jmax >= jmin) tasks += (jmax - jmin + 1) * box_segs(imax - imin + 1);
   }
   if (!EIF_CHK(a.bd.rec, (a.nchunk - a.bd_off_base) + n, a.bd.off, 3)) return;
-  a.nchunk[n] = (cells + CHUNK - 1) / CHUNK;
+  a.nchunk[n] = tasks;
 }
 
 // exclusive scan of the chunk counts (one block); off[np] = total
@@ -259,33 +250,59 @@ __global__ void k_chunk_owner(const int *__restrict__ off, int *__restrict__ own
   }
 }
 
-// locate a chunk's particle: largest n with off[n] <= c
-__device__ __forceinline__ int find_particle(const int *__restrict__ off, int np, int c) {
-  int lo = 0, hi = np - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (__ldg(off + mid) <= c) lo = mid; else hi = mid - 1;
+// A particle's tasks: image by image, row by row, segment by segment.
+struct RowTask {
+  int img, j, ib, ie;   // image -1..1, row, first and last column of the segment
+};
+// one image's box (columns bi0..bi1, rows bj0..bj1): true when task r lies in it,
+// otherwise r is reduced by the image's task count
+__device__ __forceinline__ bool row_task_in(int4 b, int img, int &r, RowTask &t) {
+  const int w = b.y - b.x + 1, h = b.w - b.z + 1;
+  if (w <= 0 || h <= 0) return false;
+  const int segs = box_segs(w);
+  const int cnt = h * segs;
+  if (r >= cnt) {
+    r -= cnt;
+    return false;
   }
-  return lo;
+  const int row = segs == 1 ? r : r / segs;
+  const int seg = r - row * segs;
+  t.img = img;
+  t.j = b.z + row;
+  t.ib = b.x + seg * CHUNK;
+  t.ie = min(t.ib + CHUNK - 1, b.y);
+  return true;
+}
+// task r of a particle whose image boxes are bm, b0, bp (images -1, 0, +1)
+__device__ __forceinline__ bool row_task(int4 bm, int4 b0, int4 bp, int r, RowTask &t) {
+  return row_task_in(bm, -1, r, t) || row_task_in(b0, 0, r, t) || row_task_in(bp, 1, r, t);
 }
 
-// map a particle-local cell index to (i, j, image) using its boxes
-__device__ __forceinline__ bool cell_of(const int *bx, int k, int &i, int &j, int &img) {
-#pragma unroll
-  for (int m = 0; m < 3; m++) {
-    const int w = bx[4 * m + 1] - bx[4 * m + 0] + 1;
-    const int h = bx[4 * m + 3] - bx[4 * m + 2] + 1;
-    if (w <= 0 || h <= 0) continue;
-    const int cnt = w * h;
-    if (k < cnt) {
-      img = m - 1;
-      j = bx[4 * m + 2] + k / w;
-      i = bx[4 * m + 0] + k % w;
-      return true;
-    }
-    k -= cnt;
+// The far-cell bounds above along one row, as ranges of the lab-frame offset
+// X from the centre at the row's offset Y: cells outside (olo, ohi) are far
+// outside (rho >= so or r >= ro), cells in [ilo, ihi] are far inside (rho <= si;
+// the disc r <= mn - md lies inside that ellipse). rho^2 = al X^2 + 2 ka X Y + de Y^2.
+template <typename T>
+__device__ __forceinline__ void row_chords(T al, T ka, T de, T so2, T si2, T ro2, T Y, T &olo, T &ohi, T &ilo,
+                                           T &ihi) {
+  const T big = T(1e30);
+  olo = big; ohi = -big; ilo = big; ihi = -big;
+  const T bY = ka * Y;
+  const T Do = bY * bY - al * (de * Y * Y - so2);
+  const T c2 = ro2 - Y * Y;
+  if (Do > T(0) && c2 > T(0)) {
+    const T sq = sqrt(Do), xc = sqrt(c2);
+    olo = fmax((-bY - sq) / al, -xc);
+    ohi = fmin((-bY + sq) / al, xc);
   }
-  return false;
+  if (si2 > T(0)) {
+    const T Di = bY * bY - al * (de * Y * Y - si2);
+    if (Di >= T(0)) {
+      const T sq = sqrt(Di);
+      ilo = (-bY - sq) / al;
+      ihi = (-bY + sq) / al;
+    }
+  }
 }
 
 struct WorkArgs {
@@ -303,8 +320,8 @@ struct WorkArgs {
   Bounds bd;
 };
 
-// one warp per chunk of box cells: indicator weights, partial sums, and (for
-// the exchange) per-cell field contributions
+// One warp per row task: indicator weights, partial sums, and (for the exchange)
+// per-cell field contributions.
 __global__ void __launch_bounds__(256) k_ibm_work(WorkArgs a) {
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -313,19 +330,21 @@ __global__ void __launch_bounds__(256) k_ibm_work(WorkArgs a) {
   const double rh = 1. / a.h;
   const double dxdy = a.dx * a.dy;
   const double dtv = a.mode == 1 ? __ldg(a.dt) : 0.;
+  const double md = FAR_CELLS_D * a.h;
   const int pc = a.pcap, ld = a.ld;
   // per warp: body-frame offsets of its near cells, overwritten by their weights
   __shared__ double2 slot_buf[8][CHUNK];
   double2 *slots = slot_buf[threadIdx.x >> 5];
   for (int c = warp; c < total; c += nwarps) {
-    const int n = find_particle(a.off, a.np, c);
+    if (!EIF_CHK(a.bd.rec, c, a.bd.partial / 3, 21)) continue;
+    const int n = __ldg(a.owner + c);
     if (!EIF_CHK(a.bd.rec, n, a.np, 11)) continue;
     if (!EIF_CHK(a.bd.rec, 12 * n + 11, a.bd.box, 12)) continue;
     if (!EIF_CHK(a.bd.rec, EIF_P_VZ * pc + n, a.bd.P, 13)) continue;
-    const int local0 = (c - __ldg(a.off + n)) * CHUNK;
-    int bx[12];
-#pragma unroll
-    for (int q = 0; q < 12; q++) bx[q] = __ldg(a.box + 12 * n + q);
+    const int4 *b4 = reinterpret_cast<const int4 *>(a.box + 12 * n);
+    const int4 bA = __ldg(b4), bB = __ldg(b4 + 1), bC = __ldg(b4 + 2);
+    RowTask t;
+    const bool task = row_task(bA, bB, bC, c - __ldg(a.off + n), t) && EIF_CHK(a.bd.rec, t.j, a.bd.yc - 1, 15);
     const double *P = a.P;
     const double pden = __ldg(P + EIF_P_DEN * pc + n), pa = __ldg(P + EIF_P_A * pc + n), pb = __ldg(P + EIF_P_B * pc + n);
     double px = __ldg(P + EIF_P_X * pc + n), py = __ldg(P + EIF_P_Y * pc + n), paz = __ldg(P + EIF_P_AZ * pc + n);
@@ -339,34 +358,50 @@ __global__ void __launch_bounds__(256) k_ibm_work(WorkArgs a) {
     const double pim = pmoi(pden, pa, pb);
     const double pux = __ldg(P + EIF_P_UX * pc + n), puy = __ldg(P + EIF_P_UY * pc + n), pvz = __ldg(P + EIF_P_VZ * pc + n);
     const Ell e = make_ell(pa, pb, px, py, paz);
-    // pass 1: cells of the chunk, body-frame offsets, far cells settled
-    int ci[2], cj[2], cimg[2], rank[2];
+    const double py_ = py + a.ly * (task ? t.img : 0);
+    const int j = task ? t.j : 1;
+    const double y = __ldg(a.yc + j);
+    const double Y = y - py_;
+    // far cells of this row (row_chords), in single precision: the far distance
+    // (10.5 cells) exceeds the saturation distance of tanh (9.53 cells) by far more
+    // than the rounding of the column bounds
+    float olo, ohi, ilo, ihi;
+    {
+      const float fa = eifd::d2f(pa), fb = eifd::d2f(pb), cz = eifd::d2f(e.cz), sz = eifd::d2f(e.sz);
+      const float mn = fminf(fa, fb), mx = fmaxf(fa, fb), fmd = eifd::d2f(md);
+      const float so = 1.f + fmd / mn, si = 1.f - fmd / mn;
+      const float al = cz * cz / (fa * fa) + sz * sz / (fb * fb);
+      const float ka = cz * sz * (1.f / (fb * fb) - 1.f / (fa * fa));
+      const float de = sz * sz / (fa * fa) + cz * cz / (fb * fb);
+      row_chords(al, ka, de, so * so, si > 0.f ? si * si : -1.f, (mx + fmd) * (mx + fmd), eifd::d2f(Y), olo, ohi,
+                 ilo, ihi);
+    }
+    // pass 1: cells of the row, far cells settled, body-frame offsets of the near ones
+    int rank[2];
     bool cin[2];
     double th2[2];
     unsigned near_mask[2];
 #pragma unroll
     for (int half = 0; half < CHUNK / 32; half++) {
-      const int kk = local0 + half * 32 + lane;
-      bool in = cell_of(bx, kk, ci[half], cj[half], cimg[half]);
+      const int i = (task ? t.ib : 1) + half * 32 + lane;
+      bool in = task && i <= t.ie;
       if (in) {
-        const int i = ci[half], j = cj[half];
-        in = EIF_CHK(a.bd.rec, i, a.bd.xc - 1, 14) && EIF_CHK(a.bd.rec, j, a.bd.yc - 1, 15) &&
-             EIF_CHK(a.bd.rec, j * ld + i, a.bd.field, 16) && EIF_CHK(a.bd.rec, (j + 1) * ld + i, a.bd.field, 17) &&
-             EIF_CHK(a.bd.rec, j * ld + (i - 1), a.bd.field, 18);
+        in = EIF_CHK(a.bd.rec, i, a.bd.xc - 1, 14) && EIF_CHK(a.bd.rec, j * ld + i, a.bd.field, 16) &&
+             EIF_CHK(a.bd.rec, (j + 1) * ld + i, a.bd.field, 17) && EIF_CHK(a.bd.rec, j * ld + (i - 1), a.bd.field, 18);
       }
       cin[half] = in;
       bool near = false;
       double x_ = 0., y_ = 0.;
       th2[half] = 0.;
       if (in) {
-        const double x = __ldg(a.xc + ci[half]), y = __ldg(a.yc + cj[half]);
-        const double ddx = x - e.px, ddy = y - (py + a.ly * cimg[half]);
-        x_ = e.cz * ddx - e.sz * ddy;
-        y_ = e.sz * ddx + e.cz * ddy;
-        const int side = far_side(x_, y_, e.a, e.b, FAR_CELLS_D * a.h);
+        const double X = __ldg(a.xc + i) - e.px;
+        const float Xf = eifd::d2f(X);
         // reference sign convention: +1 inside (auxiliary.c:36-38); tanh saturated
+        const int side = !(Xf > olo && Xf < ohi) ? -1 : ((Xf >= ilo && Xf <= ihi) ? 1 : 0);
         th2[half] = (double)side;
         near = side == 0;
+        x_ = e.cz * X - e.sz * Y;
+        y_ = e.sz * X + e.cz * Y;
       }
       near_mask[half] = __ballot_sync(0xffffffffu, near);
       rank[half] = (half ? __popc(near_mask[0]) : 0) + __popc(near_mask[half] & ((1u << lane) - 1u));
@@ -387,14 +422,13 @@ __global__ void __launch_bounds__(256) k_ibm_work(WorkArgs a) {
     double s0 = 0., s1 = 0., s2 = 0.;
 #pragma unroll
     for (int half = 0; half < CHUNK / 32; half++) {
-      const int i = ci[half], j = cj[half], img = cimg[half];
+      const int i = (task ? t.ib : 1) + half * 32 + lane;
       double2 contrib = make_double2(0., 0.);
       // cells of weight exactly zero (inertia: far outside; exchange: any far cell) are skipped
       const double th_ = th2[half];
       const bool live = a.mode == 0 ? th_ != -1. : fabs(th_) != 1.;
       if (cin[half] && live) {
-        const double py_ = py + a.ly * img;
-        const double x = __ldg(a.xc + i), y = __ldg(a.yc + j);
+        const double x = __ldg(a.xc + i);
         const double th = th_;
         const double uxf = 0.5 * (__ldg(a.ux + j * ld + (i - 1)) + __ldg(a.ux + j * ld + i));
         const double uyf = 0.5 * (__ldg(a.uy + j * ld + i) + __ldg(a.uy + (j + 1) * ld + i));
@@ -480,15 +514,6 @@ __device__ __forceinline__ float normal_t_f(const EllF &e, float x_, float y_) {
   return t;
 }
 
-// Far cells from the squared gauge rho2 = (x/a)^2 + (y/b)^2 and r2 = x^2 + y^2
-// against per-particle thresholds (the bounds of far_side): -1 far outside,
-// +1 far inside, 0 near.
-__device__ __forceinline__ int far_side_f(float rho2, float r2, float tro, float tr2o, float tri, float tr2i) {
-  if (rho2 >= tro || r2 >= tr2o) return -1;
-  if (rho2 <= tri || r2 <= tr2i) return 1;
-  return 0;
-}
-
 // tanh(2 d / h) of the signed distance (positive inside), d from the body-frame
 // offset; tanh through one exponential, accurate to a few units of 1e-7 absolute
 __device__ __forceinline__ float indicator_f(const EllF &e, float x_, float y_, float rh) {
@@ -504,7 +529,7 @@ __device__ __forceinline__ float indicator_f(const EllF &e, float x_, float y_, 
   return f0 > 0.f ? th : -th;
 }
 
-// one warp per chunk, single precision (see k_ibm_work for the decomposition)
+// one warp per row task, single precision (see k_ibm_work)
 __global__ void __launch_bounds__(256, 3) k_ibm_work_f(WorkArgs a) {
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -521,52 +546,51 @@ __global__ void __launch_bounds__(256, 3) k_ibm_work_f(WorkArgs a) {
     if (!EIF_CHK(a.bd.rec, c, a.bd.partial / 3, 51)) continue;
     const int n = __ldg(a.owner + c);
     if (!EIF_CHK(a.bd.rec, n, a.np, 52) || !EIF_CHK(a.bd.rec, 12 * n + 11, a.bd.box, 53)) continue;
-    const int local0 = (c - __ldg(a.off + n)) * CHUNK;
     const int4 *b4 = reinterpret_cast<const int4 *>(a.box + 12 * n);
     const int4 bA = __ldg(b4), bB = __ldg(b4 + 1), bC = __ldg(b4 + 2);
-    const int bx[12] = {bA.x, bA.y, bA.z, bA.w, bB.x, bB.y, bB.z, bB.w, bC.x, bC.y, bC.z, bC.w};
+    RowTask t;
+    const bool task = row_task(bA, bB, bC, c - __ldg(a.off + n), t);
     const float4 *q4 = reinterpret_cast<const float4 *>(a.pf + (size_t)PF_WORDS * n);
     const float4 qA = __ldg(q4), qB = __ldg(q4 + 1), qC = __ldg(q4 + 2), qD = __ldg(q4 + 3), qE = __ldg(q4 + 4);
     const float4 qF = __ldg(q4 + 5), qG = __ldg(q4 + 6);
-    const float ia = qE.w, ib = qF.x, tro = qF.y, tr2o = qF.z, tri = qF.w, tr2i = qG.x;
     EllF e;
     e.a = qA.x; e.b = qA.y; e.cz = qA.z; e.sz = qA.w; e.kex = qB.x; e.key = qB.y;
     const float rpm = qB.z, rpim = qB.w, pux = qC.x, puy = qC.y, pvz = qC.z, gx = qC.w;
     const int i0 = __float_as_int(qD.x);
-    const int j0m = __float_as_int(qD.y), j00 = __float_as_int(qD.z), j0p = __float_as_int(qD.w);
-    // pass 1: cells of the chunk, body-frame offsets, far cells settled
-    int ci[2], cj[2], rank[2];
-    float cX[2], cY[2], th2[2];
+    const int m = task ? t.img + 1 : 1;
+    // image row origin and fraction selected without a local array
+    const int j0i = __float_as_int(m == 0 ? qD.y : (m == 1 ? qD.z : qD.w));
+    const float gyi = m == 0 ? qE.x : (m == 1 ? qE.y : qE.z);
+    const int j = task ? t.j : 1;
+    const float Y = ((float)(j - j0i) - gyi) * dyf;
+    // far cells of this row (PF_AL .. PF_RO2: al, ka, de, so^2, si^2, ro^2)
+    float olo, ohi, ilo, ihi;
+    row_chords(qE.w, qF.x, qF.y, qF.z, qF.w, qG.x, Y, olo, ohi, ilo, ihi);
+    // pass 1: cells of the row, far cells settled, body-frame offsets of the near ones
+    int rank[2];
+    float cX[2], th2[2];
     bool cin[2];
     unsigned near_mask[2];
 #pragma unroll
     for (int half = 0; half < CHUNK / 32; half++) {
-      const int kk = local0 + half * 32 + lane;
-      int img;
-      bool in = cell_of(bx, kk, ci[half], cj[half], img);
+      const int i = (task ? t.ib : 1) + half * 32 + lane;
+      bool in = task && i <= t.ie;
       if (in) {
-        const int i = ci[half], j = cj[half];
         in = EIF_CHK(a.bd.rec, j * ld + i, a.bd.field, 54) && EIF_CHK(a.bd.rec, (j + 1) * ld + i, a.bd.field, 55) &&
              EIF_CHK(a.bd.rec, j * ld + (i - 1), a.bd.field, 56);
       }
       cin[half] = in;
       bool near = false;
       float x_ = 0.f, y_ = 0.f;
-      cX[half] = 0.f; cY[half] = 0.f; th2[half] = 0.f;
+      const float X = ((float)(i - i0) - gx) * dxf;
+      cX[half] = X;
+      th2[half] = 0.f;
       if (in) {
-        const int m = img + 1;
-        const float X = ((float)(ci[half] - i0) - gx) * dxf;
-        // image row origin and fraction selected without a local array
-        const int j0i = m == 0 ? j0m : (m == 1 ? j00 : j0p);
-        const float gyi = m == 0 ? qE.x : (m == 1 ? qE.y : qE.z);
-        const float Y = ((float)(cj[half] - j0i) - gyi) * dyf;
-        cX[half] = X; cY[half] = Y;
-        x_ = e.cz * X - e.sz * Y;
-        y_ = e.sz * X + e.cz * Y;
-        const float xa = x_ * ia, yb = y_ * ib;
-        const int side = far_side_f(xa * xa + yb * yb, x_ * x_ + y_ * y_, tro, tr2o, tri, tr2i);
+        const int side = !(X > olo && X < ohi) ? -1 : ((X >= ilo && X <= ihi) ? 1 : 0);
         th2[half] = (float)side;
         near = side == 0;
+        x_ = e.cz * X - e.sz * Y;
+        y_ = e.sz * X + e.cz * Y;
       }
       near_mask[half] = __ballot_sync(0xffffffffu, near);
       rank[half] = (half ? __popc(near_mask[0]) : 0) + __popc(near_mask[half] & ((1u << lane) - 1u));
@@ -587,13 +611,13 @@ __global__ void __launch_bounds__(256, 3) k_ibm_work_f(WorkArgs a) {
     float sacc0 = 0.f, sacc1 = 0.f, sacc2 = 0.f;
 #pragma unroll
     for (int half = 0; half < CHUNK / 32; half++) {
-      const int i = ci[half], j = cj[half];
+      const int i = (task ? t.ib : 1) + half * 32 + lane;
       float2 contrib = make_float2(0.f, 0.f);
       // cells of weight exactly zero (inertia: far outside; exchange: any far cell) are skipped
       const float th_ = th2[half];
       const bool live = a.mode == 0 ? th_ != -1.f : fabsf(th_) != 1.f;
       if (cin[half] && live) {
-        const float X = cX[half], Y = cY[half], th = th_;
+        const float X = cX[half], th = th_;
         const float uxs = eifd::d2f(__ldg(a.ux + j * ld + (i - 1))) + eifd::d2f(__ldg(a.ux + j * ld + i));
         const float uys = eifd::d2f(__ldg(a.uy + j * ld + i)) + eifd::d2f(__ldg(a.uy + (j + 1) * ld + i));
         if (a.mode == 0) {
@@ -659,25 +683,37 @@ __global__ void k_chunk_reduce(const double *__restrict__ partial, const int *__
 }
 
 // Ordered lists of the (particle, image) boxes that reach each band of GTY rows,
-// built once per exchange; entry = 3 * particle + image index, in particle order.
-__global__ void k_band_lists(const int *__restrict__ box, int np, int jtot, int *__restrict__ lists,
+// built once per exchange; entry = 3 * particle + image index, in entry order.
+// Step 1 (one thread per particle): every box sets its bit in the bitmap of each
+// band it reaches (atomicOr: the result does not depend on the order). Step 2
+// (one warp per band): the band's set bits are compacted in index order.
+__global__ void k_band_marks(const int *__restrict__ box, int np, int jtot, unsigned *__restrict__ marks,
+                             int words) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= np) return;
+  const int nbands = (jtot + GTY - 1) / GTY;
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+    const int *bx = box + 12 * n + 4 * q;
+    if (bx[1] < bx[0] || bx[3] < bx[2]) continue;
+    const int e = 3 * n + q;
+    const int b0 = max(0, (bx[2] - 1) / GTY), b1 = min(nbands - 1, (bx[3] - 1) / GTY);
+    for (int b = b0; b <= b1; b++) atomicOr(marks + (size_t)b * words + (e >> 5), 1u << (e & 31));
+  }
+}
+
+__global__ void k_band_lists(const unsigned *__restrict__ marks, int words, int jtot, int *__restrict__ lists,
                              int *__restrict__ counts, int cap, unsigned *__restrict__ flags) {
   const int lane = threadIdx.x & 31;
   const int band = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nbands = (jtot + GTY - 1) / GTY;
   if (band >= nbands) return;
-  const int j0 = 1 + band * GTY, j1 = min(j0 + GTY - 1, jtot);
   int count = 0;
   int *out = lists + (size_t)band * cap;
-  for (int base = 0; base < np; base += 32) {
-    const int n = base + lane;
-    int bits = 0;
-    if (n < np) {
-      for (int q = 0; q < 3; q++) {
-        const int *bx = box + 12 * n + 4 * q;
-        if (bx[1] >= bx[0] && bx[3] >= bx[2] && bx[2] <= j1 && bx[3] >= j0) bits |= 1 << q;
-      }
-    }
+  const unsigned *row = marks + (size_t)band * words;
+  for (int base = 0; base < words; base += 32) {
+    const int w = base + lane;
+    unsigned bits = w < words ? row[w] : 0u;
     const int m = __popc(bits);
     int sc = m;
     for (int o = 1; o < 32; o <<= 1) {
@@ -685,11 +721,11 @@ __global__ void k_band_lists(const int *__restrict__ box, int np, int jtot, int 
       if (lane >= o) sc += v;
     }
     int pos = count + sc - m;
-    for (int q = 0; q < 3; q++) {
-      if (bits & (1 << q)) {
-        if (pos < cap) out[pos] = 3 * n + q;
-        pos++;
-      }
+    while (bits) {
+      const int b = __ffs(bits) - 1;
+      bits &= bits - 1u;
+      if (pos < cap) out[pos] = 32 * w + b;
+      pos++;
     }
     count += __shfl_sync(0xffffffffu, sc, 31);
   }
@@ -715,7 +751,7 @@ struct GatherArgs {
 template <typename V2, typename Acc>
 __global__ void __launch_bounds__(GTHREADS) k_gather(GatherArgs a) {
   const V2 *wbuf = static_cast<const V2 *>(a.wbuf);
-  // per staged entry: columns, rows, row width and offset of the box in the scratch buffer
+  // per staged entry: columns, rows, row pitch and offset of the box in the scratch buffer
   __shared__ int e_i0[LMAX], e_i1[LMAX], e_j0[LMAX], e_j1[LMAX], e_w[LMAX], e_base[LMAX];
   const int i0 = 1 + blockIdx.x * GTX, j0 = 1 + blockIdx.y * GTY;
   const int i1 = min(i0 + GTX - 1, a.itot), j1 = min(j0 + GTY - 1, a.jtot);
@@ -731,22 +767,24 @@ __global__ void __launch_bounds__(GTHREADS) k_gather(GatherArgs a) {
     for (int e = threadIdx.x; e < cnt; e += GTHREADS) {
       const int ent = __ldg(blist + base + e);
       const int n = ent / 3, q = ent - 3 * n;
-      int bi0 = 1, bi1 = 0, bj0 = 1, bj1 = 0, off = 0;
+      int bi0 = 1, bi1 = 0, bj0 = 1, bj1 = 0, off = 0, pitch = 0;
       // entry = 3 * particle + image with 0 <= image < 3; anything else is recorded and skipped
       if (EIF_CHK(a.bd.rec, ent, 3LL * a.np, 46) && EIF_CHK(a.bd.rec, n, a.np, 44) &&
           EIF_CHK(a.bd.rec, 12LL * n + 4 * q + 3, a.bd.box, 45)) {
         const int *bx = a.box + 12 * n;
-        int base_q = 0;
+        // tasks of the earlier images; a box row occupies segs * CHUNK scratch slots
+        int tasks_q = 0;
         for (int m = 0; m < q; m++) {
           const int w = bx[4 * m + 1] - bx[4 * m] + 1, h = bx[4 * m + 3] - bx[4 * m + 2] + 1;
-          if (w > 0 && h > 0) base_q += w * h;
+          if (w > 0 && h > 0) tasks_q += h * box_segs(w);
         }
         bi0 = bx[4 * q]; bi1 = bx[4 * q + 1]; bj0 = bx[4 * q + 2]; bj1 = bx[4 * q + 3];
-        off = __ldg(a.off + n) * CHUNK + base_q;
+        off = (__ldg(a.off + n) + tasks_q) * CHUNK;
+        pitch = bi1 >= bi0 ? box_segs(bi1 - bi0 + 1) * CHUNK : 0;
       }
       // entries that miss this tile's columns are kept (as empty) to preserve the order
       if (bi0 > i1 || bi1 < i0) { bi0 = 1; bi1 = 0; }
-      e_i0[e] = bi0; e_i1[e] = bi1; e_j0[e] = bj0; e_j1[e] = bj1; e_w[e] = bi1 - bi0 + 1; e_base[e] = off;
+      e_i0[e] = bi0; e_i1[e] = bi1; e_j0[e] = bj0; e_j1[e] = bj1; e_w[e] = pitch; e_base[e] = off;
     }
     __syncthreads();
     for (int e = 0; e < cnt; e++) {
@@ -815,12 +853,12 @@ namespace eif {
 // most 2r/h + 2 + 2*NEXTRA + 1 cells per direction before clipping; the three
 // images are shifted by exactly jtot rows, so their clipped row ranges together
 // never exceed the unclipped height.
-static size_t box_cells_bound(const eif_ctx *c, double r) {
+static size_t box_tasks_bound(const eif_ctx *c, double r) {
   const long w = (long)std::ceil(2. * r / c->dx) + 2 + 2 * NEXTRA + 2;
   const long h = (long)std::ceil(2. * r / c->dy) + 2 + 2 * NEXTRA + 2;
   const long wc = std::min<long>(w, c->itot);
   const long hc = std::min<long>(h, 3L * c->jtot);
-  return (size_t)wc * (size_t)hc;
+  return (size_t)hc * (size_t)box_segs((int)wc);
 }
 
 // resident CTAs per SM of the IBM work kernels (a host query; done before any graph capture)
@@ -842,7 +880,7 @@ int ibm_reserve(eif_ctx *c) {
   EIF_CK(c, cudaMemcpy(b.data(), c->P + EIF_P_B * c->pcap, sizeof(double) * c->np, cudaMemcpyDeviceToHost));
   size_t chunks = 0;
   for (int n = 0; n < c->np; n++) {
-    chunks += (box_cells_bound(c, std::max(a[n], b[n])) + CHUNK - 1) / CHUNK;
+    chunks += box_tasks_bound(c, std::max(a[n], b[n]));
   }
   c->chunk_cap = (int)chunks;
   c->wcap = chunks * CHUNK;
@@ -856,6 +894,7 @@ int ibm_reserve(eif_ctx *c) {
   c->band_cap = 3 * c->np;
   EIF_CK(c, cudaMalloc((void **)&c->band_lists, sizeof(int) * (size_t)nbands * c->band_cap));
   EIF_CK(c, cudaMalloc((void **)&c->band_counts, sizeof(int) * (size_t)nbands));
+  EIF_CK(c, cudaMalloc((void **)&c->band_marks, sizeof(unsigned) * (size_t)nbands * ((3 * c->np + 31) / 32)));
   return EIF_OK;
 }
 
@@ -868,7 +907,8 @@ void ibm_free(eif_ctx *c) {
   if (c->owner) cudaFree(c->owner);
   if (c->band_lists) cudaFree(c->band_lists);
   if (c->band_counts) cudaFree(c->band_counts);
-  c->band_lists = nullptr; c->band_counts = nullptr;
+  if (c->band_marks) cudaFree(c->band_marks);
+  c->band_lists = nullptr; c->band_counts = nullptr; c->band_marks = nullptr;
   c->box = nullptr; c->chunk_off = nullptr; c->partial = nullptr; c->wbuf = nullptr;
   c->pf = nullptr; c->owner = nullptr;
   c->chunk_cap = 0; c->wcap = 0;
@@ -899,16 +939,14 @@ static int launch_boxes(eif_ctx *c, bool use_increment) {
   b.pf = c->cfg.precision == EIF_PREC_MIXED ? c->pf : nullptr;
   int *cnt = c->chunk_off + (c->np + 1);
   b.nchunk = cnt;
-  EIF_PROF(c, "ibm_boxes", c->cfg.precision == EIF_PREC_MIXED ? 3 : 2);
+  EIF_PROF(c, "ibm_boxes", 3);
   k_boxes<<<(c->np + 127) / 128, 128, 0, c->stream>>>(b);
   EIF_LAUNCH_CK(c);
   k_scan<<<1, 1024, 0, c->stream>>>(cnt, c->chunk_off, c->np, bounds_of(c));
   EIF_LAUNCH_CK(c);
-  if (c->cfg.precision == EIF_PREC_MIXED) {
-    k_chunk_owner<<<(c->np + 127) / 128, 128, 0, c->stream>>>(c->chunk_off, c->owner, c->np, bounds_of(c),
-                                                               c->chunk_cap);
-    EIF_LAUNCH_CK(c);
-  }
+  k_chunk_owner<<<(c->np + 127) / 128, 128, 0, c->stream>>>(c->chunk_off, c->owner, c->np, bounds_of(c),
+                                                             c->chunk_cap);
+  EIF_LAUNCH_CK(c);
   return EIF_OK;
 }
 
@@ -979,8 +1017,12 @@ int launch_exchange(eif_ctx *c) {
   g.lists = c->band_lists; g.counts = c->band_counts; g.cap = c->band_cap;
   {
     const int nbands = (c->jtot + GTY - 1) / GTY;
-    EIF_PROF(c, "ibm_band_lists", 1);
-    k_band_lists<<<(nbands * 32 + 255) / 256, 256, 0, c->stream>>>(c->box, c->np, c->jtot, c->band_lists,
+    const int words = (3 * c->np + 31) / 32;
+    EIF_PROF(c, "ibm_band_lists", 2);
+    EIF_CK(c, cudaMemsetAsync(c->band_marks, 0, sizeof(unsigned) * (size_t)nbands * words, c->stream));
+    k_band_marks<<<(c->np + 127) / 128, 128, 0, c->stream>>>(c->box, c->np, c->jtot, c->band_marks, words);
+    EIF_LAUNCH_CK(c);
+    k_band_lists<<<(nbands * 32 + 255) / 256, 256, 0, c->stream>>>(c->band_marks, words, c->jtot, c->band_lists,
                                                                      c->band_counts, c->band_cap, c->d_flags);
     EIF_LAUNCH_CK(c);
   }
