@@ -159,7 +159,8 @@ int check_flags(eif_ctx *c) {
   *c->h_flags = 0u;
   EIF_CK(c, cudaMemsetAsync(c->d_flags, 0, sizeof(unsigned), c->stream));
   if (f & EIF_FLAG_NONFINITE) return fail(c, EIF_ERR_NONFINITE, "non-finite velocity detected");
-  if (f & EIF_FLAG_NOCONV) return fail(c, EIF_ERR_NOCONV, "an iteration cap was reached on the device");
+  if (f & EIF_FLAG_NOCONV)
+    return fail(c, EIF_ERR_NOCONV, "an iteration cap or a device list capacity was reached on the device");
   return EIF_OK;
 }
 
@@ -178,12 +179,18 @@ int ensure_pcap(eif_ctx *c, int n) {
   if (n <= c->pcap && c->P) return EIF_OK;
   if (c->P) cudaFree(c->P);
   if (c->cpf) cudaFree(c->cpf);
+  if (c->cand) cudaFree(c->cand);
+  if (c->cand_n) cudaFree(c->cand_n);
   c->P = nullptr;
   c->cpf = nullptr;
+  c->cand = nullptr;
+  c->cand_n = nullptr;
   const int cap = n > 0 ? n : 1;
   EIF_CK(c, cudaMalloc((void **)&c->P, sizeof(double) * EIF_NFIELDS * (size_t)cap));
   EIF_CK(c, cudaMemset(c->P, 0, sizeof(double) * EIF_NFIELDS * (size_t)cap));
   EIF_CK(c, cudaMalloc((void **)&c->cpf, sizeof(float4) * (size_t)cap));
+  EIF_CK(c, cudaMalloc((void **)&c->cand, sizeof(int) * EIF_CAND_SPLIT * EIF_CAND_CAP * (size_t)cap));
+  EIF_CK(c, cudaMalloc((void **)&c->cand_n, sizeof(int) * EIF_CAND_SPLIT * (size_t)cap));
   c->pcap = cap;
   return EIF_OK;
 }
@@ -292,6 +299,8 @@ int eif_destroy(eif_ctx *c) {
   if (c->cpf) cudaFree(c->cpf);
   if (c->rdxc_df) cudaFree(c->rdxc_df);
   if (c->d_inc) cudaFree(c->d_inc);
+  if (c->cand) cudaFree(c->cand);
+  if (c->cand_n) cudaFree(c->cand_n);
   graphs_free(c);
   float *fptrs[] = {c->rdxf_f, c->rdxc_f, c->cxm_f, c->cxp_f, c->cym_f, c->cyp_f, c->sxf[0], c->sxf[1], c->syf[0],
                     c->syf[1]};

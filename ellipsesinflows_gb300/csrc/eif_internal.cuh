@@ -41,6 +41,11 @@
 #include <vector>
 #include <string>
 
+// collision candidate lists: the partner range is cut into EIF_CAND_SPLIT pieces,
+// each with room for EIF_CAND_CAP candidates per particle (particles.cu)
+#define EIF_CAND_SPLIT 8
+#define EIF_CAND_CAP 16
+
 namespace eif {
 
 // per-kernel event timing of one context
@@ -123,7 +128,8 @@ struct eif_ctx {
   cudaGraphConditionalHandle loop_handle = 0;
   int ibm_ctas_per_sm[2] = {0, 0};  // resident CTAs per SM of the IBM work kernels (FP64, mixed)
   unsigned *band_marks = nullptr;  // per band of 8 rows: bitmap over the 3*np (particle, image) boxes
-  float4 *cpf = nullptr;        // pcap: single-precision x + dx, y + dy, max(a, b) for the collision prefilter
+  float4 *cpf = nullptr;
+  int *cand = nullptr, *cand_n = nullptr;  // collision candidates (np * EIF_CAND_SPLIT * EIF_CAND_CAP), counts        // pcap: single-precision x + dx, y + dy, max(a, b) for the collision prefilter
   // immersed-boundary work
   int *box;                     // per particle: 3 images x {imin,imax,jmin,jmax}
   int *chunk_off;               // per particle: first chunk (exclusive scan), [np] = total

@@ -12,10 +12,10 @@
 //
 // Collision force on particle k accumulates, as in the reference, over the
 // pairs in the order of the pair matrix (partners m = 0..N-1, m != k) and
-// then the walls at x = 0 and x = lx. One warp owns one particle: lanes test
-// 32 partners at a time (a conservative single-precision distance test first,
-// then the exact double-precision bounding-circle test of collision.c:173-189);
-// partners that pass are evaluated one per lane and summed in partner order.
+// then the walls at x = 0 and x = lx. Candidate pairs are found by a tiled scan
+// (a conservative single-precision distance test, then the exact double-precision
+// bounding-circle test of collision.c:173-189); one warp per particle then
+// evaluates its candidates one per lane and sums them in partner order.
 #include "eif_internal.cuh"
 #include <cfloat>
 #include <algorithm>
@@ -222,47 +222,95 @@ __global__ void k_collision_prep(const double *__restrict__ P, int pcap, int np,
   cpf[n] = make_float4(eifd::d2f(v.x), eifd::d2f(v.y), eifd::d2f(fmax(v.a, v.b)), 0.f);
 }
 
-__global__ void __launch_bounds__(CWARPS * 32) k_collision(double *__restrict__ P, const float4 *__restrict__ cpf,
-                                                           int pcap, int np, int cn, double ly, double lx,
-                                                           unsigned *__restrict__ flags) {
-  __shared__ int cand[CWARPS][32];
+// Candidate partners. Block (x, s) tests particles 128x .. 128x+127 against the
+// partners of split s (the partner range cut into CSPLIT pieces, so the O(N^2)
+// scan covers many SMs). Partners' single-precision centres are staged in shared
+// memory; pairs that pass the conservative single-precision test get the exact
+// double-precision bounding-circle test of collision.c:173-189 (canonical
+// orientation), and hits are stored in partner order per (particle, split).
+constexpr int PAIR_TILE = 128;
+constexpr int CSPLIT = EIF_CAND_SPLIT;
+constexpr int CAND_CAP = EIF_CAND_CAP;   // candidates per particle and split
+
+__global__ void __launch_bounds__(PAIR_TILE) k_coll_pairs(const double *__restrict__ P, const float4 *__restrict__ cpf,
+                                                          int pcap, int np, double ly, int *__restrict__ cand,
+                                                          int *__restrict__ cand_n, unsigned *__restrict__ flags) {
+  __shared__ float4 tile[PAIR_TILE];
+  const int k = blockIdx.x * PAIR_TILE + threadIdx.x;
+  const int split = blockIdx.y;
+  const bool on = k < np;
+  const float4 fk = on ? __ldg(cpf + k) : make_float4(0.f, 0.f, 0.f, 0.f);
+  const float lyf = eifd::d2f(ly);
+  const int per_split = (np + CSPLIT - 1) / CSPLIT;
+  const int m0 = split * per_split, m1 = min(np, m0 + per_split);
+  int cnt = 0;
+  for (int base = m0; base < m1; base += PAIR_TILE) {
+    __syncthreads();
+    const int mm = base + threadIdx.x;
+    if (mm < m1) tile[threadIdx.x] = __ldg(cpf + mm);
+    __syncthreads();
+    if (!on) continue;
+    const int nt = min(PAIR_TILE, m1 - base);
+    for (int t = 0; t < nt; t++) {
+      const float4 fm = tile[t];
+      // conservative single-precision test: skip only pairs clearly apart for every image
+      const float rs = fk.z + fm.z;
+      const float dxf = fm.x - fk.x;
+      const float lim = rs * rs * 1.001f + 1e-6f;
+      bool maybe = false;
+#pragma unroll
+      for (int per = -1; per <= 1; per++) {
+        const float dyf = fm.y + lyf * per - fk.y;
+        maybe |= dxf * dxf + dyf * dyf <= lim;
+      }
+      const int m = base + t;
+      if (maybe && m != k) {
+        const PV pk = load_pv(P, pcap, k);
+        const PV pm_ = load_pv(P, pcap, m);
+        const bool hit = m < k ? bounding_overlap(pm_, pk, ly) : bounding_overlap(pk, pm_, ly);
+        if (hit) {
+          if (cnt < CAND_CAP) cand[((size_t)k * CSPLIT + split) * CAND_CAP + cnt] = m;
+          cnt++;
+        }
+      }
+    }
+  }
+  if (on) {
+    cand_n[(size_t)k * CSPLIT + split] = min(cnt, CAND_CAP);
+    if (cnt > CAND_CAP) atomicOr(flags, EIF_FLAG_NOCONV);
+  }
+}
+
+// Collision force on particle k (one warp): its candidate pairs are evaluated one
+// per lane and summed in partner order, then the walls at x = 0 and x = lx.
+__global__ void __launch_bounds__(CWARPS * 32) k_collision(double *__restrict__ P, const int *__restrict__ cand,
+                                                           const int *__restrict__ cand_n, int pcap, int np, int cn,
+                                                           double ly, double lx, unsigned *__restrict__ flags) {
   __shared__ double cval[CWARPS][32][3];
   const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
   const int k = blockIdx.x * CWARPS + wl;
   if (k >= np) return;
+  int ns[CSPLIT];
+  int total = 0;
+#pragma unroll
+  for (int s = 0; s < CSPLIT; s++) {
+    ns[s] = __ldg(cand_n + (size_t)k * CSPLIT + s);
+    total += ns[s];
+  }
   const PV pk = load_pv(P, pcap, k);
-  const float4 fk = __ldg(cpf + k);
-  const float rk = fk.z, xk = fk.x, yk = fk.y, lyf = eifd::d2f(ly);
   double acc0 = 0., acc1 = 0., acc2 = 0.;
   bool ok_all = true;
-  for (int base = 0; base < np; base += 32) {
-    const int m = base + lane;
-    bool hit = false;
-    if (m < np && m != k) {
-      const float4 fm = __ldg(cpf + m);
-      // conservative single-precision test: skip only pairs clearly apart for every image
-      const float rs = rk + fm.z;
-      const float dxf = fm.x - xk;
-      const float lim = rs * rs * 1.001f + 1e-6f;
-      bool maybe = false;
-      for (int per = -1; per <= 1; per++) {
-        const float dyf = fm.y + lyf * per - yk;
-        maybe |= dxf * dxf + dyf * dyf <= lim;
+  for (int base = 0; base < total; base += 32) {
+    const int q = base + lane;
+    const int ncand = min(32, total - base);
+    if (q < total) {
+      // q-th candidate in (split, slot) order
+      int s = 0, r = q;
+#pragma unroll
+      for (int t = 0; t < CSPLIT - 1; t++) {
+        if (s == t && r >= ns[t]) { r -= ns[t]; s = t + 1; }
       }
-      if (maybe) {
-        // exact test with the canonical orientation of the pair
-        const PV pm_ = load_pv(P, pcap, m);
-        hit = m < k ? bounding_overlap(pm_, pk, ly) : bounding_overlap(pk, pm_, ly);
-      }
-    }
-    const unsigned ball = __ballot_sync(0xffffffffu, hit);
-    if (ball == 0u) continue;
-    const int ncand = __popc(ball);
-    const int pos = __popc(ball & ((1u << lane) - 1u));
-    if (hit) cand[wl][pos] = m;
-    __syncwarp();
-    if (lane < ncand) {
-      const int mm = cand[wl][lane];
+      const int mm = __ldg(cand + ((size_t)k * CSPLIT + s) * CAND_CAP + r);
       const PV pmm = load_pv(P, pcap, mm);
       double out[3];
       bool ok;
@@ -275,10 +323,10 @@ __global__ void __launch_bounds__(CWARPS * 32) k_collision(double *__restrict__ 
     }
     __syncwarp();
     if (lane == 0) {
-      for (int q = 0; q < ncand; q++) {
-        acc0 += cval[wl][q][0];
-        acc1 += cval[wl][q][1];
-        acc2 += cval[wl][q][2];
+      for (int t = 0; t < ncand; t++) {
+        acc0 += cval[wl][t][0];
+        acc1 += cval[wl][t][1];
+        acc2 += cval[wl][t][2];
       }
     }
     __syncwarp();
@@ -384,11 +432,14 @@ namespace eif {
 
 int launch_collision(eif_ctx *c, int cn) {
   if (c->np == 0) return EIF_OK;
-  EIF_PROF(c, "collision", 2);
+  EIF_PROF(c, "collision", 3);
   k_collision_prep<<<(c->np + 127) / 128, 128, 0, c->stream>>>(c->P, c->pcap, c->np, c->cpf);
   EIF_LAUNCH_CK(c);
-  k_collision<<<(c->np + CWARPS - 1) / CWARPS, CWARPS * 32, 0, c->stream>>>(c->P, c->cpf, c->pcap, c->np, cn, c->ly,
-                                                                            c->lx, c->d_flags);
+  k_coll_pairs<<<dim3((c->np + PAIR_TILE - 1) / PAIR_TILE, CSPLIT), PAIR_TILE, 0, c->stream>>>(
+      c->P, c->cpf, c->pcap, c->np, c->ly, c->cand, c->cand_n, c->d_flags);
+  EIF_LAUNCH_CK(c);
+  k_collision<<<(c->np + CWARPS - 1) / CWARPS, CWARPS * 32, 0, c->stream>>>(c->P, c->cand, c->cand_n, c->pcap, c->np,
+                                                                            cn, c->ly, c->lx, c->d_flags);
   EIF_LAUNCH_CK(c);
   return EIF_OK;
 }
