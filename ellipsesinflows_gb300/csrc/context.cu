@@ -363,6 +363,8 @@ int eif_push_particles(eif_ctx *c, int n, const double *rec) {
   if (!c || n < 0 || (n > 0 && !rec)) return EIF_ERR_ARG;
   // the step graphs hold the particle count and buffers: rebuild them on the next advance
   graphs_free(c);
+  c->incr_zero = false;
+  c->boxes_x_valid = false;
   int rc = ensure_pcap(c, n);
   if (rc) return rc;
   std::vector<double> soa((size_t)EIF_NFIELDS * c->pcap, 0.);

@@ -53,12 +53,16 @@ int build(eif_ctx *c, eif_ctx::StepGraph &sg) {
   int rc = ibm_prepare(c);
   if (rc) return rc;
   const int cur0 = c->cur, scur0 = c->scur;
+  // the graph must not depend on boxes computed before it: start without them
+  c->boxes_x_valid = false;
+  c->incr_zero = false;
   cudaGraph_t g = nullptr;
   EIF_CK(c, cudaGraphCreate(&g, 0));
   auto fail_out = [&](int code) {
     abort_capture(c);
     c->cur = cur0;
     c->scur = scur0;
+    c->boxes_x_valid = false;
     cudaGraphDestroy(g);
     return code;
   };
@@ -88,6 +92,9 @@ int build(eif_ctx *c, eif_ctx::StepGraph &sg) {
     if (e != cudaSuccess) return fail_out(check_cuda(c, e, "cudaStreamBeginCaptureToGraph (body)"));
     c->in_loop = true;
     c->loop_handle = h;
+    // the body runs repeatedly with changing increments: it always computes its boxes
+    c->incr_zero = false;
+    c->boxes_x_valid = false;
     if ((rc = launch_inertia(c, 1))) return fail_out(rc);
     if ((rc = launch_collision(c, 1))) return fail_out(rc);
     if ((rc = launch_increment(c, rk))) return fail_out(rc);
@@ -112,9 +119,11 @@ int build(eif_ctx *c, eif_ctx::StepGraph &sg) {
   sg.scur0 = scur0;
   sg.cur1 = c->cur;
   sg.scur1 = c->scur;
-  // nothing has run yet: the step starts from the original buffers
+  // nothing has run yet: the step starts from the original buffers; the step ends
+  // with new positions, so no boxes are valid after it
   c->cur = cur0;
   c->scur = scur0;
+  c->boxes_x_valid = false;
   return EIF_OK;
 }
 

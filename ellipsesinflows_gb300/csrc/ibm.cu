@@ -929,6 +929,11 @@ static Bounds bounds_of(const eif_ctx *c) {
 }
 
 static int launch_boxes(eif_ctx *c, bool use_increment) {
+  // boxes at the positions X (no increment, or increments known to be zero) are
+  // reused until the positions or the particle set change
+  const bool x_only = !use_increment || c->incr_zero;
+  if (x_only && c->boxes_x_valid) return EIF_OK;
+  c->boxes_x_valid = false;
   BoxArgs b;
   b.bd = bounds_of(c);
   b.bd_off_base = c->chunk_off;
@@ -940,13 +945,15 @@ static int launch_boxes(eif_ctx *c, bool use_increment) {
   int *cnt = c->chunk_off + (c->np + 1);
   b.nchunk = cnt;
   EIF_PROF(c, "ibm_boxes", 3);
-  k_boxes<<<(c->np + 127) / 128, 128, 0, c->stream>>>(b);
+  // FP64-heavy per particle: small blocks spread the particles over many SMs
+  k_boxes<<<(c->np + 31) / 32, 32, 0, c->stream>>>(b);
   EIF_LAUNCH_CK(c);
   k_scan<<<1, 1024, 0, c->stream>>>(cnt, c->chunk_off, c->np, bounds_of(c));
   EIF_LAUNCH_CK(c);
   k_chunk_owner<<<(c->np + 127) / 128, 128, 0, c->stream>>>(c->chunk_off, c->owner, c->np, bounds_of(c),
                                                              c->chunk_cap);
   EIF_LAUNCH_CK(c);
+  c->boxes_x_valid = x_only;
   return EIF_OK;
 }
 

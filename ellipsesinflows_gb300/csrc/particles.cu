@@ -445,6 +445,7 @@ int launch_collision(eif_ctx *c, int cn) {
 }
 
 int launch_reset_increments(eif_ctx *c) {
+  c->incr_zero = true;
   if (c->np == 0) return EIF_OK;
   EIF_PROF(c, "particle_reset", 1);
   k_reset<<<(c->np + 127) / 128, 128, 0, c->stream>>>(c->P, c->pcap, c->np);
@@ -453,6 +454,7 @@ int launch_reset_increments(eif_ctx *c) {
 }
 
 int launch_increment(eif_ctx *c, int rk) {
+  c->incr_zero = false;
   const double Fr = c->cfg.Fr;
   EIF_PROF(c, "particle_increment", 2);
   const int blocks = std::max(1, std::min((c->np + 127) / 128, c->sms * 4));
@@ -466,6 +468,7 @@ int launch_increment(eif_ctx *c, int rk) {
 }
 
 int launch_update_particles(eif_ctx *c) {
+  c->boxes_x_valid = false;
   if (c->np == 0) return EIF_OK;
   EIF_PROF(c, "particle_update", 1);
   k_update<<<(c->np + 127) / 128, 128, 0, c->stream>>>(c->P, c->pcap, c->np, c->ly);
