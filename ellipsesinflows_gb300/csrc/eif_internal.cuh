@@ -79,6 +79,11 @@ struct PoissonPlan {
   double *red_up;   // [k][b]
   double *red_q1;   // [k][b]  correction vector of the reduced cyclic system
   double *red_coef; // [k][4]  A, B, den, pin flag
+  // second-level partition of the reduced system (g2 values per group, q2 groups; 0: not used)
+  int g2 = 0, q2 = 0;
+  double *r2_inv = nullptr, *r2_up = nullptr, *r2_phi = nullptr;   // [i][k], i < g2-1
+  double *r2_qinv = nullptr, *r2_qup = nullptr, *r2_q1 = nullptr;  // [q][k], q < q2-1
+  double *r2_coef = nullptr;                                        // [k][4] A2, B2, den2, pin flag
   double *lam;      // [k]     eigenvalue of the DCT direction
   double *ywork;    // nblk*itot: reduced right-hand sides / interface values
 };

@@ -256,6 +256,75 @@ __global__ void __launch_bounds__(RED_THREADS) k_tdm_reduced(double *__restrict_
   }
 }
 
+// The same partition one level down. The reduced system of a wavenumber (P
+// interface values, constant coefficients A, B) is cut into Q groups of G: G-1
+// interior values and one second-level interface value t_g per group. Every
+// thread solves one group's interior with zero interfaces (factors inv2/up2 for
+// the off-diagonal A and diagonal B) and its interface equation's right-hand
+// side; one thread per wavenumber solves the cyclic system of the Q values t_g
+// (A2 = A phi[G-2], B2 = B + 2 A phi[0], the reference's cyclic algorithm as at the
+// first level, kx = 0 pinned with its last value 0); every thread then adds
+// t_{g-1} phi[i] + t_g phi[G-2-i] to its interior. Block: 32 wavenumbers x Q groups.
+template <int G>
+__global__ void __launch_bounds__(1024) k_tdm_reduced2(double *__restrict__ iface, const double *__restrict__ first,
+                                                       const double *__restrict__ rcoef, const double *__restrict__ inv2,
+                                                       const double *__restrict__ up2, const double *__restrict__ phi2,
+                                                       const double *__restrict__ ri2, const double *__restrict__ ru2,
+                                                       const double *__restrict__ rq2, const double *__restrict__ rc2,
+                                                       double l, int itot, int P, int Q) {
+  extern __shared__ double sm2[];   // [Q][32] first interior values, right-hand sides, interface values
+  double *y0s = sm2, *rhs = sm2 + (size_t)Q * 32, *ts = sm2 + (size_t)2 * Q * 32;
+  const int kk = threadIdx.x & 31, g = threadIdx.x >> 5;
+  const int k = blockIdx.x * 32 + kk;
+  const bool on = k < itot;
+  const int kc = on ? k : itot - 1;
+  const double A = rcoef[4 * kc + 0];
+  double y[G];
+  // level-one reduced right-hand sides R_b = (r_iface - l y_b[M-2]) - l y_{b+1}[0]
+#pragma unroll
+  for (int i = 0; i < G; i++) {
+    const int b = g * G + i;
+    y[i] = iface[(size_t)b * itot + kc] - l * first[(size_t)((b + 1) % P) * itot + kc];
+  }
+  const double rlast = y[G - 1];
+  y[0] = y[0] * inv2[kc];
+#pragma unroll
+  for (int i = 1; i < G - 1; i++) y[i] = (y[i] - A * y[i - 1]) * inv2[(size_t)i * itot + kc];
+#pragma unroll
+  for (int i = G - 3; i >= 0; i--) y[i] = y[i] - up2[(size_t)i * itot + kc] * y[i + 1];
+  y0s[g * 32 + kk] = y[0];
+  __syncthreads();
+  rhs[g * 32 + kk] = rlast - A * y[G - 2] - A * y0s[((g + 1) % Q) * 32 + kk];
+  __syncthreads();
+  if (g == 0) {
+    const double A2 = rc2[4 * kc + 0], den2 = rc2[4 * kc + 2];
+    const bool pin = rc2[4 * kc + 3] != 0.;
+    double zprev = rhs[kk] * ri2[kc];
+    ts[kk] = zprev;
+    for (int q = 1; q < Q - 1; q++) {
+      zprev = (rhs[q * 32 + kk] - A2 * zprev) * ri2[(size_t)q * itot + kc];
+      ts[q * 32 + kk] = zprev;
+    }
+    for (int q = Q - 3; q >= 0; q--) {
+      zprev = ts[q * 32 + kk] - ru2[(size_t)q * itot + kc] * zprev;
+      ts[q * 32 + kk] = zprev;
+    }
+    const double num = rhs[(Q - 1) * 32 + kk] - A2 * ts[kk] - A2 * ts[(Q - 2) * 32 + kk];
+    const double last = pin ? 0. : num / den2;
+    for (int q = 0; q < Q - 1; q++) ts[q * 32 + kk] = ts[q * 32 + kk] + last * rq2[(size_t)q * itot + kc];
+    ts[(Q - 1) * 32 + kk] = last;
+  }
+  __syncthreads();
+  if (!on) return;
+  const double tl = ts[((g + Q - 1) % Q) * 32 + kk], tr = ts[g * 32 + kk];
+#pragma unroll
+  for (int i = 0; i < G - 1; i++) {
+    iface[(size_t)(g * G + i) * itot + k] =
+        y[i] + tl * phi2[(size_t)i * itot + k] + tr * phi2[(size_t)(G - 2 - i) * itot + k];
+  }
+  iface[(size_t)(g * G + G - 1) * itot + k] = tr;
+}
+
 // columns per block of k_tdm_reduced that fit its shared memory
 static int red_cols(int nblk) {
   for (int cols = 16; cols >= 1; cols /= 2) {
@@ -699,6 +768,20 @@ int poisson_init(eif_ctx *c) {
     std::vector<double> inv((size_t)(M - 1) * n), up((size_t)(M - 1) * n), g((size_t)(M - 1) * n);
     std::vector<double> rinv((size_t)P * n), rup((size_t)P * n), rq1((size_t)P * n), rcoef((size_t)4 * n);
     std::vector<double> ti(M), tu(M), tg(M), ri(P), ru(P), rq(P);
+    // second level: groups of G2 (16, 8 or 4) with 3 <= Q2 = P / G2 <= 32, smallest G2 + Q2
+    int G2 = 0, Q2 = 0;
+    for (int gsz : {16, 8, 4}) {
+      if (P % gsz != 0) continue;
+      const int q = P / gsz;
+      if (q < 3 || q > 32) continue;
+      if (G2 == 0 || gsz + q < G2 + Q2) { G2 = gsz; Q2 = q; }
+    }
+    pp.g2 = G2;
+    pp.q2 = Q2;
+    const size_t l2 = G2 > 0 ? (size_t)std::max(G2, Q2) * n : 1;
+    std::vector<double> inv2(l2), up2(l2), phi2(l2), ri2(l2), ru2(l2), rq2(l2), rc2(G2 > 0 ? (size_t)4 * n : 1);
+    std::vector<double> t2i(std::max(G2, 1)), t2u(std::max(G2, 1)), t2g(std::max(G2, 1));
+    std::vector<double> q2i(std::max(Q2, 1)), q2u(std::max(Q2, 1)), q2q(std::max(Q2, 1));
     for (int k = 0; k < n; k++) {
       const double cc = -l - l + lam[k];
       thomas_factors(M - 1, l, cc, ti.data(), tu.data());
@@ -727,6 +810,35 @@ int poisson_init(eif_ctx *c) {
       rcoef[4 * k + 1] = B;
       rcoef[4 * k + 2] = B + A * rq[0] + A * rq[P - 2];
       rcoef[4 * k + 3] = k == 0 ? 1. : 0.;
+      if (G2 > 0) {
+        // second level: interior factors and left response of a group, then the
+        // cyclic system of the Q second-level interface values
+        thomas_factors(G2 - 1, A, B, t2i.data(), t2u.data());
+        for (int i = 0; i < G2 - 1; i++) t2g[i] = 0.;
+        t2g[0] = -A;
+        thomas_apply(G2 - 1, A, t2i.data(), t2u.data(), t2g.data());
+        for (int i = 0; i < G2 - 1; i++) {
+          inv2[(size_t)i * n + k] = t2i[i];
+          up2[(size_t)i * n + k] = t2u[i];
+          phi2[(size_t)i * n + k] = t2g[i];
+        }
+        const double A2 = A * t2g[G2 - 2];
+        const double B2 = B + 2. * A * t2g[0];
+        thomas_factors(Q2 - 1, A2, B2, q2i.data(), q2u.data());
+        for (int q = 0; q < Q2 - 1; q++) q2q[q] = 0.;
+        q2q[0] = -A2;
+        q2q[Q2 - 2] += -A2;
+        thomas_apply(Q2 - 1, A2, q2i.data(), q2u.data(), q2q.data());
+        for (int q = 0; q < Q2 - 1; q++) {
+          ri2[(size_t)q * n + k] = q2i[q];
+          ru2[(size_t)q * n + k] = q2u[q];
+          rq2[(size_t)q * n + k] = q2q[q];
+        }
+        rc2[4 * k + 0] = A2;
+        rc2[4 * k + 1] = B2;
+        rc2[4 * k + 2] = B2 + A2 * q2q[0] + A2 * q2q[Q2 - 2];
+        rc2[4 * k + 3] = k == 0 ? 1. : 0.;
+      }
     }
     EIF_CK(c, up_load((void **)&pp.tdm_inv, inv.data(), sizeof(double) * inv.size()));
     EIF_CK(c, up_load((void **)&pp.tdm_up, up.data(), sizeof(double) * up.size()));
@@ -743,6 +855,15 @@ int poisson_init(eif_ctx *c) {
     EIF_CK(c, up_load((void **)&pp.red_up, rup.data(), sizeof(double) * rup.size()));
     EIF_CK(c, up_load((void **)&pp.red_q1, rq1.data(), sizeof(double) * rq1.size()));
     EIF_CK(c, up_load((void **)&pp.red_coef, rcoef.data(), sizeof(double) * rcoef.size()));
+    if (G2 > 0) {
+      EIF_CK(c, up_load((void **)&pp.r2_inv, inv2.data(), sizeof(double) * l2));
+      EIF_CK(c, up_load((void **)&pp.r2_up, up2.data(), sizeof(double) * l2));
+      EIF_CK(c, up_load((void **)&pp.r2_phi, phi2.data(), sizeof(double) * l2));
+      EIF_CK(c, up_load((void **)&pp.r2_qinv, ri2.data(), sizeof(double) * l2));
+      EIF_CK(c, up_load((void **)&pp.r2_qup, ru2.data(), sizeof(double) * l2));
+      EIF_CK(c, up_load((void **)&pp.r2_q1, rq2.data(), sizeof(double) * l2));
+      EIF_CK(c, up_load((void **)&pp.r2_coef, rc2.data(), sizeof(double) * rc2.size()));
+    }
     EIF_CK(c, cudaMalloc((void **)&pp.ywork, sizeof(double) * 2 * (size_t)P * n));
   } else {
     EIF_CK(c, cudaMalloc((void **)&pp.ywork, sizeof(double) * 2 * (size_t)jt * n));
@@ -765,7 +886,8 @@ int poisson_init(eif_ctx *c) {
 
 void poisson_free(eif_ctx *c) {
   PoissonPlan &pp = c->pp;
-  void *ptrs[] = {pp.tw, pp.rot, pp.wn, pp.tw_f, pp.rot_f, pp.wn_f, pp.lam, pp.tdm_inv, pp.tdm_up, pp.tdm_g, pp.tdm_g_df,
+  void *ptrs[] = {pp.r2_inv, pp.r2_up, pp.r2_phi, pp.r2_qinv, pp.r2_qup, pp.r2_q1, pp.r2_coef,
+                  pp.tw, pp.rot, pp.wn, pp.tw_f, pp.rot_f, pp.wn_f, pp.lam, pp.tdm_inv, pp.tdm_up, pp.tdm_g, pp.tdm_g_df,
                   pp.red_inv, pp.red_up, pp.red_q1, pp.red_coef, pp.ywork};
   for (void *p : ptrs) if (p) cudaFree(p);
   pp = PoissonPlan{};
@@ -828,9 +950,28 @@ int launch_potential(eif_ctx *c, int rk, bool with_ibm) {
       k_tdm_local<4><<<g, 128, 0, c->stream>>>(c->qhat, pp.tdm_inv, pp.tdm_up, iface, first, l, n, pp.nblk, c->ld);
     }
     EIF_LAUNCH_CK(c);
-    const int rcols = red_cols(pp.nblk);
-    k_tdm_reduced<<<(n + rcols - 1) / rcols, RED_THREADS, red_smem_bytes(pp.nblk, rcols), c->stream>>>(
-        iface, first, pp.red_inv, pp.red_up, pp.red_q1, pp.red_coef, l, n, pp.nblk, rcols);
+    if (pp.g2 > 0) {
+      const int Q = pp.q2;
+      const size_t sm = sizeof(double) * 3 * 32 * (size_t)Q;
+      const dim3 grid((n + 31) / 32);
+      if (pp.g2 == 16) {
+        k_tdm_reduced2<16><<<grid, 32 * Q, sm, c->stream>>>(iface, first, pp.red_coef, pp.r2_inv, pp.r2_up, pp.r2_phi,
+                                                            pp.r2_qinv, pp.r2_qup, pp.r2_q1, pp.r2_coef, l, n,
+                                                            pp.nblk, Q);
+      } else if (pp.g2 == 8) {
+        k_tdm_reduced2<8><<<grid, 32 * Q, sm, c->stream>>>(iface, first, pp.red_coef, pp.r2_inv, pp.r2_up, pp.r2_phi,
+                                                           pp.r2_qinv, pp.r2_qup, pp.r2_q1, pp.r2_coef, l, n,
+                                                           pp.nblk, Q);
+      } else {
+        k_tdm_reduced2<4><<<grid, 32 * Q, sm, c->stream>>>(iface, first, pp.red_coef, pp.r2_inv, pp.r2_up, pp.r2_phi,
+                                                           pp.r2_qinv, pp.r2_qup, pp.r2_q1, pp.r2_coef, l, n,
+                                                           pp.nblk, Q);
+      }
+    } else {
+      const int rcols = red_cols(pp.nblk);
+      k_tdm_reduced<<<(n + rcols - 1) / rcols, RED_THREADS, red_smem_bytes(pp.nblk, rcols), c->stream>>>(
+          iface, first, pp.red_inv, pp.red_up, pp.red_q1, pp.red_coef, l, n, pp.nblk, rcols);
+    }
     EIF_LAUNCH_CK(c);
   } else {
     EIF_PROF(c, "poisson_tdm", 1);
