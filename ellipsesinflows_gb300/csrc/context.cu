@@ -365,6 +365,7 @@ int eif_push_particles(eif_ctx *c, int n, const double *rec) {
   graphs_free(c);
   c->incr_zero = false;
   c->boxes_x_valid = false;
+  c->weights_x_valid = false;
   int rc = ensure_pcap(c, n);
   if (rc) return rc;
   std::vector<double> soa((size_t)EIF_NFIELDS * c->pcap, 0.);

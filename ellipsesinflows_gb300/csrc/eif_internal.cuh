@@ -131,6 +131,8 @@ struct eif_ctx {
   bool use_graphs = true;
   bool incr_zero = false;       // the particle increments are zero (after a reset)
   bool boxes_x_valid = false;   // the IBM boxes hold the positions X (see launch_boxes)
+  bool weights_x_valid = false; // wcache holds the indicator weights of those boxes
+  void *wcache = nullptr;       // indicator weight per IBM task slot (wcap entries)
   bool in_loop = false;                      // capturing the body of a sub-iteration loop
   cudaGraphConditionalHandle loop_handle = 0;
   int ibm_ctas_per_sm[2] = {0, 0};  // resident CTAs per SM of the IBM work kernels (FP64, mixed)

@@ -55,6 +55,7 @@ int build(eif_ctx *c, eif_ctx::StepGraph &sg) {
   const int cur0 = c->cur, scur0 = c->scur;
   // the graph must not depend on boxes computed before it: start without them
   c->boxes_x_valid = false;
+  c->weights_x_valid = false;
   c->incr_zero = false;
   cudaGraph_t g = nullptr;
   EIF_CK(c, cudaGraphCreate(&g, 0));
@@ -63,6 +64,7 @@ int build(eif_ctx *c, eif_ctx::StepGraph &sg) {
     c->cur = cur0;
     c->scur = scur0;
     c->boxes_x_valid = false;
+    c->weights_x_valid = false;
     cudaGraphDestroy(g);
     return code;
   };
@@ -124,6 +126,7 @@ int build(eif_ctx *c, eif_ctx::StepGraph &sg) {
   c->cur = cur0;
   c->scur = scur0;
   c->boxes_x_valid = false;
+  c->weights_x_valid = false;
   return EIF_OK;
 }
 

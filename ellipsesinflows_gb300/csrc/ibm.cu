@@ -317,6 +317,14 @@ struct WorkArgs {
   const int *owner;      // owner particle of every chunk (mixed form)
   const float *coef;     // single-precision dt products; [9] = 1/dt
   float rh_f, dx_f, dy_f, dxdy_f;
+  // Indicator weights of the cells at the positions X are kept in wcache (one per
+  // task slot, like wbuf) and reused by the evaluations that see the same
+  // geometry: wmode 0 computes, 1 computes and stores, 2 loads; when iter is set
+  // (the sub-iteration loop of a step graph) the kernel loads in the first
+  // sub-iteration (*iter == 0, increments still zero) and computes afterwards.
+  void *wcache;
+  int wmode;
+  const unsigned *iter;
   Bounds bd;
 };
 
@@ -332,6 +340,8 @@ __global__ void __launch_bounds__(256) k_ibm_work(WorkArgs a) {
   const double dtv = a.mode == 1 ? __ldg(a.dt) : 0.;
   const double md = FAR_CELLS_D * a.h;
   const int pc = a.pcap, ld = a.ld;
+  const int wmode = a.iter ? (*a.iter == 0u ? 2 : 0) : a.wmode;
+  double *wcache = static_cast<double *>(a.wcache);
   // per warp: body-frame offsets of its near cells, overwritten by their weights
   __shared__ double2 slot_buf[8][CHUNK];
   double2 *slots = slot_buf[threadIdx.x >> 5];
@@ -362,6 +372,26 @@ __global__ void __launch_bounds__(256) k_ibm_work(WorkArgs a) {
     const int j = task ? t.j : 1;
     const double y = __ldg(a.yc + j);
     const double Y = y - py_;
+    int rank[2];
+    bool cin[2];
+    double th2[2];
+    unsigned near_mask[2];
+    if (wmode == 2) {
+      // weights of the same geometry from an earlier evaluation
+#pragma unroll
+      for (int half = 0; half < CHUNK / 32; half++) {
+        const int i = (task ? t.ib : 1) + half * 32 + lane;
+        bool in = task && i <= t.ie;
+        if (in) {
+          in = EIF_CHK(a.bd.rec, i, a.bd.xc - 1, 14) && EIF_CHK(a.bd.rec, j * ld + i, a.bd.field, 16) &&
+               EIF_CHK(a.bd.rec, (j + 1) * ld + i, a.bd.field, 17) &&
+               EIF_CHK(a.bd.rec, j * ld + (i - 1), a.bd.field, 18) &&
+               EIF_CHK(a.bd.rec, (long long)c * CHUNK + half * 32 + lane, a.bd.wbuf, 22);
+        }
+        cin[half] = in;
+        th2[half] = in ? wcache[(size_t)c * CHUNK + half * 32 + lane] : 0.;
+      }
+    } else {
     // far cells of this row (row_chords), in single precision: the far distance
     // (10.5 cells) exceeds the saturation distance of tanh (9.53 cells) by far more
     // than the rounding of the column bounds
@@ -377,10 +407,6 @@ __global__ void __launch_bounds__(256) k_ibm_work(WorkArgs a) {
                  ilo, ihi);
     }
     // pass 1: cells of the row, far cells settled, body-frame offsets of the near ones
-    int rank[2];
-    bool cin[2];
-    double th2[2];
-    unsigned near_mask[2];
 #pragma unroll
     for (int half = 0; half < CHUNK / 32; half++) {
       const int i = (task ? t.ib : 1) + half * 32 + lane;
@@ -419,6 +445,13 @@ __global__ void __launch_bounds__(256) k_ibm_work(WorkArgs a) {
     for (int half = 0; half < CHUNK / 32; half++)
       if ((near_mask[half] >> lane) & 1u) th2[half] = slots[rank[half]].x;
     __syncwarp();
+    if (wmode == 1) {
+#pragma unroll
+      for (int half = 0; half < CHUNK / 32; half++)
+        if (EIF_CHK(a.bd.rec, (long long)c * CHUNK + half * 32 + lane, a.bd.wbuf, 23))
+          wcache[(size_t)c * CHUNK + half * 32 + lane] = th2[half];
+    }
+    }
     double s0 = 0., s1 = 0., s2 = 0.;
 #pragma unroll
     for (int half = 0; half < CHUNK / 32; half++) {
@@ -539,6 +572,8 @@ __global__ void __launch_bounds__(256, 3) k_ibm_work_f(WorkArgs a) {
   const float rdtv = a.mode == 1 ? __ldg(a.coef + 9) : 0.f;
   const int ld = a.ld;
   float2 *wb = reinterpret_cast<float2 *>(a.wbuf);
+  const int wmode = a.iter ? (*a.iter == 0u ? 2 : 0) : a.wmode;
+  float *wcache = static_cast<float *>(a.wcache);
   // per warp: body-frame offsets of its near cells, overwritten by their weights
   __shared__ float2 slot_buf[8][CHUNK];
   float2 *slots = slot_buf[threadIdx.x >> 5];
@@ -563,14 +598,30 @@ __global__ void __launch_bounds__(256, 3) k_ibm_work_f(WorkArgs a) {
     const float gyi = m == 0 ? qE.x : (m == 1 ? qE.y : qE.z);
     const int j = task ? t.j : 1;
     const float Y = ((float)(j - j0i) - gyi) * dyf;
-    // far cells of this row (PF_AL .. PF_RO2: al, ka, de, so^2, si^2, ro^2)
-    float olo, ohi, ilo, ihi;
-    row_chords(qE.w, qF.x, qF.y, qF.z, qF.w, qG.x, Y, olo, ohi, ilo, ihi);
-    // pass 1: cells of the row, far cells settled, body-frame offsets of the near ones
     int rank[2];
     float cX[2], th2[2];
     bool cin[2];
     unsigned near_mask[2];
+    if (wmode == 2) {
+      // weights of the same geometry from an earlier evaluation
+#pragma unroll
+      for (int half = 0; half < CHUNK / 32; half++) {
+        const int i = (task ? t.ib : 1) + half * 32 + lane;
+        bool in = task && i <= t.ie;
+        if (in) {
+          in = EIF_CHK(a.bd.rec, j * ld + i, a.bd.field, 54) && EIF_CHK(a.bd.rec, (j + 1) * ld + i, a.bd.field, 55) &&
+               EIF_CHK(a.bd.rec, j * ld + (i - 1), a.bd.field, 56) &&
+               EIF_CHK(a.bd.rec, (long long)c * CHUNK + half * 32 + lane, 2 * a.bd.wbuf, 59);
+        }
+        cin[half] = in;
+        cX[half] = ((float)(i - i0) - gx) * dxf;
+        th2[half] = in ? wcache[(size_t)c * CHUNK + half * 32 + lane] : 0.f;
+      }
+    } else {
+    // far cells of this row (PF_AL .. PF_RO2: al, ka, de, so^2, si^2, ro^2)
+    float olo, ohi, ilo, ihi;
+    row_chords(qE.w, qF.x, qF.y, qF.z, qF.w, qG.x, Y, olo, ohi, ilo, ihi);
+    // pass 1: cells of the row, far cells settled, body-frame offsets of the near ones
 #pragma unroll
     for (int half = 0; half < CHUNK / 32; half++) {
       const int i = (task ? t.ib : 1) + half * 32 + lane;
@@ -608,6 +659,13 @@ __global__ void __launch_bounds__(256, 3) k_ibm_work_f(WorkArgs a) {
     for (int half = 0; half < CHUNK / 32; half++)
       if ((near_mask[half] >> lane) & 1u) th2[half] = slots[rank[half]].x;
     __syncwarp();
+    if (wmode == 1) {
+#pragma unroll
+      for (int half = 0; half < CHUNK / 32; half++)
+        if (EIF_CHK(a.bd.rec, (long long)c * CHUNK + half * 32 + lane, 2 * a.bd.wbuf, 60))
+          wcache[(size_t)c * CHUNK + half * 32 + lane] = th2[half];
+    }
+    }
     float sacc0 = 0.f, sacc1 = 0.f, sacc2 = 0.f;
 #pragma unroll
     for (int half = 0; half < CHUNK / 32; half++) {
@@ -888,6 +946,7 @@ int ibm_reserve(eif_ctx *c) {
   EIF_CK(c, cudaMalloc((void **)&c->chunk_off, sizeof(int) * 2 * (c->np + 1)));
   EIF_CK(c, cudaMalloc((void **)&c->partial, sizeof(double) * 3 * chunks));
   EIF_CK(c, cudaMalloc((void **)&c->wbuf, sizeof(double2) * c->wcap));
+  EIF_CK(c, cudaMalloc((void **)&c->wcache, sizeof(double) * c->wcap));
   EIF_CK(c, cudaMalloc((void **)&c->pf, sizeof(float) * PF_WORDS * c->np));
   EIF_CK(c, cudaMalloc((void **)&c->owner, sizeof(int) * (size_t)chunks));
   const int nbands = (c->jtot + GTY - 1) / GTY;
@@ -903,13 +962,15 @@ void ibm_free(eif_ctx *c) {
   if (c->chunk_off) cudaFree(c->chunk_off);
   if (c->partial) cudaFree(c->partial);
   if (c->wbuf) cudaFree(c->wbuf);
+  if (c->wcache) cudaFree(c->wcache);
   if (c->pf) cudaFree(c->pf);
   if (c->owner) cudaFree(c->owner);
   if (c->band_lists) cudaFree(c->band_lists);
   if (c->band_counts) cudaFree(c->band_counts);
   if (c->band_marks) cudaFree(c->band_marks);
   c->band_lists = nullptr; c->band_counts = nullptr; c->band_marks = nullptr;
-  c->box = nullptr; c->chunk_off = nullptr; c->partial = nullptr; c->wbuf = nullptr;
+  c->box = nullptr; c->chunk_off = nullptr; c->partial = nullptr; c->wbuf = nullptr; c->wcache = nullptr;
+  c->weights_x_valid = false;
   c->pf = nullptr; c->owner = nullptr;
   c->chunk_cap = 0; c->wcap = 0;
 }
@@ -934,6 +995,7 @@ static int launch_boxes(eif_ctx *c, bool use_increment) {
   const bool x_only = !use_increment || c->incr_zero;
   if (x_only && c->boxes_x_valid) return EIF_OK;
   c->boxes_x_valid = false;
+  c->weights_x_valid = false;
   BoxArgs b;
   b.bd = bounds_of(c);
   b.bd_off_base = c->chunk_off;
@@ -971,6 +1033,22 @@ static int launch_work(eif_ctx *c, int mode, int cn) {
   w.dx_f = (float)c->dx;
   w.dy_f = (float)c->dy;
   w.dxdy_f = (float)(c->dx * c->dy);
+  // weights at the positions X (inertia with zero increments, or the exchange)
+  // are stored once and reused while the boxes at X stay valid
+  const bool x_only = mode == 1 || c->incr_zero;
+  w.wcache = c->wcache;
+  w.iter = nullptr;
+  if (c->in_loop) {
+    w.wmode = 0;
+    w.iter = reinterpret_cast<const unsigned *>(c->d_inc + 1);
+  } else if (x_only && c->boxes_x_valid && c->weights_x_valid) {
+    w.wmode = 2;
+  } else if (x_only && c->boxes_x_valid) {
+    w.wmode = 1;
+    c->weights_x_valid = true;
+  } else {
+    w.wmode = 0;
+  }
   // persistent grid: as many CTAs as are resident at once (queried once per context)
   const int per_sm_idx = c->cfg.precision == EIF_PREC_MIXED ? 1 : 0;
   if (c->ibm_ctas_per_sm[per_sm_idx] == 0) {

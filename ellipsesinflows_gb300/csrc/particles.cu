@@ -469,6 +469,7 @@ int launch_increment(eif_ctx *c, int rk) {
 
 int launch_update_particles(eif_ctx *c) {
   c->boxes_x_valid = false;
+  c->weights_x_valid = false;
   if (c->np == 0) return EIF_OK;
   EIF_PROF(c, "particle_update", 1);
   k_update<<<(c->np + 127) / 128, 128, 0, c->stream>>>(c->P, c->pcap, c->np, c->ly);
