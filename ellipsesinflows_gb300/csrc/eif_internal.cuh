@@ -135,7 +135,7 @@ struct eif_ctx {
   void *wcache = nullptr;       // indicator weight per IBM task slot (wcap entries)
   bool in_loop = false;                      // capturing the body of a sub-iteration loop
   cudaGraphConditionalHandle loop_handle = 0;
-  int ibm_ctas_per_sm[2] = {0, 0};  // resident CTAs per SM of the IBM work kernels (FP64, mixed)
+  int ibm_ctas_per_sm[3] = {0, 0, 0};  // resident CTAs per SM of the IBM work kernels (FP64, mixed, mixed cached)
   unsigned *band_marks = nullptr;  // per band of 8 rows: bitmap over the 3*np (particle, image) boxes
   float4 *cpf = nullptr;
   int *cand = nullptr, *cand_n = nullptr;  // collision candidates (np * EIF_CAND_SPLIT * EIF_CAND_CAP), counts        // pcap: single-precision x + dx, y + dy, max(a, b) for the collision prefilter

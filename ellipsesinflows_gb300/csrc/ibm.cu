@@ -325,6 +325,7 @@ struct WorkArgs {
   void *wcache;
   int wmode;
   const unsigned *iter;
+  int gate;   // with iter (mixed form): 1 runs only in the first sub-iteration, 2 only afterwards
   Bounds bd;
 };
 
@@ -572,7 +573,8 @@ __global__ void __launch_bounds__(256, 3) k_ibm_work_f(WorkArgs a) {
   const float rdtv = a.mode == 1 ? __ldg(a.coef + 9) : 0.f;
   const int ld = a.ld;
   float2 *wb = reinterpret_cast<float2 *>(a.wbuf);
-  const int wmode = a.iter ? (*a.iter == 0u ? 2 : 0) : a.wmode;
+  if (a.gate && ((a.gate == 1) != (*a.iter == 0u))) return;
+  const int wmode = a.wmode;
   float *wcache = static_cast<float *>(a.wcache);
   // per warp: body-frame offsets of its near cells, overwritten by their weights
   __shared__ float2 slot_buf[8][CHUNK];
@@ -708,6 +710,90 @@ __global__ void __launch_bounds__(256, 3) k_ibm_work_f(WorkArgs a) {
       sacc2 += __shfl_xor_sync(0xffffffffu, sacc2, o);
     }
     if (lane == 0 && EIF_CHK(a.bd.rec, 3LL * c + 2, a.bd.partial, 58)) {
+      a.partial[3 * (size_t)c + 0] = eifd::f2d(sacc0);
+      a.partial[3 * (size_t)c + 1] = eifd::f2d(sacc1);
+      a.partial[3 * (size_t)c + 2] = eifd::f2d(sacc2);
+    }
+  }
+}
+
+// The mixed form's evaluation with cached weights (wmode 2 of k_ibm_work_f): the
+// same sums and field contributions, without the geometry work, so it runs with
+// few registers and many resident warps, which hide the latency of its loads.
+__global__ void __launch_bounds__(256, 4) k_ibm_sum_f(WorkArgs a) {
+  if (a.gate && ((a.gate == 1) != (*a.iter == 0u))) return;
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const int total = EIF_CHK(a.bd.rec, a.np, a.bd.off, 70) ? __ldg(a.off + a.np) : 0;
+  const float dxf = a.dx_f, dyf = a.dy_f, dxdy = a.dxdy_f;
+  const float rdtv = a.mode == 1 ? __ldg(a.coef + 9) : 0.f;
+  const int ld = a.ld;
+  float2 *wb = reinterpret_cast<float2 *>(a.wbuf);
+  const float *wcache = static_cast<const float *>(a.wcache);
+  for (int c = warp; c < total; c += nwarps) {
+    if (!EIF_CHK(a.bd.rec, c, a.bd.partial / 3, 71)) continue;
+    const int n = __ldg(a.owner + c);
+    if (!EIF_CHK(a.bd.rec, n, a.np, 72) || !EIF_CHK(a.bd.rec, 12 * n + 11, a.bd.box, 73)) continue;
+    const int4 *b4 = reinterpret_cast<const int4 *>(a.box + 12 * n);
+    RowTask t;
+    const bool task = row_task(__ldg(b4), __ldg(b4 + 1), __ldg(b4 + 2), c - __ldg(a.off + n), t);
+    const float4 *q4 = reinterpret_cast<const float4 *>(a.pf + (size_t)PF_WORDS * n);
+    const float4 qB = __ldg(q4 + 1), qC = __ldg(q4 + 2), qD = __ldg(q4 + 3), qE = __ldg(q4 + 4);
+    const float rpm = qB.z, rpim = qB.w, pux = qC.x, puy = qC.y, pvz = qC.z, gx = qC.w;
+    const int i0 = __float_as_int(qD.x);
+    const int m = task ? t.img + 1 : 1;
+    const int j0i = __float_as_int(m == 0 ? qD.y : (m == 1 ? qD.z : qD.w));
+    const float gyi = m == 0 ? qE.x : (m == 1 ? qE.y : qE.z);
+    const int j = task ? t.j : 1;
+    const float Y = ((float)(j - j0i) - gyi) * dyf;
+    float sacc0 = 0.f, sacc1 = 0.f, sacc2 = 0.f;
+#pragma unroll
+    for (int half = 0; half < CHUNK / 32; half++) {
+      const int i = (task ? t.ib : 1) + half * 32 + lane;
+      const long long slot = (long long)c * CHUNK + half * 32 + lane;
+      bool in = task && i <= t.ie;
+      if (in) {
+        in = EIF_CHK(a.bd.rec, j * ld + i, a.bd.field, 74) && EIF_CHK(a.bd.rec, (j + 1) * ld + i, a.bd.field, 75) &&
+             EIF_CHK(a.bd.rec, j * ld + (i - 1), a.bd.field, 76) && EIF_CHK(a.bd.rec, slot, 2 * a.bd.wbuf, 77);
+      }
+      float2 contrib = make_float2(0.f, 0.f);
+      const float th = in ? wcache[slot] : 0.f;
+      // cells of weight exactly zero (inertia: far outside; exchange: any far cell) are skipped
+      const bool live = in && (a.mode == 0 ? th != -1.f : fabsf(th) != 1.f);
+      if (live) {
+        const float X = ((float)(i - i0) - gx) * dxf;
+        const float uxs = eifd::d2f(__ldg(a.ux + j * ld + (i - 1))) + eifd::d2f(__ldg(a.ux + j * ld + i));
+        const float uys = eifd::d2f(__ldg(a.uy + j * ld + i)) + eifd::d2f(__ldg(a.uy + (j + 1) * ld + i));
+        if (a.mode == 0) {
+          const float w = 0.5f * (1.f + th);
+          const float valx = w * 0.5f * uxs * dxdy;
+          const float valy = w * 0.5f * uys * dxdy;
+          sacc0 += valx * rpm;
+          sacc1 += valy * rpm;
+          sacc2 += (-Y * valx + X * valy) * rpim;
+        } else {
+          const float w = 1.f - th * th;
+          const float uxp = pux - pvz * Y;
+          const float uyp = puy + pvz * X;
+          const float gxv = w * (uxp - 0.5f * uxs);   // fx * dt
+          const float gyv = w * (uyp - 0.5f * uys);   // fy * dt
+          contrib = make_float2(gxv, gyv);
+          const float Fx = gxv * rdtv * dxdy, Fy = gyv * rdtv * dxdy;
+          sacc0 -= Fx * rpm;
+          sacc1 -= Fy * rpm;
+          sacc2 += (Y * Fx - X * Fy) * rpim;
+        }
+      }
+      if (a.mode == 1 && EIF_CHK(a.bd.rec, slot, 2 * a.bd.wbuf, 78)) wb[slot] = contrib;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      sacc0 += __shfl_xor_sync(0xffffffffu, sacc0, o);
+      sacc1 += __shfl_xor_sync(0xffffffffu, sacc1, o);
+      sacc2 += __shfl_xor_sync(0xffffffffu, sacc2, o);
+    }
+    if (lane == 0 && EIF_CHK(a.bd.rec, 3LL * c + 2, a.bd.partial, 79)) {
       a.partial[3 * (size_t)c + 0] = eifd::f2d(sacc0);
       a.partial[3 * (size_t)c + 1] = eifd::f2d(sacc1);
       a.partial[3 * (size_t)c + 2] = eifd::f2d(sacc2);
@@ -926,6 +1012,8 @@ int ibm_prepare(eif_ctx *c) {
   c->ibm_ctas_per_sm[0] = std::max(1, v);
   EIF_CK(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_ibm_work_f, 256, 0));
   c->ibm_ctas_per_sm[1] = std::max(1, v);
+  EIF_CK(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_ibm_sum_f, 256, 0));
+  c->ibm_ctas_per_sm[2] = std::max(1, v);
   return EIF_OK;
 }
 
@@ -1038,6 +1126,7 @@ static int launch_work(eif_ctx *c, int mode, int cn) {
   const bool x_only = mode == 1 || c->incr_zero;
   w.wcache = c->wcache;
   w.iter = nullptr;
+  w.gate = 0;
   if (c->in_loop) {
     w.wmode = 0;
     w.iter = reinterpret_cast<const unsigned *>(c->d_inc + 1);
@@ -1058,8 +1147,19 @@ static int launch_work(eif_ctx *c, int mode, int cn) {
   const int per_sm = c->ibm_ctas_per_sm[per_sm_idx];
   const int blocks = std::max(1, std::min(c->sms * per_sm, (c->chunk_cap * 32 + 255) / 256));
   {
-    EIF_PROF(c, mode == 0 ? "ibm_inertia" : "ibm_exchange", 1);
-    if (c->cfg.precision == EIF_PREC_MIXED) {
+    const bool mixed = c->cfg.precision == EIF_PREC_MIXED;
+    EIF_PROF(c, mode == 0 ? "ibm_inertia" : "ibm_exchange", mixed && c->in_loop ? 2 : 1);
+    if (mixed && c->in_loop) {
+      // first sub-iteration: cached weights; later ones: full evaluation (decided on the device)
+      WorkArgs w1 = w, w2 = w;
+      w1.wmode = 2; w1.gate = 1;
+      w2.wmode = 0; w2.gate = 2;
+      k_ibm_sum_f<<<c->sms * c->ibm_ctas_per_sm[2], 256, 0, c->stream>>>(w1);
+      EIF_LAUNCH_CK(c);
+      k_ibm_work_f<<<blocks, 256, 0, c->stream>>>(w2);
+    } else if (mixed && w.wmode == 2) {
+      k_ibm_sum_f<<<c->sms * c->ibm_ctas_per_sm[2], 256, 0, c->stream>>>(w);
+    } else if (mixed) {
       k_ibm_work_f<<<blocks, 256, 0, c->stream>>>(w);
     } else {
       k_ibm_work<<<blocks, 256, 0, c->stream>>>(w);
