@@ -323,9 +323,8 @@ def run_e2e(sim, case, steps, pg, device):
         sim.push_fluid(hux, huy, hp)
         sim.push_particles(hpart)
         sim.advance(1)
-        r = sim.pull_fluid()
-        hux[...], huy[...], hp[...], hpsi[...] = r
-        hpart[...] = sim.pull_particles()
+        sim.pull_fluid(out=(hux, huy, hp, hpsi))
+        sim.pull_particles(out=hpart)
     el = time.perf_counter() - t0
     el = max_over_ranks(pg, el, device)
     world = pg.get_world_size() if pg is not None else 1

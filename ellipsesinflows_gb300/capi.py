@@ -180,9 +180,16 @@ class Solver:
             raise ValueError("field shapes must be %s and %s" % (sx, sy))
         self._call("push_fluid", self.ctx, _ptr(ux), _ptr(uy), _ptr(p))
 
-    def pull_fluid(self):
+    def pull_fluid(self, out=None):
+        """ux, uy, p, psi as haloed arrays; with out=(ux, uy, p, psi) (C-contiguous float64
+        arrays of the right shapes, e.g. in pinned host memory) they are filled in place."""
         sx, sy = self.shapes()
-        ux, uy, p, psi = np.empty(sx), np.empty(sy), np.empty(sy), np.empty(sy)
+        if out is None:
+            out = (np.empty(sx), np.empty(sy), np.empty(sy), np.empty(sy))
+        for a, shape in zip(out, (sx, sy, sy, sy)):
+            if a.shape != shape or a.dtype != np.float64 or not a.flags["C_CONTIGUOUS"]:
+                raise ValueError("output arrays must be C-contiguous float64 of shapes %s, %s" % (sx, sy))
+        ux, uy, p, psi = out
         self._call("pull_fluid", self.ctx, _ptr(ux), _ptr(uy), _ptr(p), _ptr(psi))
         return ux, uy, p, psi
 
@@ -192,7 +199,15 @@ class Solver:
         buf = records if records.size else np.zeros(NFIELDS)
         self._call("push_particles", self.ctx, self.n_particles, _ptr(buf))
 
-    def pull_particles(self):
+    def pull_particles(self, out=None):
+        """(n, NFIELDS) particle records; with out (a C-contiguous float64 array of that
+        shape) they are written in place."""
+        if out is not None and self.n_particles > 0:
+            if out.shape != (self.n_particles, NFIELDS) or out.dtype != np.float64 or not out.flags["C_CONTIGUOUS"]:
+                raise ValueError("output array must be C-contiguous float64 of shape (%d, %d)"
+                                 % (self.n_particles, NFIELDS))
+            self._call("pull_particles", self.ctx, self.n_particles, _ptr(out))
+            return out
         out = np.zeros((max(self.n_particles, 1), NFIELDS))
         self._call("pull_particles", self.ctx, self.n_particles, _ptr(out))
         return out[: self.n_particles]

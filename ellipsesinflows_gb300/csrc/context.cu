@@ -361,19 +361,26 @@ int eif_pull_fluid(eif_ctx *c, double *ux, double *uy, double *p, double *psi) {
 
 int eif_push_particles(eif_ctx *c, int n, const double *rec) {
   if (!c || n < 0 || (n > 0 && !rec)) return EIF_ERR_ARG;
-  // the step graphs hold the particle count and buffers: rebuild them on the next advance
-  graphs_free(c);
+  // The IBM buffers, and the step graphs that hold them, are kept when the particle
+  // count is unchanged and the buffers already cover the pushed radii (a driver that
+  // re-pushes the state every step); otherwise they are rebuilt.
+  const size_t chunks = ibm_tasks_needed(c, rec, n);
+  const bool reuse = c->P && n == c->np && n <= c->pcap && (n == 0 || (c->box && chunks <= (size_t)c->chunk_cap));
+  if (!reuse) {
+    graphs_free(c);
+    int rc = ensure_pcap(c, n);
+    if (rc) return rc;
+  }
   c->incr_zero = false;
   c->boxes_x_valid = false;
   c->weights_x_valid = false;
-  int rc = ensure_pcap(c, n);
-  if (rc) return rc;
   std::vector<double> soa((size_t)EIF_NFIELDS * c->pcap, 0.);
   for (int f = 0; f < EIF_NFIELDS; f++)
     for (int k = 0; k < n; k++) soa[(size_t)f * c->pcap + k] = rec[(size_t)k * EIF_NFIELDS + f];
+  EIF_CK(c, cudaStreamSynchronize(c->stream));
   EIF_CK(c, cudaMemcpy(c->P, soa.data(), sizeof(double) * soa.size(), cudaMemcpyHostToDevice));
   c->np = n;
-  return ibm_reserve(c);
+  return reuse ? EIF_OK : ibm_reserve(c, chunks);
 }
 
 int eif_pull_particles(eif_ctx *c, int n, double *rec) {

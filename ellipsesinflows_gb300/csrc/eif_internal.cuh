@@ -219,7 +219,8 @@ void poisson_free(eif_ctx *c);
 int launch_potential(eif_ctx *c, int rk, bool with_ibm);
 
 // ---- immersed boundary (ibm.cu) ----
-int ibm_reserve(eif_ctx *c);
+size_t ibm_tasks_needed(const eif_ctx *c, const double *rec, int n);
+int ibm_reserve(eif_ctx *c, size_t chunks);
 void ibm_free(eif_ctx *c);
 int launch_inertia(eif_ctx *c, int cn);
 int launch_exchange(eif_ctx *c);

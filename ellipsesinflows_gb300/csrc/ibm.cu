@@ -1017,17 +1017,19 @@ int ibm_prepare(eif_ctx *c) {
   return EIF_OK;
 }
 
-int ibm_reserve(eif_ctx *c) {
-  // called after a particle push: size the chunk and scratch buffers from the radii
+// task bound of a particle set, from the radii in the host records (EIF_NFIELDS per particle)
+size_t ibm_tasks_needed(const eif_ctx *c, const double *rec, int n) {
+  size_t chunks = 0;
+  for (int k = 0; k < n; k++) {
+    chunks += box_tasks_bound(c, std::max(rec[(size_t)k * EIF_NFIELDS + EIF_P_A], rec[(size_t)k * EIF_NFIELDS + EIF_P_B]));
+  }
+  return chunks;
+}
+
+int ibm_reserve(eif_ctx *c, size_t chunks) {
+  // called after a particle push that changed the particle set: size the task and scratch buffers
   ibm_free(c);
   if (c->np == 0) return EIF_OK;
-  std::vector<double> a(c->np), b(c->np);
-  EIF_CK(c, cudaMemcpy(a.data(), c->P + EIF_P_A * c->pcap, sizeof(double) * c->np, cudaMemcpyDeviceToHost));
-  EIF_CK(c, cudaMemcpy(b.data(), c->P + EIF_P_B * c->pcap, sizeof(double) * c->np, cudaMemcpyDeviceToHost));
-  size_t chunks = 0;
-  for (int n = 0; n < c->np; n++) {
-    chunks += box_tasks_bound(c, std::max(a[n], b[n]));
-  }
   c->chunk_cap = (int)chunks;
   c->wcap = chunks * CHUNK;
   EIF_CK(c, cudaMalloc((void **)&c->box, sizeof(int) * 12 * c->np));
