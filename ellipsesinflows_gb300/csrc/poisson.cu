@@ -672,6 +672,378 @@ __global__ void __launch_bounds__(256) k_dct3_df(Dct3ArgsDF a) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Register-radix double-float FFT for power-of-two half lengths m (V <= m <= 512 V).
+//
+// T = m/V threads own one row; each holds V complex values in registers (V = 8 or
+// 16). The Stockham passes are radix V (16 = 4 x 4 and 8 = 4 x 2 splits with
+// constant inner twiddles) and, when log2 m is not a multiple of log2 V, one last
+// pass of a smaller radix R in which each thread does V/R butterflies. Every pass
+// reads its inputs, waits for the whole CTA, and writes its outputs back into the
+// same row buffer, so one buffer of m values (padded by one value every V against
+// bank conflicts) serves the transform. Sums inside a pass keep the trailing part
+// unnormalised (a TwoSum of the leading parts, the trailing parts added in single
+// precision); values are renormalised once before they are stored. The error stays
+// below a small multiple of 2^-47 of the norm of the inputs, as in the radix-4
+// version.
+template <int V> __device__ __forceinline__ int padv(int i) { return i + (i >> (V == 16 ? 4 : 3)); }
+
+__device__ __forceinline__ DF dfl_add(DF x, DF y) {
+  const DF s = two_sum(x.hi, y.hi);
+  return DF{s.hi, s.lo + (x.lo + y.lo)};
+}
+__device__ __forceinline__ DF dfl_sub(DF x, DF y) {
+  const DF s = two_sum(x.hi, -y.hi);
+  return DF{s.hi, s.lo + (x.lo - y.lo)};
+}
+// x y + sgn u v with exact leading products (df_dot2 without the final renormalisation)
+__device__ __forceinline__ DF dfl_dot2(DF x, DF y, DF u, DF v, float sgn) {
+  const float p1 = x.hi * y.hi, p2 = sgn * (u.hi * v.hi);
+  const float e1 = fmaf(x.hi, y.hi, -p1), e2 = fmaf(sgn * u.hi, v.hi, -p2);
+  const DF s = two_sum(p1, p2);
+  float t = fmaf(x.hi, y.lo, e1);
+  t = fmaf(x.lo, y.hi, t);
+  t = fmaf(sgn * u.hi, v.lo, t);
+  t = fmaf(sgn * u.lo, v.hi, t);
+  return DF{s.hi, t + e2 + s.lo};
+}
+__device__ __forceinline__ DF dfl_mulc(DF x, DF c) {
+  const float p = x.hi * c.hi;
+  const float e = fmaf(x.hi, c.lo, fmaf(x.lo, c.hi, fmaf(x.hi, c.hi, -p)));
+  return DF{p, e};
+}
+__device__ __forceinline__ CDF cl_add(CDF a, CDF b) { return CDF{dfl_add(a.re, b.re), dfl_add(a.im, b.im)}; }
+__device__ __forceinline__ CDF cl_sub(CDF a, CDF b) { return CDF{dfl_sub(a.re, b.re), dfl_sub(a.im, b.im)}; }
+__device__ __forceinline__ CDF cl_norm(CDF a) { return CDF{fast_sum(a.re.hi, a.re.lo), fast_sum(a.im.hi, a.im.lo)}; }
+// a w for a twiddle w = (c, s) given as float pairs
+__device__ __forceinline__ CDF cl_mul(CDF a, float4 w) {
+  const DF c = DF{w.x, w.y}, s = DF{w.z, w.w};
+  return CDF{dfl_dot2(a.re, c, a.im, s, -1.f), dfl_dot2(a.re, s, a.im, c, 1.f)};
+}
+// multiplication by S i
+template <int S> __device__ __forceinline__ CDF cl_mul_si(CDF a) {
+  return S > 0 ? CDF{df_neg(a.im), a.re} : CDF{a.im, df_neg(a.re)};
+}
+// sqrt(2)/2 and cos, sin of pi/8 as float pairs
+__device__ __forceinline__ DF k_h() { return DF{0x1.6a09e6p-1f, 0x1.9fcef4p-27f}; }
+__device__ __forceinline__ DF k_c1() { return DF{0x1.d906bcp-1f, 0x1.e651a8p-26f}; }
+__device__ __forceinline__ DF k_s1() { return DF{0x1.87de2ap-2f, 0x1.abaa58p-28f}; }
+// multiplication by exp(S i pi/4) = (sqrt(2)/2)(1 + S i)
+template <int S> __device__ __forceinline__ CDF cl_mul_w8(CDF a) {
+  const DF re = S > 0 ? dfl_sub(a.re, a.im) : dfl_add(a.re, a.im);
+  const DF im = S > 0 ? dfl_add(a.im, a.re) : dfl_sub(a.im, a.re);
+  return CDF{dfl_mulc(re, k_h()), dfl_mulc(im, k_h())};
+}
+// multiplication by c + S i s
+template <int S> __device__ __forceinline__ CDF cl_mul_cs(CDF a, DF c, DF s) {
+  return CDF{dfl_dot2(a.re, c, a.im, s, -(float)S), dfl_dot2(a.im, c, a.re, s, (float)S)};
+}
+
+// radix-4 butterfly on v[o], v[o + st], v[o + 2 st], v[o + 3 st], outputs in natural order
+template <int S, int O, int ST, int N> __device__ __forceinline__ void dft4(CDF (&v)[N]) {
+  const CDF s02 = cl_add(v[O], v[O + 2 * ST]), d02 = cl_sub(v[O], v[O + 2 * ST]);
+  const CDF s13 = cl_add(v[O + ST], v[O + 3 * ST]), d13 = cl_mul_si<S>(cl_sub(v[O + ST], v[O + 3 * ST]));
+  v[O] = cl_add(s02, s13);
+  v[O + ST] = cl_add(d02, d13);
+  v[O + 2 * ST] = cl_sub(s02, s13);
+  v[O + 3 * ST] = cl_sub(d02, d13);
+}
+
+// 16-point DFT of v (sign S), result in natural order
+template <int S> __device__ __forceinline__ void dft16(CDF (&v)[16]) {
+  // n = 4 n1 + n2: transforms over n1 for each n2, result A[n2][k1] in v[n2 + 4 k1]
+  dft4<S, 0, 4>(v);
+  dft4<S, 1, 4>(v);
+  dft4<S, 2, 4>(v);
+  dft4<S, 3, 4>(v);
+  // inner twiddles W16^(n2 k1)
+  v[5] = cl_mul_cs<S>(v[5], k_c1(), k_s1());                 // W^1
+  v[6] = cl_mul_w8<S>(v[6]);                                 // W^2
+  v[7] = cl_mul_cs<S>(v[7], k_s1(), k_c1());                 // W^3
+  v[9] = cl_mul_w8<S>(v[9]);                                 // W^2
+  v[10] = cl_mul_si<S>(v[10]);                               // W^4
+  v[11] = cl_mul_si<S>(cl_mul_w8<S>(v[11]));                 // W^6
+  v[13] = cl_mul_cs<S>(v[13], k_s1(), k_c1());               // W^3
+  v[14] = cl_mul_si<S>(cl_mul_w8<S>(v[14]));                 // W^6
+  {
+    const CDF w = cl_mul_cs<S>(v[15], k_c1(), k_s1());       // W^9 = -W^1
+    v[15] = CDF{df_neg(w.re), df_neg(w.im)};
+  }
+  // transforms over n2 for each k1: X[k1 + 4 k2] lands in v[4 k1 + k2]
+  dft4<S, 0, 1>(v);
+  dft4<S, 4, 1>(v);
+  dft4<S, 8, 1>(v);
+  dft4<S, 12, 1>(v);
+  // transpose the 4 x 4 index so that v[k] = X[k]
+  CDF t;
+  t = v[1]; v[1] = v[4]; v[4] = t;
+  t = v[2]; v[2] = v[8]; v[8] = t;
+  t = v[3]; v[3] = v[12]; v[12] = t;
+  t = v[6]; v[6] = v[9]; v[9] = t;
+  t = v[7]; v[7] = v[13]; v[13] = t;
+  t = v[11]; v[11] = v[14]; v[14] = t;
+}
+
+// 8-point DFT of v[G], ..., v[G + 7] (sign S), result in natural order
+template <int S, int G, int N> __device__ __forceinline__ void dft8(CDF (&v)[N]) {
+  // n = 2 n1 + n2, k = k1 + 4 k2: transforms over n1, A[n2][k1] in v[G + n2 + 2 k1]
+  dft4<S, G, 2>(v);
+  dft4<S, G + 1, 2>(v);
+  v[G + 3] = cl_mul_w8<S>(v[G + 3]);                         // W8^1
+  v[G + 5] = cl_mul_si<S>(v[G + 5]);                         // W8^2
+  v[G + 7] = cl_mul_si<S>(cl_mul_w8<S>(v[G + 7]));           // W8^3
+  CDF w[8];
+#pragma unroll
+  for (int k1 = 0; k1 < 4; k1++) {
+    w[k1] = cl_add(v[G + 2 * k1], v[G + 2 * k1 + 1]);
+    w[k1 + 4] = cl_sub(v[G + 2 * k1], v[G + 2 * k1 + 1]);
+  }
+#pragma unroll
+  for (int k = 0; k < 8; k++) v[G + k] = w[k];
+}
+
+template <int S, int V> __device__ __forceinline__ void dft_full(CDF (&v)[V]) {
+  if constexpr (V == 16) dft16<S>(v);
+  else dft8<S, 0>(v);
+}
+
+// the last pass: radix R (< V) butterflies on groups of R consecutive values
+template <int S, int R, int V> __device__ __forceinline__ void dft_small(CDF (&v)[V]) {
+  if constexpr (R == 2) {
+#pragma unroll
+    for (int q = 0; q < V / 2; q++) {
+      const CDF a = v[2 * q], b = v[2 * q + 1];
+      v[2 * q] = cl_add(a, b);
+      v[2 * q + 1] = cl_sub(a, b);
+    }
+  } else if constexpr (R == 4) {
+    dft4<S, 0, 1>(v);
+    dft4<S, 4, 1>(v);
+    if constexpr (V == 16) {
+      dft4<S, 8, 1>(v);
+      dft4<S, 12, 1>(v);
+    }
+  } else {
+    dft8<S, 0>(v);
+    if constexpr (V == 16) dft8<S, 8>(v);
+  }
+}
+
+template <int S> __device__ __forceinline__ float4 twiddle(const float4 *__restrict__ tw, int e) {
+  float4 w = __ldg(tw + e);
+  if (S > 0) { w.z = -w.z; w.w = -w.w; }
+  return w;
+}
+
+template <int S, int R, int V>
+__device__ __forceinline__ void fft_last(CDF *buf, CDF (&v)[V], int t, int T, int L, const float4 *__restrict__ tw) {
+  // L R = m: butterfly j (< L) reads and writes j + u L, twiddles w^(u j)
+#pragma unroll
+  for (int q = 0; q < V / R; q++) {
+    const int j = t + q * T;
+#pragma unroll
+    for (int u = 0; u < R; u++) {
+      CDF x = buf[padv<V>(j + u * L)];
+      if (u > 0 && j > 0) x = cl_mul(x, twiddle<S>(tw, u * j));
+      v[q * R + u] = x;
+    }
+  }
+  dft_small<S, R, V>(v);
+#pragma unroll
+  for (int q = 0; q < V / R; q++) {
+    const int j = t + q * T;
+#pragma unroll
+    for (int u = 0; u < R; u++) buf[padv<V>(j + u * L)] = cl_norm(v[q * R + u]);
+  }
+}
+
+// Transform of one row: v holds the inputs x[t + u T] of thread t on entry; on
+// exit the spectrum is in buf (padded layout) and visible to the whole CTA.
+template <int S, int V>
+__device__ void fft_row(CDF *buf, CDF (&v)[V], int t, int T, int m, const float4 *__restrict__ tw) {
+  constexpr int LGV = V == 16 ? 4 : 3;
+  dft_full<S, V>(v);
+  __syncthreads();
+#pragma unroll
+  for (int u = 0; u < V; u++) buf[padv<V>(V * t + u)] = cl_norm(v[u]);
+  __syncthreads();
+  int L = V, lgL = LGV;
+  while (L * V <= m) {
+    const int k = t & (L - 1), blk = t >> lgL;
+    const int tws = m >> (lgL + LGV);
+#pragma unroll
+    for (int u = 0; u < V; u++) {
+      CDF x = buf[padv<V>(t + u * T)];
+      if (u > 0 && k > 0) x = cl_mul(x, twiddle<S>(tw, u * k * tws));
+      v[u] = x;
+    }
+    dft_full<S, V>(v);
+    __syncthreads();
+    const int o = blk * L * V + k;
+#pragma unroll
+    for (int u = 0; u < V; u++) buf[padv<V>(o + u * L)] = cl_norm(v[u]);
+    __syncthreads();
+    L <<= LGV;
+    lgL += LGV;
+  }
+  const int R = m / L;
+  if (R > 1) {
+    if (R == 2) fft_last<S, 2, V>(buf, v, t, T, L, tw);
+    else if (R == 4) fft_last<S, 4, V>(buf, v, t, T, L, tw);
+    else if constexpr (V == 16) fft_last<S, 8, V>(buf, v, t, T, L, tw);
+    __syncthreads();
+  }
+}
+
+struct FftShape {
+  int T, lgT, rows;   // threads per row, log2 T, rows per CTA
+};
+
+// values per thread of the register-radix transforms
+constexpr int FFT_V = 8;
+constexpr int FFT_CTA = 128;
+
+// RHS + DCT-II of rows (compute_potential.c:70-92), register-radix transform
+template <int V>
+__global__ void __launch_bounds__(FFT_CTA) k_dct2_dfr(Dct2ArgsDF a, FftShape sh) {
+  extern __shared__ float4 sm4[];
+  const int n = a.itot, m = n / 2, ld = a.ld;
+  const int T = sh.T;
+  const int rloc = threadIdx.x >> sh.lgT, t = threadIdx.x & (T - 1);
+  const int jr = blockIdx.x * sh.rows + rloc;
+  const bool live = jr < a.jtot;
+  const int j = 1 + jr;
+  CDF *buf = reinterpret_cast<CDF *>(sm4) + rloc * (m + m / V);
+  DF *vq = reinterpret_cast<DF *>(buf);
+  if (live) {
+    const DF inv = DF{__ldg(a.coef + 12 + 2 * a.rk), __ldg(a.coef + 13 + 2 * a.rk)};
+#pragma unroll 4
+    for (int i0 = t; i0 < n; i0 += T) {
+      const int i = i0 + 1;
+      DF dux_ = df_of(__ldg(a.ux + ux_idx(i + 1, j, ld)) - __ldg(a.ux + ux_idx(i, j, ld)));
+      DF duy_ = df_of(__ldg(a.uy + uy_idx(i, j + 1, ld)) - __ldg(a.uy + uy_idx(i, j, ld)));
+      if (a.with_ibm) {
+        const int c = uy_idx(i, j, ld);
+        const float dw = (i >= 2) ? __ldg(a.dux + c - 1) : -__ldg(a.dux + c);
+        const float de = (i + 1 <= n) ? __ldg(a.dux + c + 1) : -__ldg(a.dux + c);
+        dux_ = df_add_nw(dux_, df_scale(two_sum(de, -dw), 0.5f));
+        duy_ = df_add_nw(duy_, df_scale(two_sum(__ldg(a.duy + c + ld), -__ldg(a.duy + c - ld)), 0.5f));
+      }
+      // Makhoul order: q[2t] -> v[t], q[2t + 1] -> v[n - 1 - t]
+      const int vpos = (i0 & 1) ? n - 1 - (i0 >> 1) : (i0 >> 1);
+      vq[vpos] = df_mul(inv, df_add_nw(df_mul(dux_, a.rdx), df_mul(duy_, a.rdy)));
+    }
+  }
+  __syncthreads();
+  CDF v[V];
+#pragma unroll
+  for (int u = 0; u < V; u++) v[u] = buf[t + u * T];   // z[s] = v[2s] + i v[2s+1], unpadded
+  fft_row<-1, V>(buf, v, t, T, m, a.tw);
+  if (!live) return;
+  double *out = a.qhat + (size_t)jr * ld;
+#pragma unroll 2
+  for (int kk = t; kk <= m; kk += T) {
+    const CDF zk = buf[padv<V>(kk & (m - 1))];
+    const CDF zm = cdf_conj(buf[padv<V>((m - kk) & (m - 1))]);
+    const CDF sm = cdf_add(zk, zm), df = cdf_sub(zk, zm);
+    const CDF e = CDF{df_scale(sm.re, 0.5f), df_scale(sm.im, 0.5f)};
+    const CDF o = CDF{df_scale(df.im, 0.5f), df_scale(df_neg(df.re), 0.5f)};  // (zk - zm) / 2i
+    const CDF vv = cdf_add(e, cdf_mul(cdf_load(a.wn, kk), o));
+    {
+      const CDF r = cdf_load(a.rot, kk);
+      out[kk] = df_to_double(df_scale(df_dot2(r.re, vv.re, r.im, vv.im, -1.f), 2.f));
+    }
+    if (kk > 0 && kk < m) {
+      const CDF r = cdf_load(a.rot, n - kk);
+      out[n - kk] = df_to_double(df_scale(df_dot2(r.re, vv.re, r.im, df_neg(vv.im), -1.f), 2.f));
+    }
+  }
+}
+
+// block reconstruction + DCT-III + scaling of rows, register-radix transform
+template <int V>
+__global__ void __launch_bounds__(FFT_CTA) k_dct3_dfr(Dct3ArgsDF a, FftShape sh) {
+  extern __shared__ float4 sm4[];
+  const int n = a.itot, m = n / 2, ld = a.ld;
+  const int T = sh.T;
+  const int rloc = threadIdx.x >> sh.lgT, t = threadIdx.x & (T - 1);
+  const int jr = blockIdx.x * sh.rows + rloc;
+  const bool live = jr < a.jtot;
+  const int j = 1 + jr;
+  CDF *buf = reinterpret_cast<CDF *>(sm4) + rloc * (m + m / V);
+  DF *xr = reinterpret_cast<DF *>(buf);
+  if (live) {
+    const double *row = a.qhat + (size_t)jr * ld;
+    if (a.blk > 0) {
+      const int M = a.blk;
+      const int b = jr / M, r = jr % M;
+      const int bm = (b + a.nblk - 1) % a.nblk;
+#pragma unroll 4
+      for (int k = t; k < n; k += T) {
+        DF val;
+        if (r == M - 1) {
+          val = df_of(__ldg(a.iface + (size_t)b * n + k));
+        } else {
+          const float2 gl = __ldg(a.g + (size_t)r * n + k);
+          const float2 gr = __ldg(a.g + (size_t)(M - 2 - r) * n + k);
+          val = df_add_nw(df_add_nw(df_of(__ldg(row + k)), df_mul(df_of(__ldg(a.iface + (size_t)bm * n + k)), DF{gl.x, gl.y})),
+                          df_mul(df_of(__ldg(a.iface + (size_t)b * n + k)), DF{gr.x, gr.y}));
+        }
+        xr[k] = val;
+      }
+    } else {
+      for (int k = t; k < n; k += T) xr[k] = df_of(__ldg(row + k));
+    }
+  }
+  __syncthreads();
+  CDF v[V];
+#pragma unroll
+  for (int u = 0; u < V; u++) {
+    const int s = t + u * T;
+    const int t0 = s, t1 = s + m;
+    const CDF r0 = cdf_conj(cdf_load(a.rot, t0)), r1 = cdf_conj(cdf_load(a.rot, t1));
+    const CDF w0 = cdf_mul(r0, CDF{xr[t0], t0 == 0 ? DF{0.f, 0.f} : df_neg(xr[n - t0])});
+    const CDF w1 = cdf_mul(r1, CDF{xr[t1], df_neg(xr[n - t1])});
+    const CDF sum = cdf_add(w0, w1);
+    const CDF dif = cdf_mul(cdf_sub(w0, w1), cdf_conj(cdf_load(a.wn, s)));
+    v[u] = CDF{df_add_nw(sum.re, df_neg(dif.im)), df_add_nw(sum.im, dif.re)};
+  }
+  fft_row<1, V>(buf, v, t, T, m, a.tw);
+  if (!live) return;
+  double *prow = a.psi + (size_t)j * ld;
+  for (int i = t; i < n; i += T) {
+    const int tt = (i & 1) ? n - 1 - (i >> 1) : (i >> 1);
+    const CDF zz = buf[padv<V>(tt >> 1)];
+    const DF w = (tt & 1) ? zz.im : zz.re;
+    const double val = df_to_double(df_mul(w, a.scale));
+    prow[i + 1] = val;
+    if (j == 1) a.psi[(size_t)(a.jtot + 1) * ld + i + 1] = val;
+    if (j == a.jtot) a.psi[i + 1] = val;
+    if (i == 0) {
+      prow[0] = val;
+      if (j == 1) a.psi[(size_t)(a.jtot + 1) * ld] = val;
+      if (j == a.jtot) a.psi[0] = val;
+    }
+    if (i == n - 1) {
+      prow[n + 1] = val;
+      if (j == 1) a.psi[(size_t)(a.jtot + 1) * ld + n + 1] = val;
+      if (j == a.jtot) a.psi[n + 1] = val;
+    }
+  }
+}
+
+// launch shape of the register-radix transforms, or T = 0 when m is not supported
+// (not a power of two, or more than FFT_CTA threads per row)
+FftShape fftr_shape(int m) {
+  FftShape s{0, 0, 0};
+  if (m < FFT_V || m > FFT_V * FFT_CTA || (m & (m - 1)) != 0) return s;
+  s.T = m / FFT_V;
+  while ((1 << s.lgT) < s.T) s.lgT++;
+  s.rows = FFT_CTA / s.T;
+  return s;
+}
+size_t fftr_smem(int m, int rows) { return sizeof(float4) * (size_t)rows * (m + m / FFT_V); }
+
 bool factorize(int m, int *fac, int *nfac) {
   int k = 0;
   while (m % 4 == 0) { fac[k++] = 4; m /= 4; }
@@ -881,6 +1253,14 @@ int poisson_init(eif_ctx *c) {
     EIF_CK(c, cudaFuncSetAttribute(k_dct2_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     EIF_CK(c, cudaFuncSetAttribute(k_dct3_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   }
+  {
+    const FftShape sh = fftr_shape(pp.m);
+    const size_t smr = sh.T > 0 ? fftr_smem(pp.m, sh.rows) : 0;
+    if (smr > 48 * 1024) {
+      EIF_CK(c, cudaFuncSetAttribute(k_dct2_dfr<FFT_V>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smr));
+      EIF_CK(c, cudaFuncSetAttribute(k_dct3_dfr<FFT_V>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smr));
+    }
+  }
   return EIF_OK;
 }
 
@@ -920,7 +1300,12 @@ int launch_potential(eif_ctx *c, int rk, bool with_ibm) {
     a.rdx = dfpair(1. / c->dx); a.rdy = dfpair(1. / c->dy);
     a.itot = n; a.jtot = jt; a.ld = c->ld; a.with_ibm = with_ibm ? 1 : 0; a.rk = rk;
     EIF_PROF(c, "poisson_dct2", 1);
-    k_dct2_df<<<jt, thr, smem, c->stream>>>(a);
+    const FftShape sh = fftr_shape(pp.m);
+    if (sh.T > 0) {
+      k_dct2_dfr<FFT_V><<<(jt + sh.rows - 1) / sh.rows, sh.T * sh.rows, fftr_smem(pp.m, sh.rows), c->stream>>>(a, sh);
+    } else {
+      k_dct2_df<<<jt, thr, smem, c->stream>>>(a);
+    }
     EIF_LAUNCH_CK(c);
   } else {
     Dct2Args a;
@@ -987,7 +1372,12 @@ int launch_potential(eif_ctx *c, int rk, bool with_ibm) {
     a.scale = dfpair(1. / (2. * n));
     a.itot = n; a.jtot = jt; a.ld = c->ld; a.blk = pp.blk; a.nblk = pp.nblk;
     EIF_PROF(c, "poisson_dct3", 1);
-    k_dct3_df<<<jt, thr, smem, c->stream>>>(a);
+    const FftShape sh = fftr_shape(pp.m);
+    if (sh.T > 0) {
+      k_dct3_dfr<FFT_V><<<(jt + sh.rows - 1) / sh.rows, sh.T * sh.rows, fftr_smem(pp.m, sh.rows), c->stream>>>(a, sh);
+    } else {
+      k_dct3_df<<<jt, thr, smem, c->stream>>>(a);
+    }
     EIF_LAUNCH_CK(c);
   } else {
     Dct3Args a;

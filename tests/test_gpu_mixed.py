@@ -115,10 +115,17 @@ def test_mixed_predictor_matches_fp64(builder, gpu_lib):
     lambda: cases.couette_circle(),
     lambda: cases.poiseuille(itot=384, jtot=768, n=8, a=0.05, b=0.03, seed=6),
     lambda: cases.poiseuille(itot=256, jtot=512, n=24, a=0.04, b=0.02, seed=4),
-], ids=["couette_circle", "poiseuille_384x768", "poiseuille_256x512"])
+    lambda: cases.poiseuille(itot=32, jtot=64, n=1, a=0.2, b=0.1, seed=2),
+    lambda: cases.poiseuille(itot=1024, jtot=2048, n=16, a=0.02, b=0.01, seed=5),
+    lambda: cases.poiseuille(itot=2048, jtot=4096, n=32, a=0.012, b=0.006, seed=3),
+], ids=["couette_circle", "poiseuille_384x768", "poiseuille_256x512", "poiseuille_32x64", "poiseuille_1024x2048",
+        "poiseuille_2048x4096"])
 def test_mixed_poisson_matches_fp64(builder, gpu_lib):
     """The double-float transforms of the mixed form solve the same Poisson problem
-    as the double-precision form to ~1e-12 relative."""
+    as the double-precision form to ~1e-12 relative. The half lengths m = itot/2
+    cover the register-radix (radix-8) transform with a last pass of radix 2
+    (m = 16, 128, 1024) and 4 (m = 32), and the radix-4/2/3 transform of the other
+    lengths (m = 192); m = 512 (no last pass) runs in the step test."""
     from conftest import interior_p
     case = builder()
     d, m = pair(case)
