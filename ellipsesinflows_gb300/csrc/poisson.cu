@@ -905,7 +905,7 @@ constexpr int FFT_CTA = 128;
 
 // RHS + DCT-II of rows (compute_potential.c:70-92), register-radix transform
 template <int V>
-__global__ void __launch_bounds__(FFT_CTA) k_dct2_dfr(Dct2ArgsDF a, FftShape sh) {
+__global__ void __launch_bounds__(FFT_CTA, 8) k_dct2_dfr(Dct2ArgsDF a, FftShape sh) {
   extern __shared__ float4 sm4[];
   const int n = a.itot, m = n / 2, ld = a.ld;
   const int T = sh.T;
@@ -916,22 +916,29 @@ __global__ void __launch_bounds__(FFT_CTA) k_dct2_dfr(Dct2ArgsDF a, FftShape sh)
   CDF *buf = reinterpret_cast<CDF *>(sm4) + rloc * (m + m / V);
   DF *vq = reinterpret_cast<DF *>(buf);
   if (live) {
+    // (1/(gamma dt)) / dx and (1/(gamma dt)) / dy
     const DF inv = DF{__ldg(a.coef + 12 + 2 * a.rk), __ldg(a.coef + 13 + 2 * a.rk)};
+    const DF ax = df_mul(inv, a.rdx), ay = df_mul(inv, a.rdy);
 #pragma unroll 4
     for (int i0 = t; i0 < n; i0 += T) {
       const int i = i0 + 1;
-      DF dux_ = df_of(__ldg(a.ux + ux_idx(i + 1, j, ld)) - __ldg(a.ux + ux_idx(i, j, ld)));
-      DF duy_ = df_of(__ldg(a.uy + uy_idx(i, j + 1, ld)) - __ldg(a.uy + uy_idx(i, j, ld)));
+      // differences of neighbouring doubles (exact), split into float pairs
+      const float2 sx = eifd::split(__ldg(a.ux + ux_idx(i + 1, j, ld)) - __ldg(a.ux + ux_idx(i, j, ld)));
+      const float2 sy = eifd::split(__ldg(a.uy + uy_idx(i, j + 1, ld)) - __ldg(a.uy + uy_idx(i, j, ld)));
+      DF dux_ = DF{sx.x, sx.y}, duy_ = DF{sy.x, sy.y};
       if (a.with_ibm) {
+        // (u + (d0 + de)/2) - (u + (dw + d0)/2) with single-precision field values:
+        // the increments (de - dw)/2 and (en - ds)/2 as exact float sums
         const int c = uy_idx(i, j, ld);
         const float dw = (i >= 2) ? __ldg(a.dux + c - 1) : -__ldg(a.dux + c);
         const float de = (i + 1 <= n) ? __ldg(a.dux + c + 1) : -__ldg(a.dux + c);
-        dux_ = df_add_nw(dux_, df_scale(two_sum(de, -dw), 0.5f));
-        duy_ = df_add_nw(duy_, df_scale(two_sum(__ldg(a.duy + c + ld), -__ldg(a.duy + c - ld)), 0.5f));
+        dux_ = dfl_add(dux_, df_scale(two_sum(de, -dw), 0.5f));
+        duy_ = dfl_add(duy_, df_scale(two_sum(__ldg(a.duy + c + ld), -__ldg(a.duy + c - ld)), 0.5f));
       }
       // Makhoul order: q[2t] -> v[t], q[2t + 1] -> v[n - 1 - t]
       const int vpos = (i0 & 1) ? n - 1 - (i0 >> 1) : (i0 >> 1);
-      vq[vpos] = df_mul(inv, df_add_nw(df_mul(dux_, a.rdx), df_mul(duy_, a.rdy)));
+      const DF q = dfl_add(dfl_mulc(dux_, ax), dfl_mulc(duy_, ay));
+      vq[vpos] = fast_sum(q.hi, q.lo);
     }
   }
   __syncthreads();
@@ -945,24 +952,21 @@ __global__ void __launch_bounds__(FFT_CTA) k_dct2_dfr(Dct2ArgsDF a, FftShape sh)
   for (int kk = t; kk <= m; kk += T) {
     const CDF zk = buf[padv<V>(kk & (m - 1))];
     const CDF zm = cdf_conj(buf[padv<V>((m - kk) & (m - 1))]);
-    const CDF sm = cdf_add(zk, zm), df = cdf_sub(zk, zm);
+    const CDF sm = cl_add(zk, zm), df = cl_sub(zk, zm);
     const CDF e = CDF{df_scale(sm.re, 0.5f), df_scale(sm.im, 0.5f)};
     const CDF o = CDF{df_scale(df.im, 0.5f), df_scale(df_neg(df.re), 0.5f)};  // (zk - zm) / 2i
-    const CDF vv = cdf_add(e, cdf_mul(cdf_load(a.wn, kk), o));
-    {
-      const CDF r = cdf_load(a.rot, kk);
-      out[kk] = df_to_double(df_scale(df_dot2(r.re, vv.re, r.im, vv.im, -1.f), 2.f));
-    }
-    if (kk > 0 && kk < m) {
-      const CDF r = cdf_load(a.rot, n - kk);
-      out[n - kk] = df_to_double(df_scale(df_dot2(r.re, vv.re, r.im, df_neg(vv.im), -1.f), 2.f));
-    }
+    const CDF vv = cl_add(e, cl_mul(o, __ldg(a.wn + kk)));
+    // rot[kk] = (c, s); rot[n - kk] = -i conj(rot[kk]) = (-s, -c)
+    const float4 r = __ldg(a.rot + kk);
+    const DF rc = DF{r.x, r.y}, rs = DF{r.z, r.w};
+    out[kk] = df_to_double(df_scale(dfl_dot2(rc, vv.re, rs, vv.im, -1.f), 2.f));
+    if (kk > 0 && kk < m) out[n - kk] = df_to_double(df_scale(dfl_dot2(rs, vv.re, rc, vv.im, 1.f), -2.f));
   }
 }
 
 // block reconstruction + DCT-III + scaling of rows, register-radix transform
 template <int V>
-__global__ void __launch_bounds__(FFT_CTA) k_dct3_dfr(Dct3ArgsDF a, FftShape sh) {
+__global__ void __launch_bounds__(FFT_CTA, 8) k_dct3_dfr(Dct3ArgsDF a, FftShape sh) {
   extern __shared__ float4 sm4[];
   const int n = a.itot, m = n / 2, ld = a.ld;
   const int T = sh.T;
@@ -984,10 +988,15 @@ __global__ void __launch_bounds__(FFT_CTA) k_dct3_dfr(Dct3ArgsDF a, FftShape sh)
         if (r == M - 1) {
           val = df_of(__ldg(a.iface + (size_t)b * n + k));
         } else {
+          // y + s_left g + s_right h in double-float from the double-precision block solution
           const float2 gl = __ldg(a.g + (size_t)r * n + k);
           const float2 gr = __ldg(a.g + (size_t)(M - 2 - r) * n + k);
-          val = df_add_nw(df_add_nw(df_of(__ldg(row + k)), df_mul(df_of(__ldg(a.iface + (size_t)bm * n + k)), DF{gl.x, gl.y})),
-                          df_mul(df_of(__ldg(a.iface + (size_t)b * n + k)), DF{gr.x, gr.y}));
+          const float2 y = eifd::split(__ldg(row + k));
+          const float2 sl = eifd::split(__ldg(a.iface + (size_t)bm * n + k));
+          const float2 sr = eifd::split(__ldg(a.iface + (size_t)b * n + k));
+          const DF acc = dfl_add(dfl_add(DF{y.x, y.y}, dfl_mulc(DF{sl.x, sl.y}, DF{gl.x, gl.y})),
+                                 dfl_mulc(DF{sr.x, sr.y}, DF{gr.x, gr.y}));
+          val = fast_sum(acc.hi, acc.lo);
         }
         xr[k] = val;
       }
@@ -1001,12 +1010,15 @@ __global__ void __launch_bounds__(FFT_CTA) k_dct3_dfr(Dct3ArgsDF a, FftShape sh)
   for (int u = 0; u < V; u++) {
     const int s = t + u * T;
     const int t0 = s, t1 = s + m;
-    const CDF r0 = cdf_conj(cdf_load(a.rot, t0)), r1 = cdf_conj(cdf_load(a.rot, t1));
-    const CDF w0 = cdf_mul(r0, CDF{xr[t0], t0 == 0 ? DF{0.f, 0.f} : df_neg(xr[n - t0])});
-    const CDF w1 = cdf_mul(r1, CDF{xr[t1], df_neg(xr[n - t1])});
-    const CDF sum = cdf_add(w0, w1);
-    const CDF dif = cdf_mul(cdf_sub(w0, w1), cdf_conj(cdf_load(a.wn, s)));
-    v[u] = CDF{df_add_nw(sum.re, df_neg(dif.im)), df_add_nw(sum.im, dif.re)};
+    float4 r0 = __ldg(a.rot + t0), r1 = __ldg(a.rot + t1), wn = __ldg(a.wn + s);
+    r0.z = -r0.z; r0.w = -r0.w;
+    r1.z = -r1.z; r1.w = -r1.w;
+    wn.z = -wn.z; wn.w = -wn.w;
+    const CDF w0 = cl_mul(CDF{xr[t0], t0 == 0 ? DF{0.f, 0.f} : df_neg(xr[n - t0])}, r0);
+    const CDF w1 = cl_mul(CDF{xr[t1], df_neg(xr[n - t1])}, r1);
+    const CDF sum = cl_add(w0, w1);
+    const CDF dif = cl_mul(cl_sub(w0, w1), wn);
+    v[u] = CDF{dfl_sub(sum.re, dif.im), dfl_add(sum.im, dif.re)};
   }
   fft_row<1, V>(buf, v, t, T, m, a.tw);
   if (!live) return;
@@ -1015,7 +1027,7 @@ __global__ void __launch_bounds__(FFT_CTA) k_dct3_dfr(Dct3ArgsDF a, FftShape sh)
     const int tt = (i & 1) ? n - 1 - (i >> 1) : (i >> 1);
     const CDF zz = buf[padv<V>(tt >> 1)];
     const DF w = (tt & 1) ? zz.im : zz.re;
-    const double val = df_to_double(df_mul(w, a.scale));
+    const double val = df_to_double(dfl_mulc(w, a.scale));
     prow[i + 1] = val;
     if (j == 1) a.psi[(size_t)(a.jtot + 1) * ld + i + 1] = val;
     if (j == a.jtot) a.psi[i + 1] = val;
