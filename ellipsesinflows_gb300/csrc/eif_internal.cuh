@@ -147,7 +147,7 @@ struct eif_ctx {
   size_t wcap;                  // capacity of wbuf in cells
   int chunk_cap;                // capacity of partial in chunks
   float *pf;                    // per-particle single-precision parameters (mixed form)
-  int *owner;                   // owner particle of every chunk (mixed form)
+  int4 *tdesc;                  // task table: particle, row, columns and image of every chunk
   int *band_lists, *band_counts;// ordered (particle, image) lists per band of gather rows
   int band_cap;
   // device scalars

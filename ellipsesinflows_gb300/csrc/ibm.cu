@@ -240,16 +240,6 @@ __global__ void k_scan(const int *__restrict__ cnt, int *__restrict__ off, int n
   if (threadIdx.x == 0 && EIF_CHK(bd.rec, np, bd.off, 6)) off[np] = carry;
 }
 
-// owner particle of every chunk (replaces a search per chunk)
-__global__ void k_chunk_owner(const int *__restrict__ off, int *__restrict__ owner, int np, Bounds bd, int cap) {
-  const int n = blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= np) return;
-  const int c0 = off[n], c1 = off[n + 1];
-  for (int c = c0; c < c1; c++) {
-    if (EIF_CHK(bd.rec, c, cap, 59)) owner[c] = n;
-  }
-}
-
 // A particle's tasks: image by image, row by row, segment by segment.
 struct RowTask {
   int img, j, ib, ie;   // image -1..1, row, first and last column of the segment
@@ -276,6 +266,33 @@ __device__ __forceinline__ bool row_task_in(int4 b, int img, int &r, RowTask &t)
 // task r of a particle whose image boxes are bm, b0, bp (images -1, 0, +1)
 __device__ __forceinline__ bool row_task(int4 bm, int4 b0, int4 bp, int r, RowTask &t) {
   return row_task_in(bm, -1, r, t) || row_task_in(b0, 0, r, t) || row_task_in(bp, 1, r, t);
+}
+
+// The task table: one int4 per task (chunk) {particle, row, first column, last
+// column * 4 + image + 1}, so that a kernel finds its task's geometry with one
+// load instead of a chain of dependent loads (owner, boxes, offsets). One warp
+// per particle.
+__global__ void k_task_table(const int *__restrict__ box, const int *__restrict__ off, int4 *__restrict__ tdesc,
+                             int np, Bounds bd, int cap) {
+  const int n = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (n >= np) return;
+  const int4 *b4 = reinterpret_cast<const int4 *>(box + 12 * n);
+  const int4 bA = b4[0], bB = b4[1], bC = b4[2];
+  const int c0 = off[n], c1 = off[n + 1];
+  for (int c = c0 + lane; c < c1; c += 32) {
+    RowTask t;
+    int4 d = make_int4(-1, 0, 0, 0);
+    if (row_task(bA, bB, bC, c - c0, t)) d = make_int4(n, t.j, t.ib, t.ie * 4 + t.img + 1);
+    if (EIF_CHK(bd.rec, c, cap, 59)) tdesc[c] = d;
+  }
+}
+__device__ __forceinline__ bool task_of(int4 d, int np, RowTask &t) {
+  t.j = d.y;
+  t.ib = d.z;
+  t.ie = d.w >> 2;
+  t.img = (d.w & 3) - 1;
+  return d.x >= 0 && d.x < np;
 }
 
 // The far-cell bounds above along one row, as ranges of the lab-frame offset
@@ -314,7 +331,7 @@ struct WorkArgs {
   int pcap, np, ld, mode, cn;   // mode 0: inertia (cn), 1: exchange
   double dx, dy, ly, h;
   const float *pf;       // per-particle single-precision parameters (mixed form)
-  const int *owner;      // owner particle of every chunk (mixed form)
+  const int4 *tdesc;     // task table (k_task_table)
   const float *coef;     // single-precision dt products; [9] = 1/dt
   float rh_f, dx_f, dy_f, dxdy_f;
   // Indicator weights of the cells at the positions X are kept in wcache (one per
@@ -348,14 +365,12 @@ __global__ void __launch_bounds__(256) k_ibm_work(WorkArgs a) {
   double2 *slots = slot_buf[threadIdx.x >> 5];
   for (int c = warp; c < total; c += nwarps) {
     if (!EIF_CHK(a.bd.rec, c, a.bd.partial / 3, 21)) continue;
-    const int n = __ldg(a.owner + c);
+    const int4 dsc = __ldg(a.tdesc + c);
+    const int n = dsc.x;
     if (!EIF_CHK(a.bd.rec, n, a.np, 11)) continue;
-    if (!EIF_CHK(a.bd.rec, 12 * n + 11, a.bd.box, 12)) continue;
     if (!EIF_CHK(a.bd.rec, EIF_P_VZ * pc + n, a.bd.P, 13)) continue;
-    const int4 *b4 = reinterpret_cast<const int4 *>(a.box + 12 * n);
-    const int4 bA = __ldg(b4), bB = __ldg(b4 + 1), bC = __ldg(b4 + 2);
     RowTask t;
-    const bool task = row_task(bA, bB, bC, c - __ldg(a.off + n), t) && EIF_CHK(a.bd.rec, t.j, a.bd.yc - 1, 15);
+    const bool task = task_of(dsc, a.np, t) && EIF_CHK(a.bd.rec, t.j, a.bd.yc - 1, 15);
     const double *P = a.P;
     const double pden = __ldg(P + EIF_P_DEN * pc + n), pa = __ldg(P + EIF_P_A * pc + n), pb = __ldg(P + EIF_P_B * pc + n);
     double px = __ldg(P + EIF_P_X * pc + n), py = __ldg(P + EIF_P_Y * pc + n), paz = __ldg(P + EIF_P_AZ * pc + n);
@@ -581,12 +596,11 @@ __global__ void __launch_bounds__(256, 3) k_ibm_work_f(WorkArgs a) {
   float2 *slots = slot_buf[threadIdx.x >> 5];
   for (int c = warp; c < total; c += nwarps) {
     if (!EIF_CHK(a.bd.rec, c, a.bd.partial / 3, 51)) continue;
-    const int n = __ldg(a.owner + c);
-    if (!EIF_CHK(a.bd.rec, n, a.np, 52) || !EIF_CHK(a.bd.rec, 12 * n + 11, a.bd.box, 53)) continue;
-    const int4 *b4 = reinterpret_cast<const int4 *>(a.box + 12 * n);
-    const int4 bA = __ldg(b4), bB = __ldg(b4 + 1), bC = __ldg(b4 + 2);
+    const int4 dsc = __ldg(a.tdesc + c);
+    const int n = dsc.x;
+    if (!EIF_CHK(a.bd.rec, n, a.np, 52)) continue;
     RowTask t;
-    const bool task = row_task(bA, bB, bC, c - __ldg(a.off + n), t);
+    const bool task = task_of(dsc, a.np, t);
     const float4 *q4 = reinterpret_cast<const float4 *>(a.pf + (size_t)PF_WORDS * n);
     const float4 qA = __ldg(q4), qB = __ldg(q4 + 1), qC = __ldg(q4 + 2), qD = __ldg(q4 + 3), qE = __ldg(q4 + 4);
     const float4 qF = __ldg(q4 + 5), qG = __ldg(q4 + 6);
@@ -733,11 +747,11 @@ __global__ void __launch_bounds__(256, 4) k_ibm_sum_f(WorkArgs a) {
   const float *wcache = static_cast<const float *>(a.wcache);
   for (int c = warp; c < total; c += nwarps) {
     if (!EIF_CHK(a.bd.rec, c, a.bd.partial / 3, 71)) continue;
-    const int n = __ldg(a.owner + c);
-    if (!EIF_CHK(a.bd.rec, n, a.np, 72) || !EIF_CHK(a.bd.rec, 12 * n + 11, a.bd.box, 73)) continue;
-    const int4 *b4 = reinterpret_cast<const int4 *>(a.box + 12 * n);
+    const int4 dsc = __ldg(a.tdesc + c);
+    const int n = dsc.x;
+    if (!EIF_CHK(a.bd.rec, n, a.np, 72)) continue;
     RowTask t;
-    const bool task = row_task(__ldg(b4), __ldg(b4 + 1), __ldg(b4 + 2), c - __ldg(a.off + n), t);
+    const bool task = task_of(dsc, a.np, t);
     const float4 *q4 = reinterpret_cast<const float4 *>(a.pf + (size_t)PF_WORDS * n);
     const float4 qB = __ldg(q4 + 1), qC = __ldg(q4 + 2), qD = __ldg(q4 + 3), qE = __ldg(q4 + 4);
     const float rpm = qB.z, rpim = qB.w, pux = qC.x, puy = qC.y, pvz = qC.z, gx = qC.w;
@@ -1038,7 +1052,7 @@ int ibm_reserve(eif_ctx *c, size_t chunks) {
   EIF_CK(c, cudaMalloc((void **)&c->wbuf, sizeof(double2) * c->wcap));
   EIF_CK(c, cudaMalloc((void **)&c->wcache, sizeof(double) * c->wcap));
   EIF_CK(c, cudaMalloc((void **)&c->pf, sizeof(float) * PF_WORDS * c->np));
-  EIF_CK(c, cudaMalloc((void **)&c->owner, sizeof(int) * (size_t)chunks));
+  EIF_CK(c, cudaMalloc((void **)&c->tdesc, sizeof(int4) * (size_t)chunks));
   const int nbands = (c->jtot + GTY - 1) / GTY;
   c->band_cap = 3 * c->np;
   EIF_CK(c, cudaMalloc((void **)&c->band_lists, sizeof(int) * (size_t)nbands * c->band_cap));
@@ -1054,14 +1068,14 @@ void ibm_free(eif_ctx *c) {
   if (c->wbuf) cudaFree(c->wbuf);
   if (c->wcache) cudaFree(c->wcache);
   if (c->pf) cudaFree(c->pf);
-  if (c->owner) cudaFree(c->owner);
+  if (c->tdesc) cudaFree(c->tdesc);
   if (c->band_lists) cudaFree(c->band_lists);
   if (c->band_counts) cudaFree(c->band_counts);
   if (c->band_marks) cudaFree(c->band_marks);
   c->band_lists = nullptr; c->band_counts = nullptr; c->band_marks = nullptr;
   c->box = nullptr; c->chunk_off = nullptr; c->partial = nullptr; c->wbuf = nullptr; c->wcache = nullptr;
   c->weights_x_valid = false;
-  c->pf = nullptr; c->owner = nullptr;
+  c->pf = nullptr; c->tdesc = nullptr;
   c->chunk_cap = 0; c->wcap = 0;
 }
 
@@ -1102,8 +1116,8 @@ static int launch_boxes(eif_ctx *c, bool use_increment) {
   EIF_LAUNCH_CK(c);
   k_scan<<<1, 1024, 0, c->stream>>>(cnt, c->chunk_off, c->np, bounds_of(c));
   EIF_LAUNCH_CK(c);
-  k_chunk_owner<<<(c->np + 127) / 128, 128, 0, c->stream>>>(c->chunk_off, c->owner, c->np, bounds_of(c),
-                                                             c->chunk_cap);
+  k_task_table<<<(c->np * 32 + 255) / 256, 256, 0, c->stream>>>(c->box, c->chunk_off, c->tdesc, c->np, bounds_of(c),
+                                                                 c->chunk_cap);
   EIF_LAUNCH_CK(c);
   c->boxes_x_valid = x_only;
   return EIF_OK;
@@ -1117,7 +1131,7 @@ static int launch_work(eif_ctx *c, int mode, int cn) {
   w.dx = c->dx; w.dy = c->dy; w.ly = c->ly; w.h = std::min(c->dx, c->dy);
   w.bd = bounds_of(c);
   w.pf = c->pf;
-  w.owner = c->owner;
+  w.tdesc = c->tdesc;
   w.coef = c->d_coef;
   w.rh_f = (float)(1. / w.h);
   w.dx_f = (float)c->dx;
