@@ -55,7 +55,7 @@ FALLBACK_HBM_GBS = 6800.0
 # written). The mixed form keeps the IBM field in single precision.
 HBM_BYTES = {
     "fp64": {"predictor": 72, "correct": 72, "poisson_dct2": 40, "poisson_dct3": 16},
-    "mixed": {"predictor": 72, "correct": 64, "poisson_dct2": 32, "poisson_dct3": 16},
+    "mixed": {"predictor": 56, "correct": 64, "poisson_dct2": 32, "poisson_dct3": 16},
 }
 
 

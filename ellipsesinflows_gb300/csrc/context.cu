@@ -189,8 +189,8 @@ int ensure_pcap(eif_ctx *c, int n) {
   EIF_CK(c, cudaMalloc((void **)&c->P, sizeof(double) * EIF_NFIELDS * (size_t)cap));
   EIF_CK(c, cudaMemset(c->P, 0, sizeof(double) * EIF_NFIELDS * (size_t)cap));
   EIF_CK(c, cudaMalloc((void **)&c->cpf, sizeof(float4) * (size_t)cap));
-  EIF_CK(c, cudaMalloc((void **)&c->cand, sizeof(int) * EIF_CAND_SPLIT * EIF_CAND_CAP * (size_t)cap));
-  EIF_CK(c, cudaMalloc((void **)&c->cand_n, sizeof(int) * EIF_CAND_SPLIT * (size_t)cap));
+  EIF_CK(c, cudaMalloc((void **)&c->cand, sizeof(int) * EIF_CAND_CAP * (size_t)cap));
+  EIF_CK(c, cudaMalloc((void **)&c->cand_n, sizeof(int) * (size_t)cap));
   c->pcap = cap;
   return EIF_OK;
 }

@@ -41,10 +41,8 @@
 #include <vector>
 #include <string>
 
-// collision candidate lists: the partner range is cut into EIF_CAND_SPLIT pieces,
-// each with room for EIF_CAND_CAP candidates per particle (particles.cu)
-#define EIF_CAND_SPLIT 8
-#define EIF_CAND_CAP 16
+// collision candidate lists: room for EIF_CAND_CAP candidates per particle (particles.cu)
+#define EIF_CAND_CAP 64
 
 namespace eif {
 
@@ -138,7 +136,7 @@ struct eif_ctx {
   int ibm_ctas_per_sm[3] = {0, 0, 0};  // resident CTAs per SM of the IBM work kernels (FP64, mixed, mixed cached)
   unsigned *band_marks = nullptr;  // per band of 8 rows: bitmap over the 3*np (particle, image) boxes
   float4 *cpf = nullptr;
-  int *cand = nullptr, *cand_n = nullptr;  // collision candidates (np * EIF_CAND_SPLIT * EIF_CAND_CAP), counts        // pcap: single-precision x + dx, y + dy, max(a, b) for the collision prefilter
+  int *cand = nullptr, *cand_n = nullptr;  // collision candidates (np * EIF_CAND_CAP), counts        // pcap: single-precision x + dx, y + dy, max(a, b) for the collision prefilter
   // immersed-boundary work
   int *box;                     // per particle: 3 images x {imin,imax,jmin,jmax}
   int *chunk_off;               // per particle: first chunk (exclusive scan), [np] = total

@@ -594,9 +594,12 @@ __global__ void __launch_bounds__(256, 3) k_ibm_work_f(WorkArgs a) {
   // per warp: body-frame offsets of its near cells, overwritten by their weights
   __shared__ float2 slot_buf[8][CHUNK];
   float2 *slots = slot_buf[threadIdx.x >> 5];
+  // the next task's table entry is loaded while the current task is processed
+  int4 nxt = make_int4(-1, 0, 0, 0);
+  if (warp < total && EIF_CHK(a.bd.rec, warp, a.bd.partial / 3, 51)) nxt = __ldg(a.tdesc + warp);
   for (int c = warp; c < total; c += nwarps) {
-    if (!EIF_CHK(a.bd.rec, c, a.bd.partial / 3, 51)) continue;
-    const int4 dsc = __ldg(a.tdesc + c);
+    const int4 dsc = nxt;
+    if (c + nwarps < total && EIF_CHK(a.bd.rec, c + nwarps, a.bd.partial / 3, 51)) nxt = __ldg(a.tdesc + c + nwarps);
     const int n = dsc.x;
     if (!EIF_CHK(a.bd.rec, n, a.np, 52)) continue;
     RowTask t;
@@ -745,9 +748,12 @@ __global__ void __launch_bounds__(256, 4) k_ibm_sum_f(WorkArgs a) {
   const int ld = a.ld;
   float2 *wb = reinterpret_cast<float2 *>(a.wbuf);
   const float *wcache = static_cast<const float *>(a.wcache);
+  // the next task's table entry is loaded while the current task is processed
+  int4 nxt = make_int4(-1, 0, 0, 0);
+  if (warp < total && EIF_CHK(a.bd.rec, warp, a.bd.partial / 3, 71)) nxt = __ldg(a.tdesc + warp);
   for (int c = warp; c < total; c += nwarps) {
-    if (!EIF_CHK(a.bd.rec, c, a.bd.partial / 3, 71)) continue;
-    const int4 dsc = __ldg(a.tdesc + c);
+    const int4 dsc = nxt;
+    if (c + nwarps < total && EIF_CHK(a.bd.rec, c + nwarps, a.bd.partial / 3, 71)) nxt = __ldg(a.tdesc + c + nwarps);
     const int n = dsc.x;
     if (!EIF_CHK(a.bd.rec, n, a.np, 72)) continue;
     RowTask t;

@@ -222,63 +222,86 @@ __global__ void k_collision_prep(const double *__restrict__ P, int pcap, int np,
   cpf[n] = make_float4(eifd::d2f(v.x), eifd::d2f(v.y), eifd::d2f(fmax(v.a, v.b)), 0.f);
 }
 
-// Candidate partners. Block (x, s) tests particles 128x .. 128x+127 against the
-// partners of split s (the partner range cut into CSPLIT pieces, so the O(N^2)
-// scan covers many SMs). Partners' single-precision centres are staged in shared
-// memory; pairs that pass the conservative single-precision test get the exact
-// double-precision bounding-circle test of collision.c:173-189 (canonical
-// orientation), and hits are stored in partner order per (particle, split).
-constexpr int PAIR_TILE = 128;
-constexpr int CSPLIT = EIF_CAND_SPLIT;
-constexpr int CAND_CAP = EIF_CAND_CAP;   // candidates per particle and split
+// Candidate partners: one warp per particle k, whose lanes test the partners
+// m = lane, lane + 32, ... in order against the partners' single-precision centres
+// and bounding radii (k_collision_prep), staged in shared memory tile by tile. The
+// pairs that pass this conservative test are listed in partner order (ballot and
+// prefix count); afterwards the lanes give them the exact double-precision
+// bounding-circle test of collision.c:173-189 (canonical orientation) together,
+// and the hits are compacted in order.
+constexpr int CAND_CAP = EIF_CAND_CAP;   // candidates per particle
+constexpr int PAIR_WARPS = 8;
+constexpr int PAIR_TILE = 1024;
+constexpr int PAIR_LOADS = PAIR_TILE / (PAIR_WARPS * 32);
 
-__global__ void __launch_bounds__(PAIR_TILE) k_coll_pairs(const double *__restrict__ P, const float4 *__restrict__ cpf,
-                                                          int pcap, int np, double ly, int *__restrict__ cand,
-                                                          int *__restrict__ cand_n, unsigned *__restrict__ flags) {
+__global__ void __launch_bounds__(PAIR_WARPS * 32) k_coll_pairs(const double *__restrict__ P, const float4 *__restrict__ cpf,
+                                                               int pcap, int np, double ly, int *__restrict__ cand,
+                                                               int *__restrict__ cand_n, unsigned *__restrict__ flags) {
   __shared__ float4 tile[PAIR_TILE];
-  const int k = blockIdx.x * PAIR_TILE + threadIdx.x;
-  const int split = blockIdx.y;
-  const bool on = k < np;
+  __shared__ int maybe_list[PAIR_WARPS][CAND_CAP];
+  const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+  const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const bool on = k < np;   // uniform over the warp
   const float4 fk = on ? __ldg(cpf + k) : make_float4(0.f, 0.f, 0.f, 0.f);
   const float lyf = eifd::d2f(ly);
-  const int per_split = (np + CSPLIT - 1) / CSPLIT;
-  const int m0 = split * per_split, m1 = min(np, m0 + per_split);
-  int cnt = 0;
-  for (int base = m0; base < m1; base += PAIR_TILE) {
+  int nmaybe = 0;
+  for (int t0 = 0; t0 < np; t0 += PAIR_TILE) {
+    const int nt = min(PAIR_TILE, np - t0);
+    float4 st[PAIR_LOADS];
+#pragma unroll
+    for (int r = 0; r < PAIR_LOADS; r++) {
+      const int q = threadIdx.x + r * PAIR_WARPS * 32;
+      st[r] = q < nt ? __ldg(cpf + t0 + q) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
     __syncthreads();
-    const int mm = base + threadIdx.x;
-    if (mm < m1) tile[threadIdx.x] = __ldg(cpf + mm);
+#pragma unroll
+    for (int r = 0; r < PAIR_LOADS; r++) tile[threadIdx.x + r * PAIR_WARPS * 32] = st[r];
     __syncthreads();
     if (!on) continue;
-    const int nt = min(PAIR_TILE, m1 - base);
-    for (int t = 0; t < nt; t++) {
-      const float4 fm = tile[t];
-      // conservative single-precision test: skip only pairs clearly apart for every image
-      const float rs = fk.z + fm.z;
-      const float dxf = fm.x - fk.x;
-      const float lim = rs * rs * 1.001f + 1e-6f;
+#pragma unroll 2
+    for (int base = 0; base < nt; base += 32) {
+      const int m = t0 + base + lane;
       bool maybe = false;
+      if (base + lane < nt && m != k) {
+        const float4 fm = tile[base + lane];
+        // conservative single-precision test: skip only pairs clearly apart for every image
+        const float rs = fk.z + fm.z;
+        const float dxf = fm.x - fk.x;
+        const float lim = rs * rs * 1.001f + 1e-6f;
 #pragma unroll
-      for (int per = -1; per <= 1; per++) {
-        const float dyf = fm.y + lyf * per - fk.y;
-        maybe |= dxf * dxf + dyf * dyf <= lim;
-      }
-      const int m = base + t;
-      if (maybe && m != k) {
-        const PV pk = load_pv(P, pcap, k);
-        const PV pm_ = load_pv(P, pcap, m);
-        const bool hit = m < k ? bounding_overlap(pm_, pk, ly) : bounding_overlap(pk, pm_, ly);
-        if (hit) {
-          if (cnt < CAND_CAP) cand[((size_t)k * CSPLIT + split) * CAND_CAP + cnt] = m;
-          cnt++;
+        for (int per = -1; per <= 1; per++) {
+          const float dyf = fm.y + lyf * per - fk.y;
+          maybe |= dxf * dxf + dyf * dyf <= lim;
         }
       }
+      const unsigned mask = __ballot_sync(0xffffffffu, maybe);
+      if (maybe) {
+        const int r = nmaybe + __popc(mask & ((1u << lane) - 1u));
+        if (r < CAND_CAP) maybe_list[wl][r] = m;
+      }
+      nmaybe += __popc(mask);
     }
   }
-  if (on) {
-    cand_n[(size_t)k * CSPLIT + split] = min(cnt, CAND_CAP);
-    if (cnt > CAND_CAP) atomicOr(flags, EIF_FLAG_NOCONV);
+  if (!on) return;
+  __syncwarp();
+  if (nmaybe > CAND_CAP && lane == 0) atomicOr(flags, EIF_FLAG_NOCONV);
+  nmaybe = min(nmaybe, CAND_CAP);
+  int cnt = 0;
+  for (int base = 0; base < nmaybe; base += 32) {
+    const int q = base + lane;
+    bool hit = false;
+    int m = 0;
+    if (q < nmaybe) {
+      m = maybe_list[wl][q];
+      const PV pk = load_pv(P, pcap, k);
+      const PV pm_ = load_pv(P, pcap, m);
+      hit = m < k ? bounding_overlap(pm_, pk, ly) : bounding_overlap(pk, pm_, ly);
+    }
+    const unsigned mask = __ballot_sync(0xffffffffu, hit);
+    if (hit) cand[(size_t)k * CAND_CAP + cnt + __popc(mask & ((1u << lane) - 1u))] = m;
+    cnt += __popc(mask);
   }
+  if (lane == 0) cand_n[k] = cnt;
 }
 
 // Collision force on particle k (one warp): its candidate pairs are evaluated one
@@ -290,13 +313,7 @@ __global__ void __launch_bounds__(CWARPS * 32) k_collision(double *__restrict__ 
   const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
   const int k = blockIdx.x * CWARPS + wl;
   if (k >= np) return;
-  int ns[CSPLIT];
-  int total = 0;
-#pragma unroll
-  for (int s = 0; s < CSPLIT; s++) {
-    ns[s] = __ldg(cand_n + (size_t)k * CSPLIT + s);
-    total += ns[s];
-  }
+  const int total = __ldg(cand_n + k);
   const PV pk = load_pv(P, pcap, k);
   double acc0 = 0., acc1 = 0., acc2 = 0.;
   bool ok_all = true;
@@ -304,13 +321,7 @@ __global__ void __launch_bounds__(CWARPS * 32) k_collision(double *__restrict__ 
     const int q = base + lane;
     const int ncand = min(32, total - base);
     if (q < total) {
-      // q-th candidate in (split, slot) order
-      int s = 0, r = q;
-#pragma unroll
-      for (int t = 0; t < CSPLIT - 1; t++) {
-        if (s == t && r >= ns[t]) { r -= ns[t]; s = t + 1; }
-      }
-      const int mm = __ldg(cand + ((size_t)k * CSPLIT + s) * CAND_CAP + r);
+      const int mm = __ldg(cand + (size_t)k * CAND_CAP + q);
       const PV pmm = load_pv(P, pcap, mm);
       double out[3];
       bool ok;
@@ -435,7 +446,7 @@ int launch_collision(eif_ctx *c, int cn) {
   EIF_PROF(c, "collision", 3);
   k_collision_prep<<<(c->np + 127) / 128, 128, 0, c->stream>>>(c->P, c->pcap, c->np, c->cpf);
   EIF_LAUNCH_CK(c);
-  k_coll_pairs<<<dim3((c->np + PAIR_TILE - 1) / PAIR_TILE, CSPLIT), PAIR_TILE, 0, c->stream>>>(
+  k_coll_pairs<<<(c->np + PAIR_WARPS - 1) / PAIR_WARPS, PAIR_WARPS * 32, 0, c->stream>>>(
       c->P, c->cpf, c->pcap, c->np, c->ly, c->cand, c->cand_n, c->d_flags);
   EIF_LAUNCH_CK(c);
   k_collision<<<(c->np + CWARPS - 1) / CWARPS, CWARPS * 32, 0, c->stream>>>(c->P, c->cand, c->cand_n, c->pcap, c->np,
