@@ -148,6 +148,7 @@ struct eif_ctx {
   int4 *tdesc;                  // task table: particle, row, columns and image of every chunk
   int *band_lists, *band_counts;// ordered (particle, image) lists per band of gather rows
   int band_cap;
+  int4 *edesc = nullptr;        // per (particle, image): box, row pitch and scratch offset (gather)
   // device scalars
   double *d_scal;               // [0] dt, [1] residual, [2] scratch
   float *d_coef;                // single-precision dt products: [3*rk+0..2] alpha/beta/gamma*dt, [9] 1/dt,

@@ -37,7 +37,7 @@ __device__ __host__ __forceinline__ int box_segs(int w) { return (w + CHUNK - 1)
 constexpr int NEXTRA = 3;       // auxiliary.c:8
 constexpr double BETA = 2.;     // auxiliary.c:49
 constexpr int GTX = 64, GTY = 8, GTHREADS = 256;  // gather tile and block
-constexpr int LMAX = 256;       // gather entries staged in shared memory at a time
+constexpr int LMAX = 256;       // gather entries staged in shared memory at a time (GTHREADS)
 
 // per-particle geometry needed by a box cell evaluation
 struct Ell {
@@ -851,17 +851,28 @@ __global__ void k_chunk_reduce(const double *__restrict__ partial, const int *__
 // Step 1 (one thread per particle): every box sets its bit in the bitmap of each
 // band it reaches (atomicOr: the result does not depend on the order). Step 2
 // (one warp per band): the band's set bits are compacted in index order.
-__global__ void k_band_marks(const int *__restrict__ box, int np, int jtot, unsigned *__restrict__ marks,
-                             int words) {
+__global__ void k_band_marks(const int *__restrict__ box, const int *__restrict__ off, int np, int jtot,
+                             unsigned *__restrict__ marks, int words, int4 *__restrict__ edesc, Bounds bd) {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= np) return;
   const int nbands = (jtot + GTY - 1) / GTY;
+  const int *bx = box + 12 * n;
+  int tasks_q = 0;   // tasks of the earlier images
+  const int off_n = off[n];
 #pragma unroll
   for (int q = 0; q < 3; q++) {
-    const int *bx = box + 12 * n + 4 * q;
-    if (bx[1] < bx[0] || bx[3] < bx[2]) continue;
+    const int bi0 = bx[4 * q], bi1 = bx[4 * q + 1], bj0 = bx[4 * q + 2], bj1 = bx[4 * q + 3];
+    const bool nonempty = bi1 >= bi0 && bj1 >= bj0;
     const int e = 3 * n + q;
-    const int b0 = max(0, (bx[2] - 1) / GTY), b1 = min(nbands - 1, (bx[3] - 1) / GTY);
+    // the entry's box and where its rows start in the scratch buffer (a box row
+    // occupies segs * CHUNK slots)
+    if (EIF_CHK(bd.rec, 2LL * e + 1, 6LL * np, 47)) {
+      edesc[2 * e] = nonempty ? make_int4(bi0, bi1, bj0, bj1) : make_int4(1, 0, 1, 0);
+      edesc[2 * e + 1] = make_int4(nonempty ? box_segs(bi1 - bi0 + 1) * CHUNK : 0, (off_n + tasks_q) * CHUNK, 0, 0);
+    }
+    if (!nonempty) continue;
+    tasks_q += (bj1 - bj0 + 1) * box_segs(bi1 - bi0 + 1);
+    const int b0 = max(0, (bj0 - 1) / GTY), b1 = min(nbands - 1, (bj1 - 1) / GTY);
     for (int b = b0; b <= b1; b++) atomicOr(marks + (size_t)b * words + (e >> 5), 1u << (e & 31));
   }
 }
@@ -900,7 +911,7 @@ __global__ void k_band_lists(const unsigned *__restrict__ marks, int words, int 
 }
 
 struct GatherArgs {
-  const int *box, *off;
+  const int4 *edesc;   // per (particle, image) entry: box, then row pitch and scratch offset
   const int *lists, *counts;
   int cap;
   const void *wbuf;
@@ -910,58 +921,60 @@ struct GatherArgs {
   Bounds bd;
 };
 
-// field response dux/duy (exchange.c:71-72,80-81): per tile, the ordered list
-// of covering (particle, image) boxes, then per cell the sum in that order
+// field response dux/duy (exchange.c:71-72,80-81): per tile, the entries of the
+// band's ordered list that reach the tile's columns are compacted in order into
+// shared memory, then every cell sums their contributions in that order
 template <typename V2, typename Acc>
-__global__ void __launch_bounds__(GTHREADS) k_gather(GatherArgs a) {
+__global__ void __launch_bounds__(GTHREADS, 4) k_gather(GatherArgs a) {
   const V2 *wbuf = static_cast<const V2 *>(a.wbuf);
-  // per staged entry: columns, rows, row pitch and offset of the box in the scratch buffer
+  // compacted entries: columns, rows, row pitch and offset of the box in the scratch buffer
   __shared__ int e_i0[LMAX], e_i1[LMAX], e_j0[LMAX], e_j1[LMAX], e_w[LMAX], e_base[LMAX];
+  __shared__ int wcount[GTHREADS / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int i0 = 1 + blockIdx.x * GTX, j0 = 1 + blockIdx.y * GTY;
   const int i1 = min(i0 + GTX - 1, a.itot), j1 = min(j0 + GTY - 1, a.jtot);
   Acc acc_x[2] = {0, 0}, acc_y[2] = {0, 0};
   // cells of this thread: (i0 + lx, j0 + ly) for two rows
   const int lx = threadIdx.x % GTX, ly0 = threadIdx.x / GTX;  // GTHREADS / GTX = 4 rows per pass
-  // the band's ordered list of boxes; keep those that also reach this tile's columns
   const int band = blockIdx.y;
   const int L = min(__ldg(a.counts + band), a.cap);
   const int *blist = a.lists + (size_t)band * a.cap;
-  for (int base = 0; base < L; base += LMAX) {
-    const int cnt = min(LMAX, L - base);
-    for (int e = threadIdx.x; e < cnt; e += GTHREADS) {
-      const int ent = __ldg(blist + base + e);
-      const int n = ent / 3, q = ent - 3 * n;
-      int bi0 = 1, bi1 = 0, bj0 = 1, bj1 = 0, off = 0, pitch = 0;
-      // entry = 3 * particle + image with 0 <= image < 3; anything else is recorded and skipped
-      if (EIF_CHK(a.bd.rec, ent, 3LL * a.np, 46) && EIF_CHK(a.bd.rec, n, a.np, 44) &&
-          EIF_CHK(a.bd.rec, 12LL * n + 4 * q + 3, a.bd.box, 45)) {
-        const int *bx = a.box + 12 * n;
-        // tasks of the earlier images; a box row occupies segs * CHUNK scratch slots
-        int tasks_q = 0;
-        for (int m = 0; m < q; m++) {
-          const int w = bx[4 * m + 1] - bx[4 * m] + 1, h = bx[4 * m + 3] - bx[4 * m + 2] + 1;
-          if (w > 0 && h > 0) tasks_q += h * box_segs(w);
-        }
-        bi0 = bx[4 * q]; bi1 = bx[4 * q + 1]; bj0 = bx[4 * q + 2]; bj1 = bx[4 * q + 3];
-        off = (__ldg(a.off + n) + tasks_q) * CHUNK;
-        pitch = bi1 >= bi0 ? box_segs(bi1 - bi0 + 1) * CHUNK : 0;
+  for (int base = 0; base < L; base += GTHREADS) {
+    const int e = base + threadIdx.x;
+    int4 b = make_int4(1, 0, 1, 0), w = make_int4(0, 0, 0, 0);
+    if (e < L) {
+      const int ent = __ldg(blist + e);
+      // entry = 3 * particle + image; anything else is recorded and skipped
+      if (EIF_CHK(a.bd.rec, ent, 3LL * a.np, 46)) {
+        b = __ldg(a.edesc + 2 * ent);
+        w = __ldg(a.edesc + 2 * ent + 1);
       }
-      // entries that miss this tile's columns are kept (as empty) to preserve the order
-      if (bi0 > i1 || bi1 < i0) { bi0 = 1; bi1 = 0; }
-      e_i0[e] = bi0; e_i1[e] = bi1; e_j0[e] = bj0; e_j1[e] = bj1; e_w[e] = pitch; e_base[e] = off;
+    }
+    const bool keep = b.y >= b.x && b.x <= i1 && b.y >= i0 && b.z <= j1 && b.w >= j0;
+    const unsigned mask = __ballot_sync(0xffffffffu, keep);
+    if (lane == 0) wcount[wid] = __popc(mask);
+    __syncthreads();
+    int pos = __popc(mask & ((1u << lane) - 1u)), cnt = 0;
+#pragma unroll
+    for (int q = 0; q < GTHREADS / 32; q++) {
+      const int wc = wcount[q];
+      pos += q < wid ? wc : 0;
+      cnt += wc;
+    }
+    if (keep) {
+      e_i0[pos] = b.x; e_i1[pos] = b.y; e_j0[pos] = b.z; e_j1[pos] = b.w; e_w[pos] = w.x; e_base[pos] = w.y;
     }
     __syncthreads();
-    for (int e = 0; e < cnt; e++) {
-      const int bi0 = e_i0[e], bi1 = e_i1[e], bj0 = e_j0[e], bj1 = e_j1[e], w = e_w[e];
-      if (bi1 < bi0) continue;
-      const size_t pbase = (size_t)e_base[e];
+    for (int k = 0; k < cnt; k++) {
+      const int bi0 = e_i0[k], bi1 = e_i1[k], bj0 = e_j0[k], bj1 = e_j1[k], pw = e_w[k];
+      const size_t pbase = (size_t)e_base[k];
 #pragma unroll
       for (int r = 0; r < 2; r++) {
         const int i = i0 + lx, j = j0 + ly0 + 4 * r;
         if (i >= bi0 && i <= bi1 && j >= bj0 && j <= bj1 &&
-            EIF_CHK(a.bd.rec, (long long)(pbase + (size_t)(j - bj0) * w + (i - bi0)),
+            EIF_CHK(a.bd.rec, (long long)(pbase + (size_t)(j - bj0) * pw + (i - bi0)),
                     a.bd.wbuf * (long long)(sizeof(double2) / sizeof(V2)), 41)) {
-          const V2 v = wbuf[pbase + (size_t)(j - bj0) * w + (i - bi0)];
+          const V2 v = wbuf[pbase + (size_t)(j - bj0) * pw + (i - bi0)];
           acc_x[r] += v.x;
           acc_y[r] += v.y;
         }
@@ -1064,6 +1077,7 @@ int ibm_reserve(eif_ctx *c, size_t chunks) {
   EIF_CK(c, cudaMalloc((void **)&c->band_lists, sizeof(int) * (size_t)nbands * c->band_cap));
   EIF_CK(c, cudaMalloc((void **)&c->band_counts, sizeof(int) * (size_t)nbands));
   EIF_CK(c, cudaMalloc((void **)&c->band_marks, sizeof(unsigned) * (size_t)nbands * ((3 * c->np + 31) / 32)));
+  EIF_CK(c, cudaMalloc((void **)&c->edesc, sizeof(int4) * 6 * (size_t)c->np));
   return EIF_OK;
 }
 
@@ -1078,7 +1092,8 @@ void ibm_free(eif_ctx *c) {
   if (c->band_lists) cudaFree(c->band_lists);
   if (c->band_counts) cudaFree(c->band_counts);
   if (c->band_marks) cudaFree(c->band_marks);
-  c->band_lists = nullptr; c->band_counts = nullptr; c->band_marks = nullptr;
+  if (c->edesc) cudaFree(c->edesc);
+  c->band_lists = nullptr; c->band_counts = nullptr; c->band_marks = nullptr; c->edesc = nullptr;
   c->box = nullptr; c->chunk_off = nullptr; c->partial = nullptr; c->wbuf = nullptr; c->wcache = nullptr;
   c->weights_x_valid = false;
   c->pf = nullptr; c->tdesc = nullptr;
@@ -1217,7 +1232,7 @@ int launch_exchange(eif_ctx *c) {
   rc = launch_work(c, 1, 0);
   if (rc) return rc;
   GatherArgs g;
-  g.box = c->box; g.off = c->chunk_off; g.wbuf = c->wbuf;
+  g.edesc = c->edesc; g.wbuf = c->wbuf;
   g.dux = c->dux; g.duy = c->duy; g.flags = c->d_flags;
   g.np = c->np; g.itot = c->itot; g.jtot = c->jtot; g.ld = c->ld;
   g.bd = bounds_of(c);
@@ -1227,7 +1242,8 @@ int launch_exchange(eif_ctx *c) {
     const int words = (3 * c->np + 31) / 32;
     EIF_PROF(c, "ibm_band_lists", 2);
     EIF_CK(c, cudaMemsetAsync(c->band_marks, 0, sizeof(unsigned) * (size_t)nbands * words, c->stream));
-    k_band_marks<<<(c->np + 127) / 128, 128, 0, c->stream>>>(c->box, c->np, c->jtot, c->band_marks, words);
+    k_band_marks<<<(c->np + 127) / 128, 128, 0, c->stream>>>(c->box, c->chunk_off, c->np, c->jtot, c->band_marks,
+                                                             words, c->edesc, bounds_of(c));
     EIF_LAUNCH_CK(c);
     k_band_lists<<<(nbands * 32 + 255) / 256, 256, 0, c->stream>>>(c->band_marks, words, c->jtot, c->band_lists,
                                                                      c->band_counts, c->band_cap, c->d_flags);
