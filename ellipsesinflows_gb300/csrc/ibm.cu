@@ -36,7 +36,8 @@ constexpr int CHUNK = 64;       // cells per warp task (a box row, or a segment 
 __device__ __host__ __forceinline__ int box_segs(int w) { return (w + CHUNK - 1) / CHUNK; }
 constexpr int NEXTRA = 3;       // auxiliary.c:8
 constexpr double BETA = 2.;     // auxiliary.c:49
-constexpr int GTX = 64, GTY = 8, GTHREADS = 256;  // gather tile and block
+constexpr int GTX = 128, GTY = 8, GTHREADS = 256;  // gather tile and block
+constexpr int GCOLS = 64;   // columns covered by the threads of one pass (GTX / GCOLS passes)
 constexpr int LMAX = 256;       // gather entries staged in shared memory at a time (GTHREADS)
 
 // per-particle geometry needed by a box cell evaluation
@@ -933,9 +934,12 @@ __global__ void __launch_bounds__(GTHREADS, 4) k_gather(GatherArgs a) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int i0 = 1 + blockIdx.x * GTX, j0 = 1 + blockIdx.y * GTY;
   const int i1 = min(i0 + GTX - 1, a.itot), j1 = min(j0 + GTY - 1, a.jtot);
-  Acc acc_x[2] = {0, 0}, acc_y[2] = {0, 0};
-  // cells of this thread: (i0 + lx, j0 + ly) for two rows
-  const int lx = threadIdx.x % GTX, ly0 = threadIdx.x / GTX;  // GTHREADS / GTX = 4 rows per pass
+  constexpr int NC = (GTX / GCOLS) * 2;
+  Acc acc_x[NC], acc_y[NC];
+#pragma unroll
+  for (int r = 0; r < NC; r++) { acc_x[r] = 0; acc_y[r] = 0; }
+  // cells of this thread: (i0 + lx + GCOLS h, j0 + ly0 + 4 r), cell index 2 h + r
+  const int lx = threadIdx.x % GCOLS, ly0 = threadIdx.x / GCOLS;  // GTHREADS / GCOLS = 4 rows per pass
   const int band = blockIdx.y;
   const int L = min(__ldg(a.counts + band), a.cap);
   const int *blist = a.lists + (size_t)band * a.cap;
@@ -969,14 +973,14 @@ __global__ void __launch_bounds__(GTHREADS, 4) k_gather(GatherArgs a) {
       const int bi0 = e_i0[k], bi1 = e_i1[k], bj0 = e_j0[k], bj1 = e_j1[k], pw = e_w[k];
       const size_t pbase = (size_t)e_base[k];
 #pragma unroll
-      for (int r = 0; r < 2; r++) {
-        const int i = i0 + lx, j = j0 + ly0 + 4 * r;
+      for (int q = 0; q < NC; q++) {
+        const int i = i0 + lx + GCOLS * (q >> 1), j = j0 + ly0 + 4 * (q & 1);
         if (i >= bi0 && i <= bi1 && j >= bj0 && j <= bj1 &&
             EIF_CHK(a.bd.rec, (long long)(pbase + (size_t)(j - bj0) * pw + (i - bi0)),
                     a.bd.wbuf * (long long)(sizeof(double2) / sizeof(V2)), 41)) {
           const V2 v = wbuf[pbase + (size_t)(j - bj0) * pw + (i - bi0)];
-          acc_x[r] += v.x;
-          acc_y[r] += v.y;
+          acc_x[q] += v.x;
+          acc_y[q] += v.y;
         }
       }
     }
@@ -986,13 +990,13 @@ __global__ void __launch_bounds__(GTHREADS, 4) k_gather(GatherArgs a) {
   // ghost columns are filled afterwards by k_ibm_halo from these cells
   const int ld = a.ld;
 #pragma unroll
-  for (int r = 0; r < 2; r++) {
-    const int i = i0 + lx, j = j0 + ly0 + 4 * r;
+  for (int q = 0; q < NC; q++) {
+    const int i = i0 + lx + GCOLS * (q >> 1), j = j0 + ly0 + 4 * (q & 1);
     if (i > i1 || j > j1) continue;
     const int cidx = j * ld + i;
     if (!EIF_CHK(a.bd.rec, cidx, a.bd.field, 42)) continue;
-    static_cast<Acc *>(a.dux)[cidx] = acc_x[r];
-    static_cast<Acc *>(a.duy)[cidx] = acc_y[r];
+    static_cast<Acc *>(a.dux)[cidx] = acc_x[q];
+    static_cast<Acc *>(a.duy)[cidx] = acc_y[q];
   }
 }
 
