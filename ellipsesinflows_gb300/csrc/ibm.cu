@@ -536,10 +536,12 @@ struct EllF {
 };
 
 // The reference's iteration (ellipse.c:30-65) in single precision. Its fixed point
-// is the normal foot whatever the accuracy of the intermediate sin/cos and square
-// roots, so the loop uses the hardware approximations (__sincosf, rsqrtf); the
-// distance at the converged angle is evaluated with the accurate sincosf, and the
-// distance is stationary in the angle.
+// is the normal foot whatever the accuracy of the intermediate sin/cos, square
+// roots and arcsine, so the loop uses the hardware approximations (__sincosf,
+// rsqrtf) and the Taylor polynomial x + x^3/6 + 3x^5/40 of asin (odd, increasing
+// and zero only at zero like asin, so the step keeps its sign and vanishes at the
+// foot); the distance at the converged angle is evaluated with the accurate
+// sincosf, and the distance is stationary in the angle.
 __device__ __forceinline__ float normal_t_f(const EllF &e, float x_, float y_) {
   const float px = fabsf(x_), py = fabsf(y_);
   float t = 0.78539816339744831f;
@@ -551,7 +553,8 @@ __device__ __forceinline__ float normal_t_f(const EllF &e, float x_, float y_) {
     const float rx = x - ex, ry = y - ey, qx = px - ex, qy = py - ey;
     const float r2 = ry * ry + rx * rx, q2 = qy * qy + qx * qx;
     const float arg = fminf(fmaxf((rx * qy - ry * qx) * rsqrtf(r2 * q2), -1.f), 1.f);
-    const float dc = r2 * rsqrtf(r2) * asinf(arg);
+    const float a2 = arg * arg;
+    const float dc = r2 * rsqrtf(r2) * (arg * fmaf(a2, fmaf(a2, 0.075f, 0.16666667f), 1.f));
     // a^2 + b^2 - x^2 - y^2 written without cancellation
     const float dt = dc * rsqrtf(e.a * e.a * (st * st) + e.b * e.b * (ct * ct));
     t += dt;
