@@ -384,6 +384,7 @@ __global__ void k_dt_colmax(const double *__restrict__ ux, const double *__restr
   unsigned long long mx = 0ull, my = 0ull;
   bool bad = false;
   if (i <= itot) {
+#pragma unroll 4
     for (int j = 1 + blockIdx.y * TY + threadIdx.y; j <= jtot; j += TY * gridDim.y) {
       if (i >= 2) {
         const unsigned long long b = __double_as_longlong(__ldg(ux + ux_idx(i, j, ld))) & 0x7fffffffffffffffull;
@@ -438,23 +439,27 @@ __device__ __forceinline__ void write_coef(double dt, float *coef) {
 }
 
 // dt from the maxima (decide_dt.c:25-80): one block.
-__global__ void k_dt_final(const unsigned long long *__restrict__ colmax, const unsigned long long *__restrict__ uymax,
-                           const double *__restrict__ dxc, int itot, double dy, double Re, double lx, double dx_uniform,
-                           double sf_adv, double sf_dif, double sf_par, const double *__restrict__ P, int pcap, int np,
-                           double *__restrict__ dt_out, float *__restrict__ coef) {
+// dt limits of one slice of columns and particles (partial minima, one triple per
+// block), then the final combination: the divisions are spread over DT_BLOCKS SMs
+constexpr int DT_BLOCKS = 32;
+
+__global__ void k_dt_partial(const unsigned long long *__restrict__ colmax, const unsigned long long *__restrict__ uymax,
+                             const double *__restrict__ dxc, int itot, double dy, double lx, double dx_uniform,
+                             const double *__restrict__ P, int pcap, int np, double *__restrict__ part) {
   const double small = 1.e-8;
   double dta = 5.e-2, dxmin = lx, dtp = DBL_MAX;
-  for (int i = 2 + threadIdx.x; i <= itot; i += blockDim.x) {
+  const int stride = gridDim.x * blockDim.x;
+  for (int i = 2 + blockIdx.x * blockDim.x + threadIdx.x; i <= itot; i += stride) {
     const double vel = fmax(__longlong_as_double((long long)colmax[i]), small);
     dta = fmin(dta, dxc[i] / vel);
     dxmin = fmin(dxmin, dxc[i]);
   }
-  if (threadIdx.x == 0) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
     const double vel = fmax(__longlong_as_double((long long)uymax[0]), small);
     dta = fmin(dta, dy / vel);
   }
   const double delta = fmin(dx_uniform, dy);
-  for (int n = threadIdx.x; n < np; n += blockDim.x) {
+  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < np; n += stride) {
     const double a = P[EIF_P_A * pcap + n], b = P[EIF_P_B * pcap + n];
     const double r = fmax(a, b);
     const double vz = P[EIF_P_VZ * pcap + n];
@@ -474,16 +479,31 @@ __global__ void k_dt_final(const unsigned long long *__restrict__ colmax, const 
   if (threadIdx.x == 0) {
     const int nw = blockDim.x >> 5;
     for (int k = 1; k < nw; k++) { dta = fmin(dta, s[0][k]); dxmin = fmin(dxmin, s[1][k]); dtp = fmin(dtp, s[2][k]); }
-    dta *= sf_adv;
-    double difx = 0.25 * Re * (dxmin * dxmin);
-    double dify = 0.25 * Re * (dy * dy);
-    difx *= sf_dif;
-    dify *= sf_dif;
-    dtp *= sf_par;
-    const double dt = fmin(fmin(dta, fmin(difx, dify)), dtp);
-    *dt_out = dt;
-    write_coef(dt, coef);
+    part[3 * blockIdx.x + 0] = dta;
+    part[3 * blockIdx.x + 1] = dxmin;
+    part[3 * blockIdx.x + 2] = dtp;
   }
+}
+
+// param_decide_dt (decide_dt.c:11-81): minima of the partial limits, the safety
+// factors, dt and the single-precision dt products
+__global__ void k_dt_final(const double *__restrict__ part, int nparts, double dy, double Re, double sf_adv,
+                           double sf_dif, double sf_par, double *__restrict__ dt_out, float *__restrict__ coef) {
+  double dta = part[0], dxmin = part[1], dtp = part[2];
+  for (int k = 1; k < nparts; k++) {
+    dta = fmin(dta, part[3 * k]);
+    dxmin = fmin(dxmin, part[3 * k + 1]);
+    dtp = fmin(dtp, part[3 * k + 2]);
+  }
+  dta *= sf_adv;
+  double difx = 0.25 * Re * (dxmin * dxmin);
+  double dify = 0.25 * Re * (dy * dy);
+  difx *= sf_dif;
+  dify *= sf_dif;
+  dtp *= sf_par;
+  const double dt = fmin(fmin(dta, fmin(difx, dify)), dtp);
+  *dt_out = dt;
+  write_coef(dt, coef);
 }
 
 __global__ void k_coef(const double *__restrict__ dt, float *__restrict__ coef) { write_coef(*dt, coef); }
@@ -656,7 +676,7 @@ int launch_update_pressure(eif_ctx *c) { return launch_corr(c, -1, 0, 0, 1); }
 int launch_decide_dt(eif_ctx *c) {
   unsigned long long *colmax = reinterpret_cast<unsigned long long *>(c->qhat);  // scratch: itot+2 words
   unsigned long long *uymax = colmax + c->itot + 2;
-  EIF_PROF(c, "decide_dt", 2);
+  EIF_PROF(c, "decide_dt", 3);
   EIF_CK(c, cudaMemsetAsync(colmax, 0, sizeof(unsigned long long) * (c->itot + 3), c->stream));
   int gy = (c->jtot + TY - 1) / TY;
   const int gx = (c->itot + TX - 1) / TX;
@@ -666,9 +686,12 @@ int launch_decide_dt(eif_ctx *c) {
   k_dt_colmax<<<dim3(gx, gy), dim3(TX, TY), 0, c->stream>>>(c->ux[c->cur], c->uy[c->cur], c->itot, c->jtot, c->ld,
                                                             colmax, uymax, c->d_flags);
   EIF_LAUNCH_CK(c);
-  k_dt_final<<<1, 256, 0, c->stream>>>(colmax, uymax, c->dxc, c->itot, c->dy, c->cfg.Re, c->lx, c->dx,
-                                       c->cfg.safefactors[0], c->cfg.safefactors[1], c->cfg.safefactors[2], c->P,
-                                       c->pcap, c->np, c->d_scal, c->d_coef);
+  double *part = reinterpret_cast<double *>(uymax + 1);   // scratch: 3 * DT_BLOCKS words
+  k_dt_partial<<<DT_BLOCKS, 64, 0, c->stream>>>(colmax, uymax, c->dxc, c->itot, c->dy, c->lx, c->dx, c->P, c->pcap,
+                                                c->np, part);
+  EIF_LAUNCH_CK(c);
+  k_dt_final<<<1, 1, 0, c->stream>>>(part, DT_BLOCKS, c->dy, c->cfg.Re, c->cfg.safefactors[0], c->cfg.safefactors[1],
+                                     c->cfg.safefactors[2], c->d_scal, c->d_coef);
   EIF_LAUNCH_CK(c);
   return EIF_OK;
 }

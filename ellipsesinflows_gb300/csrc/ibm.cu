@@ -1140,7 +1140,7 @@ static int launch_boxes(eif_ctx *c, bool use_increment) {
   b.nchunk = cnt;
   EIF_PROF(c, "ibm_boxes", 3);
   // FP64-heavy per particle: small blocks spread the particles over many SMs
-  k_boxes<<<(c->np + 31) / 32, 32, 0, c->stream>>>(b);
+  k_boxes<<<(c->np + 15) / 16, 16, 0, c->stream>>>(b);
   EIF_LAUNCH_CK(c);
   k_scan<<<1, 1024, 0, c->stream>>>(cnt, c->chunk_off, c->np, bounds_of(c));
   EIF_LAUNCH_CK(c);

@@ -468,8 +468,9 @@ int launch_increment(eif_ctx *c, int rk) {
   c->incr_zero = false;
   const double Fr = c->cfg.Fr;
   EIF_PROF(c, "particle_increment", 2);
-  const int blocks = std::max(1, std::min((c->np + 127) / 128, c->sms * 4));
-  k_increment<<<blocks, 128, 0, c->stream>>>(c->P, c->pcap, c->np, rk_coef(rk).gamma, Fr * Fr, c->d_scal,
+  // FP64-heavy per particle: small blocks spread the particles over many SMs
+  const int blocks = std::max(1, std::min((c->np + 31) / 32, c->sms * 4));
+  k_increment<<<blocks, 32, 0, c->stream>>>(c->P, c->pcap, c->np, rk_coef(rk).gamma, Fr * Fr, c->d_scal,
                                              c->d_inc);
   EIF_LAUNCH_CK(c);
   k_increment_done<<<1, 1, 0, c->stream>>>(c->d_inc, c->d_scal, reinterpret_cast<unsigned *>(c->d_inc + 1),
