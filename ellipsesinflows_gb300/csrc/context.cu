@@ -47,17 +47,101 @@ int check_records(eif_ctx *c) {
   return fail(c, EIF_ERR_CUDA, "bounds guard %llu: index %llu outside [0, %llu)", tag, idx, bound);
 }
 
-// the part of an RK stage before the particle sub-iterations (src/main.c:14-31)
+// Particle-only work beside the fluid kernels. The kernels of a stage and their
+// data dependences are unchanged; work that shares no buffer with the fluid kernels
+// launched in between is moved to the side stream, which forks from the main stream
+// and is joined back before the first kernel that needs its results. Off while the
+// per-stage profiler or per-launch synchronisation is active.
+bool overlap_on(const eif_ctx *c) { return c->side && !c->sync_debug && !c->prof.enabled; }
+
+namespace {
+
+// launches between begin and end go to the side stream, after the work already on the
+// main stream; end records `ev` on the side stream and restores the main stream
+struct SideScope {
+  eif_ctx *c;
+  bool active = false;
+  explicit SideScope(eif_ctx *c_) : c(c_) {}
+  int begin() {
+    cudaError_t e = cudaEventRecord(c->ev_fork, c->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->side, c->ev_fork, 0);
+    if (e != cudaSuccess) return check_cuda(c, e, "fork to the side stream");
+    c->main_stream = c->stream;
+    c->stream = c->side;
+    active = true;
+    return EIF_OK;
+  }
+  // records ev on the side stream at this point of its work
+  int mark(cudaEvent_t ev) {
+    const cudaError_t e = cudaEventRecord(ev, c->side);
+    return e == cudaSuccess ? EIF_OK : check_cuda(c, e, "cudaEventRecord (side stream)");
+  }
+  int end(cudaEvent_t ev) {
+    if (!active) return EIF_OK;
+    c->stream = c->main_stream;
+    active = false;
+    const cudaError_t e = cudaEventRecord(ev, c->side);
+    return e == cudaSuccess ? EIF_OK : check_cuda(c, e, "cudaEventRecord (side stream)");
+  }
+  ~SideScope() {
+    if (active) c->stream = c->main_stream;
+  }
+};
+
+int join(eif_ctx *c, cudaEvent_t ev) {
+  const cudaError_t e = cudaStreamWaitEvent(c->stream, ev, 0);
+  return e == cudaSuccess ? EIF_OK : check_cuda(c, e, "join of the side stream");
+}
+
+}  // namespace
+
+// the part of an RK stage before the particle sub-iterations (src/main.c:14-35)
 int rk_stage_front(eif_ctx *c, int rk) {
   int rc;
   const bool ibm = c->np > 0;
   if ((rc = launch_reset_increments(c))) return rc;
+  if (ibm && overlap_on(c)) {
+    // side: inertia at X (reads the current velocity buffer, which the predictor
+    // does not write), the gather's band lists, and the collision forces at X
+    // (particle fields only); main: predictor, exchange, Poisson, projection
+    SideScope side(c);
+    if ((rc = side.begin())) return rc;
+    if ((rc = launch_inertia(c, 0))) return rc;
+    if ((rc = launch_band_lists(c))) return rc;
+    if ((rc = side.mark(c->ev_ibm))) return rc;
+    if ((rc = launch_collision(c, 0))) return rc;
+    if ((rc = side.end(c->ev_coll))) return rc;
+    if ((rc = launch_predictor(c, rk))) return rc;
+    if ((rc = join(c, c->ev_ibm))) return rc;
+    if ((rc = launch_exchange(c))) return rc;
+    if ((rc = launch_potential(c, rk, ibm))) return rc;
+    if ((rc = launch_correct(c, rk, ibm, true))) return rc;
+    return join(c, c->ev_coll);
+  }
   if ((rc = launch_inertia(c, 0))) return rc;
   if ((rc = launch_predictor(c, rk))) return rc;
   if (ibm && (rc = launch_exchange(c))) return rc;
   if ((rc = launch_potential(c, rk, ibm))) return rc;
   if ((rc = launch_correct(c, rk, ibm, true))) return rc;
   return launch_collision(c, 0);
+}
+
+// one particle sub-iteration (src/main.c:36-39): inertia at X + dX and the
+// collision forces (independent, the latter on the side stream), then increments
+int sub_iteration(eif_ctx *c, int rk) {
+  int rc;
+  if (c->np > 0 && overlap_on(c)) {
+    SideScope side(c);
+    if ((rc = side.begin())) return rc;
+    if ((rc = launch_collision(c, 1))) return rc;
+    if ((rc = side.end(c->ev_coll))) return rc;
+    if ((rc = launch_inertia(c, 1))) return rc;
+    if ((rc = join(c, c->ev_coll))) return rc;
+  } else {
+    if ((rc = launch_inertia(c, 1))) return rc;
+    if ((rc = launch_collision(c, 1))) return rc;
+  }
+  return launch_increment(c, rk);
 }
 
 }  // namespace eif
@@ -203,9 +287,7 @@ int rk_stage(eif_ctx *c, int rk, int *sub) {
   if ((rc = rk_stage_front(c, rk))) return rc;
   int s = 0;
   for (s = 0;; s++) {
-    if ((rc = launch_inertia(c, 1))) return rc;
-    if ((rc = launch_collision(c, 1))) return rc;
-    if ((rc = launch_increment(c, rk))) return rc;
+    if ((rc = sub_iteration(c, rk))) return rc;
     if ((rc = sync_scalars(c))) return rc;
     if (c->h_scal[1] < 1.e-8) break;
     if (s > 100) break;
@@ -244,6 +326,10 @@ int eif_create(const eif_config_t *cfg, eif_ctx **out) {
   CK_CREATE(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
   c->sms = sms;
   CK_CREATE(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  CK_CREATE(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+  CK_CREATE(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
+  CK_CREATE(cudaEventCreateWithFlags(&c->ev_ibm, cudaEventDisableTiming));
+  CK_CREATE(cudaEventCreateWithFlags(&c->ev_coll, cudaEventDisableTiming));
   host_metrics(c);
   int rc = device_metrics(c);
   if (rc) return rc;
@@ -313,6 +399,10 @@ int eif_destroy(eif_ctx *c) {
   poisson_free(c);
   ibm_free(c);
   profile_free(c);
+  if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+  if (c->ev_ibm) cudaEventDestroy(c->ev_ibm);
+  if (c->ev_coll) cudaEventDestroy(c->ev_coll);
+  if (c->side) cudaStreamDestroy(c->side);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete[] c->h_xf; delete[] c->h_xc; delete[] c->h_dxf; delete[] c->h_dxc; delete[] c->h_yf; delete[] c->h_yc;
   delete c;

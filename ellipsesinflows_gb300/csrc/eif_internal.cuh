@@ -95,6 +95,11 @@ struct eif_ctx {
   double lx, ly, dx, dy;
   int device;
   cudaStream_t stream;
+  // second stream for particle-only work that runs beside the fluid kernels; the
+  // launch functions use `stream`, which side_begin/side_end point at it
+  cudaStream_t side = nullptr, main_stream = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_ibm = nullptr, ev_coll = nullptr;
+  bool bands_x_valid = false;   // band lists built for the current boxes at X
   // fields
   double *ux[2], *uy[2];
   int cur;                      // index of the current velocity buffer
@@ -223,6 +228,9 @@ int ibm_reserve(eif_ctx *c, size_t chunks);
 void ibm_free(eif_ctx *c);
 int launch_inertia(eif_ctx *c, int cn);
 int launch_exchange(eif_ctx *c);
+int launch_band_lists(eif_ctx *c);
+int sub_iteration(eif_ctx *c, int rk);
+bool overlap_on(const eif_ctx *c);
 
 // ---- particles (particles.cu) ----
 int launch_collision(eif_ctx *c, int cn);

@@ -3,7 +3,8 @@
 // The graph holds, in launch order, the dt decision and for each RK stage the
 // stage kernels, a conditional WHILE node whose body is one particle
 // sub-iteration (inertia at the increment, collisions, increments), and the
-// particle update (src/main.c:13-53). k_increment_done sets the loop condition
+// particle update (src/main.c:13-53). Work that the stage driver puts on the side
+// stream is captured as a parallel branch of the same graph. k_increment_done sets the loop condition
 // on the device from the residual and the sub-iteration count, so a step needs
 // no host round trip; the host synchronises once per step to read dt and the
 // error flags. The kernels and their order are those of the host-driven path
@@ -38,12 +39,15 @@ int end_capture(eif_ctx *c, std::vector<cudaGraphNode_t> *sinks) {
   return EIF_OK;
 }
 
-// abandon a capture after an error, leaving the stream usable
+// abandon a capture after an error, leaving the streams usable
 void abort_capture(eif_ctx *c) {
-  cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
-  if (cudaStreamIsCapturing(c->stream, &st) == cudaSuccess && st != cudaStreamCaptureStatusNone) {
-    cudaGraph_t g = nullptr;
-    cudaStreamEndCapture(c->stream, &g);
+  for (cudaStream_t s : {c->stream, c->side}) {
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    if (s && cudaStreamIsCapturing(s, &st) == cudaSuccess && st != cudaStreamCaptureStatusNone) {
+      cudaGraph_t g = nullptr;
+      cudaStreamEndCapture(s, &g);
+      if (g) cudaGraphDestroy(g);
+    }
   }
   cudaGetLastError();
   c->in_loop = false;
@@ -97,9 +101,7 @@ int build(eif_ctx *c, eif_ctx::StepGraph &sg) {
     // the body runs repeatedly with changing increments: it always computes its boxes
     c->incr_zero = false;
     c->boxes_x_valid = false;
-    if ((rc = launch_inertia(c, 1))) return fail_out(rc);
-    if ((rc = launch_collision(c, 1))) return fail_out(rc);
-    if ((rc = launch_increment(c, rk))) return fail_out(rc);
+    if ((rc = sub_iteration(c, rk))) return fail_out(rc);
     c->in_loop = false;
     if ((rc = end_capture(c, nullptr))) return fail_out(rc);
     e = cudaStreamBeginCaptureToGraph(c->stream, g, &loop, nullptr, 1, cudaStreamCaptureModeThreadLocal);

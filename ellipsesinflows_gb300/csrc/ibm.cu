@@ -1128,6 +1128,7 @@ static int launch_boxes(eif_ctx *c, bool use_increment) {
   if (x_only && c->boxes_x_valid) return EIF_OK;
   c->boxes_x_valid = false;
   c->weights_x_valid = false;
+  c->bands_x_valid = false;
   BoxArgs b;
   b.bd = bounds_of(c);
   b.bd_off_base = c->chunk_off;
@@ -1227,6 +1228,25 @@ int launch_inertia(eif_ctx *c, int cn) {
   return launch_work(c, 0, cn);
 }
 
+// ordered box lists per band of GTY rows for the gather, from the boxes at X
+int launch_band_lists(eif_ctx *c) {
+  if (c->np == 0) return EIF_OK;
+  int rc = launch_boxes(c, false);
+  if (rc) return rc;
+  const int nbands = (c->jtot + GTY - 1) / GTY;
+  const int words = (3 * c->np + 31) / 32;
+  EIF_PROF(c, "ibm_band_lists", 2);
+  EIF_CK(c, cudaMemsetAsync(c->band_marks, 0, sizeof(unsigned) * (size_t)nbands * words, c->stream));
+  k_band_marks<<<(c->np + 127) / 128, 128, 0, c->stream>>>(c->box, c->chunk_off, c->np, c->jtot, c->band_marks,
+                                                           words, c->edesc, bounds_of(c));
+  EIF_LAUNCH_CK(c);
+  k_band_lists<<<(nbands * 32 + 255) / 256, 256, 0, c->stream>>>(c->band_marks, words, c->jtot, c->band_lists,
+                                                                   c->band_counts, c->band_cap, c->d_flags);
+  EIF_LAUNCH_CK(c);
+  c->bands_x_valid = c->boxes_x_valid;
+  return EIF_OK;
+}
+
 int launch_exchange(eif_ctx *c) {
   if (c->np == 0) {
     EIF_PROF(c, "ibm_gather", 0);
@@ -1244,18 +1264,7 @@ int launch_exchange(eif_ctx *c) {
   g.np = c->np; g.itot = c->itot; g.jtot = c->jtot; g.ld = c->ld;
   g.bd = bounds_of(c);
   g.lists = c->band_lists; g.counts = c->band_counts; g.cap = c->band_cap;
-  {
-    const int nbands = (c->jtot + GTY - 1) / GTY;
-    const int words = (3 * c->np + 31) / 32;
-    EIF_PROF(c, "ibm_band_lists", 2);
-    EIF_CK(c, cudaMemsetAsync(c->band_marks, 0, sizeof(unsigned) * (size_t)nbands * words, c->stream));
-    k_band_marks<<<(c->np + 127) / 128, 128, 0, c->stream>>>(c->box, c->chunk_off, c->np, c->jtot, c->band_marks,
-                                                             words, c->edesc, bounds_of(c));
-    EIF_LAUNCH_CK(c);
-    k_band_lists<<<(nbands * 32 + 255) / 256, 256, 0, c->stream>>>(c->band_marks, words, c->jtot, c->band_lists,
-                                                                     c->band_counts, c->band_cap, c->d_flags);
-    EIF_LAUNCH_CK(c);
-  }
+  if (!(c->boxes_x_valid && c->bands_x_valid) && (rc = launch_band_lists(c))) return rc;
   dim3 grid((c->itot + GTX - 1) / GTX, (c->jtot + GTY - 1) / GTY);
   EIF_PROF(c, "ibm_gather", 2);
   const int nhalo = 2 * (c->itot + 2) + 2 * c->jtot;
