@@ -741,7 +741,7 @@ __global__ void __launch_bounds__(256, 3) k_ibm_work_f(WorkArgs a) {
 // The mixed form's evaluation with cached weights (wmode 2 of k_ibm_work_f): the
 // same sums and field contributions, without the geometry work, so it runs with
 // few registers and many resident warps, which hide the latency of its loads.
-__global__ void __launch_bounds__(256, 4) k_ibm_sum_f(WorkArgs a) {
+__global__ void __launch_bounds__(256, 6) k_ibm_sum_f(WorkArgs a) {
   if (a.gate && ((a.gate == 1) != (*a.iter == 0u))) return;
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -772,7 +772,7 @@ __global__ void __launch_bounds__(256, 4) k_ibm_sum_f(WorkArgs a) {
     const int j = task ? t.j : 1;
     const float Y = ((float)(j - j0i) - gyi) * dyf;
     float sacc0 = 0.f, sacc1 = 0.f, sacc2 = 0.f;
-#pragma unroll
+#pragma unroll 1
     for (int half = 0; half < CHUNK / 32; half++) {
       const int i = (task ? t.ib : 1) + half * 32 + lane;
       const long long slot = (long long)c * CHUNK + half * 32 + lane;
