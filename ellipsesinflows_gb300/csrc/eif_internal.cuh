@@ -73,6 +73,7 @@ struct PoissonPlan {
   double *tdm_up;   // [k][i]  modified upper diagonal, i < blk-1
   double *tdm_g;    // [k][i]  response of the interior block to its left neighbour
   float2 *tdm_g_df = nullptr;  // the same as (hi, lo) float pairs (mixed form)
+  float2 *tdm_inv_df = nullptr, *tdm_up_df = nullptr;  // tdm_inv, tdm_up as float pairs (mixed form)
   double *red_inv;  // [k][b]  reduced cyclic system: Thomas pivots (b < nblk-1)
   double *red_up;   // [k][b]
   double *red_q1;   // [k][b]  correction vector of the reduced cyclic system

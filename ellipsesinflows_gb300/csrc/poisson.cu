@@ -540,11 +540,11 @@ struct Dct2ArgsDF {
   const double *ux, *uy;
   const float *dux, *duy;   // IBM field response in single precision
   const float *coef;   // [12 + 2 rk] = hi, lo of 1/(gamma dt)
-  double *qhat;
+  double *qhat;             // double, or (hi, lo) float pairs when qdf is set
   const float4 *tw, *rot, *wn;
   FftDesc fd;
   DF rdx, rdy;
-  int itot, jtot, ld, with_ibm, rk;
+  int itot, jtot, ld, with_ibm, rk, qdf;
 };
 
 // RHS + DCT-II of one row in double-float arithmetic (compute_potential.c:70-92)
@@ -590,24 +590,28 @@ __global__ void __launch_bounds__(256) k_dct2_df(Dct2ArgsDF a) {
     const CDF v = cdf_add(e, cdf_mul(cdf_load(a.wn, kk), o));
     {
       const CDF r = cdf_load(a.rot, kk);
-      out[kk] = df_to_double(df_scale(df_dot2(r.re, v.re, r.im, v.im, -1.f), 2.f));
+      const DF o0 = df_scale(df_dot2(r.re, v.re, r.im, v.im, -1.f), 2.f);
+      if (a.qdf) reinterpret_cast<float2 *>(out)[kk] = make_float2(o0.hi, o0.lo);
+      else out[kk] = df_to_double(o0);
     }
     if (kk > 0 && kk < m) {
       // v conjugated for k = n - kk
       const CDF r = cdf_load(a.rot, n - kk);
-      out[n - kk] = df_to_double(df_scale(df_dot2(r.re, v.re, r.im, df_neg(v.im), -1.f), 2.f));
+      const DF o1 = df_scale(df_dot2(r.re, v.re, r.im, df_neg(v.im), -1.f), 2.f);
+      if (a.qdf) reinterpret_cast<float2 *>(out)[n - kk] = make_float2(o1.hi, o1.lo);
+      else out[n - kk] = df_to_double(o1);
     }
   }
 }
 
 struct Dct3ArgsDF {
-  const double *qhat, *iface;
+  const double *qhat, *iface;   // qhat: double, or (hi, lo) float pairs when qdf is set
   const float2 *g;   // tdm_g as (hi, lo)
   double *psi;
   const float4 *tw, *rot, *wn;
   FftDesc fd;
   DF scale;   // 1 / (2 itot)
-  int itot, jtot, ld, blk, nblk;
+  int itot, jtot, ld, blk, nblk, qdf;
 };
 
 // block reconstruction + DCT-III + scaling of one row, double-float arithmetic
@@ -630,13 +634,27 @@ __global__ void __launch_bounds__(256) k_dct3_df(Dct3ArgsDF a) {
         // y + s_left g + s_right h in double-float from the double-precision block solution
         const float2 gl = __ldg(a.g + (size_t)r * n + k);
         const float2 gr = __ldg(a.g + (size_t)(M - 2 - r) * n + k);
-        v = df_add_nw(df_add_nw(df_of(__ldg(row + k)), df_mul(df_of(__ldg(a.iface + (size_t)bm * n + k)), DF{gl.x, gl.y})),
+        DF yv;
+        if (a.qdf) {
+          const float2 t = __ldg(reinterpret_cast<const float2 *>(row) + k);
+          yv = DF{t.x, t.y};
+        } else {
+          yv = df_of(__ldg(row + k));
+        }
+        v = df_add_nw(df_add_nw(yv, df_mul(df_of(__ldg(a.iface + (size_t)bm * n + k)), DF{gl.x, gl.y})),
                       df_mul(df_of(__ldg(a.iface + (size_t)b * n + k)), DF{gr.x, gr.y}));
       }
       xr[k] = v;
     }
   } else {
-    for (int k = threadIdx.x; k < n; k += blockDim.x) xr[k] = df_of(__ldg(row + k));
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+      if (a.qdf) {
+        const float2 t = __ldg(reinterpret_cast<const float2 *>(row) + k);
+        xr[k] = DF{t.x, t.y};
+      } else {
+        xr[k] = df_of(__ldg(row + k));
+      }
+    }
   }
   __syncthreads();
   CDF *x = smd, *y = smd + m;
@@ -959,8 +977,21 @@ __global__ void __launch_bounds__(FFT_CTA, 8) k_dct2_dfr(Dct2ArgsDF a, FftShape 
     // rot[kk] = (c, s); rot[n - kk] = -i conj(rot[kk]) = (-s, -c)
     const float4 r = __ldg(a.rot + kk);
     const DF rc = DF{r.x, r.y}, rs = DF{r.z, r.w};
-    out[kk] = df_to_double(df_scale(dfl_dot2(rc, vv.re, rs, vv.im, -1.f), 2.f));
-    if (kk > 0 && kk < m) out[n - kk] = df_to_double(df_scale(dfl_dot2(rs, vv.re, rc, vv.im, 1.f), -2.f));
+    const DF o0 = df_scale(dfl_dot2(rc, vv.re, rs, vv.im, -1.f), 2.f);
+    const DF o1 = df_scale(dfl_dot2(rs, vv.re, rc, vv.im, 1.f), -2.f);
+    const bool pair = kk > 0 && kk < m;
+    if (a.qdf) {
+      float2 *outf = reinterpret_cast<float2 *>(out);
+      const DF n0 = fast_sum(o0.hi, o0.lo);
+      outf[kk] = make_float2(n0.hi, n0.lo);
+      if (pair) {
+        const DF n1 = fast_sum(o1.hi, o1.lo);
+        outf[n - kk] = make_float2(n1.hi, n1.lo);
+      }
+    } else {
+      out[kk] = df_to_double(o0);
+      if (pair) out[n - kk] = df_to_double(o1);
+    }
   }
 }
 
@@ -991,7 +1022,7 @@ __global__ void __launch_bounds__(FFT_CTA, 8) k_dct3_dfr(Dct3ArgsDF a, FftShape 
           // y + s_left g + s_right h in double-float from the double-precision block solution
           const float2 gl = __ldg(a.g + (size_t)r * n + k);
           const float2 gr = __ldg(a.g + (size_t)(M - 2 - r) * n + k);
-          const float2 y = eifd::split(__ldg(row + k));
+          const float2 y = a.qdf ? __ldg(reinterpret_cast<const float2 *>(row) + k) : eifd::split(__ldg(row + k));
           const float2 sl = eifd::split(__ldg(a.iface + (size_t)bm * n + k));
           const float2 sr = eifd::split(__ldg(a.iface + (size_t)b * n + k));
           const DF acc = dfl_add(dfl_add(DF{y.x, y.y}, dfl_mulc(DF{sl.x, sl.y}, DF{gl.x, gl.y})),
@@ -1001,7 +1032,14 @@ __global__ void __launch_bounds__(FFT_CTA, 8) k_dct3_dfr(Dct3ArgsDF a, FftShape 
         xr[k] = val;
       }
     } else {
-      for (int k = t; k < n; k += T) xr[k] = df_of(__ldg(row + k));
+      for (int k = t; k < n; k += T) {
+        if (a.qdf) {
+          const float2 q = __ldg(reinterpret_cast<const float2 *>(row) + k);
+          xr[k] = DF{q.x, q.y};
+        } else {
+          xr[k] = df_of(__ldg(row + k));
+        }
+      }
     }
   }
   __syncthreads();
@@ -1042,6 +1080,51 @@ __global__ void __launch_bounds__(FFT_CTA, 8) k_dct3_dfr(Dct3ArgsDF a, FftShape 
       if (j == a.jtot) a.psi[n + 1] = val;
     }
   }
+}
+
+// Interior Thomas solve of one block in double-float arithmetic (mixed form): the
+// right-hand side and the block solution are (hi, lo) float pairs in the qhat
+// buffer, the pivots 1/d_i and modified upper diagonals are float-pair tables, and
+// the two values the reduced system needs are written in double. The blocks are
+// diagonally dominant (|c| >= 2 l), so the recurrences carry the pairs' 2^-48
+// relative error without amplification.
+template <int M>
+__global__ void __launch_bounds__(128) k_tdm_local_df(float2 *__restrict__ qhat, const float2 *__restrict__ inv,
+                                                     const float2 *__restrict__ up, double *__restrict__ iface_a,
+                                                     double *__restrict__ first, DF l, int itot, int nblk, int ld) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int b = blockIdx.y;
+  if (k >= itot) return;
+  DF v[M - 1];
+  const size_t base = (size_t)b * M * ld + k;
+#pragma unroll
+  for (int r = 0; r < M - 1; r++) {
+    const float2 t = qhat[base + (size_t)r * ld];
+    v[r] = DF{t.x, t.y};
+  }
+  const float2 rif = qhat[base + (size_t)(M - 1) * ld];
+  {
+    const float2 iv = __ldg(inv + k);
+    const DF t = dfl_mulc(v[0], DF{iv.x, iv.y});
+    v[0] = fast_sum(t.hi, t.lo);
+  }
+#pragma unroll
+  for (int r = 1; r < M - 1; r++) {
+    const float2 iv = __ldg(inv + r * itot + k);
+    const DF t = dfl_mulc(dfl_sub(v[r], dfl_mulc(v[r - 1], l)), DF{iv.x, iv.y});
+    v[r] = fast_sum(t.hi, t.lo);
+  }
+#pragma unroll
+  for (int r = M - 3; r >= 0; r--) {
+    const float2 u = __ldg(up + r * itot + k);
+    const DF t = dfl_sub(v[r], dfl_mulc(v[r + 1], DF{u.x, u.y}));
+    v[r] = fast_sum(t.hi, t.lo);
+  }
+#pragma unroll
+  for (int r = 0; r < M - 1; r++) qhat[base + (size_t)r * ld] = make_float2(v[r].hi, v[r].lo);
+  // interface equation: r_iface - l y[M-2] (this block) - l y[0] (next block)
+  iface_a[(size_t)b * itot + k] = df_to_double(dfl_sub(DF{rif.x, rif.y}, dfl_mulc(v[M - 2], l)));
+  first[(size_t)b * itot + k] = df_to_double(v[0]);
 }
 
 // launch shape of the register-radix transforms, or T = 0 when m is not supported
@@ -1234,6 +1317,17 @@ int poisson_init(eif_ctx *c) {
         gdf[q] = make_float2(hi, (float)(g[q] - (double)hi));
       }
       EIF_CK(c, up_load((void **)&pp.tdm_g_df, gdf.data(), sizeof(float2) * gdf.size()));
+      auto pairs = [](const std::vector<double> &v) {
+        std::vector<float2> o(v.size());
+        for (size_t q = 0; q < v.size(); q++) {
+          const float hi = (float)v[q];
+          o[q] = make_float2(hi, (float)(v[q] - (double)hi));
+        }
+        return o;
+      };
+      const std::vector<float2> invdf = pairs(inv), updf = pairs(up);
+      EIF_CK(c, up_load((void **)&pp.tdm_inv_df, invdf.data(), sizeof(float2) * invdf.size()));
+      EIF_CK(c, up_load((void **)&pp.tdm_up_df, updf.data(), sizeof(float2) * updf.size()));
     }
     EIF_CK(c, up_load((void **)&pp.red_inv, rinv.data(), sizeof(double) * rinv.size()));
     EIF_CK(c, up_load((void **)&pp.red_up, rup.data(), sizeof(double) * rup.size()));
@@ -1279,7 +1373,7 @@ int poisson_init(eif_ctx *c) {
 void poisson_free(eif_ctx *c) {
   PoissonPlan &pp = c->pp;
   void *ptrs[] = {pp.r2_inv, pp.r2_up, pp.r2_phi, pp.r2_qinv, pp.r2_qup, pp.r2_q1, pp.r2_coef,
-                  pp.tw, pp.rot, pp.wn, pp.tw_f, pp.rot_f, pp.wn_f, pp.lam, pp.tdm_inv, pp.tdm_up, pp.tdm_g, pp.tdm_g_df,
+                  pp.tw, pp.rot, pp.wn, pp.tw_f, pp.rot_f, pp.wn_f, pp.lam, pp.tdm_inv, pp.tdm_up, pp.tdm_g, pp.tdm_g_df, pp.tdm_inv_df, pp.tdm_up_df,
                   pp.red_inv, pp.red_up, pp.red_q1, pp.red_coef, pp.ywork};
   for (void *p : ptrs) if (p) cudaFree(p);
   pp = PoissonPlan{};
@@ -1311,6 +1405,7 @@ int launch_potential(eif_ctx *c, int rk, bool with_ibm) {
     a.fd = fd;
     a.rdx = dfpair(1. / c->dx); a.rdy = dfpair(1. / c->dy);
     a.itot = n; a.jtot = jt; a.ld = c->ld; a.with_ibm = with_ibm ? 1 : 0; a.rk = rk;
+    a.qdf = pp.blk > 0 ? 1 : 0;   // the block solver reads and writes float pairs
     EIF_PROF(c, "poisson_dct2", 1);
     const FftShape sh = fftr_shape(pp.m);
     if (sh.T > 0) {
@@ -1339,7 +1434,17 @@ int launch_potential(eif_ctx *c, int rk, bool with_ibm) {
   if (pp.blk > 0) {
     EIF_PROF(c, "poisson_tdm", 2);
     dim3 g((n + 127) / 128, pp.nblk);
-    if (pp.blk == 16) {
+    if (mixed) {
+      float2 *qf = reinterpret_cast<float2 *>(c->qhat);
+      const DF ldf = dfpair(l);
+      if (pp.blk == 16) {
+        k_tdm_local_df<16><<<g, 128, 0, c->stream>>>(qf, pp.tdm_inv_df, pp.tdm_up_df, iface, first, ldf, n, pp.nblk, c->ld);
+      } else if (pp.blk == 8) {
+        k_tdm_local_df<8><<<g, 128, 0, c->stream>>>(qf, pp.tdm_inv_df, pp.tdm_up_df, iface, first, ldf, n, pp.nblk, c->ld);
+      } else {
+        k_tdm_local_df<4><<<g, 128, 0, c->stream>>>(qf, pp.tdm_inv_df, pp.tdm_up_df, iface, first, ldf, n, pp.nblk, c->ld);
+      }
+    } else if (pp.blk == 16) {
       k_tdm_local<16><<<g, 128, 0, c->stream>>>(c->qhat, pp.tdm_inv, pp.tdm_up, iface, first, l, n, pp.nblk, c->ld);
     } else if (pp.blk == 8) {
       k_tdm_local<8><<<g, 128, 0, c->stream>>>(c->qhat, pp.tdm_inv, pp.tdm_up, iface, first, l, n, pp.nblk, c->ld);
@@ -1383,6 +1488,7 @@ int launch_potential(eif_ctx *c, int rk, bool with_ibm) {
     a.fd = fd;
     a.scale = dfpair(1. / (2. * n));
     a.itot = n; a.jtot = jt; a.ld = c->ld; a.blk = pp.blk; a.nblk = pp.nblk;
+    a.qdf = pp.blk > 0 ? 1 : 0;
     EIF_PROF(c, "poisson_dct3", 1);
     const FftShape sh = fftr_shape(pp.m);
     if (sh.T > 0) {
