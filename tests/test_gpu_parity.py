@@ -218,6 +218,42 @@ def test_repush_between_steps_equals_uninterrupted_advance(gpu_lib):
         assert np.array_equal(a.pull_particles(), b.pull_particles())
 
 
+def test_page_locked_transfers_equal_pageable(gpu_lib):
+    """Page-locked host arrays are moved by the library's transfer kernels, pageable ones
+    by pitched copies: the same state goes in and comes out either way."""
+    torch = pytest.importorskip("torch")
+    from ellipsesinflows_gb300 import PREC_MIXED
+
+    def pinned(a):
+        t = torch.empty(a.shape, dtype=torch.float64, pin_memory=True)
+        out = t.numpy()
+        out[...] = a
+        return out
+
+    case = cases.contact_cluster()
+    a = Simulation.from_case(case, precision=PREC_MIXED)
+    b = Simulation.from_case(case, precision=PREC_MIXED)
+    a.advance(1)
+    ux, uy, p, _ = a.pull_fluid()
+    parts = a.pull_particles()
+    b.push_fluid(pinned(ux), pinned(uy), pinned(p))
+    b.push_particles(pinned(parts))
+    outs = tuple(pinned(np.full_like(x, np.nan)) for x in (ux, uy, p, p))
+    hp = pinned(np.full_like(parts, np.nan))
+    b.pull_fluid(out=outs)
+    b.pull_particles(out=hp)
+    for x, y in zip(a.pull_fluid()[:3], outs[:3]):   # psi is not part of the pushed state
+        assert np.array_equal(x, y)
+    assert np.array_equal(parts, hp)
+    a.advance(2)
+    b.advance(2)
+    b.pull_fluid(out=outs)
+    b.pull_particles(out=hp)
+    for x, y in zip(a.pull_fluid(), outs):
+        assert np.array_equal(x, y)
+    assert np.array_equal(a.pull_particles(), hp)
+
+
 def test_runs_are_deterministic(gpu_lib):
     case = cases.poiseuille(itot=128, jtot=256, n=16, a=0.04, b=0.02, seed=3)
     runs = []
