@@ -313,17 +313,19 @@ def run_e2e(sim, case, steps, pg, device):
     ux, uy, p, _ = sim.pull_fluid()
     parts = sim.pull_particles()
     pin = lambda a: torch.from_numpy(a).pin_memory().numpy()  # noqa: E731
-    hux, huy, hp, hpsi = pin(ux), pin(uy), pin(p), pin(np.zeros_like(p))
+    # the state a step reads and the result it leaves: ux, uy, p and the particle records
+    # (what the reference saves, src/save.c:41-90); psi is an intermediate of the step
+    hux, huy, hp = pin(ux), pin(uy), pin(p)
     hpart = pin(parts)
     h2d = hux.nbytes + huy.nbytes + hp.nbytes + hpart.nbytes
-    d2h = hux.nbytes + huy.nbytes + hp.nbytes + hpsi.nbytes + hpart.nbytes
+    d2h = hux.nbytes + huy.nbytes + hp.nbytes + hpart.nbytes
     barrier(pg, device)
     t0 = time.perf_counter()
     for _ in range(steps):
         sim.push_fluid(hux, huy, hp)
         sim.push_particles(hpart)
         sim.advance(1)
-        sim.pull_fluid(out=(hux, huy, hp, hpsi))
+        sim.pull_fluid(out=(hux, huy, hp, None))
         sim.pull_particles(out=hpart)
     el = time.perf_counter() - t0
     el = max_over_ranks(pg, el, device)

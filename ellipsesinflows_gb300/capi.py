@@ -182,15 +182,18 @@ class Solver:
 
     def pull_fluid(self, out=None):
         """ux, uy, p, psi as haloed arrays; with out=(ux, uy, p, psi) (C-contiguous float64
-        arrays of the right shapes, e.g. in pinned host memory) they are filled in place."""
+        arrays of the right shapes, e.g. in pinned host memory) they are filled in place,
+        and a None entry is skipped (not transferred)."""
         sx, sy = self.shapes()
         if out is None:
             out = (np.empty(sx), np.empty(sy), np.empty(sy), np.empty(sy))
         for a, shape in zip(out, (sx, sy, sy, sy)):
+            if a is None:
+                continue
             if a.shape != shape or a.dtype != np.float64 or not a.flags["C_CONTIGUOUS"]:
                 raise ValueError("output arrays must be C-contiguous float64 of shapes %s, %s" % (sx, sy))
         ux, uy, p, psi = out
-        self._call("pull_fluid", self.ctx, _ptr(ux), _ptr(uy), _ptr(p), _ptr(psi))
+        self._call("pull_fluid", self.ctx, *[None if a is None else _ptr(a) for a in (ux, uy, p, psi)])
         return ux, uy, p, psi
 
     def push_particles(self, records):
