@@ -288,6 +288,47 @@ __global__ void k_task_table(const int *__restrict__ box, const int *__restrict_
     if (EIF_CHK(bd.rec, c, cap, 59)) tdesc[c] = d;
   }
 }
+// The same table with the task offsets formed in the same kernel, for particle
+// counts up to TT_MAX_NP: every block sums the task counts of the particles before
+// its own (a few thousand integers from L2), then each warp writes its particle's
+// offset and table entries. Replaces k_scan + k_task_table (one launch and one
+// single-block pass fewer on the path of every box build).
+constexpr int TT_WARPS = 8;
+constexpr int TT_MAX_NP = 8192;
+__global__ void __launch_bounds__(TT_WARPS * 32) k_task_table_scan(const int *__restrict__ box, const int *__restrict__ cnt,
+                                                                  int *__restrict__ off, int4 *__restrict__ tdesc, int np,
+                                                                  Bounds bd, int cap) {
+  __shared__ int red[TT_WARPS], wcnt[TT_WARPS];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int n0 = blockIdx.x * TT_WARPS;
+  int s = 0;
+  for (int q = threadIdx.x; q < n0; q += blockDim.x) s += cnt[q];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  const int n = n0 + w;
+  const int my = n < np ? cnt[n] : 0;
+  if (lane == 0) {
+    red[w] = s;
+    wcnt[w] = my;
+  }
+  __syncthreads();
+  int c0 = 0;
+#pragma unroll
+  for (int q = 0; q < TT_WARPS; q++) c0 += red[q] + (q < w ? wcnt[q] : 0);
+  if (n >= np) return;
+  if (lane == 0) {
+    if (EIF_CHK(bd.rec, n, bd.off, 5)) off[n] = c0;
+    if (n == np - 1 && EIF_CHK(bd.rec, np, bd.off, 6)) off[np] = c0 + my;
+  }
+  const int4 *b4 = reinterpret_cast<const int4 *>(box + 12 * n);
+  const int4 bA = b4[0], bB = b4[1], bC = b4[2];
+  for (int c = c0 + lane; c < c0 + my; c += 32) {
+    RowTask t;
+    int4 d = make_int4(-1, 0, 0, 0);
+    if (row_task(bA, bB, bC, c - c0, t)) d = make_int4(n, t.j, t.ib, t.ie * 4 + t.img + 1);
+    if (EIF_CHK(bd.rec, c, cap, 59)) tdesc[c] = d;
+  }
+}
 __device__ __forceinline__ bool task_of(int4 d, int np, RowTask &t) {
   t.j = d.y;
   t.ib = d.z;
@@ -1139,15 +1180,21 @@ static int launch_boxes(eif_ctx *c, bool use_increment) {
   b.pf = c->cfg.precision == EIF_PREC_MIXED ? c->pf : nullptr;
   int *cnt = c->chunk_off + (c->np + 1);
   b.nchunk = cnt;
-  EIF_PROF(c, "ibm_boxes", 3);
+  EIF_PROF(c, "ibm_boxes", c->np <= TT_MAX_NP ? 2 : 3);
   // FP64-heavy per particle: small blocks spread the particles over many SMs
   k_boxes<<<(c->np + 15) / 16, 16, 0, c->stream>>>(b);
   EIF_LAUNCH_CK(c);
-  k_scan<<<1, 1024, 0, c->stream>>>(cnt, c->chunk_off, c->np, bounds_of(c));
-  EIF_LAUNCH_CK(c);
-  k_task_table<<<(c->np * 32 + 255) / 256, 256, 0, c->stream>>>(c->box, c->chunk_off, c->tdesc, c->np, bounds_of(c),
-                                                                 c->chunk_cap);
-  EIF_LAUNCH_CK(c);
+  if (c->np <= TT_MAX_NP) {
+    k_task_table_scan<<<(c->np + TT_WARPS - 1) / TT_WARPS, TT_WARPS * 32, 0, c->stream>>>(
+        c->box, cnt, c->chunk_off, c->tdesc, c->np, bounds_of(c), c->chunk_cap);
+    EIF_LAUNCH_CK(c);
+  } else {
+    k_scan<<<1, 1024, 0, c->stream>>>(cnt, c->chunk_off, c->np, bounds_of(c));
+    EIF_LAUNCH_CK(c);
+    k_task_table<<<(c->np * 32 + 255) / 256, 256, 0, c->stream>>>(c->box, c->chunk_off, c->tdesc, c->np,
+                                                                   bounds_of(c), c->chunk_cap);
+    EIF_LAUNCH_CK(c);
+  }
   c->boxes_x_valid = x_only;
   return EIF_OK;
 }

@@ -264,7 +264,9 @@ __global__ void __launch_bounds__(RED_THREADS) k_tdm_reduced(double *__restrict_
 // side; one thread per wavenumber solves the cyclic system of the Q values t_g
 // (A2 = A phi[G-2], B2 = B + 2 A phi[0], the reference's cyclic algorithm as at the
 // first level, kx = 0 pinned with its last value 0); every thread then adds
-// t_{g-1} phi[i] + t_g phi[G-2-i] to its interior. Block: 32 wavenumbers x Q groups.
+// t_{g-1} phi[i] + t_g phi[G-2-i] to its interior. Block: RED2_K wavenumbers x Q
+// groups (16 wavenumbers per block spread the FP64 work over 128 SMs at 2048 x 4096).
+constexpr int RED2_K = 16;
 template <int G>
 __global__ void __launch_bounds__(1024) k_tdm_reduced2(double *__restrict__ iface, const double *__restrict__ first,
                                                        const double *__restrict__ rcoef, const double *__restrict__ inv2,
@@ -272,10 +274,11 @@ __global__ void __launch_bounds__(1024) k_tdm_reduced2(double *__restrict__ ifac
                                                        const double *__restrict__ ri2, const double *__restrict__ ru2,
                                                        const double *__restrict__ rq2, const double *__restrict__ rc2,
                                                        double l, int itot, int P, int Q) {
-  extern __shared__ double sm2[];   // [Q][32] first interior values, right-hand sides, interface values
-  double *y0s = sm2, *rhs = sm2 + (size_t)Q * 32, *ts = sm2 + (size_t)2 * Q * 32;
-  const int kk = threadIdx.x & 31, g = threadIdx.x >> 5;
-  const int k = blockIdx.x * 32 + kk;
+  extern __shared__ double sm2[];   // [Q][RED2_K] first interior values, right-hand sides, interface values
+  constexpr int K = RED2_K;
+  double *y0s = sm2, *rhs = sm2 + (size_t)Q * K, *ts = sm2 + (size_t)2 * Q * K;
+  const int kk = threadIdx.x % K, g = threadIdx.x / K;
+  const int k = blockIdx.x * K + kk;
   const bool on = k < itot;
   const int kc = on ? k : itot - 1;
   const double A = rcoef[4 * kc + 0];
@@ -292,9 +295,9 @@ __global__ void __launch_bounds__(1024) k_tdm_reduced2(double *__restrict__ ifac
   for (int i = 1; i < G - 1; i++) y[i] = (y[i] - A * y[i - 1]) * inv2[(size_t)i * itot + kc];
 #pragma unroll
   for (int i = G - 3; i >= 0; i--) y[i] = y[i] - up2[(size_t)i * itot + kc] * y[i + 1];
-  y0s[g * 32 + kk] = y[0];
+  y0s[g * K + kk] = y[0];
   __syncthreads();
-  rhs[g * 32 + kk] = rlast - A * y[G - 2] - A * y0s[((g + 1) % Q) * 32 + kk];
+  rhs[g * K + kk] = rlast - A * y[G - 2] - A * y0s[((g + 1) % Q) * K + kk];
   __syncthreads();
   if (g == 0) {
     const double A2 = rc2[4 * kc + 0], den2 = rc2[4 * kc + 2];
@@ -302,21 +305,21 @@ __global__ void __launch_bounds__(1024) k_tdm_reduced2(double *__restrict__ ifac
     double zprev = rhs[kk] * ri2[kc];
     ts[kk] = zprev;
     for (int q = 1; q < Q - 1; q++) {
-      zprev = (rhs[q * 32 + kk] - A2 * zprev) * ri2[(size_t)q * itot + kc];
-      ts[q * 32 + kk] = zprev;
+      zprev = (rhs[q * K + kk] - A2 * zprev) * ri2[(size_t)q * itot + kc];
+      ts[q * K + kk] = zprev;
     }
     for (int q = Q - 3; q >= 0; q--) {
-      zprev = ts[q * 32 + kk] - ru2[(size_t)q * itot + kc] * zprev;
-      ts[q * 32 + kk] = zprev;
+      zprev = ts[q * K + kk] - ru2[(size_t)q * itot + kc] * zprev;
+      ts[q * K + kk] = zprev;
     }
-    const double num = rhs[(Q - 1) * 32 + kk] - A2 * ts[kk] - A2 * ts[(Q - 2) * 32 + kk];
+    const double num = rhs[(Q - 1) * K + kk] - A2 * ts[kk] - A2 * ts[(Q - 2) * K + kk];
     const double last = pin ? 0. : num / den2;
-    for (int q = 0; q < Q - 1; q++) ts[q * 32 + kk] = ts[q * 32 + kk] + last * rq2[(size_t)q * itot + kc];
-    ts[(Q - 1) * 32 + kk] = last;
+    for (int q = 0; q < Q - 1; q++) ts[q * K + kk] = ts[q * K + kk] + last * rq2[(size_t)q * itot + kc];
+    ts[(Q - 1) * K + kk] = last;
   }
   __syncthreads();
   if (!on) return;
-  const double tl = ts[((g + Q - 1) % Q) * 32 + kk], tr = ts[g * 32 + kk];
+  const double tl = ts[((g + Q - 1) % Q) * K + kk], tr = ts[g * K + kk];
 #pragma unroll
   for (int i = 0; i < G - 1; i++) {
     iface[(size_t)(g * G + i) * itot + k] =
@@ -1454,18 +1457,18 @@ int launch_potential(eif_ctx *c, int rk, bool with_ibm) {
     EIF_LAUNCH_CK(c);
     if (pp.g2 > 0) {
       const int Q = pp.q2;
-      const size_t sm = sizeof(double) * 3 * 32 * (size_t)Q;
-      const dim3 grid((n + 31) / 32);
+      const size_t sm = sizeof(double) * 3 * RED2_K * (size_t)Q;
+      const dim3 grid((n + RED2_K - 1) / RED2_K);
       if (pp.g2 == 16) {
-        k_tdm_reduced2<16><<<grid, 32 * Q, sm, c->stream>>>(iface, first, pp.red_coef, pp.r2_inv, pp.r2_up, pp.r2_phi,
+        k_tdm_reduced2<16><<<grid, RED2_K * Q, sm, c->stream>>>(iface, first, pp.red_coef, pp.r2_inv, pp.r2_up, pp.r2_phi,
                                                             pp.r2_qinv, pp.r2_qup, pp.r2_q1, pp.r2_coef, l, n,
                                                             pp.nblk, Q);
       } else if (pp.g2 == 8) {
-        k_tdm_reduced2<8><<<grid, 32 * Q, sm, c->stream>>>(iface, first, pp.red_coef, pp.r2_inv, pp.r2_up, pp.r2_phi,
+        k_tdm_reduced2<8><<<grid, RED2_K * Q, sm, c->stream>>>(iface, first, pp.red_coef, pp.r2_inv, pp.r2_up, pp.r2_phi,
                                                            pp.r2_qinv, pp.r2_qup, pp.r2_q1, pp.r2_coef, l, n,
                                                            pp.nblk, Q);
       } else {
-        k_tdm_reduced2<4><<<grid, 32 * Q, sm, c->stream>>>(iface, first, pp.red_coef, pp.r2_inv, pp.r2_up, pp.r2_phi,
+        k_tdm_reduced2<4><<<grid, RED2_K * Q, sm, c->stream>>>(iface, first, pp.red_coef, pp.r2_inv, pp.r2_up, pp.r2_phi,
                                                            pp.r2_qinv, pp.r2_qup, pp.r2_q1, pp.r2_coef, l, n,
                                                            pp.nblk, Q);
       }
