@@ -146,74 +146,89 @@ struct BoxArgs {
   Bounds bd;
 };
 
-// per-particle boxes of the three periodic images and their chunk counts
-__global__ void k_boxes(BoxArgs a) {
-  const int n = blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= a.np) return;
+// Per-particle boxes of the three periodic images and their task counts, and the
+// single-precision parameters. The double-precision work of one particle is a long
+// chain of dependent operations (divisions, sincos), so eight lanes share it: lanes
+// 0-2 the boxes of images -1, 0, +1, lanes 3-7 groups of parameters.
+constexpr int BOX_LANES = 8;
+__global__ void __launch_bounds__(128) k_boxes(BoxArgs a) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = t / BOX_LANES, sub = t % BOX_LANES;   // a particle's lanes lie in one warp
   const double *P = a.P;
   const int pc = a.pcap;
-  if (!EIF_CHK(a.bd.rec, EIF_P_DY * pc + n, a.bd.P, 1)) return;
-  const double pa = P[EIF_P_A * pc + n], pb = P[EIF_P_B * pc + n];
-  double px = P[EIF_P_X * pc + n], py = P[EIF_P_Y * pc + n];
-  if (a.use_increment) {
-    px = px + P[EIF_P_DX * pc + n];
-    py = py + P[EIF_P_DY * pc + n];
-  }
-  const double r = fmax(pa, pb);
-  if (a.pf) {
-    // everything the single-precision cell loop needs, formed once per particle in double
-    float *q = a.pf + (size_t)PF_WORDS * n;
-    const double den = P[EIF_P_DEN * pc + n];
-    double az = P[EIF_P_AZ * pc + n];
-    if (a.use_increment) az = az + P[EIF_P_DAZ * pc + n];
-    double sz, cz;
-    sincos(-az, &sz, &cz);
-    q[PF_A] = (float)pa;
-    q[PF_B] = (float)pb;
-    q[PF_CZ] = (float)cz;
-    q[PF_SZ] = (float)sz;
-    q[PF_KEX] = (float)(pa * (1. - (pb / pa) * (pb / pa)));
-    q[PF_KEY] = (float)(pb * (1. - (pa / pb) * (pa / pb)));
-    q[PF_RPM] = (float)(1. / pmass(den, pa, pb));
-    q[PF_RPIM] = (float)(1. / pmoi(den, pa, pb));
-    q[PF_UX] = (float)P[EIF_P_UX * pc + n];
-    q[PF_UY] = (float)P[EIF_P_UY * pc + n];
-    q[PF_VZ] = (float)P[EIF_P_VZ * pc + n];
-    // cell centres XC(i) = (i - 1/2) dx, YC(j) = (j - 1/2) dy: offsets in grid units are
-    // (i - i0) - gx and (j - j0[m]) - gy[m] for the periodic images m = -1, 0, +1
-    const double sx = px / a.dx;
-    const int i0 = (int)floor(sx);
-    q[PF_GX] = (float)(sx - i0 + 0.5);
-    q[PF_I0] = __int_as_float(i0);
-    for (int m = 0; m < 3; m++) {
-      const double sy = (py + a.ly * (m - 1)) / a.dy;
-      const int j0 = (int)floor(sy);
-      q[PF_J0 + m] = __int_as_float(j0);
-      q[PF_GY + m] = (float)(sy - j0 + 0.5);
-    }
-    // rho^2 = al X^2 + 2 ka X Y + de Y^2 for lab-frame offsets (X, Y); far-cell scales
-    const double mn = fmin(pa, pb), mx = fmax(pa, pb);
-    const double md = FAR_CELLS_F * fmin(a.dx, a.dy);
-    const double so = 1. + md / mn, si = 1. - md / mn;
-    q[PF_AL] = (float)(cz * cz / (pa * pa) + sz * sz / (pb * pb));
-    q[PF_KA] = (float)(cz * sz * (1. / (pb * pb) - 1. / (pa * pa)));
-    q[PF_DE] = (float)(sz * sz / (pa * pa) + cz * cz / (pb * pb));
-    q[PF_SO2] = (float)(so * so);
-    q[PF_SI2] = si > 0. ? (float)(si * si) : -1.f;
-    q[PF_RO2] = (float)((mx + md) * (mx + md));
-  }
+  bool on = n < a.np;
+  if (on && !EIF_CHK(a.bd.rec, EIF_P_DY * pc + n, a.bd.P, 1)) on = false;
   int tasks = 0;
-  for (int per = -1; per <= 1; per++) {
-    int imin, imax, jmin, jmax;
-    loop_size(1, a.itot, a.dx, r, px, imin, imax);
-    loop_size(1, a.jtot, a.dy, r, py + a.ly * per - a.yf1, jmin, jmax);
-    int *bx = a.box + 12 * n + 4 * (per + 1);
-    if (!EIF_CHK(a.bd.rec, 12 * n + 4 * (per + 1) + 3, a.bd.box, 2)) return;
-    bx[0] = imin; bx[1] = imax; bx[2] = jmin; bx[3] = jmax;
-    if (imax >= imin && jmax >= jmin) tasks += (jmax - jmin + 1) * box_segs(imax - imin + 1);
+  if (on) {
+    const double pa = P[EIF_P_A * pc + n], pb = P[EIF_P_B * pc + n];
+    double px = P[EIF_P_X * pc + n], py = P[EIF_P_Y * pc + n];
+    if (a.use_increment) {
+      px = px + P[EIF_P_DX * pc + n];
+      py = py + P[EIF_P_DY * pc + n];
+    }
+    const double r = fmax(pa, pb);
+    float *q = a.pf ? a.pf + (size_t)PF_WORDS * n : nullptr;
+    if (sub < 3) {
+      const int per = sub - 1;
+      int imin, imax, jmin, jmax;
+      loop_size(1, a.itot, a.dx, r, px, imin, imax);
+      loop_size(1, a.jtot, a.dy, r, py + a.ly * per - a.yf1, jmin, jmax);
+      if (EIF_CHK(a.bd.rec, 12 * n + 4 * sub + 3, a.bd.box, 2)) {
+        int *bx = a.box + 12 * n + 4 * sub;
+        bx[0] = imin; bx[1] = imax; bx[2] = jmin; bx[3] = jmax;
+        if (imax >= imin && jmax >= jmin) tasks = (jmax - jmin + 1) * box_segs(imax - imin + 1);
+      }
+    } else if (q && sub == 3) {
+      // orientation and the quadratic form rho^2 = al X^2 + 2 ka X Y + de Y^2 of the
+      // ellipse for lab-frame offsets (X, Y)
+      double az = P[EIF_P_AZ * pc + n];
+      if (a.use_increment) az = az + P[EIF_P_DAZ * pc + n];
+      double sz, cz;
+      sincos(-az, &sz, &cz);
+      q[PF_CZ] = (float)cz;
+      q[PF_SZ] = (float)sz;
+      q[PF_AL] = (float)(cz * cz / (pa * pa) + sz * sz / (pb * pb));
+      q[PF_KA] = (float)(cz * sz * (1. / (pb * pb) - 1. / (pa * pa)));
+      q[PF_DE] = (float)(sz * sz / (pa * pa) + cz * cz / (pb * pb));
+    } else if (q && sub == 4) {
+      q[PF_A] = (float)pa;
+      q[PF_B] = (float)pb;
+      q[PF_KEX] = (float)(pa * (1. - (pb / pa) * (pb / pa)));
+      q[PF_KEY] = (float)(pb * (1. - (pa / pb) * (pa / pb)));
+    } else if (q && sub == 5) {
+      const double den = P[EIF_P_DEN * pc + n];
+      q[PF_RPM] = (float)(1. / pmass(den, pa, pb));
+      q[PF_RPIM] = (float)(1. / pmoi(den, pa, pb));
+      q[PF_UX] = (float)P[EIF_P_UX * pc + n];
+      q[PF_UY] = (float)P[EIF_P_UY * pc + n];
+      q[PF_VZ] = (float)P[EIF_P_VZ * pc + n];
+    } else if (q && sub == 6) {
+      // cell centres XC(i) = (i - 1/2) dx, YC(j) = (j - 1/2) dy: offsets in grid units are
+      // (i - i0) - gx and (j - j0[m]) - gy[m] for the periodic images m = -1, 0, +1
+      const double sx = px / a.dx;
+      const int i0 = (int)floor(sx);
+      q[PF_GX] = (float)(sx - i0 + 0.5);
+      q[PF_I0] = __int_as_float(i0);
+      for (int m = 0; m < 3; m++) {
+        const double sy = (py + a.ly * (m - 1)) / a.dy;
+        const int j0 = (int)floor(sy);
+        q[PF_J0 + m] = __int_as_float(j0);
+        q[PF_GY + m] = (float)(sy - j0 + 0.5);
+      }
+    } else if (q && sub == 7) {
+      // far-cell scales (row_chords)
+      const double mn = fmin(pa, pb), mx = fmax(pa, pb);
+      const double md = FAR_CELLS_F * fmin(a.dx, a.dy);
+      const double so = 1. + md / mn, si = 1. - md / mn;
+      q[PF_SO2] = (float)(so * so);
+      q[PF_SI2] = si > 0. ? (float)(si * si) : -1.f;
+      q[PF_RO2] = (float)((mx + md) * (mx + md));
+    }
   }
-  if (!EIF_CHK(a.bd.rec, (a.nchunk - a.bd_off_base) + n, a.bd.off, 3)) return;
-  a.nchunk[n] = tasks;
+  // task count of the particle: the sum over its lanes (only lanes 0-2 count)
+#pragma unroll
+  for (int o = 1; o < BOX_LANES; o <<= 1) tasks += __shfl_xor_sync(0xffffffffu, tasks, o, BOX_LANES);
+  if (on && sub == 0 && EIF_CHK(a.bd.rec, (a.nchunk - a.bd_off_base) + n, a.bd.off, 3)) a.nchunk[n] = tasks;
 }
 
 // exclusive scan of the chunk counts (one block); off[np] = total
@@ -1181,8 +1196,7 @@ static int launch_boxes(eif_ctx *c, bool use_increment) {
   int *cnt = c->chunk_off + (c->np + 1);
   b.nchunk = cnt;
   EIF_PROF(c, "ibm_boxes", c->np <= TT_MAX_NP ? 2 : 3);
-  // FP64-heavy per particle: small blocks spread the particles over many SMs
-  k_boxes<<<(c->np + 15) / 16, 16, 0, c->stream>>>(b);
+  k_boxes<<<(c->np * BOX_LANES + 127) / 128, 128, 0, c->stream>>>(b);
   EIF_LAUNCH_CK(c);
   if (c->np <= TT_MAX_NP) {
     k_task_table_scan<<<(c->np + TT_WARPS - 1) / TT_WARPS, TT_WARPS * 32, 0, c->stream>>>(
