@@ -148,12 +148,15 @@ struct BoxArgs {
 
 // Per-particle boxes of the three periodic images and their task counts, and the
 // single-precision parameters. The double-precision work of one particle is a long
-// chain of dependent operations (divisions, sincos), so eight lanes share it: lanes
-// 0-2 the boxes of images -1, 0, +1, lanes 3-7 groups of parameters.
-constexpr int BOX_LANES = 8;
-__global__ void __launch_bounds__(128) k_boxes(BoxArgs a) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int n = t / BOX_LANES, sub = t % BOX_LANES;   // a particle's lanes lie in one warp
+// chain (divisions, sincos) and the FP64 pipe takes a warp instruction at a time, so
+// the work is split into eight parts run by different warps (grid row blockIdx.y),
+// each over 32 particles: rows 0-2 the boxes of images -1, 0, +1 (their task counts
+// are added to nchunk, zeroed before the launch), rows 3-7 groups of parameters
+// (mixed form only).
+constexpr int BOX_PARTS = 8;
+__global__ void __launch_bounds__(32) k_boxes(BoxArgs a) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  const int sub = blockIdx.y;
   const double *P = a.P;
   const int pc = a.pcap;
   bool on = n < a.np;
@@ -225,10 +228,7 @@ __global__ void __launch_bounds__(128) k_boxes(BoxArgs a) {
       q[PF_RO2] = (float)((mx + md) * (mx + md));
     }
   }
-  // task count of the particle: the sum over its lanes (only lanes 0-2 count)
-#pragma unroll
-  for (int o = 1; o < BOX_LANES; o <<= 1) tasks += __shfl_xor_sync(0xffffffffu, tasks, o, BOX_LANES);
-  if (on && sub == 0 && EIF_CHK(a.bd.rec, (a.nchunk - a.bd_off_base) + n, a.bd.off, 3)) a.nchunk[n] = tasks;
+  if (on && tasks && EIF_CHK(a.bd.rec, (a.nchunk - a.bd_off_base) + n, a.bd.off, 3)) atomicAdd(a.nchunk + n, tasks);
 }
 
 // exclusive scan of the chunk counts (one block); off[np] = total
@@ -1196,7 +1196,8 @@ static int launch_boxes(eif_ctx *c, bool use_increment) {
   int *cnt = c->chunk_off + (c->np + 1);
   b.nchunk = cnt;
   EIF_PROF(c, "ibm_boxes", c->np <= TT_MAX_NP ? 2 : 3);
-  k_boxes<<<(c->np * BOX_LANES + 127) / 128, 128, 0, c->stream>>>(b);
+  EIF_CK(c, cudaMemsetAsync(cnt, 0, sizeof(int) * c->np, c->stream));
+  k_boxes<<<dim3((c->np + 31) / 32, b.pf ? BOX_PARTS : 3), 32, 0, c->stream>>>(b);
   EIF_LAUNCH_CK(c);
   if (c->np <= TT_MAX_NP) {
     k_task_table_scan<<<(c->np + TT_WARPS - 1) / TT_WARPS, TT_WARPS * 32, 0, c->stream>>>(
