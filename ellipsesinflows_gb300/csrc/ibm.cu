@@ -787,9 +787,11 @@ __global__ void __launch_bounds__(256, 3) k_ibm_work_f(WorkArgs a) {
       sacc2 += __shfl_xor_sync(0xffffffffu, sacc2, o);
     }
     if (lane == 0 && EIF_CHK(a.bd.rec, 3LL * c + 2, a.bd.partial, 58)) {
-      a.partial[3 * (size_t)c + 0] = eifd::f2d(sacc0);
-      a.partial[3 * (size_t)c + 1] = eifd::f2d(sacc1);
-      a.partial[3 * (size_t)c + 2] = eifd::f2d(sacc2);
+      // single-precision partial sums, reduced per particle by k_chunk_reduce_f
+      float *pf3 = reinterpret_cast<float *>(a.partial);
+      pf3[3 * (size_t)c + 0] = sacc0;
+      pf3[3 * (size_t)c + 1] = sacc1;
+      pf3[3 * (size_t)c + 2] = sacc2;
     }
   }
 }
@@ -874,9 +876,11 @@ __global__ void __launch_bounds__(256, 6) k_ibm_sum_f(WorkArgs a) {
       sacc2 += __shfl_xor_sync(0xffffffffu, sacc2, o);
     }
     if (lane == 0 && EIF_CHK(a.bd.rec, 3LL * c + 2, a.bd.partial, 79)) {
-      a.partial[3 * (size_t)c + 0] = eifd::f2d(sacc0);
-      a.partial[3 * (size_t)c + 1] = eifd::f2d(sacc1);
-      a.partial[3 * (size_t)c + 2] = eifd::f2d(sacc2);
+      // single-precision partial sums, reduced per particle by k_chunk_reduce_f
+      float *pf3 = reinterpret_cast<float *>(a.partial);
+      pf3[3 * (size_t)c + 0] = sacc0;
+      pf3[3 * (size_t)c + 1] = sacc1;
+      pf3[3 * (size_t)c + 2] = sacc2;
     }
   }
 }
@@ -903,6 +907,45 @@ __global__ void k_chunk_reduce(const double *__restrict__ partial, const int *__
     P[f0 * pcap + n] = s0;
     P[f1 * pcap + n] = s1;
     P[f2 * pcap + n] = s2;
+  }
+}
+
+// The same per-particle sums from the single-precision partials of the mixed form,
+// accumulated in double-float arithmetic (TwoSum) on the FP32 pipe: the sum of at most
+// a few hundred floats is kept to about 48 bits, and the result is rounded once to
+// double.
+__global__ void k_chunk_reduce_f(const float *__restrict__ partial, const int *__restrict__ off, double *__restrict__ P,
+                                 int pcap, int np, int f0, int f1, int f2, Bounds bd) {
+  const int lane = threadIdx.x & 31;
+  const int n = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (n >= np) return;
+  if (!EIF_CHK(bd.rec, n + 1, bd.off, 33)) return;
+  const int c0 = off[n], c1 = off[n + 1];
+  float h[3] = {0.f, 0.f, 0.f}, l[3] = {0.f, 0.f, 0.f};
+  for (int c = c0 + lane; c < c1; c += 32) {
+    if (!EIF_CHK(bd.rec, 3LL * c + 2, 2 * bd.partial, 34)) break;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      const float v = partial[3 * (size_t)c + k];
+      const float s = h[k] + v, bb = s - h[k];
+      l[k] += (h[k] - (s - bb)) + (v - bb);
+      h[k] = s;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      const float vh = __shfl_xor_sync(0xffffffffu, h[k], o), vl = __shfl_xor_sync(0xffffffffu, l[k], o);
+      const float s = h[k] + vh, bb = s - h[k];
+      l[k] += ((h[k] - (s - bb)) + (vh - bb)) + vl;
+      h[k] = s;
+    }
+  }
+  if (lane == 0 && EIF_CHK(bd.rec, f2 * pcap + n, bd.P, 35)) {
+    P[f0 * pcap + n] = eifd::f2d(h[0]) + eifd::f2d(l[0]);
+    P[f1 * pcap + n] = eifd::f2d(h[1]) + eifd::f2d(l[1]);
+    P[f2 * pcap + n] = eifd::f2d(h[2]) + eifd::f2d(l[2]);
   }
 }
 
@@ -1277,8 +1320,14 @@ static int launch_work(eif_ctx *c, int mode, int cn) {
   const int f1 = mode == 0 ? EIF_P_IUY0 + cn : EIF_P_FUY;
   const int f2 = mode == 0 ? EIF_P_IVZ0 + cn : EIF_P_TVZ;
   EIF_PROF(c, "ibm_reduce", 1);
-  k_chunk_reduce<<<(c->np * 32 + 255) / 256, 256, 0, c->stream>>>(c->partial, c->chunk_off, c->P, c->pcap, c->np, f0,
-                                                                    f1, f2, bounds_of(c));
+  if (c->cfg.precision == EIF_PREC_MIXED) {
+    k_chunk_reduce_f<<<(c->np * 32 + 255) / 256, 256, 0, c->stream>>>(reinterpret_cast<const float *>(c->partial),
+                                                                        c->chunk_off, c->P, c->pcap, c->np, f0, f1,
+                                                                        f2, bounds_of(c));
+  } else {
+    k_chunk_reduce<<<(c->np * 32 + 255) / 256, 256, 0, c->stream>>>(c->partial, c->chunk_off, c->P, c->pcap, c->np,
+                                                                      f0, f1, f2, bounds_of(c));
+  }
   EIF_LAUNCH_CK(c);
   return EIF_OK;
 }
