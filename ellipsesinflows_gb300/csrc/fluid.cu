@@ -377,40 +377,47 @@ __global__ void __launch_bounds__(TX *TY) k_correct_df(CorrArgsDF a) {
 // dt: column maxima of |ux| and the global maximum of |uy| as order-preserving
 // integer maxima of the IEEE bit patterns (non-negative doubles order like
 // their bits), so the result is independent of the reduction order.
-__global__ void k_dt_colmax(const double *__restrict__ ux, const double *__restrict__ uy, int itot, int jtot, int ld,
-                            unsigned long long *__restrict__ colmax, unsigned long long *__restrict__ uymax,
-                            unsigned *__restrict__ flags) {
-  const int i = 1 + blockIdx.x * TX + threadIdx.x;
-  unsigned long long mx = 0ull, my = 0ull;
+constexpr int CM_THREADS = 256;   // column pairs per block: 8 KB of a row per block and row
+__global__ void __launch_bounds__(CM_THREADS) k_dt_colmax(const double *__restrict__ ux, const double *__restrict__ uy,
+                                                          int itot, int jtot, int ld,
+                                                          unsigned long long *__restrict__ colmax,
+                                                          unsigned long long *__restrict__ uymax,
+                                                          unsigned *__restrict__ flags) {
+  // each thread owns the pair of row entries 2p, 2p + 1 (16-byte loads; rows start on
+  // 256-byte boundaries) over the rows blockIdx.y + 1, + gridDim.y, ...: ux entry k is
+  // UX(k + 1), counted for 2 <= k + 1 <= itot; uy entry k is UY(k), for 1 <= k <= itot
+  const int p = blockIdx.x * CM_THREADS + threadIdx.x;
+  const int k0 = 2 * p;
+  unsigned long long mx0 = 0ull, mx1 = 0ull, my = 0ull;
   bool bad = false;
-  if (i <= itot) {
+  if (k0 <= itot) {
+    const bool x0 = k0 >= 1 && k0 <= itot - 1, x1 = k0 + 1 <= itot - 1;
+    const bool y0 = k0 >= 1, y1 = k0 + 1 <= itot;
 #pragma unroll 4
-    for (int j = 1 + blockIdx.y * TY + threadIdx.y; j <= jtot; j += TY * gridDim.y) {
-      if (i >= 2) {
-        const unsigned long long b = __double_as_longlong(__ldg(ux + ux_idx(i, j, ld))) & 0x7fffffffffffffffull;
-        bad |= b >= 0x7ff0000000000000ull;
-        mx = b > mx ? b : mx;
-      }
-      const unsigned long long b = __double_as_longlong(__ldg(uy + uy_idx(i, j, ld))) & 0x7fffffffffffffffull;
-      bad |= b >= 0x7ff0000000000000ull;
-      my = b > my ? b : my;
+    for (int j = 1 + blockIdx.y; j <= jtot; j += gridDim.y) {
+      const double2 u = __ldg(reinterpret_cast<const double2 *>(ux + (size_t)j * ld) + p);
+      const double2 v = __ldg(reinterpret_cast<const double2 *>(uy + (size_t)j * ld) + p);
+      const unsigned long long bu0 = __double_as_longlong(u.x) & 0x7fffffffffffffffull;
+      const unsigned long long bu1 = __double_as_longlong(u.y) & 0x7fffffffffffffffull;
+      const unsigned long long bv0 = y0 ? __double_as_longlong(v.x) & 0x7fffffffffffffffull : 0ull;
+      const unsigned long long bv1 = y1 ? __double_as_longlong(v.y) & 0x7fffffffffffffffull : 0ull;
+      if (x0) mx0 = bu0 > mx0 ? bu0 : mx0;
+      if (x1) mx1 = bu1 > mx1 ? bu1 : mx1;
+      const unsigned long long bv = bv0 > bv1 ? bv0 : bv1;
+      my = bv > my ? bv : my;
+      bad |= (x0 && bu0 >= 0x7ff0000000000000ull) || (x1 && bu1 >= 0x7ff0000000000000ull) ||
+             bv >= 0x7ff0000000000000ull;
     }
   }
-  __shared__ unsigned long long sx[TY][TX];
-  sx[threadIdx.y][threadIdx.x] = mx;
   // maximum of uy over the block: warp reduce then one atomic per warp
   for (int o = 16; o > 0; o >>= 1) {
     const unsigned long long other = __shfl_xor_sync(0xffffffffu, my, o);
     my = other > my ? other : my;
   }
-  if (threadIdx.x == 0 && my) atomicMax(uymax, my);
+  if ((threadIdx.x & 31) == 0 && my) atomicMax(uymax, my);
   if (bad) atomicOr(flags, EIF_FLAG_NONFINITE);
-  __syncthreads();
-  if (threadIdx.y == 0 && i <= itot && i >= 2) {
-    unsigned long long m = 0ull;
-    for (int r = 0; r < TY; r++) m = sx[r][threadIdx.x] > m ? sx[r][threadIdx.x] : m;
-    if (m) atomicMax(colmax + i, m);
-  }
+  if (mx0) atomicMax(colmax + k0 + 1, mx0);
+  if (mx1) atomicMax(colmax + k0 + 2, mx1);
 }
 
 // single-precision products of dt used by the mixed-precision kernels, formed
@@ -487,14 +494,19 @@ __global__ void k_dt_partial(const unsigned long long *__restrict__ colmax, cons
 
 // param_decide_dt (decide_dt.c:11-81): minima of the partial limits, the safety
 // factors, dt and the single-precision dt products
+// one warp: every lane loads one block's partial limits (nparts <= 32), a shuffle
+// reduction forms the minima (exact, so independent of the order)
 __global__ void k_dt_final(const double *__restrict__ part, int nparts, double dy, double Re, double sf_adv,
                            double sf_dif, double sf_par, double *__restrict__ dt_out, float *__restrict__ coef) {
-  double dta = part[0], dxmin = part[1], dtp = part[2];
-  for (int k = 1; k < nparts; k++) {
-    dta = fmin(dta, part[3 * k]);
-    dxmin = fmin(dxmin, part[3 * k + 1]);
-    dtp = fmin(dtp, part[3 * k + 2]);
+  const int l = threadIdx.x;
+  const int q = l < nparts ? l : 0;
+  double dta = part[3 * q], dxmin = part[3 * q + 1], dtp = part[3 * q + 2];
+  for (int o = 16; o > 0; o >>= 1) {
+    dta = fmin(dta, __shfl_xor_sync(0xffffffffu, dta, o));
+    dxmin = fmin(dxmin, __shfl_xor_sync(0xffffffffu, dxmin, o));
+    dtp = fmin(dtp, __shfl_xor_sync(0xffffffffu, dtp, o));
   }
+  if (l != 0) return;
   dta *= sf_adv;
   double difx = 0.25 * Re * (dxmin * dxmin);
   double dify = 0.25 * Re * (dy * dy);
@@ -678,19 +690,17 @@ int launch_decide_dt(eif_ctx *c) {
   unsigned long long *uymax = colmax + c->itot + 2;
   EIF_PROF(c, "decide_dt", 3);
   EIF_CK(c, cudaMemsetAsync(colmax, 0, sizeof(unsigned long long) * (c->itot + 3), c->stream));
-  int gy = (c->jtot + TY - 1) / TY;
-  const int gx = (c->itot + TX - 1) / TX;
-  const int target = c->sms * 8;
-  if (gx * gy > target) gy = (target + gx - 1) / gx;
-  if (gy < 1) gy = 1;
-  k_dt_colmax<<<dim3(gx, gy), dim3(TX, TY), 0, c->stream>>>(c->ux[c->cur], c->uy[c->cur], c->itot, c->jtot, c->ld,
+  const int gx = (c->itot / 2 + 1 + CM_THREADS - 1) / CM_THREADS;   // column pairs 0 .. itot/2
+  const int gy = std::max(1, std::min(c->jtot, (c->sms * 8 + gx - 1) / gx));
+  k_dt_colmax<<<dim3(gx, gy), CM_THREADS, 0, c->stream>>>(c->ux[c->cur], c->uy[c->cur], c->itot, c->jtot, c->ld,
                                                             colmax, uymax, c->d_flags);
   EIF_LAUNCH_CK(c);
   double *part = reinterpret_cast<double *>(uymax + 1);   // scratch: 3 * DT_BLOCKS words
   k_dt_partial<<<DT_BLOCKS, 64, 0, c->stream>>>(colmax, uymax, c->dxc, c->itot, c->dy, c->lx, c->dx, c->P, c->pcap,
                                                 c->np, part);
   EIF_LAUNCH_CK(c);
-  k_dt_final<<<1, 1, 0, c->stream>>>(part, DT_BLOCKS, c->dy, c->cfg.Re, c->cfg.safefactors[0], c->cfg.safefactors[1],
+  static_assert(DT_BLOCKS <= 32, "one warp combines the dt partials");
+  k_dt_final<<<1, 32, 0, c->stream>>>(part, DT_BLOCKS, c->dy, c->cfg.Re, c->cfg.safefactors[0], c->cfg.safefactors[1],
                                      c->cfg.safefactors[2], c->d_scal, c->d_coef);
   EIF_LAUNCH_CK(c);
   return EIF_OK;
