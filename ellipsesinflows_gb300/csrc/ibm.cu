@@ -143,6 +143,10 @@ struct BoxArgs {
   float *pf;                // PF_WORDS per particle, or null (double-precision form)
   int *box, *nchunk;
   const int *bd_off_base;   // start of the buffer nchunk points into
+  // inside the sub-iteration loop of a step graph: the loop's counter. In the first
+  // sub-iteration the increments are zero, the positions are X and the boxes built at
+  // X before the loop are still in place, so the box kernels return at once.
+  const unsigned *iter;
   Bounds bd;
 };
 
@@ -155,6 +159,7 @@ struct BoxArgs {
 // (mixed form only).
 constexpr int BOX_PARTS = 8;
 __global__ void __launch_bounds__(32) k_boxes(BoxArgs a) {
+  if (a.iter && *a.iter == 0u) return;
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   const int sub = blockIdx.y;
   const double *P = a.P;
@@ -232,7 +237,9 @@ __global__ void __launch_bounds__(32) k_boxes(BoxArgs a) {
 }
 
 // exclusive scan of the chunk counts (one block); off[np] = total
-__global__ void k_scan(const int *__restrict__ cnt, int *__restrict__ off, int np, Bounds bd) {
+__global__ void k_scan(const int *__restrict__ cnt, int *__restrict__ off, int np, Bounds bd,
+                       const unsigned *__restrict__ iter) {
+  if (iter && *iter == 0u) return;
   __shared__ int s[1024];
   __shared__ int carry;
   if (threadIdx.x == 0) carry = 0;
@@ -289,7 +296,8 @@ __device__ __forceinline__ bool row_task(int4 bm, int4 b0, int4 bp, int r, RowTa
 // load instead of a chain of dependent loads (owner, boxes, offsets). One warp
 // per particle.
 __global__ void k_task_table(const int *__restrict__ box, const int *__restrict__ off, int4 *__restrict__ tdesc,
-                             int np, Bounds bd, int cap) {
+                             int np, Bounds bd, int cap, const unsigned *__restrict__ iter) {
+  if (iter && *iter == 0u) return;
   const int n = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (n >= np) return;
@@ -312,7 +320,8 @@ constexpr int TT_WARPS = 8;
 constexpr int TT_MAX_NP = 8192;
 __global__ void __launch_bounds__(TT_WARPS * 32) k_task_table_scan(const int *__restrict__ box, const int *__restrict__ cnt,
                                                                   int *__restrict__ off, int4 *__restrict__ tdesc, int np,
-                                                                  Bounds bd, int cap) {
+                                                                  Bounds bd, int cap, const unsigned *__restrict__ iter) {
+  if (iter && *iter == 0u) return;
   __shared__ int red[TT_WARPS], wcnt[TT_WARPS];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int n0 = blockIdx.x * TT_WARPS;
@@ -1236,6 +1245,7 @@ static int launch_boxes(eif_ctx *c, bool use_increment) {
   b.dx = c->dx; b.dy = c->dy; b.ly = c->ly; b.yf1 = c->h_yf[0];
   b.box = c->box;
   b.pf = c->cfg.precision == EIF_PREC_MIXED ? c->pf : nullptr;
+  b.iter = c->in_loop ? reinterpret_cast<const unsigned *>(c->d_inc + 1) : nullptr;
   int *cnt = c->chunk_off + (c->np + 1);
   b.nchunk = cnt;
   EIF_PROF(c, "ibm_boxes", c->np <= TT_MAX_NP ? 2 : 3);
@@ -1244,13 +1254,13 @@ static int launch_boxes(eif_ctx *c, bool use_increment) {
   EIF_LAUNCH_CK(c);
   if (c->np <= TT_MAX_NP) {
     k_task_table_scan<<<(c->np + TT_WARPS - 1) / TT_WARPS, TT_WARPS * 32, 0, c->stream>>>(
-        c->box, cnt, c->chunk_off, c->tdesc, c->np, bounds_of(c), c->chunk_cap);
+        c->box, cnt, c->chunk_off, c->tdesc, c->np, bounds_of(c), c->chunk_cap, b.iter);
     EIF_LAUNCH_CK(c);
   } else {
-    k_scan<<<1, 1024, 0, c->stream>>>(cnt, c->chunk_off, c->np, bounds_of(c));
+    k_scan<<<1, 1024, 0, c->stream>>>(cnt, c->chunk_off, c->np, bounds_of(c), b.iter);
     EIF_LAUNCH_CK(c);
     k_task_table<<<(c->np * 32 + 255) / 256, 256, 0, c->stream>>>(c->box, c->chunk_off, c->tdesc, c->np,
-                                                                   bounds_of(c), c->chunk_cap);
+                                                                   bounds_of(c), c->chunk_cap, b.iter);
     EIF_LAUNCH_CK(c);
   }
   c->boxes_x_valid = x_only;
