@@ -819,12 +819,26 @@ __global__ void __launch_bounds__(256, 6) k_ibm_sum_f(WorkArgs a) {
   const int ld = a.ld;
   float2 *wb = reinterpret_cast<float2 *>(a.wbuf);
   const float *wcache = static_cast<const float *>(a.wcache);
-  // the next task's table entry is loaded while the current task is processed
+  // the next task's table entry and cached weights are loaded while the current task
+  // is processed, so that its field loads need not wait for them
   int4 nxt = make_int4(-1, 0, 0, 0);
-  if (warp < total && EIF_CHK(a.bd.rec, warp, a.bd.partial / 3, 71)) nxt = __ldg(a.tdesc + warp);
+  float nth0 = 0.f, nth1 = 0.f;
+  if (warp < total && EIF_CHK(a.bd.rec, warp, a.bd.partial / 3, 71) &&
+      EIF_CHK(a.bd.rec, (long long)warp * CHUNK + CHUNK - 1, 2 * a.bd.wbuf, 77)) {
+    nxt = __ldg(a.tdesc + warp);
+    nth0 = wcache[(size_t)warp * CHUNK + lane];
+    nth1 = wcache[(size_t)warp * CHUNK + 32 + lane];
+  }
   for (int c = warp; c < total; c += nwarps) {
     const int4 dsc = nxt;
-    if (c + nwarps < total && EIF_CHK(a.bd.rec, c + nwarps, a.bd.partial / 3, 71)) nxt = __ldg(a.tdesc + c + nwarps);
+    const float th_pre[2] = {nth0, nth1};
+    const int cn = c + nwarps;
+    if (cn < total && EIF_CHK(a.bd.rec, cn, a.bd.partial / 3, 71) &&
+        EIF_CHK(a.bd.rec, (long long)cn * CHUNK + CHUNK - 1, 2 * a.bd.wbuf, 77)) {
+      nxt = __ldg(a.tdesc + cn);
+      nth0 = wcache[(size_t)cn * CHUNK + lane];
+      nth1 = wcache[(size_t)cn * CHUNK + 32 + lane];
+    }
     const int n = dsc.x;
     if (!EIF_CHK(a.bd.rec, n, a.np, 72)) continue;
     RowTask t;
@@ -846,10 +860,10 @@ __global__ void __launch_bounds__(256, 6) k_ibm_sum_f(WorkArgs a) {
       bool in = task && i <= t.ie;
       if (in) {
         in = EIF_CHK(a.bd.rec, j * ld + i, a.bd.field, 74) && EIF_CHK(a.bd.rec, (j + 1) * ld + i, a.bd.field, 75) &&
-             EIF_CHK(a.bd.rec, j * ld + (i - 1), a.bd.field, 76) && EIF_CHK(a.bd.rec, slot, 2 * a.bd.wbuf, 77);
+             EIF_CHK(a.bd.rec, j * ld + (i - 1), a.bd.field, 76);
       }
       float2 contrib = make_float2(0.f, 0.f);
-      const float th = in ? wcache[slot] : 0.f;
+      const float th = in ? th_pre[half] : 0.f;
       // cells of weight exactly zero (inertia: far outside; exchange: any far cell) are skipped
       const bool live = in && (a.mode == 0 ? th != -1.f : fabsf(th) != 1.f);
       if (live) {
