@@ -1051,7 +1051,7 @@ struct GatherArgs {
 // band's ordered list that reach the tile's columns are compacted in order into
 // shared memory, then every cell sums their contributions in that order
 template <typename V2, typename Acc>
-__global__ void __launch_bounds__(GTHREADS, 4) k_gather(GatherArgs a) {
+__global__ void __launch_bounds__(GTHREADS, 6) k_gather(GatherArgs a) {
   const V2 *wbuf = static_cast<const V2 *>(a.wbuf);
   // compacted entries: columns, rows, row pitch and offset of the box in the scratch buffer
   __shared__ int e_i0[LMAX], e_i1[LMAX], e_j0[LMAX], e_j1[LMAX], e_w[LMAX], e_base[LMAX];
