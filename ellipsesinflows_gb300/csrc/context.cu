@@ -434,6 +434,8 @@ int eif_create(const eif_config_t *cfg, eif_ctx **out) {
   CK_CREATE(cudaMallocHost((void **)&c->h_flags, sizeof(unsigned)));
   *c->h_flags = 0u;
   CK_CREATE(cudaMallocHost((void **)&c->h_check, sizeof(unsigned long long) * 4));
+  CK_CREATE(cudaMallocHost((void **)&c->h_slots, sizeof(eif_ctx::StepSlot) * 2));
+  for (auto &e : c->ev_step) CK_CREATE(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   CK_CREATE(cudaMalloc((void **)&c->d_check, sizeof(unsigned long long) * 4));
   CK_CREATE(cudaMemset(c->d_check, 0, sizeof(unsigned long long) * 4));
   c->sync_debug = getenv("EIF_SYNC_DEBUG") != nullptr;
@@ -470,6 +472,9 @@ int eif_destroy(eif_ctx *c) {
   if (c->d_flags) cudaFree(c->d_flags);
   if (c->d_check) cudaFree(c->d_check);
   if (c->h_check) cudaFreeHost(c->h_check);
+  if (c->h_slots) cudaFreeHost(c->h_slots);
+  for (auto &e : c->ev_step)
+    if (e) cudaEventDestroy(e);
   if (c->h_scal) cudaFreeHost(c->h_scal);
   if (c->h_flags) cudaFreeHost(c->h_flags);
   poisson_free(c);
@@ -687,14 +692,50 @@ int eif_advance(eif_ctx *c, int nsteps) {
   if (!c || nsteps < 0) return EIF_ERR_ARG;
   if (!c->fluid_pushed) return fail(c, EIF_ERR_STATE, "push the fluid state before integrating");
   if (c->use_graphs && !c->sync_debug && !c->prof.enabled) {
-    // one graph launch and one synchronisation per step (see graph.cu)
+    // one graph launch per step (see graph.cu), queued one step ahead: step s + 1 is
+    // launched before the host waits for the copies of step s's dt, flags and bounds
+    // record, so the GPU does not idle between steps. After an error the state may
+    // include the step launched after the failing one.
+    auto finish = [&](int s) -> int {
+      eif_ctx::StepSlot &h = c->h_slots[s & 1];
+      EIF_CK(c, cudaEventSynchronize(c->ev_step[s & 1]));
+      for (int k = 0; k < 4; k++) c->h_scal[k] = h.scal[k];
+      c->dt_host = h.scal[0];
+      c->step += 1;
+      c->time += c->dt_host;
+      if (h.check[0] != 0ull) {
+        for (int k = 0; k < 4; k++) c->h_check[k] = h.check[k];
+        EIF_CK(c, cudaStreamSynchronize(c->stream));
+        EIF_CK(c, cudaMemsetAsync(c->d_check, 0, sizeof(unsigned long long) * 4, c->stream));
+        return fail(c, EIF_ERR_CUDA, "bounds guard %llu: index %llu outside [0, %llu)", h.check[1], h.check[2],
+                    h.check[3]);
+      }
+      if (h.flags != 0u) {
+        EIF_CK(c, cudaStreamSynchronize(c->stream));
+        *c->h_flags = h.flags;
+        return check_flags(c);
+      }
+      return EIF_OK;
+    };
     for (int s = 0; s < nsteps; s++) {
       int rc = step_graph_launch(c);
       if (rc) return rc;
-      rc = sync_scalars(c);
+      eif_ctx::StepSlot &h = c->h_slots[s & 1];
+      EIF_CK(c, cudaMemcpyAsync(h.scal, c->d_scal, sizeof(double) * 4, cudaMemcpyDeviceToHost, c->stream));
+      EIF_CK(c, cudaMemcpyAsync(&h.flags, c->d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+      if (c->d_check) {
+        EIF_CK(c, cudaMemcpyAsync(h.check, c->d_check, sizeof(unsigned long long) * 4, cudaMemcpyDeviceToHost,
+                                  c->stream));
+      } else {
+        h.check[0] = 0ull;
+      }
+      EIF_CK(c, cudaEventRecord(c->ev_step[s & 1], c->stream));
+      if (s > 0 && (rc = finish(s - 1))) return rc;
+    }
+    if (nsteps > 0) {
+      const int rc = finish(nsteps - 1);
       if (rc) return rc;
-      c->step += 1;
-      c->time += c->dt_host;
+      EIF_CK(c, cudaStreamSynchronize(c->stream));
     }
     return EIF_OK;
   }

@@ -172,6 +172,15 @@ struct eif_ctx {
   bool sync_debug;
   unsigned long long *d_check;  // bounds-guard record: flag, tag, index, bound
   unsigned long long *h_check;  // pinned mirror
+  // per-step copies of dt, the flags and the bounds record for graph steps queued one
+  // ahead (eif_advance): two pinned slots and the events that mark their copies
+  struct StepSlot {
+    double scal[4];
+    unsigned long long check[4];
+    unsigned flags;
+  };
+  StepSlot *h_slots = nullptr;
+  cudaEvent_t ev_step[2] = {nullptr, nullptr};
   eif::Profiler prof;
   char err[512];
 };
