@@ -102,17 +102,19 @@ int rk_stage_front(eif_ctx *c, int rk) {
   if ((rc = launch_reset_increments(c))) return rc;
   if (ibm && overlap_on(c)) {
     // side: inertia at X (reads the current velocity buffer, which the predictor
-    // does not write), the gather's band lists, and the collision forces at X
-    // (particle fields only); main: predictor, exchange, Poisson, projection
+    // does not write) and the collision forces at X (particle fields only); main:
+    // predictor, band lists, exchange, Poisson, projection
     SideScope side(c);
     if ((rc = side.begin())) return rc;
     if ((rc = launch_inertia(c, 0))) return rc;
-    if ((rc = launch_band_lists(c))) return rc;
     if ((rc = side.mark(c->ev_ibm))) return rc;
     if ((rc = launch_collision(c, 0))) return rc;
     if ((rc = side.end(c->ev_coll))) return rc;
     if ((rc = launch_predictor(c, rk))) return rc;
     if ((rc = join(c, c->ev_ibm))) return rc;
+    // the band lists after the join: the side stream's chain (boxes, inertia) is the
+    // longer of the two branches
+    if ((rc = launch_band_lists(c))) return rc;
     if ((rc = launch_exchange(c))) return rc;
     if ((rc = launch_potential(c, rk, ibm))) return rc;
     if ((rc = launch_correct(c, rk, ibm, true))) return rc;
