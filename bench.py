@@ -67,7 +67,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--no-fp64-leg", action="store_true")
-    ap.add_argument("--workload", default="mixed_target", choices=["mixed_target", "poiseuille", "couette_circle"])
+    ap.add_argument("--workload", default="mixed_target",
+                    choices=["mixed_target", "poiseuille", "couette_circle", "batch_c5"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
@@ -239,6 +240,59 @@ def run_ours(args, world, rank, local, pg):
     return out, rank
 
 
+def run_batch(args, world, rank, local, pg):
+    """64 independent suspensions of uneven sizes (cases.batch_c5) advanced by one
+    step graph per step (eif_batch_*): aggregate cell-steps/s, against the same
+    suspensions advanced one after another with eif_advance."""
+    import torch
+    from ellipsesinflows_gb300 import PREC_FP64, PREC_MIXED, Batch, Simulation, build, cases
+    build.build()
+    torch.cuda.set_device(local)
+    cs = cases.batch_c5()
+    prec = PREC_MIXED if args.precision == "mixed" else PREC_FP64
+    sims = [Simulation.from_case(c, precision=prec, device=local) for c in cs]
+    cells = sum(c.cells for c in cs)
+    batch = Batch(sims)
+    stream = torch.cuda.ExternalStream(batch.stream(), device=local)
+    batch.advance(args.warmup)
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier(pg, local)
+        torch.cuda.synchronize()
+        start.record(stream)
+        batch.advance(args.steps)
+        stop.record(stream)
+        torch.cuda.synchronize()
+        barrier(pg, local)
+    ms = max_over_ranks(pg, start.elapsed_time(stop), local)
+    # the same suspensions one after another (one graph launch per suspension and step)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for s in sims:
+            s.advance(1)
+    torch.cuda.synchronize()
+    sep_ms = (time.perf_counter() - t0) * 1e3
+    batch.close()
+    grids = sorted({"%dx%d" % (c.itot, c.jtot) for c in cs})
+    out = {
+        "metric": "cell-steps/s", "value": world * cells * args.steps / (ms / 1e3), "unit": "cell-steps/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if prec == PREC_FP64 else "f32+f64",
+        "data": "synthetic (seeded ellipse placement, fluid at rest)",
+        "config": {"workload": "batch_c5_%d" % len(cs), "suspensions": len(cs), "grids": grids,
+                   "total_cells": cells, "n_particles_total": int(sum(c.n_particles for c in cs)),
+                   "precision": args.precision, "l2": "inputs larger than L2 (~%d MB of device state)" % (cells * 13 * 8 // 10**6),
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "separate": {"value": cells * args.steps / (sep_ms / 1e3), "unit": "cell-steps/s",
+                     "ms_per_step": sep_ms / args.steps,
+                     "how": "the same suspensions advanced one after another with eif_advance, host-timed"},
+        "e2e": None, "roofline": None, "clocks": clk.summary(),
+    }
+    return out, rank
+
+
 def fp64_leg(args, case, mixed_sim, device, pg, world):
     """The plain double-precision form on the same workload and step count, and the
     error of the mixed-precision state against it after the same number of steps."""
@@ -387,6 +441,8 @@ def main():
     world, rank, local, pg = dist_init(args.gpus)
     if args.impl == "reference":
         out, rank = run_reference(args, world, rank)
+    elif args.workload == "batch_c5":
+        out, rank = run_batch(args, world, rank, local, pg)
     else:
         out, rank = run_ours(args, world, rank, local, pg)
     if rank == 0 and out is not None:

@@ -12,7 +12,7 @@ import ctypes
 import os
 
 from . import capi
-from .capi import (EifError, F, FIELDS, NFIELDS, PREC_FP64, PREC_MIXED,  # noqa: F401
+from .capi import (Batch, EifError, F, FIELDS, NFIELDS, PREC_FP64, PREC_MIXED,  # noqa: F401
                    make_config)
 
 PKG = os.path.dirname(os.path.abspath(__file__))

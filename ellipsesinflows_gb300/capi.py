@@ -114,6 +114,25 @@ def bind(lib, prefix):
         if fn is not None:
             fn.argtypes = args
             fn.restype = ctypes.c_int
+    bsigs = {
+        "batch_create": [ctypes.POINTER(_vp), ctypes.c_int, ctypes.POINTER(_vp)],
+        "batch_advance": [_vp, ctypes.c_int],
+        "batch_size": [_vp],
+        "batch_destroy": [_vp],
+    }
+    for name, args in bsigs.items():
+        fn = getattr(lib, prefix + name, None)
+        if fn is not None:
+            fn.argtypes = args
+            fn.restype = ctypes.c_int
+    bst = getattr(lib, prefix + "batch_stream", None)
+    if bst is not None:
+        bst.argtypes = [_vp]
+        bst.restype = _vp
+    ble = getattr(lib, prefix + "batch_last_error", None)
+    if ble is not None:
+        ble.argtypes = [_vp]
+        ble.restype = ctypes.c_char_p
     le = getattr(lib, prefix + "last_error")
     le.argtypes = [_vp]
     le.restype = ctypes.c_char_p
@@ -324,3 +343,50 @@ class Solver:
 
     def update_particles(self):
         self._call("update_particles", self.ctx)
+
+
+class Batch:
+    """Several suspensions (Solver objects on one device) advanced together, one CUDA
+    graph launch per step (eif_batch_* in include/eif.h). The solvers stay usable on
+    their own; close the batch before them."""
+
+    def __init__(self, solvers):
+        if not solvers:
+            raise ValueError("a batch needs at least one suspension")
+        self.solvers = list(solvers)
+        self.lib, self.prefix = self.solvers[0].lib, self.solvers[0].prefix
+        arr = (_vp * len(self.solvers))(*[s.ctx for s in self.solvers])
+        self.handle = _vp()
+        rc = getattr(self.lib, self.prefix + "batch_create")(arr, len(self.solvers), ctypes.byref(self.handle))
+        if rc != 0:
+            raise EifError(rc, "batch_create")
+
+    def advance(self, nsteps=1):
+        rc = getattr(self.lib, self.prefix + "batch_advance")(self.handle, nsteps)
+        if rc != 0:
+            msg = getattr(self.lib, self.prefix + "batch_last_error")(self.handle) or b""
+            raise EifError(rc, msg.decode(errors="replace"))
+
+    def cells(self):
+        return sum(s.itot * s.jtot for s in self.solvers)
+
+    def stream(self):
+        """The cudaStream_t (as an integer) the batch's step graphs run on."""
+        return getattr(self.lib, self.prefix + "batch_stream")(self.handle)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            getattr(self.lib, self.prefix + "batch_destroy")(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

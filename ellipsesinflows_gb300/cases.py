@@ -166,6 +166,31 @@ def contact_cluster(itot=64, jtot=128, seed=7):
                 steps=20)
 
 
+def batch_c5(count=64, seed=3, n_max=128, steps=300):
+    """Many independent suspensions of uneven sizes: grids drawn from 128x256, 256x512,
+    384x768 and 512x1024; ellipse counts proportional to the cell count (4 .. n_max,
+    n_max = 128 keeps the bounding discs of a = 0.04 below 35 % of the area, where
+    random sequential placement still succeeds); a = 0.04, aspect ratio U[1, 2.5],
+    Re U[100, 400], Poiseuille forcing 8/Re, fluid at rest."""
+    rng = np.random.default_rng(seed)
+    grids = [(128, 256), (256, 512), (384, 768), (512, 1024)]
+    max_cells = 512 * 1024
+    out = []
+    for k in range(count):
+        itot, jtot = grids[int(rng.integers(len(grids)))]
+        n = int(round(4 + (n_max - 4) * (itot * jtot) / max_cells))
+        a = 0.04
+        ar = rng.uniform(1.0, 2.5, n)
+        Re = float(rng.uniform(100.0, 400.0))
+        dx = 1.0 / itot
+        xs, ys = place(n, a, 2.0, dx, rng, dx)
+        az = rng.uniform(0.0, math.pi, n)
+        rec = particle_records(np.ones(n), np.full(n, a), a / ar, xs, ys, az)
+        out.append(Case("batch%02d_%dx%d_n%d" % (k, itot, jtot, n), itot, jtot, 2.0, Re, extfrcy=8.0 / Re,
+                        particles=rec, steps=steps))
+    return out
+
+
 CONFIGS = {
     "couette_circle": couette_circle,
     "poiseuille": poiseuille,

@@ -1,0 +1,195 @@
+// Batches of independent suspensions advanced by one CUDA graph per step.
+//
+// A batch groups existing contexts (any grid sizes, particle counts and both
+// precisions). Its step graph holds one branch per context, each the context's own
+// step (capture_step in graph.cu: dt, three RK stages with their device-driven
+// sub-iteration loops, the particle updates); the branches have no dependences on
+// one another, so the kernels of small suspensions run side by side and fill the
+// GPU. One graph launch advances every suspension by one step. The kernels, their
+// order within a suspension and the data they touch are those of eif_advance, so
+// every suspension gets the same bits as when advanced alone.
+//
+// The branches swap double buffers, so a batch graph is tied to the buffer indices
+// of all its contexts at the start of a step; two graphs are kept (the indices
+// alternate with period one or two steps). A context whose buffers are
+// reallocated (a push with another particle count) makes the batch rebuild.
+#include "eif_internal.cuh"
+#include <string>
+#include <vector>
+
+struct eif_batch {
+  std::vector<eif_ctx *> ctx;
+  struct Graph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<int> cur0, scur0, cur1, scur1;
+    std::vector<unsigned> gen;
+  } graphs[2];
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev = nullptr;
+  std::string err;
+};
+
+namespace {
+
+int batch_fail(eif_batch *b, int code, const std::string &msg) {
+  b->err = msg;
+  return code;
+}
+
+void free_graph(eif_batch::Graph &g) {
+  if (g.exec) cudaGraphExecDestroy(g.exec);
+  if (g.graph) cudaGraphDestroy(g.graph);
+  g = eif_batch::Graph{};
+}
+
+bool matches(const eif_batch *b, const eif_batch::Graph &g) {
+  if (!g.exec) return false;
+  for (size_t i = 0; i < b->ctx.size(); i++) {
+    const eif_ctx *c = b->ctx[i];
+    if (g.cur0[i] != c->cur || g.scur0[i] != c->scur || g.gen[i] != c->buf_gen) return false;
+  }
+  return true;
+}
+
+int build(eif_batch *b, eif_batch::Graph &out) {
+  eif_batch::Graph g;
+  cudaError_t e = cudaGraphCreate(&g.graph, 0);
+  if (e != cudaSuccess) return batch_fail(b, EIF_ERR_CUDA, std::string("cudaGraphCreate: ") + cudaGetErrorString(e));
+  for (size_t i = 0; i < b->ctx.size(); i++) {
+    eif_ctx *c = b->ctx[i];
+    int cur1 = 0, scur1 = 0;
+    g.cur0.push_back(c->cur);
+    g.scur0.push_back(c->scur);
+    g.gen.push_back(c->buf_gen);
+    const int rc = eif::capture_step(c, g.graph, &cur1, &scur1);
+    if (rc) {
+      free_graph(g);
+      return batch_fail(b, rc, "suspension " + std::to_string(i) + ": " + eif_last_error(c));
+    }
+    g.cur1.push_back(cur1);
+    g.scur1.push_back(scur1);
+  }
+  e = cudaGraphInstantiate(&g.exec, g.graph, 0);
+  if (e != cudaSuccess) {
+    free_graph(g);
+    return batch_fail(b, EIF_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+  }
+  free_graph(out);
+  out = g;
+  return EIF_OK;
+}
+
+// reads dt, the flags and the bounds record of every suspension after a step
+int finish_step(eif_batch *b, const eif_batch::Graph &g) {
+  cudaError_t e = cudaStreamSynchronize(b->stream);
+  if (e != cudaSuccess) return batch_fail(b, EIF_ERR_CUDA, std::string("batch step: ") + cudaGetErrorString(e));
+  int first_rc = EIF_OK;
+  for (size_t i = 0; i < b->ctx.size(); i++) {
+    eif_ctx *c = b->ctx[i];
+    const eif_ctx::StepSlot &h = c->h_slots[0];
+    c->cur = g.cur1[i];
+    c->scur = g.scur1[i];
+    for (int k = 0; k < 4; k++) c->h_scal[k] = h.scal[k];
+    c->dt_host = h.scal[0];
+    c->step += 1;
+    c->time += c->dt_host;
+    int rc = EIF_OK;
+    if (h.check[0] != 0ull) {
+      cudaMemset(c->d_check, 0, sizeof(unsigned long long) * 4);
+      rc = eif::fail(c, EIF_ERR_CUDA, "bounds guard %llu: index %llu outside [0, %llu)", h.check[1], h.check[2],
+                     h.check[3]);
+    } else if (h.flags != 0u) {
+      *c->h_flags = h.flags;
+      rc = eif::check_flags(c);
+    }
+    if (rc && first_rc == EIF_OK) {
+      first_rc = batch_fail(b, rc, "suspension " + std::to_string(i) + ": " + eif_last_error(c));
+    }
+  }
+  return first_rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+int eif_batch_create(eif_ctx *const *ctxs, int n, eif_batch **out) {
+  if (!ctxs || n <= 0 || !out) return EIF_ERR_ARG;
+  for (int i = 0; i < n; i++) {
+    if (!ctxs[i]) return EIF_ERR_ARG;
+    if (ctxs[i]->device != ctxs[0]->device) return EIF_ERR_ARG;
+    for (int k = 0; k < i; k++)
+      if (ctxs[k] == ctxs[i]) return EIF_ERR_ARG;
+  }
+  eif_batch *b = new (std::nothrow) eif_batch;
+  if (!b) return EIF_ERR_NOMEM;
+  b->ctx.assign(ctxs, ctxs + n);
+  if (cudaSetDevice(ctxs[0]->device) != cudaSuccess || cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->ev, cudaEventDisableTiming) != cudaSuccess) {
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return EIF_ERR_CUDA;
+  }
+  *out = b;
+  return EIF_OK;
+}
+
+int eif_batch_destroy(eif_batch *b) {
+  if (!b) return EIF_ERR_ARG;
+  cudaStreamSynchronize(b->stream);
+  for (auto &g : b->graphs) free_graph(g);
+  if (b->ev) cudaEventDestroy(b->ev);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+  return EIF_OK;
+}
+
+const char *eif_batch_last_error(const eif_batch *b) { return b ? b->err.c_str() : "null batch"; }
+
+int eif_batch_size(const eif_batch *b) { return b ? (int)b->ctx.size() : 0; }
+
+void *eif_batch_stream(eif_batch *b) { return b ? (void *)b->stream : nullptr; }
+
+int eif_batch_advance(eif_batch *b, int nsteps) {
+  if (!b || nsteps < 0) return EIF_ERR_ARG;
+  for (size_t i = 0; i < b->ctx.size(); i++) {
+    eif_ctx *c = b->ctx[i];
+    if (!c->fluid_pushed) return batch_fail(b, EIF_ERR_STATE, "suspension " + std::to_string(i) + ": push the fluid state first");
+  }
+  if (cudaSetDevice(b->ctx[0]->device) != cudaSuccess) return batch_fail(b, EIF_ERR_CUDA, "cudaSetDevice");
+  for (int s = 0; s < nsteps; s++) {
+    eif_batch::Graph *g = nullptr;
+    for (auto &cand : b->graphs)
+      if (matches(b, cand)) g = &cand;
+    if (!g) {
+      eif_batch::Graph *slot = !b->graphs[0].exec ? &b->graphs[0] : (!b->graphs[1].exec ? &b->graphs[1] : &b->graphs[0]);
+      if (b->graphs[0].exec && b->graphs[1].exec) {
+        free_graph(b->graphs[0]);
+        free_graph(b->graphs[1]);
+      }
+      const int rc = build(b, *slot);
+      if (rc) return rc;
+      g = slot;
+    }
+    // the step follows whatever the suspensions' own streams hold (pushes, stage calls)
+    for (eif_ctx *c : b->ctx) {
+      if (cudaEventRecord(b->ev, c->stream) != cudaSuccess || cudaStreamWaitEvent(b->stream, b->ev, 0) != cudaSuccess)
+        return batch_fail(b, EIF_ERR_CUDA, "ordering after the suspensions' streams");
+    }
+    cudaError_t e = cudaGraphLaunch(g->exec, b->stream);
+    if (e != cudaSuccess) return batch_fail(b, EIF_ERR_CUDA, std::string("cudaGraphLaunch: ") + cudaGetErrorString(e));
+    for (eif_ctx *c : b->ctx) {
+      eif_ctx::StepSlot &h = c->h_slots[0];
+      e = cudaMemcpyAsync(h.scal, c->d_scal, sizeof(double) * 4, cudaMemcpyDeviceToHost, b->stream);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(&h.flags, c->d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost, b->stream);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(h.check, c->d_check, sizeof(unsigned long long) * 4, cudaMemcpyDeviceToHost, b->stream);
+      if (e != cudaSuccess) return batch_fail(b, EIF_ERR_CUDA, std::string("batch scalars: ") + cudaGetErrorString(e));
+    }
+    const int rc = finish_step(b, *g);
+    if (rc) return rc;
+  }
+  return EIF_OK;
+}
+
+}  // extern "C"

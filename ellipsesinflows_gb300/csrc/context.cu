@@ -314,6 +314,9 @@ int device_metrics(eif_ctx *c) {
   return EIF_OK;
 }
 
+}  // namespace
+
+namespace eif {
 int check_flags(eif_ctx *c) {
   // called after a synchronisation; reports and clears kernel error flags
   unsigned f = *c->h_flags;
@@ -325,6 +328,9 @@ int check_flags(eif_ctx *c) {
     return fail(c, EIF_ERR_NOCONV, "an iteration cap or a device list capacity was reached on the device");
   return EIF_OK;
 }
+}  // namespace eif
+
+namespace {
 
 // copy the scalars and flags to the host and wait
 int sync_scalars(eif_ctx *c) {
@@ -537,6 +543,7 @@ int eif_push_particles(eif_ctx *c, int n, const double *rec) {
   const bool reuse = c->P && n == c->np && n <= c->pcap && (n == 0 || (c->box && chunks <= (size_t)c->chunk_cap));
   if (!reuse) {
     graphs_free(c);
+    c->buf_gen++;
     int rc = ensure_pcap(c, n);
     if (rc) return rc;
   }

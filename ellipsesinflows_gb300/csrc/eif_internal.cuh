@@ -133,6 +133,7 @@ struct eif_ctx {
     int cur0 = -1, scur0 = -1, cur1 = 0, scur1 = 0;
   } graphs[2];
   bool use_graphs = true;
+  unsigned buf_gen = 0;         // bumped when device buffers are reallocated (batch graphs hold them)
   bool incr_zero = false;       // the particle increments are zero (after a reset)
   bool boxes_x_valid = false;   // the IBM boxes hold the positions X (see launch_boxes)
   bool weights_x_valid = false; // wcache holds the indicator weights of those boxes
@@ -201,12 +202,14 @@ int check_records(eif_ctx *c);
 // ---- step graphs (graph.cu) ----
 int step_graph_launch(eif_ctx *c);
 void graphs_free(eif_ctx *c);
+int capture_step(eif_ctx *c, cudaGraph_t g, int *cur1, int *scur1);
 int rk_stage_front(eif_ctx *c, int rk);
 int ibm_prepare(eif_ctx *c);
 void profile_free(eif_ctx *c);
 
 // ---- launch helpers ----
 int fail(eif_ctx *c, int code, const char *fmt, ...);
+int check_flags(eif_ctx *c);   // after a synchronisation: reports and clears the kernel error flags
 int check_cuda(eif_ctx *c, cudaError_t e, const char *what);
 #define EIF_CK(c, call) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) return eif::check_cuda((c), e_, #call); } while (0)
 // After a launch: report launch errors; with EIF_SYNC_DEBUG set in the

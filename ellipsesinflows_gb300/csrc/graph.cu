@@ -53,7 +53,13 @@ void abort_capture(eif_ctx *c) {
   c->in_loop = false;
 }
 
-int build(eif_ctx *c, eif_ctx::StepGraph &sg) {
+}  // namespace
+
+// Captures one time step of c into g (appended as an independent branch: its first
+// nodes have no dependences) and returns the buffer indices the step ends with. The
+// host state of c is left as before the capture; on failure g may hold a partial
+// branch and should be discarded.
+int capture_step(eif_ctx *c, cudaGraph_t g, int *cur1, int *scur1) {
   int rc = ibm_prepare(c);
   if (rc) return rc;
   const int cur0 = c->cur, scur0 = c->scur;
@@ -61,15 +67,12 @@ int build(eif_ctx *c, eif_ctx::StepGraph &sg) {
   c->boxes_x_valid = false;
   c->weights_x_valid = false;
   c->incr_zero = false;
-  cudaGraph_t g = nullptr;
-  EIF_CK(c, cudaGraphCreate(&g, 0));
   auto fail_out = [&](int code) {
     abort_capture(c);
     c->cur = cur0;
     c->scur = scur0;
     c->boxes_x_valid = false;
     c->weights_x_valid = false;
-    cudaGraphDestroy(g);
     return code;
   };
   std::vector<cudaGraphNode_t> sinks;
@@ -109,26 +112,40 @@ int build(eif_ctx *c, eif_ctx::StepGraph &sg) {
     if ((rc = launch_update_particles(c))) return fail_out(rc);
   }
   if ((rc = end_capture(c, nullptr))) return fail_out(rc);
-  cudaGraphExec_t exec = nullptr;
-  e = cudaGraphInstantiate(&exec, g, 0);
-  if (e != cudaSuccess) {
-    c->cur = cur0;
-    c->scur = scur0;
-    cudaGraphDestroy(g);
-    return check_cuda(c, e, "cudaGraphInstantiate");
-  }
-  sg.graph = g;
-  sg.exec = exec;
-  sg.cur0 = cur0;
-  sg.scur0 = scur0;
-  sg.cur1 = c->cur;
-  sg.scur1 = c->scur;
+  *cur1 = c->cur;
+  *scur1 = c->scur;
   // nothing has run yet: the step starts from the original buffers; the step ends
   // with new positions, so no boxes are valid after it
   c->cur = cur0;
   c->scur = scur0;
   c->boxes_x_valid = false;
   c->weights_x_valid = false;
+  return EIF_OK;
+}
+
+namespace {
+
+int build(eif_ctx *c, eif_ctx::StepGraph &sg) {
+  cudaGraph_t g = nullptr;
+  EIF_CK(c, cudaGraphCreate(&g, 0));
+  int cur1 = 0, scur1 = 0;
+  int rc = capture_step(c, g, &cur1, &scur1);
+  if (rc) {
+    cudaGraphDestroy(g);
+    return rc;
+  }
+  cudaGraphExec_t exec = nullptr;
+  const cudaError_t e = cudaGraphInstantiate(&exec, g, 0);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return check_cuda(c, e, "cudaGraphInstantiate");
+  }
+  sg.graph = g;
+  sg.exec = exec;
+  sg.cur0 = c->cur;
+  sg.scur0 = c->scur;
+  sg.cur1 = cur1;
+  sg.scur1 = scur1;
   return EIF_OK;
 }
 

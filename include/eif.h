@@ -117,6 +117,24 @@ int eif_advance(eif_ctx *ctx, int nsteps);
 int eif_get_time(eif_ctx *ctx, int *step, double *time);
 int eif_set_time(eif_ctx *ctx, int step, double time);
 
+/* ---- batches of independent suspensions (no counterpart in the reference,
+ * which runs one suspension per process) ----
+ * A batch groups n existing contexts on one device (any grid sizes, particle
+ * counts and precisions, each pushed as usual). eif_batch_advance moves every
+ * suspension nsteps steps with one CUDA graph launch per step; each suspension
+ * gets the same bits as with eif_advance on its own context, and its step
+ * counter and time advance likewise. The batch does not own the contexts:
+ * destroy it before them. On an error the message names the suspension
+ * (eif_batch_last_error); that context's eif_last_error has the detail. */
+typedef struct eif_batch eif_batch;
+int eif_batch_create(eif_ctx *const *ctxs, int n, eif_batch **batch);
+int eif_batch_advance(eif_batch *batch, int nsteps);
+int eif_batch_size(const eif_batch *batch);
+/* the stream the batch's step graphs are launched on (a cudaStream_t) */
+void *eif_batch_stream(eif_batch *batch);
+const char *eif_batch_last_error(const eif_batch *batch);
+int eif_batch_destroy(eif_batch *batch);
+
 /* ---- stage-level entry points, one per reference function ---- */
 int eif_update_boundaries(eif_ctx *ctx);                              /* src/fluid/boundary_conditions.c:7-62 */
 int eif_reset_particle_increments(eif_ctx *ctx);                      /* src/suspensions/reset.c:7-18 */
