@@ -14,6 +14,7 @@
 // alternate with period one or two steps). A context whose buffers are
 // reallocated (a push with another particle count) makes the batch rebuild.
 #include "eif_internal.cuh"
+#include <cstring>
 #include <string>
 #include <vector>
 
@@ -27,10 +28,30 @@ struct eif_batch {
   } graphs[2];
   cudaStream_t stream = nullptr;
   cudaEvent_t ev = nullptr;
+  cudaEvent_t ev_step[2] = {nullptr, nullptr};
+  // per suspension: device addresses of dt (scal), flags and bounds record, gathered
+  // after every step into one packed buffer and copied to the host in one transfer
+  const void **d_src = nullptr;
+  unsigned long long *d_pack = nullptr, *h_pack[2] = {nullptr, nullptr};
   std::string err;
 };
 
+// words per suspension in the packed scalars: scal[4], check[4], flags
+constexpr int PACK_WORDS = 9;
+
 namespace {
+
+__global__ void k_pack_scalars(const void *const *__restrict__ src, unsigned long long *__restrict__ pack, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const unsigned long long *scal = static_cast<const unsigned long long *>(src[3 * i]);
+  const unsigned long long *check = static_cast<const unsigned long long *>(src[3 * i + 2]);
+  const unsigned *flags = static_cast<const unsigned *>(src[3 * i + 1]);
+  unsigned long long *o = pack + (size_t)PACK_WORDS * i;
+  for (int k = 0; k < 4; k++) o[k] = scal[k];
+  for (int k = 0; k < 4; k++) o[4 + k] = check ? check[k] : 0ull;
+  o[8] = *flags;
+}
 
 int batch_fail(eif_batch *b, int code, const std::string &msg) {
   b->err = msg;
@@ -80,27 +101,27 @@ int build(eif_batch *b, eif_batch::Graph &out) {
   return EIF_OK;
 }
 
-// reads dt, the flags and the bounds record of every suspension after a step
-int finish_step(eif_batch *b, const eif_batch::Graph &g) {
-  cudaError_t e = cudaStreamSynchronize(b->stream);
+// reads dt, the flags and the bounds record of every suspension after step s
+int finish_step(eif_batch *b, int s) {
+  cudaError_t e = cudaEventSynchronize(b->ev_step[s & 1]);
   if (e != cudaSuccess) return batch_fail(b, EIF_ERR_CUDA, std::string("batch step: ") + cudaGetErrorString(e));
+  const unsigned long long *pk = b->h_pack[s & 1];
   int first_rc = EIF_OK;
   for (size_t i = 0; i < b->ctx.size(); i++) {
     eif_ctx *c = b->ctx[i];
-    const eif_ctx::StepSlot &h = c->h_slots[0];
-    c->cur = g.cur1[i];
-    c->scur = g.scur1[i];
-    for (int k = 0; k < 4; k++) c->h_scal[k] = h.scal[k];
-    c->dt_host = h.scal[0];
+    const unsigned long long *w = pk + (size_t)PACK_WORDS * i;
+    std::memcpy(c->h_scal, w, sizeof(double) * 4);
+    c->dt_host = c->h_scal[0];
     c->step += 1;
     c->time += c->dt_host;
     int rc = EIF_OK;
-    if (h.check[0] != 0ull) {
+    if (w[4] != 0ull) {
+      cudaStreamSynchronize(b->stream);
       cudaMemset(c->d_check, 0, sizeof(unsigned long long) * 4);
-      rc = eif::fail(c, EIF_ERR_CUDA, "bounds guard %llu: index %llu outside [0, %llu)", h.check[1], h.check[2],
-                     h.check[3]);
-    } else if (h.flags != 0u) {
-      *c->h_flags = h.flags;
+      rc = eif::fail(c, EIF_ERR_CUDA, "bounds guard %llu: index %llu outside [0, %llu)", w[5], w[6], w[7]);
+    } else if (w[8] != 0ull) {
+      cudaStreamSynchronize(b->stream);
+      *c->h_flags = (unsigned)w[8];
       rc = eif::check_flags(c);
     }
     if (rc && first_rc == EIF_OK) {
@@ -125,10 +146,24 @@ int eif_batch_create(eif_ctx *const *ctxs, int n, eif_batch **out) {
   eif_batch *b = new (std::nothrow) eif_batch;
   if (!b) return EIF_ERR_NOMEM;
   b->ctx.assign(ctxs, ctxs + n);
-  if (cudaSetDevice(ctxs[0]->device) != cudaSuccess || cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaEventCreateWithFlags(&b->ev, cudaEventDisableTiming) != cudaSuccess) {
-    if (b->stream) cudaStreamDestroy(b->stream);
-    delete b;
+  std::vector<const void *> src;
+  for (int i = 0; i < n; i++) {
+    src.push_back(ctxs[i]->d_scal);
+    src.push_back(ctxs[i]->d_flags);
+    src.push_back(ctxs[i]->d_check);
+  }
+  bool ok = cudaSetDevice(ctxs[0]->device) == cudaSuccess &&
+            cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaEventCreateWithFlags(&b->ev, cudaEventDisableTiming) == cudaSuccess &&
+            cudaEventCreateWithFlags(&b->ev_step[0], cudaEventDisableTiming) == cudaSuccess &&
+            cudaEventCreateWithFlags(&b->ev_step[1], cudaEventDisableTiming) == cudaSuccess &&
+            cudaMalloc((void **)&b->d_src, sizeof(void *) * src.size()) == cudaSuccess &&
+            cudaMemcpy(b->d_src, src.data(), sizeof(void *) * src.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
+            cudaMalloc((void **)&b->d_pack, sizeof(unsigned long long) * PACK_WORDS * n) == cudaSuccess &&
+            cudaMallocHost((void **)&b->h_pack[0], sizeof(unsigned long long) * PACK_WORDS * n) == cudaSuccess &&
+            cudaMallocHost((void **)&b->h_pack[1], sizeof(unsigned long long) * PACK_WORDS * n) == cudaSuccess;
+  if (!ok) {
+    eif_batch_destroy(b);
     return EIF_ERR_CUDA;
   }
   *out = b;
@@ -137,9 +172,15 @@ int eif_batch_create(eif_ctx *const *ctxs, int n, eif_batch **out) {
 
 int eif_batch_destroy(eif_batch *b) {
   if (!b) return EIF_ERR_ARG;
-  cudaStreamSynchronize(b->stream);
+  if (b->stream) cudaStreamSynchronize(b->stream);
   for (auto &g : b->graphs) free_graph(g);
   if (b->ev) cudaEventDestroy(b->ev);
+  for (auto &e : b->ev_step)
+    if (e) cudaEventDestroy(e);
+  if (b->d_src) cudaFree(b->d_src);
+  if (b->d_pack) cudaFree(b->d_pack);
+  for (auto &h : b->h_pack)
+    if (h) cudaFreeHost(h);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
   return EIF_OK;
@@ -158,11 +199,15 @@ int eif_batch_advance(eif_batch *b, int nsteps) {
     if (!c->fluid_pushed) return batch_fail(b, EIF_ERR_STATE, "suspension " + std::to_string(i) + ": push the fluid state first");
   }
   if (cudaSetDevice(b->ctx[0]->device) != cudaSuccess) return batch_fail(b, EIF_ERR_CUDA, "cudaSetDevice");
+  // steps are queued one ahead of the host's read of the previous step's scalars
   for (int s = 0; s < nsteps; s++) {
     eif_batch::Graph *g = nullptr;
     for (auto &cand : b->graphs)
       if (matches(b, cand)) g = &cand;
     if (!g) {
+      // a rebuild captures every suspension again: let the queued step finish first
+      cudaError_t e = cudaStreamSynchronize(b->stream);
+      if (e != cudaSuccess) return batch_fail(b, EIF_ERR_CUDA, std::string("batch step: ") + cudaGetErrorString(e));
       eif_batch::Graph *slot = !b->graphs[0].exec ? &b->graphs[0] : (!b->graphs[1].exec ? &b->graphs[1] : &b->graphs[0]);
       if (b->graphs[0].exec && b->graphs[1].exec) {
         free_graph(b->graphs[0]);
@@ -179,16 +224,27 @@ int eif_batch_advance(eif_batch *b, int nsteps) {
     }
     cudaError_t e = cudaGraphLaunch(g->exec, b->stream);
     if (e != cudaSuccess) return batch_fail(b, EIF_ERR_CUDA, std::string("cudaGraphLaunch: ") + cudaGetErrorString(e));
-    for (eif_ctx *c : b->ctx) {
-      eif_ctx::StepSlot &h = c->h_slots[0];
-      e = cudaMemcpyAsync(h.scal, c->d_scal, sizeof(double) * 4, cudaMemcpyDeviceToHost, b->stream);
-      if (e == cudaSuccess) e = cudaMemcpyAsync(&h.flags, c->d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost, b->stream);
-      if (e == cudaSuccess) e = cudaMemcpyAsync(h.check, c->d_check, sizeof(unsigned long long) * 4, cudaMemcpyDeviceToHost, b->stream);
-      if (e != cudaSuccess) return batch_fail(b, EIF_ERR_CUDA, std::string("batch scalars: ") + cudaGetErrorString(e));
+    for (size_t i = 0; i < b->ctx.size(); i++) {
+      b->ctx[i]->cur = g->cur1[i];
+      b->ctx[i]->scur = g->scur1[i];
     }
-    const int rc = finish_step(b, *g);
+    const int n = (int)b->ctx.size();
+    k_pack_scalars<<<(n + 63) / 64, 64, 0, b->stream>>>(b->d_src, b->d_pack, n);
+    e = cudaMemcpyAsync(b->h_pack[s & 1], b->d_pack, sizeof(unsigned long long) * PACK_WORDS * n,
+                        cudaMemcpyDeviceToHost, b->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(b->ev_step[s & 1], b->stream);
+    if (e != cudaSuccess) return batch_fail(b, EIF_ERR_CUDA, std::string("batch scalars: ") + cudaGetErrorString(e));
+    if (s > 0) {
+      const int rc = finish_step(b, s - 1);
+      if (rc) return rc;
+    }
+  }
+  if (nsteps > 0) {
+    const int rc = finish_step(b, nsteps - 1);
     if (rc) return rc;
   }
+  const cudaError_t e = cudaStreamSynchronize(b->stream);
+  if (e != cudaSuccess) return batch_fail(b, EIF_ERR_CUDA, std::string("batch step: ") + cudaGetErrorString(e));
   return EIF_OK;
 }
 
