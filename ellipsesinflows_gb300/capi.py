@@ -108,6 +108,13 @@ def bind(lib, prefix):
         "update_particles": [_vp],
         "divergence": [_vp, _dp, _dp],
         "set_threads": [_vp, ctypes.c_int],
+        "adjoint_begin": [_vp, ctypes.c_int],
+        "adjoint_forward": [_vp, ctypes.c_int],
+        "adjoint_seed": [_vp, _dp, _dp, _dp],
+        "adjoint_backward": [_vp],
+        "adjoint_pull": [_vp, _dp, _dp, _dp],
+        "adjoint_recorded": [_vp],
+        "adjoint_end": [_vp],
     }
     for name, args in sigs.items():
         fn = getattr(lib, prefix + name, None)
@@ -343,6 +350,42 @@ class Solver:
 
     def update_particles(self):
         self._call("update_particles", self.ctx)
+
+    # ---- discrete adjoint (frozen particles, double-precision form) ----
+    def adjoint_begin(self, max_steps):
+        self._call("adjoint_begin", self.ctx, int(max_steps))
+
+    def adjoint_forward(self, record=True):
+        self._call("adjoint_forward", self.ctx, 1 if record else 0)
+
+    def adjoint_seed(self, ux_bar, uy_bar, p_bar=None):
+        sx, sy = self.shapes()
+        ux_bar = np.ascontiguousarray(ux_bar, dtype=np.float64)
+        uy_bar = np.ascontiguousarray(uy_bar, dtype=np.float64)
+        if ux_bar.shape != sx or uy_bar.shape != sy:
+            raise ValueError("cotangent shapes must be %s and %s" % (sx, sy))
+        pb = None
+        if p_bar is not None:
+            p_bar = np.ascontiguousarray(p_bar, dtype=np.float64)
+            if p_bar.shape != sy:
+                raise ValueError("pressure cotangent shape must be %s" % (sy,))
+            pb = _ptr(p_bar)
+        self._call("adjoint_seed", self.ctx, _ptr(ux_bar), _ptr(uy_bar), pb)
+
+    def adjoint_backward(self):
+        self._call("adjoint_backward", self.ctx)
+
+    def adjoint_pull(self):
+        sx, sy = self.shapes()
+        ub, vb, pb = np.zeros(sx), np.zeros(sy), np.zeros(sy)
+        self._call("adjoint_pull", self.ctx, _ptr(ub), _ptr(vb), _ptr(pb))
+        return ub, vb, pb
+
+    def adjoint_recorded(self):
+        return self._fn("adjoint_recorded")(self.ctx)
+
+    def adjoint_end(self):
+        self._call("adjoint_end", self.ctx)
 
 
 class Batch:

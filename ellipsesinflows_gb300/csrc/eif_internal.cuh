@@ -87,6 +87,7 @@ struct PoissonPlan {
   double *ywork;    // nblk*itot: reduced right-hand sides / interface values
 };
 
+struct Adjoint;  // adjoint.cu
 }  // namespace eif
 
 struct eif_ctx {
@@ -101,6 +102,12 @@ struct eif_ctx {
   cudaStream_t side = nullptr, main_stream = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_ibm = nullptr, ev_coll = nullptr;
   bool bands_x_valid = false;   // band lists built for the current boxes at X
+  // discrete adjoint (adjoint.cu): right-hand side that replaces the divergence in the
+  // double-precision Poisson solve while set; the exchange writes the summed weights
+  // instead of the forcing while ibm_weights_only is set; the adjoint state
+  const double *adj_rhs = nullptr;
+  bool ibm_weights_only = false;
+  eif::Adjoint *adj = nullptr;
   // fields
   double *ux[2], *uy[2];
   int cur;                      // index of the current velocity buffer

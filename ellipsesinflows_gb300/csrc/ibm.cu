@@ -409,6 +409,7 @@ struct WorkArgs {
   int wmode;
   const unsigned *iter;
   int gate;   // with iter (mixed form): 1 runs only in the first sub-iteration, 2 only afterwards
+  int weights_only;   // exchange (double precision): the cell contributions are the weights (w, w)
   Bounds bd;
 };
 
@@ -562,7 +563,7 @@ __global__ void __launch_bounds__(256) k_ibm_work(WorkArgs a) {
           const double uyp = puy + pvz * (x - px);
           const double fx = w * (uxp - uxf) / dtv;
           const double fy = w * (uyp - uyf) / dtv;
-          contrib = make_double2(fx * dtv, fy * dtv);
+          contrib = a.weights_only ? make_double2(w, w) : make_double2(fx * dtv, fy * dtv);
           const double Fx = fx * a.dx * a.dy, Fy = fy * a.dx * a.dy;
           s0 += -(Fx / pm);
           s1 += -(Fy / pm);
@@ -1301,6 +1302,7 @@ static int launch_work(eif_ctx *c, int mode, int cn) {
   w.wcache = c->wcache;
   w.iter = nullptr;
   w.gate = 0;
+  w.weights_only = c->ibm_weights_only ? 1 : 0;
   if (c->in_loop) {
     w.wmode = 0;
     w.iter = reinterpret_cast<const unsigned *>(c->d_inc + 1);

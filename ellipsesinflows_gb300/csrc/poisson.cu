@@ -118,6 +118,7 @@ __device__ double2 *fft_smem(double2 *x, double2 *y, const FftDesc &d, const dou
 
 struct Dct2Args {
   const double *ux, *uy, *dux, *duy, *dt;
+  const double *rhs;   // when set: the right-hand side itself (uy layout), used as given
   double *qhat;
   const double2 *tw, *rot, *wn;
   FftDesc fd;
@@ -133,6 +134,10 @@ __global__ void __launch_bounds__(256) k_dct2(Dct2Args a) {
   const int j = 1 + blockIdx.x;
   const double inv = 1. / (a.gamma * __ldg(a.dt));
   for (int i = 1 + threadIdx.x; i <= n; i += blockDim.x) {
+    if (a.rhs) {
+      q[i - 1] = __ldg(a.rhs + uy_idx(i, j, ld));
+      continue;
+    }
     // velocities after the IBM response, evaluated as the reference stores them
     double uxm = __ldg(a.ux + ux_idx(i, j, ld)), uxp = __ldg(a.ux + ux_idx(i + 1, j, ld));
     double uym = __ldg(a.uy + uy_idx(i, j, ld)), uyp = __ldg(a.uy + uy_idx(i, j + 1, ld));
@@ -1427,6 +1432,7 @@ int launch_potential(eif_ctx *c, int rk, bool with_ibm) {
     a.gamma = rk_coef(rk).gamma;
     a.rdx = 1. / c->dx; a.rdy = 1. / c->dy;
     a.itot = n; a.jtot = jt; a.ld = c->ld; a.with_ibm = with_ibm ? 1 : 0;
+    a.rhs = c->adj_rhs;
     EIF_PROF(c, "poisson_dct2", 1);
     k_dct2<<<jt, thr, smem, c->stream>>>(a);
     EIF_LAUNCH_CK(c);

@@ -135,6 +135,34 @@ void *eif_batch_stream(eif_batch *batch);
 const char *eif_batch_last_error(const eif_batch *batch);
 int eif_batch_destroy(eif_batch *batch);
 
+/* ---- discrete adjoint of the step (no counterpart in the reference) ----
+ * Transposed linearisation of integrate (src/main.c:14-31) in the double-precision
+ * form, with the particles frozen: their records are parameters of the step, the
+ * immersed-boundary forcing (src/suspensions/exchange.c:61-72, update.c:36-59) acts
+ * with their rigid-body velocities and no inertia, collision or Newton-Euler update
+ * runs. dt is held at the value eif_set_dt / eif_decide_dt left on the device.
+ *   begin(max_steps)   allocates a tape of max_steps steps (3 stage inputs each)
+ *                      and computes the summed indicator weights of the particles
+ *   forward(record)    one step, recorded for backward when record != 0; step and
+ *                      time advance as in eif_advance
+ *   seed(ub, vb, pb)   cotangents of the state after the last recorded step (host
+ *                      arrays in the eif_push_fluid layouts; pb may be NULL for zero).
+ *                      The cotangents of halo rows and of the pressure's wall
+ *                      columns are added to the entries they copy; the velocity
+ *                      wall columns are constants; the mean of pb over the cells is
+ *                      removed (the pressure is determined up to a constant)
+ *   backward()         transposed step of the last recorded step, which leaves the tape
+ *   pull(ub, vb, pb)   current cotangents, zero on halo rows and wall columns (the
+ *                      pushed state's are recomputed on push); any pointer may be NULL
+ * FP64 form only (EIF_ERR_ARG otherwise). */
+int eif_adjoint_begin(eif_ctx *ctx, int max_steps);
+int eif_adjoint_forward(eif_ctx *ctx, int record);
+int eif_adjoint_seed(eif_ctx *ctx, const double *ux_bar, const double *uy_bar, const double *p_bar);
+int eif_adjoint_backward(eif_ctx *ctx);
+int eif_adjoint_pull(eif_ctx *ctx, double *ux_bar, double *uy_bar, double *p_bar);
+int eif_adjoint_recorded(eif_ctx *ctx);
+int eif_adjoint_end(eif_ctx *ctx);
+
 /* ---- stage-level entry points, one per reference function ---- */
 int eif_update_boundaries(eif_ctx *ctx);                              /* src/fluid/boundary_conditions.c:7-62 */
 int eif_reset_particle_increments(eif_ctx *ctx);                      /* src/suspensions/reset.c:7-18 */
