@@ -69,6 +69,8 @@ def make_config(itot, jtot, ly=1.0, Re=2334.0, Fr=np.finfo(np.float64).max, extf
     return cfg
 
 
+ADJOINT_COUPLED, ADJOINT_FROZEN = 0, 1   # eif_adjoint_begin modes
+
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int)
 _vp = ctypes.c_void_p
@@ -108,7 +110,11 @@ def bind(lib, prefix):
         "update_particles": [_vp],
         "divergence": [_vp, _dp, _dp],
         "set_threads": [_vp, ctypes.c_int],
-        "adjoint_begin": [_vp, ctypes.c_int],
+        "adjoint_begin": [_vp, ctypes.c_int, ctypes.c_int],
+        "adjoint_seed_particles": [_vp, ctypes.c_int, _dp],
+        "adjoint_pull_particles": [_vp, ctypes.c_int, _dp],
+        "adjoint_wall_gradient": [_vp, _dp],
+        "adjoint_substeps": [_vp, ctypes.c_int, _ip],
         "adjoint_forward": [_vp, ctypes.c_int],
         "adjoint_seed": [_vp, _dp, _dp, _dp],
         "adjoint_backward": [_vp],
@@ -351,9 +357,9 @@ class Solver:
     def update_particles(self):
         self._call("update_particles", self.ctx)
 
-    # ---- discrete adjoint (frozen particles, double-precision form) ----
-    def adjoint_begin(self, max_steps):
-        self._call("adjoint_begin", self.ctx, int(max_steps))
+    # ---- discrete adjoint (double-precision form) ----
+    def adjoint_begin(self, max_steps, mode=ADJOINT_COUPLED):
+        self._call("adjoint_begin", self.ctx, int(max_steps), int(mode))
 
     def adjoint_forward(self, record=True):
         self._call("adjoint_forward", self.ctx, 1 if record else 0)
@@ -380,6 +386,28 @@ class Solver:
         ub, vb, pb = np.zeros(sx), np.zeros(sy), np.zeros(sy)
         self._call("adjoint_pull", self.ctx, _ptr(ub), _ptr(vb), _ptr(pb))
         return ub, vb, pb
+
+    def adjoint_seed_particles(self, records_bar):
+        rb = np.ascontiguousarray(records_bar, dtype=np.float64).reshape(-1, NFIELDS)
+        if rb.shape[0] != self.n_particles:
+            raise ValueError("expected %d particle records" % self.n_particles)
+        buf = rb if rb.size else np.zeros(NFIELDS)
+        self._call("adjoint_seed_particles", self.ctx, self.n_particles, _ptr(buf))
+
+    def adjoint_pull_particles(self):
+        out = np.zeros((max(self.n_particles, 1), NFIELDS))
+        self._call("adjoint_pull_particles", self.ctx, self.n_particles, _ptr(out))
+        return out[: self.n_particles]
+
+    def adjoint_wall_gradient(self):
+        g = np.zeros(2)
+        self._call("adjoint_wall_gradient", self.ctx, _ptr(g))
+        return g
+
+    def adjoint_substeps(self, step):
+        k = (ctypes.c_int * 3)()
+        self._call("adjoint_substeps", self.ctx, int(step), k)
+        return list(k)
 
     def adjoint_recorded(self):
         return self._fn("adjoint_recorded")(self.ctx)

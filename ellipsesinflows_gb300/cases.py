@@ -147,6 +147,18 @@ def mixed_target(itot=2048, jtot=4096, n=2048, a=0.012, Re=400.0, seed=1, steps=
                 steps=steps)
 
 
+def adjoint_couette(itot=256, jtot=512, n=8, a=0.06, b=0.03, seed=2, steps=400):
+    """Couette flow (walls -0.5, 0.5, linear initial profile), Re = 100, with n ellipses
+    whose centres are at least 4a apart: the configuration of the adjoint checks."""
+    rng = np.random.default_rng(seed)
+    dx = 1.0 / itot
+    xs, ys = place(n, a, 2.0, 2.0 * a, rng, 2 * dx)
+    az = rng.uniform(0.0, math.pi, n)
+    rec = particle_records(np.ones(n), np.full(n, a), np.full(n, b), xs, ys, az)
+    return Case("couette_%dx%d_n%d" % (itot, jtot, n), itot, jtot, 2.0, 100.0, uy_wall=(-0.5, 0.5), particles=rec,
+                couette_init=True, steps=steps)
+
+
 def contact_cluster(itot=64, jtot=128, seed=7):
     """Small case with ellipses overlapping tip to tip, across the periodic
     boundary and into a wall, so that every branch of the collision model is

@@ -249,6 +249,20 @@ void ibm_free(eif_ctx *c);
 int launch_inertia(eif_ctx *c, int cn);
 int launch_exchange(eif_ctx *c);
 int launch_band_lists(eif_ctx *c);
+// transposed box evaluation of the discrete adjoint (ibm.cu): mode 0 the inertia
+// integrals at X (+ dX with use_increment), mode 1 the momentum exchange at X; bar
+// holds 3 x np cotangents of the integrals (mode 0) or of the particle forces
+// (mode 1); gx, gy (mode 1) the cell cotangents of the field response. Writes
+// out (6 x np: cotangents of x, y, az, ux, uy, vz) and the cell cotangents of the
+// face-averaged velocity into fx, fy (interior cells).
+struct AdjPass {
+  int mode = 0;
+  bool use_increment = false;
+  const double *ux = nullptr, *uy = nullptr, *bar = nullptr, *gx = nullptr, *gy = nullptr;
+  double *part = nullptr, *out = nullptr, *fx = nullptr, *fy = nullptr;
+};
+int launch_adj_pass(eif_ctx *c, const AdjPass &p);
+int adj_chunk_cap(const eif_ctx *c);
 int sub_iteration(eif_ctx *c, int rk);
 bool overlap_on(const eif_ctx *c);
 

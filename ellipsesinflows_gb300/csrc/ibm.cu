@@ -1365,11 +1365,18 @@ int launch_inertia(eif_ctx *c, int cn) {
   return launch_work(c, 0, cn);
 }
 
+static int band_lists_of_boxes(eif_ctx *c);
+
 // ordered box lists per band of GTY rows for the gather, from the boxes at X
 int launch_band_lists(eif_ctx *c) {
   if (c->np == 0) return EIF_OK;
   int rc = launch_boxes(c, false);
   if (rc) return rc;
+  return band_lists_of_boxes(c);
+}
+
+// the band lists of the boxes currently built
+static int band_lists_of_boxes(eif_ctx *c) {
   const int nbands = (c->jtot + GTY - 1) / GTY;
   const int words = (3 * c->np + 31) / 32;
   EIF_PROF(c, "ibm_band_lists", 2);
@@ -1419,5 +1426,221 @@ int launch_exchange(eif_ctx *c) {
   EIF_LAUNCH_CK(c);
   return EIF_OK;
 }
+
+}  // namespace eif
+
+// ---------------------------------------------------------------------------
+// Transposed box evaluations for the discrete adjoint (double precision).
+//
+// The inertia integrals I = sum_cells w_v(D) (u_c, r x u_c) dxdy / (m, I_z)
+// (inertia.c:41-52) and the exchange sums F = -sum_cells w_s(D) (U_r - u_c) dxdy
+// / (dt m, dt I_z) with the field response dux = sum w_s (U_r - u_c)
+// (exchange.c:61-76) depend on the cell velocities u_c (face averages), on the
+// particle velocities U, Omega, and on the centre and angle through the lever arm
+// r = x - X and the signed distance D = d/h of the cell centre. With q = R(-az) r
+// the body-frame offset and the distance computed through the normal foot
+// (ellipse.c:30-65), dD/dq at the foot is minus the outward unit normal over h
+// (the foot parameter is stationary, so it does not contribute), hence
+//   dD/dX = -g,   dD/daz = g_x r_y - g_y r_x,   g = R(az) dD/dq.
+// w_v = (1 + tanh(2D))/2 has dw_v/dD = w_s, and w_s = 1 - tanh^2(2D) has
+// dw_s/dD = -4 tanh(2D) w_s.
+//
+// One warp per box row task as in k_ibm_work. Per cell the kernel writes the cell
+// cotangent of the face-averaged velocity into the scratch buffer (gathered per
+// cell afterwards in the fixed order of the forward exchange) and sums per task the
+// cotangents of (X, Y, az) and (U, V, Omega). Boxes are those of the forward
+// evaluation (the loop bounds are piecewise constant in the positions).
+namespace {
+
+struct AdjWorkArgs {
+  const double *P;
+  const double *ux, *uy, *xc, *yc, *dt;
+  const int *off;
+  const int4 *tdesc;
+  const double *bar;        // 3 x np: inertia cotangent (mode 0) or force cotangent (mode 1)
+  const double *gx, *gy;    // mode 1: cell cotangents of the field response
+  double *part;             // 6 per task
+  double2 *wbuf;
+  int pcap, np, ld, mode, use_increment;
+  double dx, dy, ly, h;
+  Bounds bd;
+};
+
+__global__ void __launch_bounds__(256) k_ibm_adj(AdjWorkArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const int total = EIF_CHK(a.bd.rec, a.np, a.bd.off, 70) ? __ldg(a.off + a.np) : 0;
+  const double rh = 1. / a.h;
+  const double dxdy = a.dx * a.dy;
+  const double kdt = a.mode == 1 ? dxdy / __ldg(a.dt) : 0.;
+  const int pc = a.pcap, ld = a.ld;
+  for (int c = warp; c < total; c += nwarps) {
+    if (!EIF_CHK(a.bd.rec, 6LL * c + 5, 6LL * (a.bd.partial / 3), 71)) continue;
+    const int4 dsc = __ldg(a.tdesc + c);
+    const int n = dsc.x;
+    if (!EIF_CHK(a.bd.rec, n, a.np, 72)) continue;
+    RowTask t;
+    const bool task = task_of(dsc, a.np, t) && EIF_CHK(a.bd.rec, t.j, a.bd.yc - 1, 73);
+    const double *P = a.P;
+    const double pden = __ldg(P + EIF_P_DEN * pc + n), pa = __ldg(P + EIF_P_A * pc + n), pb = __ldg(P + EIF_P_B * pc + n);
+    double px = __ldg(P + EIF_P_X * pc + n), py = __ldg(P + EIF_P_Y * pc + n), paz = __ldg(P + EIF_P_AZ * pc + n);
+    if (a.use_increment) {
+      px = px + __ldg(P + EIF_P_DX * pc + n);
+      py = py + __ldg(P + EIF_P_DY * pc + n);
+      paz = paz + __ldg(P + EIF_P_DAZ * pc + n);
+    }
+    const double pm = pmass(pden, pa, pb), pim = pmoi(pden, pa, pb);
+    const double pux = __ldg(P + EIF_P_UX * pc + n), puy = __ldg(P + EIF_P_UY * pc + n), pvz = __ldg(P + EIF_P_VZ * pc + n);
+    const double b0 = __ldg(a.bar + n), b1 = __ldg(a.bar + a.np + n), b2 = __ldg(a.bar + 2 * a.np + n);
+    const Ell e = make_ell(pa, pb, px, py, paz);
+    const double py_ = py + a.ly * (task ? t.img : 0);
+    const int j = task ? t.j : 1;
+    const double y = __ldg(a.yc + j);
+    const double ry = y - py_;
+    const double mn = fmin(pa, pb);
+    double sX = 0., sY = 0., sA = 0., sU = 0., sV = 0., sW = 0.;
+#pragma unroll 1
+    for (int half = 0; half < CHUNK / 32; half++) {
+      const int i = (task ? t.ib : 1) + half * 32 + lane;
+      bool in = task && i <= t.ie;
+      if (in) {
+        in = EIF_CHK(a.bd.rec, i, a.bd.xc - 1, 74) && EIF_CHK(a.bd.rec, j * ld + i, a.bd.field, 75) &&
+             EIF_CHK(a.bd.rec, (j + 1) * ld + i, a.bd.field, 76) && EIF_CHK(a.bd.rec, j * ld + (i - 1), a.bd.field, 77);
+      }
+      double2 contrib = make_double2(0., 0.);
+      if (in) {
+        const double x = __ldg(a.xc + i);
+        const double rx = x - px;
+        const double qx = e.cz * rx - e.sz * ry, qy = e.sz * rx + e.cz * ry;
+        // distance bound from the gauge of the ellipse: beyond FAR_CELLS_D cells tanh(2D)
+        // is +-1 in double precision and both weights' derivatives vanish
+        const double rho = sqrt((qx / pa) * (qx / pa) + (qy / pb) * (qy / pb));
+        double th, gwx = 0., gwy = 0.;
+        if (mn * fabs(rho - 1.) * rh >= FAR_CELLS_D) {
+          th = rho < 1. ? 1. : -1.;
+        } else {
+          const double f0 = 1. - (qx / pa) * (qx / pa) - (qy / pb) * (qy / pb);
+          const double sign = f0 > 0. ? 1. : -1.;
+          const double tt = normal_t(e, qx, qy);
+          double st, ct;
+          sincos(tt, &st, &ct);
+          const double fx = pa * ct - qx, fy = pb * st - qy;
+          th = tanh(BETA * (sign * sqrt(fx * fx + fy * fy) * rh));
+          // outward normal at the foot (cos t / a, sin t / b); dD/dq = -n / h
+          double nx = ct / pa, ny = st / pb;
+          const double nn = 1. / sqrt(nx * nx + ny * ny);
+          nx *= nn;
+          ny *= nn;
+          const double gbx = -nx * rh, gby = -ny * rh;
+          // g = R(az) dD/dq with cz = cos(-az), sz = sin(-az)
+          gwx = e.cz * gbx + e.sz * gby;
+          gwy = -e.sz * gbx + e.cz * gby;
+        }
+        const double ws = 0.5 * BETA * (1. - th * th);
+        const double uxf = 0.5 * (__ldg(a.ux + j * ld + (i - 1)) + __ldg(a.ux + j * ld + i));
+        const double uyf = 0.5 * (__ldg(a.uy + j * ld + i) + __ldg(a.uy + (j + 1) * ld + i));
+        const double dDdaz = gwx * ry - gwy * rx;
+        if (a.mode == 0) {
+          const double wv = 0.5 * (1. + th);
+          const double cx = b0 / pm, cy = b1 / pm, cz = b2 / pim;
+          contrib = make_double2(wv * dxdy * (cx - cz * ry), wv * dxdy * (cy + cz * rx));
+          const double sv = dxdy * (cx * uxf + cy * uyf + cz * (-ry * uxf + rx * uyf));
+          const double dw = ws * sv;
+          sX += -dw * gwx - wv * dxdy * cz * uyf;
+          sY += -dw * gwy + wv * dxdy * cz * uxf;
+          sA += dw * dDdaz;
+        } else {
+          const int cc = j * ld + i;
+          const double urx = pux - pvz * ry, ury = puy + pvz * rx;
+          const double ex = urx - uxf, ey = ury - uyf;
+          const double Cx = __ldg(a.gx + cc) - b0 * kdt / pm + b2 * ry * kdt / pim;
+          const double Cy = __ldg(a.gy + cc) - b1 * kdt / pm - b2 * rx * kdt / pim;
+          const double Ex = ws * Cx, Ey = ws * Cy;
+          contrib = make_double2(-Ex, -Ey);
+          sU += Ex;
+          sV += Ey;
+          sW += -ry * Ex + rx * Ey;
+          const double dw = (ex * Cx + ey * Cy) * (-2. * BETA * th * ws);
+          sX += -dw * gwx - pvz * Ey + b2 * ws * ey * kdt / pim;
+          sY += -dw * gwy + pvz * Ex - b2 * ws * ex * kdt / pim;
+          sA += dw * dDdaz;
+        }
+      }
+      if (EIF_CHK(a.bd.rec, (long long)c * CHUNK + half * 32 + lane, a.bd.wbuf, 78))
+        a.wbuf[(size_t)c * CHUNK + half * 32 + lane] = contrib;
+    }
+    sX = eifd::warp_sum(sX);
+    sY = eifd::warp_sum(sY);
+    sA = eifd::warp_sum(sA);
+    sU = eifd::warp_sum(sU);
+    sV = eifd::warp_sum(sV);
+    sW = eifd::warp_sum(sW);
+    if (lane == 0) {
+      double *q = a.part + 6 * (size_t)c;
+      q[0] = sX; q[1] = sY; q[2] = sA; q[3] = sU; q[4] = sV; q[5] = sW;
+    }
+  }
+}
+
+// per-particle sums of the task cotangents in task order: out[k * np + n]
+__global__ void k_adj_chunk_reduce(const double *__restrict__ part, const int *__restrict__ off,
+                                   double *__restrict__ out, int np, Bounds bd) {
+  const int lane = threadIdx.x & 31;
+  const int n = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (n >= np) return;
+  if (!EIF_CHK(bd.rec, n + 1, bd.off, 79)) return;
+  const int c0 = off[n], c1 = off[n + 1];
+  double s[6] = {0., 0., 0., 0., 0., 0.};
+  for (int c = c0 + lane; c < c1; c += 32) {
+    if (!EIF_CHK(bd.rec, 6LL * c + 5, 6LL * (bd.partial / 3), 80)) break;
+#pragma unroll
+    for (int k = 0; k < 6; k++) s[k] += part[6 * (size_t)c + k];
+  }
+#pragma unroll
+  for (int k = 0; k < 6; k++) {
+    const double v = eifd::warp_sum(s[k]);
+    if (lane == 0) out[(size_t)k * np + n] = v;
+  }
+}
+
+}  // namespace
+
+namespace eif {
+
+int launch_adj_pass(eif_ctx *c, const AdjPass &p) {
+  if (c->np == 0) return EIF_OK;
+  if (p.use_increment) c->incr_zero = false;
+  int rc = launch_boxes(c, p.use_increment);
+  if (rc) return rc;
+  AdjWorkArgs w;
+  w.P = c->P; w.ux = p.ux; w.uy = p.uy; w.xc = c->xc; w.yc = c->yc; w.dt = c->d_scal;
+  w.off = c->chunk_off; w.tdesc = c->tdesc;
+  w.bar = p.bar; w.gx = p.gx; w.gy = p.gy;
+  w.part = p.part;
+  w.wbuf = reinterpret_cast<double2 *>(c->wbuf);
+  w.pcap = c->pcap; w.np = c->np; w.ld = c->ld; w.mode = p.mode; w.use_increment = p.use_increment ? 1 : 0;
+  w.dx = c->dx; w.dy = c->dy; w.ly = c->ly; w.h = std::min(c->dx, c->dy);
+  w.bd = bounds_of(c);
+  const int blocks = std::max(1, std::min(c->sms * 8, (c->chunk_cap * 32 + 255) / 256));
+  k_ibm_adj<<<blocks, 256, 0, c->stream>>>(w);
+  EIF_LAUNCH_CK(c);
+  k_adj_chunk_reduce<<<(c->np * 32 + 255) / 256, 256, 0, c->stream>>>(p.part, c->chunk_off, p.out, c->np,
+                                                                        bounds_of(c));
+  EIF_LAUNCH_CK(c);
+  if ((rc = band_lists_of_boxes(c))) return rc;
+  GatherArgs g;
+  g.edesc = c->edesc; g.wbuf = c->wbuf;
+  g.dux = p.fx; g.duy = p.fy; g.flags = c->d_flags;
+  g.np = c->np; g.itot = c->itot; g.jtot = c->jtot; g.ld = c->ld;
+  g.bd = bounds_of(c);
+  g.lists = c->band_lists; g.counts = c->band_counts; g.cap = c->band_cap;
+  dim3 grid((c->itot + GTX - 1) / GTX, (c->jtot + GTY - 1) / GTY);
+  k_gather<double2, double><<<grid, GTHREADS, 0, c->stream>>>(g);
+  EIF_LAUNCH_CK(c);
+  return EIF_OK;
+}
+
+int adj_chunk_cap(const eif_ctx *c) { return c->chunk_cap; }
 
 }  // namespace eif

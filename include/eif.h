@@ -136,30 +136,50 @@ const char *eif_batch_last_error(const eif_batch *batch);
 int eif_batch_destroy(eif_batch *batch);
 
 /* ---- discrete adjoint of the step (no counterpart in the reference) ----
- * Transposed linearisation of integrate (src/main.c:14-31) in the double-precision
- * form, with the particles frozen: their records are parameters of the step, the
- * immersed-boundary forcing (src/suspensions/exchange.c:61-72, update.c:36-59) acts
- * with their rigid-body velocities and no inertia, collision or Newton-Euler update
- * runs. dt is held at the value eif_set_dt / eif_decide_dt left on the device.
- *   begin(max_steps)   allocates a tape of max_steps steps (3 stage inputs each)
- *                      and computes the summed indicator weights of the particles
+ * Transposed linearisation of integrate (src/main.c:13-55) in the double-precision
+ * form with dt held at the value eif_set_dt / eif_decide_dt left on the device.
+ * EIF_ADJOINT_COUPLED: the whole step, particles moving: predictor, immersed-boundary
+ * exchange (src/suspensions/exchange.c:13-88) and field update (update.c:36-59),
+ * Poisson solve and projection, inertia integrals (inertia.c:9-70), Newton-Euler
+ * increments and the recorded sub-iterations of the particle fixed point
+ * (increment.c, main.c:32-52). Collision forces enter as constants: the adjoint is
+ * that of contact-free motion, and backward fails (EIF_ERR_STATE) for a recorded step
+ * in which a collision force was non-zero.
+ * EIF_ADJOINT_FROZEN: the particle records are parameters of the step (no inertia,
+ * collision, increment or update runs; the forcing acts with their rigid-body
+ * velocities).
+ *   begin(max_steps, mode)  allocates a tape of max_steps steps
  *   forward(record)    one step, recorded for backward when record != 0; step and
- *                      time advance as in eif_advance
- *   seed(ub, vb, pb)   cotangents of the state after the last recorded step (host
- *                      arrays in the eif_push_fluid layouts; pb may be NULL for zero).
+ *                      time advance as in eif_advance (coupled mode: the same bits as
+ *                      eif_integrate)
+ *   seed(ub, vb, pb)   cotangents of the fluid state after the last recorded step
+ *                      (host arrays in the eif_push_fluid layouts; pb may be NULL).
  *                      The cotangents of halo rows and of the pressure's wall
  *                      columns are added to the entries they copy; the velocity
- *                      wall columns are constants; the mean of pb over the cells is
- *                      removed (the pressure is determined up to a constant)
+ *                      wall columns are no state (those of vb start the wall-velocity
+ *                      gradient); the mean of pb over the cells is removed (the
+ *                      pressure is determined up to a constant). Resets the
+ *                      particle cotangents.
+ *   seed_particles(n, rb)  particle cotangents (n records of EIF_NFIELDS doubles;
+ *                      x, y, az, ux, uy, vz are read)
  *   backward()         transposed step of the last recorded step, which leaves the tape
- *   pull(ub, vb, pb)   current cotangents, zero on halo rows and wall columns (the
+ *   pull(ub, vb, pb)   current fluid cotangents, zero on halo rows and wall columns (the
  *                      pushed state's are recomputed on push); any pointer may be NULL
+ *   pull_particles(n, rb)  current particle cotangents (other fields zero)
+ *   wall_gradient(g)   d/d uy_wall[0..1] accumulated over the steps gone back through
+ *   substeps(s, k)     sub-iteration counts of the three stages of recorded step s
  * FP64 form only (EIF_ERR_ARG otherwise). */
-int eif_adjoint_begin(eif_ctx *ctx, int max_steps);
+#define EIF_ADJOINT_COUPLED 0
+#define EIF_ADJOINT_FROZEN 1
+int eif_adjoint_begin(eif_ctx *ctx, int max_steps, int mode);
 int eif_adjoint_forward(eif_ctx *ctx, int record);
 int eif_adjoint_seed(eif_ctx *ctx, const double *ux_bar, const double *uy_bar, const double *p_bar);
+int eif_adjoint_seed_particles(eif_ctx *ctx, int n, const double *records_bar);
 int eif_adjoint_backward(eif_ctx *ctx);
 int eif_adjoint_pull(eif_ctx *ctx, double *ux_bar, double *uy_bar, double *p_bar);
+int eif_adjoint_pull_particles(eif_ctx *ctx, int n, double *records_bar);
+int eif_adjoint_wall_gradient(eif_ctx *ctx, double *d_uy_wall);
+int eif_adjoint_substeps(eif_ctx *ctx, int step, int *substeps);
 int eif_adjoint_recorded(eif_ctx *ctx);
 int eif_adjoint_end(eif_ctx *ctx);
 
