@@ -147,6 +147,27 @@ def mixed_target(itot=2048, jtot=4096, n=2048, a=0.012, Re=400.0, seed=1, steps=
                 steps=steps)
 
 
+def adjoint_channel(n=8, itot=64, jtot=128, seed=11):
+    """The inputs of the adjoint checks at 64x128: a channel (walls at rest) with n
+    ellipses a = 0.07, b = 0.035 moving at random velocities, and a sheared,
+    rotating initial flow with noise, so that every advective and coupling term is
+    active. Returns (case, (ux, uy, p), records)."""
+    case = poiseuille(itot=itot, jtot=jtot, n=max(n, 1), a=0.07, b=0.035, Re=150.0, seed=seed)
+    rng = np.random.default_rng(seed + 100)
+    rec = case.particles[:n].copy()
+    rec[:, F["ux"]] = rng.uniform(-0.1, 0.1, n)
+    rec[:, F["uy"]] = rng.uniform(-0.1, 0.1, n)
+    rec[:, F["vz"]] = rng.uniform(-0.5, 0.5, n)
+    case.particles = rec
+    ux, uy, p = (np.array(a, dtype=np.float64) for a in case.fluid())
+    jj, ii = np.meshgrid(np.arange(jtot + 2), np.arange(itot + 1), indexing="ij")
+    ux += 0.2 * np.sin(2 * np.pi * jj / jtot) * np.sin(np.pi * ii / itot) + 0.02 * rng.standard_normal(ux.shape)
+    jj, ii = np.meshgrid(np.arange(jtot + 2), np.arange(itot + 2), indexing="ij")
+    uy += 0.3 * np.cos(np.pi * (ii - 0.5) / itot) + 0.02 * rng.standard_normal(uy.shape)
+    p += 0.05 * rng.standard_normal(p.shape)
+    return case, (ux, uy, p), rec
+
+
 def adjoint_couette(itot=256, jtot=512, n=8, a=0.06, b=0.03, seed=2, steps=400):
     """Couette flow (walls -0.5, 0.5, linear initial profile), Re = 100, with n ellipses
     whose centres are at least 4a apart: the configuration of the adjoint checks."""

@@ -37,22 +37,11 @@ DT = 2e-3
 
 
 def make_case(n_particles=8, itot=64, jtot=128, seed=11, wall=(-0.1, 0.2)):
-    case = cases.poiseuille(itot=itot, jtot=jtot, n=max(n_particles, 1), a=0.07, b=0.035, Re=150.0, seed=seed)
-    rng = np.random.default_rng(seed + 100)
-    rec = case.particles[:n_particles].copy()
-    rec[:, F["ux"]] = rng.uniform(-0.1, 0.1, n_particles)
-    rec[:, F["uy"]] = rng.uniform(-0.1, 0.1, n_particles)
-    rec[:, F["vz"]] = rng.uniform(-0.5, 0.5, n_particles)
-    ux, uy, p = (np.array(a, dtype=np.float64) for a in case.fluid())
-    # a sheared, rotating initial flow so that every advective partial derivative is active
-    jj, ii = np.meshgrid(np.arange(jtot + 2), np.arange(itot + 1), indexing="ij")
-    ux += 0.2 * np.sin(2 * np.pi * jj / jtot) * np.sin(np.pi * ii / itot) + 0.02 * rng.standard_normal(ux.shape)
-    jj, ii = np.meshgrid(np.arange(jtot + 2), np.arange(itot + 2), indexing="ij")
-    uy += 0.3 * np.cos(np.pi * (ii - 0.5) / itot) + 0.02 * rng.standard_normal(uy.shape)
-    p += 0.05 * rng.standard_normal(p.shape)
+    case, state, rec = cases.adjoint_channel(n_particles, itot, jtot, seed)
+    rng = np.random.default_rng(seed + 200)
     cfg = case.config()
     cfg.uy_wall[0], cfg.uy_wall[1] = wall
-    return cfg, (ux, uy, p), rec, rng
+    return cfg, state, rec, rng
 
 
 def new_sim(cfg, wall=None):
@@ -342,4 +331,29 @@ def test_adjoint_couette_256x512_400_steps():
     adj = float(np.dot(grads[4], dwall))
     print("Couette adjoint vs central difference [wall]: %.15e %.15e rel %.2e" % (adj, fd, abs(adj - fd) / abs(fd)))
     assert abs(adj - fd) <= TOL_FD * abs(fd)
+    sim.close()
+
+
+def test_adjoint_matches_reference_central_differences():
+    """Directional derivatives of the GPU adjoint against central differences of the
+    reference solver's own CPU step (fixture written by tests/golden/make_adjoint_fd.py)."""
+    import importlib.util
+    import os
+    here = os.path.dirname(os.path.abspath(__file__))
+    spec = importlib.util.spec_from_file_location("make_adjoint_fd", os.path.join(here, "golden", "make_adjoint_fd.py"))
+    G = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(G)
+    ref = np.load(os.path.join(here, "golden", "adjoint_fd_64x128.npz"))
+    case, state, rec, w, dirs = G.inputs()
+    sim = Simulation(case.config())
+    out, subs = run(sim, state, rec, G.NSTEPS, G.DT, ADJOINT_COUPLED)
+    # the same sub-iteration counts as the reference run, and the same loss (1e-11 parity)
+    assert np.array_equal(np.array(subs), ref["substeps"])
+    assert loss(out, w) == pytest.approx(float(ref["loss"]), rel=1e-11)
+    grads, _ = gradients(sim, state, rec, w, G.NSTEPS, 3, ADJOINT_COUPLED)
+    for name, d in dirs.items():
+        fd = float(ref["fd_" + name])
+        adj = sum(float(np.sum(g * e)) for g, e in zip(grads[:4], d))
+        print("adjoint vs reference central difference [%s]: %.15e %.15e rel %.2e" % (name, adj, fd, abs(adj - fd) / abs(fd)))
+        assert abs(adj - fd) <= TOL_FD * abs(fd), (name, adj, fd)
     sim.close()
