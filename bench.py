@@ -68,7 +68,8 @@ def parse():
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--no-fp64-leg", action="store_true")
     ap.add_argument("--workload", default="mixed_target",
-                    choices=["mixed_target", "poiseuille", "couette_circle", "batch_c5"])
+                    choices=["mixed_target", "poiseuille", "couette_circle", "batch_c5", "adjoint_couette",
+                             "adjoint_large"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
@@ -293,6 +294,68 @@ def run_batch(args, world, rank, local, pg):
     return out, rank
 
 
+def run_adjoint(args, world, rank, local, pg):
+    """Gradient of a loss of the state after K steps through the discrete adjoint
+    (eif_adjoint_*, double-precision form, particles moving): per step one recorded
+    forward step and one transposed step, i.e. the work of a checkpoint segment's
+    recomputation and reverse sweep. value: cells x steps / time of (recorded
+    forward + backward); cost_vs_forward: that time over the plain forward steps
+    (eif_integrate with the same dt) on the same state."""
+    import numpy as np
+    import torch
+    from ellipsesinflows_gb300 import Simulation, build
+    build.build()
+    torch.cuda.set_device(local)
+    case = make_case(args.workload)
+    sim = Simulation.from_case(case, device=local)
+    ux, uy, p = case.fluid()
+    uy = uy + getattr(case, "uy_offset", 0.0)
+    sim.push_fluid(ux, uy, p)
+    sim.dt = 0.5 * sim.decide_dt()
+    k = args.steps
+    sim.adjoint_begin(k)
+    for _ in range(args.warmup):
+        sim.integrate()
+    state = sim.pull_fluid()[:3]
+    rec = sim.pull_particles()
+
+    def timed(fn):
+        barrier(pg, local)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fn()
+        torch.cuda.synchronize()
+        barrier(pg, local)
+        return max_over_ranks(pg, (time.perf_counter() - t0) * 1e3, local)
+
+    with ClockSampler(local) as clk:
+        fwd_ms = timed(lambda: [sim.integrate() for _ in range(k)])
+        sim.push_fluid(*state)
+        sim.push_particles(rec)
+        rec_ms = timed(lambda: [sim.adjoint_forward(record=True) for _ in range(k)])
+        sx, sy = sim.shapes()
+        rng = np.random.default_rng(0)
+        sim.adjoint_seed(rng.standard_normal(sx), rng.standard_normal(sy))
+        bwd_ms = timed(lambda: [sim.adjoint_backward() for _ in range(k)])
+    sim.adjoint_end()
+    cells = case.cells
+    out = {
+        "metric": "cell-steps/s", "value": world * cells * k / ((rec_ms + bwd_ms) / 1e3), "unit": "cell-steps/s",
+        "n_gpus": world, "steps": k, "warmup": args.warmup, "ms_per_step": (rec_ms + bwd_ms) / k,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded ellipse placement)",
+        "config": {"workload": case.name, "itot": case.itot, "jtot": case.jtot, "n_particles": case.n_particles,
+                   "what": "discrete adjoint, coupled particles: recorded forward + backward per step",
+                   "l2": "state larger than L2" if cells * 8 * 13 > 129e6 else "state fits in L2",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "forward_ms_per_step": fwd_ms / k, "recorded_forward_ms_per_step": rec_ms / k,
+        "backward_ms_per_step": bwd_ms / k,
+        "cost_vs_forward": {"backward": bwd_ms / fwd_ms, "recompute_and_backward": (rec_ms + bwd_ms) / fwd_ms},
+        "e2e": None, "roofline": None, "clocks": clk.summary(), "gpu_launches": None,
+    }
+    return out, rank
+
+
 def fp64_leg(args, case, mixed_sim, device, pg, world):
     """The plain double-precision form on the same workload and step count, and the
     error of the mixed-precision state against it after the same number of steps."""
@@ -443,6 +506,8 @@ def main():
         out, rank = run_reference(args, world, rank)
     elif args.workload == "batch_c5":
         out, rank = run_batch(args, world, rank, local, pg)
+    elif args.workload.startswith("adjoint"):
+        out, rank = run_adjoint(args, world, rank, local, pg)
     else:
         out, rank = run_ours(args, world, rank, local, pg)
     if rank == 0 and out is not None:

@@ -224,9 +224,21 @@ def batch_c5(count=64, seed=3, n_max=128, steps=300):
     return out
 
 
+def adjoint_large(itot=2048, jtot=4096, n=2048, a=0.012, b=0.006, seed=1, steps=10):
+    """2048 x 4096 channel with 2048 ellipses of aspect ratio 2 (about 4.6 % area, so
+    the motion stays contact-free over the measured steps), fluid sheared by a
+    uniform 0.3 in y: the large workload of the adjoint cost measurement."""
+    c = poiseuille(itot=itot, jtot=jtot, n=n, a=a, b=b, Re=400.0, seed=seed, steps=steps)
+    c.name = "adjoint_channel_%dx%d_n%d" % (itot, jtot, n)
+    c.uy_offset = 0.3
+    return c
+
+
 CONFIGS = {
     "couette_circle": couette_circle,
     "poiseuille": poiseuille,
     "mixed_target": mixed_target,
     "contact_cluster": contact_cluster,
+    "adjoint_couette": adjoint_couette,
+    "adjoint_large": adjoint_large,
 }
