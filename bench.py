@@ -229,6 +229,7 @@ def run_ours(args, world, rank, local, pg):
         "config": {"workload": case.name, "itot": case.itot, "jtot": case.jtot, "n_particles": case.n_particles,
                    "Re": case.Re, "precision": args.precision,
                    "l2": "inputs larger than L2 (~1 GB of device state per step)",
+                   "tiles": sim.tiles(),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "e2e": e2e, "roofline": roof, "gpu_launches": launches,
         "fp64_form": fp64, "accuracy_vs_fp64": accuracy,

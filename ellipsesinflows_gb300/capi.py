@@ -110,6 +110,7 @@ def bind(lib, prefix):
         "update_particles": [_vp],
         "divergence": [_vp, _dp, _dp],
         "set_threads": [_vp, ctypes.c_int],
+        "tiles": [_vp, _ip],
         "adjoint_begin": [_vp, ctypes.c_int, ctypes.c_int],
         "adjoint_seed_particles": [_vp, ctypes.c_int, _dp],
         "adjoint_pull_particles": [_vp, ctypes.c_int, _dp],
@@ -356,6 +357,13 @@ class Solver:
 
     def update_particles(self):
         self._call("update_particles", self.ctx)
+
+    def tiles(self):
+        """tile shapes chosen by the tuner: {"predictor_rows", "projection_rows",
+        "thomas_threads", "tuned"}"""
+        t = (ctypes.c_int * 4)()
+        self._call("tiles", self.ctx, t)
+        return {"predictor_rows": t[0], "projection_rows": t[1], "thomas_threads": t[2], "tuned": bool(t[3])}
 
     # ---- discrete adjoint (double-precision form) ----
     def adjoint_begin(self, max_steps, mode=ADJOINT_COUPLED):

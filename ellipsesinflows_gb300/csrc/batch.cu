@@ -166,6 +166,13 @@ int eif_batch_create(eif_ctx *const *ctxs, int n, eif_batch **out) {
     eif_batch_destroy(b);
     return EIF_ERR_CUDA;
   }
+  // tile shapes of every suspension before the step graphs capture their launches
+  for (int i = 0; i < n; i++) {
+    if (ctxs[i]->fluid_pushed && eif::tune_tiles(ctxs[i]) != EIF_OK) {
+      eif_batch_destroy(b);
+      return EIF_ERR_CUDA;
+    }
+  }
   *out = b;
   return EIF_OK;
 }

@@ -689,6 +689,7 @@ int eif_get_dt(eif_ctx *c, double *dt) {
 int eif_integrate(eif_ctx *c, int *substeps) {
   if (!c) return EIF_ERR_ARG;
   if (!c->fluid_pushed) return fail(c, EIF_ERR_STATE, "push the fluid state before integrating");
+  if (int rc = tune_tiles(c)) return rc;
   for (int rk = 0; rk < 3; rk++) {
     int sub = 0;
     int rc = rk_stage(c, rk, &sub);
@@ -701,6 +702,7 @@ int eif_integrate(eif_ctx *c, int *substeps) {
 int eif_advance(eif_ctx *c, int nsteps) {
   if (!c || nsteps < 0) return EIF_ERR_ARG;
   if (!c->fluid_pushed) return fail(c, EIF_ERR_STATE, "push the fluid state before integrating");
+  if (int rc = tune_tiles(c)) return rc;
   if (c->use_graphs && !c->sync_debug && !c->prof.enabled) {
     // one graph launch per step (see graph.cu), queued one step ahead: step s + 1 is
     // launched before the host waits for the copies of step s's dt, flags and bounds

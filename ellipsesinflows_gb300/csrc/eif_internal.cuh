@@ -140,6 +140,13 @@ struct eif_ctx {
     int cur0 = -1, scur0 = -1, cur1 = 0, scur1 = 0;
   } graphs[2];
   bool use_graphs = true;
+  // tile shapes of the stencil and block-Thomas kernels, chosen once per grid size by the
+  // tuner (tune.cu) among shapes that give the same results: predictor and projection
+  // tile heights (rows per block of 32 columns), threads per block of the block Thomas
+  struct Tiles {
+    int pred = 8, corr = 8, tdm = 128;
+    bool tuned = false;
+  } tiles;
   unsigned buf_gen = 0;         // bumped when device buffers are reallocated (batch graphs hold them)
   bool incr_zero = false;       // the particle increments are zero (after a reset)
   bool boxes_x_valid = false;   // the IBM boxes hold the positions X (see launch_boxes)
@@ -262,6 +269,9 @@ struct AdjPass {
   double *part = nullptr, *out = nullptr, *fx = nullptr, *fy = nullptr;
 };
 int launch_adj_pass(eif_ctx *c, const AdjPass &p);
+// choose c->tiles by timing the candidate shapes on scratch copies of the fields
+// (once per context; results are cached per grid size and precision); not during capture
+int tune_tiles(eif_ctx *c);
 int adj_chunk_cap(const eif_ctx *c);
 int sub_iteration(eif_ctx *c, int rk);
 bool overlap_on(const eif_ctx *c);

@@ -19,7 +19,9 @@ namespace {
 using eifd::ux_idx;
 using eifd::uy_idx;
 
-constexpr int TX = 32, TY = 8;
+constexpr int TX = 32;
+// tile heights of the stencil kernels the tuner chooses from (results do not depend on it)
+constexpr int TY_DEFAULT = 8;
 
 // ---------------------------------------------------------------------------
 // boundary and halo values of one field kind
@@ -70,6 +72,7 @@ struct PredArgs {
   int itot, jtot, ld;
 };
 
+template <int TY>
 __global__ void __launch_bounds__(TX *TY) k_predictor(PredArgs a) {
   const int i = 1 + blockIdx.x * TX + threadIdx.x;
   const int j = 1 + blockIdx.y * TY + threadIdx.y;
@@ -160,12 +163,12 @@ struct PredArgsF {
   int itot, jtot, ld;
 };
 
-constexpr int PX = TX + 2, PY = TY + 2;
-
 __device__ __forceinline__ float dif(float2 a, float2 b) { return (a.x - b.x) + (a.y - b.y); }
 __device__ __forceinline__ float val(float2 a) { return a.x + a.y; }
 
+template <int TY>
 __global__ void __launch_bounds__(TX *TY) k_predictor_mixed(PredArgsF a) {
+  constexpr int PX = TX + 2, PY = TY + 2;
   __shared__ float2 tux[PY][PX], tuy[PY][PX], tp[PY][PX];
   const int ld = a.ld, itot = a.itot, jtot = a.jtot;
   const int ib = 1 + blockIdx.x * TX, jb = 1 + blockIdx.y * TY;
@@ -257,6 +260,7 @@ struct CorrArgs {
   int itot, jtot, ld, with_ibm, with_proj, with_pressure;
 };
 
+template <int TY>
 __global__ void __launch_bounds__(TX *TY) k_correct(CorrArgs a) {
   const int i = 1 + blockIdx.x * TX + threadIdx.x;
   const int j = 1 + blockIdx.y * TY + threadIdx.y;
@@ -317,6 +321,7 @@ struct CorrArgsDF {
   int rk, itot, jtot, ld, with_ibm, with_proj, with_pressure;
 };
 
+template <int TY>
 __global__ void __launch_bounds__(TX *TY) k_correct_df(CorrArgsDF a) {
   using namespace eifdf;
   const int i = 1 + blockIdx.x * TX + threadIdx.x;
@@ -556,8 +561,20 @@ RK rk_coef(int rk) {
   return RK{al[rk], be[rk], al[rk] + be[rk]};
 }
 
-static dim3 cell_grid(const eif_ctx *c) {
-  return dim3((c->itot + TX - 1) / TX, (c->jtot + TY - 1) / TY);
+static dim3 cell_grid(const eif_ctx *c, int ty) {
+  return dim3((c->itot + TX - 1) / TX, (c->jtot + ty - 1) / ty);
+}
+
+// launch of a stencil kernel with the tile height chosen by the tuner (4, 8 or 16 rows)
+template <typename Args>
+static void launch_tiled(void (*k4)(Args), void (*k8)(Args), void (*k16)(Args), int ty, eif_ctx *c, const Args &a) {
+  if (ty == 4) {
+    k4<<<cell_grid(c, 4), dim3(TX, 4), 0, c->stream>>>(a);
+  } else if (ty == 16) {
+    k16<<<cell_grid(c, 16), dim3(TX, 16), 0, c->stream>>>(a);
+  } else {
+    k8<<<cell_grid(c, 8), dim3(TX, 8), 0, c->stream>>>(a);
+  }
 }
 
 int launch_bc_p_like(eif_ctx *c, double *a) {
@@ -602,7 +619,7 @@ static int launch_predictor_mixed(eif_ctx *c, int rk) {
   a.ext = (float)c->cfg.extfrcy;
   a.itot = c->itot; a.jtot = c->jtot; a.ld = c->ld;
   EIF_PROF(c, "predictor", 1);
-  k_predictor_mixed<<<cell_grid(c), dim3(TX, TY), 0, c->stream>>>(a);
+  launch_tiled(k_predictor_mixed<4>, k_predictor_mixed<8>, k_predictor_mixed<16>, c->tiles.pred, c, a);
   EIF_LAUNCH_CK(c);
   c->cur = 1 - c->cur;
   return EIF_OK;
@@ -632,7 +649,7 @@ int launch_predictor(eif_ctx *c, int rk) {
   a.ext = c->cfg.extfrcy;
   a.itot = c->itot; a.jtot = c->jtot; a.ld = c->ld;
   EIF_PROF(c, "predictor", 1);
-  k_predictor<<<cell_grid(c), dim3(TX, TY), 0, c->stream>>>(a);
+  launch_tiled(k_predictor<4>, k_predictor<8>, k_predictor<16>, c->tiles.pred, c, a);
   EIF_LAUNCH_CK(c);
   c->cur = 1 - c->cur;
   return EIF_OK;
@@ -656,7 +673,7 @@ static int launch_corr(eif_ctx *c, int rk, int with_ibm, int with_proj, int with
     a.itot = c->itot; a.jtot = c->jtot; a.ld = c->ld;
     a.with_ibm = with_ibm; a.with_proj = with_proj; a.with_pressure = with_pressure;
     EIF_PROF(c, "correct", 1);
-    k_correct_df<<<cell_grid(c), dim3(TX, TY), 0, c->stream>>>(a);
+    launch_tiled(k_correct_df<4>, k_correct_df<8>, k_correct_df<16>, c->tiles.corr, c, a);
     EIF_LAUNCH_CK(c);
     return EIF_OK;
   }
@@ -674,7 +691,7 @@ static int launch_corr(eif_ctx *c, int rk, int with_ibm, int with_proj, int with
   a.itot = c->itot; a.jtot = c->jtot; a.ld = c->ld;
   a.with_ibm = with_ibm; a.with_proj = with_proj; a.with_pressure = with_pressure;
   EIF_PROF(c, "correct", 1);
-  k_correct<<<cell_grid(c), dim3(TX, TY), 0, c->stream>>>(a);
+  launch_tiled(k_correct<4>, k_correct<8>, k_correct<16>, c->tiles.corr, c, a);
   EIF_LAUNCH_CK(c);
   return EIF_OK;
 }

@@ -1097,7 +1097,7 @@ __global__ void __launch_bounds__(FFT_CTA, 8) k_dct3_dfr(Dct3ArgsDF a, FftShape 
 // diagonally dominant (|c| >= 2 l), so the recurrences carry the pairs' 2^-48
 // relative error without amplification.
 template <int M>
-__global__ void __launch_bounds__(128) k_tdm_local_df(float2 *__restrict__ qhat, const float2 *__restrict__ inv,
+__global__ void __launch_bounds__(256) k_tdm_local_df(float2 *__restrict__ qhat, const float2 *__restrict__ inv,
                                                      const float2 *__restrict__ up, double *__restrict__ iface_a,
                                                      double *__restrict__ first, DF l, int itot, int nblk, int ld) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1442,23 +1442,25 @@ int launch_potential(eif_ctx *c, int rk, bool with_ibm) {
   double *first = pp.ywork + (size_t)pp.nblk * n;
   if (pp.blk > 0) {
     EIF_PROF(c, "poisson_tdm", 2);
-    dim3 g((n + 127) / 128, pp.nblk);
+    // one thread per wavenumber column; the threads per block come from the tuner
+    const int tt = c->tiles.tdm;
+    dim3 g((n + tt - 1) / tt, pp.nblk);
     if (mixed) {
       float2 *qf = reinterpret_cast<float2 *>(c->qhat);
       const DF ldf = dfpair(l);
       if (pp.blk == 16) {
-        k_tdm_local_df<16><<<g, 128, 0, c->stream>>>(qf, pp.tdm_inv_df, pp.tdm_up_df, iface, first, ldf, n, pp.nblk, c->ld);
+        k_tdm_local_df<16><<<g, tt, 0, c->stream>>>(qf, pp.tdm_inv_df, pp.tdm_up_df, iface, first, ldf, n, pp.nblk, c->ld);
       } else if (pp.blk == 8) {
-        k_tdm_local_df<8><<<g, 128, 0, c->stream>>>(qf, pp.tdm_inv_df, pp.tdm_up_df, iface, first, ldf, n, pp.nblk, c->ld);
+        k_tdm_local_df<8><<<g, tt, 0, c->stream>>>(qf, pp.tdm_inv_df, pp.tdm_up_df, iface, first, ldf, n, pp.nblk, c->ld);
       } else {
-        k_tdm_local_df<4><<<g, 128, 0, c->stream>>>(qf, pp.tdm_inv_df, pp.tdm_up_df, iface, first, ldf, n, pp.nblk, c->ld);
+        k_tdm_local_df<4><<<g, tt, 0, c->stream>>>(qf, pp.tdm_inv_df, pp.tdm_up_df, iface, first, ldf, n, pp.nblk, c->ld);
       }
     } else if (pp.blk == 16) {
-      k_tdm_local<16><<<g, 128, 0, c->stream>>>(c->qhat, pp.tdm_inv, pp.tdm_up, iface, first, l, n, pp.nblk, c->ld);
+      k_tdm_local<16><<<g, tt, 0, c->stream>>>(c->qhat, pp.tdm_inv, pp.tdm_up, iface, first, l, n, pp.nblk, c->ld);
     } else if (pp.blk == 8) {
-      k_tdm_local<8><<<g, 128, 0, c->stream>>>(c->qhat, pp.tdm_inv, pp.tdm_up, iface, first, l, n, pp.nblk, c->ld);
+      k_tdm_local<8><<<g, tt, 0, c->stream>>>(c->qhat, pp.tdm_inv, pp.tdm_up, iface, first, l, n, pp.nblk, c->ld);
     } else {
-      k_tdm_local<4><<<g, 128, 0, c->stream>>>(c->qhat, pp.tdm_inv, pp.tdm_up, iface, first, l, n, pp.nblk, c->ld);
+      k_tdm_local<4><<<g, tt, 0, c->stream>>>(c->qhat, pp.tdm_inv, pp.tdm_up, iface, first, l, n, pp.nblk, c->ld);
     }
     EIF_LAUNCH_CK(c);
     if (pp.g2 > 0) {

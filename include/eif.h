@@ -135,6 +135,15 @@ void *eif_batch_stream(eif_batch *batch);
 const char *eif_batch_last_error(const eif_batch *batch);
 int eif_batch_destroy(eif_batch *batch);
 
+/* Tile shapes of the stencil and block-Thomas kernels: the tuner times the
+ * candidates (tiles of 32 columns by 4, 8 or 16 rows for the predictor and the
+ * projection; 64, 128 or 256 threads per block of the block Thomas) once per grid
+ * size and precision, before the first eif_integrate / eif_advance / batch capture,
+ * and keeps the fastest. The shapes do not change any result. EIF_TUNE=0 in the
+ * environment keeps the defaults (8, 8, 128). tiles[4]: predictor rows, projection
+ * rows, Thomas threads, 1 if tuned. No counterpart in the reference. */
+int eif_tiles(eif_ctx *ctx, int *tiles);
+
 /* ---- discrete adjoint of the step (no counterpart in the reference) ----
  * Transposed linearisation of integrate (src/main.c:13-55) in the double-precision
  * form with dt held at the value eif_set_dt / eif_decide_dt left on the device.
