@@ -210,6 +210,13 @@ def run_ours(args, world, rank, local, pg):
     sim.synchronize()
     sim._call("profile_enable", sim.ctx, 0)
     prof = profile_entries(sim)
+    # ---- the logging reductions of one log event (divergence, momentum, energy) on
+    # the device, against pulling the two velocity fields for a host reduction ----
+    sim.log_quantities()
+    t0 = time.perf_counter()
+    for _ in range(5):
+        sim.log_quantities()
+    log_ms = (time.perf_counter() - t0) * 1e3 / 5
     # ---- end-to-end through the public API with host buffers ----
     e2e = None
     if not args.no_e2e:
@@ -233,6 +240,7 @@ def run_ours(args, world, rank, local, pg):
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "e2e": e2e, "roofline": roof, "gpu_launches": launches,
         "fp64_form": fp64, "accuracy_vs_fp64": accuracy,
+        "log_reductions_ms": log_ms,
         "clocks": clk.summary(),
         "kernels_per_step": {e["name"]: {"launches": round(e["launches"] / prof_steps, 2),
                                          "ms": round(e["ms"] / prof_steps, 4)} for e in prof},

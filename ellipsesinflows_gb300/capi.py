@@ -109,6 +109,9 @@ def bind(lib, prefix):
         "increment_particles": [_vp, ctypes.c_int, _dp],
         "update_particles": [_vp],
         "divergence": [_vp, _dp, _dp],
+        "momentum": [_vp, _dp],
+        "energy": [_vp, _dp],
+        "log_quantities": [_vp, _dp],
         "set_threads": [_vp, ctypes.c_int],
         "tiles": [_vp, _ip],
         "adjoint_begin": [_vp, ctypes.c_int, ctypes.c_int],
@@ -318,6 +321,22 @@ class Solver:
         mx, sm = ctypes.c_double(), ctypes.c_double()
         self._call("divergence", self.ctx, ctypes.byref(mx), ctypes.byref(sm))
         return mx.value, sm.value
+
+    def momentum(self):
+        m = (ctypes.c_double * 2)()
+        self._call("momentum", self.ctx, m)
+        return m[0], m[1]
+
+    def energy(self):
+        e = (ctypes.c_double * 2)()
+        self._call("energy", self.ctx, e)
+        return e[0], e[1]
+
+    def log_quantities(self):
+        """{divmax, divsum, momentum (x, y), energy (x, y)} in one call"""
+        q = (ctypes.c_double * 6)()
+        self._call("log_quantities", self.ctx, q)
+        return {"divmax": q[0], "divsum": q[1], "momentum": (q[2], q[3]), "energy": (q[4], q[5])}
 
     # ---- stage-level entry points ----
     def update_boundaries(self):

@@ -307,6 +307,11 @@ int device_metrics(eif_ctx *c) {
   if ((rc = upload(c, &c->rdxf, rdxf))) return rc;
   if ((rc = upload(c, &c->rdxc, rdxc))) return rc;
   if ((rc = upload(c, &c->dxc, dxc))) return rc;
+  {
+    std::vector<double> dxf(itot + 2, 0.);
+    for (int i = 1; i <= itot; i++) dxf[i] = DXF(i);
+    if ((rc = upload(c, &c->dxf, dxf))) return rc;
+  }
   if ((rc = upload(c, &c->cxm, cxm))) return rc;
   if ((rc = upload(c, &c->cxp, cxp))) return rc;
   if ((rc = upload(c, &c->cym, cym))) return rc;
@@ -466,7 +471,7 @@ int eif_destroy(eif_ctx *c) {
   if (c->adj) eif_adjoint_end(c);
   double *ptrs[] = {c->ux[0], c->ux[1], c->uy[0], c->uy[1], c->p, c->psi, c->sxa[0], c->sxa[1], c->sya[0],
                     c->sya[1], c->dux, c->duy, c->qhat, c->xc, c->yc, c->rdxf, c->rdxc, c->cxm, c->cxp, c->cym,
-                    c->cyp, c->dxc, c->P, c->d_scal};
+                    c->cyp, c->dxc, c->dxf, c->P, c->d_scal};
   for (double *p : ptrs) if (p) cudaFree(p);
   if (c->d_coef) cudaFree(c->d_coef);
   if (c->cpf) cudaFree(c->cpf);
@@ -825,6 +830,33 @@ int eif_update_particles(eif_ctx *c) { return c ? launch_update_particles(c) : E
 int eif_divergence(eif_ctx *c, double *divmax, double *divsum) {
   if (!c || !divmax || !divsum) return EIF_ERR_ARG;
   return launch_divergence(c, divmax, divsum);
+}
+
+int eif_momentum(eif_ctx *c, double *moms) {
+  if (!c || !moms) return EIF_ERR_ARG;
+  double q[4];
+  int rc = launch_field_sums(c, q);
+  if (rc) return rc;
+  moms[0] = q[0];
+  moms[1] = q[1];
+  return EIF_OK;
+}
+
+int eif_energy(eif_ctx *c, double *energy) {
+  if (!c || !energy) return EIF_ERR_ARG;
+  double q[4];
+  int rc = launch_field_sums(c, q);
+  if (rc) return rc;
+  energy[0] = q[2];
+  energy[1] = q[3];
+  return EIF_OK;
+}
+
+int eif_log_quantities(eif_ctx *c, double *q) {
+  if (!c || !q) return EIF_ERR_ARG;
+  int rc = launch_field_sums(c, q + 2);
+  if (rc) return rc;
+  return launch_divergence(c, q, q + 1);
 }
 
 }  // extern "C"

@@ -122,6 +122,7 @@ struct eif_ctx {
   double *rdxf, *rdxc;          // 1/DXF(i), 1/DXC(i) at [i]
   double *cxm, *cxp, *cym, *cyp;// stencil interpolation weights at [i]
   double *dxc;                  // DXC(i) at [i]
+  double *dxf = nullptr;        // DXF(i) at [i]
   float *rdxf_f, *rdxc_f, *cxm_f, *cxp_f, *cym_f, *cyp_f;  // single-precision copies
   float2 *rdxc_df = nullptr;    // 1/dxc as double-float pairs (hi, lo)
   float *sxf[2], *syf[2];       // RK explicit terms of the mixed form
@@ -269,6 +270,8 @@ struct AdjPass {
   double *part = nullptr, *out = nullptr, *fx = nullptr, *fy = nullptr;
 };
 int launch_adj_pass(eif_ctx *c, const AdjPass &p);
+// logging.c:87-172: q[0..1] x/y momentum, q[2..3] x/y kinetic energy (synchronising)
+int launch_field_sums(eif_ctx *c, double *q);
 // choose c->tiles by timing the candidate shapes on scratch copies of the fields
 // (once per context; results are cached per grid size and precision); not during capture
 int tune_tiles(eif_ctx *c);

@@ -526,14 +526,15 @@ __global__ void k_dt_final(const double *__restrict__ part, int nparts, double d
 __global__ void k_coef(const double *__restrict__ dt, float *__restrict__ coef) { write_coef(*dt, coef); }
 
 // ---------------------------------------------------------------------------
-__global__ void k_divergence(const double *__restrict__ ux, const double *__restrict__ uy, const double *__restrict__ rdxf,
-                             double rdy, int itot, int jtot, int ld, double *__restrict__ out /* per block: max, sum */) {
+// check_divergence (logging.c:52-65): (UX(i+1) - UX(i)) / DXF(i) + (UY(j+1) - UY(j)) / dy
+__global__ void k_divergence(const double *__restrict__ ux, const double *__restrict__ uy, const double *__restrict__ dxf,
+                             double dy, int itot, int jtot, int ld, double *__restrict__ out /* per block: max, sum */) {
   double mx = 0., sm = 0.;
   const int n = itot * jtot;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
     const int i = 1 + t % itot, j = 1 + t / itot;
-    const double d = (ux[ux_idx(i + 1, j, ld)] - ux[ux_idx(i, j, ld)]) * rdxf[i] +
-                     (uy[uy_idx(i, j + 1, ld)] - uy[uy_idx(i, j, ld)]) * rdy;
+    const double d = (ux[ux_idx(i + 1, j, ld)] - ux[ux_idx(i, j, ld)]) / dxf[i] +
+                     (uy[uy_idx(i, j + 1, ld)] - uy[uy_idx(i, j, ld)]) / dy;
     mx = fmax(mx, fabs(d));
     sm += d;
   }
@@ -550,9 +551,67 @@ __global__ void k_divergence(const double *__restrict__ ux, const double *__rest
   }
 }
 
+// Sums of the logging diagnostics (logging.c:87-172) over the interior rows: x momentum
+// and energy over the faces i = 1..itot+1 with the cell size DXC(i) dy, y momentum and
+// energy over the cells i = 1..itot with DXF(i) dy. One partial sum of each per block,
+// in a fixed grid-stride order; the host adds the partials in block order.
+constexpr int FS_BLOCKS = 296, FS_THREADS = 256;
+__global__ void __launch_bounds__(FS_THREADS) k_field_sums(const double *__restrict__ ux,
+                                                          const double *__restrict__ uy,
+                                                          const double *__restrict__ dxc,
+                                                          const double *__restrict__ dxf, double dy, int itot,
+                                                          int jtot, int ld, double *__restrict__ out) {
+  double s[4] = {0., 0., 0., 0.};
+  const long long nx = (long long)(itot + 1) * jtot, ny = (long long)itot * jtot;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nx; t += (long long)gridDim.x * blockDim.x) {
+    const int i = 1 + (int)(t % (itot + 1)), j = 1 + (int)(t / (itot + 1));
+    const double u = ux[ux_idx(i, j, ld)];
+    const double cs = dxc[i] * dy;
+    s[0] += u * cs;
+    s[2] += 0.5 * (u * u) * cs;
+  }
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ny; t += (long long)gridDim.x * blockDim.x) {
+    const int i = 1 + (int)(t % itot), j = 1 + (int)(t / itot);
+    const double v = uy[uy_idx(i, j, ld)];
+    const double cs = dxf[i] * dy;
+    s[1] += v * cs;
+    s[3] += 0.5 * (v * v) * cs;
+  }
+  __shared__ double sh[4][FS_THREADS / 32];
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const double v = eifd::warp_sum(s[k]);
+    if (l == 0) sh[k][w] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 4) {
+    double v = 0.;
+    for (int q = 0; q < FS_THREADS / 32; q++) v += sh[threadIdx.x][q];
+    out[4 * blockIdx.x + threadIdx.x] = v;
+  }
+}
+
 }  // namespace
 
 namespace eif {
+
+int launch_field_sums(eif_ctx *c, double *q) {
+  double *part = c->qhat;  // scratch: 4 per block
+  EIF_PROF(c, "field_sums", 1);
+  k_field_sums<<<FS_BLOCKS, FS_THREADS, 0, c->stream>>>(c->ux[c->cur], c->uy[c->cur], c->dxc, c->dxf, c->dy, c->itot,
+                                                        c->jtot, c->ld, part);
+  EIF_LAUNCH_CK(c);
+  double h[4 * FS_BLOCKS];
+  EIF_CK(c, cudaMemcpyAsync(h, part, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  EIF_CK(c, cudaStreamSynchronize(c->stream));
+  for (int k = 0; k < 4; k++) {
+    double v = 0.;
+    for (int b = 0; b < FS_BLOCKS; b++) v += h[4 * b + k];
+    q[k] = v;
+  }
+  return EIF_OK;
+}
 
 RK rk_coef(int rk) {
   // src/param/init.c:177-189
@@ -727,8 +786,8 @@ int launch_divergence(eif_ctx *c, double *divmax, double *divsum) {
   const int blocks = c->sms * 2;
   double *part = c->qhat;  // scratch
   EIF_PROF(c, "divergence", 1);
-  k_divergence<<<blocks, 256, 0, c->stream>>>(c->ux[c->cur], c->uy[c->cur], c->rdxf, 1. / c->dy, c->itot, c->jtot,
-                                               c->ld, part);
+  k_divergence<<<blocks, 256, 0, c->stream>>>(c->ux[c->cur], c->uy[c->cur], c->dxf, c->dy, c->itot, c->jtot, c->ld,
+                                               part);
   EIF_LAUNCH_CK(c);
   double *h = new double[2 * blocks];
   cudaError_t e = cudaMemcpyAsync(h, part, sizeof(double) * 2 * blocks, cudaMemcpyDeviceToHost, c->stream);

@@ -237,8 +237,19 @@ int eif_decide_dt_noalloc(const double *ux, int ux_pitch, const double *uy, int 
  * at all (f2d). */
 int eif_selftest_conversions(int device, int n, long long *d2f_mismatch, long long *f2d_mismatch);
 
-/* ---- diagnostics (src/logging.c:40-80) ---- */
+/* ---- diagnostics: the reductions of the reference's logging (src/logging.c:40-172),
+ * on the device, so that a log event needs no field pull ----
+ * divergence: max |div u| and the sum of div u over the cells (check_divergence, :40-85)
+ * momentum:   moms[0] = sum UX(i,j) DXC(i) dy over i = 1..itot+1, moms[1] = sum UY DXF dy
+ *             over i = 1..itot (check_momentum, :87-128)
+ * energy:     the same sums of UX^2/2 and UY^2/2 (check_energy, :130-172)
+ * log_quantities: q[6] = {divmax, divsum, mom_x, mom_y, energy_x, energy_y}
+ * Sums are accumulated in a fixed order (deterministic), not in the reference's loop
+ * order: they agree with it to rounding (relative 1e-14 at 2048 x 4096). */
 int eif_divergence(eif_ctx *ctx, double *divmax, double *divsum);
+int eif_momentum(eif_ctx *ctx, double *moms);
+int eif_energy(eif_ctx *ctx, double *energy);
+int eif_log_quantities(eif_ctx *ctx, double *q);
 
 /* ---- kernel timing (no counterpart in the reference, which only times the
  * whole run with MPI_Wtime, src/main.c:60-61,97-105) ----

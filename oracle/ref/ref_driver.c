@@ -205,6 +205,15 @@ int ref_get_grid(const ref_ctx *c, double *xf, double *xc, double *dxf, double *
   return 0;
 }
 
+/* the reference's own logging() (src/logging.c:197-208): writes output/log/*.dat under
+ * the current directory for the given step, time and log rate */
+int ref_logging(ref_ctx *c, int step, double time, double log_rate){
+  c->param->step = step;
+  c->param->time = time;
+  c->param->log.rate = log_rate;
+  return logging(c->param, c->parallel, c->fluid, c->suspensions);
+}
+
 double ref_decide_dt(ref_ctx *c){
   param_decide_dt(c->param, c->parallel, c->fluid, c->suspensions);
   return c->param->dt;
