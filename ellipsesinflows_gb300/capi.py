@@ -114,6 +114,8 @@ def bind(lib, prefix):
         "log_quantities": [_vp, _dp],
         "set_threads": [_vp, ctypes.c_int],
         "tiles": [_vp, _ip],
+        "snapshot_take": [_vp],
+        "snapshot_wait": [_vp, _dp, _dp, _dp, ctypes.c_int, _dp, _ip, _dp],
         "adjoint_begin": [_vp, ctypes.c_int, ctypes.c_int],
         "adjoint_seed_particles": [_vp, ctypes.c_int, _dp],
         "adjoint_pull_particles": [_vp, ctypes.c_int, _dp],
@@ -376,6 +378,22 @@ class Solver:
 
     def update_particles(self):
         self._call("update_particles", self.ctx)
+
+    def snapshot_take(self):
+        """start an asynchronous copy of the state (eif_snapshot_take)"""
+        self._call("snapshot_take", self.ctx)
+        self._snap_n = self.n_particles
+
+    def snapshot_wait(self):
+        """(ux, uy, p, records, step, time) of the last snapshot (eif_snapshot_wait)"""
+        sx, sy = self.shapes()
+        ux, uy, p = np.empty(sx), np.empty(sy), np.empty(sy)
+        n = getattr(self, "_snap_n", self.n_particles)
+        rec = np.zeros((max(n, 1), NFIELDS))
+        step, time = ctypes.c_int(), ctypes.c_double()
+        self._call("snapshot_wait", self.ctx, _ptr(ux), _ptr(uy), _ptr(p), n, _ptr(rec), ctypes.byref(step),
+                   ctypes.byref(time))
+        return ux, uy, p, rec[:n], step.value, time.value
 
     def tiles(self):
         """tile shapes chosen by the tuner: {"predictor_rows", "projection_rows",

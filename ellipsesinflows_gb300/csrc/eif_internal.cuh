@@ -88,6 +88,7 @@ struct PoissonPlan {
 };
 
 struct Adjoint;  // adjoint.cu
+struct Snapshot;  // snapshot.cu
 }  // namespace eif
 
 struct eif_ctx {
@@ -108,6 +109,7 @@ struct eif_ctx {
   const double *adj_rhs = nullptr;
   bool ibm_weights_only = false;
   eif::Adjoint *adj = nullptr;
+  eif::Snapshot *snap = nullptr;  // asynchronous checkpoint copies (snapshot.cu)
   // fields
   double *ux[2], *uy[2];
   int cur;                      // index of the current velocity buffer
@@ -275,6 +277,7 @@ int launch_field_sums(eif_ctx *c, double *q);
 // choose c->tiles by timing the candidate shapes on scratch copies of the fields
 // (once per context; results are cached per grid size and precision); not during capture
 int tune_tiles(eif_ctx *c);
+void snapshot_free(eif_ctx *c);
 int adj_chunk_cap(const eif_ctx *c);
 int sub_iteration(eif_ctx *c, int rk);
 bool overlap_on(const eif_ctx *c);

@@ -135,6 +135,18 @@ void *eif_batch_stream(eif_batch *batch);
 const char *eif_batch_last_error(const eif_batch *batch);
 int eif_batch_destroy(eif_batch *batch);
 
+/* ---- asynchronous snapshots for checkpoints (the state save() writes,
+ * src/save.c:109-122) ----
+ * take: copies ux, uy, p and the particle records on the device, in order with the
+ * steps, and starts their transfer to page-locked host memory on a stream of its own:
+ * steps launched afterwards overlap with the transfer.
+ * wait: waits for the transfer and writes the snapshot in the eif_push_fluid layouts
+ * (any pointer may be NULL) and n records (n = the particle count at take), with the
+ * step and time at take. A new take waits for the previous transfer. */
+int eif_snapshot_take(eif_ctx *ctx);
+int eif_snapshot_wait(eif_ctx *ctx, double *ux, double *uy, double *p, int n, double *records, int *step,
+                      double *time);
+
 /* Tile shapes of the stencil and block-Thomas kernels: the tuner times the
  * candidates (tiles of 32 columns by 4, 8 or 16 rows for the predictor and the
  * projection; 64, 128 or 256 threads per block of the block Thomas) once per grid

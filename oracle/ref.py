@@ -51,6 +51,7 @@ def _lib(variant):
         lib.ref_get_step.argtypes = [vp]
         lib.ref_get_grid.argtypes = [vp] + [_dp] * 6
         lib.ref_logging.argtypes = [vp, ctypes.c_int, ctypes.c_double, ctypes.c_double]
+        lib.ref_save.argtypes = [vp, ctypes.c_int, ctypes.c_double]
         lib.ref_decide_dt.restype = ctypes.c_double
         lib.ref_decide_dt.argtypes = [vp]
         lib.ref_integrate.argtypes = [vp]

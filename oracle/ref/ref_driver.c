@@ -214,6 +214,14 @@ int ref_logging(ref_ctx *c, int step, double time, double log_rate){
   return logging(c->param, c->parallel, c->fluid, c->suspensions);
 }
 
+/* the reference's own save() (src/save.c:109-122): writes output/save/step%010d/*.npy
+ * under the current directory for the given step and time */
+int ref_save(ref_ctx *c, int step, double time){
+  c->param->step = step;
+  c->param->time = time;
+  return save(c->param, c->parallel, c->fluid, c->suspensions);
+}
+
 double ref_decide_dt(ref_ctx *c){
   param_decide_dt(c->param, c->parallel, c->fluid, c->suspensions);
   return c->param->dt;
