@@ -114,6 +114,9 @@ def bind(lib, prefix):
         "log_quantities": [_vp, _dp],
         "set_threads": [_vp, ctypes.c_int],
         "tiles": [_vp, _ip],
+        "stats_reset": [_vp],
+        "stats_collect": [_vp],
+        "stats_pull": [_vp, _dp, _dp, _dp, _dp, _dp, _ip],
         "snapshot_take": [_vp],
         "snapshot_wait": [_vp, _dp, _dp, _dp, ctypes.c_int, _dp, _ip, _dp],
         "adjoint_begin": [_vp, ctypes.c_int, ctypes.c_int],
@@ -378,6 +381,20 @@ class Solver:
 
     def update_particles(self):
         self._call("update_particles", self.ctx)
+
+    def stats_reset(self):
+        self._call("stats_reset", self.ctx)
+
+    def stats_collect(self):
+        self._call("stats_collect", self.ctx)
+
+    def stats_pull(self):
+        """(ux1, ux2, uy1, uy2, phi, num): the accumulated sums (eif_stats_pull)"""
+        sx, sy = self.shapes()
+        arrs = [np.zeros(sx), np.zeros(sx), np.zeros(sy), np.zeros(sy), np.zeros(sy)]
+        num = ctypes.c_int()
+        self._call("stats_pull", self.ctx, *[_ptr(a) for a in arrs], ctypes.byref(num))
+        return tuple(arrs) + (num.value,)
 
     def snapshot_take(self):
         """start an asynchronous copy of the state (eif_snapshot_take)"""

@@ -470,6 +470,7 @@ int eif_destroy(eif_ctx *c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->adj) eif_adjoint_end(c);
   snapshot_free(c);
+  stats_free(c);
   double *ptrs[] = {c->ux[0], c->ux[1], c->uy[0], c->uy[1], c->p, c->psi, c->sxa[0], c->sxa[1], c->sya[0],
                     c->sya[1], c->dux, c->duy, c->qhat, c->xc, c->yc, c->rdxf, c->rdxc, c->cxm, c->cxp, c->cym,
                     c->cyp, c->dxc, c->dxf, c->P, c->d_scal};

@@ -89,6 +89,7 @@ struct PoissonPlan {
 
 struct Adjoint;  // adjoint.cu
 struct Snapshot;  // snapshot.cu
+struct Stats;     // stats.cu
 }  // namespace eif
 
 struct eif_ctx {
@@ -110,6 +111,7 @@ struct eif_ctx {
   bool ibm_weights_only = false;
   eif::Adjoint *adj = nullptr;
   eif::Snapshot *snap = nullptr;  // asynchronous checkpoint copies (snapshot.cu)
+  eif::Stats *stats = nullptr;    // time-averaged statistics (stats.cu)
   // fields
   double *ux[2], *uy[2];
   int cur;                      // index of the current velocity buffer
@@ -278,6 +280,7 @@ int launch_field_sums(eif_ctx *c, double *q);
 // (once per context; results are cached per grid size and precision); not during capture
 int tune_tiles(eif_ctx *c);
 void snapshot_free(eif_ctx *c);
+void stats_free(eif_ctx *c);
 int adj_chunk_cap(const eif_ctx *c);
 int sub_iteration(eif_ctx *c, int rk);
 bool overlap_on(const eif_ctx *c);

@@ -135,6 +135,16 @@ void *eif_batch_stream(eif_batch *batch);
 const char *eif_batch_last_error(const eif_batch *batch);
 int eif_batch_destroy(eif_batch *batch);
 
+/* ---- time-averaged statistics (src/statistics/collect.c:10-95) on the device ----
+ * collect adds ux, ux^2 (faces 1..itot+1), uy, uy^2 (i = 0..itot+1) and the sharp
+ * particle indicator phi (cells) of the current state to device accumulators and
+ * counts the collect (asynchronous); reset zeroes them; pull copies them out in the
+ * reference's layouts (include/arrays/statistics.h; ux-like (jtot+2) x (itot+1),
+ * uy-like and phi (jtot+2) x (itot+2), halo rows zero) with the number of collects. */
+int eif_stats_reset(eif_ctx *ctx);
+int eif_stats_collect(eif_ctx *ctx);
+int eif_stats_pull(eif_ctx *ctx, double *ux1, double *ux2, double *uy1, double *uy2, double *phi, int *num);
+
 /* ---- asynchronous snapshots for checkpoints (the state save() writes,
  * src/save.c:109-122) ----
  * take: copies ux, uy, p and the particle records on the device, in order with the

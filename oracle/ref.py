@@ -52,6 +52,8 @@ def _lib(variant):
         lib.ref_get_grid.argtypes = [vp] + [_dp] * 6
         lib.ref_logging.argtypes = [vp, ctypes.c_int, ctypes.c_double, ctypes.c_double]
         lib.ref_save.argtypes = [vp, ctypes.c_int, ctypes.c_double]
+        lib.ref_stats_collect.argtypes = [vp]
+        lib.ref_stats_output.argtypes = [vp, ctypes.c_int, ctypes.c_double]
         lib.ref_decide_dt.restype = ctypes.c_double
         lib.ref_decide_dt.argtypes = [vp]
         lib.ref_integrate.argtypes = [vp]

@@ -222,6 +222,24 @@ int ref_save(ref_ctx *c, int step, double time){
   return save(c->param, c->parallel, c->fluid, c->suspensions);
 }
 
+/* the reference's statistics (src/statistics/): statistics_init on first use,
+ * statistics_collect on the current state, statistics_output (writes
+ * output/stat/step%010d/ under the current directory) for the given step and time */
+static statistics_t *ref_stats = NULL;
+int ref_stats_collect(ref_ctx *c){
+  if(!ref_stats) ref_stats = statistics_init(c->param, c->parallel);
+  return statistics_collect(c->param, c->parallel, c->fluid, c->suspensions, ref_stats);
+}
+int ref_stats_output(ref_ctx *c, int step, double time){
+  if(!ref_stats) return 1;
+  c->param->step = step;
+  c->param->time = time;
+  int rc = statistics_output(c->param, c->parallel, ref_stats);
+  statistics_finalise(ref_stats);
+  ref_stats = NULL;
+  return rc;
+}
+
 double ref_decide_dt(ref_ctx *c){
   param_decide_dt(c->param, c->parallel, c->fluid, c->suspensions);
   return c->param->dt;
