@@ -17,7 +17,10 @@ BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libeif_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# host code: no contraction into fused multiply-adds (the default of gcc on Arm), so that
+# host arithmetic gives the same bits on the x86 build machine and the Arm GPU hosts
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+              "-Xcompiler", "-ffp-contract=off",
               "--expt-relaxed-constexpr", "-I" + CSRC, "-I" + os.path.join(ROOT, "include")]
 
 
