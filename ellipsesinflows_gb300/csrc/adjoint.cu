@@ -55,6 +55,10 @@ struct Adjoint {
   double *xb = nullptr, *vpb = nullptr, *dub = nullptr, *fb = nullptr, *i0b = nullptr, *i1b = nullptr;
   double *pout = nullptr, *part = nullptr;
   int part_cap = 0;
+  // indicator geometry of the box cells at X, shared by the three transposed evaluations
+  // at X of a stage (last sub-iteration, exchange, inertia at the stage start)
+  double *geom = nullptr;
+  size_t geom_cap = 0;
   // wall-velocity cotangent: per row (2 x jtot) and accumulated (2)
   double *wall_rows = nullptr, *wall = nullptr;
   double *pbackup = nullptr;   // particle records during backward
@@ -409,7 +413,7 @@ void adj_free(eif_ctx *c) {
     for (double *p : *v)
       if (p) cudaFree(p);
   for (double *p : {a->ub, a->vb, a->pb, a->abx, a->aby, a->tu, a->tv, a->rhs, a->w, a->fcx, a->fcy, a->gcx, a->gcy, a->xb, a->vpb,
-                    a->dub, a->fb, a->i0b, a->i1b, a->pout, a->part, a->wall_rows, a->wall, a->pbackup})
+                    a->dub, a->fb, a->i0b, a->i1b, a->pout, a->part, a->wall_rows, a->wall, a->pbackup, a->geom})
     if (p) cudaFree(p);
   if (a->d_contact) cudaFree(a->d_contact);
   delete a;
@@ -739,6 +743,12 @@ int eif_adjoint_backward(eif_ctx *c) {
       a->part_cap = adj_chunk_cap(c);
       EIF_CK(c, cudaMalloc((void **)&a->part, sizeof(double) * 6 * a->part_cap));
     }
+    if (adj_slot_cap(c) > a->geom_cap) {
+      if (a->geom) cudaFree(a->geom);
+      a->geom = nullptr;
+      a->geom_cap = adj_slot_cap(c);
+      EIF_CK(c, cudaMalloc((void **)&a->geom, sizeof(double) * 3 * a->geom_cap));
+    }
     EIF_CK(c, cudaMemcpyAsync(a->pbackup, c->P, sizeof(double) * EIF_NFIELDS * c->pcap, cudaMemcpyDeviceToDevice,
                               c->stream));
   }
@@ -772,6 +782,8 @@ int eif_adjoint_backward(eif_ctx *c) {
         k_adj_dxload<<<pblocks(np), 128, 0, c->stream>>>(c->P, c->pcap, np, a->tape_dx[slot] + (size_t)3 * np * m);
         EIF_LAUNCH_CK(c);
         pass.use_increment = m > 0;
+        pass.geo = m == 0 ? 1 : 0;   // the pass at X keeps the geometry for the two below
+        pass.geom = a->geom;
         if ((rc = launch_adj_pass(c, pass))) return rc;
         k_adj_avgT_add<<<G, B, 0, c->stream>>>(a->fcx, a->fcy, a->ub, a->vb, c->itot, c->jtot, c->ld);
         EIF_LAUNCH_CK(c);
@@ -780,8 +792,7 @@ int eif_adjoint_backward(eif_ctx *c) {
       }
       k_adj_dxload<<<pblocks(np), 128, 0, c->stream>>>(c->P, c->pcap, np, a->tape_dx[slot]);   // dX_0 = 0
       EIF_LAUNCH_CK(c);
-      c->boxes_x_valid = false;
-      c->bands_x_valid = false;
+      // the boxes of the last pass (m = 0) are those at X, kept for the passes below
     }
     // projection: phi = L^-1 (D ubar' + pbar' / (g dt)), ubar** = ubar' - G phi
     k_adj_rhs<<<G, B, 0, c->stream>>>(a->ub, a->vb, a->pb, a->rhs, 1. / c->dx, 1. / c->dy, 1. / gdt, c->itot, c->jtot,
@@ -799,6 +810,7 @@ int eif_adjoint_backward(eif_ctx *c) {
       EIF_LAUNCH_CK(c);
       pass.mode = 1;
       pass.use_increment = false;
+      pass.geo = a->tape_k[slot] > 0 ? 2 : 0;
       pass.ux = a->tape_us[slot];
       pass.uy = a->tape_vs[slot];
       pass.bar = a->fb;
@@ -838,6 +850,7 @@ int eif_adjoint_backward(eif_ctx *c) {
     if (coupled && np > 0) {
       pass.mode = 0;
       pass.use_increment = false;
+      pass.geo = a->tape_k[slot] > 0 ? 2 : 0;
       pass.ux = a->tape_u[slot];
       pass.uy = a->tape_v[slot];
       pass.bar = a->i0b;

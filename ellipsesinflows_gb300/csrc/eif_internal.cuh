@@ -267,12 +267,18 @@ int launch_band_lists(eif_ctx *c);
 // (mode 1); gx, gy (mode 1) the cell cotangents of the field response. Writes
 // out (6 x np: cotangents of x, y, az, ux, uy, vz) and the cell cotangents of the
 // face-averaged velocity into fx, fy (interior cells).
+// geo: 0 evaluates the indicator geometry of every box cell, 1 evaluates and stores it
+// per task slot in geom (3 doubles per slot: tanh(2D), the x and y components of the
+// gradient of D), 2 reads it back (same boxes and positions)
 struct AdjPass {
   int mode = 0;
   bool use_increment = false;
   const double *ux = nullptr, *uy = nullptr, *bar = nullptr, *gx = nullptr, *gy = nullptr;
   double *part = nullptr, *out = nullptr, *fx = nullptr, *fy = nullptr;
+  int geo = 0;
+  double *geom = nullptr;
 };
+size_t adj_slot_cap(const eif_ctx *c);
 int launch_adj_pass(eif_ctx *c, const AdjPass &p);
 // logging.c:87-172: q[0..1] x/y momentum, q[2..3] x/y kinetic energy (synchronising)
 int launch_field_sums(eif_ctx *c, double *q);

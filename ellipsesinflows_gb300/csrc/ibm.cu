@@ -1461,6 +1461,9 @@ struct AdjWorkArgs {
   const double *gx, *gy;    // mode 1: cell cotangents of the field response
   double *part;             // 6 per task
   double2 *wbuf;
+  double *geom;             // geo 1/2: per task slot th, gwx, gwy (3 x slots, by component)
+  long long nslot;
+  int geo;
   int pcap, np, ld, mode, use_increment;
   double dx, dy, ly, h;
   Bounds bd;
@@ -1517,7 +1520,13 @@ __global__ void __launch_bounds__(256) k_ibm_adj(AdjWorkArgs a) {
         // is +-1 in double precision and both weights' derivatives vanish
         const double rho = sqrt((qx / pa) * (qx / pa) + (qy / pb) * (qy / pb));
         double th, gwx = 0., gwy = 0.;
-        if (mn * fabs(rho - 1.) * rh >= FAR_CELLS_D) {
+        const long long slot = (long long)c * CHUNK + half * 32 + lane;
+        const bool cached = a.geo == 2 && EIF_CHK(a.bd.rec, slot, a.nslot, 81);
+        if (cached) {
+          th = a.geom[slot];
+          gwx = a.geom[a.nslot + slot];
+          gwy = a.geom[2 * a.nslot + slot];
+        } else if (mn * fabs(rho - 1.) * rh >= FAR_CELLS_D) {
           th = rho < 1. ? 1. : -1.;
         } else {
           const double f0 = 1. - (qx / pa) * (qx / pa) - (qy / pb) * (qy / pb);
@@ -1536,6 +1545,11 @@ __global__ void __launch_bounds__(256) k_ibm_adj(AdjWorkArgs a) {
           // g = R(az) dD/dq with cz = cos(-az), sz = sin(-az)
           gwx = e.cz * gbx + e.sz * gby;
           gwy = -e.sz * gbx + e.cz * gby;
+        }
+        if (a.geo == 1 && EIF_CHK(a.bd.rec, slot, a.nslot, 82)) {
+          a.geom[slot] = th;
+          a.geom[a.nslot + slot] = gwx;
+          a.geom[2 * a.nslot + slot] = gwy;
         }
         const double ws = 0.5 * BETA * (1. - th * th);
         const double uxf = 0.5 * (__ldg(a.ux + j * ld + (i - 1)) + __ldg(a.ux + j * ld + i));
@@ -1619,6 +1633,9 @@ int launch_adj_pass(eif_ctx *c, const AdjPass &p) {
   w.bar = p.bar; w.gx = p.gx; w.gy = p.gy;
   w.part = p.part;
   w.wbuf = reinterpret_cast<double2 *>(c->wbuf);
+  w.geom = p.geom;
+  w.nslot = (long long)c->wcap;
+  w.geo = p.geom ? p.geo : 0;
   w.pcap = c->pcap; w.np = c->np; w.ld = c->ld; w.mode = p.mode; w.use_increment = p.use_increment ? 1 : 0;
   w.dx = c->dx; w.dy = c->dy; w.ly = c->ly; w.h = std::min(c->dx, c->dy);
   w.bd = bounds_of(c);
@@ -1642,5 +1659,6 @@ int launch_adj_pass(eif_ctx *c, const AdjPass &p) {
 }
 
 int adj_chunk_cap(const eif_ctx *c) { return c->chunk_cap; }
+size_t adj_slot_cap(const eif_ctx *c) { return c->wcap; }
 
 }  // namespace eif
