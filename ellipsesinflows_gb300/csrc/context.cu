@@ -351,19 +351,10 @@ int sync_scalars(eif_ctx *c) {
 int ensure_pcap(eif_ctx *c, int n) {
   if (n <= c->pcap && c->P) return EIF_OK;
   if (c->P) cudaFree(c->P);
-  if (c->cpf) cudaFree(c->cpf);
-  if (c->cand) cudaFree(c->cand);
-  if (c->cand_n) cudaFree(c->cand_n);
   c->P = nullptr;
-  c->cpf = nullptr;
-  c->cand = nullptr;
-  c->cand_n = nullptr;
   const int cap = n > 0 ? n : 1;
   EIF_CK(c, cudaMalloc((void **)&c->P, sizeof(double) * EIF_NFIELDS * (size_t)cap));
   EIF_CK(c, cudaMemset(c->P, 0, sizeof(double) * EIF_NFIELDS * (size_t)cap));
-  EIF_CK(c, cudaMalloc((void **)&c->cpf, sizeof(float4) * (size_t)cap));
-  EIF_CK(c, cudaMalloc((void **)&c->cand, sizeof(int) * EIF_CAND_CAP * (size_t)cap));
-  EIF_CK(c, cudaMalloc((void **)&c->cand_n, sizeof(int) * (size_t)cap));
   c->pcap = cap;
   return EIF_OK;
 }
@@ -476,11 +467,8 @@ int eif_destroy(eif_ctx *c) {
                     c->cyp, c->dxc, c->dxf, c->P, c->d_scal};
   for (double *p : ptrs) if (p) cudaFree(p);
   if (c->d_coef) cudaFree(c->d_coef);
-  if (c->cpf) cudaFree(c->cpf);
   if (c->rdxc_df) cudaFree(c->rdxc_df);
   if (c->d_inc) cudaFree(c->d_inc);
-  if (c->cand) cudaFree(c->cand);
-  if (c->cand_n) cudaFree(c->cand_n);
   graphs_free(c);
   float *fptrs[] = {c->rdxf_f, c->rdxc_f, c->cxm_f, c->cxp_f, c->cym_f, c->cyp_f, c->sxf[0], c->sxf[1], c->syf[0],
                     c->syf[1]};

@@ -161,8 +161,6 @@ struct eif_ctx {
   cudaGraphConditionalHandle loop_handle = 0;
   int ibm_ctas_per_sm[3] = {0, 0, 0};  // resident CTAs per SM of the IBM work kernels (FP64, mixed, mixed cached)
   unsigned *band_marks = nullptr;  // per band of 8 rows: bitmap over the 3*np (particle, image) boxes
-  float4 *cpf = nullptr;
-  int *cand = nullptr, *cand_n = nullptr;  // collision candidates (np * EIF_CAND_CAP), counts        // pcap: single-precision x + dx, y + dy, max(a, b) for the collision prefilter
   // immersed-boundary work
   int *box;                     // per particle: 3 images x {imin,imax,jmin,jmax}
   int *chunk_off;               // per particle: first chunk (exclusive scan), [np] = total

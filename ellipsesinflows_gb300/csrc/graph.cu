@@ -4,8 +4,9 @@
 // stage kernels, a conditional WHILE node whose body is one particle
 // sub-iteration (inertia at the increment, collisions, increments), and the
 // particle update (src/main.c:13-53). Work that the stage driver puts on the side
-// stream is captured as a parallel branch of the same graph. k_increment_done sets the loop condition
-// on the device from the residual and the sub-iteration count, so a step needs
+// stream is captured as a parallel branch of the same graph. The last block of
+// k_increment sets the loop condition on the device from the residual and the
+// sub-iteration count, so a step needs
 // no host round trip; the host synchronises once per step to read dt and the
 // error flags. The kernels and their order are those of the host-driven path
 // (rk_stage), so both paths give bit-identical results.

@@ -212,37 +212,36 @@ __device__ void wall_contribution(const PV &p, double wallx, double out[3], bool
   }
 }
 
-constexpr int CWARPS = 4;
-
-// single-precision centre (at X^k + dX) and bounding radius of every particle
-__global__ void k_collision_prep(const double *__restrict__ P, int pcap, int np, float4 *__restrict__ cpf) {
-  const int n = blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= np) return;
-  const PV v = load_pv(P, pcap, n);
-  cpf[n] = make_float4(eifd::d2f(v.x), eifd::d2f(v.y), eifd::d2f(fmax(v.a, v.b)), 0.f);
-}
-
-// Candidate partners: one warp per particle k, whose lanes test the partners
-// m = lane, lane + 32, ... in order against the partners' single-precision centres
-// and bounding radii (k_collision_prep), staged in shared memory tile by tile. The
-// pairs that pass this conservative test are listed in partner order (ballot and
-// prefix count); afterwards the lanes give them the exact double-precision
-// bounding-circle test of collision.c:173-189 (canonical orientation) together,
-// and the hits are compacted in order.
+// Collision forces (collision.c:306-367) in one launch, one warp per particle k:
+//  1. candidate partners: the lanes test the partners m = lane, lane + 32, ... in order
+//     against single-precision centres (at X^k + dX) and bounding radii, staged in shared
+//     memory tile by tile (every block forms them from the records as it loads a tile);
+//     the pairs that pass this conservative test are listed in partner order (ballot and
+//     prefix count);
+//  2. the lanes give the listed pairs the exact double-precision bounding-circle test of
+//     collision.c:173-189 (canonical orientation) and compact the hits in order;
+//  3. the hits are evaluated one per lane (circle fit, force and torque) and summed in
+//     partner order by lane 0, then the walls at x = 0 and x = lx are added.
 constexpr int CAND_CAP = EIF_CAND_CAP;   // candidates per particle
 constexpr int PAIR_WARPS = 8;
 constexpr int PAIR_TILE = 1024;
 constexpr int PAIR_LOADS = PAIR_TILE / (PAIR_WARPS * 32);
 
-__global__ void __launch_bounds__(PAIR_WARPS * 32) k_coll_pairs(const double *__restrict__ P, const float4 *__restrict__ cpf,
-                                                               int pcap, int np, double ly, int *__restrict__ cand,
-                                                               int *__restrict__ cand_n, unsigned *__restrict__ flags) {
+__device__ __forceinline__ float4 pair_prefilter(const double *P, int pcap, int n) {
+  const double x = P[EIF_P_X * pcap + n] + P[EIF_P_DX * pcap + n];
+  const double y = P[EIF_P_Y * pcap + n] + P[EIF_P_DY * pcap + n];
+  return make_float4(eifd::d2f(x), eifd::d2f(y), eifd::d2f(fmax(P[EIF_P_A * pcap + n], P[EIF_P_B * pcap + n])), 0.f);
+}
+
+__global__ void __launch_bounds__(PAIR_WARPS * 32) k_collision(double *__restrict__ P, int pcap, int np, int cn,
+                                                               double ly, double lx, unsigned *__restrict__ flags) {
   __shared__ float4 tile[PAIR_TILE];
-  __shared__ int maybe_list[PAIR_WARPS][CAND_CAP];
+  __shared__ int list[PAIR_WARPS][CAND_CAP];
+  __shared__ double cval[PAIR_WARPS][32][3];
   const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
   const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const bool on = k < np;   // uniform over the warp
-  const float4 fk = on ? __ldg(cpf + k) : make_float4(0.f, 0.f, 0.f, 0.f);
+  const float4 fk = on ? pair_prefilter(P, pcap, k) : make_float4(0.f, 0.f, 0.f, 0.f);
   const float lyf = eifd::d2f(ly);
   int nmaybe = 0;
   for (int t0 = 0; t0 < np; t0 += PAIR_TILE) {
@@ -251,7 +250,7 @@ __global__ void __launch_bounds__(PAIR_WARPS * 32) k_coll_pairs(const double *__
 #pragma unroll
     for (int r = 0; r < PAIR_LOADS; r++) {
       const int q = threadIdx.x + r * PAIR_WARPS * 32;
-      st[r] = q < nt ? __ldg(cpf + t0 + q) : make_float4(0.f, 0.f, 0.f, 0.f);
+      st[r] = q < nt ? pair_prefilter(P, pcap, t0 + q) : make_float4(0.f, 0.f, 0.f, 0.f);
     }
     __syncthreads();
 #pragma unroll
@@ -277,7 +276,7 @@ __global__ void __launch_bounds__(PAIR_WARPS * 32) k_coll_pairs(const double *__
       const unsigned mask = __ballot_sync(0xffffffffu, maybe);
       if (maybe) {
         const int r = nmaybe + __popc(mask & ((1u << lane) - 1u));
-        if (r < CAND_CAP) maybe_list[wl][r] = m;
+        if (r < CAND_CAP) list[wl][r] = m;
       }
       nmaybe += __popc(mask);
     }
@@ -286,42 +285,31 @@ __global__ void __launch_bounds__(PAIR_WARPS * 32) k_coll_pairs(const double *__
   __syncwarp();
   if (nmaybe > CAND_CAP && lane == 0) atomicOr(flags, EIF_FLAG_NOCONV);
   nmaybe = min(nmaybe, CAND_CAP);
+  const PV pk = load_pv(P, pcap, k);
+  // exact test, hits compacted in place (a write never passes the entries still to read)
   int cnt = 0;
   for (int base = 0; base < nmaybe; base += 32) {
     const int q = base + lane;
     bool hit = false;
     int m = 0;
     if (q < nmaybe) {
-      m = maybe_list[wl][q];
-      const PV pk = load_pv(P, pcap, k);
+      m = list[wl][q];
       const PV pm_ = load_pv(P, pcap, m);
       hit = m < k ? bounding_overlap(pm_, pk, ly) : bounding_overlap(pk, pm_, ly);
     }
     const unsigned mask = __ballot_sync(0xffffffffu, hit);
-    if (hit) cand[(size_t)k * CAND_CAP + cnt + __popc(mask & ((1u << lane) - 1u))] = m;
+    if (hit) list[wl][cnt + __popc(mask & ((1u << lane) - 1u))] = m;
     cnt += __popc(mask);
+    __syncwarp();
   }
-  if (lane == 0) cand_n[k] = cnt;
-}
-
-// Collision force on particle k (one warp): its candidate pairs are evaluated one
-// per lane and summed in partner order, then the walls at x = 0 and x = lx.
-__global__ void __launch_bounds__(CWARPS * 32) k_collision(double *__restrict__ P, const int *__restrict__ cand,
-                                                           const int *__restrict__ cand_n, int pcap, int np, int cn,
-                                                           double ly, double lx, unsigned *__restrict__ flags) {
-  __shared__ double cval[CWARPS][32][3];
-  const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
-  const int k = blockIdx.x * CWARPS + wl;
-  if (k >= np) return;
-  const int total = __ldg(cand_n + k);
-  const PV pk = load_pv(P, pcap, k);
+  // forces of the hits, summed in partner order
   double acc0 = 0., acc1 = 0., acc2 = 0.;
   bool ok_all = true;
-  for (int base = 0; base < total; base += 32) {
+  for (int base = 0; base < cnt; base += 32) {
     const int q = base + lane;
-    const int ncand = min(32, total - base);
-    if (q < total) {
-      const int mm = __ldg(cand + (size_t)k * CAND_CAP + q);
+    const int ncand = min(32, cnt - base);
+    if (q < cnt) {
+      const int mm = list[wl][q];
       const PV pmm = load_pv(P, pcap, mm);
       double out[3];
       bool ok;
@@ -369,7 +357,9 @@ __global__ void k_reset(double *__restrict__ P, int pcap, int np) {
 // of the order). The FP64 work is spread over many SMs: one SM alone has only a
 // few FP64 lanes.
 __global__ void k_increment(double *__restrict__ P, int pcap, int np, double gamma, double Fr2,
-                            const double *__restrict__ scal, unsigned long long *__restrict__ res_bits) {
+                            double *__restrict__ scal, unsigned long long *__restrict__ res_bits,
+                            unsigned *__restrict__ counter, unsigned *__restrict__ arrivals,
+                            cudaGraphConditionalHandle handle, int use_handle) {
   const double dt = scal[0];
   double res = 0.;
   for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < np; n += gridDim.x * blockDim.x) {
@@ -398,25 +388,29 @@ __global__ void k_increment(double *__restrict__ P, int pcap, int np, double gam
   __shared__ double s[32];
   if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = res;
   __syncthreads();
+  __shared__ bool last;
   if (threadIdx.x == 0) {
     for (int w = 1; w < (int)(blockDim.x >> 5); w++) res = fmax(res, s[w]);
     if (res > 0.) atomicMax(res_bits, (unsigned long long)__double_as_longlong(res));
+    // the last block to finish publishes the residual (its maximum is complete)
+    __threadfence();
+    last = atomicAdd(arrivals, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (last && threadIdx.x == 0) {
+    __threadfence();
+    *arrivals = 0u;
+    const double r = __longlong_as_double((long long)atomicExch(res_bits, 0ull));
+    scal[1] = r;
+    // inside a step graph: the condition of the sub-iteration loop (main.c:40-48):
+    // continue while the residual is not below 1e-8 and at most 101 sub-iterations ran
+    if (use_handle) {
+      const unsigned count = ++*counter;
+      cudaGraphSetConditional(handle, (!(r < 1.e-8) && count <= 101u) ? 1u : 0u);
+    }
   }
 }
 
-// Publishes the residual, clears the accumulator, and, inside a step graph, sets
-// the condition of the sub-iteration loop: continue while the residual is not
-// below 1e-8 and at most 101 sub-iterations have run (main.c:32-49).
-__global__ void k_increment_done(unsigned long long *__restrict__ res_bits, double *__restrict__ scal,
-                                 unsigned *__restrict__ counter, cudaGraphConditionalHandle handle, int use_handle) {
-  const double res = __longlong_as_double((long long)*res_bits);
-  *res_bits = 0ull;
-  scal[1] = res;
-  if (use_handle) {
-    const unsigned count = ++*counter;
-    cudaGraphSetConditional(handle, (!(res < 1.e-8) && count <= 101u) ? 1u : 0u);
-  }
-}
 
 // update.c:8-34
 __global__ void k_update(double *__restrict__ P, int pcap, int np, double ly) {
@@ -443,14 +437,9 @@ namespace eif {
 
 int launch_collision(eif_ctx *c, int cn) {
   if (c->np == 0) return EIF_OK;
-  EIF_PROF(c, "collision", 3);
-  k_collision_prep<<<(c->np + 127) / 128, 128, 0, c->stream>>>(c->P, c->pcap, c->np, c->cpf);
-  EIF_LAUNCH_CK(c);
-  k_coll_pairs<<<(c->np + PAIR_WARPS - 1) / PAIR_WARPS, PAIR_WARPS * 32, 0, c->stream>>>(
-      c->P, c->cpf, c->pcap, c->np, c->ly, c->cand, c->cand_n, c->d_flags);
-  EIF_LAUNCH_CK(c);
-  k_collision<<<(c->np + CWARPS - 1) / CWARPS, CWARPS * 32, 0, c->stream>>>(c->P, c->cand, c->cand_n, c->pcap, c->np,
-                                                                            cn, c->ly, c->lx, c->d_flags);
+  EIF_PROF(c, "collision", 1);
+  k_collision<<<(c->np + PAIR_WARPS - 1) / PAIR_WARPS, PAIR_WARPS * 32, 0, c->stream>>>(c->P, c->pcap, c->np, cn,
+                                                                                      c->ly, c->lx, c->d_flags);
   EIF_LAUNCH_CK(c);
   return EIF_OK;
 }
@@ -467,14 +456,12 @@ int launch_reset_increments(eif_ctx *c) {
 int launch_increment(eif_ctx *c, int rk) {
   c->incr_zero = false;
   const double Fr = c->cfg.Fr;
-  EIF_PROF(c, "particle_increment", 2);
+  EIF_PROF(c, "particle_increment", 1);
   // FP64-heavy per particle: small blocks spread the particles over many SMs
   const int blocks = std::max(1, std::min((c->np + 31) / 32, c->sms * 4));
-  k_increment<<<blocks, 32, 0, c->stream>>>(c->P, c->pcap, c->np, rk_coef(rk).gamma, Fr * Fr, c->d_scal,
-                                             c->d_inc);
-  EIF_LAUNCH_CK(c);
-  k_increment_done<<<1, 1, 0, c->stream>>>(c->d_inc, c->d_scal, reinterpret_cast<unsigned *>(c->d_inc + 1),
-                                           c->loop_handle, c->in_loop ? 1 : 0);
+  unsigned *counter = reinterpret_cast<unsigned *>(c->d_inc + 1);   // low word: loop counter
+  k_increment<<<blocks, 32, 0, c->stream>>>(c->P, c->pcap, c->np, rk_coef(rk).gamma, Fr * Fr, c->d_scal, c->d_inc,
+                                             counter, counter + 1, c->loop_handle, c->in_loop ? 1 : 0);
   EIF_LAUNCH_CK(c);
   return EIF_OK;
 }
