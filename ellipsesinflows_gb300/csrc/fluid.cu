@@ -172,21 +172,42 @@ __global__ void __launch_bounds__(TX *TY) k_predictor_mixed(PredArgsF a) {
   __shared__ float2 tux[PY][PX], tuy[PY][PX], tp[PY][PX];
   const int ld = a.ld, itot = a.itot, jtot = a.jtot;
   const int ib = 1 + blockIdx.x * TX, jb = 1 + blockIdx.y * TY;
-  // stage the tile: tile (tx, ty) holds index (ib - 1 + tx, jb - 1 + ty)
-  for (int t = threadIdx.y * TX + threadIdx.x; t < PX * PY; t += TX * TY) {
-    const int tx = t % PX, ty = t / PX;
+  // stage the tile: tile (tx, ty) holds index (ib - 1 + tx, jb - 1 + ty). Every thread
+  // stages its own cell (and keeps its two doubles for the update), the first threads
+  // the ring of 2 (TX + 2) + 2 TY halo cells.
+  auto stage = [&](int tx, int ty, double *u_keep, double *v_keep) {
     const int i = ib - 1 + tx, j = jb - 1 + ty;
     float2 vux = make_float2(0.f, 0.f), vuy = vux, vp = vux;
     if (j <= jtot + 1) {
-      if (i >= 1 && i <= itot + 1) vux = eifd::split(__ldg(a.ux + j * ld + (i - 1)));
+      if (i >= 1 && i <= itot + 1) {
+        const double u = __ldg(a.ux + j * ld + (i - 1));
+        if (u_keep) *u_keep = u;
+        vux = eifd::split(u);
+      }
       if (i <= itot + 1) {
-        vuy = eifd::split(__ldg(a.uy + j * ld + i));
+        const double v = __ldg(a.uy + j * ld + i);
+        if (v_keep) *v_keep = v;
+        vuy = eifd::split(v);
         vp = eifd::split(__ldg(a.p + j * ld + i));
       }
     }
     tux[ty][tx] = vux;
     tuy[ty][tx] = vuy;
     tp[ty][tx] = vp;
+  };
+  double u_own = 0., v_own = 0.;
+  stage(threadIdx.x + 1, threadIdx.y + 1, &u_own, &v_own);
+  {
+    constexpr int RING = 2 * PX + 2 * TY;
+    const int t = threadIdx.y * TX + threadIdx.x;
+    if (t < RING) {
+      int tx, ty;
+      if (t < PX) { tx = t; ty = 0; }                              // bottom halo row
+      else if (t < 2 * PX) { tx = t - PX; ty = PY - 1; }          // top halo row
+      else if (t < 2 * PX + TY) { tx = 0; ty = 1 + (t - 2 * PX); } // left column
+      else { tx = PX - 1; ty = 1 + (t - 2 * PX - TY); }            // right column
+      stage(tx, ty, nullptr, nullptr);
+    }
   }
   __syncthreads();
   const int i = ib + threadIdx.x, j = jb + threadIdx.y;
@@ -215,7 +236,7 @@ __global__ void __launch_bounds__(TX *TY) k_predictor_mixed(PredArgsF a) {
     const int c = j * ld + (i - 1);
     const float B = __ldg(a.sxb + c);
     a.sxa[c] = A;
-    const double un_ = __ldg(a.ux + c) + eifd::f2d(adt * A + bdt * B + gdt * pre);
+    const double un_ = u_own + eifd::f2d(adt * A + bdt * B + gdt * pre);
     a.uxn[c] = un_;
     if (j == 1) a.uxn[c + jtot * ld] = un_;
     if (j == jtot) a.uxn[c - jtot * ld] = un_;
@@ -240,7 +261,7 @@ __global__ void __launch_bounds__(TX *TY) k_predictor_mixed(PredArgsF a) {
     const int c = j * ld + i;
     const float B = __ldg(a.syb + c);
     a.sya[c] = A;
-    const double vn_ = __ldg(a.uy + c) + eifd::f2d(adt * A + bdt * B + gdt * pre);
+    const double vn_ = v_own + eifd::f2d(adt * A + bdt * B + gdt * pre);
     a.uyn[c] = vn_;
     if (j == 1) a.uyn[c + jtot * ld] = vn_;
     if (j == jtot) a.uyn[c - jtot * ld] = vn_;
