@@ -58,6 +58,14 @@ HBM_BYTES = {
     "mixed": {"predictor": 56, "correct": 64, "poisson_dct2": 32, "poisson_dct3": 16},
 }
 
+# DRAM bytes (read + write) per launch from one ncu capture of the mixed form at
+# 2048 x 4096 (profiles/kernels_suspension_2048x4096_mixed.md); used as the roofline's
+# `traffic` at that grid size only
+NCU_TRAFFIC = {
+    ("mixed", 2048, 4096): {"predictor": 436e6, "correct": 489e6, "poisson_dct2": 246e6,
+                            "poisson_dct3": 86e6},
+}
+
 
 def parse():
     ap = argparse.ArgumentParser()
@@ -228,7 +236,7 @@ def run_ours(args, world, rank, local, pg):
     cells = case.cells
     value = world * cells * args.steps / (ms / 1e3)
     hbm, hbm_src = peaks()
-    roof = roofline(prof, cells, hbm, hbm_src, args.precision)
+    roof = roofline(prof, cells, hbm, hbm_src, args.precision, (case.itot, case.jtot))
     # kernels launched in the timed region: the same kernels per step as the profiled pass
     launches = int(round(sum(e["launches"] for e in prof) * args.steps / prof_steps))
     out = {
@@ -418,9 +426,10 @@ def profile_entries(sim):
     return out
 
 
-def roofline(prof, cells, hbm, hbm_src, precision):
+def roofline(prof, cells, hbm, hbm_src, precision, grid=None):
     """Roofline of the dominant streaming kernel against the measured copy bandwidth."""
     table = HBM_BYTES[precision]
+    ncu = NCU_TRAFFIC.get((precision,) + tuple(grid or ()), {})
     total = sum(e["ms"] for e in prof) or 1.0
     stream = [e for e in prof if e["name"] in table and e["launches"] > 0]
     if not stream:
@@ -431,7 +440,8 @@ def roofline(prof, cells, hbm, hbm_src, precision):
     achieved = bytes_per_launch / (per_launch_ms / 1e3) / 1e9
     dominant = prof[0]
     return {"bound": "hbm", "kernel": top["name"], "achieved": achieved, "peak": hbm, "unit": "GB/s",
-            "frac": achieved / hbm, "peak_source": hbm_src, "traffic": None,
+            "frac": achieved / hbm, "peak_source": hbm_src, "traffic": ncu.get(top["name"]),
+            "traffic_source": "ncu capture, one launch" if top["name"] in ncu else None,
             "algorithmic_bytes_per_launch": bytes_per_launch, "share_of_step": top["ms"] / total,
             "dominant_kernel": dominant["name"], "dominant_share": dominant["ms"] / total}
 

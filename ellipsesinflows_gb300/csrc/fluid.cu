@@ -195,6 +195,15 @@ __global__ void __launch_bounds__(TX *TY) k_predictor_mixed(PredArgsF a) {
     tuy[ty][tx] = vuy;
     tp[ty][tx] = vp;
   };
+  // the old explicit terms are streamed once and used after the barrier: their loads
+  // are issued first, so that they are in flight together with the staging loads
+  const int i = ib + threadIdx.x, j = jb + threadIdx.y;
+  const bool live = i <= itot && j <= jtot;
+  float Bx = 0.f, By = 0.f;
+  if (live) {
+    if (i >= 2) Bx = __ldg(a.sxb + j * ld + (i - 1));
+    By = __ldg(a.syb + j * ld + i);
+  }
   double u_own = 0., v_own = 0.;
   stage(threadIdx.x + 1, threadIdx.y + 1, &u_own, &v_own);
   {
@@ -210,8 +219,7 @@ __global__ void __launch_bounds__(TX *TY) k_predictor_mixed(PredArgsF a) {
     }
   }
   __syncthreads();
-  const int i = ib + threadIdx.x, j = jb + threadIdx.y;
-  if (i > itot || j > jtot) return;
+  if (!live) return;
   const int x = threadIdx.x + 1, y = threadIdx.y + 1;
   const float adt = __ldg(a.coef), bdt = __ldg(a.coef + 1), gdt = __ldg(a.coef + 2);
   const float rdy = a.rdy;
@@ -234,9 +242,8 @@ __global__ void __launch_bounds__(TX *TY) k_predictor_mixed(PredArgsF a) {
     const float pre = -dif(tp[y][x], tp[y][x - 1]) * rdxc;
     const float A = (adv1 + adv2) + dif_;
     const int c = j * ld + (i - 1);
-    const float B = __ldg(a.sxb + c);
     a.sxa[c] = A;
-    const double un_ = u_own + eifd::f2d(adt * A + bdt * B + gdt * pre);
+    const double un_ = u_own + eifd::f2d(adt * A + bdt * Bx + gdt * pre);
     a.uxn[c] = un_;
     if (j == 1) a.uxn[c + jtot * ld] = un_;
     if (j == jtot) a.uxn[c - jtot * ld] = un_;
@@ -259,9 +266,8 @@ __global__ void __launch_bounds__(TX *TY) k_predictor_mixed(PredArgsF a) {
     const float pre = -dif(tp[y][x], tp[y - 1][x]) * rdy;
     const float A = (adv1 + adv2) + dif_ + a.ext;
     const int c = j * ld + i;
-    const float B = __ldg(a.syb + c);
     a.sya[c] = A;
-    const double vn_ = v_own + eifd::f2d(adt * A + bdt * B + gdt * pre);
+    const double vn_ = v_own + eifd::f2d(adt * A + bdt * By + gdt * pre);
     a.uyn[c] = vn_;
     if (j == 1) a.uyn[c + jtot * ld] = vn_;
     if (j == jtot) a.uyn[c - jtot * ld] = vn_;
