@@ -355,40 +355,55 @@ __global__ void __launch_bounds__(TX *TY) k_correct_df(CorrArgsDF a) {
   const int j = 1 + blockIdx.y * TY + threadIdx.y;
   if (i > a.itot || j > a.jtot) return;
   const int ld = a.ld, jtot = a.jtot, itot = a.itot;
-  const DF gdt = a.with_proj ? DF{__ldg(a.coef + 20 + 2 * a.rk), __ldg(a.coef + 21 + 2 * a.rk)} : DF{0.f, 0.f};
-  const int cy = uy_idx(i, j, ld);
-  const double psi0 = (a.with_proj || a.with_pressure) ? __ldg(a.psi + cy) : 0.;
+  const int cy = uy_idx(i, j, ld), c = ux_idx(i, j, ld);
   const bool vel = a.with_ibm || a.with_proj;
-  if (vel && i >= 2) {
-    const int c = ux_idx(i, j, ld);
+  const bool xface = vel && i >= 2;
+  // Every load is issued before the first store: a thread reads only its own cells
+  // and the read-only psi and responses, and writes only its own cells and halo copies
+  // that no thread of this launch reads, so the order does not change a result, but
+  // the three old values then come from memory together instead of one after another.
+  const double u_old = xface ? a.ux[c] : 0.;
+  const double v_old = vel ? a.uy[cy] : 0.;
+  const double p_old = a.with_pressure ? a.p[cy] : 0.;
+  const double psi0 = (a.with_proj || a.with_pressure) ? __ldg(a.psi + cy) : 0.;
+  const double psi_w = (a.with_proj && xface) ? __ldg(a.psi + cy - 1) : 0.;
+  const double psi_s = (a.with_proj && vel) ? __ldg(a.psi + cy - ld) : 0.;
+  float dw = 0.f, de = 0.f, ds = 0.f, dn = 0.f;
+  if (a.with_ibm) {
+    if (xface) { dw = __ldg(a.dux + cy - 1); de = __ldg(a.dux + cy); }
+    ds = __ldg(a.duy + cy - ld);
+    dn = __ldg(a.duy + cy);
+  }
+  const float2 r = xface ? __ldg(a.rdxc + i) : make_float2(0.f, 0.f);
+  const DF gdt = a.with_proj ? DF{__ldg(a.coef + 20 + 2 * a.rk), __ldg(a.coef + 21 + 2 * a.rk)} : DF{0.f, 0.f};
+  if (xface) {
     DF inc{0.f, 0.f};
-    if (a.with_ibm) inc = two_sum(__ldg(a.dux + cy - 1), __ldg(a.dux + cy));
+    if (a.with_ibm) inc = two_sum(dw, de);
     inc = df_scale(inc, 0.5f);
     if (a.with_proj) {
-      const float2 r = __ldg(a.rdxc + i);
-      const DF g = df_mul(df_mul(gdt, df_of(psi0 - __ldg(a.psi + cy - 1))), DF{r.x, r.y});
+      const DF g = df_mul(df_mul(gdt, df_of(psi0 - psi_w)), DF{r.x, r.y});
       inc = df_add_nw(inc, df_neg(g));
     }
-    const double u = a.ux[c] + df_to_double(inc);
+    const double u = u_old + df_to_double(inc);
     a.ux[c] = u;
     if (j == 1) a.ux[c + jtot * ld] = u;
     if (j == jtot) a.ux[c - jtot * ld] = u;
   }
   if (vel) {
     DF inc{0.f, 0.f};
-    if (a.with_ibm) inc = two_sum(__ldg(a.duy + cy - ld), __ldg(a.duy + cy));
+    if (a.with_ibm) inc = two_sum(ds, dn);
     inc = df_scale(inc, 0.5f);
     if (a.with_proj) {
-      const DF g = df_mul(df_mul(gdt, df_of(psi0 - __ldg(a.psi + cy - ld))), a.rdy);
+      const DF g = df_mul(df_mul(gdt, df_of(psi0 - psi_s)), a.rdy);
       inc = df_add_nw(inc, df_neg(g));
     }
-    const double v = a.uy[cy] + df_to_double(inc);
+    const double v = v_old + df_to_double(inc);
     a.uy[cy] = v;
     if (j == 1) a.uy[cy + jtot * ld] = v;
     if (j == jtot) a.uy[cy - jtot * ld] = v;
   }
   if (a.with_pressure) {
-    const double pv = a.p[cy] + psi0;
+    const double pv = p_old + psi0;
     a.p[cy] = pv;
     if (j == 1) a.p[cy + jtot * ld] = pv;
     if (j == jtot) a.p[cy - jtot * ld] = pv;
