@@ -62,7 +62,7 @@ HBM_BYTES = {
 # 2048 x 4096 (profiles/kernels_suspension_2048x4096_mixed.md); used as the roofline's
 # `traffic` at that grid size only
 NCU_TRAFFIC = {
-    ("mixed", 2048, 4096): {"predictor": 436e6, "correct": 489e6, "poisson_dct2": 246e6,
+    ("mixed", 2048, 4096): {"predictor": 434e6, "correct": 488e6, "poisson_dct2": 246e6,
                             "poisson_dct3": 86e6},
 }
 
@@ -70,7 +70,7 @@ NCU_TRAFFIC = {
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
@@ -91,24 +91,34 @@ def make_case(name):
 
 
 class ClockSampler:
-    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region.
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    Samples carry nvidia-smi's own timestamp; `begin()` and `end()` mark the timed region
+    on the same clock, and the summary keeps the samples inside it (all samples when the
+    region was not marked, the nearest one when it was shorter than the interval)."""
+
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    INTERVAL_MS = 20
 
     def __init__(self, device):
         self.device = device
         self.proc = None
         self.lines = []
+        self.t0 = self.t1 = None
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", str(self.INTERVAL_MS)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            # the sampler is running before the region starts
+            deadline = time.time() + 3.0
+            while not self.lines and time.time() < deadline and self.proc.poll() is None:
+                time.sleep(0.01)
         except OSError:
             self.proc = None
         return self
@@ -116,6 +126,12 @@ class ClockSampler:
     def _read(self):
         for line in self.proc.stdout:
             self.lines.append(line.strip())
+
+    def begin(self):
+        self.t0 = time.time()
+
+    def end(self):
+        self.t1 = time.time()
 
     def __exit__(self, *exc):
         if self.proc is not None:
@@ -125,23 +141,41 @@ class ClockSampler:
             except subprocess.TimeoutExpired:
                 self.proc.kill()
 
+    @staticmethod
+    def _stamp(text):
+        import datetime
+        try:
+            return datetime.datetime.strptime(text, "%Y/%m/%d %H:%M:%S.%f").timestamp()
+        except ValueError:
+            return None
+
     def summary(self):
-        sm, smax, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        rows = []
         for line in self.lines:
             parts = [p.strip() for p in line.split(",")]
-            if len(parts) < 9:
+            if len(parts) < 10:
                 continue
             try:
-                sm.append(float(parts[1]))
-                smax = float(parts[2])
+                rows.append((self._stamp(parts[0]), float(parts[2]), float(parts[3]),
+                             [name for k, name in enumerate(names) if parts[6 + k].lower().startswith("active")]))
             except ValueError:
                 continue
-            for k, name in enumerate(names):
-                if parts[5 + k].lower().startswith("active"):
-                    reasons.add(name)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
-                "reasons": sorted(reasons), "samples": len(sm)}
+        where = "all samples"
+        if self.t0 is not None and self.t1 is not None and rows:
+            inside = [r for r in rows if r[0] is not None and self.t0 <= r[0] <= self.t1]
+            if inside:
+                rows, where = inside, "timed region"
+            else:
+                mid = 0.5 * (self.t0 + self.t1)
+                stamped = [r for r in rows if r[0] is not None]
+                if stamped:
+                    rows = [min(stamped, key=lambda r: abs(r[0] - mid))]
+                    where = "nearest sample (region shorter than the %d ms interval)" % self.INTERVAL_MS
+        sm = [r[1] for r in rows]
+        reasons = sorted({n for r in rows for n in r[3]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": rows[-1][2] if rows else None,
+                "reasons": reasons, "samples": len(sm), "window": where}
 
 
 def peaks():
@@ -200,10 +234,12 @@ def run_ours(args, world, rank, local, pg):
     with ClockSampler(local) as clk:
         barrier(pg, local)
         torch.cuda.synchronize()
+        clk.begin()
         start.record(stream)
         sim.advance(args.steps)
         stop.record(stream)
         torch.cuda.synchronize()
+        clk.end()
         barrier(pg, local)
     ms = start.elapsed_time(stop)
     ms = max_over_ranks(pg, ms, local)
@@ -281,10 +317,12 @@ def run_batch(args, world, rank, local, pg):
     with ClockSampler(local) as clk:
         barrier(pg, local)
         torch.cuda.synchronize()
+        clk.begin()
         start.record(stream)
         batch.advance(args.steps)
         stop.record(stream)
         torch.cuda.synchronize()
+        clk.end()
         barrier(pg, local)
     ms = max_over_ranks(pg, start.elapsed_time(stop), local)
     # the same suspensions one after another (one graph launch per suspension and step)
