@@ -25,6 +25,7 @@ ERRORS = {
     -4: "out of memory",
     -5: "call out of order",
     -6: "non-finite velocity",
+    -7: "size beyond the fixed scratch",
 }
 
 # particle record fields (include/eif.h enum eif_particle_field)
@@ -114,6 +115,7 @@ def bind(lib, prefix):
         "log_quantities": [_vp, _dp],
         "set_threads": [_vp, ctypes.c_int],
         "tiles": [_vp, _ip],
+        "counters": [_vp, ctypes.POINTER(ctypes.c_longlong)],
         "stats_reset": [_vp],
         "stats_collect": [_vp],
         "stats_pull": [_vp, _dp, _dp, _dp, _dp, _dp, _ip],
@@ -411,6 +413,12 @@ class Solver:
         self._call("snapshot_wait", self.ctx, _ptr(ux), _ptr(uy), _ptr(p), n, _ptr(rec), ctypes.byref(step),
                    ctypes.byref(time))
         return ux, uy, p, rec[:n], step.value, time.value
+
+    def counters(self):
+        """{"substeps", "indicator_cells", "normal_foot_evals"} (eif_counters)"""
+        v = (ctypes.c_longlong * 3)()
+        self._call("counters", self.ctx, v)
+        return {"substeps": v[0], "indicator_cells": v[1], "normal_foot_evals": v[2]}
 
     def tiles(self):
         """tile shapes chosen by the tuner: {"predictor_rows", "projection_rows",

@@ -328,7 +328,10 @@ int check_flags(eif_ctx *c) {
   if (f == 0u) return EIF_OK;
   *c->h_flags = 0u;
   EIF_CK(c, cudaMemsetAsync(c->d_flags, 0, sizeof(unsigned), c->stream));
-  if (f & EIF_FLAG_NONFINITE) return fail(c, EIF_ERR_NONFINITE, "non-finite velocity detected");
+  if (f & EIF_FLAG_NONFINITE) {
+    c->src_nonfinite = true;
+    return fail(c, EIF_ERR_NONFINITE, "non-finite velocity detected");
+  }
   if (f & EIF_FLAG_NOCONV)
     return fail(c, EIF_ERR_NOCONV, "an iteration cap or a device list capacity was reached on the device");
   return EIF_OK;
@@ -430,8 +433,8 @@ int eif_create(const eif_config_t *cfg, eif_ctx **out) {
   CK_CREATE(cudaMemset(c->d_coef, 0, sizeof(float) * 32));
   CK_CREATE(cudaMalloc((void **)&c->d_scal, sizeof(double) * 4));
   CK_CREATE(cudaMemset(c->d_scal, 0, sizeof(double) * 4));
-  CK_CREATE(cudaMalloc((void **)&c->d_inc, sizeof(unsigned long long) * 2));
-  CK_CREATE(cudaMemset(c->d_inc, 0, sizeof(unsigned long long) * 2));
+  CK_CREATE(cudaMalloc((void **)&c->d_inc, sizeof(unsigned long long) * 5));
+  CK_CREATE(cudaMemset(c->d_inc, 0, sizeof(unsigned long long) * 5));
   CK_CREATE(cudaMalloc((void **)&c->d_flags, sizeof(unsigned)));
   CK_CREATE(cudaMemset(c->d_flags, 0, sizeof(unsigned)));
   CK_CREATE(cudaMallocHost((void **)&c->h_scal, sizeof(double) * 4));
@@ -511,6 +514,14 @@ int eif_push_fluid(eif_ctx *c, const double *ux, const double *uy, const double 
   if ((rc = rows_in(c, c->ux[c->cur], ux, c->itot + 1, rows))) return rc;
   if ((rc = rows_in(c, c->uy[c->cur], uy, c->itot + 2, rows))) return rc;
   if ((rc = rows_in(c, c->p, p, c->itot + 2, rows))) return rc;
+  if (c->src_nonfinite) {
+    for (double *f : {c->sxa[0], c->sxa[1], c->sya[0], c->sya[1]})
+      EIF_CK(c, cudaMemsetAsync(f, 0, sizeof(double) * c->nfield, c->stream));
+    if (c->cfg.precision == EIF_PREC_MIXED)
+      for (float *f : {c->sxf[0], c->sxf[1], c->syf[0], c->syf[1]})
+        EIF_CK(c, cudaMemsetAsync(f, 0, sizeof(float) * c->nfield, c->stream));
+    c->src_nonfinite = false;
+  }
   rc = launch_boundaries(c);
   if (rc) return rc;
   EIF_CK(c, cudaStreamSynchronize(c->stream));
@@ -701,8 +712,9 @@ int eif_advance(eif_ctx *c, int nsteps) {
   if (c->use_graphs && !c->sync_debug && !c->prof.enabled) {
     // one graph launch per step (see graph.cu), queued one step ahead: step s + 1 is
     // launched before the host waits for the copies of step s's dt, flags and bounds
-    // record, so the GPU does not idle between steps. After an error the state may
-    // include the step launched after the failing one.
+    // record, so the GPU does not idle between steps. When step s reports an error,
+    // step s + 1 has already run on the device: it is waited for and counted too, so
+    // that the step counter and time always describe the device state.
     auto finish = [&](int s) -> int {
       eif_ctx::StepSlot &h = c->h_slots[s & 1];
       EIF_CK(c, cudaEventSynchronize(c->ev_step[s & 1]));
@@ -737,7 +749,13 @@ int eif_advance(eif_ctx *c, int nsteps) {
         h.check[0] = 0ull;
       }
       EIF_CK(c, cudaEventRecord(c->ev_step[s & 1], c->stream));
-      if (s > 0 && (rc = finish(s - 1))) return rc;
+      if (s > 0 && (rc = finish(s - 1))) {
+        if (cudaEventSynchronize(c->ev_step[s & 1]) == cudaSuccess) {
+          c->step += 1;
+          c->time += c->h_slots[s & 1].scal[0];
+        }
+        return rc;
+      }
     }
     if (nsteps > 0) {
       const int rc = finish(nsteps - 1);
@@ -930,6 +948,15 @@ int eif_profile_count(eif_ctx *c, int *count) {
   int rc = profile_flush(c);
   *count = (int)c->prof.entries.size();
   return rc;
+}
+
+int eif_counters(eif_ctx *c, long long *counts) {
+  if (!c || !counts) return EIF_ERR_ARG;
+  unsigned long long v[3];
+  EIF_CK(c, cudaStreamSynchronize(c->stream));
+  EIF_CK(c, cudaMemcpy(v, c->d_inc + 2, sizeof(v), cudaMemcpyDeviceToHost));
+  for (int k = 0; k < 3; k++) counts[k] = (long long)v[k];
+  return EIF_OK;
 }
 
 int eif_profile_get(eif_ctx *c, int k, char *name, int name_len, long long *launches, double *ms) {

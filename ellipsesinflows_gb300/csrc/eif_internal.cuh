@@ -137,6 +137,9 @@ struct eif_ctx {
   int np, pcap;
   double *P;                    // EIF_NFIELDS * pcap
   // particle sub-iteration: [0] residual accumulator (IEEE bits), [1] loop counter (low word)
+  // and block arrivals (high word); counters reported by eif_counters: [2] sub-iterations
+  // run, [3] box cells whose indicator geometry was evaluated and [4] of those the near
+  // cells that ran the normal-foot iteration ([3] and [4] while kernel timing is on)
   unsigned long long *d_inc = nullptr;
   // step graphs (eif_advance): one per parity of the double-buffer indices at the step's start
   struct StepGraph {
@@ -154,6 +157,10 @@ struct eif_ctx {
   } tiles;
   unsigned buf_gen = 0;         // bumped when device buffers are reallocated (batch graphs hold them)
   bool incr_zero = false;       // the particle increments are zero (after a reset)
+  // a non-finite velocity was reported: the RK explicit terms kept for the next stage may
+  // hold NaN (multiplied by beta = 0 in the first stage, which still gives NaN), so the
+  // next fluid push clears them, as the reference's fluid_init starts them at zero
+  bool src_nonfinite = false;
   bool boxes_x_valid = false;   // the IBM boxes hold the positions X (see launch_boxes)
   bool weights_x_valid = false; // wcache holds the indicator weights of those boxes
   void *wcache = nullptr;       // indicator weight per IBM task slot (wcap entries)

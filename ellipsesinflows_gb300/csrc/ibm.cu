@@ -410,6 +410,9 @@ struct WorkArgs {
   const unsigned *iter;
   int gate;   // with iter (mixed form): 1 runs only in the first sub-iteration, 2 only afterwards
   int weights_only;   // exchange (double precision): the cell contributions are the weights (w, w)
+  // box cells whose geometry is evaluated and, of those, the near cells that run the
+  // normal-foot iteration, added to count[0] and count[1] (null: not counted)
+  unsigned long long *count;
   Bounds bd;
 };
 
@@ -518,6 +521,13 @@ __global__ void __launch_bounds__(256) k_ibm_work(WorkArgs a) {
     }
     // pass 2: the near cells, packed onto consecutive lanes
     const int nnear = __popc(near_mask[0]) + __popc(near_mask[1]);
+    if (a.count) {
+      const unsigned in0 = __ballot_sync(0xffffffffu, cin[0]), in1 = __ballot_sync(0xffffffffu, cin[1]);
+      if (lane == 0) {
+        atomicAdd(a.count, (unsigned long long)(__popc(in0) + __popc(in1)));
+        atomicAdd(a.count + 1, (unsigned long long)nnear);
+      }
+    }
     __syncwarp();
     for (int k = lane; k < nnear; k += 32) {
       const double2 o = slots[k];
@@ -738,6 +748,13 @@ __global__ void __launch_bounds__(256, 3) k_ibm_work_f(WorkArgs a) {
     }
     // pass 2: the near cells, packed onto consecutive lanes
     const int nnear = __popc(near_mask[0]) + __popc(near_mask[1]);
+    if (a.count) {
+      const unsigned in0 = __ballot_sync(0xffffffffu, cin[0]), in1 = __ballot_sync(0xffffffffu, cin[1]);
+      if (lane == 0) {
+        atomicAdd(a.count, (unsigned long long)(__popc(in0) + __popc(in1)));
+        atomicAdd(a.count + 1, (unsigned long long)nnear);
+      }
+    }
     __syncwarp();
     for (int k = lane; k < nnear; k += 32) {
       const float2 o = slots[k];
@@ -1303,6 +1320,7 @@ static int launch_work(eif_ctx *c, int mode, int cn) {
   w.iter = nullptr;
   w.gate = 0;
   w.weights_only = c->ibm_weights_only ? 1 : 0;
+  w.count = c->prof.enabled ? c->d_inc + 3 : nullptr;
   if (c->in_loop) {
     w.wmode = 0;
     w.iter = reinterpret_cast<const unsigned *>(c->d_inc + 1);
@@ -1324,7 +1342,11 @@ static int launch_work(eif_ctx *c, int mode, int cn) {
   const int blocks = std::max(1, std::min(c->sms * per_sm, (c->chunk_cap * 32 + 255) / 256));
   {
     const bool mixed = c->cfg.precision == EIF_PREC_MIXED;
-    EIF_PROF(c, mode == 0 ? "ibm_inertia" : "ibm_exchange", mixed && c->in_loop ? 2 : 1);
+    // launches that evaluate the indicator geometry are timed as ibm_indicator, those
+    // with stored weights (sums and field contributions only) as inertia or exchange
+    const bool geometry = w.wmode != 2 && !(mixed && c->in_loop);
+    EIF_PROF(c, geometry ? "ibm_indicator" : (mode == 0 ? "ibm_inertia" : "ibm_exchange"),
+             mixed && c->in_loop ? 2 : 1);
     if (mixed && c->in_loop) {
       // first sub-iteration: cached weights; later ones: full evaluation (decided on the device)
       WorkArgs w1 = w, w2 = w;

@@ -9,8 +9,9 @@
 // straight from the caller's device arrays, using only a fixed scratch array
 // that lives in this library's static device memory.
 //
-// Scratch. g_noalloc_scratch below holds the column maxima of |ux| and the
-// maximum of |uy|: EIF_NOALLOC_MAX_ITOT + 3 64-bit words (about 128 KiB) on
+// Scratch. g_noalloc_scratch below holds the column maxima of |ux|, the
+// maximum of |uy| and a non-finite marker: EIF_NOALLOC_MAX_ITOT + 4 64-bit
+// words (about 128 KiB) on
 // every GPU that loads the library, kept until the process exits. Host code
 // cannot use the symbol as a device address, so the address is looked up with
 // cudaGetSymbolAddress once per device, on the first call made while that
@@ -24,15 +25,18 @@
 
 namespace {
 
-__device__ __align__(256) unsigned long long g_noalloc_scratch[EIF_NOALLOC_MAX_ITOT + 3];
+__device__ __align__(256) unsigned long long g_noalloc_scratch[EIF_NOALLOC_MAX_ITOT + 4];
 
 constexpr int NTX = 32, NTY = 8;
 constexpr int MAX_DEVICES = 64;
 
 // column maxima of |UX(i, j)| (i = 2..itot) and the maximum of |UY(i, j)| over
-// rows 1..jtot, as bit patterns of non-negative doubles (ordered like the values)
+// rows 1..jtot, as bit patterns of non-negative doubles (ordered like the values);
+// a NaN or an infinity among the values read sets *nonfinite
+constexpr unsigned long long INF_BITS = 0x7ff0000000000000ull;
 __global__ void k_noalloc_max(const double *__restrict__ ux, const double *__restrict__ uy, int ldx, int ldy, int itot,
-                              int jtot, unsigned long long *__restrict__ colmax, unsigned long long *__restrict__ uymax) {
+                              int jtot, unsigned long long *__restrict__ colmax, unsigned long long *__restrict__ uymax,
+                              unsigned long long *__restrict__ nonfinite) {
   const int i = 1 + blockIdx.x * NTX + threadIdx.x;
   unsigned long long mx = 0ull, my = 0ull;
   if (i <= itot) {
@@ -45,6 +49,7 @@ __global__ void k_noalloc_max(const double *__restrict__ ux, const double *__res
       my = b > my ? b : my;
     }
   }
+  if (mx >= INF_BITS || my >= INF_BITS) atomicOr(nonfinite, 1ull);
   for (int o = 16; o > 0; o >>= 1) {
     const unsigned long long other = __shfl_xor_sync(0xffffffffu, my, o);
     my = other > my ? other : my;
@@ -66,7 +71,8 @@ __device__ __forceinline__ double xc_of(int i, int itot, double dx) {
 // dt from the maxima and the particle records (src/param/decide_dt.c:25-80)
 __global__ void k_noalloc_final(const unsigned long long *__restrict__ colmax, const unsigned long long *__restrict__ uymax,
                                 int itot, double dx, double dy, double Re, double sf_adv, double sf_dif, double sf_par,
-                                const double *__restrict__ rec, int np, double *__restrict__ dt_out) {
+                                const double *__restrict__ rec, int np, const unsigned long long *__restrict__ nonfinite,
+                                double *__restrict__ dt_out) {
   const double small = 1.e-8;
   double dta = 5.e-2, dxmin = 1., dtp = DBL_MAX;
   for (int i = 2 + threadIdx.x; i <= itot; i += blockDim.x) {
@@ -101,7 +107,9 @@ __global__ void k_noalloc_final(const unsigned long long *__restrict__ colmax, c
     const double difx = 0.25 * Re * (dxmin * dxmin) * sf_dif;
     const double dify = 0.25 * Re * (dy * dy) * sf_dif;
     dtp *= sf_par;
-    *dt_out = fmin(fmin(dta, fmin(difx, dify)), dtp);
+    // a non-finite velocity gives no valid step: NaN, which no comparison accepts
+    // (eif_decide_dt reports the same state as EIF_ERR_NONFINITE)
+    *dt_out = *nonfinite ? __longlong_as_double(0x7ff8000000000000ll) : fmin(fmin(dta, fmin(difx, dify)), dtp);
   }
 }
 
@@ -137,9 +145,9 @@ extern "C" int eif_decide_dt_noalloc(const double *ux, int ux_pitch, const doubl
   unsigned long long *scratch = nullptr;
   if (scratch_for_current_device(&scratch) != cudaSuccess) return EIF_ERR_CUDA;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  unsigned long long *colmax = scratch, *uymax = scratch + itot + 2;
-  // the array keeps the previous call's maxima: clear what this call reads
-  if (cudaMemsetAsync(scratch, 0, sizeof(unsigned long long) * (itot + 3), s) != cudaSuccess) return EIF_ERR_CUDA;
+  unsigned long long *colmax = scratch, *uymax = scratch + itot + 2, *nonfinite = scratch + itot + 3;
+  // the array keeps the previous call's maxima and marker: clear what this call reads
+  if (cudaMemsetAsync(scratch, 0, sizeof(unsigned long long) * (itot + 4), s) != cudaSuccess) return EIF_ERR_CUDA;
   int sms = 0;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return EIF_ERR_CUDA;
@@ -148,11 +156,12 @@ extern "C" int eif_decide_dt_noalloc(const double *ux, int ux_pitch, const doubl
   int gy = (jtot + NTY - 1) / NTY;
   if (gx * gy > sms * 8) gy = (sms * 8 + gx - 1) / gx;
   if (gy < 1) gy = 1;
-  k_noalloc_max<<<dim3(gx, gy), dim3(NTX, NTY), 0, s>>>(ux, uy, ux_pitch, uy_pitch, itot, jtot, colmax, uymax);
+  k_noalloc_max<<<dim3(gx, gy), dim3(NTX, NTY), 0, s>>>(ux, uy, ux_pitch, uy_pitch, itot, jtot, colmax, uymax,
+                                                         nonfinite);
   if (cudaGetLastError() != cudaSuccess) return EIF_ERR_CUDA;
   const double dx = 1. / itot, dy = ly / jtot;
   k_noalloc_final<<<1, 256, 0, s>>>(colmax, uymax, itot, dx, dy, Re, safefactors[0], safefactors[1], safefactors[2],
-                                    particles, n_particles, dt);
+                                    particles, n_particles, nonfinite, dt);
   if (cudaGetLastError() != cudaSuccess) return EIF_ERR_CUDA;
   return EIF_OK;
 }

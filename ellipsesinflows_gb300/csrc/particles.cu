@@ -359,7 +359,8 @@ __global__ void k_reset(double *__restrict__ P, int pcap, int np) {
 __global__ void k_increment(double *__restrict__ P, int pcap, int np, double gamma, double Fr2,
                             double *__restrict__ scal, unsigned long long *__restrict__ res_bits,
                             unsigned *__restrict__ counter, unsigned *__restrict__ arrivals,
-                            cudaGraphConditionalHandle handle, int use_handle) {
+                            unsigned long long *__restrict__ total, cudaGraphConditionalHandle handle,
+                            int use_handle) {
   const double dt = scal[0];
   double res = 0.;
   for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < np; n += gridDim.x * blockDim.x) {
@@ -402,6 +403,7 @@ __global__ void k_increment(double *__restrict__ P, int pcap, int np, double gam
     *arrivals = 0u;
     const double r = __longlong_as_double((long long)atomicExch(res_bits, 0ull));
     scal[1] = r;
+    *total += 1ull;   // sub-iterations run (eif_counters)
     // inside a step graph: the condition of the sub-iteration loop (main.c:40-48):
     // continue while the residual is not below 1e-8 and at most 101 sub-iterations ran
     if (use_handle) {
@@ -461,7 +463,8 @@ int launch_increment(eif_ctx *c, int rk) {
   const int blocks = std::max(1, std::min((c->np + 31) / 32, c->sms * 4));
   unsigned *counter = reinterpret_cast<unsigned *>(c->d_inc + 1);   // low word: loop counter
   k_increment<<<blocks, 32, 0, c->stream>>>(c->P, c->pcap, c->np, rk_coef(rk).gamma, Fr * Fr, c->d_scal, c->d_inc,
-                                             counter, counter + 1, c->loop_handle, c->in_loop ? 1 : 0);
+                                             counter, counter + 1, c->d_inc + 2, c->loop_handle,
+                                             c->in_loop ? 1 : 0);
   EIF_LAUNCH_CK(c);
   return EIF_OK;
 }

@@ -111,7 +111,10 @@ int eif_get_dt(eif_ctx *ctx, double *dt);
  * substeps[3] (may be NULL) receives the sub-iteration count of each stage */
 int eif_integrate(eif_ctx *ctx, int *substeps);
 /* nsteps times { decide_dt; integrate; step += 1; time += dt } without host
- * synchronisation between steps (src/main.c:71-77) */
+ * synchronisation between steps (src/main.c:71-77). Each step's error flags are
+ * read while the next step already runs: after an error the device state, the
+ * step counter and the time include the step that followed the failing one
+ * (at most one), and the counters always match the device state. */
 int eif_advance(eif_ctx *ctx, int nsteps);
 /* step counter and simulated time accumulated by eif_advance */
 int eif_get_time(eif_ctx *ctx, int *step, double *time);
@@ -243,6 +246,9 @@ int eif_update_particles(eif_ctx *ctx);                               /* src/sus
  *   particles:  device array of n_particles * EIF_NFIELDS doubles (may be NULL if 0)
  *   dt:         device pointer that receives the result, written on `stream`
  *   stream:     a cudaStream_t (NULL: the legacy default stream)
+ * A NaN or an infinity in the velocities read gives *dt = NaN (eif_decide_dt
+ * returns EIF_ERR_NONFINITE for the same state; this entry point has no flag
+ * output, and a NaN step fails every comparison a caller makes with it).
  * The first call on a device looks up the scratch address (do it before any
  * stream capture). All calls share the scratch array: calls that overlap on
  * the GPU race and must be serialised by the caller. */
@@ -283,6 +289,12 @@ int eif_profile_reset(eif_ctx *ctx);
 int eif_profile_count(eif_ctx *ctx, int *count);
 /* name, launch count and total device time (ms) of entry k */
 int eif_profile_get(eif_ctx *ctx, int k, char *name, int name_len, long long *launches, double *ms);
+/* work counters of the context (synchronises the stream): counts[0] = particle
+ * sub-iterations run since eif_create (every stage of every step, src/main.c:36-50);
+ * counts[1] = box cells whose indicator geometry was evaluated and counts[2] = those
+ * of them that ran the normal-foot iteration (src/ellipse.c:30-65), both counted
+ * only while kernel timing is enabled. No counterpart in the reference. */
+int eif_counters(eif_ctx *ctx, long long *counts);
 
 #ifdef __cplusplus
 }

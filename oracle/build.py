@@ -3,7 +3,8 @@
 ``build_port()`` compiles the C restatement (oracle/port/eif_port.c) into
 oracle/port/libeifport.so on any machine. ``build_ref()`` compiles the
 reference's own sources into oracle/_ref/ with oracle/ref/Makefile, which is
-possible only where the reference sources exist.
+possible only where the reference sources exist: the checkout named by
+EIF_REFERENCE_DIR, else a checkout called ``reference`` beside this repository.
 """
 import os
 import subprocess
@@ -11,7 +12,7 @@ import subprocess
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 PORT_SO = os.path.join(HERE, "port", "libeifport.so")
-REFERENCE_DIR = os.environ.get("EIF_REFERENCE_DIR", "/root/reference")
+REFERENCE_DIR = os.environ.get("EIF_REFERENCE_DIR") or os.path.join(os.path.dirname(ROOT), "reference")
 
 
 def build_port(force=False):

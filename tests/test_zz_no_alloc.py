@@ -66,6 +66,25 @@ def test_noalloc_dt_matches_decide_dt_on_two_calls_in_a_row(gpu_lib):
         assert call_noalloc(fn, case_b, ux_b, uy_b, p_b) == ref_b
 
 
+def test_noalloc_dt_is_nan_for_a_nonfinite_velocity(gpu_lib):
+    """One NaN cell: eif_decide_dt reports EIF_ERR_NONFINITE, this entry point returns a
+    NaN step; a following call on a finite state gets its dt again (the marker in the
+    shared scratch is cleared by every call)."""
+    from ellipsesinflows_gb300.capi import EifError
+    fn = noalloc_fn(gpu_lib)
+    case = cases.contact_cluster()
+    sim, ux, uy, parts = state_after(case, 2)
+    ref = sim.decide_dt()
+    bad = ux.copy()
+    bad[case.jtot // 2, case.itot // 3] = np.nan
+    assert np.isnan(call_noalloc(fn, case, bad, uy, parts))
+    sim.push_fluid(bad, uy, sim.pull_fluid()[2])
+    with pytest.raises(EifError) as err:
+        sim.decide_dt()
+    assert err.value.code == -6
+    assert call_noalloc(fn, case, ux, uy, parts) == ref
+
+
 def test_noalloc_rejects_grids_beyond_its_scratch(gpu_lib):
     fn = noalloc_fn(gpu_lib)
     sf = (ctypes.c_double * 3)(0.75, 0.75, 0.95)
