@@ -58,20 +58,40 @@ HBM_BYTES = {
     "mixed": {"predictor": 56, "correct": 64, "poisson_dct2": 32, "poisson_dct3": 16},
 }
 
-# DRAM bytes (read + write) per launch from one ncu capture of the mixed form at
-# 2048 x 4096 (profiles/kernels_suspension_2048x4096_mixed.md); used as the roofline's
-# `traffic` at that grid size only
+# DRAM bytes (read + write) per launch from ncu captures of the mixed form at
+# 2048 x 4096, with the source file each kernel is built from and that file's SHA-1 at
+# the capture: the roofline's `traffic` reports a stored value only while the source is
+# unchanged (otherwise null, marked stale)
 NCU_TRAFFIC = {
-    ("mixed", 2048, 4096): {"predictor": 434e6, "correct": 488e6, "poisson_dct2": 246e6,
-                            "poisson_dct3": 86e6},
+    ("mixed", 2048, 4096): {
+        "predictor": (434e6, "fluid.cu", None, "profiles/kernels_suspension_2048x4096_mixed.md"),
+        "correct": (488e6, "fluid.cu", None, "profiles/kernels_suspension_2048x4096_mixed.md"),
+        "poisson_dct2": (246e6, "poisson.cu", None, "profiles/kernels_suspension_2048x4096_mixed.md"),
+        "poisson_dct3": (86e6, "poisson.cu", None, "profiles/kernels_suspension_2048x4096_mixed.md"),
+    },
 }
+
+# Algorithmic bytes per cell-step of the whole step (three RK stages): the sum over
+# the streaming passes of one stage (predictor 9, IBM field update 4, right-hand side
+# and DCT-II 3, tridiagonal solve 2, DCT-III 2, projection and pressure 7 words) times
+# three stages, 81 words of 8 bytes; the mixed form keeps the explicit terms in single
+# precision (6 words of 4 bytes fewer per stage)
+STEP_BYTES = {"fp64": 81 * 8, "mixed": 81 * 8 - 3 * 6 * 4}
+
+# Measured single-precision FMA throughput of this GPU (an FMA-chain probe, 2 flops per
+# FMA), the denominator of the indicator kernel's pipe roofline
+FP32_TFLOPS_MEASURED = 69.9
+
+# FP32 flops (FFMA counted twice, FADD and FMUL once) per normal-foot evaluation of the
+# mixed-form indicator kernel, from an ncu capture (value, source), or None
+INDICATOR_FLOPS_PER_EVAL = None
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--no-fp64-leg", action="store_true")
@@ -82,6 +102,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-log-timing", action="store_true",
                     help="skip timing the logging reductions (keeps launch lists to the step's kernels)")
+    ap.add_argument("--accuracy-steps", type=int, default=None,
+                    help="steps of the mixed-vs-double comparison (default: the workload's run length)")
     return ap.parse_args()
 
 
@@ -217,6 +239,29 @@ def max_over_ranks(pg, value, device):
     return float(t.item())
 
 
+def workload_config(case, world):
+    """The config object both arms print (the same keys and values for the same workload)."""
+    return {"workload": case.name, "itot": case.itot, "jtot": case.jtot, "n_particles": case.n_particles,
+            "Re": case.Re,
+            "l2": "inputs larger than L2 (~%d MB of device state per step)" % (case.cells * 13 * 8 // 10**6),
+            "parallelism": "replicas" if world > 1 else "single GPU"}
+
+
+def timed_advance(sim, stream, steps, pg, device):
+    """Device time (ms, max over ranks) of `steps` steps of eif_advance, CUDA events on
+    the library's stream, with a barrier and a synchronisation on both sides."""
+    import torch
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier(pg, device)
+    torch.cuda.synchronize()
+    start.record(stream)
+    sim.advance(steps)
+    stop.record(stream)
+    torch.cuda.synchronize()
+    barrier(pg, device)
+    return max_over_ranks(pg, start.elapsed_time(stop), device)
+
+
 def run_ours(args, world, rank, local, pg):
     import torch
     from ellipsesinflows_gb300 import PREC_FP64, PREC_MIXED, Simulation, build
@@ -229,6 +274,7 @@ def run_ours(args, world, rank, local, pg):
     for _ in range(args.warmup):
         sim.advance(1)
     sim.synchronize()
+    sub0 = sim.counters()["substeps"]
     # ---- device-timed region: state resident in HBM, one CUDA graph per step ----
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
@@ -243,19 +289,19 @@ def run_ours(args, world, rank, local, pg):
         barrier(pg, local)
     ms = start.elapsed_time(stop)
     ms = max_over_ranks(pg, ms, local)
-    accuracy = None
-    fp64 = None
-    if prec == PREC_MIXED and not args.no_fp64_leg:
-        fp64, accuracy = fp64_leg(args, case, sim, local, pg, world)
+    substeps_timed = (sim.counters()["substeps"] - sub0) / (3.0 * args.steps)
     # ---- per-kernel device times: a separate pass with the library's event timer
-    # (host-driven launches, same kernels), after the comparison above ----
+    # (host-driven launches, same kernels), with the indicator work counted ----
     prof_steps = max(1, min(args.steps, 3))
+    cnt0 = sim.counters()
     sim._call("profile_reset", sim.ctx)
     sim._call("profile_enable", sim.ctx, 1)
     sim.advance(prof_steps)
     sim.synchronize()
     sim._call("profile_enable", sim.ctx, 0)
+    cnt1 = sim.counters()
     prof = profile_entries(sim)
+    counts = {k: cnt1[k] - cnt0[k] for k in cnt1}
     # ---- the logging reductions of one log event (divergence, momentum, energy) on
     # the device, against pulling the two velocity fields for a host reduction ----
     log_ms = None
@@ -269,6 +315,12 @@ def run_ours(args, world, rank, local, pg):
     e2e = None
     if not args.no_e2e:
         e2e = run_e2e(sim, case, args.steps, pg, local)
+    tiles = sim.tiles()
+    sim.close()
+    # ---- the double-precision form and the accuracy of the mixed form against it ----
+    accuracy = fp64 = developed = None
+    if prec == PREC_MIXED and not args.no_fp64_leg:
+        fp64, accuracy, developed = accuracy_leg(args, case, local, pg, world)
     cells = case.cells
     value = world * cells * args.steps / (ms / 1e3)
     hbm, hbm_src = peaks()
@@ -281,15 +333,19 @@ def run_ours(args, world, rank, local, pg):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if prec == PREC_FP64 else "f32+f64",
         "data": "synthetic (seeded ellipse placement, fluid at rest)",
-        "config": {"workload": case.name, "itot": case.itot, "jtot": case.jtot, "n_particles": case.n_particles,
-                   "Re": case.Re, "precision": args.precision,
-                   "l2": "inputs larger than L2 (~1 GB of device state per step)",
-                   "tiles": sim.tiles(),
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "config": workload_config(case, world),
+        "precision": args.precision,
         "e2e": e2e, "roofline": roof, "gpu_launches": launches,
-        "fp64_form": fp64, "accuracy_vs_fp64": accuracy,
+        "step_roofline": {"bytes_per_cell_step": STEP_BYTES[args.precision],
+                          "achieved": STEP_BYTES[args.precision] * value / world / 1e9, "peak": hbm,
+                          "unit": "GB/s", "frac": STEP_BYTES[args.precision] * value / world / 1e9 / hbm,
+                          "what": "algorithmic bytes of the whole step's streaming passes x cell-steps/s"},
+        "indicator": indicator_roofline(prof, counts, prof_steps),
+        "substeps_per_stage": substeps_timed,
+        "fp64_form": fp64, "accuracy_vs_fp64": accuracy, "developed_window": developed,
         "log_reductions_ms": log_ms,
         "clocks": clk.summary(),
+        "tiles": tiles,
         "kernels_per_step": {e["name"]: {"launches": round(e["launches"] / prof_steps, 2),
                                          "ms": round(e["ms"] / prof_steps, 4)} for e in prof},
     }
@@ -325,14 +381,13 @@ def run_batch(args, world, rank, local, pg):
         clk.end()
         barrier(pg, local)
     ms = max_over_ranks(pg, start.elapsed_time(stop), local)
-    # the same suspensions one after another (one graph launch per suspension and step)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        for s in sims:
-            s.advance(1)
-    torch.cuda.synchronize()
-    sep_ms = (time.perf_counter() - t0) * 1e3
+    # the same suspensions one after another, each advanced the same steps with
+    # eif_advance on its own stream, timed with CUDA events like the batch; the
+    # separate time is the sum of the suspensions' device times
+    sep_ms = 0.0
+    for s in sims:
+        st = torch.cuda.ExternalStream(s._fn("stream")(s.ctx), device=local)
+        sep_ms += timed_advance(s, st, args.steps, pg, local)
     batch.close()
     grids = sorted({"%dx%d" % (c.itot, c.jtot) for c in cs})
     out = {
@@ -347,7 +402,8 @@ def run_batch(args, world, rank, local, pg):
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "separate": {"value": cells * args.steps / (sep_ms / 1e3), "unit": "cell-steps/s",
                      "ms_per_step": sep_ms / args.steps,
-                     "how": "the same suspensions advanced one after another with eif_advance, host-timed"},
+                     "how": "the same suspensions advanced one after another with eif_advance, each "
+                            "timed with CUDA events on its own stream; the sum of their device times"},
         "e2e": None, "roofline": None, "clocks": clk.summary(),
     }
     return out, rank
@@ -415,36 +471,103 @@ def run_adjoint(args, world, rank, local, pg):
     return out, rank
 
 
-def fp64_leg(args, case, mixed_sim, device, pg, world):
-    """The plain double-precision form on the same workload and step count, and the
-    error of the mixed-precision state against it after the same number of steps."""
-    import torch
-    from ellipsesinflows_gb300 import PREC_FP64, Simulation
-    sim = Simulation.from_case(case, precision=PREC_FP64, device=device)
-    stream = torch.cuda.ExternalStream(sim._fn("stream")(sim.ctx), device=device)
-    for _ in range(args.warmup):
-        sim.advance(1)
-    sim.synchronize()
-    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    barrier(pg, device)
-    torch.cuda.synchronize()
-    start.record(stream)
-    sim.advance(args.steps)
-    stop.record(stream)
-    torch.cuda.synchronize()
-    ms = max_over_ranks(pg, start.elapsed_time(stop), device)
-    value = world * case.cells * args.steps / (ms / 1e3)
-    # both forms have now advanced warmup + steps steps from the same initial state
-    du, dv, _, _ = sim.pull_fluid()
-    mu, mv, _, _ = mixed_sim.pull_fluid()
+def field_errors(mix, ref):
+    """Errors of the mixed form's state against the double-precision form's after the
+    same number of steps: u, v (each relative to its own maximum), p with its mean
+    removed (relative), particle centres and angles (absolute), translational velocity
+    (relative to the largest |U|, |V|) and angular velocity (relative to the largest |W|)."""
+    from ellipsesinflows_gb300.capi import F
+    mu, mv, mp, _ = mix.pull_fluid()
+    du, dv, dp, _ = ref.pull_fluid()
+    rel = lambda a, b: float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))  # noqa: E731
+    pi_m, pi_d = mp[1:-1, 1:-1] - mp[1:-1, 1:-1].mean(), dp[1:-1, 1:-1] - dp[1:-1, 1:-1].mean()
+    out = {"u": rel(mu, du), "v": rel(mv, dv), "p": rel(pi_m, pi_d)}
+    pm, pd = mix.pull_particles(), ref.pull_particles()
+    if len(pd):
+        dyw = np.abs(pm[:, F["y"]] - pd[:, F["y"]])
+        dyw = np.minimum(dyw, ref.cfg.ly - dyw)   # centres wrap in y
+        daz = np.abs(pm[:, F["az"]] - pd[:, F["az"]])
+        daz = np.minimum(daz, 2 * np.pi - daz)    # angles wrap at 2 pi
+        uscale = max(np.abs(pd[:, F["ux"]]).max(), np.abs(pd[:, F["uy"]]).max(), 1e-300)
+        out.update({"x": float(np.abs(pm[:, F["x"]] - pd[:, F["x"]]).max()), "y": float(dyw.max()),
+                    "az": float(daz.max()),
+                    "U": float(np.abs(pm[:, F["ux"]] - pd[:, F["ux"]]).max() / uscale),
+                    "V": float(np.abs(pm[:, F["uy"]] - pd[:, F["uy"]]).max() / uscale),
+                    "Omega": rel(pm[:, F["vz"]], pd[:, F["vz"]])})
     umag = max(np.abs(du).max(), np.abs(dv).max())
-    err = max(np.abs(mu - du).max(), np.abs(mv - dv).max()) / umag
-    divmax, _ = mixed_sim.divergence()
-    divmax64, _ = sim.divergence()
-    sim.close()
-    return ({"value": value, "unit": "cell-steps/s", "ms_per_step": ms / args.steps},
-            {"steps_compared": args.warmup + args.steps, "velocity_rel_err": err, "max_divergence": divmax,
-             "max_divergence_fp64": divmax64})
+    vel = float(max(np.abs(mu - du).max(), np.abs(mv - dv).max()) / umag)
+    return out, vel
+
+
+def accuracy_leg(args, case, device, pg, world):
+    """The plain double-precision form on the same workload: its cell-steps/s on the
+    headline's window (steps W+1 .. W+K from the initial state) and on the last steps of
+    the run, and the error of the mixed form against it after the workload's full run
+    length (per field), with both forms' maximum divergence."""
+    import torch
+    from ellipsesinflows_gb300 import PREC_FP64, PREC_MIXED, Simulation
+    n = args.accuracy_steps or case.steps
+    win = max(1, min(20, n // 5))
+    ref = Simulation.from_case(case, precision=PREC_FP64, device=device)
+    mix = Simulation.from_case(case, precision=PREC_MIXED, device=device)
+    rs = torch.cuda.ExternalStream(ref._fn("stream")(ref.ctx), device=device)
+    ms_ = torch.cuda.ExternalStream(mix._fn("stream")(mix.ctx), device=device)
+    w, k = args.warmup, args.steps
+    if n < w + k + win:
+        raise ValueError("accuracy run of %d steps is shorter than warm-up + timed steps + %d" % (n, win))
+    ref.advance(w)
+    ms64 = timed_advance(ref, rs, k, pg, device)
+    ref.advance(n - w - k - win)
+    s0 = ref.counters()["substeps"]
+    ms64_dev = timed_advance(ref, rs, win, pg, device)
+    sub64 = (ref.counters()["substeps"] - s0) / (3.0 * win)
+    mix.advance(n - win)
+    s0 = mix.counters()["substeps"]
+    msmx_dev = timed_advance(mix, ms_, win, pg, device)
+    submx = (mix.counters()["substeps"] - s0) / (3.0 * win)
+    fields, vel = field_errors(mix, ref)
+    divmax, _ = mix.divergence()
+    divmax64, _ = ref.divergence()
+    tm, td = mix.time_state()[1], ref.time_state()[1]
+    ref.close()
+    mix.close()
+    cells = case.cells
+    window = "steps %d-%d" % (n - win + 1, n)
+    fp64 = {"value": world * cells * k / (ms64 / 1e3), "unit": "cell-steps/s", "ms_per_step": ms64 / k,
+            "window": "steps %d-%d (the headline's window)" % (w + 1, w + k),
+            "developed": {"window": window, "value": world * cells * win / (ms64_dev / 1e3),
+                          "ms_per_step": ms64_dev / win, "substeps_per_stage": sub64}}
+    accuracy = {"steps_compared": n, "fields": fields, "velocity_rel_err": vel, "max_divergence": divmax,
+                "max_divergence_fp64": divmax64, "time_mixed": tm, "time_fp64": td,
+                "how": "both forms advanced %d steps from the same initial state, each with its own dt; "
+                       "u, v, p (mean removed), U, V, Omega relative; x, y, az absolute" % n}
+    developed = {"window": window, "value": world * cells * win / (msmx_dev / 1e3), "unit": "cell-steps/s",
+                 "ms_per_step": msmx_dev / win, "substeps_per_stage": submx,
+                 "vs_fp64_developed": ms64_dev / msmx_dev}
+    return fp64, accuracy, developed
+
+
+def indicator_roofline(prof, counts, prof_steps):
+    """The indicator kernel (normal-foot iteration of every near cell, the step's largest
+    kernel): work counted on the device during the profiling pass, over its live event
+    time; FP32 pipe use from the flops per normal-foot evaluation of an ncu capture."""
+    e = next((q for q in prof if q["name"] == "ibm_indicator"), None)
+    if e is None or e["ms"] <= 0 or counts.get("normal_foot_evals", 0) <= 0:
+        return None
+    total = sum(q["ms"] for q in prof) or 1.0
+    sec = e["ms"] / 1e3
+    evals, cells = counts["normal_foot_evals"], counts["indicator_cells"]
+    out = {"kernel": "ibm_indicator", "bound": "issue", "launches_per_step": e["launches"] / prof_steps,
+           "box_cells_per_launch": cells / e["launches"], "normal_foot_evals_per_launch": evals / e["launches"],
+           "box_cells_per_s": cells / sec, "normal_foot_evals_per_s": evals / sec,
+           "share_of_step": e["ms"] / total}
+    fl = INDICATOR_FLOPS_PER_EVAL
+    if fl is not None:
+        achieved = evals / sec * fl[0] / 1e12
+        out.update({"fp32_flops_per_eval": fl[0], "flops_source": fl[1], "achieved": achieved,
+                    "peak": FP32_TFLOPS_MEASURED, "unit": "TFLOP/s", "frac": achieved / FP32_TFLOPS_MEASURED,
+                    "peak_source": "measured FP32 FMA-chain probe"})
+    return out
 
 
 def profile_entries(sim):
@@ -464,10 +587,30 @@ def profile_entries(sim):
     return out
 
 
+def source_sha(name):
+    import hashlib
+    path = os.path.join(ROOT, "ellipsesinflows_gb300", "csrc", name)
+    try:
+        with open(path, "rb") as f:
+            return hashlib.sha1(f.read()).hexdigest()
+    except OSError:
+        return None
+
+
+def stored_traffic(precision, grid, kernel):
+    """(bytes, source) of a stored ncu capture of `kernel`, or (None, why not)."""
+    rec = NCU_TRAFFIC.get((precision,) + tuple(grid or ()), {}).get(kernel)
+    if rec is None:
+        return None, None
+    value, src, sha, where = rec
+    if sha is None or source_sha(src) != sha:
+        return None, "stale: %s changed since the capture in %s" % (src, where)
+    return value, "ncu capture (%s, %s at sha1 %s)" % (where, src, sha[:12])
+
+
 def roofline(prof, cells, hbm, hbm_src, precision, grid=None):
     """Roofline of the dominant streaming kernel against the measured copy bandwidth."""
     table = HBM_BYTES[precision]
-    ncu = NCU_TRAFFIC.get((precision,) + tuple(grid or ()), {})
     total = sum(e["ms"] for e in prof) or 1.0
     stream = [e for e in prof if e["name"] in table and e["launches"] > 0]
     if not stream:
@@ -477,9 +620,10 @@ def roofline(prof, cells, hbm, hbm_src, precision, grid=None):
     bytes_per_launch = table[top["name"]] * float(cells)
     achieved = bytes_per_launch / (per_launch_ms / 1e3) / 1e9
     dominant = prof[0]
+    traffic, traffic_src = stored_traffic(precision, grid, top["name"])
     return {"bound": "hbm", "kernel": top["name"], "achieved": achieved, "peak": hbm, "unit": "GB/s",
-            "frac": achieved / hbm, "peak_source": hbm_src, "traffic": ncu.get(top["name"]),
-            "traffic_source": "ncu capture, one launch" if top["name"] in ncu else None,
+            "frac": achieved / hbm, "peak_source": hbm_src, "traffic": traffic,
+            "traffic_source": traffic_src,
             "algorithmic_bytes_per_launch": bytes_per_launch, "share_of_step": top["ms"] / total,
             "dominant_kernel": dominant["name"], "dominant_share": dominant["ms"] / total}
 
@@ -527,7 +671,10 @@ def cpu_baseline(args, case):
 
 
 def run_reference(args, world, rank):
-    """Reference arm: the CPU restatement of the reference algorithm on all host threads."""
+    """Reference arm: the CPU restatement of the reference algorithm (oracle/port, pinned
+    bit-for-bit to the reference's own sources) on all host threads, on the same
+    workload, metric and step counts: W warm-up steps, then K timed steps, each one
+    full time step of the workload from its initial state."""
     if rank != 0:
         return None, rank
     from oracle import port
@@ -536,23 +683,20 @@ def run_reference(args, world, rank):
     s = port.PortSolver(case.config(), threads=threads)
     s.push_fluid(*case.fluid())
     s.push_particles(case.particles)
-    # bounded sample: each timed step is one full time step of the workload
-    warm = min(args.warmup, 1)
-    steps = max(1, min(args.steps, 2))
-    for _ in range(warm):
+    for _ in range(args.warmup):
         s.step()
     t0 = time.perf_counter()
-    for _ in range(steps):
+    for _ in range(args.steps):
         s.step()
     el = time.perf_counter() - t0
-    value = case.cells * steps / el
-    sample = "%d timed + %d warm-up full time steps of %s (cap of 2 timed steps keeps the CPU run bounded)" % (
-        steps, warm, case.name)
-    out = {"metric": "cell-steps/s", "value": value, "unit": "cell-steps/s", "n_gpus": world, "steps": steps,
-           "warmup": warm, "ms_per_step": 1e3 * el / steps, "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded ellipse placement, fluid at rest)",
-           "config": {"workload": case.name, "itot": case.itot, "jtot": case.jtot, "n_particles": case.n_particles,
-                      "Re": case.Re, "precision": "fp64"},
+    value = case.cells * args.steps / el
+    sample = "%d timed full time steps of %s after %d warm-up steps, from its initial state" % (
+        args.steps, case.name, args.warmup)
+    out = {"metric": "cell-steps/s", "value": value, "unit": "cell-steps/s", "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (seeded ellipse placement, fluid at rest)",
+           "config": workload_config(case, world), "precision": "fp64",
            "impl": "reference",
            "cpu_baseline": {"value": value, "unit": "cell-steps/s", "cores": threads, "kind": "port",
                             "sample": sample},
