@@ -52,10 +52,15 @@ FALLBACK_HBM_GBS = 6800.0
 # kernel per timer scope: predictor (u, v, p, srcB read; srcA, u', v' written),
 # projection (u, v, p read and written, psi and the IBM field read), DCT-II (u, v and
 # the IBM field read, the transformed row written), DCT-III (solution read, psi
-# written). The mixed form keeps the IBM field in single precision.
+# written). The mixed form keeps the IBM field in single precision and solves the
+# Poisson equation in two single-precision passes: DCT-II of the first pass reads u,
+# v and the IBM field (24 B) and writes the right-hand side as a float pair (8 B) and
+# its transform (4 B); that of the second reads the pair and psi1 (12 B) and writes
+# its transform (4 B): 26 B per launch on average; each DCT-III reads the block
+# solution (4 B) and writes psi1 or psi2 (4 B).
 HBM_BYTES = {
     "fp64": {"predictor": 72, "correct": 72, "poisson_dct2": 40, "poisson_dct3": 16},
-    "mixed": {"predictor": 56, "correct": 64, "poisson_dct2": 32, "poisson_dct3": 16},
+    "mixed": {"predictor": 56, "correct": 64, "poisson_dct2": 26, "poisson_dct3": 8},
 }
 
 # DRAM bytes (read + write) per launch from ncu captures of the mixed form at
@@ -71,11 +76,12 @@ NCU_TRAFFIC = {
     },
 }
 
-# Algorithmic bytes per cell-step of the whole step (three RK stages): the sum over
-# the streaming passes of one stage (predictor 9, IBM field update 4, right-hand side
-# and DCT-II 3, tridiagonal solve 2, DCT-III 2, projection and pressure 7 words) times
-# three stages, 81 words of 8 bytes; the mixed form keeps the explicit terms in single
-# precision (6 words of 4 bytes fewer per stage)
+# Algorithmic bytes per cell-step of the whole step (three RK stages), the formula of
+# the double-precision algorithm: the sum over the streaming passes of one stage
+# (predictor 9, IBM field update 4, right-hand side and DCT-II 3, tridiagonal solve 2,
+# DCT-III 2, projection and pressure 7 words) times three stages, 81 words of 8 bytes;
+# the mixed form keeps the explicit terms in single precision (6 words of 4 bytes
+# fewer per stage)
 STEP_BYTES = {"fp64": 81 * 8, "mixed": 81 * 8 - 3 * 6 * 4}
 
 # Measured single-precision FMA throughput of this GPU (an FMA-chain probe, 2 flops per

@@ -536,7 +536,15 @@ int eif_pull_fluid(eif_ctx *c, double *ux, double *uy, double *p, double *psi) {
   if (ux && (rc = rows_out(c, ux, c->ux[c->cur], c->itot + 1, rows))) return rc;
   if (uy && (rc = rows_out(c, uy, c->uy[c->cur], c->itot + 2, rows))) return rc;
   if (p && (rc = rows_out(c, p, c->p, c->itot + 2, rows))) return rc;
-  if (psi && (rc = rows_out(c, psi, c->psi, c->itot + 2, rows))) return rc;
+  if (psi) {
+    // psi in double: the field itself, or psi1 + psi2 of the refined solve widened in scratch
+    const double *src = c->psi;
+    if (c->psi_pair) {
+      if ((rc = launch_psi_to_double(c, c->qhat))) return rc;
+      src = c->qhat;
+    }
+    if ((rc = rows_out(c, psi, src, c->itot + 2, rows))) return rc;
+  }
   EIF_CK(c, cudaStreamSynchronize(c->stream));
   return check_records(c);
 }

@@ -66,6 +66,11 @@ struct PoissonPlan {
   double2 *rot;     // exp(-i pi k / 2n), k < n
   double2 *wn;      // exp(-2 pi i k / n), k < n
   float4 *tw_f, *rot_f, *wn_f;  // the same tables as float pairs (re hi, re lo, im hi, im lo)
+  // single-precision tables of the refined solve (mixed form): twiddles (re, im) and
+  // the block Thomas factors and left responses, [i][k] like tdm_inv, tdm_up, tdm_g
+  float2 *tw2 = nullptr, *rot2 = nullptr, *wn2 = nullptr;
+  float *tdm_inv_f = nullptr, *tdm_up_f = nullptr, *tdm_g_f = nullptr;
+  float2 *qdf = nullptr;   // right-hand side of the first pass as (hi, lo) pairs, jtot rows of pitch ld
   // tridiagonal solver along y (jtot rows, one system per wavenumber)
   int blk;          // interior rows per block + 1 (EIF_TDM_M), or 0: serial path
   int nblk;         // blocks per column (jtot / blk)
@@ -161,6 +166,12 @@ struct eif_ctx {
   // hold NaN (multiplied by beta = 0 in the first stage, which still gives NaN), so the
   // next fluid push clears them, as the reference's fluid_init starts them at zero
   bool src_nonfinite = false;
+  // the mixed form solves the Poisson equation in single precision with one refinement
+  // whose right-hand side is the residual formed in double-float arithmetic: psi is then
+  // kept as the two single-precision solutions psi1, psi2 (psi = psi1 + psi2), psi1 in
+  // the first nfield floats of the psi buffer and psi2 in the next nfield, both with the
+  // uy layout (pitch ld, halo rows and ghost columns)
+  bool psi_pair = false;
   bool boxes_x_valid = false;   // the IBM boxes hold the positions X (see launch_boxes)
   bool weights_x_valid = false; // wcache holds the indicator weights of those boxes
   void *wcache = nullptr;       // indicator weight per IBM task slot (wcap entries)
@@ -258,6 +269,8 @@ int launch_coef(eif_ctx *c);
 int poisson_init(eif_ctx *c);
 void poisson_free(eif_ctx *c);
 int launch_potential(eif_ctx *c, int rk, bool with_ibm);
+// psi as doubles (psi1 + psi2 when psi_pair is set) into dst (nfield doubles)
+int launch_psi_to_double(eif_ctx *c, double *dst);
 
 // ---- immersed boundary (ibm.cu) ----
 size_t ibm_tasks_needed(const eif_ctx *c, const double *rec, int n);

@@ -341,6 +341,10 @@ __global__ void __launch_bounds__(TX *TY) k_correct(CorrArgs a) {
 struct CorrArgsDF {
   double *ux, *uy, *p;
   const double *psi;
+  // psi as the float pair psi1 + psi2 of the refined solve (psi1 at psi, psi2 at
+  // psi1 + psi2_off floats), or null: psi in double
+  const float *psi1;
+  size_t psi2_off;
   const float *dux, *duy;   // IBM field response in single precision
   const float2 *rdxc;       // 1/dxc as (hi, lo)
   const float *coef;        // [20 + 2 rk], [21 + 2 rk]: gamma dt
@@ -365,9 +369,29 @@ __global__ void __launch_bounds__(TX *TY) k_correct_df(CorrArgsDF a) {
   const double u_old = xface ? a.ux[c] : 0.;
   const double v_old = vel ? a.uy[cy] : 0.;
   const double p_old = a.with_pressure ? a.p[cy] : 0.;
-  const double psi0 = (a.with_proj || a.with_pressure) ? __ldg(a.psi + cy) : 0.;
-  const double psi_w = (a.with_proj && xface) ? __ldg(a.psi + cy - 1) : 0.;
-  const double psi_s = (a.with_proj && vel) ? __ldg(a.psi + cy - ld) : 0.;
+  // psi at the cell and its west and south neighbours: doubles, or float pairs
+  double psi0 = 0., psi_w = 0., psi_s = 0.;
+  DF q0{0.f, 0.f}, qw{0.f, 0.f}, qs{0.f, 0.f};
+  const bool need0 = a.with_proj || a.with_pressure, needw = a.with_proj && xface, needs = a.with_proj && vel;
+  if (a.psi1) {
+    const float *p2 = a.psi1 + a.psi2_off;
+    if (need0) q0 = DF{__ldg(a.psi1 + cy), __ldg(p2 + cy)};
+    if (needw) qw = DF{__ldg(a.psi1 + cy - 1), __ldg(p2 + cy - 1)};
+    if (needs) qs = DF{__ldg(a.psi1 + cy - ld), __ldg(p2 + cy - ld)};
+  } else {
+    if (need0) psi0 = __ldg(a.psi + cy);
+    if (needw) psi_w = __ldg(a.psi + cy - 1);
+    if (needs) psi_s = __ldg(a.psi + cy - ld);
+  }
+  // psi_0 - psi_nb as a double-float: exact double differences, or the difference of
+  // two float pairs (an exact difference of the leading parts)
+  auto dpsi = [&](double pnb, DF qnb) -> DF {
+    if (a.psi1) {
+      const DF s = two_sum(q0.hi, -qnb.hi);
+      return fast_sum(s.hi, s.lo + (q0.lo - qnb.lo));
+    }
+    return df_of(psi0 - pnb);
+  };
   float dw = 0.f, de = 0.f, ds = 0.f, dn = 0.f;
   if (a.with_ibm) {
     if (xface) { dw = __ldg(a.dux + cy - 1); de = __ldg(a.dux + cy); }
@@ -381,7 +405,7 @@ __global__ void __launch_bounds__(TX *TY) k_correct_df(CorrArgsDF a) {
     if (a.with_ibm) inc = two_sum(dw, de);
     inc = df_scale(inc, 0.5f);
     if (a.with_proj) {
-      const DF g = df_mul(df_mul(gdt, df_of(psi0 - psi_w)), DF{r.x, r.y});
+      const DF g = df_mul(df_mul(gdt, dpsi(psi_w, qw)), DF{r.x, r.y});
       inc = df_add_nw(inc, df_neg(g));
     }
     const double u = u_old + df_to_double(inc);
@@ -394,7 +418,7 @@ __global__ void __launch_bounds__(TX *TY) k_correct_df(CorrArgsDF a) {
     if (a.with_ibm) inc = two_sum(ds, dn);
     inc = df_scale(inc, 0.5f);
     if (a.with_proj) {
-      const DF g = df_mul(df_mul(gdt, df_of(psi0 - psi_s)), a.rdy);
+      const DF g = df_mul(df_mul(gdt, dpsi(psi_s, qs)), a.rdy);
       inc = df_add_nw(inc, df_neg(g));
     }
     const double v = v_old + df_to_double(inc);
@@ -403,7 +427,7 @@ __global__ void __launch_bounds__(TX *TY) k_correct_df(CorrArgsDF a) {
     if (j == jtot) a.uy[cy - jtot * ld] = v;
   }
   if (a.with_pressure) {
-    const double pv = p_old + psi0;
+    const double pv = p_old + (a.psi1 ? eifd::f2d(q0.hi) + eifd::f2d(q0.lo) : psi0);
     a.p[cy] = pv;
     if (j == 1) a.p[cy + jtot * ld] = pv;
     if (j == jtot) a.p[cy - jtot * ld] = pv;
@@ -763,6 +787,8 @@ static int launch_corr(eif_ctx *c, int rk, int with_ibm, int with_proj, int with
     a.uy = c->uy[c->cur];
     a.p = c->p;
     a.psi = c->psi;
+    a.psi1 = c->psi_pair ? reinterpret_cast<const float *>(c->psi) : nullptr;
+    a.psi2_off = c->nfield;
     a.dux = reinterpret_cast<const float *>(c->dux);
     a.duy = reinterpret_cast<const float *>(c->duy);
     a.rdxc = c->rdxc_df;

@@ -270,8 +270,11 @@ __global__ void __launch_bounds__(RED_THREADS) k_tdm_reduced(double *__restrict_
 // (A2 = A phi[G-2], B2 = B + 2 A phi[0], the reference's cyclic algorithm as at the
 // first level, kx = 0 pinned with its last value 0); every thread then adds
 // t_{g-1} phi[i] + t_g phi[G-2-i] to its interior. Block: RED2_K wavenumbers x Q
-// groups (16 wavenumbers per block spread the FP64 work over 128 SMs at 2048 x 4096).
-constexpr int RED2_K = 16;
+// groups (8 wavenumbers per block spread the FP64 work over 256 blocks at 2048 x 4096);
+// the factors of the Q-value solve are staged in shared memory by the whole block
+// before its serial sweep.
+constexpr int RED2_K = 8;
+constexpr size_t red2_smem_bytes(int Q) { return sizeof(double) * 6 * RED2_K * (size_t)Q; }
 template <int G>
 __global__ void __launch_bounds__(1024) k_tdm_reduced2(double *__restrict__ iface, const double *__restrict__ first,
                                                        const double *__restrict__ rcoef, const double *__restrict__ inv2,
@@ -279,14 +282,23 @@ __global__ void __launch_bounds__(1024) k_tdm_reduced2(double *__restrict__ ifac
                                                        const double *__restrict__ ri2, const double *__restrict__ ru2,
                                                        const double *__restrict__ rq2, const double *__restrict__ rc2,
                                                        double l, int itot, int P, int Q) {
-  extern __shared__ double sm2[];   // [Q][RED2_K] first interior values, right-hand sides, interface values
+  // [Q][RED2_K] first interior values, right-hand sides, interface values, and the
+  // second-level factors ri2, ru2, rq2
+  extern __shared__ double sm2[];
   constexpr int K = RED2_K;
   double *y0s = sm2, *rhs = sm2 + (size_t)Q * K, *ts = sm2 + (size_t)2 * Q * K;
+  double *s_ri = sm2 + (size_t)3 * Q * K, *s_ru = sm2 + (size_t)4 * Q * K, *s_rq = sm2 + (size_t)5 * Q * K;
   const int kk = threadIdx.x % K, g = threadIdx.x / K;
   const int k = blockIdx.x * K + kk;
   const bool on = k < itot;
   const int kc = on ? k : itot - 1;
   const double A = rcoef[4 * kc + 0];
+  // the factors of the second-level sweep (q < Q - 1; the tables hold max(G, Q) rows)
+  if (g < Q - 1) {
+    s_ri[g * K + kk] = ri2[(size_t)g * itot + kc];
+    s_ru[g * K + kk] = ru2[(size_t)g * itot + kc];
+    s_rq[g * K + kk] = rq2[(size_t)g * itot + kc];
+  }
   double y[G];
   // level-one reduced right-hand sides R_b = (r_iface - l y_b[M-2]) - l y_{b+1}[0]
 #pragma unroll
@@ -307,19 +319,19 @@ __global__ void __launch_bounds__(1024) k_tdm_reduced2(double *__restrict__ ifac
   if (g == 0) {
     const double A2 = rc2[4 * kc + 0], den2 = rc2[4 * kc + 2];
     const bool pin = rc2[4 * kc + 3] != 0.;
-    double zprev = rhs[kk] * ri2[kc];
+    double zprev = rhs[kk] * s_ri[kk];
     ts[kk] = zprev;
     for (int q = 1; q < Q - 1; q++) {
-      zprev = (rhs[q * K + kk] - A2 * zprev) * ri2[(size_t)q * itot + kc];
+      zprev = (rhs[q * K + kk] - A2 * zprev) * s_ri[q * K + kk];
       ts[q * K + kk] = zprev;
     }
     for (int q = Q - 3; q >= 0; q--) {
-      zprev = ts[q * K + kk] - ru2[(size_t)q * itot + kc] * zprev;
+      zprev = ts[q * K + kk] - s_ru[q * K + kk] * zprev;
       ts[q * K + kk] = zprev;
     }
     const double num = rhs[(Q - 1) * K + kk] - A2 * ts[kk] - A2 * ts[(Q - 2) * K + kk];
     const double last = pin ? 0. : num / den2;
-    for (int q = 0; q < Q - 1; q++) ts[q * K + kk] = ts[q * K + kk] + last * rq2[(size_t)q * itot + kc];
+    for (int q = 0; q < Q - 1; q++) ts[q * K + kk] = ts[q * K + kk] + last * s_rq[q * K + kk];
     ts[(Q - 1) * K + kk] = last;
   }
   __syncthreads();
@@ -1135,6 +1147,330 @@ __global__ void __launch_bounds__(256) k_tdm_local_df(float2 *__restrict__ qhat,
   first[(size_t)b * itot + k] = df_to_double(v[0]);
 }
 
+// ---------------------------------------------------------------------------
+// Single-precision solve with one refinement (mixed form, power-of-two half lengths
+// with the block tridiagonal solver). The Poisson equation L psi = q (q the
+// divergence of u** over gamma dt, compute_potential.c:70-134) is solved twice with
+// single-precision transforms and block Thomas sweeps (the reduced cyclic systems of
+// the interface values stay in double precision):
+//   pass 1: L psi1 = q,               psi1 stored as float
+//   pass 2: L psi2 = q - L psi1,      the residual formed in double-float arithmetic
+//                                      from the exact double differences of u** and the
+//                                      float values of psi1
+// and psi = psi1 + psi2 is kept as the float pair (psi1, psi2). A single-precision
+// solve leaves a residual of about 1e-6 (smooth right-hand sides: 1e-2) of |q|; the
+// refinement solves for that residual and leaves about 1e-12 (1e-8).
+struct CF { float re, im; };
+__device__ __forceinline__ CF cf_add(CF a, CF b) { return CF{a.re + b.re, a.im + b.im}; }
+__device__ __forceinline__ CF cf_sub(CF a, CF b) { return CF{a.re - b.re, a.im - b.im}; }
+__device__ __forceinline__ CF cf_mul(CF a, float2 w) {
+  return CF{fmaf(a.re, w.x, -a.im * w.y), fmaf(a.re, w.y, a.im * w.x)};
+}
+template <int S> __device__ __forceinline__ CF cf_mul_si(CF a) { return S > 0 ? CF{-a.im, a.re} : CF{a.im, -a.re}; }
+// multiplication by exp(S i pi/4) = (sqrt(2)/2)(1 + S i)
+template <int S> __device__ __forceinline__ CF cf_mul_w8(CF a) {
+  const float h = 0.70710678118654752f;
+  return S > 0 ? CF{(a.re - a.im) * h, (a.im + a.re) * h} : CF{(a.re + a.im) * h, (a.im - a.re) * h};
+}
+// radix-4 butterfly on v[o], v[o + st], v[o + 2 st], v[o + 3 st], outputs in natural order
+template <int S, int O, int ST, int N> __device__ __forceinline__ void dft4_f(CF (&v)[N]) {
+  const CF s02 = cf_add(v[O], v[O + 2 * ST]), d02 = cf_sub(v[O], v[O + 2 * ST]);
+  const CF s13 = cf_add(v[O + ST], v[O + 3 * ST]), d13 = cf_mul_si<S>(cf_sub(v[O + ST], v[O + 3 * ST]));
+  v[O] = cf_add(s02, s13);
+  v[O + ST] = cf_add(d02, d13);
+  v[O + 2 * ST] = cf_sub(s02, s13);
+  v[O + 3 * ST] = cf_sub(d02, d13);
+}
+// 8-point DFT of v (sign S), result in natural order (n = 2 n1 + n2, k = k1 + 4 k2)
+template <int S> __device__ __forceinline__ void dft8_f(CF (&v)[8]) {
+  dft4_f<S, 0, 2>(v);
+  dft4_f<S, 1, 2>(v);
+  v[3] = cf_mul_w8<S>(v[3]);
+  v[5] = cf_mul_si<S>(v[5]);
+  v[7] = cf_mul_si<S>(cf_mul_w8<S>(v[7]));
+  CF w[8];
+#pragma unroll
+  for (int k1 = 0; k1 < 4; k1++) {
+    w[k1] = cf_add(v[2 * k1], v[2 * k1 + 1]);
+    w[k1 + 4] = cf_sub(v[2 * k1], v[2 * k1 + 1]);
+  }
+#pragma unroll
+  for (int k = 0; k < 8; k++) v[k] = w[k];
+}
+template <int S> __device__ __forceinline__ float2 twiddle_f(const float2 *__restrict__ tw, int e) {
+  float2 w = __ldg(tw + e);
+  if (S > 0) w.y = -w.y;
+  return w;
+}
+// the last pass of radix R = 2 or 4: butterfly j (< L) reads and writes j + u L
+template <int S, int R>
+__device__ __forceinline__ void fft_last_f(CF *buf, CF (&v)[8], int t, int T, int L, const float2 *__restrict__ tw) {
+#pragma unroll
+  for (int q = 0; q < 8 / R; q++) {
+    const int j = t + q * T;
+#pragma unroll
+    for (int u = 0; u < R; u++) {
+      CF x = buf[padv<8>(j + u * L)];
+      if (u > 0 && j > 0) x = cf_mul(x, twiddle_f<S>(tw, u * j));
+      v[q * R + u] = x;
+    }
+  }
+  if constexpr (R == 2) {
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const CF a = v[2 * q], b = v[2 * q + 1];
+      v[2 * q] = cf_add(a, b);
+      v[2 * q + 1] = cf_sub(a, b);
+    }
+  } else {
+    dft4_f<S, 0, 1>(v);
+    dft4_f<S, 4, 1>(v);
+  }
+#pragma unroll
+  for (int q = 0; q < 8 / R; q++) {
+    const int j = t + q * T;
+#pragma unroll
+    for (int u = 0; u < R; u++) buf[padv<8>(j + u * L)] = v[q * R + u];
+  }
+}
+// Stockham transform of one row of m = 8 T values (radix-8 passes, then radix 2 or 4):
+// v holds the inputs x[t + u T] of thread t on entry; on exit the spectrum is in buf
+// (padded layout) and visible to the whole CTA
+template <int S>
+__device__ void fft_row_f(CF *buf, CF (&v)[8], int t, int T, int m, const float2 *__restrict__ tw) {
+  dft8_f<S>(v);
+  __syncthreads();
+#pragma unroll
+  for (int u = 0; u < 8; u++) buf[padv<8>(8 * t + u)] = v[u];
+  __syncthreads();
+  int L = 8, lgL = 3;
+  while (L * 8 <= m) {
+    const int k = t & (L - 1), blk = t >> lgL;
+    const int tws = m >> (lgL + 3);
+#pragma unroll
+    for (int u = 0; u < 8; u++) {
+      CF x = buf[padv<8>(t + u * T)];
+      if (u > 0 && k > 0) x = cf_mul(x, twiddle_f<S>(tw, u * k * tws));
+      v[u] = x;
+    }
+    dft8_f<S>(v);
+    __syncthreads();
+    const int o = blk * L * 8 + k;
+#pragma unroll
+    for (int u = 0; u < 8; u++) buf[padv<8>(o + u * L)] = v[u];
+    __syncthreads();
+    L <<= 3;
+    lgL += 3;
+  }
+  const int R = m / L;
+  if (R > 1) {
+    if (R == 2) fft_last_f<S, 2>(buf, v, t, T, L, tw);
+    else fft_last_f<S, 4>(buf, v, t, T, L, tw);
+    __syncthreads();
+  }
+}
+
+struct Dct2ArgsF {
+  const double *ux, *uy;
+  const float *dux, *duy;   // IBM field response in single precision
+  const float *coef;        // [12 + 2 rk], [13 + 2 rk]: 1/(gamma dt) as a float pair
+  const float *psi1;        // refinement pass: the first solution (uy layout), else null
+  float2 *qdf;              // q as (hi, lo) pairs: written by the first pass, read by the second
+  float *q;                 // transformed right-hand side, rows of pitch ld floats
+  const float2 *tw, *rot, *wn;
+  DF rdx, rdy, rdx2, rdy2;  // 1/dx, 1/dy, 1/dx^2, 1/dy^2
+  int itot, jtot, ld, with_ibm, rk;
+};
+
+// right-hand side (or the residual of the first solution) + single-precision DCT-II
+// of rows; one row of m = itot/2 complex values per T = m/8 threads
+__global__ void __launch_bounds__(FFT_CTA) k_dct2_f(Dct2ArgsF a, FftShape sh) {
+  extern __shared__ float4 sm4[];
+  const int n = a.itot, m = n / 2, ld = a.ld;
+  const int T = sh.T;
+  const int rloc = threadIdx.x >> sh.lgT, t = threadIdx.x & (T - 1);
+  const int jr = blockIdx.x * sh.rows + rloc;
+  const bool live = jr < a.jtot;
+  const int j = 1 + jr;
+  CF *buf = reinterpret_cast<CF *>(sm4) + rloc * (m + m / 8);
+  float *vq = reinterpret_cast<float *>(buf);
+  if (live && !a.psi1) {
+    // (1/(gamma dt)) / dx and (1/(gamma dt)) / dy
+    const DF inv = DF{__ldg(a.coef + 12 + 2 * a.rk), __ldg(a.coef + 13 + 2 * a.rk)};
+    const DF ax = df_mul(inv, a.rdx), ay = df_mul(inv, a.rdy);
+    float2 *qrow = a.qdf + (size_t)jr * ld;
+#pragma unroll 4
+    for (int i0 = t; i0 < n; i0 += T) {
+      const int i = i0 + 1;
+      const int c = uy_idx(i, j, ld);
+      // differences of neighbouring doubles as float pairs, from their integer splits
+      // (no double arithmetic): exact leading parts, trailing parts to 2^-48 of |u|
+      const float2 ue = eifd::split(__ldg(a.ux + ux_idx(i + 1, j, ld))), uw = eifd::split(__ldg(a.ux + ux_idx(i, j, ld)));
+      const float2 vn = eifd::split(__ldg(a.uy + c + ld)), vs = eifd::split(__ldg(a.uy + c));
+      DF dux_ = dfl_sub(DF{ue.x, ue.y}, DF{uw.x, uw.y}), duy_ = dfl_sub(DF{vn.x, vn.y}, DF{vs.x, vs.y});
+      if (a.with_ibm) {
+        // (u + (d0 + de)/2) - (u + (dw + d0)/2): the increments (de - dw)/2, (en - ds)/2
+        const float dw = (i >= 2) ? __ldg(a.dux + c - 1) : -__ldg(a.dux + c);
+        const float de = (i + 1 <= n) ? __ldg(a.dux + c + 1) : -__ldg(a.dux + c);
+        dux_ = dfl_add(dux_, df_scale(two_sum(de, -dw), 0.5f));
+        duy_ = dfl_add(duy_, df_scale(two_sum(__ldg(a.duy + c + ld), -__ldg(a.duy + c - ld)), 0.5f));
+      }
+      const DF qq = dfl_add(dfl_mulc(dux_, ax), dfl_mulc(duy_, ay));
+      const DF q = fast_sum(qq.hi, qq.lo);
+      qrow[i0] = make_float2(q.hi, q.lo);
+      // Makhoul order: q[2t] -> v[t], q[2t + 1] -> v[n - 1 - t]
+      vq[(i0 & 1) ? n - 1 - (i0 >> 1) : (i0 >> 1)] = q.hi;
+    }
+  } else if (live) {
+    // residual q - L psi1: the first differences of float neighbours are exact pairs
+    const float2 *qrow = a.qdf + (size_t)jr * ld;
+#pragma unroll 4
+    for (int i0 = t; i0 < n; i0 += T) {
+      const int c = uy_idx(i0 + 1, j, ld);
+      const float2 qv = __ldg(qrow + i0);
+      const float p0 = __ldg(a.psi1 + c);
+      const DF dxx = dfl_sub(two_sum(__ldg(a.psi1 + c + 1), -p0), two_sum(p0, -__ldg(a.psi1 + c - 1)));
+      const DF dyy = dfl_sub(two_sum(__ldg(a.psi1 + c + ld), -p0), two_sum(p0, -__ldg(a.psi1 + c - ld)));
+      const DF r = dfl_sub(DF{qv.x, qv.y}, dfl_add(dfl_mulc(dxx, a.rdx2), dfl_mulc(dyy, a.rdy2)));
+      vq[(i0 & 1) ? n - 1 - (i0 >> 1) : (i0 >> 1)] = r.hi + r.lo;
+    }
+  }
+  __syncthreads();
+  CF v[8];
+#pragma unroll
+  for (int u = 0; u < 8; u++) v[u] = buf[t + u * T];   // z[s] = v[2s] + i v[2s+1], unpadded
+  fft_row_f<-1>(buf, v, t, T, m, a.tw);
+  if (!live) return;
+  float *out = a.q + (size_t)jr * ld;
+#pragma unroll 2
+  for (int kk = t; kk <= m; kk += T) {
+    const CF zk = buf[padv<8>(kk & (m - 1))];
+    const CF zm0 = buf[padv<8>((m - kk) & (m - 1))];
+    const CF zm = CF{zm0.re, -zm0.im};
+    const CF sm = cf_add(zk, zm), df = cf_sub(zk, zm);
+    const CF e = CF{0.5f * sm.re, 0.5f * sm.im};
+    const CF o = CF{0.5f * df.im, -0.5f * df.re};   // (zk - zm) / 2i
+    const CF vv = cf_add(e, cf_mul(o, __ldg(a.wn + kk)));
+    // rot[kk] = (c, s); rot[n - kk] = -i conj(rot[kk]) = (-s, -c)
+    const float2 r = __ldg(a.rot + kk);
+    out[kk] = 2.f * fmaf(r.x, vv.re, -r.y * vv.im);
+    if (kk > 0 && kk < m) out[n - kk] = -2.f * fmaf(r.y, vv.re, r.x * vv.im);
+  }
+}
+
+// block Thomas sweep of one block and wavenumber column in single precision (the
+// blocks are diagonally dominant); the two values the reduced system needs in double
+template <int M>
+__global__ void __launch_bounds__(256) k_tdm_local_f(float *__restrict__ q, const float *__restrict__ inv,
+                                                    const float *__restrict__ up, double *__restrict__ iface_a,
+                                                    double *__restrict__ first, float l, int itot, int nblk, int ld) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int b = blockIdx.y;
+  if (k >= itot) return;
+  float v[M - 1];
+  const size_t base = (size_t)b * M * ld + k;
+#pragma unroll
+  for (int r = 0; r < M - 1; r++) v[r] = q[base + (size_t)r * ld];
+  const float rif = q[base + (size_t)(M - 1) * ld];
+  v[0] = v[0] * __ldg(inv + k);
+#pragma unroll
+  for (int r = 1; r < M - 1; r++) v[r] = fmaf(-l, v[r - 1], v[r]) * __ldg(inv + r * itot + k);
+#pragma unroll
+  for (int r = M - 3; r >= 0; r--) v[r] = fmaf(-__ldg(up + r * itot + k), v[r + 1], v[r]);
+#pragma unroll
+  for (int r = 0; r < M - 1; r++) q[base + (size_t)r * ld] = v[r];
+  // interface equation: r_iface - l y[M-2] (this block) - l y[0] (next block)
+  iface_a[(size_t)b * itot + k] = eifd::f2d(fmaf(-l, v[M - 2], rif));
+  first[(size_t)b * itot + k] = eifd::f2d(v[0]);
+}
+
+struct Dct3ArgsF {
+  const float *q;        // block solutions, rows of pitch ld floats
+  const double *iface;   // solved interface values [block][k]
+  const float *g;        // left responses of the block interior [r][k]
+  float *psi;            // output (uy layout, with halo rows and ghost columns)
+  const float2 *tw, *rot, *wn;
+  float scale;           // 1/(2 itot)
+  int itot, jtot, ld, blk, nblk;
+};
+
+// block reconstruction + single-precision DCT-III + scaling of rows (compute_potential.c:120-134)
+__global__ void __launch_bounds__(FFT_CTA) k_dct3_f(Dct3ArgsF a, FftShape sh) {
+  extern __shared__ float4 sm4[];
+  const int n = a.itot, m = n / 2, ld = a.ld;
+  const int T = sh.T;
+  const int rloc = threadIdx.x >> sh.lgT, t = threadIdx.x & (T - 1);
+  const int jr = blockIdx.x * sh.rows + rloc;
+  const bool live = jr < a.jtot;
+  const int j = 1 + jr;
+  CF *buf = reinterpret_cast<CF *>(sm4) + rloc * (m + m / 8);
+  float *xr = reinterpret_cast<float *>(buf);
+  if (live) {
+    const float *row = a.q + (size_t)jr * ld;
+    const int M = a.blk;
+    const int b = jr / M, r = jr % M;
+    const int bm = (b + a.nblk - 1) % a.nblk;
+#pragma unroll 4
+    for (int k = t; k < n; k += T) {
+      float val;
+      if (r == M - 1) {
+        val = eifd::d2f(__ldg(a.iface + (size_t)b * n + k));
+      } else {
+        // y + s_left g + s_right h (h = g reversed, the blocks are symmetric)
+        const float gl = __ldg(a.g + (size_t)r * n + k), gr = __ldg(a.g + (size_t)(M - 2 - r) * n + k);
+        const float sl = eifd::d2f(__ldg(a.iface + (size_t)bm * n + k));
+        const float sr = eifd::d2f(__ldg(a.iface + (size_t)b * n + k));
+        val = fmaf(sr, gr, fmaf(sl, gl, __ldg(row + k)));
+      }
+      xr[k] = val;
+    }
+  }
+  __syncthreads();
+  CF v[8];
+#pragma unroll
+  for (int u = 0; u < 8; u++) {
+    const int s = t + u * T;
+    const int t0 = s, t1 = s + m;
+    float2 r0 = __ldg(a.rot + t0), r1 = __ldg(a.rot + t1), wn = __ldg(a.wn + s);
+    r0.y = -r0.y;
+    r1.y = -r1.y;
+    wn.y = -wn.y;
+    const CF w0 = cf_mul(CF{xr[t0], t0 == 0 ? 0.f : -xr[n - t0]}, r0);
+    const CF w1 = cf_mul(CF{xr[t1], -xr[n - t1]}, r1);
+    const CF sum = cf_add(w0, w1);
+    const CF dif = cf_mul(cf_sub(w0, w1), wn);
+    v[u] = CF{sum.re - dif.im, sum.im + dif.re};
+  }
+  fft_row_f<1>(buf, v, t, T, m, a.tw);
+  if (!live) return;
+  float *prow = a.psi + (size_t)j * ld;
+  for (int i = t; i < n; i += T) {
+    const int tt = (i & 1) ? n - 1 - (i >> 1) : (i >> 1);
+    const CF zz = buf[padv<8>(tt >> 1)];
+    const float val = ((tt & 1) ? zz.im : zz.re) * a.scale;
+    prow[i + 1] = val;
+    if (j == 1) a.psi[(size_t)(a.jtot + 1) * ld + i + 1] = val;
+    if (j == a.jtot) a.psi[i + 1] = val;
+    if (i == 0) {
+      prow[0] = val;
+      if (j == 1) a.psi[(size_t)(a.jtot + 1) * ld] = val;
+      if (j == a.jtot) a.psi[0] = val;
+    }
+    if (i == n - 1) {
+      prow[n + 1] = val;
+      if (j == 1) a.psi[(size_t)(a.jtot + 1) * ld + n + 1] = val;
+      if (j == a.jtot) a.psi[n + 1] = val;
+    }
+  }
+}
+
+// psi as doubles: psi1 + psi2 (float pair) or the double field itself
+__global__ void k_psi_pair_to_double(const float *__restrict__ p1, const float *__restrict__ p2,
+                                     double *__restrict__ out, size_t n) {
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
+    out[t] = eifd::f2d(p1[t]) + eifd::f2d(p2[t]);
+}
+
 // launch shape of the register-radix transforms, or T = 0 when m is not supported
 // (not a power of two, or more than FFT_CTA threads per row)
 FftShape fftr_shape(int m) {
@@ -1234,6 +1570,16 @@ int poisson_init(eif_ctx *c) {
     if ((rc = df_table(pp.m, -2.L * PI / pp.m, &pp.tw_f))) return rc;
     if ((rc = df_table(n, -PI / (2.L * n), &pp.rot_f))) return rc;
     if ((rc = df_table(n, -2.L * PI / n, &pp.wn_f))) return rc;
+    // single-precision twiddles of the refined solve, rounded from long double
+    auto f_table = [&](int len, long double step, float2 **dst) -> int {
+      std::vector<float2> v(len);
+      for (int k = 0; k < len; k++) v[k] = make_float2((float)cosl(step * k), (float)sinl(step * k));
+      EIF_CK(c, up_load((void **)dst, v.data(), sizeof(float2) * len));
+      return EIF_OK;
+    };
+    if ((rc = f_table(pp.m, -2.L * PI / pp.m, &pp.tw2))) return rc;
+    if ((rc = f_table(n, -PI / (2.L * n), &pp.rot2))) return rc;
+    if ((rc = f_table(n, -2.L * PI / n, &pp.wn2))) return rc;
   }
   EIF_CK(c, up_load((void **)&pp.rot, rot.data(), sizeof(double2) * n));
   EIF_CK(c, up_load((void **)&pp.wn, wn.data(), sizeof(double2) * n));
@@ -1336,6 +1682,10 @@ int poisson_init(eif_ctx *c) {
       const std::vector<float2> invdf = pairs(inv), updf = pairs(up);
       EIF_CK(c, up_load((void **)&pp.tdm_inv_df, invdf.data(), sizeof(float2) * invdf.size()));
       EIF_CK(c, up_load((void **)&pp.tdm_up_df, updf.data(), sizeof(float2) * updf.size()));
+      const std::vector<float> invf(inv.begin(), inv.end()), upf(up.begin(), up.end()), gf(g.begin(), g.end());
+      EIF_CK(c, up_load((void **)&pp.tdm_inv_f, invf.data(), sizeof(float) * invf.size()));
+      EIF_CK(c, up_load((void **)&pp.tdm_up_f, upf.data(), sizeof(float) * upf.size()));
+      EIF_CK(c, up_load((void **)&pp.tdm_g_f, gf.data(), sizeof(float) * gf.size()));
     }
     EIF_CK(c, up_load((void **)&pp.red_inv, rinv.data(), sizeof(double) * rinv.size()));
     EIF_CK(c, up_load((void **)&pp.red_up, rup.data(), sizeof(double) * rup.size()));
@@ -1374,6 +1724,9 @@ int poisson_init(eif_ctx *c) {
       EIF_CK(c, cudaFuncSetAttribute(k_dct2_dfr<FFT_V>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smr));
       EIF_CK(c, cudaFuncSetAttribute(k_dct3_dfr<FFT_V>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smr));
     }
+    // the refined single-precision solve: power-of-two half lengths with the block solver
+    c->psi_pair = c->cfg.precision == EIF_PREC_MIXED && sh.T > 0 && pp.blk > 0;
+    if (c->psi_pair) EIF_CK(c, cudaMalloc((void **)&pp.qdf, sizeof(float2) * (size_t)c->ld * jt));
   }
   return EIF_OK;
 }
@@ -1382,12 +1735,114 @@ void poisson_free(eif_ctx *c) {
   PoissonPlan &pp = c->pp;
   void *ptrs[] = {pp.r2_inv, pp.r2_up, pp.r2_phi, pp.r2_qinv, pp.r2_qup, pp.r2_q1, pp.r2_coef,
                   pp.tw, pp.rot, pp.wn, pp.tw_f, pp.rot_f, pp.wn_f, pp.lam, pp.tdm_inv, pp.tdm_up, pp.tdm_g, pp.tdm_g_df, pp.tdm_inv_df, pp.tdm_up_df,
-                  pp.red_inv, pp.red_up, pp.red_q1, pp.red_coef, pp.ywork};
+                  pp.red_inv, pp.red_up, pp.red_q1, pp.red_coef, pp.ywork, pp.tw2, pp.rot2, pp.wn2, pp.tdm_inv_f,
+                  pp.tdm_up_f, pp.tdm_g_f, pp.qdf};
   for (void *p : ptrs) if (p) cudaFree(p);
   pp = PoissonPlan{};
 }
 
 static int fft_threads(int m) { return m >= 512 ? 256 : (m >= 128 ? 128 : 64); }
+
+// the reduced cyclic systems of the interface values (double precision), in place in iface
+static int reduced_solve(eif_ctx *c, double *iface, double *first) {
+  PoissonPlan &pp = c->pp;
+  const int n = c->itot;
+  const double l = 1. / c->dy / c->dy;
+  if (pp.g2 > 0) {
+    const int Q = pp.q2;
+    const size_t sm = red2_smem_bytes(Q);
+    const dim3 grid((n + RED2_K - 1) / RED2_K);
+    if (pp.g2 == 16) {
+      k_tdm_reduced2<16><<<grid, RED2_K * Q, sm, c->stream>>>(iface, first, pp.red_coef, pp.r2_inv, pp.r2_up, pp.r2_phi,
+                                                          pp.r2_qinv, pp.r2_qup, pp.r2_q1, pp.r2_coef, l, n, pp.nblk, Q);
+    } else if (pp.g2 == 8) {
+      k_tdm_reduced2<8><<<grid, RED2_K * Q, sm, c->stream>>>(iface, first, pp.red_coef, pp.r2_inv, pp.r2_up, pp.r2_phi,
+                                                         pp.r2_qinv, pp.r2_qup, pp.r2_q1, pp.r2_coef, l, n, pp.nblk, Q);
+    } else {
+      k_tdm_reduced2<4><<<grid, RED2_K * Q, sm, c->stream>>>(iface, first, pp.red_coef, pp.r2_inv, pp.r2_up, pp.r2_phi,
+                                                         pp.r2_qinv, pp.r2_qup, pp.r2_q1, pp.r2_coef, l, n, pp.nblk, Q);
+    }
+  } else {
+    const int rcols = red_cols(pp.nblk);
+    k_tdm_reduced<<<(n + rcols - 1) / rcols, RED_THREADS, red_smem_bytes(pp.nblk, rcols), c->stream>>>(
+        iface, first, pp.red_inv, pp.red_up, pp.red_q1, pp.red_coef, l, n, pp.nblk, rcols);
+  }
+  EIF_LAUNCH_CK(c);
+  return EIF_OK;
+}
+
+// the mixed form's Poisson solve: two single-precision passes, the second on the
+// double-float residual of the first (see k_dct2_f); psi1, psi2 into the psi buffer
+static int potential_refined(eif_ctx *c, int rk, bool with_ibm) {
+  PoissonPlan &pp = c->pp;
+  const int n = c->itot, jt = c->jtot;
+  const FftShape sh = fftr_shape(pp.m);
+  const size_t smem = sizeof(CF) * (size_t)sh.rows * (pp.m + pp.m / 8);
+  auto dfpair = [](double v) {
+    const float hi = (float)v;
+    return DF{hi, (float)(v - (double)hi)};
+  };
+  float *qf = reinterpret_cast<float *>(c->qhat);
+  float *psi1 = reinterpret_cast<float *>(c->psi), *psi2 = psi1 + c->nfield;
+  double *iface = pp.ywork;
+  double *first = pp.ywork + (size_t)pp.nblk * n;
+  const float lf = (float)(1. / c->dy / c->dy);
+  const int tt = c->tiles.tdm;
+  const dim3 gt((n + tt - 1) / tt, pp.nblk);
+  const unsigned blocks = (unsigned)((jt + sh.rows - 1) / sh.rows);
+  for (int pass = 0; pass < 2; pass++) {
+    Dct2ArgsF a;
+    a.ux = c->ux[c->cur]; a.uy = c->uy[c->cur];
+    a.dux = reinterpret_cast<const float *>(c->dux); a.duy = reinterpret_cast<const float *>(c->duy);
+    a.coef = c->d_coef;
+    a.psi1 = pass ? psi1 : nullptr;
+    a.qdf = pp.qdf;
+    a.q = qf;
+    a.tw = pp.tw2; a.rot = pp.rot2; a.wn = pp.wn2;
+    a.rdx = dfpair(1. / c->dx); a.rdy = dfpair(1. / c->dy);
+    a.rdx2 = dfpair(1. / (c->dx * c->dx)); a.rdy2 = dfpair(1. / (c->dy * c->dy));
+    a.itot = n; a.jtot = jt; a.ld = c->ld; a.with_ibm = with_ibm ? 1 : 0; a.rk = rk;
+    {
+      EIF_PROF(c, "poisson_dct2", 1);
+      k_dct2_f<<<blocks, sh.T * sh.rows, smem, c->stream>>>(a, sh);
+      EIF_LAUNCH_CK(c);
+    }
+    {
+      EIF_PROF(c, "poisson_tdm", 2);
+      if (pp.blk == 16) {
+        k_tdm_local_f<16><<<gt, tt, 0, c->stream>>>(qf, pp.tdm_inv_f, pp.tdm_up_f, iface, first, lf, n, pp.nblk, c->ld);
+      } else if (pp.blk == 8) {
+        k_tdm_local_f<8><<<gt, tt, 0, c->stream>>>(qf, pp.tdm_inv_f, pp.tdm_up_f, iface, first, lf, n, pp.nblk, c->ld);
+      } else {
+        k_tdm_local_f<4><<<gt, tt, 0, c->stream>>>(qf, pp.tdm_inv_f, pp.tdm_up_f, iface, first, lf, n, pp.nblk, c->ld);
+      }
+      EIF_LAUNCH_CK(c);
+      int rc = reduced_solve(c, iface, first);
+      if (rc) return rc;
+    }
+    Dct3ArgsF b;
+    b.q = qf; b.iface = iface; b.g = pp.tdm_g_f;
+    b.psi = pass ? psi2 : psi1;
+    b.tw = pp.tw2; b.rot = pp.rot2; b.wn = pp.wn2;
+    b.scale = (float)(1. / (2. * n));
+    b.itot = n; b.jtot = jt; b.ld = c->ld; b.blk = pp.blk; b.nblk = pp.nblk;
+    EIF_PROF(c, "poisson_dct3", 1);
+    k_dct3_f<<<blocks, sh.T * sh.rows, smem, c->stream>>>(b, sh);
+    EIF_LAUNCH_CK(c);
+  }
+  return EIF_OK;
+}
+
+int launch_psi_to_double(eif_ctx *c, double *dst) {
+  if (!c->psi_pair) {
+    EIF_CK(c, cudaMemcpyAsync(dst, c->psi, sizeof(double) * c->nfield, cudaMemcpyDeviceToDevice, c->stream));
+    return EIF_OK;
+  }
+  const float *p1 = reinterpret_cast<const float *>(c->psi);
+  k_psi_pair_to_double<<<c->sms * 4, 256, 0, c->stream>>>(p1, p1 + c->nfield, dst, c->nfield);
+  EIF_LAUNCH_CK(c);
+  return EIF_OK;
+}
 
 int launch_potential(eif_ctx *c, int rk, bool with_ibm) {
   PoissonPlan &pp = c->pp;
@@ -1403,6 +1858,7 @@ int launch_potential(eif_ctx *c, int rk, bool with_ibm) {
     const float hi = (float)v;
     return DF{hi, (float)(v - (double)hi)};
   };
+  if (c->psi_pair) return potential_refined(c, rk, with_ibm);
   if (mixed) {
     Dct2ArgsDF a;
     a.ux = c->ux[c->cur]; a.uy = c->uy[c->cur];
@@ -1465,7 +1921,7 @@ int launch_potential(eif_ctx *c, int rk, bool with_ibm) {
     EIF_LAUNCH_CK(c);
     if (pp.g2 > 0) {
       const int Q = pp.q2;
-      const size_t sm = sizeof(double) * 3 * RED2_K * (size_t)Q;
+      const size_t sm = red2_smem_bytes(Q);
       const dim3 grid((n + RED2_K - 1) / RED2_K);
       if (pp.g2 == 16) {
         k_tdm_reduced2<16><<<grid, RED2_K * Q, sm, c->stream>>>(iface, first, pp.red_coef, pp.r2_inv, pp.r2_up, pp.r2_phi,

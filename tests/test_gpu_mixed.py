@@ -2,10 +2,12 @@
 
 The double-precision form is pinned to the reference (test_gpu_parity.py).
 The mixed form computes the indicator, the immersed-boundary forcing and the
-predictor stencils in single precision while keeping storage, the Poisson
-solve, the projection and the particle dynamics in double precision. Its
-error bars are those of the target: velocity within 1e-4 relative to the
-double-precision run, maximum divergence below 1e-5.
+predictor stencils in single precision while keeping storage, the projection
+and the particle dynamics in double precision; its Poisson solve is two
+single-precision passes (the second on the residual of the first, formed in
+double-float arithmetic) with the reduced tridiagonal systems in double
+precision. Its error bars are those of the target: velocity within 1e-4
+relative to the double-precision run, maximum divergence below 1e-5.
 """
 import numpy as np
 import pytest
@@ -121,11 +123,12 @@ def test_mixed_predictor_matches_fp64(builder, gpu_lib):
 ], ids=["couette_circle", "poiseuille_384x768", "poiseuille_256x512", "poiseuille_32x64", "poiseuille_1024x2048",
         "poiseuille_2048x4096"])
 def test_mixed_poisson_matches_fp64(builder, gpu_lib):
-    """The double-float transforms of the mixed form solve the same Poisson problem
-    as the double-precision form to ~1e-12 relative. The half lengths m = itot/2
-    cover the register-radix (radix-8) transform with a last pass of radix 2
-    (m = 16, 128, 1024) and 4 (m = 32), and the radix-4/2/3 transform of the other
-    lengths (m = 192); m = 512 (no last pass) runs in the step test."""
+    """The mixed form's Poisson solve agrees with the double-precision form's to 1e-10
+    relative in psi and in the projected velocity. The half lengths m = itot/2 cover
+    the refined single-precision solve (register-radix, radix-8, transforms) with a
+    last pass of radix 2 (m = 16, 128, 1024) and 4 (m = 32), and the double-float
+    radix-4/2/3 transform of the other lengths (m = 192); m = 512 (no last pass) runs
+    in the step test."""
     from conftest import interior_p
     case = builder()
     d, m = pair(case)
