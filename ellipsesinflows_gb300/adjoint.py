@@ -95,6 +95,35 @@ class Steps(torch.autograd.Function):
                 torch.from_numpy(wb), None, None, None, None)
 
 
+def grid_cells(itot, jtot, ly):
+    """DXF(1..itot) and DXC(1..itot+1) of the uniform grid with walls at x = 0 and 1 (as
+    set_coordinate forms them, src/param/init.c:105-167) and dy, as float64 tensors."""
+    dx = 1.0 / itot
+    xf = [1.0 * (i - 1) * dx for i in range(1, itot + 2)]
+    xf[0], xf[itot] = 0.0, 1.0
+    xc = [xf[0]] + [0.5 * (xf[i - 1] + xf[i]) for i in range(1, itot + 1)] + [xf[itot]]
+    dxf = torch.tensor([xf[i] - xf[i - 1] for i in range(1, itot + 1)], dtype=torch.float64)
+    dxc = torch.tensor([xc[i] - xc[i - 1] for i in range(1, itot + 2)], dtype=torch.float64)
+    return dxf, dxc, ly / jtot
+
+
+def kinetic_energy(ux, uy, ly):
+    """Kinetic energy of the fluid as the reference logs it (check_energy,
+    src/logging.c:130-172): the sum over the rows j = 1..jtot of UX(i,j)^2/2 DXC(i) dy
+    (faces i = 1..itot+1) plus UY(i,j)^2/2 DXF(i) dy (cells i = 1..itot), for fields in
+    the eif_push_fluid layouts (torch tensors, differentiable)."""
+    jtot, itot = uy.shape[0] - 2, uy.shape[1] - 2
+    dxf, dxc, dy = grid_cells(itot, jtot, ly)
+    ex = 0.5 * (ux[1:-1, :] ** 2 * dxc[None, :]).sum() * dy
+    ey = 0.5 * (uy[1:-1, 1:-1] ** 2 * dxf[None, :]).sum() * dy
+    return ex + ey
+
+
+def mean_x_plus_energy(ux, uy, rec, ly):
+    """The mean ellipse x-centre plus the fluid's kinetic energy (kinetic_energy)."""
+    return rec[:, F["x"]].mean() + kinetic_energy(ux, uy, ly)
+
+
 def steps(sim, ux0, uy0, p0, rec0, nsteps, every=16, mode=ADJOINT_COUPLED, wall=None):
     """Functional form of ``Steps.apply``; ``wall`` defaults to the solver's wall velocities."""
     if wall is None:

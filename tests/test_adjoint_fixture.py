@@ -46,3 +46,35 @@ def test_port_reproduces_reference_central_differences():
             assert np.array_equal(sb, ref["substeps_" + name][0 if sgn > 0 else 1])
             vals.append(G.loss(o, w))
         assert (vals[0] - vals[1]) / (2 * eps) == float(ref["fd_" + name])
+
+
+def test_port_reproduces_reference_c4_objective_differences():
+    """The 256 x 512 Couette fixture (400 steps, objective mean x-centre + kinetic
+    energy): the restatement gives the reference's objective, sub-iteration counts and
+    central difference along the angle direction bit for bit."""
+    import os as _os
+    spec = importlib.util.spec_from_file_location("make_c4", os.path.join(HERE, "golden", "make_adjoint_c4_fd.py"))
+    G = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(G)
+    ref = np.load(os.path.join(HERE, "golden", "adjoint_fd_c4_256x512.npz"))
+    case, state, rec, dirs = G.inputs()
+    dt = float(ref["dt"])
+
+    def run(r):
+        s = port.PortSolver(case.config(), threads=_os.cpu_count() or 1)
+        s.push_fluid(*state)
+        s.push_particles(r)
+        s.dt = dt
+        subs = [s.integrate() for _ in range(G.NSTEPS)]
+        ux, uy, _, _ = s.pull_fluid()
+        out = G.objective(ux, uy, s.pull_particles(), case.ly)
+        s.close()
+        return out, np.array(subs, dtype=np.int32)
+
+    base, subs = run(rec)
+    assert np.array_equal(subs, ref["substeps"])
+    assert base == float(ref["loss"])
+    eps = float(ref["eps"])
+    (vp, sp), (vm, sm) = run(rec + eps * dirs["angles"]), run(rec - eps * dirs["angles"])
+    assert np.array_equal(sp, ref["substeps_angles"][0]) and np.array_equal(sm, ref["substeps_angles"][1])
+    assert (vp - vm) / (2 * eps) == float(ref["fd_angles"])

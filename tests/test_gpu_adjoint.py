@@ -357,3 +357,84 @@ def test_adjoint_matches_reference_central_differences():
         print("adjoint vs reference central difference [%s]: %.15e %.15e rel %.2e" % (name, adj, fd, abs(adj - fd) / abs(fd)))
         assert abs(adj - fd) <= TOL_FD * abs(fd), (name, adj, fd)
     sim.close()
+
+
+def c4_objective_run(cfg, state, rec, nsteps, dt, wall=None):
+    """objective (mean x-centre + kinetic energy) after nsteps forward steps, and the
+    sub-iteration counts"""
+    from ellipsesinflows_gb300.adjoint import mean_x_plus_energy
+    sim = new_sim(cfg, wall)
+    out, subs = run(sim, state, rec, nsteps, dt, ADJOINT_COUPLED)
+    sim.close()
+    val = mean_x_plus_energy(torch.from_numpy(out[0]), torch.from_numpy(out[1]), torch.from_numpy(out[3]),
+                             cfg.ly)
+    return float(val), subs
+
+
+def test_adjoint_c4_objective_matches_central_differences():
+    """256x512 Couette flow (walls at -0.5 and 0.5, Re 100), 8 ellipses a = 0.06, b = 0.03
+    at least 4a apart, 400 steps with a checkpoint every 50: the gradient of the mean
+    ellipse x-centre plus the fluid's kinetic energy (src/logging.c:130-172) with
+    respect to the initial angles, the initial centres and the wall speed s (walls at
+    -s and s), against central differences of the GPU step (step 1e-7 for angles and
+    centres, 1e-5 for the wall speed) and of the reference's own CPU step (fixture
+    written by tests/golden/make_adjoint_c4_fd.py: the same 400 steps)."""
+    import importlib.util
+    import os
+    from ellipsesinflows_gb300.adjoint import mean_x_plus_energy
+    here = os.path.dirname(os.path.abspath(__file__))
+    spec = importlib.util.spec_from_file_location("make_c4", os.path.join(here, "golden", "make_adjoint_c4_fd.py"))
+    G = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(G)
+    ref = np.load(os.path.join(here, "golden", "adjoint_fd_c4_256x512.npz"))
+    case, state, rec, dirs = G.inputs()
+    cfg = case.config()
+    nsteps, dt = int(ref["nsteps"]), float(ref["dt"])
+    sim = Simulation(cfg)
+    sim.push_fluid(*state)
+    sim.push_particles(rec)
+    assert 0.5 * sim.decide_dt() == dt       # the reference's dt, bit for bit
+    base, subs = c4_objective_run(cfg, state, rec, nsteps, dt)
+    assert np.array_equal(np.array(subs), ref["substeps"])
+    assert base == pytest.approx(float(ref["loss"]), rel=1e-10)
+    # gradients through the adjoint (checkpoints every 50 steps)
+    sim.push_fluid(*state)
+    sim.push_particles(rec)
+    sim.dt = dt
+    t = [torch.tensor(a, requires_grad=True) for a in state + (rec,)]
+    wall = torch.tensor([cfg.uy_wall[0], cfg.uy_wall[1]], dtype=torch.float64, requires_grad=True)
+    ux, uy, p, r = Steps.apply(t[0], t[1], t[2], t[3], wall, sim, nsteps, 50, ADJOINT_COUPLED)
+    J = mean_x_plus_energy(ux, uy, r, cfg.ly)
+    assert float(J) == pytest.approx(base, rel=1e-13)
+    J.backward()
+    grec, gwall = t[3].grad.numpy(), wall.grad.numpy()
+    sim.close()
+    for name in ("angles", "centres"):
+        d = dirs[name]
+        adj = float(np.sum(grec * d))
+        # against the reference's central difference
+        fd_ref = float(ref["fd_" + name])
+        assert np.array_equal(ref["substeps_" + name][0], ref["substeps"])
+        assert np.array_equal(ref["substeps_" + name][1], ref["substeps"])
+        print("C4 objective, adjoint vs reference central difference [%s]: %.15e %.15e rel %.2e"
+              % (name, adj, fd_ref, abs(adj - fd_ref) / abs(fd_ref)))
+        assert abs(adj - fd_ref) <= TOL_FD * abs(fd_ref), (name, adj, fd_ref)
+        # against the GPU step's own central difference
+        eps = float(ref["eps"])
+        vp, sp = c4_objective_run(cfg, state, rec + eps * d, nsteps, dt)
+        vm, sm = c4_objective_run(cfg, state, rec - eps * d, nsteps, dt)
+        assert sp == subs and sm == subs
+        fd = (vp - vm) / (2 * eps)
+        print("C4 objective, adjoint vs GPU central difference [%s]: %.15e %.15e rel %.2e"
+              % (name, adj, fd, abs(adj - fd) / abs(fd)))
+        assert abs(adj - fd) <= TOL_FD * abs(fd), (name, adj, fd)
+    # wall speed s: walls at (-s, s), d/ds = -dJ/d uy_wall[0] + dJ/d uy_wall[1]
+    adj = float(-gwall[0] + gwall[1])
+    s0, eps = cfg.uy_wall[1], 1e-5
+    vp, sp = c4_objective_run(cfg, state, rec, nsteps, dt, wall=(-(s0 + eps), s0 + eps))
+    vm, sm = c4_objective_run(cfg, state, rec, nsteps, dt, wall=(-(s0 - eps), s0 - eps))
+    assert sp == subs and sm == subs
+    fd = (vp - vm) / (2 * eps)
+    print("C4 objective, adjoint vs GPU central difference [wall speed]: %.15e %.15e rel %.2e"
+          % (adj, fd, abs(adj - fd) / abs(fd)))
+    assert abs(adj - fd) <= TOL_FD * abs(fd)
