@@ -116,6 +116,68 @@ def place(n, radius, ly, clearance, rng, xmargin, max_tries=2_000_000):
     return xs, ys
 
 
+def _boundary(a, b, az, x, y, k=72):
+    """k points on the ellipse (a, b) turned by az about (x, y)"""
+    t = np.linspace(0.0, 2 * math.pi, k, endpoint=False)
+    c, s = math.cos(az), math.sin(az)
+    bx, by = a * np.cos(t), b * np.sin(t)
+    return x + c * bx - s * by, y + s * bx + c * by
+
+
+def _inside(px, py, a, b, az, x, y):
+    """mask of the points (px, py) inside the ellipse (a, b) turned by az about (x, y)"""
+    c, s = math.cos(-az), math.sin(-az)
+    dx, dy = px - x, py - y
+    u, v = c * dx - s * dy, s * dx + c * dy
+    return (u / a) ** 2 + (v / b) ** 2 < 1.0
+
+
+def place_ellipses(a, b, az, ly, clearance, rng, xmargin, max_tries=20_000_000):
+    """Random sequential addition of ellipses (semi-axes a, b, angles az; arrays) with
+    no ellipse closer than `clearance` to another (periodic in y, nearest image): a
+    candidate is kept when, for every earlier ellipse whose bounding circle comes
+    within reach, neither ellipse, grown by the clearance, contains any of 72 boundary
+    points of the other. Bounding circles may overlap, so elongated ellipses pack
+    beyond the bounding-circle rule (centres kept max(a, b) + xmargin from the walls)."""
+    n = len(a)
+    r = np.maximum(a, b)
+    cell = 2 * r.max() + clearance
+    ncy = max(1, int(ly // cell))
+    grid = {}
+    xs, ys = np.empty(n), np.empty(n)
+    placed, tries = 0, 0
+    while placed < n:
+        tries += 1
+        if tries > max_tries:
+            raise RuntimeError("could not place %d ellipses (placed %d)" % (n, placed))
+        k = placed
+        x = rng.uniform(r[k] + xmargin, 1.0 - r[k] - xmargin)
+        y = rng.uniform(0.0, ly)
+        cy = min(int(y / (ly / ncy)), ncy - 1)
+        ok = True
+        for dyc in (-1, 0, 1):
+            for m in grid.get((cy + dyc) % ncy, ()):
+                ddy = y - ys[m]
+                ddy -= ly * round(ddy / ly)
+                ym = y - ddy     # the earlier ellipse's nearest image, seen from the candidate
+                if math.hypot(xs[m] - x, ym - y) >= r[k] + r[m] + clearance:
+                    continue
+                c = clearance
+                px, py = _boundary(a[k], b[k], az[k], x, y)
+                qx, qy = _boundary(a[m], b[m], az[m], xs[m], ym)
+                if (_inside(px, py, a[m] + c, b[m] + c, az[m], xs[m], ym).any() or
+                        _inside(qx, qy, a[k] + c, b[k] + c, az[k], x, y).any()):
+                    ok = False
+                    break
+            if not ok:
+                break
+        if ok:
+            xs[k], ys[k] = x, y
+            grid.setdefault(cy, []).append(k)
+            placed += 1
+    return xs, ys
+
+
 def couette_circle(itot=64, jtot=128, steps=200):
     """Single neutrally buoyant circle in Couette flow (lateral migration, case1)."""
     rec = particle_records([1.0], [0.125], [0.125], [0.3], [1.0], [0.0])
@@ -199,12 +261,13 @@ def contact_cluster(itot=64, jtot=128, seed=7):
                 steps=20)
 
 
-def batch_c5(count=64, seed=3, n_max=128, steps=300):
+def batch_c5(count=64, seed=3, n_max=256, steps=300):
     """Many independent suspensions of uneven sizes: grids drawn from 128x256, 256x512,
-    384x768 and 512x1024; ellipse counts proportional to the cell count (4 .. n_max,
-    n_max = 128 keeps the bounding discs of a = 0.04 below 35 % of the area, where
-    random sequential placement still succeeds); a = 0.04, aspect ratio U[1, 2.5],
-    Re U[100, 400], Poiseuille forcing 8/Re, fluid at rest."""
+    384x768 and 512x1024; ellipse counts proportional to the cell count (4 .. n_max =
+    256); a = 0.04, aspect ratio U[1, 2.5], Re U[100, 400], Poiseuille forcing 8/Re,
+    fluid at rest. 256 bounding discs of a = 0.04 would cover 64 % of the 1 x 2 domain,
+    beyond what random sequential addition of discs reaches (about 55 %), so the
+    ellipses themselves are kept apart (place_ellipses, clearance one cell)."""
     rng = np.random.default_rng(seed)
     grids = [(128, 256), (256, 512), (384, 768), (512, 1024)]
     max_cells = 512 * 1024
@@ -216,8 +279,8 @@ def batch_c5(count=64, seed=3, n_max=128, steps=300):
         ar = rng.uniform(1.0, 2.5, n)
         Re = float(rng.uniform(100.0, 400.0))
         dx = 1.0 / itot
-        xs, ys = place(n, a, 2.0, dx, rng, dx)
         az = rng.uniform(0.0, math.pi, n)
+        xs, ys = place_ellipses(np.full(n, a), a / ar, az, 2.0, dx, rng, dx)
         rec = particle_records(np.ones(n), np.full(n, a), a / ar, xs, ys, az)
         out.append(Case("batch%02d_%dx%d_n%d" % (k, itot, jtot, n), itot, jtot, 2.0, Re, extfrcy=8.0 / Re,
                         particles=rec, steps=steps))

@@ -47,3 +47,37 @@ def test_couette_initial_profile():
     xc = c.xc()
     assert np.allclose(uy[5, 1:-1], -0.5 + xc[1:-1])
     assert np.all(ux == 0) and np.all(p == 0)
+
+
+def test_place_ellipses_keeps_ellipses_apart():
+    """256 ellipses a = 0.04, aspect ratio U[1, 2.5] in the 1 x 2 channel (the largest
+    suspension of the batch workload): no ellipse, grown by the clearance less a
+    margin, contains a point of another's boundary sampled 4x finer than the
+    placement's test; the bounding circles do overlap (a denser packing than the
+    bounding-circle rule allows)."""
+    import math
+    import numpy as np
+    from ellipsesinflows_gb300 import cases
+    rng = np.random.default_rng(8)
+    n, a, ly, clr = 256, 0.04, 2.0, 1.0 / 512
+    ar = rng.uniform(1.0, 2.5, n)
+    az = rng.uniform(0.0, math.pi, n)
+    A, B = np.full(n, a), a / ar
+    xs, ys = cases.place_ellipses(A, B, az, ly, clr, rng, clr)
+    overlapping_discs = 0
+    for k in range(n):
+        for m in range(k):
+            dy = ys[k] - ys[m]
+            dy -= ly * round(dy / ly)
+            if math.hypot(xs[k] - xs[m], dy) < 2 * a:
+                overlapping_discs += 1
+            else:
+                continue
+            ym = ys[k] - dy
+            px, py = cases._boundary(A[k], B[k], az[k], xs[k], ys[k], k=288)
+            qx, qy = cases._boundary(A[m], B[m], az[m], xs[m], ym, k=288)
+            c = 0.5 * clr
+            assert not cases._inside(px, py, A[m] + c, B[m] + c, az[m], xs[m], ym).any()
+            assert not cases._inside(qx, qy, A[k] + c, B[k] + c, az[k], xs[k], ys[k]).any()
+    assert overlapping_discs > 0
+    assert np.all((xs > a) & (xs < 1 - a)) and np.all((ys >= 0) & (ys < ly))
