@@ -422,10 +422,11 @@ class Solver:
 
     def tiles(self):
         """tile shapes chosen by the tuner: {"predictor_rows", "projection_rows",
-        "thomas_threads", "tuned"}"""
+        "thomas_threads", "tuned", "predictor_tensor_copies"}"""
         t = (ctypes.c_int * 4)()
         self._call("tiles", self.ctx, t)
-        return {"predictor_rows": t[0], "projection_rows": t[1], "thomas_threads": t[2], "tuned": bool(t[3])}
+        return {"predictor_rows": t[0], "projection_rows": t[1], "thomas_threads": t[2], "tuned": bool(t[3] & 1),
+                "predictor_tensor_copies": bool(t[3] & 2)}
 
     # ---- discrete adjoint (double-precision form) ----
     def adjoint_begin(self, max_steps, mode=ADJOINT_COUPLED):

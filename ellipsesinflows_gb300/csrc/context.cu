@@ -334,6 +334,7 @@ int check_flags(eif_ctx *c) {
   }
   if (f & EIF_FLAG_NOCONV)
     return fail(c, EIF_ERR_NOCONV, "an iteration cap or a device list capacity was reached on the device");
+  if (f & EIF_FLAG_TIMEOUT) return fail(c, EIF_ERR_CUDA, "a bounded wait for an asynchronous tile copy gave up");
   return EIF_OK;
 }
 }  // namespace eif
@@ -450,6 +451,7 @@ int eif_create(const eif_config_t *cfg, eif_ctx **out) {
 #undef CK_CREATE
   rc = poisson_init(c);
   if (rc) return rc;
+  if ((rc = predictor_prepare(c))) return rc;
   rc = ensure_pcap(c, 1);
   if (rc) return rc;
   rc = launch_boundaries(c);

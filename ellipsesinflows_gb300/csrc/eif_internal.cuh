@@ -28,6 +28,7 @@
 // error flags raised by kernels (bit mask in ctx->d_flags)
 #define EIF_FLAG_NOCONV 1u
 #define EIF_FLAG_NONFINITE 2u
+#define EIF_FLAG_TIMEOUT 4u   // a bounded wait for an asynchronous copy gave up
 
 // cap of the equivalent-circle fixed point (the reference has none,
 // src/suspensions/collision.c:117-133,141-152)
@@ -158,6 +159,7 @@ struct eif_ctx {
   // tile heights (rows per block of 32 columns), threads per block of the block Thomas
   struct Tiles {
     int pred = 8, corr = 8, tdm = 128;
+    bool pred_copy = true;   // mixed predictor: tiles staged by tensor copies where available
     bool tuned = false;
   } tiles;
   unsigned buf_gen = 0;         // bumped when device buffers are reallocated (batch graphs hold them)
@@ -172,6 +174,9 @@ struct eif_ctx {
   // the first nfield floats of the psi buffer and psi2 in the next nfield, both with the
   // uy layout (pitch ld, halo rows and ghost columns)
   bool psi_pair = false;
+  // the mixed predictor stages its tiles with bulk tensor copies (fluid.cu): resident
+  // blocks per SM of the three tile heights (0: not available, the plain kernel runs)
+  int pred_tma_ctas[3] = {0, 0, 0};
   bool boxes_x_valid = false;   // the IBM boxes hold the positions X (see launch_boxes)
   bool weights_x_valid = false; // wcache holds the indicator weights of those boxes
   void *wcache = nullptr;       // indicator weight per IBM task slot (wcap entries)
@@ -264,6 +269,8 @@ int launch_divergence(eif_ctx *c, double *divmax, double *divsum);
 int launch_f2d_copy(eif_ctx *c, const float *in, double *out, size_t n);
 int launch_d2f_copy(eif_ctx *c, const double *in, float *out, size_t n);
 int launch_coef(eif_ctx *c);
+// the tensor-copy predictor's launch shapes (a host query, before any graph capture)
+int predictor_prepare(eif_ctx *c);
 
 // ---- Poisson (poisson.cu) ----
 int poisson_init(eif_ctx *c);

@@ -12,7 +12,12 @@
 //   check_divergence                    src/logging.c:40-80
 #include "eif_internal.cuh"
 #include "eif_df.cuh"
+#include <algorithm>
 #include <cfloat>
+#include <cstdint>
+#include <cstdlib>
+#include <cuda.h>
+#include <cudaTypedefs.h>
 
 namespace {
 
@@ -166,6 +171,67 @@ struct PredArgsF {
 __device__ __forceinline__ float dif(float2 a, float2 b) { return (a.x - b.x) + (a.y - b.y); }
 __device__ __forceinline__ float val(float2 a) { return a.x + a.y; }
 
+// the update of cell (i, j) of the mixed predictor from the staged float-pair tiles (the
+// cell at tile position (x, y)); u_own, v_own are the cell's old velocities in double,
+// Bx, By its old explicit terms
+template <int PY, int PX>
+__device__ __forceinline__ void pred_mixed_cell(const PredArgsF &a, const float2 (&tux)[PY][PX],
+                                                const float2 (&tuy)[PY][PX], const float2 (&tp)[PY][PX], int i, int j,
+                                                int x, int y, double u_own, double v_own, float Bx, float By) {
+  const int ld = a.ld, jtot = a.jtot;
+  const float adt = __ldg(a.coef), bdt = __ldg(a.coef + 1), gdt = __ldg(a.coef + 2);
+  const float rdy = a.rdy;
+  if (i >= 2) {
+    const float2 u0 = tux[y][x], uw = tux[y][x - 1], ue = tux[y][x + 1], us = tux[y - 1][x], un = tux[y + 1][x];
+    const float cxm = __ldg(a.cxm + i), cxp = __ldg(a.cxp + i);
+    const float duxdx_xm = dif(u0, uw) * __ldg(a.rdxf + i - 1);
+    const float duxdx_xp = dif(ue, u0) * __ldg(a.rdxf + i);
+    const float duxdy_ym = dif(u0, us) * rdy;
+    const float duxdy_yp = dif(un, u0) * rdy;
+    const float ux_xm = 0.5f * (val(uw) + val(u0));
+    const float ux_xp = 0.5f * (val(u0) + val(ue));
+    const float adv1 = -cxm * ux_xm * duxdx_xm - cxp * ux_xp * duxdx_xp;
+    const float uy_ym = cxm * val(tuy[y][x - 1]) + cxp * val(tuy[y][x]);
+    const float uy_yp = cxm * val(tuy[y + 1][x - 1]) + cxp * val(tuy[y + 1][x]);
+    const float adv2 = -0.5f * uy_ym * duxdy_ym - 0.5f * uy_yp * duxdy_yp;
+    const float rdxc = __ldg(a.rdxc + i);
+    const float dif_ = a.rRe * ((dif(ue, u0) * __ldg(a.rdxf + i) - dif(u0, uw) * __ldg(a.rdxf + i - 1)) * rdxc +
+                                (dif(un, u0) - dif(u0, us)) * rdy * rdy);
+    const float pre = -dif(tp[y][x], tp[y][x - 1]) * rdxc;
+    const float A = (adv1 + adv2) + dif_;
+    const int c = j * ld + (i - 1);
+    a.sxa[c] = A;
+    const double un_ = u_own + eifd::f2d(adt * A + bdt * Bx + gdt * pre);
+    a.uxn[c] = un_;
+    if (j == 1) a.uxn[c + jtot * ld] = un_;
+    if (j == jtot) a.uxn[c - jtot * ld] = un_;
+  }
+  {
+    const float2 v0 = tuy[y][x], vw = tuy[y][x - 1], ve = tuy[y][x + 1], vs = tuy[y - 1][x], vn = tuy[y + 1][x];
+    const float rdxc_m = __ldg(a.rdxc + i), rdxc_p = __ldg(a.rdxc + i + 1);
+    const float duydx_xm = dif(v0, vw) * rdxc_m;
+    const float duydx_xp = dif(ve, v0) * rdxc_p;
+    const float duydy_ym = dif(v0, vs) * rdy;
+    const float duydy_yp = dif(vn, v0) * rdy;
+    const float cym = __ldg(a.cym + i), cyp = __ldg(a.cyp + i);
+    const float ux_xm = 0.5f * (val(tux[y - 1][x]) + val(tux[y][x]));
+    const float ux_xp = 0.5f * (val(tux[y - 1][x + 1]) + val(tux[y][x + 1]));
+    const float adv1 = -cym * ux_xm * duydx_xm - cyp * ux_xp * duydx_xp;
+    const float uy_ym = 0.5f * (val(vs) + val(v0));
+    const float uy_yp = 0.5f * (val(v0) + val(vn));
+    const float adv2 = -0.5f * uy_ym * duydy_ym - 0.5f * uy_yp * duydy_yp;
+    const float dif_ = a.rRe * ((duydx_xp - duydx_xm) * __ldg(a.rdxf + i) + (duydy_yp - duydy_ym) * rdy);
+    const float pre = -dif(tp[y][x], tp[y - 1][x]) * rdy;
+    const float A = (adv1 + adv2) + dif_ + a.ext;
+    const int c = j * ld + i;
+    a.sya[c] = A;
+    const double vn_ = v_own + eifd::f2d(adt * A + bdt * By + gdt * pre);
+    a.uyn[c] = vn_;
+    if (j == 1) a.uyn[c + jtot * ld] = vn_;
+    if (j == jtot) a.uyn[c - jtot * ld] = vn_;
+  }
+}
+
 template <int TY>
 __global__ void __launch_bounds__(TX *TY) k_predictor_mixed(PredArgsF a) {
   constexpr int PX = TX + 2, PY = TY + 2;
@@ -220,57 +286,133 @@ __global__ void __launch_bounds__(TX *TY) k_predictor_mixed(PredArgsF a) {
   }
   __syncthreads();
   if (!live) return;
-  const int x = threadIdx.x + 1, y = threadIdx.y + 1;
-  const float adt = __ldg(a.coef), bdt = __ldg(a.coef + 1), gdt = __ldg(a.coef + 2);
-  const float rdy = a.rdy;
-  if (i >= 2) {
-    const float2 u0 = tux[y][x], uw = tux[y][x - 1], ue = tux[y][x + 1], us = tux[y - 1][x], un = tux[y + 1][x];
-    const float cxm = __ldg(a.cxm + i), cxp = __ldg(a.cxp + i);
-    const float duxdx_xm = dif(u0, uw) * __ldg(a.rdxf + i - 1);
-    const float duxdx_xp = dif(ue, u0) * __ldg(a.rdxf + i);
-    const float duxdy_ym = dif(u0, us) * rdy;
-    const float duxdy_yp = dif(un, u0) * rdy;
-    const float ux_xm = 0.5f * (val(uw) + val(u0));
-    const float ux_xp = 0.5f * (val(u0) + val(ue));
-    const float adv1 = -cxm * ux_xm * duxdx_xm - cxp * ux_xp * duxdx_xp;
-    const float uy_ym = cxm * val(tuy[y][x - 1]) + cxp * val(tuy[y][x]);
-    const float uy_yp = cxm * val(tuy[y + 1][x - 1]) + cxp * val(tuy[y + 1][x]);
-    const float adv2 = -0.5f * uy_ym * duxdy_ym - 0.5f * uy_yp * duxdy_yp;
-    const float rdxc = __ldg(a.rdxc + i);
-    const float dif_ = a.rRe * ((dif(ue, u0) * __ldg(a.rdxf + i) - dif(u0, uw) * __ldg(a.rdxf + i - 1)) * rdxc +
-                                (dif(un, u0) - dif(u0, us)) * rdy * rdy);
-    const float pre = -dif(tp[y][x], tp[y][x - 1]) * rdxc;
-    const float A = (adv1 + adv2) + dif_;
-    const int c = j * ld + (i - 1);
-    a.sxa[c] = A;
-    const double un_ = u_own + eifd::f2d(adt * A + bdt * Bx + gdt * pre);
-    a.uxn[c] = un_;
-    if (j == 1) a.uxn[c + jtot * ld] = un_;
-    if (j == jtot) a.uxn[c - jtot * ld] = un_;
+  pred_mixed_cell(a, tux, tuy, tp, i, j, threadIdx.x + 1, threadIdx.y + 1, u_own, v_own, Bx, By);
+}
+
+// ---------------------------------------------------------------------------
+// The mixed predictor with its tiles staged by the tensor memory accelerator. A
+// persistent grid walks the (32 x TY)-cell tiles; for each tile one thread issues three
+// 2-D bulk tensor copies (ux, uy, p as doubles, with their one-cell halo) into one of two
+// shared-memory stages, so that the copies of the next tile are in flight while a tile
+// is computed; an mbarrier per stage counts the bytes in. The staged doubles are then
+// split into the float-pair tiles of k_predictor_mixed and the cell update is that
+// kernel's (pred_mixed_cell): the results are identical. Tensor coordinates: the ux box
+// starts at column 32 bx - 2 (UX(32 bx - 1) sits at column 32 bx - 2; an even column
+// keeps the copy on a 16-byte boundary), the uy and p boxes at column 32 bx; rows from
+// TY by (the halo row below the tile). Cells outside the tensor are filled with zeros,
+// as k_predictor_mixed stages them; the padding columns of the fields are zero.
+constexpr int TMA_BWX = 36, TMA_BWY = 34;   // box columns (doubles): ux, and uy / p
+__host__ __device__ constexpr int round128(int v) { return (v + 127) & ~127; }
+template <int TY> struct TmaLayout {
+  static constexpr int PY = TY + 2;
+  static constexpr int UX = 0;
+  static constexpr int UY = round128(TMA_BWX * PY * 8);
+  static constexpr int P = UY + round128(TMA_BWY * PY * 8);
+  static constexpr int STAGE = P + round128(TMA_BWY * PY * 8);
+  static constexpr unsigned BYTES = (TMA_BWX + 2 * TMA_BWY) * PY * 8;   // expected per stage
+  static constexpr int SMEM = 2 * STAGE + 128;                          // + alignment slack
+};
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+// bounded wait for the phase of the given parity: false when it did not complete
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
+  const unsigned addr = smem_u32(bar);
+  for (int it = 0; it < (1 << 22); it++) {
+    unsigned done;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(done) : "r"(addr), "r"(parity) : "memory");
+    if (done) return true;
   }
-  {
-    const float2 v0 = tuy[y][x], vw = tuy[y][x - 1], ve = tuy[y][x + 1], vs = tuy[y - 1][x], vn = tuy[y + 1][x];
-    const float rdxc_m = __ldg(a.rdxc + i), rdxc_p = __ldg(a.rdxc + i + 1);
-    const float duydx_xm = dif(v0, vw) * rdxc_m;
-    const float duydx_xp = dif(ve, v0) * rdxc_p;
-    const float duydy_ym = dif(v0, vs) * rdy;
-    const float duydy_yp = dif(vn, v0) * rdy;
-    const float cym = __ldg(a.cym + i), cyp = __ldg(a.cyp + i);
-    const float ux_xm = 0.5f * (val(tux[y - 1][x]) + val(tux[y][x]));
-    const float ux_xp = 0.5f * (val(tux[y - 1][x + 1]) + val(tux[y][x + 1]));
-    const float adv1 = -cym * ux_xm * duydx_xm - cyp * ux_xp * duydx_xp;
-    const float uy_ym = 0.5f * (val(vs) + val(v0));
-    const float uy_yp = 0.5f * (val(v0) + val(vn));
-    const float adv2 = -0.5f * uy_ym * duydy_ym - 0.5f * uy_yp * duydy_yp;
-    const float dif_ = a.rRe * ((duydx_xp - duydx_xm) * __ldg(a.rdxf + i) + (duydy_yp - duydy_ym) * rdy);
-    const float pre = -dif(tp[y][x], tp[y - 1][x]) * rdy;
-    const float A = (adv1 + adv2) + dif_ + a.ext;
-    const int c = j * ld + i;
-    a.sya[c] = A;
-    const double vn_ = v_own + eifd::f2d(adt * A + bdt * By + gdt * pre);
-    a.uyn[c] = vn_;
-    if (j == 1) a.uyn[c + jtot * ld] = vn_;
-    if (j == jtot) a.uyn[c - jtot * ld] = vn_;
+  return false;
+}
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y, uint64_t *bar) {
+  asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+               ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+               : "memory");
+}
+
+template <int TY>
+__global__ void __launch_bounds__(TX *TY) k_predictor_tma(const __grid_constant__ CUtensorMap mux,
+                                                          const __grid_constant__ CUtensorMap muy,
+                                                          const __grid_constant__ CUtensorMap mp, PredArgsF a, int nbx,
+                                                          int ntiles, unsigned *flags) {
+  using L = TmaLayout<TY>;
+  constexpr int PX = TX + 2, PY = TY + 2;
+  extern __shared__ unsigned char smem_dyn[];
+  unsigned char *base = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_dyn) + 127) & ~uintptr_t(127));
+  __shared__ float2 tux[PY][PX], tuy[PY][PX], tp[PY][PX];
+  __shared__ uint64_t bar[2];
+  const int tid = threadIdx.y * TX + threadIdx.x;
+  const int ld = a.ld;
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  auto issue = [&](int tile, int s) {
+    const int bx = tile % nbx, by = tile / nbx;
+    unsigned char *st = base + s * L::STAGE;
+    mbar_expect_tx(&bar[s], L::BYTES);
+    tma_load_2d(st + L::UX, &mux, TX * bx - 2, TY * by, &bar[s]);
+    tma_load_2d(st + L::UY, &muy, TX * bx, TY * by, &bar[s]);
+    tma_load_2d(st + L::P, &mp, TX * bx, TY * by, &bar[s]);
+  };
+  const int g = gridDim.x;
+  if (tid == 0) {
+    if ((int)blockIdx.x < ntiles) issue(blockIdx.x, 0);
+    if ((int)blockIdx.x + g < ntiles) issue(blockIdx.x + g, 1);
+  }
+  int n = 0;
+  for (int tile = blockIdx.x; tile < ntiles; tile += g, n++) {
+    const int s = n & 1;
+    const int bx = tile % nbx, by = tile / nbx;
+    const int i = 1 + TX * bx + threadIdx.x, j = 1 + TY * by + threadIdx.y;
+    const bool live = i <= a.itot && j <= a.jtot;
+    // the old explicit terms are streamed once: their loads go first
+    float Bx = 0.f, By = 0.f;
+    if (live) {
+      if (i >= 2) Bx = __ldg(a.sxb + j * ld + (i - 1));
+      By = __ldg(a.syb + j * ld + i);
+    }
+    const bool ok = mbar_wait(&bar[s], (n >> 1) & 1);
+    if (__syncthreads_or(!ok)) {
+      // a copy did not arrive: report it, wait (bounded) for the copies still in flight
+      // into this block's shared memory, and stop
+      if (tid == 0) {
+        atomicOr(flags, EIF_FLAG_TIMEOUT);
+        mbar_wait(&bar[s], (n >> 1) & 1);
+        if (tile + g < ntiles) mbar_wait(&bar[s ^ 1], ((n + 1) >> 1) & 1);
+      }
+      return;
+    }
+    const unsigned char *st = base + s * L::STAGE;
+    const double *rux = reinterpret_cast<const double *>(st + L::UX);
+    const double *ruy = reinterpret_cast<const double *>(st + L::UY);
+    const double *rp = reinterpret_cast<const double *>(st + L::P);
+    // tile (tx, ty) holds index (ib - 1 + tx, jb - 1 + ty): ux column tx + 1, uy and p column tx
+    for (int q = tid; q < PY * PX; q += TX * TY) {
+      const int ty = q / PX, tx = q - ty * PX;
+      tux[ty][tx] = eifd::split(rux[ty * TMA_BWX + tx + 1]);
+      tuy[ty][tx] = eifd::split(ruy[ty * TMA_BWY + tx]);
+      tp[ty][tx] = eifd::split(rp[ty * TMA_BWY + tx]);
+    }
+    const double u_own = rux[(threadIdx.y + 1) * TMA_BWX + threadIdx.x + 2];
+    const double v_own = ruy[(threadIdx.y + 1) * TMA_BWY + threadIdx.x + 1];
+    __syncthreads();
+    // the stage is consumed: the copies of the tile after next go into it
+    if (tid == 0 && tile + 2 * g < ntiles) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      issue(tile + 2 * g, s);
+    }
+    if (live) pred_mixed_cell(a, tux, tuy, tp, i, j, threadIdx.x + 1, threadIdx.y + 1, u_own, v_own, Bx, By);
+    __syncthreads();
   }
 }
 
@@ -723,6 +865,62 @@ int launch_boundaries(eif_ctx *c) {
   return EIF_OK;
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link to the driver library)
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    cudaGetLastError();
+  }
+  return fn;
+}
+
+// 2-D map of a double field (ld columns, jtot + 2 rows) with boxes of w x h values
+static bool field_map(CUtensorMap *m, const double *field, const eif_ctx *c, int w, int h) {
+  auto enc = tensor_map_encoder();
+  if (!enc) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)c->ld, (cuuint64_t)(c->jtot + 2)};
+  const cuuint64_t strides[1] = {(cuuint64_t)c->ld * sizeof(double)};
+  const cuuint32_t box[2] = {(cuuint32_t)w, (cuuint32_t)h};
+  const cuuint32_t es[2] = {1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, const_cast<double *>(field), dims, strides, box, es,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// launches the tensor-copy predictor of tile height TY; false when it cannot run
+template <int TY>
+static bool launch_predictor_tma(eif_ctx *c, const PredArgsF &a, int per_sm) {
+  using L = TmaLayout<TY>;
+  alignas(64) CUtensorMap mux, muy, mp;
+  if (!field_map(&mux, a.ux, c, TMA_BWX, TY + 2) || !field_map(&muy, a.uy, c, TMA_BWY, TY + 2) ||
+      !field_map(&mp, a.p, c, TMA_BWY, TY + 2))
+    return false;
+  const int nbx = (c->itot + TX - 1) / TX, nby = (c->jtot + TY - 1) / TY;
+  const int ntiles = nbx * nby;
+  const int grid = std::min(ntiles, c->sms * per_sm);
+  k_predictor_tma<TY><<<grid, dim3(TX, TY), L::SMEM, c->stream>>>(mux, muy, mp, a, nbx, ntiles, c->d_flags);
+  return true;
+}
+
+int predictor_prepare(eif_ctx *c) {
+  if (c->cfg.precision != EIF_PREC_MIXED || getenv("EIF_NO_TMA") || !tensor_map_encoder()) return EIF_OK;
+  int v = 0;
+  EIF_CK(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_predictor_tma<4>, TX * 4, TmaLayout<4>::SMEM));
+  c->pred_tma_ctas[0] = v;
+  EIF_CK(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_predictor_tma<8>, TX * 8, TmaLayout<8>::SMEM));
+  c->pred_tma_ctas[1] = v;
+  EIF_CK(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_predictor_tma<16>, TX * 16, TmaLayout<16>::SMEM));
+  c->pred_tma_ctas[2] = v;
+  return EIF_OK;
+}
+
 static int launch_predictor_mixed(eif_ctx *c, int rk) {
   const RK k = rk_coef(rk);
   PredArgsF a;
@@ -744,7 +942,15 @@ static int launch_predictor_mixed(eif_ctx *c, int rk) {
   a.ext = (float)c->cfg.extfrcy;
   a.itot = c->itot; a.jtot = c->jtot; a.ld = c->ld;
   EIF_PROF(c, "predictor", 1);
-  launch_tiled(k_predictor_mixed<4>, k_predictor_mixed<8>, k_predictor_mixed<16>, c->tiles.pred, c, a);
+  const int ty = c->tiles.pred;
+  const int slot = ty == 4 ? 0 : (ty == 16 ? 2 : 1);
+  bool done = false;
+  if (c->tiles.pred_copy && c->pred_tma_ctas[slot] > 0) {
+    if (ty == 4) done = launch_predictor_tma<4>(c, a, c->pred_tma_ctas[0]);
+    else if (ty == 16) done = launch_predictor_tma<16>(c, a, c->pred_tma_ctas[2]);
+    else done = launch_predictor_tma<8>(c, a, c->pred_tma_ctas[1]);
+  }
+  if (!done) launch_tiled(k_predictor_mixed<4>, k_predictor_mixed<8>, k_predictor_mixed<16>, ty, c, a);
   EIF_LAUNCH_CK(c);
   c->cur = 1 - c->cur;
   return EIF_OK;

@@ -156,6 +156,41 @@ __device__ __forceinline__ bool bounding_overlap(const PV &p0, const PV &p1, dou
   return !(fmax(p0.a, p0.b) + fmax(p1.a, p1.b) - norm < 0.);
 }
 
+// Pairs whose bounding circles overlap (collision.c:173-189) but whose ellipses are
+// apart. The reference then iterates the equivalent-circle fit (collision.c:111-135) to
+// the circles of curvature at the mutually nearest points, whose overlap is minus the
+// gap, and the pair adds no force; for nearly touching ellipses that fixed point
+// converges slowly (thousands of iterations in double precision). A line that separates
+// the two ellipses with a gap above a hundredth of the smaller minor semi-axis (far above
+// the fit's stopping error) proves the same zero contribution without the iteration.
+// Candidate normals: the centre line, the four semi-axis directions and 16 fixed
+// directions; along a unit normal n the ellipses' extents are their support values
+// sqrt(a^2 (n.u)^2 + b^2 (n.v)^2) about the centres.
+__device__ bool apart(const PV &p0, const PV &p1, double ly) {
+  const double yoff = image_offset(p0.y, p1.y, ly);
+  const double dx = p1.x - p0.x, dy = (p1.y + yoff) - p0.y;
+  double s0, c0, s1, c1;
+  sincos(p0.az, &s0, &c0);
+  sincos(p1.az, &s1, &c1);
+  const double margin = 0.01 * fmin(fmin(p0.a, p0.b), fmin(p1.a, p1.b));
+  auto gap = [&](double nx, double ny) {
+    const double u0 = nx * c0 + ny * s0, v0 = ny * c0 - nx * s0;
+    const double u1 = nx * c1 + ny * s1, v1 = ny * c1 - nx * s1;
+    const double h0 = sqrt(p0.a * p0.a * u0 * u0 + p0.b * p0.b * v0 * v0);
+    const double h1 = sqrt(p1.a * p1.a * u1 * u1 + p1.b * p1.b * v1 * v1);
+    return fabs(nx * dx + ny * dy) - h0 - h1;
+  };
+  const double d = hypot(dx, dy);
+  if (d > 0. && gap(dx / d, dy / d) > margin) return true;
+  if (gap(c0, s0) > margin || gap(-s0, c0) > margin || gap(c1, s1) > margin || gap(-s1, c1) > margin) return true;
+  for (int q = 0; q < 16; q++) {
+    double s, c;
+    sincospi(q / 16., &s, &c);
+    if (gap(c, s) > margin) return true;
+  }
+  return false;
+}
+
 // force/torque contribution of pair (n0 < n1) on particle `self` (collision.c:190-246)
 __device__ void pair_contribution(const PV &p0, const PV &p1, bool self_is_0, double ly, double out[3], bool &ok) {
   out[0] = out[1] = out[2] = 0.;
@@ -311,10 +346,13 @@ __global__ void __launch_bounds__(PAIR_WARPS * 32) k_collision(double *__restric
     if (q < cnt) {
       const int mm = list[wl][q];
       const PV pmm = load_pv(P, pcap, mm);
-      double out[3];
-      bool ok;
-      if (mm < k) pair_contribution(pmm, pk, false, ly, out, ok);
-      else pair_contribution(pk, pmm, true, ly, out, ok);
+      double out[3] = {0., 0., 0.};
+      bool ok = true;
+      if (mm < k) {
+        if (!apart(pmm, pk, ly)) pair_contribution(pmm, pk, false, ly, out, ok);
+      } else {
+        if (!apart(pk, pmm, ly)) pair_contribution(pk, pmm, true, ly, out, ok);
+      }
       ok_all &= ok;
       cval[wl][lane][0] = out[0];
       cval[wl][lane][1] = out[1];

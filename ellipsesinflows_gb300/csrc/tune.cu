@@ -117,14 +117,20 @@ int tune_tiles(eif_ctx *c) {
     const int tys[3] = {4, 8, 16};
     float best = 1e30f;
     int pick = c->tiles.pred;
-    for (int ty : tys) {
-      c->tiles.pred = ty;
-      float ms = 0.f;
-      int rc = best_ms(c, e0, e1, [&]() { return launch_predictor(c, 0); }, &ms);
-      if (rc) return rc;
-      if (ms < best) { best = ms; pick = ty; }
+    bool pick_copy = c->tiles.pred_copy;
+    // the mixed predictor with tensor-copy staging and the plain one, each tile height
+    for (int copy = 0; copy < (mixed ? 2 : 1); copy++) {
+      for (int ty : tys) {
+        c->tiles.pred = ty;
+        c->tiles.pred_copy = copy == 1;
+        float ms = 0.f;
+        int rc = best_ms(c, e0, e1, [&]() { return launch_predictor(c, 0); }, &ms);
+        if (rc) return rc;
+        if (ms < best) { best = ms; pick = ty; pick_copy = copy == 1; }
+      }
     }
     c->tiles.pred = pick;
+    c->tiles.pred_copy = pick_copy;
     best = 1e30f;
     pick = c->tiles.corr;
     for (int ty : tys) {
@@ -170,6 +176,6 @@ extern "C" int eif_tiles(eif_ctx *c, int *tiles) {
   tiles[0] = c->tiles.pred;
   tiles[1] = c->tiles.corr;
   tiles[2] = c->tiles.tdm;
-  tiles[3] = c->tiles.tuned ? 1 : 0;
+  tiles[3] = (c->tiles.tuned ? 1 : 0) | (c->tiles.pred_copy && c->pred_tma_ctas[1] > 0 ? 2 : 0);
   return EIF_OK;
 }

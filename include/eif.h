@@ -165,8 +165,11 @@ int eif_snapshot_wait(eif_ctx *ctx, double *ux, double *uy, double *p, int n, do
  * projection; 64, 128 or 256 threads per block of the block Thomas) once per grid
  * size and precision, before the first eif_integrate / eif_advance / batch capture,
  * and keeps the fastest. The shapes do not change any result. EIF_TUNE=0 in the
- * environment keeps the defaults (8, 8, 128). tiles[4]: predictor rows, projection
- * rows, Thomas threads, 1 if tuned. No counterpart in the reference. */
+ * environment keeps the defaults (8, 8, 128). In the mixed form the predictor runs either
+ * with its tiles staged by bulk tensor copies (double-buffered, TMA) or with plain loads,
+ * whichever the tuner timed faster (EIF_NO_TMA=1 at context creation: plain loads only).
+ * tiles[4]: predictor rows, projection rows, Thomas threads, flags (bit 0: tuned, bit 1:
+ * predictor tiles staged by tensor copies). No counterpart in the reference. */
 int eif_tiles(eif_ctx *ctx, int *tiles);
 
 /* ---- discrete adjoint of the step (no counterpart in the reference) ----

@@ -149,3 +149,24 @@ def test_mixed_poisson_matches_fp64(builder, gpu_lib):
     assert rel_err(interior_p(mpsi), interior_p(dpsi)) < 1e-10
     umag = max(np.abs(du).max(), np.abs(dv).max())
     assert max(np.abs(mu - du).max(), np.abs(mv - dv).max()) / umag < 1e-10
+
+
+@pytest.mark.parametrize("rows", [4, 8, 16])
+def test_tensor_copy_predictor_equals_plain_kernel(rows, gpu_lib, monkeypatch):
+    """The mixed predictor whose tiles are staged by bulk tensor copies gives the bits of
+    the plain kernel (EIF_NO_TMA=1), for every tile height, on a grid with partial tiles
+    in x (itot = 96) and in y (jtot = 200)."""
+    monkeypatch.setenv("EIF_TILES", "%d,8,128" % rows)
+    case = cases.poiseuille(itot=96, jtot=200, n=6, a=0.06, b=0.03, seed=2)
+    a = Simulation.from_case(case, precision=PREC_MIXED)
+    monkeypatch.setenv("EIF_NO_TMA", "1")
+    b = Simulation.from_case(case, precision=PREC_MIXED)
+    a.advance(3)
+    b.advance(3)
+    assert a.tiles()["predictor_rows"] == rows
+    assert a.tiles()["predictor_tensor_copies"] and not b.tiles()["predictor_tensor_copies"]
+    for x, y in zip(a.pull_fluid(), b.pull_fluid()):
+        assert np.array_equal(x, y)
+    assert np.array_equal(a.pull_particles(), b.pull_particles())
+    a.close()
+    b.close()
