@@ -67,12 +67,16 @@ HBM_BYTES = {
 # 2048 x 4096, with the source file each kernel is built from and that file's SHA-1 at
 # the capture: the roofline's `traffic` reports a stored value only while the source is
 # unchanged (otherwise null, marked stale)
+# (the DCT entries are the mean of the two passes' launches)
+_KPROF = "profiles/kernels_suspension_2048x4096_mixed.md"
+_FLUID_SHA = "30d878c1627eb34f6fdf1fa97f7dae03d8c1f6e2"
+_POISSON_SHA = "9d65ff262c0a9c373bdb119de223c6128e2de25e"
 NCU_TRAFFIC = {
     ("mixed", 2048, 4096): {
-        "predictor": (434e6, "fluid.cu", None, "profiles/kernels_suspension_2048x4096_mixed.md"),
-        "correct": (488e6, "fluid.cu", None, "profiles/kernels_suspension_2048x4096_mixed.md"),
-        "poisson_dct2": (246e6, "poisson.cu", None, "profiles/kernels_suspension_2048x4096_mixed.md"),
-        "poisson_dct3": (86e6, "poisson.cu", None, "profiles/kernels_suspension_2048x4096_mixed.md"),
+        "predictor": (435e6, "fluid.cu", _FLUID_SHA, _KPROF),
+        "correct": (490e6, "fluid.cu", _FLUID_SHA, _KPROF),
+        "poisson_dct2": (189e6, "poisson.cu", _POISSON_SHA, _KPROF),
+        "poisson_dct3": (36e6, "poisson.cu", _POISSON_SHA, _KPROF),
     },
 }
 
@@ -88,9 +92,11 @@ STEP_BYTES = {"fp64": 81 * 8, "mixed": 81 * 8 - 3 * 6 * 4}
 # FMA), the denominator of the indicator kernel's pipe roofline
 FP32_TFLOPS_MEASURED = 69.9
 
-# FP32 flops (FFMA counted twice, FADD and FMUL once) per normal-foot evaluation of the
-# mixed-form indicator kernel, from an ncu capture (value, source), or None
-INDICATOR_FLOPS_PER_EVAL = None
+# FP32 flops (FFMA counted twice, FADD and FMUL once) of the mixed-form indicator kernel
+# per normal-foot evaluation (all of the launch's flops, the far-cell tests and sums
+# included, over its evaluations): 9.03e8 flops in the captured launch of k_ibm_work_f
+# over the 2.86e6 evaluations that launch counts at this workload (value, source)
+INDICATOR_FLOPS_PER_EVAL = (316, "ncu capture of k_ibm_work_f, " + "profiles/kernels_suspension_2048x4096_mixed.md")
 
 
 def parse():
