@@ -366,33 +366,60 @@ def run_ours(args, world, rank, local, pg):
     return out, rank
 
 
+def time_batch(sims, mode, args, pg, local, clk=None):
+    """device time (ms, max over ranks) of args.steps batch steps of sims after
+    args.warmup, with the sub-iteration loops in stage kernels or per branch (mode)"""
+    import torch
+    from ellipsesinflows_gb300 import Batch
+    if mode == "branches":
+        os.environ["EIF_BATCH_SUBITER"] = "branches"
+    else:
+        os.environ.pop("EIF_BATCH_SUBITER", None)
+    try:
+        batch = Batch(sims)
+    finally:
+        os.environ.pop("EIF_BATCH_SUBITER", None)
+    stream = torch.cuda.ExternalStream(batch.stream(), device=local)
+    batch.advance(args.warmup)
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier(pg, local)
+    torch.cuda.synchronize()
+    if clk:
+        clk.begin()
+    start.record(stream)
+    batch.advance(args.steps)
+    stop.record(stream)
+    torch.cuda.synchronize()
+    if clk:
+        clk.end()
+    barrier(pg, local)
+    batch.close()
+    return max_over_ranks(pg, start.elapsed_time(stop), local)
+
+
 def run_batch(args, world, rank, local, pg):
     """64 independent suspensions of uneven sizes (cases.batch_c5) advanced by one
-    step graph per step (eif_batch_*): aggregate cell-steps/s, against the same
-    suspensions advanced one after another with eif_advance."""
+    step graph per step (eif_batch_*): aggregate cell-steps/s, with the particle
+    sub-iterations of all suspensions in one persistent kernel per RK stage; against
+    the same batch with a sub-iteration loop per suspension in its graph branch, and
+    against the suspensions advanced one after another with eif_advance."""
     import torch
-    from ellipsesinflows_gb300 import PREC_FP64, PREC_MIXED, Batch, Simulation, build, cases
+    from ellipsesinflows_gb300 import PREC_FP64, PREC_MIXED, Simulation, build, cases
     build.build()
     torch.cuda.set_device(local)
     cs = cases.batch_c5()
     prec = PREC_MIXED if args.precision == "mixed" else PREC_FP64
-    sims = [Simulation.from_case(c, precision=prec, device=local) for c in cs]
     cells = sum(c.cells for c in cs)
-    batch = Batch(sims)
-    stream = torch.cuda.ExternalStream(batch.stream(), device=local)
-    batch.advance(args.warmup)
-    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
-        barrier(pg, local)
-        torch.cuda.synchronize()
-        clk.begin()
-        start.record(stream)
-        batch.advance(args.steps)
-        stop.record(stream)
-        torch.cuda.synchronize()
-        clk.end()
-        barrier(pg, local)
-    ms = max_over_ranks(pg, start.elapsed_time(stop), local)
+        sims = [Simulation.from_case(c, precision=prec, device=local) for c in cs]
+        ms = time_batch(sims, "stage_kernels", args, pg, local, clk)
+    for s in sims:
+        s.close()
+    sims = [Simulation.from_case(c, precision=prec, device=local) for c in cs]
+    br_ms = time_batch(sims, "branches", args, pg, local)
+    for s in sims:
+        s.close()
+    sims = [Simulation.from_case(c, precision=prec, device=local) for c in cs]
     # the same suspensions one after another, each advanced the same steps with
     # eif_advance on its own stream, timed with CUDA events like the batch; the
     # separate time is the sum of the suspensions' device times
@@ -400,7 +427,6 @@ def run_batch(args, world, rank, local, pg):
     for s in sims:
         st = torch.cuda.ExternalStream(s._fn("stream")(s.ctx), device=local)
         sep_ms += timed_advance(s, st, args.steps, pg, local)
-    batch.close()
     grids = sorted({"%dx%d" % (c.itot, c.jtot) for c in cs})
     out = {
         "metric": "cell-steps/s", "value": world * cells * args.steps / (ms / 1e3), "unit": "cell-steps/s",
@@ -412,6 +438,10 @@ def run_batch(args, world, rank, local, pg):
                    "total_cells": cells, "n_particles_total": int(sum(c.n_particles for c in cs)),
                    "precision": args.precision, "l2": "inputs larger than L2 (~%d MB of device state)" % (cells * 13 * 8 // 10**6),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
+        "branches": {"value": world * cells * args.steps / (br_ms / 1e3), "unit": "cell-steps/s",
+                     "ms_per_step": br_ms / args.steps,
+                     "how": "the same batch with the sub-iteration loop of every suspension as a "
+                            "conditional node in its own graph branch (EIF_BATCH_SUBITER=branches)"},
         "separate": {"value": cells * args.steps / (sep_ms / 1e3), "unit": "cell-steps/s",
                      "ms_per_step": sep_ms / args.steps,
                      "how": "the same suspensions advanced one after another with eif_advance, each "

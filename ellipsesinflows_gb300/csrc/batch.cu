@@ -1,19 +1,26 @@
 // Batches of independent suspensions advanced by one CUDA graph per step.
 //
 // A batch groups existing contexts (any grid sizes, particle counts and both
-// precisions). Its step graph holds one branch per context, each the context's own
-// step (capture_step in graph.cu: dt, three RK stages with their device-driven
-// sub-iteration loops, the particle updates); the branches have no dependences on
-// one another, so the kernels of small suspensions run side by side and fill the
-// GPU. One graph launch advances every suspension by one step. The kernels, their
-// order within a suspension and the data they touch are those of eif_advance, so
-// every suspension gets the same bits as when advanced alone.
+// precisions). Its step graph holds one branch per context for the context's own
+// kernels (capture_step_part in graph.cu: dt, the fronts of the three RK stages, the
+// particle updates); the branches have no dependences on one another, so the kernels
+// of small suspensions run side by side and fill the GPU. The particle sub-iteration
+// loops of all suspensions with up to TT_MAX_NP particles run in one persistent kernel
+// per stage (subiter.cu): the branches join before it and fork after it. A suspension
+// with more particles keeps its own loop (a conditional node) in its branch, which then
+// runs its whole step independently; so do all suspensions when the environment
+// variable EIF_BATCH_SUBITER is "branches". One graph launch advances every suspension
+// by one step. The kernel bodies, their order within a suspension and the data they
+// touch are those of eif_advance, so every suspension gets the same bits as when
+// advanced alone.
 //
 // The branches swap double buffers, so a batch graph is tied to the buffer indices
 // of all its contexts at the start of a step; two graphs are kept (the indices
 // alternate with period one or two steps). A context whose buffers are
 // reallocated (a push with another particle count) makes the batch rebuild.
 #include "eif_internal.cuh"
+#include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -25,7 +32,9 @@ struct eif_batch {
     cudaGraphExec_t exec = nullptr;
     std::vector<int> cur0, scur0, cur1, scur1;
     std::vector<unsigned> gen;
+    std::vector<eif::SubiterPlan *> plans;   // stage kernels of the joined suspensions
   } graphs[2];
+  bool stage_kernels = true;   // joined sub-iteration loops (false: a loop per branch)
   cudaStream_t stream = nullptr;
   cudaEvent_t ev = nullptr;
   cudaEvent_t ev_step[2] = {nullptr, nullptr};
@@ -61,6 +70,7 @@ int batch_fail(eif_batch *b, int code, const std::string &msg) {
 void free_graph(eif_batch::Graph &g) {
   if (g.exec) cudaGraphExecDestroy(g.exec);
   if (g.graph) cudaGraphDestroy(g.graph);
+  for (eif::SubiterPlan *p : g.plans) eif::subiter_plan_destroy(p);
   g = eif_batch::Graph{};
 }
 
@@ -73,23 +83,96 @@ bool matches(const eif_batch *b, const eif_batch::Graph &g) {
   return true;
 }
 
+// Suspensions `idx` (at most one stage kernel's worth) with their sub-iteration loops
+// in one kernel per stage: the branches of the stage fronts join before the stage's
+// kernel, which also follows the same stage's kernel of the previous group (`prev`:
+// cooperative kernels run one at a time).
+int build_joined(eif_batch *b, eif_batch::Graph &g, const std::vector<size_t> &idx, std::vector<cudaGraphNode_t> &prev) {
+  std::vector<eif_ctx *> cs;
+  for (size_t i : idx) cs.push_back(b->ctx[i]);
+  const int m = (int)cs.size();
+  eif::SubiterPlan *plan = nullptr;
+  std::string err;
+  int rc = eif::subiter_plan_create(cs.data(), m, &plan, &err);
+  if (rc) return batch_fail(b, rc, "stage kernel: " + err);
+  g.plans.push_back(plan);
+  cudaGraphNode_t reset = nullptr;
+  if ((rc = eif::subiter_add_reset(plan, g.graph, &reset, &err))) return batch_fail(b, rc, "stage kernel: " + err);
+  for (int k = 0; k < m; k++) {
+    if ((rc = eif::step_capture_begin(cs[k])))
+      return batch_fail(b, rc, "suspension " + std::to_string(idx[k]) + ": " + eif_last_error(cs[k]));
+  }
+  std::vector<std::vector<cudaGraphNode_t>> tails(m);
+  std::vector<cudaGraphNode_t> kernel;
+  auto restore = [&]() {
+    for (int k = 0; k < m; k++) eif::step_capture_end(cs[k], g.cur0[idx[k]], g.scur0[idx[k]]);
+  };
+  for (int part = 0; part < 4; part++) {
+    for (int k = 0; k < m; k++) {
+      if ((rc = eif::capture_step_part(cs[k], g.graph, kernel, part, &tails[k]))) {
+        restore();
+        return batch_fail(b, rc, "suspension " + std::to_string(idx[k]) + ": " + eif_last_error(cs[k]));
+      }
+    }
+    if (part == 3) break;
+    std::vector<cudaGraphNode_t> deps{reset};
+    for (int k = 0; k < m; k++) {
+      eif::subiter_describe(plan, part, k, cs[k]);
+      deps.insert(deps.end(), tails[k].begin(), tails[k].end());
+    }
+    if (prev.size() == 3) deps.push_back(prev[part]);
+    cudaGraphNode_t node = nullptr;
+    if ((rc = eif::subiter_add_stage(plan, part, g.graph, deps, &node, &err))) {
+      restore();
+      return batch_fail(b, rc, "stage kernel: " + err);
+    }
+    kernel.assign(1, node);
+    if (prev.size() == 3) prev[part] = node;
+    else if (part == (int)prev.size()) prev.push_back(node);
+  }
+  for (int k = 0; k < m; k++) {
+    g.cur1[idx[k]] = cs[k]->cur;
+    g.scur1[idx[k]] = cs[k]->scur;
+  }
+  restore();
+  if ((rc = eif::subiter_upload(plan, &err))) return batch_fail(b, rc, "stage kernel: " + err);
+  return EIF_OK;
+}
+
 int build(eif_batch *b, eif_batch::Graph &out) {
   eif_batch::Graph g;
   cudaError_t e = cudaGraphCreate(&g.graph, 0);
   if (e != cudaSuccess) return batch_fail(b, EIF_ERR_CUDA, std::string("cudaGraphCreate: ") + cudaGetErrorString(e));
-  for (size_t i = 0; i < b->ctx.size(); i++) {
+  const size_t n = b->ctx.size();
+  g.cur1.assign(n, 0);
+  g.scur1.assign(n, 0);
+  std::vector<size_t> joined;
+  for (size_t i = 0; i < n; i++) {
     eif_ctx *c = b->ctx[i];
-    int cur1 = 0, scur1 = 0;
     g.cur0.push_back(c->cur);
     g.scur0.push_back(c->scur);
     g.gen.push_back(c->buf_gen);
+    if (b->stage_kernels && eif::subiter_joinable(c)) {
+      joined.push_back(i);
+      continue;
+    }
+    int cur1 = 0, scur1 = 0;
     const int rc = eif::capture_step(c, g.graph, &cur1, &scur1);
     if (rc) {
       free_graph(g);
       return batch_fail(b, rc, "suspension " + std::to_string(i) + ": " + eif_last_error(c));
     }
-    g.cur1.push_back(cur1);
-    g.scur1.push_back(scur1);
+    g.cur1[i] = cur1;
+    g.scur1[i] = scur1;
+  }
+  std::vector<cudaGraphNode_t> prev;
+  for (size_t k0 = 0; k0 < joined.size(); k0 += eif::SUBITER_MAX) {
+    const std::vector<size_t> group(joined.begin() + k0, joined.begin() + std::min(joined.size(), k0 + eif::SUBITER_MAX));
+    const int rc = build_joined(b, g, group, prev);
+    if (rc) {
+      free_graph(g);
+      return rc;
+    }
   }
   e = cudaGraphInstantiate(&g.exec, g.graph, 0);
   if (e != cudaSuccess) {
@@ -146,6 +229,8 @@ int eif_batch_create(eif_ctx *const *ctxs, int n, eif_batch **out) {
   eif_batch *b = new (std::nothrow) eif_batch;
   if (!b) return EIF_ERR_NOMEM;
   b->ctx.assign(ctxs, ctxs + n);
+  const char *mode = std::getenv("EIF_BATCH_SUBITER");
+  b->stage_kernels = !(mode && std::strcmp(mode, "branches") == 0);
   std::vector<const void *> src;
   for (int i = 0; i < n; i++) {
     src.push_back(ctxs[i]->d_scal);

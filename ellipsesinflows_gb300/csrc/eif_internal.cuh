@@ -243,6 +243,27 @@ int check_records(eif_ctx *c);
 int step_graph_launch(eif_ctx *c);
 void graphs_free(eif_ctx *c);
 int capture_step(eif_ctx *c, cudaGraph_t g, int *cur1, int *scur1);
+int step_capture_begin(eif_ctx *c);
+void step_capture_end(eif_ctx *c, int cur0, int scur0);
+int capture_step_part(eif_ctx *c, cudaGraph_t g, const std::vector<cudaGraphNode_t> &deps, int part,
+                      std::vector<cudaGraphNode_t> *sinks);
+int capture_subiteration_loop(eif_ctx *c, cudaGraph_t g, const std::vector<cudaGraphNode_t> &deps, int rk,
+                              std::vector<cudaGraphNode_t> *sinks);
+
+// ---- sub-iterations of many suspensions in one persistent kernel per stage (subiter.cu) ----
+struct SubiterPlan;
+constexpr size_t SUBITER_MAX = 1024;   // suspensions per stage kernel
+bool subiter_joinable(const eif_ctx *c);
+int subiter_plan_create(eif_ctx *const *ctx, int n, SubiterPlan **out, std::string *err);
+void subiter_plan_destroy(SubiterPlan *p);
+// the descriptor of suspension j (context c) in RK stage rk, from the state of c after
+// the capture of that stage's front
+void subiter_describe(SubiterPlan *p, int rk, int j, const eif_ctx *c);
+// the plan's memset node (arrival counters; no dependences) and the kernel node of stage rk
+int subiter_add_reset(SubiterPlan *p, cudaGraph_t g, cudaGraphNode_t *node, std::string *err);
+int subiter_add_stage(SubiterPlan *p, int rk, cudaGraph_t g, const std::vector<cudaGraphNode_t> &deps,
+                      cudaGraphNode_t *node, std::string *err);
+int subiter_upload(SubiterPlan *p, std::string *err);
 int rk_stage_front(eif_ctx *c, int rk);
 int ibm_prepare(eif_ctx *c);
 void profile_free(eif_ctx *c);
@@ -351,6 +372,12 @@ __device__ __forceinline__ bool chk(unsigned long long *rec, long long idx, long
 #else
 #define EIF_CHK(rec, idx, bound, tag) true
 #endif
+
+// mass and moment of inertia of an ellipse (src/suspensions/auxiliary.c:63-75)
+__device__ __forceinline__ double pmass(double den, double a, double b) { return den * (M_PI * a * b); }
+__device__ __forceinline__ double pmoi(double den, double a, double b) {
+  return 0.25 * pmass(den, a, b) * (a * a + b * b);
+}
 
 __device__ __forceinline__ int ux_idx(int i, int j, int ld) { return j * ld + (i - 1); }
 __device__ __forceinline__ int uy_idx(int i, int j, int ld) { return j * ld + i; }

@@ -56,71 +56,115 @@ void abort_capture(eif_ctx *c) {
 
 }  // namespace
 
+// Host state of c before the capture of a step: the graph must not depend on boxes
+// computed before it, so it starts without them.
+int step_capture_begin(eif_ctx *c) {
+  int rc = ibm_prepare(c);
+  if (rc) return rc;
+  c->boxes_x_valid = false;
+  c->weights_x_valid = false;
+  c->incr_zero = false;
+  return EIF_OK;
+}
+
+// Host state of c after the capture of a step (or after a failed capture): nothing
+// has run yet, so the step starts from the buffers (cur0, scur0); the step ends with
+// new positions, so no boxes are valid after it.
+void step_capture_end(eif_ctx *c, int cur0, int scur0) {
+  abort_capture(c);
+  c->cur = cur0;
+  c->scur = scur0;
+  c->boxes_x_valid = false;
+  c->weights_x_valid = false;
+}
+
+// Captures part `part` of one time step of c into g after the nodes deps (none: an
+// independent branch) and returns its last nodes in sinks. Part 0 is the dt decision
+// and the front of RK stage 0 (src/main.c:14-35), parts 1 and 2 the particle update
+// of the stage before (main.c:51-53) and the front of the next stage, part 3 the
+// particle update of stage 2. The sub-iteration loops (main.c:36-50) go between the
+// parts: a conditional node per context (capture_subiteration_loop), or one kernel for
+// all the suspensions of a batch.
+int capture_step_part(eif_ctx *c, cudaGraph_t g, const std::vector<cudaGraphNode_t> &deps, int part,
+                      std::vector<cudaGraphNode_t> *sinks) {
+  cudaError_t e = cudaStreamBeginCaptureToGraph(c->stream, g, deps.data(), nullptr, deps.size(),
+                                                cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return check_cuda(c, e, "cudaStreamBeginCaptureToGraph");
+  int rc;
+  if (part == 0) {
+    if ((rc = launch_decide_dt(c))) return rc;
+  } else {
+    // after a sub-iteration loop: the increments are not zero and the boxes of the
+    // loop's last positions are not those at X
+    c->incr_zero = false;
+    c->boxes_x_valid = false;
+    c->weights_x_valid = false;
+    c->bands_x_valid = false;
+    if ((rc = launch_update_particles(c))) return rc;
+  }
+  if (part < 3 && (rc = rk_stage_front(c, part))) return rc;
+  return end_capture(c, sinks);
+}
+
+// The sub-iteration loop of RK stage rk of c as a conditional WHILE node after the
+// nodes deps (its counter reset before it); sinks = {the loop node}. The last block
+// of k_increment sets the loop condition on the device.
+int capture_subiteration_loop(eif_ctx *c, cudaGraph_t g, const std::vector<cudaGraphNode_t> &deps, int rk,
+                              std::vector<cudaGraphNode_t> *sinks) {
+  std::vector<cudaGraphNode_t> tail;
+  cudaError_t e = cudaStreamBeginCaptureToGraph(c->stream, g, deps.data(), nullptr, deps.size(),
+                                                cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return check_cuda(c, e, "cudaStreamBeginCaptureToGraph");
+  // the sub-iteration counter starts at zero for every stage
+  e = cudaMemsetAsync(reinterpret_cast<unsigned *>(c->d_inc + 1), 0, sizeof(unsigned), c->stream);
+  if (e != cudaSuccess) return check_cuda(c, e, "cudaMemsetAsync");
+  int rc = end_capture(c, &tail);
+  if (rc) return rc;
+  cudaGraphConditionalHandle h;
+  e = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault);
+  if (e != cudaSuccess) return check_cuda(c, e, "cudaGraphConditionalHandleCreate");
+  cudaGraphNodeParams p = {};
+  p.type = cudaGraphNodeTypeConditional;
+  p.conditional.handle = h;
+  p.conditional.type = cudaGraphCondTypeWhile;
+  p.conditional.size = 1;
+  cudaGraphNode_t loop = nullptr;
+  e = cudaGraphAddNode(&loop, g, tail.data(), nullptr, tail.size(), &p);
+  if (e != cudaSuccess) return check_cuda(c, e, "cudaGraphAddNode (while)");
+  cudaGraph_t body = p.conditional.phGraph_out[0];
+  e = cudaStreamBeginCaptureToGraph(c->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return check_cuda(c, e, "cudaStreamBeginCaptureToGraph (body)");
+  c->in_loop = true;
+  c->loop_handle = h;
+  // the body runs repeatedly with changing increments: it always computes its boxes
+  c->incr_zero = false;
+  c->boxes_x_valid = false;
+  if ((rc = sub_iteration(c, rk))) return rc;
+  c->in_loop = false;
+  if ((rc = end_capture(c, nullptr))) return rc;
+  sinks->assign(1, loop);
+  return EIF_OK;
+}
+
 // Captures one time step of c into g (appended as an independent branch: its first
 // nodes have no dependences) and returns the buffer indices the step ends with. The
 // host state of c is left as before the capture; on failure g may hold a partial
 // branch and should be discarded.
 int capture_step(eif_ctx *c, cudaGraph_t g, int *cur1, int *scur1) {
-  int rc = ibm_prepare(c);
+  int rc = step_capture_begin(c);
   if (rc) return rc;
   const int cur0 = c->cur, scur0 = c->scur;
-  // the graph must not depend on boxes computed before it: start without them
-  c->boxes_x_valid = false;
-  c->weights_x_valid = false;
-  c->incr_zero = false;
-  auto fail_out = [&](int code) {
-    abort_capture(c);
-    c->cur = cur0;
-    c->scur = scur0;
-    c->boxes_x_valid = false;
-    c->weights_x_valid = false;
-    return code;
-  };
-  std::vector<cudaGraphNode_t> sinks;
-  cudaError_t e = cudaStreamBeginCaptureToGraph(c->stream, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
-  if (e != cudaSuccess) return fail_out(check_cuda(c, e, "cudaStreamBeginCaptureToGraph"));
-  if ((rc = launch_decide_dt(c))) return fail_out(rc);
-  for (int rk = 0; rk < 3; rk++) {
-    if ((rc = rk_stage_front(c, rk))) return fail_out(rc);
-    // the sub-iteration counter starts at zero for every stage
-    e = cudaMemsetAsync(reinterpret_cast<unsigned *>(c->d_inc + 1), 0, sizeof(unsigned), c->stream);
-    if (e != cudaSuccess) return fail_out(check_cuda(c, e, "cudaMemsetAsync"));
-    if ((rc = end_capture(c, &sinks))) return fail_out(rc);
-    cudaGraphConditionalHandle h;
-    e = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault);
-    if (e != cudaSuccess) return fail_out(check_cuda(c, e, "cudaGraphConditionalHandleCreate"));
-    cudaGraphNodeParams p = {};
-    p.type = cudaGraphNodeTypeConditional;
-    p.conditional.handle = h;
-    p.conditional.type = cudaGraphCondTypeWhile;
-    p.conditional.size = 1;
-    cudaGraphNode_t loop = nullptr;
-    e = cudaGraphAddNode(&loop, g, sinks.data(), nullptr, sinks.size(), &p);
-    if (e != cudaSuccess) return fail_out(check_cuda(c, e, "cudaGraphAddNode (while)"));
-    cudaGraph_t body = p.conditional.phGraph_out[0];
-    e = cudaStreamBeginCaptureToGraph(c->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
-    if (e != cudaSuccess) return fail_out(check_cuda(c, e, "cudaStreamBeginCaptureToGraph (body)"));
-    c->in_loop = true;
-    c->loop_handle = h;
-    // the body runs repeatedly with changing increments: it always computes its boxes
-    c->incr_zero = false;
-    c->boxes_x_valid = false;
-    if ((rc = sub_iteration(c, rk))) return fail_out(rc);
-    c->in_loop = false;
-    if ((rc = end_capture(c, nullptr))) return fail_out(rc);
-    e = cudaStreamBeginCaptureToGraph(c->stream, g, &loop, nullptr, 1, cudaStreamCaptureModeThreadLocal);
-    if (e != cudaSuccess) return fail_out(check_cuda(c, e, "cudaStreamBeginCaptureToGraph (after loop)"));
-    if ((rc = launch_update_particles(c))) return fail_out(rc);
+  std::vector<cudaGraphNode_t> tail;
+  for (int part = 0; part < 4; part++) {
+    if ((rc = capture_step_part(c, g, tail, part, &tail)) ||
+        (part < 3 && (rc = capture_subiteration_loop(c, g, tail, part, &tail)))) {
+      step_capture_end(c, cur0, scur0);
+      return rc;
+    }
   }
-  if ((rc = end_capture(c, nullptr))) return fail_out(rc);
   *cur1 = c->cur;
   *scur1 = c->scur;
-  // nothing has run yet: the step starts from the original buffers; the step ends
-  // with new positions, so no boxes are valid after it
-  c->cur = cur0;
-  c->scur = scur0;
-  c->boxes_x_valid = false;
-  c->weights_x_valid = false;
+  step_capture_end(c, cur0, scur0);
   return EIF_OK;
 }
 

@@ -1,5 +1,8 @@
 """Batches of independent suspensions (eif_batch_*): one CUDA graph launch per step
-advances every suspension, and each gets the same bits as when advanced alone."""
+advances every suspension, and each gets the same bits as when advanced alone, with
+the same sub-iteration counts. The sub-iteration loops of the batch run in one
+persistent kernel per RK stage (the default) or as a conditional loop per suspension
+(EIF_BATCH_SUBITER=branches); both are checked."""
 import numpy as np
 import pytest
 
@@ -22,9 +25,19 @@ def assert_same(a, b):
         assert np.array_equal(x, y)
     assert np.array_equal(a.pull_particles(), b.pull_particles())
     assert a.time_state() == b.time_state()
+    assert a.counters()["substeps"] == b.counters()["substeps"]
 
 
-def test_batch_equals_separate_advance(gpu_lib):
+@pytest.fixture(params=["stage_kernels", "branches"])
+def subiter_mode(request, monkeypatch):
+    if request.param == "branches":
+        monkeypatch.setenv("EIF_BATCH_SUBITER", "branches")
+    else:
+        monkeypatch.delenv("EIF_BATCH_SUBITER", raising=False)
+    return request.param
+
+
+def test_batch_equals_separate_advance(gpu_lib, subiter_mode):
     specs = members()
     solo = [Simulation.from_case(f(), precision=p) for f, p in specs]
     together = [Simulation.from_case(f(), precision=p) for f, p in specs]
@@ -35,6 +48,23 @@ def test_batch_equals_separate_advance(gpu_lib):
         batch.advance(1)
     for a, b in zip(solo, together):
         assert_same(a, b)
+
+
+def test_batch_c5_members_equal_separate_advance(gpu_lib, subiter_mode):
+    """Ten suspensions of the uneven batch workload (4 to 256 ellipses, all four grid
+    sizes) plus one without particles, five steps."""
+    specs = cases.batch_c5(count=10, seed=3)
+    empty = cases.poiseuille(itot=128, jtot=256, n=1, seed=2)
+    empty.particles = empty.particles[:0]
+    solo = [Simulation.from_case(c, precision=PREC_MIXED) for c in specs + [empty]]
+    together = [Simulation.from_case(c, precision=PREC_MIXED) for c in specs + [empty]]
+    for s in solo:
+        s.advance(5)
+    with Batch(together) as batch:
+        batch.advance(5)
+    for a, b in zip(solo, together):
+        assert_same(a, b)
+    print("sub-iterations per suspension over 5 steps:", [s.counters()["substeps"] for s in solo])
 
 
 def test_batch_rebuilds_after_a_particle_count_change(gpu_lib):
