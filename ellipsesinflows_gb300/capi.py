@@ -116,6 +116,7 @@ def bind(lib, prefix):
         "set_threads": [_vp, ctypes.c_int],
         "tiles": [_vp, _ip],
         "counters": [_vp, ctypes.POINTER(ctypes.c_longlong)],
+        "memo_count": [_vp, ctypes.POINTER(ctypes.c_longlong)],
         "stats_reset": [_vp],
         "stats_collect": [_vp],
         "stats_pull": [_vp, _dp, _dp, _dp, _dp, _dp, _ip],
@@ -419,6 +420,13 @@ class Solver:
         v = (ctypes.c_longlong * 3)()
         self._call("counters", self.ctx, v)
         return {"substeps": v[0], "indicator_cells": v[1], "normal_foot_evals": v[2]}
+
+    def memo_count(self):
+        """indicator tasks whose weights were taken from the last sub-iteration loop's
+        evaluation (eif_memo_count; counted while kernel timing is enabled)"""
+        v = ctypes.c_longlong()
+        self._call("memo_count", self.ctx, ctypes.byref(v))
+        return v.value
 
     def tiles(self):
         """tile shapes chosen by the tuner: {"predictor_rows", "projection_rows",

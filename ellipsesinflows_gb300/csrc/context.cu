@@ -434,8 +434,8 @@ int eif_create(const eif_config_t *cfg, eif_ctx **out) {
   CK_CREATE(cudaMemset(c->d_coef, 0, sizeof(float) * 32));
   CK_CREATE(cudaMalloc((void **)&c->d_scal, sizeof(double) * 4));
   CK_CREATE(cudaMemset(c->d_scal, 0, sizeof(double) * 4));
-  CK_CREATE(cudaMalloc((void **)&c->d_inc, sizeof(unsigned long long) * 5));
-  CK_CREATE(cudaMemset(c->d_inc, 0, sizeof(unsigned long long) * 5));
+  CK_CREATE(cudaMalloc((void **)&c->d_inc, sizeof(unsigned long long) * 6));
+  CK_CREATE(cudaMemset(c->d_inc, 0, sizeof(unsigned long long) * 6));
   CK_CREATE(cudaMalloc((void **)&c->d_flags, sizeof(unsigned)));
   CK_CREATE(cudaMemset(c->d_flags, 0, sizeof(unsigned)));
   CK_CREATE(cudaMallocHost((void **)&c->h_scal, sizeof(double) * 4));
@@ -448,6 +448,7 @@ int eif_create(const eif_config_t *cfg, eif_ctx **out) {
   CK_CREATE(cudaMemset(c->d_check, 0, sizeof(unsigned long long) * 4));
   c->sync_debug = getenv("EIF_SYNC_DEBUG") != nullptr;
   c->use_graphs = getenv("EIF_NO_GRAPHS") == nullptr;
+  c->memo_on = getenv("EIF_NO_MEMO") == nullptr;
 #undef CK_CREATE
   rc = poisson_init(c);
   if (rc) return rc;
@@ -966,6 +967,15 @@ int eif_counters(eif_ctx *c, long long *counts) {
   EIF_CK(c, cudaStreamSynchronize(c->stream));
   EIF_CK(c, cudaMemcpy(v, c->d_inc + 2, sizeof(v), cudaMemcpyDeviceToHost));
   for (int k = 0; k < 3; k++) counts[k] = (long long)v[k];
+  return EIF_OK;
+}
+
+int eif_memo_count(eif_ctx *c, long long *tasks) {
+  if (!c || !tasks) return EIF_ERR_ARG;
+  unsigned long long v = 0;
+  EIF_CK(c, cudaStreamSynchronize(c->stream));
+  EIF_CK(c, cudaMemcpy(&v, c->d_inc + 5, sizeof(v), cudaMemcpyDeviceToHost));
+  *tasks = (long long)v;
   return EIF_OK;
 }
 

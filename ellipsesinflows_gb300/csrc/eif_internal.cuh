@@ -145,7 +145,8 @@ struct eif_ctx {
   // particle sub-iteration: [0] residual accumulator (IEEE bits), [1] loop counter (low word)
   // and block arrivals (high word); counters reported by eif_counters: [2] sub-iterations
   // run, [3] box cells whose indicator geometry was evaluated and [4] of those the near
-  // cells that ran the normal-foot iteration ([3] and [4] while kernel timing is on)
+  // cells that ran the normal-foot iteration, [5] indicator tasks whose weights came from
+  // the memo ([3] to [5] while kernel timing is on; [5] by eif_memo_count)
   unsigned long long *d_inc = nullptr;
   // step graphs (eif_advance): one per parity of the double-buffer indices at the step's start
   struct StepGraph {
@@ -193,6 +194,11 @@ struct eif_ctx {
   int chunk_cap;                // capacity of partial in chunks
   float *pf;                    // per-particle single-precision parameters (mixed form)
   int4 *tdesc;                  // task table: particle, row, columns and image of every chunk
+  // weights of the last indicator evaluation in a sub-iteration loop (mixed form), with
+  // the particles' geometry words, boxes and first tasks (WeightMemo in ibm_device.cuh)
+  float *memo_w = nullptr, *memo_pf = nullptr;
+  int *memo_box = nullptr, *memo_off = nullptr, *memo_valid = nullptr;
+  bool memo_on = true;          // false: EIF_NO_MEMO set, every evaluation computes
   int *band_lists, *band_counts;// ordered (particle, image) lists per band of gather rows
   int band_cap;
   int4 *edesc = nullptr;        // per (particle, image): box, row pitch and scratch offset (gather)

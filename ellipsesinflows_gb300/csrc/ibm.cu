@@ -75,9 +75,15 @@ __global__ void k_chunk_reduce(const double *__restrict__ partial, const int *__
   chunk_reduce_warp(partial, off, P, pcap, np, f0, f1, f2, bd, (blockIdx.x * blockDim.x + threadIdx.x) >> 5);
 }
 
+// save: after an indicator evaluation that stored its weights in the memo (with iter:
+// only in the sub-iterations after the first, which evaluate the geometry)
 __global__ void k_chunk_reduce_f(const float *__restrict__ partial, const int *__restrict__ off, double *__restrict__ P,
-                                 int pcap, int np, int f0, int f1, int f2, Bounds bd) {
-  chunk_reduce_f_warp(partial, off, P, pcap, np, f0, f1, f2, bd, (blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+                                 int pcap, int np, int f0, int f1, int f2, Bounds bd, WeightMemo memo, int save,
+                                 const unsigned *__restrict__ iter, const float *__restrict__ pf,
+                                 const int *__restrict__ box) {
+  const bool s = save && (!iter || *iter != 0u);
+  chunk_reduce_f_warp(partial, off, P, pcap, np, f0, f1, f2, bd, (blockIdx.x * blockDim.x + threadIdx.x) >> 5,
+                      s ? &memo : nullptr, pf, box);
 }
 
 // exclusive scan of the chunk counts (one block); off[np] = total
@@ -364,6 +370,14 @@ int ibm_reserve(eif_ctx *c, size_t chunks) {
   EIF_CK(c, cudaMalloc((void **)&c->band_counts, sizeof(int) * (size_t)nbands));
   EIF_CK(c, cudaMalloc((void **)&c->band_marks, sizeof(unsigned) * (size_t)nbands * ((3 * c->np + 31) / 32)));
   EIF_CK(c, cudaMalloc((void **)&c->edesc, sizeof(int4) * 6 * (size_t)c->np));
+  if (c->cfg.precision == EIF_PREC_MIXED) {
+    EIF_CK(c, cudaMalloc((void **)&c->memo_w, sizeof(float) * c->wcap));
+    EIF_CK(c, cudaMalloc((void **)&c->memo_pf, sizeof(float) * PF_WORDS * c->np));
+    EIF_CK(c, cudaMalloc((void **)&c->memo_box, sizeof(int) * 12 * c->np));
+    EIF_CK(c, cudaMalloc((void **)&c->memo_off, sizeof(int) * c->np));
+    EIF_CK(c, cudaMalloc((void **)&c->memo_valid, sizeof(int)));
+    EIF_CK(c, cudaMemset(c->memo_valid, 0, sizeof(int)));
+  }
   return EIF_OK;
 }
 
@@ -379,6 +393,9 @@ void ibm_free(eif_ctx *c) {
   if (c->band_counts) cudaFree(c->band_counts);
   if (c->band_marks) cudaFree(c->band_marks);
   if (c->edesc) cudaFree(c->edesc);
+  for (void *m : {(void *)c->memo_w, (void *)c->memo_pf, (void *)c->memo_box, (void *)c->memo_off, (void *)c->memo_valid})
+    if (m) cudaFree(m);
+  c->memo_w = nullptr; c->memo_pf = nullptr; c->memo_box = nullptr; c->memo_off = nullptr; c->memo_valid = nullptr;
   c->band_lists = nullptr; c->band_counts = nullptr; c->band_marks = nullptr; c->edesc = nullptr;
   c->box = nullptr; c->chunk_off = nullptr; c->partial = nullptr; c->wbuf = nullptr; c->wcache = nullptr;
   c->weights_x_valid = false;
@@ -418,6 +435,7 @@ static int launch_boxes(eif_ctx *c, bool use_increment) {
 
 static int launch_work(eif_ctx *c, int mode, int cn) {
   WorkArgs w = work_args(c, mode, cn);
+  const bool mixed = c->cfg.precision == EIF_PREC_MIXED;
   // weights at the positions X (inertia with zero increments, or the exchange)
   // are stored once and reused while the boxes at X stay valid
   const bool x_only = mode == 1 || c->incr_zero;
@@ -441,8 +459,12 @@ static int launch_work(eif_ctx *c, int mode, int cn) {
   }
   const int per_sm = c->ibm_ctas_per_sm[per_sm_idx];
   const int blocks = std::max(1, std::min(c->sms * per_sm, (c->chunk_cap * 32 + 255) / 256));
+  // the weight memo (mixed form): the loop's evaluations with geometry (integrals 1)
+  // store their weights in it; the first evaluation at X of a stage (integrals 0,
+  // weights stored for the stage) takes them where the geometry is the memo's
+  const bool memo_store = mixed && mode == 0 && cn == 1 && (c->in_loop || w.wmode == 0);
+  if (mixed && mode == 0 && cn == 0 && w.wmode == 1 && c->memo_on) w.memo_mode = 1;
   {
-    const bool mixed = c->cfg.precision == EIF_PREC_MIXED;
     // launches that evaluate the indicator geometry are timed as ibm_indicator, those
     // with stored weights (sums and field contributions only) as inertia or exchange
     const bool geometry = w.wmode != 2 && !(mixed && c->in_loop);
@@ -452,13 +474,14 @@ static int launch_work(eif_ctx *c, int mode, int cn) {
       // first sub-iteration: cached weights; later ones: full evaluation (decided on the device)
       WorkArgs w1 = w, w2 = w;
       w1.wmode = 2; w1.gate = 1;
-      w2.wmode = 0; w2.gate = 2;
+      w2.wmode = 0; w2.gate = 2; w2.memo_mode = 2;
       k_ibm_sum_f<<<c->sms * c->ibm_ctas_per_sm[2], 256, 0, c->stream>>>(w1);
       EIF_LAUNCH_CK(c);
       k_ibm_work_f<<<blocks, 256, 0, c->stream>>>(w2);
     } else if (mixed && w.wmode == 2) {
       k_ibm_sum_f<<<c->sms * c->ibm_ctas_per_sm[2], 256, 0, c->stream>>>(w);
     } else if (mixed) {
+      if (memo_store) w.memo_mode = 2;
       k_ibm_work_f<<<blocks, 256, 0, c->stream>>>(w);
     } else {
       k_ibm_work<<<blocks, 256, 0, c->stream>>>(w);
@@ -469,10 +492,10 @@ static int launch_work(eif_ctx *c, int mode, int cn) {
   const int f1 = mode == 0 ? EIF_P_IUY0 + cn : EIF_P_FUY;
   const int f2 = mode == 0 ? EIF_P_IVZ0 + cn : EIF_P_TVZ;
   EIF_PROF(c, "ibm_reduce", 1);
-  if (c->cfg.precision == EIF_PREC_MIXED) {
-    k_chunk_reduce_f<<<(c->np * 32 + 255) / 256, 256, 0, c->stream>>>(reinterpret_cast<const float *>(c->partial),
-                                                                        c->chunk_off, c->P, c->pcap, c->np, f0, f1,
-                                                                        f2, bounds_of(c));
+  if (mixed) {
+    k_chunk_reduce_f<<<(c->np * 32 + 255) / 256, 256, 0, c->stream>>>(
+        reinterpret_cast<const float *>(c->partial), c->chunk_off, c->P, c->pcap, c->np, f0, f1, f2, bounds_of(c),
+        memo_of(c), memo_store ? 1 : 0, c->in_loop ? w.iter : nullptr, c->pf, c->box);
   } else {
     k_chunk_reduce<<<(c->np * 32 + 255) / 256, 256, 0, c->stream>>>(c->partial, c->chunk_off, c->P, c->pcap, c->np,
                                                                       f0, f1, f2, bounds_of(c));

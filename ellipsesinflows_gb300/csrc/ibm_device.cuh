@@ -333,6 +333,24 @@ __device__ __forceinline__ void row_chords(T al, T ka, T de, T so2, T si2, T ro2
   }
 }
 
+// The last indicator evaluation of the mixed form inside a sub-iteration loop (at the
+// positions X + dX of a sub-iteration after the first): its weights, one per task slot,
+// and the particles' geometry parameters (the PF_WORDS block), boxes and first task,
+// with a flag set once a complete evaluation is stored. The loop stops when the
+// increments have settled, so the positions X of the next stage differ from those by
+// the last change of the increments (below 1e-8 dt in velocity); the single-precision
+// geometry of nearly every particle is then bitwise the stored one, and so are its
+// weights, which the next stage's first evaluation copies instead of recomputing.
+struct WeightMemo {
+  float *w;
+  float *pf;
+  int *box, *off;
+  int *valid;
+};
+// geometry words of the per-particle parameter block (everything but the mass, inertia
+// and velocity words PF_RPM .. PF_VZ); with the 12 box bounds, 32 words: one per lane
+__device__ __forceinline__ int memo_word(int lane) { return lane < 6 ? lane : lane + 5; }
+
 struct WorkArgs {
   const double *P;
   const double *ux, *uy, *xc, *yc, *dt;
@@ -356,8 +374,13 @@ struct WorkArgs {
   int gate;   // with iter (mixed form): 1 runs only in the first sub-iteration, 2 only afterwards
   int weights_only;   // exchange (double precision): the cell contributions are the weights (w, w)
   // box cells whose geometry is evaluated and, of those, the near cells that run the
-  // normal-foot iteration, added to count[0] and count[1] (null: not counted)
+  // normal-foot iteration, added to count[0] and count[1], and the tasks whose weights
+  // come from the memo, added to count[2] (null: not counted)
   unsigned long long *count;
+  // mixed form: memo_mode 1 takes the weights of a task from the memo when its
+  // particle's geometry and boxes are the memo's; 2 stores computed weights in it
+  WeightMemo memo;
+  int memo_mode;
   Bounds bd;
 };
 
@@ -642,8 +665,28 @@ __device__ __forceinline__ void ibm_work_f_tasks(const WorkArgs &a, int wmode, i
     float cX[2], th2[2];
     bool cin[2];
     unsigned near_mask[2];
-    if (wmode == 2) {
+    // the memo's weights for this task when the particle's geometry words and boxes are
+    // bitwise those of the stored evaluation (its tasks are then the same rows, shifted
+    // by the difference of the first tasks)
+    bool reuse = false;
+    long long src = c;
+    if (a.memo_mode == 1 && ldro<NC>(a.memo.valid) != 0) {
+      bool eq;
+      if (lane < 20) {
+        const size_t q = (size_t)PF_WORDS * n + memo_word(lane);
+        eq = __float_as_uint(ldro<NC>(a.pf + q)) == __float_as_uint(ldro<NC>(a.memo.pf + q));
+      } else {
+        const size_t q = 12 * (size_t)n + (lane - 20);
+        eq = ldro<NC>(a.box + q) == ldro<NC>(a.memo.box + q);
+      }
+      reuse = __all_sync(0xffffffffu, eq);
+      if (reuse) src = (long long)c + (ldro<NC>(a.memo.off + n) - ldro<NC>(a.off + n));
+      if (reuse && a.count && lane == 0) atomicAdd(a.count + 2, 1ull);
+    }
+    if (wmode == 2 || reuse) {
       // weights of the same geometry from an earlier evaluation
+      const float *wsrc = reuse ? a.memo.w : wcache;
+      const long long bound = reuse ? a.bd.wbuf : 2 * a.bd.wbuf;
 #pragma unroll
       for (int half = 0; half < CHUNK / 32; half++) {
         const int i = (task ? t.ib : 1) + half * 32 + lane;
@@ -651,11 +694,11 @@ __device__ __forceinline__ void ibm_work_f_tasks(const WorkArgs &a, int wmode, i
         if (in) {
           in = EIF_CHK(a.bd.rec, j * ld + i, a.bd.field, 54) && EIF_CHK(a.bd.rec, (j + 1) * ld + i, a.bd.field, 55) &&
                EIF_CHK(a.bd.rec, j * ld + (i - 1), a.bd.field, 56) &&
-               EIF_CHK(a.bd.rec, (long long)c * CHUNK + half * 32 + lane, 2 * a.bd.wbuf, 59);
+               EIF_CHK(a.bd.rec, src * CHUNK + half * 32 + lane, bound, 59);
         }
         cin[half] = in;
         cX[half] = ((float)(i - i0) - gx) * dxf;
-        th2[half] = in ? wcache[(size_t)c * CHUNK + half * 32 + lane] : 0.f;
+        th2[half] = in ? wsrc[(size_t)src * CHUNK + half * 32 + lane] : 0.f;
       }
     } else {
     // far cells of this row (PF_AL .. PF_RO2: al, ka, de, so^2, si^2, ro^2)
@@ -706,12 +749,18 @@ __device__ __forceinline__ void ibm_work_f_tasks(const WorkArgs &a, int wmode, i
     for (int half = 0; half < CHUNK / 32; half++)
       if ((near_mask[half] >> lane) & 1u) th2[half] = slots[rank[half]].x;
     __syncwarp();
+    if (a.memo_mode == 2) {
+#pragma unroll
+      for (int half = 0; half < CHUNK / 32; half++)
+        if (EIF_CHK(a.bd.rec, (long long)c * CHUNK + half * 32 + lane, a.bd.wbuf, 61))
+          a.memo.w[(size_t)c * CHUNK + half * 32 + lane] = th2[half];
+    }
+    }
     if (wmode == 1) {
 #pragma unroll
       for (int half = 0; half < CHUNK / 32; half++)
         if (EIF_CHK(a.bd.rec, (long long)c * CHUNK + half * 32 + lane, 2 * a.bd.wbuf, 60))
           wcache[(size_t)c * CHUNK + half * 32 + lane] = th2[half];
-    }
     }
     float sacc0 = 0.f, sacc1 = 0.f, sacc2 = 0.f;
 #pragma unroll
@@ -895,10 +944,25 @@ __device__ __forceinline__ void chunk_reduce_warp(const double *partial, const i
 // accumulated in double-float arithmetic (TwoSum) on the FP32 pipe: the sum of at most
 // a few hundred floats is kept to about 48 bits, and the result is rounded once to
 // double.
+// With memo set (after a sub-iteration's indicator evaluation that stored its weights in
+// it), the particle's geometry words, boxes and first task are copied to the memo.
 __device__ __forceinline__ void chunk_reduce_f_warp(const float *partial, const int *off, double *P, int pcap, int np,
-                                                    int f0, int f1, int f2, const Bounds &bd, int n) {
+                                                    int f0, int f1, int f2, const Bounds &bd, int n,
+                                                    const WeightMemo *memo = nullptr, const float *pf = nullptr,
+                                                    const int *box = nullptr) {
   const int lane = threadIdx.x & 31;
   if (n >= np) return;
+  if (memo) {
+    if (lane < 20) {
+      const size_t q = (size_t)PF_WORDS * n + memo_word(lane);
+      memo->pf[q] = pf[q];
+    } else {
+      const size_t q = 12 * (size_t)n + (lane - 20);
+      memo->box[q] = box[q];
+    }
+    if (lane == 0) memo->off[n] = off[n];
+    if (lane == 0 && n == 0) *memo->valid = 1;
+  }
   if (!EIF_CHK(bd.rec, n + 1, bd.off, 33)) return;
   const int c0 = off[n], c1 = off[n + 1];
   float h[3] = {0.f, 0.f, 0.f}, l[3] = {0.f, 0.f, 0.f};
@@ -945,6 +1009,16 @@ inline Bounds bounds_of(const eif_ctx *c) {
   return b;
 }
 
+inline WeightMemo memo_of(const eif_ctx *c) {
+  WeightMemo m;
+  m.w = c->memo_w;
+  m.pf = c->memo_pf;
+  m.box = c->memo_box;
+  m.off = c->memo_off;
+  m.valid = c->memo_valid;
+  return m;
+}
+
 // boxes of the particles at X (+ dX with use_increment); their task counts go to
 // nchunk = chunk_off + np + 1
 inline BoxArgs box_args(const eif_ctx *c, bool use_increment) {
@@ -983,6 +1057,8 @@ inline WorkArgs work_args(const eif_ctx *c, int mode, int cn) {
   w.gate = 0;
   w.weights_only = c->ibm_weights_only ? 1 : 0;
   w.count = nullptr;
+  w.memo = memo_of(c);
+  w.memo_mode = 0;
   return w;
 }
 

@@ -187,8 +187,10 @@ __global__ void __launch_bounds__(SUB_THREADS, 2) k_subiterations(StageArgs s) {
       unsigned long long *res = s.res + 2 * j + (it & 1u);
       for (int m = first_unit(wid, d.u_part, W); m < d.np; m += W) {
         if (d.mixed) {
+          // after a sub-iteration with the indicator geometry: its weights are in the memo
           chunk_reduce_f_warp(reinterpret_cast<const float *>(d.work.partial), d.off, d.P, d.pcap, d.np,
-                              EIF_P_IUX0 + 1, EIF_P_IUY0 + 1, EIF_P_IVZ0 + 1, d.box.bd, m);
+                              EIF_P_IUX0 + 1, EIF_P_IUY0 + 1, EIF_P_IVZ0 + 1, d.box.bd, m,
+                              it > 0 && d.work.memo_mode == 2 ? &d.work.memo : nullptr, d.work.pf, d.box.box);
         } else {
           chunk_reduce_warp(d.work.partial, d.off, d.P, d.pcap, d.np, EIF_P_IUX0 + 1, EIF_P_IUY0 + 1,
                             EIF_P_IVZ0 + 1, d.box.bd, m);
@@ -289,6 +291,8 @@ void subiter_describe(SubiterPlan *p, int rk, int j, const eif_ctx *c) {
   SubDesc &d = p->h[(size_t)rk * p->n + j];
   d.box = box_args(c, true);
   d.work = work_args(c, 0, 1);
+  // the evaluations with geometry (sub-iterations after the first) store their weights
+  if (c->cfg.precision == EIF_PREC_MIXED) d.work.memo_mode = 2;
   d.P = c->P;
   d.pcap = c->pcap;
   d.np = c->np;

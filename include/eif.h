@@ -298,6 +298,13 @@ int eif_profile_get(eif_ctx *ctx, int k, char *name, int name_len, long long *la
  * of them that ran the normal-foot iteration (src/ellipse.c:30-65), both counted
  * only while kernel timing is enabled. No counterpart in the reference. */
 int eif_counters(eif_ctx *ctx, long long *counts);
+/* indicator tasks (box rows) of the mixed form whose weights the first evaluation of an
+ * RK stage took from the last evaluation of the previous sub-iteration loop instead of
+ * computing them (the particle's single-precision geometry and boxes bitwise equal to
+ * that evaluation's, so the weights are too); counted while kernel timing is enabled.
+ * EIF_NO_MEMO=1 in the environment at eif_create turns the reuse off. No counterpart in
+ * the reference. */
+int eif_memo_count(eif_ctx *ctx, long long *tasks);
 
 #ifdef __cplusplus
 }

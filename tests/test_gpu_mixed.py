@@ -170,3 +170,41 @@ def test_tensor_copy_predictor_equals_plain_kernel(rows, gpu_lib, monkeypatch):
     assert np.array_equal(a.pull_particles(), b.pull_particles())
     a.close()
     b.close()
+
+
+def test_weight_memo_gives_the_same_bits(gpu_lib, monkeypatch):
+    """The first indicator evaluation of an RK stage takes the weights of the particles
+    whose single-precision geometry is bitwise that of the previous loop's last
+    evaluation: the states with and without the memo (EIF_NO_MEMO) are equal bit for
+    bit, through the step graphs and through the host-driven stages (kernel timing on),
+    and with timing on the memo is seen to serve tasks."""
+    case = cases.poiseuille(itot=256, jtot=512, n=24, a=0.04, b=0.02, seed=4)
+
+    def make(memo):
+        if memo:
+            monkeypatch.delenv("EIF_NO_MEMO", raising=False)
+        else:
+            monkeypatch.setenv("EIF_NO_MEMO", "1")
+        s = Simulation.from_case(case, precision=PREC_MIXED)
+        monkeypatch.delenv("EIF_NO_MEMO", raising=False)
+        return s
+
+    def same(a, b):
+        for x, y in zip(a.pull_fluid(), b.pull_fluid()):
+            assert np.array_equal(x, y)
+        assert np.array_equal(a.pull_particles(), b.pull_particles())
+
+    off, on = make(False), make(True)
+    for s in (off, on):
+        s.advance(4)
+    same(off, on)
+    for s in (off, on):
+        s._call("profile_enable", s.ctx, 1)
+        s.advance(3)
+        s._call("profile_enable", s.ctx, 0)
+    same(off, on)
+    assert off.memo_count() == 0
+    print("tasks from the memo:", on.memo_count(), "box cells evaluated:", on.counters()["indicator_cells"],
+          "without the memo:", off.counters()["indicator_cells"])
+    assert on.memo_count() > 0
+    assert on.counters()["indicator_cells"] < off.counters()["indicator_cells"]
