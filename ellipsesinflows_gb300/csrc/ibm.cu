@@ -65,7 +65,7 @@ __global__ void __launch_bounds__(256, 3) k_ibm_work_f(WorkArgs a) {
                          slot_buf[threadIdx.x >> 5]);
 }
 
-__global__ void __launch_bounds__(256, 6) k_ibm_sum_f(WorkArgs a) {
+__global__ void __launch_bounds__(256, 4) k_ibm_sum_f(WorkArgs a) {
   if (a.gate && ((a.gate == 1) != (*a.iter == 0u))) return;
   ibm_sum_f_tasks<true>(a, (blockIdx.x * blockDim.x + threadIdx.x) >> 5, (gridDim.x * blockDim.x) >> 5);
 }

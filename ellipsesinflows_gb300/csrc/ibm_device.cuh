@@ -860,24 +860,42 @@ __device__ __forceinline__ void ibm_sum_f_tasks(const WorkArgs &a, int first, in
     const float gyi = m == 0 ? qE.x : (m == 1 ? qE.y : qE.z);
     const int j = task ? t.j : 1;
     const float Y = ((float)(j - j0i) - gyi) * dyf;
-    float sacc0 = 0.f, sacc1 = 0.f, sacc2 = 0.f;
-#pragma unroll 1
+    // the field values of both halves are loaded before either is used, so that the
+    // warp has all eight loads of the task in flight at once
+    bool live[2];
+    float thv[2];
+    double uw[2], ue[2], vs[2], vn[2];
+#pragma unroll
     for (int half = 0; half < CHUNK / 32; half++) {
       const int i = (task ? t.ib : 1) + half * 32 + lane;
-      const long long slot = (long long)c * CHUNK + half * 32 + lane;
       bool in = task && i <= t.ie;
       if (in) {
         in = EIF_CHK(a.bd.rec, j * ld + i, a.bd.field, 74) && EIF_CHK(a.bd.rec, (j + 1) * ld + i, a.bd.field, 75) &&
              EIF_CHK(a.bd.rec, j * ld + (i - 1), a.bd.field, 76);
       }
-      float2 contrib = make_float2(0.f, 0.f);
       const float th = in ? th_pre[half] : 0.f;
+      thv[half] = th;
       // cells of weight exactly zero (inertia: far outside; exchange: any far cell) are skipped
-      const bool live = in && (a.mode == 0 ? th != -1.f : fabsf(th) != 1.f);
-      if (live) {
+      live[half] = in && (a.mode == 0 ? th != -1.f : fabsf(th) != 1.f);
+      uw[half] = ue[half] = vs[half] = vn[half] = 0.;
+      if (live[half]) {
+        uw[half] = __ldg(a.ux + j * ld + (i - 1));
+        ue[half] = __ldg(a.ux + j * ld + i);
+        vs[half] = __ldg(a.uy + j * ld + i);
+        vn[half] = __ldg(a.uy + (j + 1) * ld + i);
+      }
+    }
+    float sacc0 = 0.f, sacc1 = 0.f, sacc2 = 0.f;
+#pragma unroll
+    for (int half = 0; half < CHUNK / 32; half++) {
+      const int i = (task ? t.ib : 1) + half * 32 + lane;
+      const long long slot = (long long)c * CHUNK + half * 32 + lane;
+      float2 contrib = make_float2(0.f, 0.f);
+      const float th = thv[half];
+      if (live[half]) {
         const float X = ((float)(i - i0) - gx) * dxf;
-        const float uxs = eifd::d2f(__ldg(a.ux + j * ld + (i - 1))) + eifd::d2f(__ldg(a.ux + j * ld + i));
-        const float uys = eifd::d2f(__ldg(a.uy + j * ld + i)) + eifd::d2f(__ldg(a.uy + (j + 1) * ld + i));
+        const float uxs = eifd::d2f(uw[half]) + eifd::d2f(ue[half]);
+        const float uys = eifd::d2f(vs[half]) + eifd::d2f(vn[half]);
         if (a.mode == 0) {
           const float w = 0.5f * (1.f + th);
           const float valx = w * 0.5f * uxs * dxdy;
