@@ -41,3 +41,22 @@ def test_create_rejects_invalid_configuration():
     rc = lib.eif_create(ctypes.byref(cfg), ctypes.byref(ctx))
     assert rc == -1
     lib.eif_destroy(ctx)
+
+
+def test_plain_c_host_builds_against_the_header(tmp_path):
+    """tests/c/eif_abi_run.c, a C99 host that uses only include/eif.h, compiles without
+    warnings and links against the library (it runs on the GPU in
+    tests/test_gpu_c_host.py)."""
+    import shutil
+    import subprocess
+    from ellipsesinflows_gb300 import build
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    lib = build.build()
+    exe = str(tmp_path / "eif_abi_run")
+    subprocess.run([cc, "-std=c99", "-O2", "-Wall", "-Werror", "-I" + os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "c", "eif_abi_run.c"), "-o", exe, "-L" + os.path.dirname(lib),
+                    "-leif_gb300", "-Wl,-rpath," + os.path.dirname(lib)], check=True)
+    run = subprocess.run([exe], capture_output=True, text=True)
+    assert run.returncode == 2 and "usage" in run.stderr
