@@ -665,6 +665,26 @@ __device__ __forceinline__ void ibm_work_f_tasks(const WorkArgs &a, int wmode, i
     float cX[2], th2[2];
     bool cin[2];
     unsigned near_mask[2];
+    // the cells of the task and their field values: loaded before the geometry, so that
+    // the loads are in flight while the weights are evaluated
+    double fuw[2], fue[2], fvs[2], fvn[2];
+#pragma unroll
+    for (int half = 0; half < CHUNK / 32; half++) {
+      const int i = (task ? t.ib : 1) + half * 32 + lane;
+      bool in = task && i <= t.ie;
+      if (in) {
+        in = EIF_CHK(a.bd.rec, j * ld + i, a.bd.field, 54) && EIF_CHK(a.bd.rec, (j + 1) * ld + i, a.bd.field, 55) &&
+             EIF_CHK(a.bd.rec, j * ld + (i - 1), a.bd.field, 56);
+      }
+      cin[half] = in;
+      fuw[half] = fue[half] = fvs[half] = fvn[half] = 0.;
+      if (in) {
+        fuw[half] = __ldg(a.ux + j * ld + (i - 1));
+        fue[half] = __ldg(a.ux + j * ld + i);
+        fvs[half] = __ldg(a.uy + j * ld + i);
+        fvn[half] = __ldg(a.uy + (j + 1) * ld + i);
+      }
+    }
     // the memo's weights for this task when the particle's geometry words and boxes are
     // bitwise those of the stored evaluation (its tasks are then the same rows, shifted
     // by the difference of the first tasks)
@@ -690,15 +710,9 @@ __device__ __forceinline__ void ibm_work_f_tasks(const WorkArgs &a, int wmode, i
 #pragma unroll
       for (int half = 0; half < CHUNK / 32; half++) {
         const int i = (task ? t.ib : 1) + half * 32 + lane;
-        bool in = task && i <= t.ie;
-        if (in) {
-          in = EIF_CHK(a.bd.rec, j * ld + i, a.bd.field, 54) && EIF_CHK(a.bd.rec, (j + 1) * ld + i, a.bd.field, 55) &&
-               EIF_CHK(a.bd.rec, j * ld + (i - 1), a.bd.field, 56) &&
-               EIF_CHK(a.bd.rec, src * CHUNK + half * 32 + lane, bound, 59);
-        }
-        cin[half] = in;
+        if (cin[half]) cin[half] = EIF_CHK(a.bd.rec, src * CHUNK + half * 32 + lane, bound, 59);
         cX[half] = ((float)(i - i0) - gx) * dxf;
-        th2[half] = in ? wsrc[(size_t)src * CHUNK + half * 32 + lane] : 0.f;
+        th2[half] = cin[half] ? wsrc[(size_t)src * CHUNK + half * 32 + lane] : 0.f;
       }
     } else {
     // far cells of this row (PF_AL .. PF_RO2: al, ka, de, so^2, si^2, ro^2)
@@ -708,12 +722,7 @@ __device__ __forceinline__ void ibm_work_f_tasks(const WorkArgs &a, int wmode, i
 #pragma unroll
     for (int half = 0; half < CHUNK / 32; half++) {
       const int i = (task ? t.ib : 1) + half * 32 + lane;
-      bool in = task && i <= t.ie;
-      if (in) {
-        in = EIF_CHK(a.bd.rec, j * ld + i, a.bd.field, 54) && EIF_CHK(a.bd.rec, (j + 1) * ld + i, a.bd.field, 55) &&
-             EIF_CHK(a.bd.rec, j * ld + (i - 1), a.bd.field, 56);
-      }
-      cin[half] = in;
+      const bool in = cin[half];
       bool near = false;
       float x_ = 0.f, y_ = 0.f;
       const float X = ((float)(i - i0) - gx) * dxf;
@@ -772,8 +781,8 @@ __device__ __forceinline__ void ibm_work_f_tasks(const WorkArgs &a, int wmode, i
       const bool live = a.mode == 0 ? th_ != -1.f : fabsf(th_) != 1.f;
       if (cin[half] && live) {
         const float X = cX[half], th = th_;
-        const float uxs = eifd::d2f(__ldg(a.ux + j * ld + (i - 1))) + eifd::d2f(__ldg(a.ux + j * ld + i));
-        const float uys = eifd::d2f(__ldg(a.uy + j * ld + i)) + eifd::d2f(__ldg(a.uy + (j + 1) * ld + i));
+        const float uxs = eifd::d2f(fuw[half]) + eifd::d2f(fue[half]);
+        const float uys = eifd::d2f(fvs[half]) + eifd::d2f(fvn[half]);
         if (a.mode == 0) {
           const float w = 0.5f * (1.f + th);
           const float valx = w * 0.5f * uxs * dxdy;
