@@ -306,6 +306,7 @@ def run_ours(args, world, rank, local, pg):
     # (host-driven launches, same kernels), with the indicator work counted ----
     prof_steps = max(1, min(args.steps, 3))
     cnt0 = sim.counters()
+    memo0 = sim.memo_count() if precision_is_mixed(args) else 0
     sim._call("profile_reset", sim.ctx)
     sim._call("profile_enable", sim.ctx, 1)
     sim.advance(prof_steps)
@@ -314,6 +315,7 @@ def run_ours(args, world, rank, local, pg):
     cnt1 = sim.counters()
     prof = profile_entries(sim)
     counts = {k: cnt1[k] - cnt0[k] for k in cnt1}
+    counts["memo_tasks"] = (sim.memo_count() - memo0) if precision_is_mixed(args) else 0
     # ---- the logging reductions of one log event (divergence, momentum, energy) on
     # the device, against pulling the two velocity fields for a host reduction ----
     log_ms = None
@@ -589,10 +591,16 @@ def accuracy_leg(args, case, device, pg, world):
     return fp64, accuracy, developed
 
 
+def precision_is_mixed(args):
+    return args.precision == "mixed"
+
+
 def indicator_roofline(prof, counts, prof_steps):
     """The indicator kernel (normal-foot iteration of every near cell, the step's largest
-    kernel): work counted on the device during the profiling pass, over its live event
-    time; FP32 pipe use from the flops per normal-foot evaluation of an ncu capture."""
+    kernel): work counted on the device during the profiling pass, over the live event
+    time of its launches with geometry (scope ibm_indicator; the stage starts' launches,
+    whose weights come from the memo, are timed as ibm_stage_start and reported beside);
+    FP32 pipe use from the flops per normal-foot evaluation of an ncu capture."""
     e = next((q for q in prof if q["name"] == "ibm_indicator"), None)
     if e is None or e["ms"] <= 0 or counts.get("normal_foot_evals", 0) <= 0:
         return None
@@ -603,6 +611,14 @@ def indicator_roofline(prof, counts, prof_steps):
            "box_cells_per_launch": cells / e["launches"], "normal_foot_evals_per_launch": evals / e["launches"],
            "box_cells_per_s": cells / sec, "normal_foot_evals_per_s": evals / sec,
            "share_of_step": e["ms"] / total}
+    st = next((q for q in prof if q["name"] == "ibm_stage_start"), None)
+    if st is not None and st["launches"] > 0:
+        out["stage_start"] = {"launches_per_step": st["launches"] / prof_steps,
+                              "us_per_launch": 1e3 * st["ms"] / st["launches"], "share_of_step": st["ms"] / total,
+                              "tasks_from_memo_per_step": counts.get("memo_tasks", 0) / prof_steps,
+                              "what": "the first evaluation of each RK stage: weights copied from the memo where "
+                                      "the particle's single-precision geometry is bitwise unchanged, computed "
+                                      "(and counted above) elsewhere"}
     fl = INDICATOR_FLOPS_PER_EVAL
     if fl is not None:
         achieved = evals / sec * fl[0] / 1e12

@@ -109,7 +109,7 @@ int build_joined(eif_batch *b, eif_batch::Graph &g, const std::vector<size_t> &i
   };
   for (int part = 0; part < 4; part++) {
     for (int k = 0; k < m; k++) {
-      if ((rc = eif::capture_step_part(cs[k], g.graph, kernel, part, &tails[k]))) {
+      if ((rc = eif::capture_step_part(cs[k], g.graph, kernel, part, &tails[k], true))) {
         restore();
         return batch_fail(b, rc, "suspension " + std::to_string(idx[k]) + ": " + eif_last_error(cs[k]));
       }

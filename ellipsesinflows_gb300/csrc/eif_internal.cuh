@@ -182,6 +182,7 @@ struct eif_ctx {
   bool weights_x_valid = false; // wcache holds the indicator weights of those boxes
   void *wcache = nullptr;       // indicator weight per IBM task slot (wcap entries)
   bool in_loop = false;                      // capturing the body of a sub-iteration loop
+  bool reset_in_stage_kernel = false;        // batch capture: the stage kernel resets the increments
   cudaGraphConditionalHandle loop_handle = 0;
   int ibm_ctas_per_sm[3] = {0, 0, 0};  // resident CTAs per SM of the IBM work kernels (FP64, mixed, mixed cached)
   unsigned *band_marks = nullptr;  // per band of 8 rows: bitmap over the 3*np (particle, image) boxes
@@ -252,7 +253,7 @@ int capture_step(eif_ctx *c, cudaGraph_t g, int *cur1, int *scur1);
 int step_capture_begin(eif_ctx *c);
 void step_capture_end(eif_ctx *c, int cur0, int scur0);
 int capture_step_part(eif_ctx *c, cudaGraph_t g, const std::vector<cudaGraphNode_t> &deps, int part,
-                      std::vector<cudaGraphNode_t> *sinks);
+                      std::vector<cudaGraphNode_t> *sinks, bool particles_in_stage_kernel = false);
 int capture_subiteration_loop(eif_ctx *c, cudaGraph_t g, const std::vector<cudaGraphNode_t> &deps, int rk,
                               std::vector<cudaGraphNode_t> *sinks);
 

@@ -84,9 +84,11 @@ void step_capture_end(eif_ctx *c, int cur0, int scur0) {
 // of the stage before (main.c:51-53) and the front of the next stage, part 3 the
 // particle update of stage 2. The sub-iteration loops (main.c:36-50) go between the
 // parts: a conditional node per context (capture_subiteration_loop), or one kernel for
-// all the suspensions of a batch.
+// all the suspensions of a batch, which then also updates the particles at the end of the
+// stage and resets the increments for the next (particles_in_stage_kernel: those launches
+// are left out of parts 1-3).
 int capture_step_part(eif_ctx *c, cudaGraph_t g, const std::vector<cudaGraphNode_t> &deps, int part,
-                      std::vector<cudaGraphNode_t> *sinks) {
+                      std::vector<cudaGraphNode_t> *sinks, bool particles_in_stage_kernel) {
   cudaError_t e = cudaStreamBeginCaptureToGraph(c->stream, g, deps.data(), nullptr, deps.size(),
                                                 cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return check_cuda(c, e, "cudaStreamBeginCaptureToGraph");
@@ -100,9 +102,14 @@ int capture_step_part(eif_ctx *c, cudaGraph_t g, const std::vector<cudaGraphNode
     c->boxes_x_valid = false;
     c->weights_x_valid = false;
     c->bands_x_valid = false;
-    if ((rc = launch_update_particles(c))) return rc;
+    if (!particles_in_stage_kernel && (rc = launch_update_particles(c))) return rc;
   }
-  if (part < 3 && (rc = rk_stage_front(c, part))) return rc;
+  if (part < 3) {
+    c->reset_in_stage_kernel = particles_in_stage_kernel && part > 0;
+    rc = rk_stage_front(c, part);
+    c->reset_in_stage_kernel = false;
+    if (rc) return rc;
+  }
   return end_capture(c, sinks);
 }
 

@@ -466,9 +466,12 @@ static int launch_work(eif_ctx *c, int mode, int cn) {
   if (mixed && mode == 0 && cn == 0 && w.wmode == 1 && c->memo_on) w.memo_mode = 1;
   {
     // launches that evaluate the indicator geometry are timed as ibm_indicator, those
-    // with stored weights (sums and field contributions only) as inertia or exchange
+    // with stored weights (sums and field contributions only) as inertia or exchange,
+    // the stage start's evaluation that takes its weights from the memo as
+    // ibm_stage_start
     const bool geometry = w.wmode != 2 && !(mixed && c->in_loop);
-    EIF_PROF(c, geometry ? "ibm_indicator" : (mode == 0 ? "ibm_inertia" : "ibm_exchange"),
+    EIF_PROF(c, w.memo_mode == 1 ? "ibm_stage_start" :
+                (geometry ? "ibm_indicator" : (mode == 0 ? "ibm_inertia" : "ibm_exchange")),
              mixed && c->in_loop ? 2 : 1);
     if (mixed && c->in_loop) {
       // first sub-iteration: cached weights; later ones: full evaluation (decided on the device)

@@ -404,4 +404,28 @@ __device__ __forceinline__ double increment_particle(double *p, int pcap, int n,
   return res;
 }
 
+// reset.c:7-18 for particle n: increments of the new stage start at zero
+__device__ __forceinline__ void reset_particle(double *P, int pcap, int n) {
+  P[EIF_P_DUX * pcap + n] = 0.; P[EIF_P_DUY * pcap + n] = 0.; P[EIF_P_DVZ * pcap + n] = 0.;
+  P[EIF_P_DX * pcap + n] = 0.; P[EIF_P_DY * pcap + n] = 0.; P[EIF_P_DAZ * pcap + n] = 0.;
+}
+
+// update.c:8-34 for particle n: velocities and positions advanced by the increments,
+// the centre wrapped into [0, ly] and the angle into [0, 2 pi]
+__device__ __forceinline__ void update_particle(double *P, int pcap, int n, double ly) {
+  P[EIF_P_UX * pcap + n] += P[EIF_P_DUX * pcap + n];
+  P[EIF_P_UY * pcap + n] += P[EIF_P_DUY * pcap + n];
+  P[EIF_P_VZ * pcap + n] += P[EIF_P_DVZ * pcap + n];
+  double x = P[EIF_P_X * pcap + n] + P[EIF_P_DX * pcap + n];
+  double y = P[EIF_P_Y * pcap + n] + P[EIF_P_DY * pcap + n];
+  double az = P[EIF_P_AZ * pcap + n] + P[EIF_P_DAZ * pcap + n];
+  if (y < 0.) y += ly;
+  if (y > ly) y -= ly;
+  if (az < 0.) az += 2. * M_PI;
+  if (az > 2. * M_PI) az -= 2. * M_PI;
+  P[EIF_P_X * pcap + n] = x;
+  P[EIF_P_Y * pcap + n] = y;
+  P[EIF_P_AZ * pcap + n] = az;
+}
+
 }  // namespace

@@ -28,9 +28,7 @@ __global__ void __launch_bounds__(PAIR_WARPS * 32) k_collision(double *__restric
 
 __global__ void k_reset(double *__restrict__ P, int pcap, int np) {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= np) return;
-  P[EIF_P_DUX * pcap + n] = 0.; P[EIF_P_DUY * pcap + n] = 0.; P[EIF_P_DVZ * pcap + n] = 0.;
-  P[EIF_P_DX * pcap + n] = 0.; P[EIF_P_DY * pcap + n] = 0.; P[EIF_P_DAZ * pcap + n] = 0.;
+  if (n < np) reset_particle(P, pcap, n);
 }
 
 // increment.c:10-72; residual = max |change of the increments|, combined over
@@ -78,20 +76,7 @@ __global__ void k_increment(double *__restrict__ P, int pcap, int np, double gam
 // update.c:8-34
 __global__ void k_update(double *__restrict__ P, int pcap, int np, double ly) {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= np) return;
-  P[EIF_P_UX * pcap + n] += P[EIF_P_DUX * pcap + n];
-  P[EIF_P_UY * pcap + n] += P[EIF_P_DUY * pcap + n];
-  P[EIF_P_VZ * pcap + n] += P[EIF_P_DVZ * pcap + n];
-  double x = P[EIF_P_X * pcap + n] + P[EIF_P_DX * pcap + n];
-  double y = P[EIF_P_Y * pcap + n] + P[EIF_P_DY * pcap + n];
-  double az = P[EIF_P_AZ * pcap + n] + P[EIF_P_DAZ * pcap + n];
-  if (y < 0.) y += ly;
-  if (y > ly) y -= ly;
-  if (az < 0.) az += 2. * M_PI;
-  if (az > 2. * M_PI) az -= 2. * M_PI;
-  P[EIF_P_X * pcap + n] = x;
-  P[EIF_P_Y * pcap + n] = y;
-  P[EIF_P_AZ * pcap + n] = az;
+  if (n < np) update_particle(P, pcap, n, ly);
 }
 
 }  // namespace
@@ -109,7 +94,8 @@ int launch_collision(eif_ctx *c, int cn) {
 
 int launch_reset_increments(eif_ctx *c) {
   c->incr_zero = true;
-  if (c->np == 0) return EIF_OK;
+  // in a batch graph the stage kernel before this front has reset the increments
+  if (c->np == 0 || c->reset_in_stage_kernel) return EIF_OK;
   EIF_PROF(c, "particle_reset", 1);
   k_reset<<<(c->np + 127) / 128, 128, 0, c->stream>>>(c->P, c->pcap, c->np);
   EIF_LAUNCH_CK(c);

@@ -23,6 +23,9 @@
 // stops takes no part in later sub-iterations. Every body is the one of the stand-alone
 // kernels (ibm_device.cuh, particle_device.cuh) with the same decomposition per task,
 // particle and block, so each suspension gets the same bits as in its own loop.
+// When no suspension iterates any more, the kernel updates every suspension's particles
+// (update.c) and, before stages 1 and 2, resets their increments (reset.c): the particle
+// launches around the loop, which the suspensions' own branches then leave out.
 //
 // The units of a phase are numbered suspension by suspension (fixed offsets from the
 // particle counts) and worker w (a CTA or a warp) takes units w, w + W, ... of that
@@ -62,6 +65,7 @@ struct SubDesc {
 struct StageArgs {
   const SubDesc *d;
   int n;
+  int reset_next;               // the particles' increments are reset for a following stage
   unsigned *sync;               // [0] arrivals, [1] error
   unsigned long long *res;      // two residual words per suspension (alternating sub-iterations)
 };
@@ -222,8 +226,22 @@ __global__ void __launch_bounds__(SUB_THREADS, 2) k_subiterations(StageArgs s) {
     for (int q = 0; q < SUB_MAX / 32; q++) any |= act[q] != 0u;
     if (!any) break;
   }
-  if (!ok && threadIdx.x == 0)
-    for (int j = 0; j < n; j++) atomicOr(s.d[j].flags, EIF_FLAG_TIMEOUT);
+  if (!ok) {
+    if (threadIdx.x == 0)
+      for (int j = 0; j < n; j++) atomicOr(s.d[j].flags, EIF_FLAG_TIMEOUT);
+    return;
+  }
+  // the particle update of the stage (update.c:8-34) and, before a following stage, the
+  // reset of the increments (reset.c:7-18); the last increments were written before the
+  // last grid barrier
+  for (int j = 0; j < n; j++) {
+    const SubDesc &d = s.d[j];
+    for (int m = first_unit(blockIdx.x * SUB_THREADS + threadIdx.x, d.u_part, G * SUB_THREADS); m < d.np;
+         m += G * SUB_THREADS) {
+      update_particle(d.P, d.pcap, m, d.ly);
+      if (s.reset_next) reset_particle(d.P, d.pcap, m);
+    }
+  }
 }
 
 }  // namespace
@@ -329,6 +347,7 @@ int subiter_add_stage(SubiterPlan *p, int rk, cudaGraph_t g, const std::vector<c
   a.n = p->n;
   a.sync = p->d_sync + SYNC_WORDS * rk;
   a.res = p->d_res + (size_t)2 * p->n * rk;
+  a.reset_next = rk < 2 ? 1 : 0;
   void *args[] = {&a};
   cudaKernelNodeParams k = {};
   k.func = reinterpret_cast<void *>(k_subiterations);
