@@ -50,12 +50,15 @@ __global__ void __launch_bounds__(TT_WARPS * 32) k_task_table_scan(const int *__
   task_table_block(box, cnt, off, tdesc, np, bd, cap, blockIdx.x);
 }
 
+// The double-precision body is the batch stage kernel's instantiation (ordinary loads):
+// one function, compiled alike in both translation units, gives both kernels the same
+// bits.
 __global__ void __launch_bounds__(256) k_ibm_work(WorkArgs a) {
   // per warp: body-frame offsets of its near cells, overwritten by their weights
   __shared__ double2 slot_buf[8][CHUNK];
   const int wmode = a.iter ? (*a.iter == 0u ? 2 : 0) : a.wmode;
-  ibm_work_tasks<true>(a, wmode, (blockIdx.x * blockDim.x + threadIdx.x) >> 5, (gridDim.x * blockDim.x) >> 5,
-                       slot_buf[threadIdx.x >> 5]);
+  ibm_work_tasks<false>(a, wmode, (blockIdx.x * blockDim.x + threadIdx.x) >> 5, (gridDim.x * blockDim.x) >> 5,
+                        slot_buf[threadIdx.x >> 5]);
 }
 
 __global__ void __launch_bounds__(256, 3) k_ibm_work_f(WorkArgs a) {

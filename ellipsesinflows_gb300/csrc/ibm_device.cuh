@@ -54,10 +54,69 @@ __device__ __forceinline__ Ell make_ell(double a, double b, double px, double py
   return e;
 }
 
-// ellipse.c:30-65 (x_, y_ in the body frame)
-__device__ __forceinline__ double normal_t(const Ell &e, double x_, double y_) {
+// ---------------------------------------------------------------------------
+// The normal-foot iteration of ellipse.c:30-65 in single precision (the mixed form's
+// indicator, and the start of the double-precision iteration below). The distance at
+// the foot is stationary in t, so an angle error dt changes it by O(a dt^2): stopping
+// once the step is below 1e-3 leaves distance errors near 1e-9 cells (checked against
+// fully converged iterations over the aspect ratios 1-3).
+constexpr float NORMAL_TOL_F = 1.e-3f;
+constexpr int NORMAL_MAX_F = 24;
+
+struct EllF {
+  float a, b, cz, sz, kex, key;
+};
+
+// The reference's iteration (ellipse.c:30-65) in single precision, on the first-quadrant
+// offsets (px, py) = (|x_|, |y_|); normal_t_f unfolds the angle. Its fixed point
+// is the normal foot whatever the accuracy of the intermediate sin/cos, square
+// roots and arcsine, so the loop uses the hardware approximations (__sincosf,
+// rsqrtf) and the Taylor polynomial x + x^3/6 + 3x^5/40 of asin (odd, increasing
+// and zero only at zero like asin, so the step keeps its sign and vanishes at the
+// foot); the distance at the converged angle is evaluated with the accurate
+// sincosf, and the distance is stationary in the angle.
+__device__ __forceinline__ float normal_t_f_q1(const EllF &e, float px, float py) {
+  float t = 0.78539816339744831f;
+  for (int n = 0; n < NORMAL_MAX_F; n++) {
+    float st, ct;
+    __sincosf(t, &st, &ct);
+    const float x = e.a * ct, y = e.b * st;
+    const float ex = e.kex * (ct * ct * ct), ey = e.key * (st * st * st);
+    const float rx = x - ex, ry = y - ey, qx = px - ex, qy = py - ey;
+    const float r2 = ry * ry + rx * rx, q2 = qy * qy + qx * qx;
+    const float arg = fminf(fmaxf((rx * qy - ry * qx) * rsqrtf(r2 * q2), -1.f), 1.f);
+    const float a2 = arg * arg;
+    const float dc = r2 * rsqrtf(r2) * (arg * fmaf(a2, fmaf(a2, 0.075f, 0.16666667f), 1.f));
+    // a^2 + b^2 - x^2 - y^2 written without cancellation
+    const float dt = dc * rsqrtf(e.a * e.a * (st * st) + e.b * e.b * (ct * ct));
+    t += dt;
+    t = fminf(1.5707963267948966f, t);
+    t = fmaxf(0.f, t);
+    if (fabsf(dt) < NORMAL_TOL_F) break;
+  }
+  return t;
+}
+__device__ __forceinline__ float normal_t_f(const EllF &e, float x_, float y_) {
+  float t = normal_t_f_q1(e, fabsf(x_), fabsf(y_));
+  if (x_ < 0.f) t = 3.14159265358979323846f - t;
+  if (y_ < 0.f) t = -t;
+  return t;
+}
+
+
+// ellipse.c:30-65 (x_, y_ in the body frame). The iteration, its stopping rule and its
+// cap are the reference's; it starts from the foot that the same iteration finds in
+// single precision (on the FP32 pipe, about 1e-4 or closer) instead of from pi/4. The
+// fixed point is the same, and the double-precision iterations (the expensive part on
+// this GPU's FP64 pipe) drop from about four to two: the first moves t by the start's
+// error, the second by its square, below the 1e-8 stop. Not inlined, like
+// ibm_work_tasks: compiled on its own it gives the same bits in every kernel.
+__device__ __noinline__ double normal_t(const Ell &e, double x_, double y_) {
   const double px = fabs(x_), py = fabs(y_);
-  double t = 0.25 * M_PI;
+  EllF ef;
+  ef.a = eifd::d2f(e.a); ef.b = eifd::d2f(e.b); ef.kex = eifd::d2f(e.kex); ef.key = eifd::d2f(e.key);
+  ef.cz = 0.f; ef.sz = 0.f;
+  double t = eifd::f2d(normal_t_f_q1(ef, eifd::d2f(px), eifd::d2f(py)));
   for (int n = 0;; n++) {
     double st, ct;
     sincos(t, &st, &ct);
@@ -568,49 +627,7 @@ __device__ __noinline__ void ibm_work_tasks(const WorkArgs &a, int wmode, int fi
 // centre are formed in grid units, (x - px)/dx = (i - i0) - g with the integer
 // i0 and the fraction g computed once per chunk in double precision, so the
 // per-cell arithmetic is single precision without cancellation. The normal
-// foot iteration is the reference's (ellipse.c:30-65) with a stopping threshold
-// suited to single precision.
-// The distance at the foot is stationary in t, so an angle error dt changes it by
-// O(a dt^2): stopping once the step is below 1e-3 leaves distance errors near 1e-9
-// cells (checked against fully converged iterations over the aspect ratios 1-3).
-constexpr float NORMAL_TOL_F = 1.e-3f;
-constexpr int NORMAL_MAX_F = 24;
-
-struct EllF {
-  float a, b, cz, sz, kex, key;
-};
-
-// The reference's iteration (ellipse.c:30-65) in single precision. Its fixed point
-// is the normal foot whatever the accuracy of the intermediate sin/cos, square
-// roots and arcsine, so the loop uses the hardware approximations (__sincosf,
-// rsqrtf) and the Taylor polynomial x + x^3/6 + 3x^5/40 of asin (odd, increasing
-// and zero only at zero like asin, so the step keeps its sign and vanishes at the
-// foot); the distance at the converged angle is evaluated with the accurate
-// sincosf, and the distance is stationary in the angle.
-__device__ __forceinline__ float normal_t_f(const EllF &e, float x_, float y_) {
-  const float px = fabsf(x_), py = fabsf(y_);
-  float t = 0.78539816339744831f;
-  for (int n = 0; n < NORMAL_MAX_F; n++) {
-    float st, ct;
-    __sincosf(t, &st, &ct);
-    const float x = e.a * ct, y = e.b * st;
-    const float ex = e.kex * (ct * ct * ct), ey = e.key * (st * st * st);
-    const float rx = x - ex, ry = y - ey, qx = px - ex, qy = py - ey;
-    const float r2 = ry * ry + rx * rx, q2 = qy * qy + qx * qx;
-    const float arg = fminf(fmaxf((rx * qy - ry * qx) * rsqrtf(r2 * q2), -1.f), 1.f);
-    const float a2 = arg * arg;
-    const float dc = r2 * rsqrtf(r2) * (arg * fmaf(a2, fmaf(a2, 0.075f, 0.16666667f), 1.f));
-    // a^2 + b^2 - x^2 - y^2 written without cancellation
-    const float dt = dc * rsqrtf(e.a * e.a * (st * st) + e.b * e.b * (ct * ct));
-    t += dt;
-    t = fminf(1.5707963267948966f, t);
-    t = fmaxf(0.f, t);
-    if (fabsf(dt) < NORMAL_TOL_F) break;
-  }
-  if (x_ < 0.f) t = 3.14159265358979323846f - t;
-  if (y_ < 0.f) t = -t;
-  return t;
-}
+// foot iteration is normal_t_f (above).
 
 // tanh(2 d / h) of the signed distance (positive inside), d from the body-frame
 // offset; tanh through one exponential, accurate to a few units of 1e-7 absolute
