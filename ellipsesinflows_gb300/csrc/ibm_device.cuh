@@ -456,6 +456,7 @@ __device__ __noinline__ void ibm_work_tasks(const WorkArgs &a, int wmode, int fi
   const double rh = 1. / a.h;
   const double dxdy = a.dx * a.dy;
   const double dtv = a.mode == 1 ? __ldg(a.dt) : 0.;
+  const double rdtv = a.mode == 1 ? 1. / dtv : 0.;
   const double md = FAR_CELLS_D * a.h;
   const int pc = a.pcap, ld = a.ld;
   double *wcache = static_cast<double *>(a.wcache);
@@ -477,8 +478,11 @@ __device__ __noinline__ void ibm_work_tasks(const WorkArgs &a, int wmode, int fi
       py = py + ldro<NC>(P + EIF_P_DY * pc + n);
       paz = paz + ldro<NC>(P + EIF_P_DAZ * pc + n);
     }
-    const double pm = pmass(pden, pa, pb);
-    const double pim = pmoi(pden, pa, pb);
+    // reciprocals of the mass and the moment of inertia, once per task: the per-cell
+    // divisions of inertia.c and exchange.c become multiplications (a division costs
+    // about ten FP64 operations; the results change by an ulp per term)
+    const double rpm = 1. / pmass(pden, pa, pb);
+    const double rpim = 1. / pmoi(pden, pa, pb);
     const double pux = ldro<NC>(P + EIF_P_UX * pc + n), puy = ldro<NC>(P + EIF_P_UY * pc + n),
                  pvz = ldro<NC>(P + EIF_P_VZ * pc + n);
     const Ell e = make_ell(pa, pb, px, py, paz);
@@ -591,21 +595,21 @@ __device__ __noinline__ void ibm_work_tasks(const WorkArgs &a, int wmode, int fi
           const double w = 0.5 * (1. + th);
           const double valx = w * 0.5 * (2. * uxf) * dxdy;
           const double valy = w * 0.5 * (2. * uyf) * dxdy;
-          s0 += valx / pm;
-          s1 += valy / pm;
-          s2 += (-(y - py_) * valx / pim) + ((x - px) * valy / pim);
+          s0 += valx * rpm;
+          s1 += valy * rpm;
+          s2 += (-(y - py_) * valx * rpim) + ((x - px) * valy * rpim);
         } else {
           // exchange.c:61-76
           const double w = 0.5 * BETA * (1. - th * th);
           const double uxp = pux - pvz * (y - py_);
           const double uyp = puy + pvz * (x - px);
-          const double fx = w * (uxp - uxf) / dtv;
-          const double fy = w * (uyp - uyf) / dtv;
+          const double fx = w * (uxp - uxf) * rdtv;
+          const double fy = w * (uyp - uyf) * rdtv;
           contrib = a.weights_only ? make_double2(w, w) : make_double2(fx * dtv, fy * dtv);
           const double Fx = fx * a.dx * a.dy, Fy = fy * a.dx * a.dy;
-          s0 += -(Fx / pm);
-          s1 += -(Fy / pm);
-          s2 += ((y - py_) * Fx / pim) - ((x - px) * Fy / pim);
+          s0 += -(Fx * rpm);
+          s1 += -(Fy * rpm);
+          s2 += ((y - py_) * Fx * rpim) - ((x - px) * Fy * rpim);
         }
       }
       if (a.mode == 1 && EIF_CHK(a.bd.rec, (long long)c * CHUNK + half * 32 + lane, a.bd.wbuf, 19))
@@ -791,7 +795,6 @@ __device__ __forceinline__ void ibm_work_f_tasks(const WorkArgs &a, int wmode, i
     float sacc0 = 0.f, sacc1 = 0.f, sacc2 = 0.f;
 #pragma unroll
     for (int half = 0; half < CHUNK / 32; half++) {
-      const int i = (task ? t.ib : 1) + half * 32 + lane;
       float2 contrib = make_float2(0.f, 0.f);
       // cells of weight exactly zero (inertia: far outside; exchange: any far cell) are skipped
       const float th_ = th2[half];
