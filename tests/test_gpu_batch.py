@@ -85,3 +85,20 @@ def test_batch_rebuilds_after_a_particle_count_change(gpu_lib):
         batch.advance(2)
     for a, b in zip(solo, together):
         assert_same(a, b)
+
+
+def test_batch_with_a_suspension_beyond_the_stage_kernel(gpu_lib):
+    """A suspension with more than 8192 ellipses keeps its own sub-iteration loops in its
+    graph branch, beside the stage kernels of the other suspensions: every suspension
+    still gets the bits of its separate run."""
+    big = cases.poiseuille(itot=512, jtot=1024, n=8300, a=0.005, b=0.003, seed=21)
+    specs = [(big, PREC_MIXED), (cases.couette_circle(), PREC_MIXED),
+             (cases.poiseuille(itot=128, jtot=256, n=8, a=0.05, b=0.025, seed=11), PREC_FP64)]
+    solo = [Simulation.from_case(c, precision=p) for c, p in specs]
+    together = [Simulation.from_case(c, precision=p) for c, p in specs]
+    for s in solo:
+        s.advance(2)
+    with Batch(together) as batch:
+        batch.advance(2)
+    for a, b in zip(solo, together):
+        assert_same(a, b)
