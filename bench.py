@@ -687,7 +687,8 @@ def roofline(prof, cells, hbm, hbm_src, precision, grid=None):
 
 
 def run_e2e(sim, case, steps, pg, device):
-    """Every step: host->device copy of the state, one step, device->host copy of the result."""
+    """Every step: host->device copy of the state, one step, device->host copy of the result
+    (eif_push_fluid, eif_push_particles, eif_advance_pull)."""
     import torch
     from ellipsesinflows_gb300.capi import NFIELDS
     ux, uy, p, _ = sim.pull_fluid()
@@ -704,9 +705,9 @@ def run_e2e(sim, case, steps, pg, device):
     for _ in range(steps):
         sim.push_fluid(hux, huy, hp)
         sim.push_particles(hpart)
-        sim.advance(1)
-        sim.pull_fluid(out=(hux, huy, hp, None))
-        sim.pull_particles(out=hpart)
+        # eif_advance_pull: the step, then its fields and records into the host arrays
+        # (the fields' copy overlaps the last stage's particle work)
+        sim.advance_pull(1, (hux, huy, hp), hpart)
     el = time.perf_counter() - t0
     el = max_over_ranks(pg, el, device)
     world = pg.get_world_size() if pg is not None else 1

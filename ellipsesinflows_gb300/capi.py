@@ -95,6 +95,7 @@ def bind(lib, prefix):
         "get_dt": [_vp, _dp],
         "integrate": [_vp, _ip],
         "advance": [_vp, ctypes.c_int],
+        "advance_pull": [_vp, ctypes.c_int, _dp, _dp, _dp, ctypes.c_int, _dp],
         "get_time": [_vp, _ip, _dp],
         "set_time": [_vp, ctypes.c_int, ctypes.c_double],
         "update_boundaries": [_vp],
@@ -308,6 +309,24 @@ class Solver:
 
     def advance(self, nsteps):
         self._call("advance", self.ctx, int(nsteps))
+
+    def advance_pull(self, nsteps, fluid, records=None):
+        """advance(nsteps), then the fields into fluid = (ux, uy, p) (C-contiguous float64
+        arrays of the haloed shapes, None entries skipped) and the particle records into
+        records ((n, NFIELDS) or None), filled in place (eif_advance_pull: the fields'
+        copy runs beside the last stage's particle work)."""
+        sx, sy = self.shapes()
+        for a, shape in zip(fluid, (sx, sy, sy)):
+            if a is not None and (a.shape != shape or a.dtype != np.float64 or not a.flags["C_CONTIGUOUS"]):
+                raise ValueError("output arrays must be C-contiguous float64 of shapes %s, %s" % (sx, sy))
+        n = 0
+        if records is not None:
+            if records.shape != (self.n_particles, NFIELDS) or records.dtype != np.float64 or \
+                    not records.flags["C_CONTIGUOUS"]:
+                raise ValueError("records must be C-contiguous float64 of shape (%d, %d)" % (self.n_particles, NFIELDS))
+            n = self.n_particles
+        rec = _ptr(records) if records is not None and n > 0 else None
+        self._call("advance_pull", self.ctx, int(nsteps), *[None if a is None else _ptr(a) for a in fluid], n, rec)
 
     def time_state(self):
         s, t = ctypes.c_int(), ctypes.c_double()

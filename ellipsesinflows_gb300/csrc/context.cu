@@ -209,14 +209,15 @@ int rows_in(eif_ctx *c, double *dst, const double *host, int w, int rows) {
   return EIF_OK;
 }
 
-int rows_out(eif_ctx *c, double *host, const double *src, int w, int rows) {
+int rows_out(eif_ctx *c, double *host, const double *src, int w, int rows, cudaStream_t stream = nullptr) {
+  if (!stream) stream = c->stream;
   if (double *hd = static_cast<double *>(mapped(host))) {
-    k_rows_out<<<c->sms * 4, 512, 0, c->stream>>>(src, hd, w, rows, c->ld);
+    k_rows_out<<<c->sms * 4, 512, 0, stream>>>(src, hd, w, rows, c->ld);
     EIF_LAUNCH_CK(c);
     return EIF_OK;
   }
   EIF_CK(c, cudaMemcpy2DAsync(host, sizeof(double) * w, src, sizeof(double) * c->ld, sizeof(double) * w, rows,
-                              cudaMemcpyDeviceToHost, c->stream));
+                              cudaMemcpyDeviceToHost, stream));
   return EIF_OK;
 }
 
@@ -414,6 +415,8 @@ int eif_create(const eif_config_t *cfg, eif_ctx **out) {
   CK_CREATE(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
   CK_CREATE(cudaEventCreateWithFlags(&c->ev_ibm, cudaEventDisableTiming));
   CK_CREATE(cudaEventCreateWithFlags(&c->ev_coll, cudaEventDisableTiming));
+  CK_CREATE(cudaEventCreateWithFlags(&c->ev_fields, cudaEventDisableTiming));
+  CK_CREATE(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
   host_metrics(c);
   int rc = device_metrics(c);
   if (rc) return rc;
@@ -493,6 +496,8 @@ int eif_destroy(eif_ctx *c) {
   if (c->ev_fork) cudaEventDestroy(c->ev_fork);
   if (c->ev_ibm) cudaEventDestroy(c->ev_ibm);
   if (c->ev_coll) cudaEventDestroy(c->ev_coll);
+  if (c->ev_fields) cudaEventDestroy(c->ev_fields);
+  if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   if (c->side) cudaStreamDestroy(c->side);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete[] c->h_xf; delete[] c->h_xc; delete[] c->h_dxf; delete[] c->h_dxc; delete[] c->h_yf; delete[] c->h_yc;
@@ -716,10 +721,18 @@ int eif_integrate(eif_ctx *c, int *substeps) {
   return sync_scalars(c);
 }
 
-int eif_advance(eif_ctx *c, int nsteps) {
+namespace {
+
+// host arrays that eif_advance_pull fills with the fields after the last step
+struct FieldTargets {
+  double *ux, *uy, *p;
+};
+
+int advance(eif_ctx *c, int nsteps, const FieldTargets *ft) {
   if (!c || nsteps < 0) return EIF_ERR_ARG;
   if (!c->fluid_pushed) return fail(c, EIF_ERR_STATE, "push the fluid state before integrating");
   if (int rc = tune_tiles(c)) return rc;
+  bool fields_queued = false;
   if (c->use_graphs && !c->sync_debug && !c->prof.enabled) {
     // one graph launch per step (see graph.cu), queued one step ahead: step s + 1 is
     // launched before the host waits for the copies of step s's dt, flags and bounds
@@ -760,6 +773,16 @@ int eif_advance(eif_ctx *c, int nsteps) {
         h.check[0] = 0ull;
       }
       EIF_CK(c, cudaEventRecord(c->ev_step[s & 1], c->stream));
+      if (ft && s == nsteps - 1) {
+        // the fields are final once the graph has recorded ev_fields (after the last
+        // stage's projection): their copy runs beside that stage's particle work
+        EIF_CK(c, cudaStreamWaitEvent(c->copy_stream, c->ev_fields, 0));
+        const int rows = c->jtot + 2;
+        if (ft->ux && (rc = rows_out(c, ft->ux, c->ux[c->cur], c->itot + 1, rows, c->copy_stream))) return rc;
+        if (ft->uy && (rc = rows_out(c, ft->uy, c->uy[c->cur], c->itot + 2, rows, c->copy_stream))) return rc;
+        if (ft->p && (rc = rows_out(c, ft->p, c->p, c->itot + 2, rows, c->copy_stream))) return rc;
+        fields_queued = true;
+      }
       if (s > 0 && (rc = finish(s - 1))) {
         if (cudaEventSynchronize(c->ev_step[s & 1]) == cudaSuccess) {
           c->step += 1;
@@ -770,19 +793,40 @@ int eif_advance(eif_ctx *c, int nsteps) {
     }
     if (nsteps > 0) {
       const int rc = finish(nsteps - 1);
-      if (rc) return rc;
+      if (rc) {
+        cudaStreamSynchronize(c->copy_stream);
+        return rc;
+      }
       EIF_CK(c, cudaStreamSynchronize(c->stream));
     }
-    return EIF_OK;
+    if (fields_queued) EIF_CK(c, cudaStreamSynchronize(c->copy_stream));
+  } else {
+    for (int s = 0; s < nsteps; s++) {
+      int rc = launch_decide_dt(c);
+      if (rc) return rc;
+      rc = eif_integrate(c, nullptr);
+      if (rc) return rc;
+      c->step += 1;
+      c->time += c->dt_host;
+    }
   }
-  for (int s = 0; s < nsteps; s++) {
-    int rc = launch_decide_dt(c);
+  if (ft && !fields_queued) {
+    const int rc = eif_pull_fluid(c, ft->ux, ft->uy, ft->p, nullptr);
     if (rc) return rc;
-    rc = eif_integrate(c, nullptr);
-    if (rc) return rc;
-    c->step += 1;
-    c->time += c->dt_host;
   }
+  return ft ? check_records(c) : EIF_OK;
+}
+
+}  // namespace
+
+int eif_advance(eif_ctx *c, int nsteps) { return advance(c, nsteps, nullptr); }
+
+int eif_advance_pull(eif_ctx *c, int nsteps, double *ux, double *uy, double *p, int n, double *records) {
+  if (!c || nsteps < 0 || (records && n != c->np)) return EIF_ERR_ARG;
+  const FieldTargets ft{ux, uy, p};
+  int rc = advance(c, nsteps, &ft);
+  if (rc) return rc;
+  if (records && (rc = eif_pull_particles(c, n, records))) return rc;
   return EIF_OK;
 }
 

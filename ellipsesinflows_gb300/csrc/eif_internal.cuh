@@ -109,6 +109,10 @@ struct eif_ctx {
   // launch functions use `stream`, which side_begin/side_end point at it
   cudaStream_t side = nullptr, main_stream = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_ibm = nullptr, ev_coll = nullptr;
+  // eif_advance_pull: the step graphs record ev_fields once the last RK stage's
+  // projection has written the fields; their copy to the host runs on copy_stream
+  cudaEvent_t ev_fields = nullptr;
+  cudaStream_t copy_stream = nullptr;
   bool bands_x_valid = false;   // band lists built for the current boxes at X
   // discrete adjoint (adjoint.cu): right-hand side that replaces the divergence in the
   // double-precision Poisson solve while set; the exchange writes the summed weights

@@ -110,6 +110,12 @@ int capture_step_part(eif_ctx *c, cudaGraph_t g, const std::vector<cudaGraphNode
     c->reset_in_stage_kernel = false;
     if (rc) return rc;
   }
+  if (part == 2 && !particles_in_stage_kernel && c->ev_fields) {
+    // the last stage's projection is done: the fields are final for this step
+    // (eif_advance_pull copies them to the host beside the particle work that follows)
+    const cudaError_t e = cudaEventRecordWithFlags(c->ev_fields, c->stream, cudaEventRecordExternal);
+    if (e != cudaSuccess) return check_cuda(c, e, "cudaEventRecordWithFlags (fields)");
+  }
   return end_capture(c, sinks);
 }
 

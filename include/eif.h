@@ -116,6 +116,14 @@ int eif_integrate(eif_ctx *ctx, int *substeps);
  * step counter and the time include the step that followed the failing one
  * (at most one), and the counters always match the device state. */
 int eif_advance(eif_ctx *ctx, int nsteps);
+/* eif_advance(nsteps), then the state after the last step copied into host arrays in
+ * the layouts of eif_pull_fluid and eif_pull_particles (any pointer may be NULL; n must
+ * be the particle count). With the step graphs the fields are final once the last RK
+ * stage's projection is done, so their copy to the host (page-locked arrays: one
+ * streaming pass over the interconnect) runs beside that stage's particle
+ * sub-iterations and update; the records follow when the step has ended. After an error
+ * the arrays' contents are unspecified. No counterpart in the reference. */
+int eif_advance_pull(eif_ctx *ctx, int nsteps, double *ux, double *uy, double *p, int n, double *records);
 /* step counter and simulated time accumulated by eif_advance */
 int eif_get_time(eif_ctx *ctx, int *step, double *time);
 int eif_set_time(eif_ctx *ctx, int step, double time);
