@@ -69,7 +69,7 @@ HBM_BYTES = {
 # unchanged (otherwise null, marked stale)
 # (the DCT entries are the mean of the two passes' launches)
 _KPROF = "profiles/kernels_suspension_2048x4096_mixed.md"
-_FLUID_SHA = "30d878c1627eb34f6fdf1fa97f7dae03d8c1f6e2"
+_FLUID_SHA = "52b69b617a3a686d26584b2389729d3f3b7affaa"
 _POISSON_SHA = "9d65ff262c0a9c373bdb119de223c6128e2de25e"
 NCU_TRAFFIC = {
     ("mixed", 2048, 4096): {

@@ -420,6 +420,31 @@ __device__ __forceinline__ double f2d(float x) {
   return __hiloint2double((int)hi, (int)lo);
 }
 
+// f2d(hi) + f2d(lo) rounded to double, the value of that FP64 addition, with integer
+// operations where the exact sum lies in the binade of hi: then |lo| is a whole number
+// d of double ulps at hi's exponent (lo's exponent at most 29 below hi's), the sum is
+// exact, and its bit pattern is hi's plus or minus d. The other cases (and zeros,
+// subnormals, infinities) take the FP64 addition.
+__device__ __forceinline__ double pair_to_double(float hi, float lo) {
+  const double h = f2d(hi);
+  const unsigned hb = __float_as_uint(hi), lb = __float_as_uint(lo);
+  const unsigned eh = (hb >> 23) & 0xffu, el = (lb >> 23) & 0xffu;
+  const bool hi_normal = eh != 0u && eh != 255u;
+  if (hi_normal && el == 0u) return h;   // f2d(lo) is a signed zero
+  const int k = (int)eh - (int)el;
+  if (hi_normal && el != 255u && k >= 0 && k <= 29) {
+    const unsigned long long d = (unsigned long long)((lb & 0x007fffffu) | 0x00800000u) << (29 - k);
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(h);
+    const unsigned long long m = bits & 0x000fffffffffffffull;
+    if (((hb ^ lb) >> 31) == 0u) {
+      if (m + d < (1ull << 52)) return __longlong_as_double((long long)(bits + d));
+    } else if (m >= d) {
+      return __longlong_as_double((long long)(bits - d));
+    }
+  }
+  return h + f2d(lo);
+}
+
 // a double as an unevaluated sum hi + lo of two floats, split with integer
 // operations only: hi keeps the leading 24 significant bits (truncated), lo is
 // the remaining 29 bits rounded to a float, so hi + lo carries about 48 bits.

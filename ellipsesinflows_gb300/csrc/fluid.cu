@@ -569,7 +569,9 @@ __global__ void __launch_bounds__(TX *TY) k_correct_df(CorrArgsDF a) {
     if (j == jtot) a.uy[cy - jtot * ld] = v;
   }
   if (a.with_pressure) {
-    const double pv = p_old + (a.psi1 ? eifd::f2d(q0.hi) + eifd::f2d(q0.lo) : psi0);
+    // psi1 + psi2 as a double without the FP64 pipe (bit-identical to the FP64 addition;
+    // the pipe is the kernel's bound)
+    const double pv = p_old + (a.psi1 ? eifd::pair_to_double(q0.hi, q0.lo) : psi0);
     a.p[cy] = pv;
     if (j == 1) a.p[cy + jtot * ld] = pv;
     if (j == jtot) a.p[cy - jtot * ld] = pv;
@@ -1122,6 +1124,15 @@ __global__ void k_selftest_cvt(int n, unsigned long long *counts) {
     if (mag >= 0x00800000u && mag < 0x7f800000u) {
       if (__double_as_longlong(eifd::f2d(xf)) != __double_as_longlong((double)xf)) bad_f2d++;
     }
+    // float pairs -> double (eifd::pair_to_double against the FP64 addition it stands
+    // for): lo of every size below hi, of either sign, and zero
+    const unsigned long long r2 = mix64(r);
+    const float lo = (r2 & 0xffull) == 0ull ? 0.f
+                   : xf * __uint_as_float((unsigned)(127 - (int)((r2 >> 8) % 48ull)) << 23) *
+                         ((float)((r2 >> 16) & 0xffffffull) * (1.f / 16777216.f)) * ((r2 >> 63) ? -1.f : 1.f);
+    const double want = eifd::f2d(xf) + eifd::f2d(lo);
+    const double got = eifd::pair_to_double(xf, lo);
+    if (__double_as_longlong(want) != __double_as_longlong(got) && !(want != want && got != got)) bad_f2d++;
   }
   atomicAdd(counts, bad_d2f);
   atomicAdd(counts + 1, bad_f2d);

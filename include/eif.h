@@ -273,7 +273,8 @@ int eif_decide_dt_noalloc(const double *ux, int ux_pitch, const double *uy, int 
  * Converts n values spread over the normal range (plus zeros and the range
  * limits) with both the library's conversions and the hardware ones and
  * returns how many results differ by more than the rounding of a tie (d2f) or
- * at all (f2d). */
+ * at all (f2d; the count includes the float pairs whose integer conversion to
+ * double differs from the FP64 sum of the two parts). */
 int eif_selftest_conversions(int device, int n, long long *d2f_mismatch, long long *f2d_mismatch);
 
 /* ---- diagnostics: the reductions of the reference's logging (src/logging.c:40-172),
