@@ -116,80 +116,120 @@ __device__ __forceinline__ int first_unit(int w, int base, int W) {
   return r < 0 ? r + W : r;
 }
 
+// per suspension, in shared memory: the loop control of the phases, so that a worker
+// walks the suspensions without loading their descriptors
+enum { ST_NP, ST_UBOX, ST_UCOLL, ST_UTAB, ST_UPART, ST_MIXED, ST_TASKS, ST_WORDS = 8 };
+
 __global__ void __launch_bounds__(SUB_THREADS, 2) k_subiterations(StageArgs s) {
   __shared__ unsigned act[SUB_MAX / 32];   // suspensions still iterating
   __shared__ float2 slot_f[SUB_WARPS][CHUNK];
   __shared__ double2 slot_d[SUB_WARPS][CHUNK];
+  extern __shared__ int stab[];            // ST_WORDS per suspension
   const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
-  const int G = gridDim.x, W = G * SUB_WARPS;
-  const int wid = blockIdx.x * SUB_WARPS + wl;
+  const int G = gridDim.x, W = G * SUB_WARPS, T = G * SUB_THREADS;
+  const int wid = blockIdx.x * SUB_WARPS + wl, tid = blockIdx.x * SUB_THREADS + threadIdx.x;
   const int n = s.n;
   for (int q = threadIdx.x; q < SUB_MAX / 32; q += SUB_THREADS) {
     const int lo = 32 * q;
     act[q] = lo >= n ? 0u : (n - lo >= 32 ? 0xffffffffu : ((1u << (n - lo)) - 1u));
   }
+  for (int j = threadIdx.x; j < n; j += SUB_THREADS) {
+    const SubDesc &d = s.d[j];
+    int *e = stab + ST_WORDS * j;
+    e[ST_NP] = d.np;
+    e[ST_UBOX] = d.u_box;
+    e[ST_UCOLL] = d.u_coll;
+    e[ST_UTAB] = d.u_tab;
+    e[ST_UPART] = d.u_part;
+    e[ST_MIXED] = d.mixed;
+    e[ST_TASKS] = 0;
+  }
   if (blockIdx.x == 0)
     for (int j = threadIdx.x; j < 2 * n; j += SUB_THREADS) s.res[j] = 0ull;
   __syncthreads();
+  auto active = [&](int j) { return ((act[j >> 5] >> (j & 31)) & 1u) != 0u; };
   unsigned bar = 0;
   bool ok = true;
   for (unsigned it = 0; it < SUB_CAP; it++) {
     // 1. collision forces; boxes after the first sub-iteration
     for (int j = 0; j < n; j++) {
-      if (!((act[j >> 5] >> (j & 31)) & 1u)) continue;
+      if (!active(j)) continue;
+      const int *e = stab + ST_WORDS * j;
+      const int units = (e[ST_NP] + PAIR_WARPS - 1) / PAIR_WARPS;
+      int b = first_unit(blockIdx.x, e[ST_UCOLL], G);
+      if (b >= units) continue;
       const SubDesc &d = s.d[j];
-      const int units = (d.np + PAIR_WARPS - 1) / PAIR_WARPS;
-      for (int b = first_unit(blockIdx.x, d.u_coll, G); b < units; b += G) {
+      for (; b < units; b += G) {
         collision_block(d.P, d.pcap, d.np, 1, d.ly, d.lx, d.flags, b);
         __syncthreads();
       }
     }
     if (it > 0) {
       for (int j = 0; j < n; j++) {
-        if (!((act[j >> 5] >> (j & 31)) & 1u)) continue;
+        if (!active(j)) continue;
+        const int *e = stab + ST_WORDS * j;
+        const int groups = (e[ST_NP] + 31) / 32;
+        const int units = groups * (e[ST_MIXED] ? BOX_PARTS : 3);
+        int u = first_unit(wid, e[ST_UBOX], W);
+        if (u >= units) continue;
         const SubDesc &d = s.d[j];
-        const int groups = (d.np + 31) / 32;
-        const int units = groups * (d.mixed ? BOX_PARTS : 3);
-        for (int u = first_unit(wid, d.u_box, W); u < units; u += W) box_part(d.box, (u % groups) * 32 + lane, u / groups);
+        for (; u < units; u += W) box_part(d.box, (u % groups) * 32 + lane, u / groups);
       }
       if (!(ok = grid_barrier(s.sync, bar++))) break;
       // 2. task tables
       for (int j = 0; j < n; j++) {
-        if (!((act[j >> 5] >> (j & 31)) & 1u)) continue;
+        if (!active(j)) continue;
+        const int *e = stab + ST_WORDS * j;
+        const int units = (e[ST_NP] + TT_WARPS - 1) / TT_WARPS;
+        int b = first_unit(blockIdx.x, e[ST_UTAB], G);
+        if (b >= units) continue;
         const SubDesc &d = s.d[j];
-        const int units = (d.np + TT_WARPS - 1) / TT_WARPS;
-        for (int b = first_unit(blockIdx.x, d.u_tab, G); b < units; b += G) {
+        for (; b < units; b += G) {
           task_table_block(d.box.box, d.cnt, d.off, d.tdesc, d.np, d.box.bd, d.tcap, b);
           __syncthreads();
         }
       }
     }
     if (!(ok = grid_barrier(s.sync, bar++))) break;
-    // 3. row tasks of the inertia integrals; task counts zeroed for the next boxes
+    // 3. row tasks of the inertia integrals; task counts zeroed for the next boxes. The
+    // task totals of phase 2 are read into shared memory first, one load per suspension.
+    for (int j = threadIdx.x; j < n; j += SUB_THREADS) {
+      int *e = stab + ST_WORDS * j;
+      e[ST_TASKS] = active(j) && e[ST_NP] > 0 ? s.d[j].off[e[ST_NP]] : 0;
+    }
+    __syncthreads();
     int base = 0;
     for (int j = 0; j < n; j++) {
-      if (!((act[j >> 5] >> (j & 31)) & 1u)) continue;
-      const SubDesc &d = s.d[j];
-      if (d.np == 0) continue;
-      const int total = d.off[d.np];
+      if (!active(j)) continue;
+      const int *e = stab + ST_WORDS * j;
+      const int np = e[ST_NP], total = e[ST_TASKS];
+      if (np == 0) continue;
       const int first = first_unit(wid, base, W);
-      if (d.mixed) {
-        if (it == 0) ibm_sum_f_tasks<false>(d.work, first, W);
-        else ibm_work_f_tasks<false>(d.work, 0, first, W, slot_f[wl]);
-      } else {
-        ibm_work_tasks<false>(d.work, it == 0 ? 2 : 0, first, W, slot_d[wl]);
-      }
       base += total;
-      for (int q = blockIdx.x * SUB_THREADS + threadIdx.x; q < d.np; q += G * SUB_THREADS) d.cnt[q] = 0;
+      const bool zero_cnt = blockIdx.x * SUB_THREADS < np;
+      if (first >= total && !zero_cnt) continue;
+      const SubDesc &d = s.d[j];
+      if (first < total) {
+        if (e[ST_MIXED]) {
+          if (it == 0) ibm_sum_f_tasks<false>(d.work, first, W);
+          else ibm_work_f_tasks<false>(d.work, 0, first, W, slot_f[wl]);
+        } else {
+          ibm_work_tasks<false>(d.work, it == 0 ? 2 : 0, first, W, slot_d[wl]);
+        }
+      }
+      for (int q = tid; q < np; q += T) d.cnt[q] = 0;
     }
     if (!(ok = grid_barrier(s.sync, bar++))) break;
     // 4. sums over the tasks, increments, residuals
     for (int j = 0; j < n; j++) {
-      if (!((act[j >> 5] >> (j & 31)) & 1u)) continue;
+      if (!active(j)) continue;
+      const int *e = stab + ST_WORDS * j;
+      int m = first_unit(wid, e[ST_UPART], W);
+      if (m >= e[ST_NP]) continue;
       const SubDesc &d = s.d[j];
       const double dt = d.scal[0];
       unsigned long long *res = s.res + 2 * j + (it & 1u);
-      for (int m = first_unit(wid, d.u_part, W); m < d.np; m += W) {
+      for (; m < d.np; m += W) {
         if (d.mixed) {
           // after a sub-iteration with the indicator geometry: its weights are in the memo
           chunk_reduce_f_warp(reinterpret_cast<const float *>(d.work.partial), d.off, d.P, d.pcap, d.np,
@@ -208,7 +248,7 @@ __global__ void __launch_bounds__(SUB_THREADS, 2) k_subiterations(StageArgs s) {
     if (!(ok = grid_barrier(s.sync, bar++))) break;
     // the stopping rule of every suspension, evaluated alike by all CTAs
     for (int j = threadIdx.x; j < n; j += SUB_THREADS) {
-      if (!((act[j >> 5] >> (j & 31)) & 1u)) continue;
+      if (!active(j)) continue;
       const double r = __longlong_as_double(
           (long long)*reinterpret_cast<volatile unsigned long long *>(s.res + 2 * j + (it & 1u)));
       const unsigned count = it + 1u;
@@ -235,9 +275,11 @@ __global__ void __launch_bounds__(SUB_THREADS, 2) k_subiterations(StageArgs s) {
   // reset of the increments (reset.c:7-18); the last increments were written before the
   // last grid barrier
   for (int j = 0; j < n; j++) {
+    const int *e = stab + ST_WORDS * j;
+    int m = first_unit(tid, e[ST_UPART], T);
+    if (m >= e[ST_NP]) continue;
     const SubDesc &d = s.d[j];
-    for (int m = first_unit(blockIdx.x * SUB_THREADS + threadIdx.x, d.u_part, G * SUB_THREADS); m < d.np;
-         m += G * SUB_THREADS) {
+    for (; m < d.np; m += T) {
       update_particle(d.P, d.pcap, m, d.ly);
       if (s.reset_next) reset_particle(d.P, d.pcap, m);
     }
@@ -284,7 +326,11 @@ int subiter_plan_create(eif_ctx *const *ctx, int n, SubiterPlan **out, std::stri
     *err = "the device has no cooperative launch";
     return EIF_ERR_CUDA;
   }
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_subiterations, SUB_THREADS, 0);
+  // the loop-control table in dynamic shared memory: ST_WORDS ints per suspension
+  e = cudaFuncSetAttribute(k_subiterations, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)(sizeof(int) * ST_WORDS * SUB_MAX));
+  if (e != cudaSuccess) return plan_fail(err, "cudaFuncSetAttribute", e);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_subiterations, SUB_THREADS, sizeof(int) * ST_WORDS * n);
   if (e != cudaSuccess) return plan_fail(err, "cudaOccupancyMaxActiveBlocksPerMultiprocessor", e);
   if (occ < 1) {
     *err = "the stage kernel does not fit on an SM";
@@ -353,7 +399,7 @@ int subiter_add_stage(SubiterPlan *p, int rk, cudaGraph_t g, const std::vector<c
   k.func = reinterpret_cast<void *>(k_subiterations);
   k.gridDim = dim3(p->grid);
   k.blockDim = dim3(SUB_THREADS);
-  k.sharedMemBytes = 0;
+  k.sharedMemBytes = (unsigned)(sizeof(int) * ST_WORDS * p->n);
   k.kernelParams = args;
   cudaError_t e = cudaGraphAddKernelNode(node, g, deps.data(), deps.size(), &k);
   if (e != cudaSuccess) return plan_fail(err, "cudaGraphAddKernelNode", e);
