@@ -14,9 +14,11 @@
 //
 // Loads through the read-only data path (__ldg) are only valid for data that no
 // thread writes while the kernel runs. The bodies take a template flag NC: true in
-// the stand-alone kernels, false in the persistent sub-iteration kernel, whose
-// phases write the particle records, boxes, task table and parameters that later
-// phases read; there those loads are ordinary (coherent after the grid barrier).
+// the stand-alone single-precision kernels, false in the persistent sub-iteration
+// kernel, whose phases write the particle records, boxes, task table and parameters
+// that later phases read (there those loads are ordinary, coherent after the grid
+// barrier), and false in both for the double-precision task body, so that both run
+// one instantiation of it.
 #pragma once
 #include "eif_internal.cuh"
 #include <cfloat>
