@@ -1284,7 +1284,9 @@ struct Dct2ArgsF {
 
 // right-hand side (or the residual of the first solution) + single-precision DCT-II
 // of rows; one row of m = itot/2 complex values per T = m/8 threads
-__global__ void __launch_bounds__(FFT_CTA) k_dct2_f(Dct2ArgsF a, FftShape sh) {
+// capped at 32 registers (64 bytes spilled) for 16 resident CTAs per SM: measured faster
+// than 40 registers and 12 CTAs
+__global__ void __launch_bounds__(FFT_CTA, 16) k_dct2_f(Dct2ArgsF a, FftShape sh) {
   extern __shared__ float4 sm4[];
   const int n = a.itot, m = n / 2, ld = a.ld;
   const int T = sh.T;
@@ -1395,7 +1397,9 @@ struct Dct3ArgsF {
 };
 
 // block reconstruction + single-precision DCT-III + scaling of rows (compute_potential.c:120-134)
-__global__ void __launch_bounds__(FFT_CTA) k_dct3_f(Dct3ArgsF a, FftShape sh) {
+// capped at 48 registers for 10 resident CTAs per SM: measured faster than 53 registers
+// and 9 CTAs
+__global__ void __launch_bounds__(FFT_CTA, 10) k_dct3_f(Dct3ArgsF a, FftShape sh) {
   extern __shared__ float4 sm4[];
   const int n = a.itot, m = n / 2, ld = a.ld;
   const int T = sh.T;
