@@ -449,11 +449,11 @@ class Solver:
 
     def tiles(self):
         """tile shapes chosen by the tuner: {"predictor_rows", "projection_rows",
-        "thomas_threads", "tuned", "predictor_tensor_copies"}"""
+        "thomas_threads", "tuned", "predictor_tensor_copies", "predictor_uniform_x"}"""
         t = (ctypes.c_int * 4)()
         self._call("tiles", self.ctx, t)
         return {"predictor_rows": t[0], "projection_rows": t[1], "thomas_threads": t[2], "tuned": bool(t[3] & 1),
-                "predictor_tensor_copies": bool(t[3] & 2)}
+                "predictor_tensor_copies": bool(t[3] & 2), "predictor_uniform_x": bool(t[3] & 4)}
 
     # ---- discrete adjoint (double-precision form) ----
     def adjoint_begin(self, max_steps, mode=ADJOINT_COUPLED):

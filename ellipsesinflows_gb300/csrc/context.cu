@@ -303,6 +303,26 @@ int device_metrics(eif_ctx *c) {
   if ((rc = upload_f(&c->cxp_f, cxp))) return rc;
   if ((rc = upload_f(&c->cym_f, cym))) return rc;
   if ((rc = upload_f(&c->cyp_f, cyp))) return rc;
+  {
+    // the mixed predictor's x metrics as floats are one value each away from the walls:
+    // rdxf(1..itot), rdxc(2..itot), cxm and cxp (2..itot), cym (2..itot), cyp (1..itot-1);
+    // only rdxc(1), cym(1) (cell 1) and rdxc(itot+1), cyp(itot) (cell itot) see the half
+    // cells at the walls. Checked bitwise, so that the arguments give the loads' values.
+    eif_ctx::UniformX u;
+    u.rdxf = (float)rdxf[1];
+    u.rdxc = (float)rdxc[2];
+    u.cx = (float)cxm[2];
+    u.cy = (float)cym[2];
+    bool ok = itot >= 3 && !std::getenv("EIF_NO_UNIFORM_X");
+    for (int i = 1; ok && i <= itot; i++) {
+      ok = (float)rdxf[i] == u.rdxf;
+      if (ok && i >= 2) ok = (float)rdxc[i] == u.rdxc && (float)cxm[i] == u.cx && (float)cxp[i] == u.cx &&
+                             (float)cym[i] == u.cy;
+      if (ok && i <= itot - 1) ok = (float)cyp[i] == u.cy;
+    }
+    u.on = ok;
+    c->uni_x = u;
+  }
   if ((rc = upload(c, &c->xc, xc))) return rc;
   if ((rc = upload(c, &c->yc, yc))) return rc;
   if ((rc = upload(c, &c->rdxf, rdxf))) return rc;

@@ -138,6 +138,12 @@ struct eif_ctx {
   double *dxc;                  // DXC(i) at [i]
   double *dxf = nullptr;        // DXF(i) at [i]
   float *rdxf_f, *rdxc_f, *cxm_f, *cxp_f, *cym_f, *cyp_f;  // single-precision copies
+  // the single-precision x metrics when they are uniform in the interior (the mixed
+  // predictor then takes them as arguments and loads only at the wall columns)
+  struct UniformX {
+    bool on = false;
+    float rdxf = 0.f, rdxc = 0.f, cx = 0.f, cy = 0.f;
+  } uni_x;
   float2 *rdxc_df = nullptr;    // 1/dxc as double-float pairs (hi, lo)
   float *sxf[2], *syf[2];       // RK explicit terms of the mixed form
   // host copies of the metrics

@@ -165,6 +165,9 @@ struct PredArgsF {
   const float *rdxf, *rdxc, *cxm, *cxp, *cym, *cyp;
   const float *coef;   // alpha dt, beta dt, gamma dt of this stage
   float rRe, rdy, ext;
+  // uniform x metrics (kernels with UNI set): rdxf, rdxc, cxm = cxp, cym = cyp away
+  // from the wall cells, bitwise the values of the arrays
+  float u_rdxf, u_rdxc, u_cx, u_cy;
   int itot, jtot, ld;
 };
 
@@ -173,8 +176,10 @@ __device__ __forceinline__ float val(float2 a) { return a.x + a.y; }
 
 // the update of cell (i, j) of the mixed predictor from the staged float-pair tiles (the
 // cell at tile position (x, y)); u_own, v_own are the cell's old velocities in double,
-// Bx, By its old explicit terms
-template <int PY, int PX>
+// Bx, By its old explicit terms. UNI: the x metrics are the uniform arguments except at
+// the wall cells i = 1 (rdxc(1), cym(1)) and i = itot (rdxc(itot + 1), cyp(itot)), which
+// are loaded; the values, and so the results, are those of the arrays.
+template <int PY, int PX, bool UNI = false>
 __device__ __forceinline__ void pred_mixed_cell(const PredArgsF &a, const float2 (&tux)[PY][PX],
                                                 const float2 (&tuy)[PY][PX], const float2 (&tp)[PY][PX], int i, int j,
                                                 int x, int y, double u_own, double v_own, float Bx, float By) {
@@ -183,9 +188,10 @@ __device__ __forceinline__ void pred_mixed_cell(const PredArgsF &a, const float2
   const float rdy = a.rdy;
   if (i >= 2) {
     const float2 u0 = tux[y][x], uw = tux[y][x - 1], ue = tux[y][x + 1], us = tux[y - 1][x], un = tux[y + 1][x];
-    const float cxm = __ldg(a.cxm + i), cxp = __ldg(a.cxp + i);
-    const float duxdx_xm = dif(u0, uw) * __ldg(a.rdxf + i - 1);
-    const float duxdx_xp = dif(ue, u0) * __ldg(a.rdxf + i);
+    const float cxm = UNI ? a.u_cx : __ldg(a.cxm + i), cxp = UNI ? a.u_cx : __ldg(a.cxp + i);
+    const float rdxf_m = UNI ? a.u_rdxf : __ldg(a.rdxf + i - 1), rdxf_p = UNI ? a.u_rdxf : __ldg(a.rdxf + i);
+    const float duxdx_xm = dif(u0, uw) * rdxf_m;
+    const float duxdx_xp = dif(ue, u0) * rdxf_p;
     const float duxdy_ym = dif(u0, us) * rdy;
     const float duxdy_yp = dif(un, u0) * rdy;
     const float ux_xm = 0.5f * (val(uw) + val(u0));
@@ -194,8 +200,8 @@ __device__ __forceinline__ void pred_mixed_cell(const PredArgsF &a, const float2
     const float uy_ym = cxm * val(tuy[y][x - 1]) + cxp * val(tuy[y][x]);
     const float uy_yp = cxm * val(tuy[y + 1][x - 1]) + cxp * val(tuy[y + 1][x]);
     const float adv2 = -0.5f * uy_ym * duxdy_ym - 0.5f * uy_yp * duxdy_yp;
-    const float rdxc = __ldg(a.rdxc + i);
-    const float dif_ = a.rRe * ((dif(ue, u0) * __ldg(a.rdxf + i) - dif(u0, uw) * __ldg(a.rdxf + i - 1)) * rdxc +
+    const float rdxc = UNI ? a.u_rdxc : __ldg(a.rdxc + i);
+    const float dif_ = a.rRe * ((dif(ue, u0) * rdxf_p - dif(u0, uw) * rdxf_m) * rdxc +
                                 (dif(un, u0) - dif(u0, us)) * rdy * rdy);
     const float pre = -dif(tp[y][x], tp[y][x - 1]) * rdxc;
     const float A = (adv1 + adv2) + dif_;
@@ -208,19 +214,22 @@ __device__ __forceinline__ void pred_mixed_cell(const PredArgsF &a, const float2
   }
   {
     const float2 v0 = tuy[y][x], vw = tuy[y][x - 1], ve = tuy[y][x + 1], vs = tuy[y - 1][x], vn = tuy[y + 1][x];
-    const float rdxc_m = __ldg(a.rdxc + i), rdxc_p = __ldg(a.rdxc + i + 1);
+    const bool wall_w = !UNI || i == 1, wall_e = !UNI || i == a.itot;
+    const float rdxc_m = wall_w ? __ldg(a.rdxc + i) : a.u_rdxc;
+    const float rdxc_p = wall_e ? __ldg(a.rdxc + i + 1) : a.u_rdxc;
     const float duydx_xm = dif(v0, vw) * rdxc_m;
     const float duydx_xp = dif(ve, v0) * rdxc_p;
     const float duydy_ym = dif(v0, vs) * rdy;
     const float duydy_yp = dif(vn, v0) * rdy;
-    const float cym = __ldg(a.cym + i), cyp = __ldg(a.cyp + i);
+    const float cym = wall_w ? __ldg(a.cym + i) : a.u_cy, cyp = wall_e ? __ldg(a.cyp + i) : a.u_cy;
     const float ux_xm = 0.5f * (val(tux[y - 1][x]) + val(tux[y][x]));
     const float ux_xp = 0.5f * (val(tux[y - 1][x + 1]) + val(tux[y][x + 1]));
     const float adv1 = -cym * ux_xm * duydx_xm - cyp * ux_xp * duydx_xp;
     const float uy_ym = 0.5f * (val(vs) + val(v0));
     const float uy_yp = 0.5f * (val(v0) + val(vn));
     const float adv2 = -0.5f * uy_ym * duydy_ym - 0.5f * uy_yp * duydy_yp;
-    const float dif_ = a.rRe * ((duydx_xp - duydx_xm) * __ldg(a.rdxf + i) + (duydy_yp - duydy_ym) * rdy);
+    const float dif_ = a.rRe * ((duydx_xp - duydx_xm) * (UNI ? a.u_rdxf : __ldg(a.rdxf + i)) +
+                                (duydy_yp - duydy_ym) * rdy);
     const float pre = -dif(tp[y][x], tp[y - 1][x]) * rdy;
     const float A = (adv1 + adv2) + dif_ + a.ext;
     const int c = j * ld + i;
@@ -232,7 +241,7 @@ __device__ __forceinline__ void pred_mixed_cell(const PredArgsF &a, const float2
   }
 }
 
-template <int TY>
+template <int TY, bool UNI>
 __global__ void __launch_bounds__(TX *TY) k_predictor_mixed(PredArgsF a) {
   constexpr int PX = TX + 2, PY = TY + 2;
   __shared__ float2 tux[PY][PX], tuy[PY][PX], tp[PY][PX];
@@ -286,7 +295,7 @@ __global__ void __launch_bounds__(TX *TY) k_predictor_mixed(PredArgsF a) {
   }
   __syncthreads();
   if (!live) return;
-  pred_mixed_cell(a, tux, tuy, tp, i, j, threadIdx.x + 1, threadIdx.y + 1, u_own, v_own, Bx, By);
+  pred_mixed_cell<PY, PX, UNI>(a, tux, tuy, tp, i, j, threadIdx.x + 1, threadIdx.y + 1, u_own, v_own, Bx, By);
 }
 
 // ---------------------------------------------------------------------------
@@ -944,6 +953,7 @@ static int launch_predictor_mixed(eif_ctx *c, int rk) {
   a.rRe = (float)(1. / c->cfg.Re);
   a.rdy = (float)(1. / c->dy);
   a.ext = (float)c->cfg.extfrcy;
+  a.u_rdxf = c->uni_x.rdxf; a.u_rdxc = c->uni_x.rdxc; a.u_cx = c->uni_x.cx; a.u_cy = c->uni_x.cy;
   a.itot = c->itot; a.jtot = c->jtot; a.ld = c->ld;
   EIF_PROF(c, "predictor", 1);
   const int ty = c->tiles.pred;
@@ -954,7 +964,10 @@ static int launch_predictor_mixed(eif_ctx *c, int rk) {
     else if (ty == 16) done = launch_predictor_tma<16>(c, a, c->pred_tma_ctas[2]);
     else done = launch_predictor_tma<8>(c, a, c->pred_tma_ctas[1]);
   }
-  if (!done) launch_tiled(k_predictor_mixed<4>, k_predictor_mixed<8>, k_predictor_mixed<16>, ty, c, a);
+  if (!done && c->uni_x.on)
+    launch_tiled(k_predictor_mixed<4, true>, k_predictor_mixed<8, true>, k_predictor_mixed<16, true>, ty, c, a);
+  else if (!done)
+    launch_tiled(k_predictor_mixed<4, false>, k_predictor_mixed<8, false>, k_predictor_mixed<16, false>, ty, c, a);
   EIF_LAUNCH_CK(c);
   c->cur = 1 - c->cur;
   return EIF_OK;

@@ -176,6 +176,7 @@ extern "C" int eif_tiles(eif_ctx *c, int *tiles) {
   tiles[0] = c->tiles.pred;
   tiles[1] = c->tiles.corr;
   tiles[2] = c->tiles.tdm;
-  tiles[3] = (c->tiles.tuned ? 1 : 0) | (c->tiles.pred_copy && c->pred_tma_ctas[1] > 0 ? 2 : 0);
+  tiles[3] = (c->tiles.tuned ? 1 : 0) | (c->tiles.pred_copy && c->pred_tma_ctas[1] > 0 ? 2 : 0) |
+             (c->cfg.precision == EIF_PREC_MIXED && c->uni_x.on ? 4 : 0);
   return EIF_OK;
 }

@@ -177,7 +177,10 @@ int eif_snapshot_wait(eif_ctx *ctx, double *ux, double *uy, double *p, int n, do
  * with its tiles staged by bulk tensor copies (double-buffered, TMA) or with plain loads,
  * whichever the tuner timed faster (EIF_NO_TMA=1 at context creation: plain loads only).
  * tiles[4]: predictor rows, projection rows, Thomas threads, flags (bit 0: tuned, bit 1:
- * predictor tiles staged by tensor copies). No counterpart in the reference. */
+ * predictor tiles staged by tensor copies, bit 2: the mixed predictor with plain loads
+ * takes the x metrics as uniform values away from the wall cells, which it does when
+ * their single-precision values are bitwise uniform there; EIF_NO_UNIFORM_X=1 at context
+ * creation: always from the arrays). No counterpart in the reference. */
 int eif_tiles(eif_ctx *ctx, int *tiles);
 
 /* ---- discrete adjoint of the step (no counterpart in the reference) ----

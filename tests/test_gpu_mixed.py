@@ -168,6 +168,24 @@ def test_tensor_copy_predictor_equals_plain_kernel(rows, gpu_lib, monkeypatch):
     for x, y in zip(a.pull_fluid(), b.pull_fluid()):
         assert np.array_equal(x, y)
     assert np.array_equal(a.pull_particles(), b.pull_particles())
+
+
+@pytest.mark.parametrize("itot,jtot", [(96, 200), (2048, 512)])
+def test_uniform_x_metrics_equal_loaded_metrics(itot, jtot, gpu_lib, monkeypatch):
+    """The mixed predictor that takes the x metrics as uniform arguments away from the wall
+    cells gives the bits of the one that loads them from the arrays (EIF_NO_UNIFORM_X=1),
+    plain loads both, tiles partial in x at itot = 96."""
+    monkeypatch.setenv("EIF_NO_TMA", "1")
+    case = cases.poiseuille(itot=itot, jtot=jtot, n=6, a=0.04, b=0.02, seed=2)
+    a = Simulation.from_case(case, precision=PREC_MIXED)
+    monkeypatch.setenv("EIF_NO_UNIFORM_X", "1")
+    b = Simulation.from_case(case, precision=PREC_MIXED)
+    assert a.tiles()["predictor_uniform_x"] and not b.tiles()["predictor_uniform_x"]
+    a.advance(3)
+    b.advance(3)
+    for x, y in zip(a.pull_fluid(), b.pull_fluid()):
+        assert np.array_equal(x, y)
+    assert np.array_equal(a.pull_particles(), b.pull_particles())
     a.close()
     b.close()
 
