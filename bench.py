@@ -69,12 +69,11 @@ HBM_BYTES = {
 # unchanged (otherwise null, marked stale)
 # (the DCT entries are the mean of the two passes' launches)
 _KPROF = "profiles/kernels_suspension_2048x4096_mixed.md"
-_FLUID_SHA = "841771c17643f0780def177c58058f05c8c63c0d"
-_FLUID_SHA_PRED = "52b69b617a3a686d26584b2389729d3f3b7affaa"   # the predictor's capture
+_FLUID_SHA = "4f127f15a85642621dcb0c4f1ea17fcb27220098"
 _POISSON_SHA = "d416f6dceb2475e242e4a162f6d50ebb46f4d06d"
 NCU_TRAFFIC = {
     ("mixed", 2048, 4096): {
-        "predictor": (435e6, "fluid.cu", _FLUID_SHA_PRED, _KPROF),
+        "predictor": (435e6, "fluid.cu", _FLUID_SHA, _KPROF),
         "correct": (489e6, "fluid.cu", _FLUID_SHA, _KPROF),
         "poisson_dct2": (200e6, "poisson.cu", _POISSON_SHA, _KPROF),
         "poisson_dct3": (36e6, "poisson.cu", _POISSON_SHA, _KPROF),
