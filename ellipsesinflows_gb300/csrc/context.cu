@@ -209,9 +209,12 @@ int rows_in(eif_ctx *c, double *dst, const double *host, int w, int rows) {
   return EIF_OK;
 }
 
-int rows_out(eif_ctx *c, double *host, const double *src, int w, int rows, cudaStream_t stream = nullptr) {
+// engine: the DMA engines even for mapped memory (a copy beside running kernels, which
+// the copy kernel would take SMs from)
+int rows_out(eif_ctx *c, double *host, const double *src, int w, int rows, cudaStream_t stream = nullptr,
+             bool engine = false) {
   if (!stream) stream = c->stream;
-  if (double *hd = static_cast<double *>(mapped(host))) {
+  if (double *hd = engine ? nullptr : static_cast<double *>(mapped(host))) {
     k_rows_out<<<c->sms * 4, 512, 0, stream>>>(src, hd, w, rows, c->ld);
     EIF_LAUNCH_CK(c);
     return EIF_OK;
@@ -795,12 +798,22 @@ int advance(eif_ctx *c, int nsteps, const FieldTargets *ft) {
       EIF_CK(c, cudaEventRecord(c->ev_step[s & 1], c->stream));
       if (ft && s == nsteps - 1) {
         // the fields are final once the graph has recorded ev_fields (after the last
-        // stage's projection): their copy runs beside that stage's particle work
+        // stage's projection): the first of them is copied on the DMA engines beside that
+        // stage's particle work, which keeps the SMs; the others by the copy kernel (the
+        // faster copy) once the step is done
         EIF_CK(c, cudaStreamWaitEvent(c->copy_stream, c->ev_fields, 0));
         const int rows = c->jtot + 2;
-        if (ft->ux && (rc = rows_out(c, ft->ux, c->ux[c->cur], c->itot + 1, rows, c->copy_stream))) return rc;
-        if (ft->uy && (rc = rows_out(c, ft->uy, c->uy[c->cur], c->itot + 2, rows, c->copy_stream))) return rc;
-        if (ft->p && (rc = rows_out(c, ft->p, c->p, c->itot + 2, rows, c->copy_stream))) return rc;
+        double *hosts[3] = {ft->ux, ft->uy, ft->p};
+        const double *srcs[3] = {c->ux[c->cur], c->uy[c->cur], c->p};
+        const int widths[3] = {c->itot + 1, c->itot + 2, c->itot + 2};
+        bool first = true;
+        for (int f = 0; f < 3; f++) {
+          if (!hosts[f]) continue;
+          rc = first ? rows_out(c, hosts[f], srcs[f], widths[f], rows, c->copy_stream, true)
+                     : rows_out(c, hosts[f], srcs[f], widths[f], rows, c->stream);
+          if (rc) return rc;
+          first = false;
+        }
         fields_queued = true;
       }
       if (s > 0 && (rc = finish(s - 1))) {
