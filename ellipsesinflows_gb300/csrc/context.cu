@@ -358,7 +358,8 @@ int check_flags(eif_ctx *c) {
   }
   if (f & EIF_FLAG_NOCONV)
     return fail(c, EIF_ERR_NOCONV, "an iteration cap or a device list capacity was reached on the device");
-  if (f & EIF_FLAG_TIMEOUT) return fail(c, EIF_ERR_CUDA, "a bounded wait for an asynchronous tile copy gave up");
+  if (f & EIF_FLAG_TIMEOUT)
+    return fail(c, EIF_ERR_CUDA, "a bounded wait on the device (a tile copy or a grid barrier) gave up");
   return EIF_OK;
 }
 }  // namespace eif

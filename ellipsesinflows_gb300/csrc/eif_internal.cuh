@@ -28,7 +28,7 @@
 // error flags raised by kernels (bit mask in ctx->d_flags)
 #define EIF_FLAG_NOCONV 1u
 #define EIF_FLAG_NONFINITE 2u
-#define EIF_FLAG_TIMEOUT 4u   // a bounded wait for an asynchronous copy gave up
+#define EIF_FLAG_TIMEOUT 4u   // a bounded wait (an asynchronous copy, a grid barrier) gave up
 
 // cap of the equivalent-circle fixed point (the reference has none,
 // src/suspensions/collision.c:117-133,141-152)

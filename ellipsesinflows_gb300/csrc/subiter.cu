@@ -36,7 +36,9 @@
 // the CTA sets the plan's error word, which makes the others give up at their next
 // poll, and every suspension's EIF_FLAG_TIMEOUT, and the CTAs return. Data that one
 // phase writes and a later one reads is read with ordinary loads, not through the
-// read-only path.
+// read-only path. For the tests of that bounded wait, EIF_TEST_HOLD_BARRIER=1 in the
+// environment when a batch's graph is built keeps CTA 0 of the first stage's kernel
+// from arriving at its first barrier: the other CTAs give up, and the step reports it.
 #ifndef EIF_CHECK
 #define EIF_CHECK 1
 #endif
@@ -44,6 +46,7 @@
 #include "ibm_device.cuh"
 #include "particle_device.cuh"
 #include <algorithm>
+#include <cstdlib>
 
 namespace {
 
@@ -66,6 +69,7 @@ struct StageArgs {
   const SubDesc *d;
   int n;
   int reset_next;               // the particles' increments are reset for a following stage
+  int hold;                     // a CTA that does not arrive at the first barrier (tests), or -1
   unsigned *sync;               // [0] arrivals, [1] error
   unsigned long long *res;      // two residual words per suspension (alternating sub-iterations)
 };
@@ -84,14 +88,15 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
   return v;
 }
 
-// grid barrier number idx (0, 1, ...) of this launch; false when it gave up
-__device__ bool grid_barrier(unsigned *sync, unsigned idx) {
+// grid barrier number idx (0, 1, ...) of this launch; false when it gave up. arrive:
+// the CTA counts itself (false only for the tests of the bounded wait)
+__device__ bool grid_barrier(unsigned *sync, unsigned idx, bool arrive) {
   __shared__ int ok;
   __syncthreads();
   if (threadIdx.x == 0) {
     const unsigned target = gridDim.x * (idx + 1u);
     __threadfence();
-    atomicAdd(sync, 1u);
+    if (arrive) atomicAdd(sync, 1u);
     int good = 0;
     for (unsigned k = 0; k < SPIN_MAX; k++) {
       if (ld_acquire(sync) >= target) {
@@ -150,6 +155,10 @@ __global__ void __launch_bounds__(SUB_THREADS, 2) k_subiterations(StageArgs s) {
   auto active = [&](int j) { return ((act[j >> 5] >> (j & 31)) & 1u) != 0u; };
   unsigned bar = 0;
   bool ok = true;
+  auto barrier = [&]() {
+    const bool arrive = bar != 0u || (int)blockIdx.x != s.hold;
+    return grid_barrier(s.sync, bar++, arrive);
+  };
   for (unsigned it = 0; it < SUB_CAP; it++) {
     // 1. collision forces; boxes after the first sub-iteration
     for (int j = 0; j < n; j++) {
@@ -175,7 +184,7 @@ __global__ void __launch_bounds__(SUB_THREADS, 2) k_subiterations(StageArgs s) {
         const SubDesc &d = s.d[j];
         for (; u < units; u += W) box_part(d.box, (u % groups) * 32 + lane, u / groups);
       }
-      if (!(ok = grid_barrier(s.sync, bar++))) break;
+      if (!(ok = barrier())) break;
       // 2. task tables
       for (int j = 0; j < n; j++) {
         if (!active(j)) continue;
@@ -190,7 +199,7 @@ __global__ void __launch_bounds__(SUB_THREADS, 2) k_subiterations(StageArgs s) {
         }
       }
     }
-    if (!(ok = grid_barrier(s.sync, bar++))) break;
+    if (!(ok = barrier())) break;
     // 3. row tasks of the inertia integrals; task counts zeroed for the next boxes. The
     // task totals of phase 2 are read into shared memory first, one load per suspension.
     for (int j = threadIdx.x; j < n; j += SUB_THREADS) {
@@ -219,7 +228,7 @@ __global__ void __launch_bounds__(SUB_THREADS, 2) k_subiterations(StageArgs s) {
       }
       for (int q = tid; q < np; q += T) d.cnt[q] = 0;
     }
-    if (!(ok = grid_barrier(s.sync, bar++))) break;
+    if (!(ok = barrier())) break;
     // 4. sums over the tasks, increments, residuals
     for (int j = 0; j < n; j++) {
       if (!active(j)) continue;
@@ -245,7 +254,7 @@ __global__ void __launch_bounds__(SUB_THREADS, 2) k_subiterations(StageArgs s) {
         }
       }
     }
-    if (!(ok = grid_barrier(s.sync, bar++))) break;
+    if (!(ok = barrier())) break;
     // the stopping rule of every suspension, evaluated alike by all CTAs
     for (int j = threadIdx.x; j < n; j += SUB_THREADS) {
       if (!active(j)) continue;
@@ -296,6 +305,7 @@ struct SubiterPlan {
   SubDesc *d_desc = nullptr;
   unsigned *d_sync = nullptr;           // 3 stages x SYNC_WORDS
   unsigned long long *d_res = nullptr;  // 3 stages x 2n
+  int hold = -1;                        // EIF_TEST_HOLD_BARRIER: CTA 0 of stage 0 held back
 };
 
 bool subiter_joinable(const eif_ctx *c) { return c->np <= TT_MAX_NP; }
@@ -340,6 +350,8 @@ int subiter_plan_create(eif_ctx *const *ctx, int n, SubiterPlan **out, std::stri
   if (!p) return EIF_ERR_NOMEM;
   p->n = n;
   p->grid = occ * ctx[0]->sms;
+  const char *hold = std::getenv("EIF_TEST_HOLD_BARRIER");
+  p->hold = hold && hold[0] == '1' ? 0 : -1;
   p->h.assign((size_t)3 * n, SubDesc{});
   if ((e = cudaMalloc((void **)&p->d_desc, sizeof(SubDesc) * 3 * n)) != cudaSuccess ||
       (e = cudaMalloc((void **)&p->d_sync, sizeof(unsigned) * 3 * SYNC_WORDS)) != cudaSuccess ||
@@ -394,6 +406,7 @@ int subiter_add_stage(SubiterPlan *p, int rk, cudaGraph_t g, const std::vector<c
   a.sync = p->d_sync + SYNC_WORDS * rk;
   a.res = p->d_res + (size_t)2 * p->n * rk;
   a.reset_next = rk < 2 ? 1 : 0;
+  a.hold = rk == 0 ? p->hold : -1;
   void *args[] = {&a};
   cudaKernelNodeParams k = {};
   k.func = reinterpret_cast<void *>(k_subiterations);

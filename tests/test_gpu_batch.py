@@ -102,3 +102,28 @@ def test_batch_with_a_suspension_beyond_the_stage_kernel(gpu_lib):
         batch.advance(2)
     for a, b in zip(solo, together):
         assert_same(a, b)
+
+
+def test_stage_kernel_barrier_timeout_is_reported(gpu_lib, monkeypatch):
+    """The stage kernel's grid barrier is a bounded wait. With CTA 0 of the first stage's
+    kernel held back from its first barrier (EIF_TEST_HOLD_BARRIER=1, read when the batch's
+    graph is built) the other CTAs give up after their 2^22 polls, return, and the step
+    reports the bounded wait; the GPU context stays usable: a new batch of fresh
+    suspensions then gives the bits of separate runs."""
+    from ellipsesinflows_gb300.capi import EifError
+    monkeypatch.delenv("EIF_BATCH_SUBITER", raising=False)
+    specs = members()[:2]
+    held = [Simulation.from_case(f(), precision=p) for f, p in specs]
+    monkeypatch.setenv("EIF_TEST_HOLD_BARRIER", "1")
+    with Batch(held) as batch:
+        with pytest.raises(EifError, match="bounded wait"):
+            batch.advance(1)
+    monkeypatch.delenv("EIF_TEST_HOLD_BARRIER")
+    solo = [Simulation.from_case(f(), precision=p) for f, p in specs]
+    together = [Simulation.from_case(f(), precision=p) for f, p in specs]
+    for s in solo:
+        s.advance(2)
+    with Batch(together) as batch:
+        batch.advance(2)
+    for a, b in zip(solo, together):
+        assert_same(a, b)
