@@ -45,7 +45,7 @@ def _worker(rank, port, out):
 
 def test_max_over_ranks_with_gloo():
     import torch.multiprocessing as mp
-    mgr = mp.Manager()
+    mgr = mp.get_context("spawn").Manager()   # no fork of a threaded process
     out = mgr.dict()
     mp.spawn(_worker, args=(_free_port(), out), nprocs=2, join=True)
     assert out[0] == 2.5 and out[1] == 2.5
