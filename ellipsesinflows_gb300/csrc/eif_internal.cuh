@@ -91,6 +91,7 @@ struct PoissonPlan {
   double *r2_coef = nullptr;                                        // [k][4] A2, B2, den2, pin flag
   double *lam;      // [k]     eigenvalue of the DCT direction
   double *ywork;    // nblk*itot: reduced right-hand sides / interface values
+  float *iface_f = nullptr;  // nblk*itot: the solved interface values rounded to float (refined solve)
 };
 
 struct Adjoint;  // adjoint.cu

@@ -207,13 +207,16 @@ __global__ void __launch_bounds__(256) k_tdm_local(double *__restrict__ qhat, co
 // wavenumber runs the serial sweeps; the block's other threads first stage the
 // right-hand sides and the elimination factors of its `cols` wavenumbers in
 // shared memory (many loads in flight), so that the sweeps run at shared-memory
-// latency, and afterwards write the results back.
+// latency, and afterwards write the results back. With iface_f set, the solved values
+// are also stored rounded to float (eifd::d2f), the input of the single-precision DCT-III,
+// which then converts each of them once instead of once per row of its block.
 constexpr int RED_THREADS = 256;
 
 __global__ void __launch_bounds__(RED_THREADS) k_tdm_reduced(double *__restrict__ iface, const double *__restrict__ first,
                                                              const double *__restrict__ rinv, const double *__restrict__ rup,
                                                              const double *__restrict__ rq1, const double *__restrict__ rcoef,
-                                                             double l, int itot, int nblk, int cols) {
+                                                             double l, int itot, int nblk, int cols,
+                                                             float *__restrict__ iface_f) {
   extern __shared__ double zs[];  // [nblk][cols] right-hand sides, then [nblk][cols] rinv, rup; [cols] last
   const int P = nblk;
   double *fi = zs + (size_t)P * cols, *fu = fi + (size_t)P * cols, *lastv = fu + (size_t)P * cols;
@@ -257,7 +260,9 @@ __global__ void __launch_bounds__(RED_THREADS) k_tdm_reduced(double *__restrict_
     const int k = k0 + tt;
     if (k >= itot) continue;
     const double last = lastv[tt];
-    iface[(size_t)b * itot + k] = b == P - 1 ? last : zs[idx] + last * rq1[(size_t)b * itot + k];
+    const double v = b == P - 1 ? last : zs[idx] + last * rq1[(size_t)b * itot + k];
+    iface[(size_t)b * itot + k] = v;
+    if (iface_f) iface_f[(size_t)b * itot + k] = eifd::d2f(v);
   }
 }
 
@@ -272,7 +277,8 @@ __global__ void __launch_bounds__(RED_THREADS) k_tdm_reduced(double *__restrict_
 // t_{g-1} phi[i] + t_g phi[G-2-i] to its interior. Block: RED2_K wavenumbers x Q
 // groups (8 wavenumbers per block spread the FP64 work over 256 blocks at 2048 x 4096);
 // the factors of the Q-value solve are staged in shared memory by the whole block
-// before its serial sweep.
+// before its serial sweep. iface_f (optional): the solved values rounded to float, as in
+// k_tdm_reduced.
 constexpr int RED2_K = 8;
 constexpr size_t red2_smem_bytes(int Q) { return sizeof(double) * 6 * RED2_K * (size_t)Q; }
 template <int G>
@@ -281,7 +287,7 @@ __global__ void __launch_bounds__(1024) k_tdm_reduced2(double *__restrict__ ifac
                                                        const double *__restrict__ up2, const double *__restrict__ phi2,
                                                        const double *__restrict__ ri2, const double *__restrict__ ru2,
                                                        const double *__restrict__ rq2, const double *__restrict__ rc2,
-                                                       double l, int itot, int P, int Q) {
+                                                       double l, int itot, int P, int Q, float *__restrict__ iface_f) {
   // [Q][RED2_K] first interior values, right-hand sides, interface values, and the
   // second-level factors ri2, ru2, rq2
   extern __shared__ double sm2[];
@@ -339,10 +345,12 @@ __global__ void __launch_bounds__(1024) k_tdm_reduced2(double *__restrict__ ifac
   const double tl = ts[((g + Q - 1) % Q) * K + kk], tr = ts[g * K + kk];
 #pragma unroll
   for (int i = 0; i < G - 1; i++) {
-    iface[(size_t)(g * G + i) * itot + k] =
-        y[i] + tl * phi2[(size_t)i * itot + k] + tr * phi2[(size_t)(G - 2 - i) * itot + k];
+    const double v = y[i] + tl * phi2[(size_t)i * itot + k] + tr * phi2[(size_t)(G - 2 - i) * itot + k];
+    iface[(size_t)(g * G + i) * itot + k] = v;
+    if (iface_f) iface_f[(size_t)(g * G + i) * itot + k] = eifd::d2f(v);
   }
   iface[(size_t)(g * G + G - 1) * itot + k] = tr;
+  if (iface_f) iface_f[(size_t)(g * G + G - 1) * itot + k] = eifd::d2f(tr);
 }
 
 // columns per block of k_tdm_reduced that fit its shared memory
@@ -1388,7 +1396,7 @@ __global__ void __launch_bounds__(256) k_tdm_local_f(float *__restrict__ q, cons
 
 struct Dct3ArgsF {
   const float *q;        // block solutions, rows of pitch ld floats
-  const double *iface;   // solved interface values [block][k]
+  const float *iface;    // solved interface values [block][k], rounded to float by the reduced solve
   const float *g;        // left responses of the block interior [r][k]
   float *psi;            // output (uy layout, with halo rows and ghost columns)
   const float2 *tw, *rot, *wn;
@@ -1418,12 +1426,12 @@ __global__ void __launch_bounds__(FFT_CTA, 10) k_dct3_f(Dct3ArgsF a, FftShape sh
     for (int k = t; k < n; k += T) {
       float val;
       if (r == M - 1) {
-        val = eifd::d2f(__ldg(a.iface + (size_t)b * n + k));
+        val = __ldg(a.iface + (size_t)b * n + k);
       } else {
         // y + s_left g + s_right h (h = g reversed, the blocks are symmetric)
         const float gl = __ldg(a.g + (size_t)r * n + k), gr = __ldg(a.g + (size_t)(M - 2 - r) * n + k);
-        const float sl = eifd::d2f(__ldg(a.iface + (size_t)bm * n + k));
-        const float sr = eifd::d2f(__ldg(a.iface + (size_t)b * n + k));
+        const float sl = __ldg(a.iface + (size_t)bm * n + k);
+        const float sr = __ldg(a.iface + (size_t)b * n + k);
         val = fmaf(sr, gr, fmaf(sl, gl, __ldg(row + k)));
       }
       xr[k] = val;
@@ -1730,7 +1738,10 @@ int poisson_init(eif_ctx *c) {
     }
     // the refined single-precision solve: power-of-two half lengths with the block solver
     c->psi_pair = c->cfg.precision == EIF_PREC_MIXED && sh.T > 0 && pp.blk > 0;
-    if (c->psi_pair) EIF_CK(c, cudaMalloc((void **)&pp.qdf, sizeof(float2) * (size_t)c->ld * jt));
+    if (c->psi_pair) {
+      EIF_CK(c, cudaMalloc((void **)&pp.qdf, sizeof(float2) * (size_t)c->ld * jt));
+      EIF_CK(c, cudaMalloc((void **)&pp.iface_f, sizeof(float) * (size_t)pp.nblk * n));
+    }
   }
   return EIF_OK;
 }
@@ -1740,7 +1751,7 @@ void poisson_free(eif_ctx *c) {
   void *ptrs[] = {pp.r2_inv, pp.r2_up, pp.r2_phi, pp.r2_qinv, pp.r2_qup, pp.r2_q1, pp.r2_coef,
                   pp.tw, pp.rot, pp.wn, pp.tw_f, pp.rot_f, pp.wn_f, pp.lam, pp.tdm_inv, pp.tdm_up, pp.tdm_g, pp.tdm_g_df, pp.tdm_inv_df, pp.tdm_up_df,
                   pp.red_inv, pp.red_up, pp.red_q1, pp.red_coef, pp.ywork, pp.tw2, pp.rot2, pp.wn2, pp.tdm_inv_f,
-                  pp.tdm_up_f, pp.tdm_g_f, pp.qdf};
+                  pp.tdm_up_f, pp.tdm_g_f, pp.qdf, pp.iface_f};
   for (void *p : ptrs) if (p) cudaFree(p);
   pp = PoissonPlan{};
 }
@@ -1748,7 +1759,7 @@ void poisson_free(eif_ctx *c) {
 static int fft_threads(int m) { return m >= 512 ? 256 : (m >= 128 ? 128 : 64); }
 
 // the reduced cyclic systems of the interface values (double precision), in place in iface
-static int reduced_solve(eif_ctx *c, double *iface, double *first) {
+static int reduced_solve(eif_ctx *c, double *iface, double *first, float *iface_f) {
   PoissonPlan &pp = c->pp;
   const int n = c->itot;
   const double l = 1. / c->dy / c->dy;
@@ -1758,18 +1769,21 @@ static int reduced_solve(eif_ctx *c, double *iface, double *first) {
     const dim3 grid((n + RED2_K - 1) / RED2_K);
     if (pp.g2 == 16) {
       k_tdm_reduced2<16><<<grid, RED2_K * Q, sm, c->stream>>>(iface, first, pp.red_coef, pp.r2_inv, pp.r2_up, pp.r2_phi,
-                                                          pp.r2_qinv, pp.r2_qup, pp.r2_q1, pp.r2_coef, l, n, pp.nblk, Q);
+                                                          pp.r2_qinv, pp.r2_qup, pp.r2_q1, pp.r2_coef, l, n, pp.nblk, Q,
+                                                         iface_f);
     } else if (pp.g2 == 8) {
       k_tdm_reduced2<8><<<grid, RED2_K * Q, sm, c->stream>>>(iface, first, pp.red_coef, pp.r2_inv, pp.r2_up, pp.r2_phi,
-                                                         pp.r2_qinv, pp.r2_qup, pp.r2_q1, pp.r2_coef, l, n, pp.nblk, Q);
+                                                         pp.r2_qinv, pp.r2_qup, pp.r2_q1, pp.r2_coef, l, n, pp.nblk, Q,
+                                                         iface_f);
     } else {
       k_tdm_reduced2<4><<<grid, RED2_K * Q, sm, c->stream>>>(iface, first, pp.red_coef, pp.r2_inv, pp.r2_up, pp.r2_phi,
-                                                         pp.r2_qinv, pp.r2_qup, pp.r2_q1, pp.r2_coef, l, n, pp.nblk, Q);
+                                                         pp.r2_qinv, pp.r2_qup, pp.r2_q1, pp.r2_coef, l, n, pp.nblk, Q,
+                                                         iface_f);
     }
   } else {
     const int rcols = red_cols(pp.nblk);
     k_tdm_reduced<<<(n + rcols - 1) / rcols, RED_THREADS, red_smem_bytes(pp.nblk, rcols), c->stream>>>(
-        iface, first, pp.red_inv, pp.red_up, pp.red_q1, pp.red_coef, l, n, pp.nblk, rcols);
+        iface, first, pp.red_inv, pp.red_up, pp.red_q1, pp.red_coef, l, n, pp.nblk, rcols, iface_f);
   }
   EIF_LAUNCH_CK(c);
   return EIF_OK;
@@ -1821,11 +1835,11 @@ static int potential_refined(eif_ctx *c, int rk, bool with_ibm) {
         k_tdm_local_f<4><<<gt, tt, 0, c->stream>>>(qf, pp.tdm_inv_f, pp.tdm_up_f, iface, first, lf, n, pp.nblk, c->ld);
       }
       EIF_LAUNCH_CK(c);
-      int rc = reduced_solve(c, iface, first);
+      int rc = reduced_solve(c, iface, first, pp.iface_f);
       if (rc) return rc;
     }
     Dct3ArgsF b;
-    b.q = qf; b.iface = iface; b.g = pp.tdm_g_f;
+    b.q = qf; b.iface = pp.iface_f; b.g = pp.tdm_g_f;
     b.psi = pass ? psi2 : psi1;
     b.tw = pp.tw2; b.rot = pp.rot2; b.wn = pp.wn2;
     b.scale = (float)(1. / (2. * n));
@@ -1930,20 +1944,20 @@ int launch_potential(eif_ctx *c, int rk, bool with_ibm) {
       if (pp.g2 == 16) {
         k_tdm_reduced2<16><<<grid, RED2_K * Q, sm, c->stream>>>(iface, first, pp.red_coef, pp.r2_inv, pp.r2_up, pp.r2_phi,
                                                             pp.r2_qinv, pp.r2_qup, pp.r2_q1, pp.r2_coef, l, n,
-                                                            pp.nblk, Q);
+                                                            pp.nblk, Q, nullptr);
       } else if (pp.g2 == 8) {
         k_tdm_reduced2<8><<<grid, RED2_K * Q, sm, c->stream>>>(iface, first, pp.red_coef, pp.r2_inv, pp.r2_up, pp.r2_phi,
                                                            pp.r2_qinv, pp.r2_qup, pp.r2_q1, pp.r2_coef, l, n,
-                                                           pp.nblk, Q);
+                                                           pp.nblk, Q, nullptr);
       } else {
         k_tdm_reduced2<4><<<grid, RED2_K * Q, sm, c->stream>>>(iface, first, pp.red_coef, pp.r2_inv, pp.r2_up, pp.r2_phi,
                                                            pp.r2_qinv, pp.r2_qup, pp.r2_q1, pp.r2_coef, l, n,
-                                                           pp.nblk, Q);
+                                                           pp.nblk, Q, nullptr);
       }
     } else {
       const int rcols = red_cols(pp.nblk);
       k_tdm_reduced<<<(n + rcols - 1) / rcols, RED_THREADS, red_smem_bytes(pp.nblk, rcols), c->stream>>>(
-          iface, first, pp.red_inv, pp.red_up, pp.red_q1, pp.red_coef, l, n, pp.nblk, rcols);
+          iface, first, pp.red_inv, pp.red_up, pp.red_q1, pp.red_coef, l, n, pp.nblk, rcols, nullptr);
     }
     EIF_LAUNCH_CK(c);
   } else {
