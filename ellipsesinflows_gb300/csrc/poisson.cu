@@ -1205,21 +1205,35 @@ template <int S> __device__ __forceinline__ void dft8_f(CF (&v)[8]) {
 #pragma unroll
   for (int k = 0; k < 8; k++) v[k] = w[k];
 }
-template <int S> __device__ __forceinline__ float2 twiddle_f(const float2 *__restrict__ tw, int e) {
-  float2 w = __ldg(tw + e);
+// The single-precision transforms are instantiated for each power-of-two half length
+// m = 2^LGM (8 <= m <= 8 FFT_CTA): thread counts, pass lengths and strides are compile-time
+// constants, so the shared-memory offsets are immediates. The twiddles are read from a
+// table laid out in pass order (pass_twiddles below): for the radix-8 pass of length L,
+// butterfly k reads its seven twiddles w^(u k m / 8L), u = 1..7, as consecutive values.
+constexpr int ilog2c(int x) { return x <= 1 ? 0 : 1 + ilog2c(x / 2); }
+// offset of the twiddles of the radix-8 pass of length L (L = 8, 64, ...) in the table;
+// the last pass's twiddles follow those of all radix-8 passes
+constexpr int twp_off(int L) { return L <= 8 ? 0 : twp_off(L / 8) + 7 * (L / 8); }
+__device__ __forceinline__ int padv8(int i) { return i + (i >> 3); }
+template <int S> __device__ __forceinline__ float2 twiddle_p(const float2 *__restrict__ p) {
+  float2 w = __ldg(p);
   if (S > 0) w.y = -w.y;
   return w;
 }
-// the last pass of radix R = 2 or 4: butterfly j (< L) reads and writes j + u L
-template <int S, int R>
-__device__ __forceinline__ void fft_last_f(CF *buf, CF (&v)[8], int t, int T, int L, const float2 *__restrict__ tw) {
+// the last pass of radix R = 2 or 4 (L = M / R): butterfly j = t + q T (q < 8/R) reads and
+// writes j + u L; its twiddles w^(u j), u = 1..R-1, are twp[(R-1) j + u - 1]
+template <int S, int R, int M>
+__device__ __forceinline__ void fft_last_f(CF *buf, CF (&v)[8], int t, const float2 *__restrict__ twp) {
+  constexpr int T = M / 8, L = M / R, SL = L + L / 8;
+  static_assert(L % 8 == 0, "the last pass follows a radix-8 pass");
 #pragma unroll
   for (int q = 0; q < 8 / R; q++) {
     const int j = t + q * T;
+    const int jb = padv8(j);
 #pragma unroll
     for (int u = 0; u < R; u++) {
-      CF x = buf[padv<8>(j + u * L)];
-      if (u > 0 && j > 0) x = cf_mul(x, twiddle_f<S>(tw, u * j));
+      CF x = buf[jb + u * SL];
+      if (u > 0 && j > 0) x = cf_mul(x, twiddle_p<S>(twp + (R - 1) * j + u - 1));
       v[q * R + u] = x;
     }
   }
@@ -1236,46 +1250,50 @@ __device__ __forceinline__ void fft_last_f(CF *buf, CF (&v)[8], int t, int T, in
   }
 #pragma unroll
   for (int q = 0; q < 8 / R; q++) {
-    const int j = t + q * T;
+    const int jb = padv8(t + q * T);
 #pragma unroll
-    for (int u = 0; u < R; u++) buf[padv<8>(j + u * L)] = v[q * R + u];
+    for (int u = 0; u < R; u++) buf[jb + u * SL] = v[q * R + u];
   }
 }
-// Stockham transform of one row of m = 8 T values (radix-8 passes, then radix 2 or 4):
-// v holds the inputs x[t + u T] of thread t on entry; on exit the spectrum is in buf
-// (padded layout) and visible to the whole CTA
-template <int S>
-__device__ void fft_row_f(CF *buf, CF (&v)[8], int t, int T, int m, const float2 *__restrict__ tw) {
-  dft8_f<S>(v);
-  __syncthreads();
-#pragma unroll
-  for (int u = 0; u < 8; u++) buf[padv<8>(8 * t + u)] = v[u];
-  __syncthreads();
-  int L = 8, lgL = 3;
-  while (L * 8 <= m) {
-    const int k = t & (L - 1), blk = t >> lgL;
-    const int tws = m >> (lgL + 3);
+// the Stockham passes from length L on: radix 8 while 8 L <= M, then radix M / L
+template <int S, int M, int L>
+__device__ __forceinline__ void fft_passes_f(CF *buf, CF (&v)[8], int t, const float2 *__restrict__ twp) {
+  constexpr int T = M / 8;
+  if constexpr (L * 8 <= M) {
+    static_assert(T % 8 == 0 && L % 8 == 0, "radix-8 passes need 8 | T and 8 | L");
+    constexpr int LG = ilog2c(L), ST = T + T / 8, SL = L + L / 8;
+    const int k = t & (L - 1), blk = t >> LG;
+    const float2 *w = twp + twp_off(L) + 7 * k;
+    const int ib = padv8(t);
 #pragma unroll
     for (int u = 0; u < 8; u++) {
-      CF x = buf[padv<8>(t + u * T)];
-      if (u > 0 && k > 0) x = cf_mul(x, twiddle_f<S>(tw, u * k * tws));
+      CF x = buf[ib + u * ST];
+      if (u > 0 && k > 0) x = cf_mul(x, twiddle_p<S>(w + u - 1));
       v[u] = x;
     }
     dft8_f<S>(v);
     __syncthreads();
-    const int o = blk * L * 8 + k;
+    const int ob = padv8(blk * L * 8 + k);
 #pragma unroll
-    for (int u = 0; u < 8; u++) buf[padv<8>(o + u * L)] = v[u];
+    for (int u = 0; u < 8; u++) buf[ob + u * SL] = v[u];
     __syncthreads();
-    L <<= 3;
-    lgL += 3;
-  }
-  const int R = m / L;
-  if (R > 1) {
-    if (R == 2) fft_last_f<S, 2>(buf, v, t, T, L, tw);
-    else fft_last_f<S, 4>(buf, v, t, T, L, tw);
+    fft_passes_f<S, M, L * 8>(buf, v, t, twp);
+  } else if constexpr (M / L > 1) {
+    fft_last_f<S, M / L, M>(buf, v, t, twp + twp_off(L));
     __syncthreads();
   }
+}
+// Stockham transform of one row of M = 8 T values (radix-8 passes, then radix 2 or 4):
+// v holds the inputs x[t + u T] of thread t on entry; on exit the spectrum is in buf
+// (padded layout) and visible to the whole CTA
+template <int S, int M>
+__device__ void fft_row_f(CF *buf, CF (&v)[8], int t, const float2 *__restrict__ twp) {
+  dft8_f<S>(v);
+  __syncthreads();
+#pragma unroll
+  for (int u = 0; u < 8; u++) buf[9 * t + u] = v[u];   // padded index of 8 t + u
+  __syncthreads();
+  fft_passes_f<S, M, 8>(buf, v, t, twp);
 }
 
 struct Dct2ArgsF {
@@ -1285,21 +1303,22 @@ struct Dct2ArgsF {
   const float *psi1;        // refinement pass: the first solution (uy layout), else null
   float2 *qdf;              // q as (hi, lo) pairs: written by the first pass, read by the second
   float *q;                 // transformed right-hand side, rows of pitch ld floats
-  const float2 *tw, *rot, *wn;
+  const float2 *tw, *rot, *wn;   // tw: twiddles in pass order (pass_twiddles)
   DF rdx, rdy, rdx2, rdy2;  // 1/dx, 1/dy, 1/dx^2, 1/dy^2
   int itot, jtot, ld, with_ibm, rk;
 };
 
 // right-hand side (or the residual of the first solution) + single-precision DCT-II
 // of rows; one row of m = itot/2 complex values per T = m/8 threads
-// capped at 32 registers (64 bytes spilled) for 16 resident CTAs per SM: measured faster
-// than 40 registers and 12 CTAs
-__global__ void __launch_bounds__(FFT_CTA, 16) k_dct2_f(Dct2ArgsF a, FftShape sh) {
+// (itot = 2 m, m = 2^LGM); capped at 32 registers for 16 resident CTAs per SM: measured
+// faster than 40 registers and 12 CTAs
+template <int LGM>
+__global__ void __launch_bounds__(FFT_CTA, 16) k_dct2_f(Dct2ArgsF a) {
   extern __shared__ float4 sm4[];
-  const int n = a.itot, m = n / 2, ld = a.ld;
-  const int T = sh.T;
-  const int rloc = threadIdx.x >> sh.lgT, t = threadIdx.x & (T - 1);
-  const int jr = blockIdx.x * sh.rows + rloc;
+  constexpr int m = 1 << LGM, n = 2 * m, T = m / 8, ROWS = FFT_CTA / T;
+  const int ld = a.ld;
+  const int rloc = threadIdx.x >> (LGM - 3), t = threadIdx.x & (T - 1);
+  const int jr = blockIdx.x * ROWS + rloc;
   const bool live = jr < a.jtot;
   const int j = 1 + jr;
   CF *buf = reinterpret_cast<CF *>(sm4) + rloc * (m + m / 8);
@@ -1349,7 +1368,7 @@ __global__ void __launch_bounds__(FFT_CTA, 16) k_dct2_f(Dct2ArgsF a, FftShape sh
   CF v[8];
 #pragma unroll
   for (int u = 0; u < 8; u++) v[u] = buf[t + u * T];   // z[s] = v[2s] + i v[2s+1], unpadded
-  fft_row_f<-1>(buf, v, t, T, m, a.tw);
+  fft_row_f<-1, m>(buf, v, t, a.tw);
   if (!live) return;
   float *out = a.q + (size_t)jr * ld;
 #pragma unroll 2
@@ -1399,20 +1418,21 @@ struct Dct3ArgsF {
   const float *iface;    // solved interface values [block][k], rounded to float by the reduced solve
   const float *g;        // left responses of the block interior [r][k]
   float *psi;            // output (uy layout, with halo rows and ghost columns)
-  const float2 *tw, *rot, *wn;
+  const float2 *tw, *rot, *wn;   // tw: twiddles in pass order (pass_twiddles)
   float scale;           // 1/(2 itot)
   int itot, jtot, ld, blk, nblk;
 };
 
 // block reconstruction + single-precision DCT-III + scaling of rows (compute_potential.c:120-134)
-// capped at 48 registers for 10 resident CTAs per SM: measured faster than 53 registers
-// and 9 CTAs
-__global__ void __launch_bounds__(FFT_CTA, 10) k_dct3_f(Dct3ArgsF a, FftShape sh) {
+// (itot = 2 m, m = 2^LGM); capped at 48 registers for 10 resident CTAs per SM: measured
+// faster than 53 registers and 9 CTAs
+template <int LGM>
+__global__ void __launch_bounds__(FFT_CTA, 10) k_dct3_f(Dct3ArgsF a) {
   extern __shared__ float4 sm4[];
-  const int n = a.itot, m = n / 2, ld = a.ld;
-  const int T = sh.T;
-  const int rloc = threadIdx.x >> sh.lgT, t = threadIdx.x & (T - 1);
-  const int jr = blockIdx.x * sh.rows + rloc;
+  constexpr int m = 1 << LGM, n = 2 * m, T = m / 8, ROWS = FFT_CTA / T;
+  const int ld = a.ld;
+  const int rloc = threadIdx.x >> (LGM - 3), t = threadIdx.x & (T - 1);
+  const int jr = blockIdx.x * ROWS + rloc;
   const bool live = jr < a.jtot;
   const int j = 1 + jr;
   CF *buf = reinterpret_cast<CF *>(sm4) + rloc * (m + m / 8);
@@ -1453,7 +1473,7 @@ __global__ void __launch_bounds__(FFT_CTA, 10) k_dct3_f(Dct3ArgsF a, FftShape sh
     const CF dif = cf_mul(cf_sub(w0, w1), wn);
     v[u] = CF{sum.re - dif.im, sum.im + dif.re};
   }
-  fft_row_f<1>(buf, v, t, T, m, a.tw);
+  fft_row_f<1, m>(buf, v, t, a.tw);
   if (!live) return;
   float *prow = a.psi + (size_t)j * ld;
   for (int i = t; i < n; i += T) {
@@ -1494,6 +1514,26 @@ FftShape fftr_shape(int m) {
   return s;
 }
 size_t fftr_smem(int m, int rows) { return sizeof(float4) * (size_t)rows * (m + m / FFT_V); }
+
+// The twiddles w^e (w = exp(-2 pi i / m), tw[e] for e < m) of the single-precision
+// transforms in the order fft_passes_f reads them: for each radix-8 pass of length
+// L = 8, 64, ... (8 L <= m) and each butterfly k < L the seven values w^(u k m / 8L),
+// u = 1..7; then, when the last pass has radix R = m / L > 1, for each butterfly j < L
+// the R - 1 values w^(u j). Values are copied, not recomputed: the transforms read the
+// same floats as from tw itself.
+std::vector<float2> pass_twiddles(const std::vector<float2> &tw, int m) {
+  std::vector<float2> out;
+  int L = 8;
+  for (; L * 8 <= m; L *= 8)
+    for (int k = 0; k < L; k++)
+      for (int u = 1; u < 8; u++) out.push_back(tw[(size_t)u * k * (m / (8 * L))]);
+  const int R = m / L;
+  if (R > 1)
+    for (int j = 0; j < L; j++)
+      for (int u = 1; u < R; u++) out.push_back(tw[(size_t)u * j]);
+  if (out.empty()) out.push_back(tw[0]);   // m = 8: one radix-8 stage, no twiddles
+  return out;
+}
 
 bool factorize(int m, int *fac, int *nfac) {
   int k = 0;
@@ -1583,13 +1623,20 @@ int poisson_init(eif_ctx *c) {
     if ((rc = df_table(n, -PI / (2.L * n), &pp.rot_f))) return rc;
     if ((rc = df_table(n, -2.L * PI / n, &pp.wn_f))) return rc;
     // single-precision twiddles of the refined solve, rounded from long double
-    auto f_table = [&](int len, long double step, float2 **dst) -> int {
+    auto f_values = [&](int len, long double step) {
       std::vector<float2> v(len);
       for (int k = 0; k < len; k++) v[k] = make_float2((float)cosl(step * k), (float)sinl(step * k));
+      return v;
+    };
+    auto f_table = [&](int len, long double step, float2 **dst) -> int {
+      const std::vector<float2> v = f_values(len, step);
       EIF_CK(c, up_load((void **)dst, v.data(), sizeof(float2) * len));
       return EIF_OK;
     };
-    if ((rc = f_table(pp.m, -2.L * PI / pp.m, &pp.tw2))) return rc;
+    {
+      const std::vector<float2> tw = pass_twiddles(f_values(pp.m, -2.L * PI / pp.m), pp.m);
+      EIF_CK(c, up_load((void **)&pp.tw2, tw.data(), sizeof(float2) * tw.size()));
+    }
     if ((rc = f_table(n, -PI / (2.L * n), &pp.rot2))) return rc;
     if ((rc = f_table(n, -2.L * PI / n, &pp.wn2))) return rc;
   }
@@ -1789,12 +1836,30 @@ static int reduced_solve(eif_ctx *c, double *iface, double *first, float *iface_
   return EIF_OK;
 }
 
+// one launch of the single-precision DCT-II (a) or DCT-III (b) instance for m = 2^lgm
+static void launch_dct_f(int lgm, unsigned blocks, size_t smem, cudaStream_t s, const Dct2ArgsF *a,
+                         const Dct3ArgsF *b) {
+#define EIF_DCT_F_CASE(L)                                          \
+  case L:                                                          \
+    if (a) k_dct2_f<L><<<blocks, FFT_CTA, smem, s>>>(*a);          \
+    else k_dct3_f<L><<<blocks, FFT_CTA, smem, s>>>(*b);            \
+    break;
+  switch (lgm) {
+    EIF_DCT_F_CASE(3) EIF_DCT_F_CASE(4) EIF_DCT_F_CASE(5) EIF_DCT_F_CASE(6)
+    EIF_DCT_F_CASE(7) EIF_DCT_F_CASE(8) EIF_DCT_F_CASE(9) EIF_DCT_F_CASE(10)
+    default: break;
+  }
+#undef EIF_DCT_F_CASE
+}
+
 // the mixed form's Poisson solve: two single-precision passes, the second on the
 // double-float residual of the first (see k_dct2_f); psi1, psi2 into the psi buffer
 static int potential_refined(eif_ctx *c, int rk, bool with_ibm) {
   PoissonPlan &pp = c->pp;
   const int n = c->itot, jt = c->jtot;
   const FftShape sh = fftr_shape(pp.m);
+  static_assert(FFT_V * FFT_CTA == 1 << 10, "instances of the single-precision transforms: m = 2^3 .. 2^10");
+  const int lgm = sh.lgT + 3;   // m = 8 T, T = 2^lgT
   const size_t smem = sizeof(CF) * (size_t)sh.rows * (pp.m + pp.m / 8);
   auto dfpair = [](double v) {
     const float hi = (float)v;
@@ -1822,7 +1887,7 @@ static int potential_refined(eif_ctx *c, int rk, bool with_ibm) {
     a.itot = n; a.jtot = jt; a.ld = c->ld; a.with_ibm = with_ibm ? 1 : 0; a.rk = rk;
     {
       EIF_PROF(c, "poisson_dct2", 1);
-      k_dct2_f<<<blocks, sh.T * sh.rows, smem, c->stream>>>(a, sh);
+      launch_dct_f(lgm, blocks, smem, c->stream, &a, nullptr);
       EIF_LAUNCH_CK(c);
     }
     {
@@ -1845,7 +1910,7 @@ static int potential_refined(eif_ctx *c, int rk, bool with_ibm) {
     b.scale = (float)(1. / (2. * n));
     b.itot = n; b.jtot = jt; b.ld = c->ld; b.blk = pp.blk; b.nblk = pp.nblk;
     EIF_PROF(c, "poisson_dct3", 1);
-    k_dct3_f<<<blocks, sh.T * sh.rows, smem, c->stream>>>(b, sh);
+    launch_dct_f(lgm, blocks, smem, c->stream, nullptr, &b);
     EIF_LAUNCH_CK(c);
   }
   return EIF_OK;
