@@ -157,11 +157,15 @@ namespace eif_xfer {
 // device pitch in the same pass: one streaming pass over the interconnect, faster
 // than the copy engines' pitched copies (measured 208 vs 166 GB/s host to device,
 // 192 vs 153 GB/s device to host on GB300). Pageable arrays use cudaMemcpy2DAsync.
-__global__ void k_rows_in(const double *__restrict__ h, double *__restrict__ d, int w, int rows, int ld) {
+// s (velocities of the mixed form, else null): the values rounded to float as well
+__global__ void k_rows_in(const double *__restrict__ h, double *__restrict__ d, float *__restrict__ s, int w,
+                          int rows, int ld) {
   const size_t n = (size_t)w * rows;
   for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
     const size_t r = t / (unsigned)w, col = t - r * w;
-    d[r * ld + col] = h[t];
+    const double v = h[t];
+    d[r * ld + col] = v;
+    if (s) s[r * ld + col] = eifd::d2f(v);
   }
 }
 __global__ void k_rows_out(const double *__restrict__ d, double *__restrict__ h, int w, int rows, int ld) {
@@ -198,14 +202,16 @@ void *mapped(const void *host) {
   return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
 }
 
-int rows_in(eif_ctx *c, double *dst, const double *host, int w, int rows) {
+// shadow (velocities of the mixed form, else null): the float copy of dst, kept with it
+int rows_in(eif_ctx *c, double *dst, const double *host, int w, int rows, float *shadow = nullptr) {
   if (const double *hd = static_cast<const double *>(mapped(host))) {
-    k_rows_in<<<c->sms * 4, 512, 0, c->stream>>>(hd, dst, w, rows, c->ld);
+    k_rows_in<<<c->sms * 4, 512, 0, c->stream>>>(hd, dst, shadow, w, rows, c->ld);
     EIF_LAUNCH_CK(c);
     return EIF_OK;
   }
   EIF_CK(c, cudaMemcpy2DAsync(dst, sizeof(double) * c->ld, host, sizeof(double) * w, sizeof(double) * w, rows,
                               cudaMemcpyHostToDevice, c->stream));
+  if (shadow) return launch_round_to_float(c, dst, shadow, c->nfield);
   return EIF_OK;
 }
 
@@ -451,7 +457,8 @@ int eif_create(const eif_config_t *cfg, eif_ctx **out) {
     CK_CREATE(cudaMemset(*f, 0, sizeof(double) * c->nfield));
   }
   if (cfg->precision == EIF_PREC_MIXED) {
-    float **ffields[] = {&c->sxf[0], &c->sxf[1], &c->syf[0], &c->syf[1]};
+    float **ffields[] = {&c->sxf[0], &c->sxf[1], &c->syf[0], &c->syf[1], &c->uxf[0], &c->uxf[1], &c->uyf[0],
+                         &c->uyf[1]};
     for (float **f : ffields) {
       CK_CREATE(cudaMalloc((void **)f, sizeof(float) * c->nfield));
       CK_CREATE(cudaMemset(*f, 0, sizeof(float) * c->nfield));
@@ -504,7 +511,7 @@ int eif_destroy(eif_ctx *c) {
   if (c->d_inc) cudaFree(c->d_inc);
   graphs_free(c);
   float *fptrs[] = {c->rdxf_f, c->rdxc_f, c->cxm_f, c->cxp_f, c->cym_f, c->cyp_f, c->sxf[0], c->sxf[1], c->syf[0],
-                    c->syf[1]};
+                    c->syf[1], c->uxf[0], c->uxf[1], c->uyf[0], c->uyf[1]};
   for (float *p : fptrs) if (p) cudaFree(p);
   if (c->d_flags) cudaFree(c->d_flags);
   if (c->d_check) cudaFree(c->d_check);
@@ -543,8 +550,8 @@ int eif_push_fluid(eif_ctx *c, const double *ux, const double *uy, const double 
   if (!c || !ux || !uy || !p) return EIF_ERR_ARG;
   const int rows = c->jtot + 2;
   int rc;
-  if ((rc = rows_in(c, c->ux[c->cur], ux, c->itot + 1, rows))) return rc;
-  if ((rc = rows_in(c, c->uy[c->cur], uy, c->itot + 2, rows))) return rc;
+  if ((rc = rows_in(c, c->ux[c->cur], ux, c->itot + 1, rows, c->uxf[c->cur]))) return rc;
+  if ((rc = rows_in(c, c->uy[c->cur], uy, c->itot + 2, rows, c->uyf[c->cur]))) return rc;
   if ((rc = rows_in(c, c->p, p, c->itot + 2, rows))) return rc;
   if (c->src_nonfinite) {
     for (double *f : {c->sxa[0], c->sxa[1], c->sya[0], c->sya[1]})

@@ -147,6 +147,10 @@ struct eif_ctx {
   } uni_x;
   float2 *rdxc_df = nullptr;    // 1/dxc as double-float pairs (hi, lo)
   float *sxf[2], *syf[2];       // RK explicit terms of the mixed form
+  // mixed form: ux, uy rounded to float (eifd::d2f), entry by entry, the velocities the
+  // single-precision immersed-boundary kernels read; written with the doubles by the
+  // predictor and the projection, and refreshed whole after the boundary conditions
+  float *uxf[2] = {nullptr, nullptr}, *uyf[2] = {nullptr, nullptr};
   // host copies of the metrics
   double *h_xf, *h_xc, *h_dxf, *h_dxc, *h_yf, *h_yc;
   eif::PoissonPlan pp;
@@ -307,6 +311,8 @@ int launch_decide_dt(eif_ctx *c);
 int launch_divergence(eif_ctx *c, double *divmax, double *divsum);
 int launch_f2d_copy(eif_ctx *c, const float *in, double *out, size_t n);
 int launch_d2f_copy(eif_ctx *c, const double *in, float *out, size_t n);
+// out = eifd::d2f(in) element by element (the float copies of the mixed form's velocities)
+int launch_round_to_float(eif_ctx *c, const double *in, float *out, size_t n);
 int launch_coef(eif_ctx *c);
 // the tensor-copy predictor's launch shapes (a host query, before any graph capture)
 int predictor_prepare(eif_ctx *c);

@@ -33,25 +33,31 @@ constexpr int TY_DEFAULT = 8;
 // kind 0: ux-like (halo i=2..itot, walls i=1,itot+1 set to 0)
 // kind 1: uy-like (halo i=1..itot, walls i=0,itot+1 set to the wall velocity)
 // kind 2: p-like  (halo i=1..itot, Neumann copies at i=0,itot+1 incl. halo rows)
-__global__ void k_bc(double *__restrict__ a, int kind, int itot, int jtot, int ld, double w0, double w1) {
+// s (velocities of the mixed form, else null): the field rounded to float, kept with it
+__global__ void k_bc(double *__restrict__ a, float *__restrict__ s, int kind, int itot, int jtot, int ld, double w0,
+                     double w1) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  auto put = [&](int idx, double v) {
+    a[idx] = v;
+    if (s) s[idx] = eifd::d2f(v);
+  };
   // halo rows
   const int ilo = kind == 0 ? 2 : 1;
   const int ihi = itot;
   const int col = kind == 0 ? -1 : 0;  // ux stores UX(i) at i-1
   if (t >= ilo && t <= ihi) {
-    a[0 * ld + t + col] = a[jtot * ld + t + col];
-    a[(jtot + 1) * ld + t + col] = a[1 * ld + t + col];
+    put(0 * ld + t + col, a[jtot * ld + t + col]);
+    put((jtot + 1) * ld + t + col, a[1 * ld + t + col]);
   }
   // wall columns, rows 0..jtot+1
   if (t <= jtot + 1) {
     const int j = t;
     if (kind == 0) {
-      a[ux_idx(1, j, ld)] = 0.;
-      a[ux_idx(itot + 1, j, ld)] = 0.;
+      put(ux_idx(1, j, ld), 0.);
+      put(ux_idx(itot + 1, j, ld), 0.);
     } else if (kind == 1) {
-      a[uy_idx(0, j, ld)] = w0;
-      a[uy_idx(itot + 1, j, ld)] = w1;
+      put(uy_idx(0, j, ld), w0);
+      put(uy_idx(itot + 1, j, ld), w1);
     } else {
       // source row of the (already periodic) value: halo rows mirror rows jtot and 1
       const int js = j == 0 ? jtot : (j == jtot + 1 ? 1 : j);
@@ -162,6 +168,7 @@ struct PredArgsF {
   const float *sxb, *syb;
   float *sxa, *sya;
   double *uxn, *uyn;
+  float *uxfn, *uyfn;  // the new velocities rounded to float (eifd::d2f)
   const float *rdxf, *rdxc, *cxm, *cxp, *cym, *cyp;
   const float *coef;   // alpha dt, beta dt, gamma dt of this stage
   float rRe, rdy, ext;
@@ -208,9 +215,11 @@ __device__ __forceinline__ void pred_mixed_cell(const PredArgsF &a, const float2
     const int c = j * ld + (i - 1);
     a.sxa[c] = A;
     const double un_ = u_own + eifd::f2d(adt * A + bdt * Bx + gdt * pre);
+    const float unf = eifd::d2f(un_);
     a.uxn[c] = un_;
-    if (j == 1) a.uxn[c + jtot * ld] = un_;
-    if (j == jtot) a.uxn[c - jtot * ld] = un_;
+    a.uxfn[c] = unf;
+    if (j == 1) { a.uxn[c + jtot * ld] = un_; a.uxfn[c + jtot * ld] = unf; }
+    if (j == jtot) { a.uxn[c - jtot * ld] = un_; a.uxfn[c - jtot * ld] = unf; }
   }
   {
     const float2 v0 = tuy[y][x], vw = tuy[y][x - 1], ve = tuy[y][x + 1], vs = tuy[y - 1][x], vn = tuy[y + 1][x];
@@ -235,9 +244,11 @@ __device__ __forceinline__ void pred_mixed_cell(const PredArgsF &a, const float2
     const int c = j * ld + i;
     a.sya[c] = A;
     const double vn_ = v_own + eifd::f2d(adt * A + bdt * By + gdt * pre);
+    const float vnf = eifd::d2f(vn_);
     a.uyn[c] = vn_;
-    if (j == 1) a.uyn[c + jtot * ld] = vn_;
-    if (j == jtot) a.uyn[c - jtot * ld] = vn_;
+    a.uyfn[c] = vnf;
+    if (j == 1) { a.uyn[c + jtot * ld] = vn_; a.uyfn[c + jtot * ld] = vnf; }
+    if (j == jtot) { a.uyn[c - jtot * ld] = vn_; a.uyfn[c - jtot * ld] = vnf; }
   }
 }
 
@@ -491,6 +502,7 @@ __global__ void __launch_bounds__(TX *TY) k_correct(CorrArgs a) {
 // precision field values, summed exactly) are formed in double-float arithmetic.
 struct CorrArgsDF {
   double *ux, *uy, *p;
+  float *uxf, *uyf;         // the velocities rounded to float (eifd::d2f), kept with ux, uy
   const double *psi;
   // psi as the float pair psi1 + psi2 of the refined solve (psi1 at psi, psi2 at
   // psi1 + psi2_off floats), or null: psi in double
@@ -562,9 +574,11 @@ __global__ void __launch_bounds__(TX *TY, 48 / TY) k_correct_df(CorrArgsDF a) {
       inc = df_add_nw(inc, df_neg(g));
     }
     const double u = u_old + df_to_double(inc);
+    const float uf = eifd::d2f(u);
     a.ux[c] = u;
-    if (j == 1) a.ux[c + jtot * ld] = u;
-    if (j == jtot) a.ux[c - jtot * ld] = u;
+    a.uxf[c] = uf;
+    if (j == 1) { a.ux[c + jtot * ld] = u; a.uxf[c + jtot * ld] = uf; }
+    if (j == jtot) { a.ux[c - jtot * ld] = u; a.uxf[c - jtot * ld] = uf; }
   }
   if (vel) {
     DF inc{0.f, 0.f};
@@ -575,9 +589,11 @@ __global__ void __launch_bounds__(TX *TY, 48 / TY) k_correct_df(CorrArgsDF a) {
       inc = df_add_nw(inc, df_neg(g));
     }
     const double v = v_old + df_to_double(inc);
+    const float vf = eifd::d2f(v);
     a.uy[cy] = v;
-    if (j == 1) a.uy[cy + jtot * ld] = v;
-    if (j == jtot) a.uy[cy - jtot * ld] = v;
+    a.uyf[cy] = vf;
+    if (j == 1) { a.uy[cy + jtot * ld] = v; a.uyf[cy + jtot * ld] = vf; }
+    if (j == jtot) { a.uy[cy - jtot * ld] = v; a.uyf[cy - jtot * ld] = vf; }
   }
   if (a.with_pressure) {
     // psi1 + psi2 as a double without the FP64 pipe (bit-identical to the FP64 addition;
@@ -857,10 +873,21 @@ static void launch_tiled(void (*k4)(Args), void (*k8)(Args), void (*k16)(Args), 
   }
 }
 
+// out[t] = eifd::d2f(in[t]): the rounding the single-precision kernels apply to the doubles
+__global__ void k_round_to_float(const double *__restrict__ in, float *__restrict__ out, size_t n) {
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
+    out[t] = eifd::d2f(in[t]);
+}
+int launch_round_to_float(eif_ctx *c, const double *in, float *out, size_t n) {
+  k_round_to_float<<<c->sms * 4, 256, 0, c->stream>>>(in, out, n);
+  EIF_LAUNCH_CK(c);
+  return EIF_OK;
+}
+
 int launch_bc_p_like(eif_ctx *c, double *a) {
   EIF_PROF(c, "boundaries", 1);
   const int n = (c->itot > c->jtot ? c->itot : c->jtot) + 2;
-  k_bc<<<(n + 255) / 256, 256, 0, c->stream>>>(a, 2, c->itot, c->jtot, c->ld, 0., 0.);
+  k_bc<<<(n + 255) / 256, 256, 0, c->stream>>>(a, nullptr, 2, c->itot, c->jtot, c->ld, 0., 0.);
   EIF_LAUNCH_CK(c);
   return EIF_OK;
 }
@@ -869,11 +896,11 @@ int launch_boundaries(eif_ctx *c) {
   EIF_PROF(c, "boundaries", 5);
   const int n = (c->itot > c->jtot ? c->itot : c->jtot) + 2;
   for (int b = 0; b < 2; b++) {
-    k_bc<<<(n + 255) / 256, 256, 0, c->stream>>>(c->ux[b], 0, c->itot, c->jtot, c->ld, 0., 0.);
-    k_bc<<<(n + 255) / 256, 256, 0, c->stream>>>(c->uy[b], 1, c->itot, c->jtot, c->ld, c->cfg.uy_wall[0],
-                                                 c->cfg.uy_wall[1]);
+    k_bc<<<(n + 255) / 256, 256, 0, c->stream>>>(c->ux[b], c->uxf[b], 0, c->itot, c->jtot, c->ld, 0., 0.);
+    k_bc<<<(n + 255) / 256, 256, 0, c->stream>>>(c->uy[b], c->uyf[b], 1, c->itot, c->jtot, c->ld,
+                                                 c->cfg.uy_wall[0], c->cfg.uy_wall[1]);
   }
-  k_bc<<<(n + 255) / 256, 256, 0, c->stream>>>(c->p, 2, c->itot, c->jtot, c->ld, 0., 0.);
+  k_bc<<<(n + 255) / 256, 256, 0, c->stream>>>(c->p, nullptr, 2, c->itot, c->jtot, c->ld, 0., 0.);
   EIF_LAUNCH_CK(c);
   return EIF_OK;
 }
@@ -946,6 +973,8 @@ static int launch_predictor_mixed(eif_ctx *c, int rk) {
   a.sya = c->syf[c->scur];
   a.uxn = c->ux[1 - c->cur];
   a.uyn = c->uy[1 - c->cur];
+  a.uxfn = c->uxf[1 - c->cur];
+  a.uyfn = c->uyf[1 - c->cur];
   a.rdxf = c->rdxf_f; a.rdxc = c->rdxc_f;
   a.cxm = c->cxm_f; a.cxp = c->cxp_f; a.cym = c->cym_f; a.cyp = c->cyp_f;
   (void)k;
@@ -1008,6 +1037,8 @@ static int launch_corr(eif_ctx *c, int rk, int with_ibm, int with_proj, int with
     CorrArgsDF a;
     a.ux = c->ux[c->cur];
     a.uy = c->uy[c->cur];
+    a.uxf = c->uxf[c->cur];
+    a.uyf = c->uyf[c->cur];
     a.p = c->p;
     a.psi = c->psi;
     a.psi1 = c->psi_pair ? reinterpret_cast<const float *>(c->psi) : nullptr;

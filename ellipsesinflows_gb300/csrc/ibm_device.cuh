@@ -415,6 +415,9 @@ __device__ __forceinline__ int memo_word(int lane) { return lane < 6 ? lane : la
 struct WorkArgs {
   const double *P;
   const double *ux, *uy, *xc, *yc, *dt;
+  // mixed form: ux, uy rounded to float (eifd::d2f), kept with them by the kernels that
+  // write the velocities; the single-precision bodies read these
+  const float *uxf, *uyf;
   const int *box, *off;
   double *partial;   // 3 per chunk
   double2 *wbuf;     // CHUNK per chunk (exchange only)
@@ -690,7 +693,7 @@ __device__ __forceinline__ void ibm_work_f_tasks(const WorkArgs &a, int wmode, i
     unsigned near_mask[2];
     // the cells of the task and their field values: loaded before the geometry, so that
     // the loads are in flight while the weights are evaluated
-    double fuw[2], fue[2], fvs[2], fvn[2];
+    float fuw[2], fue[2], fvs[2], fvn[2];
 #pragma unroll
     for (int half = 0; half < CHUNK / 32; half++) {
       const int i = (task ? t.ib : 1) + half * 32 + lane;
@@ -700,12 +703,12 @@ __device__ __forceinline__ void ibm_work_f_tasks(const WorkArgs &a, int wmode, i
              EIF_CHK(a.bd.rec, j * ld + (i - 1), a.bd.field, 56);
       }
       cin[half] = in;
-      fuw[half] = fue[half] = fvs[half] = fvn[half] = 0.;
+      fuw[half] = fue[half] = fvs[half] = fvn[half] = 0.f;
       if (in) {
-        fuw[half] = __ldg(a.ux + j * ld + (i - 1));
-        fue[half] = __ldg(a.ux + j * ld + i);
-        fvs[half] = __ldg(a.uy + j * ld + i);
-        fvn[half] = __ldg(a.uy + (j + 1) * ld + i);
+        fuw[half] = __ldg(a.uxf + j * ld + (i - 1));
+        fue[half] = __ldg(a.uxf + j * ld + i);
+        fvs[half] = __ldg(a.uyf + j * ld + i);
+        fvn[half] = __ldg(a.uyf + (j + 1) * ld + i);
       }
     }
     // the memo's weights for this task when the particle's geometry words and boxes are
@@ -803,8 +806,8 @@ __device__ __forceinline__ void ibm_work_f_tasks(const WorkArgs &a, int wmode, i
       const bool live = a.mode == 0 ? th_ != -1.f : fabsf(th_) != 1.f;
       if (cin[half] && live) {
         const float X = cX[half], th = th_;
-        const float uxs = eifd::d2f(fuw[half]) + eifd::d2f(fue[half]);
-        const float uys = eifd::d2f(fvs[half]) + eifd::d2f(fvn[half]);
+        const float uxs = fuw[half] + fue[half];
+        const float uys = fvs[half] + fvn[half];
         if (a.mode == 0) {
           const float w = 0.5f * (1.f + th);
           const float valx = w * 0.5f * uxs * dxdy;
@@ -895,7 +898,7 @@ __device__ __forceinline__ void ibm_sum_f_tasks(const WorkArgs &a, int first, in
     // warp has all eight loads of the task in flight at once
     bool live[2];
     float thv[2];
-    double uw[2], ue[2], vs[2], vn[2];
+    float uw[2], ue[2], vs[2], vn[2];
 #pragma unroll
     for (int half = 0; half < CHUNK / 32; half++) {
       const int i = (task ? t.ib : 1) + half * 32 + lane;
@@ -908,12 +911,12 @@ __device__ __forceinline__ void ibm_sum_f_tasks(const WorkArgs &a, int first, in
       thv[half] = th;
       // cells of weight exactly zero (inertia: far outside; exchange: any far cell) are skipped
       live[half] = in && (a.mode == 0 ? th != -1.f : fabsf(th) != 1.f);
-      uw[half] = ue[half] = vs[half] = vn[half] = 0.;
+      uw[half] = ue[half] = vs[half] = vn[half] = 0.f;
       if (live[half]) {
-        uw[half] = __ldg(a.ux + j * ld + (i - 1));
-        ue[half] = __ldg(a.ux + j * ld + i);
-        vs[half] = __ldg(a.uy + j * ld + i);
-        vn[half] = __ldg(a.uy + (j + 1) * ld + i);
+        uw[half] = __ldg(a.uxf + j * ld + (i - 1));
+        ue[half] = __ldg(a.uxf + j * ld + i);
+        vs[half] = __ldg(a.uyf + j * ld + i);
+        vn[half] = __ldg(a.uyf + (j + 1) * ld + i);
       }
     }
     float sacc0 = 0.f, sacc1 = 0.f, sacc2 = 0.f;
@@ -925,8 +928,8 @@ __device__ __forceinline__ void ibm_sum_f_tasks(const WorkArgs &a, int first, in
       const float th = thv[half];
       if (live[half]) {
         const float X = ((float)(i - i0) - gx) * dxf;
-        const float uxs = eifd::d2f(uw[half]) + eifd::d2f(ue[half]);
-        const float uys = eifd::d2f(vs[half]) + eifd::d2f(vn[half]);
+        const float uxs = uw[half] + ue[half];
+        const float uys = vs[half] + vn[half];
         if (a.mode == 0) {
           const float w = 0.5f * (1.f + th);
           const float valx = w * 0.5f * uxs * dxdy;
@@ -1089,6 +1092,7 @@ inline BoxArgs box_args(const eif_ctx *c, bool use_increment) {
 inline WorkArgs work_args(const eif_ctx *c, int mode, int cn) {
   WorkArgs w;
   w.P = c->P; w.ux = c->ux[c->cur]; w.uy = c->uy[c->cur]; w.xc = c->xc; w.yc = c->yc; w.dt = c->d_scal;
+  w.uxf = c->uxf[c->cur]; w.uyf = c->uyf[c->cur];
   w.box = c->box; w.off = c->chunk_off; w.partial = c->partial; w.wbuf = reinterpret_cast<double2 *>(c->wbuf);
   w.pcap = c->pcap; w.np = c->np; w.ld = c->ld; w.mode = mode; w.cn = cn;
   w.dx = c->dx; w.dy = c->dy; w.ly = c->ly; w.h = c->dx < c->dy ? c->dx : c->dy;

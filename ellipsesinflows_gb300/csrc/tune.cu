@@ -75,7 +75,7 @@ int tune_tiles(eif_ctx *c) {
   std::vector<double **> dfields = {&c->ux[0], &c->ux[1], &c->uy[0], &c->uy[1], &c->p, &c->psi,
                                     &c->sxa[0], &c->sxa[1], &c->sya[0], &c->sya[1]};
   std::vector<float **> ffields;
-  if (mixed) ffields = {&c->sxf[0], &c->sxf[1], &c->syf[0], &c->syf[1]};
+  if (mixed) ffields = {&c->sxf[0], &c->sxf[1], &c->syf[0], &c->syf[1], &c->uxf[0], &c->uxf[1], &c->uyf[0], &c->uyf[1]};
   std::vector<double *> dkeep, dscr;
   std::vector<float *> fkeep, fscr;
   const int cur = c->cur, scur = c->scur;
