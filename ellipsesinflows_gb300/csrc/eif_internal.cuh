@@ -212,6 +212,8 @@ struct eif_ctx {
   int4 *tdesc;                  // task table: particle, row, columns and image of every chunk
   // weights of the last indicator evaluation in a sub-iteration loop (mixed form), with
   // the particles' geometry words, boxes and first tasks (WeightMemo in ibm_device.cuh)
+  // tasks of a stage start the memo did not serve: [0] count, then their numbers
+  int *memo_miss = nullptr;
   float *memo_w = nullptr, *memo_pf = nullptr;
   int *memo_box = nullptr, *memo_off = nullptr, *memo_valid = nullptr;
   bool memo_on = true;          // false: EIF_NO_MEMO set, every evaluation computes

@@ -68,6 +68,11 @@ __global__ void __launch_bounds__(256, 3) k_ibm_work_f(WorkArgs a) {
                          slot_buf[threadIdx.x >> 5]);
 }
 
+// the stage start's evaluation at X (mixed form): memo-served tasks, the rest listed
+__global__ void __launch_bounds__(256, 4) k_ibm_memo_f(WorkArgs a) {
+  ibm_memo_f_tasks<true>(a, (blockIdx.x * blockDim.x + threadIdx.x) >> 5, (gridDim.x * blockDim.x) >> 5);
+}
+
 __global__ void __launch_bounds__(256, 4) k_ibm_sum_f(WorkArgs a) {
   if (a.gate && ((a.gate == 1) != (*a.iter == 0u))) return;
   ibm_sum_f_tasks<true>(a, (blockIdx.x * blockDim.x + threadIdx.x) >> 5, (gridDim.x * blockDim.x) >> 5);
@@ -380,6 +385,7 @@ int ibm_reserve(eif_ctx *c, size_t chunks) {
     EIF_CK(c, cudaMalloc((void **)&c->memo_off, sizeof(int) * c->np));
     EIF_CK(c, cudaMalloc((void **)&c->memo_valid, sizeof(int)));
     EIF_CK(c, cudaMemset(c->memo_valid, 0, sizeof(int)));
+    EIF_CK(c, cudaMalloc((void **)&c->memo_miss, sizeof(int) * ((size_t)chunks + 1)));
   }
   return EIF_OK;
 }
@@ -396,9 +402,11 @@ void ibm_free(eif_ctx *c) {
   if (c->band_counts) cudaFree(c->band_counts);
   if (c->band_marks) cudaFree(c->band_marks);
   if (c->edesc) cudaFree(c->edesc);
-  for (void *m : {(void *)c->memo_w, (void *)c->memo_pf, (void *)c->memo_box, (void *)c->memo_off, (void *)c->memo_valid})
+  for (void *m : {(void *)c->memo_w, (void *)c->memo_pf, (void *)c->memo_box, (void *)c->memo_off, (void *)c->memo_valid,
+                  (void *)c->memo_miss})
     if (m) cudaFree(m);
   c->memo_w = nullptr; c->memo_pf = nullptr; c->memo_box = nullptr; c->memo_off = nullptr; c->memo_valid = nullptr;
+  c->memo_miss = nullptr;
   c->band_lists = nullptr; c->band_counts = nullptr; c->band_marks = nullptr; c->edesc = nullptr;
   c->box = nullptr; c->chunk_off = nullptr; c->partial = nullptr; c->wbuf = nullptr; c->wcache = nullptr;
   c->weights_x_valid = false;
@@ -475,8 +483,19 @@ static int launch_work(eif_ctx *c, int mode, int cn) {
     const bool geometry = w.wmode != 2 && !(mixed && c->in_loop);
     EIF_PROF(c, w.memo_mode == 1 ? "ibm_stage_start" :
                 (geometry ? "ibm_indicator" : (mode == 0 ? "ibm_inertia" : "ibm_exchange")),
-             mixed && c->in_loop ? 2 : 1);
-    if (mixed && c->in_loop) {
+             (mixed && c->in_loop) || w.memo_mode == 1 ? 2 : 1);
+    if (w.memo_mode == 1) {
+      // the stage start: the memo-served tasks in the light kernel (sums-kernel
+      // registers), then the full evaluation of the tasks it listed as not served
+      EIF_CK(c, cudaMemsetAsync(c->memo_miss, 0, sizeof(int), c->stream));
+      WorkArgs wm = w, wf = w;
+      wm.miss = c->memo_miss;
+      wf.only = c->memo_miss;
+      wf.memo_mode = 0;
+      k_ibm_memo_f<<<c->sms * c->ibm_ctas_per_sm[2], 256, 0, c->stream>>>(wm);
+      EIF_LAUNCH_CK(c);
+      k_ibm_work_f<<<blocks, 256, 0, c->stream>>>(wf);
+    } else if (mixed && c->in_loop) {
       // first sub-iteration: cached weights; later ones: full evaluation (decided on the device)
       WorkArgs w1 = w, w2 = w;
       w1.wmode = 2; w1.gate = 1;

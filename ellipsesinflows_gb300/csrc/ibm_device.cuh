@@ -445,6 +445,11 @@ struct WorkArgs {
   // particle's geometry and boxes are the memo's; 2 stores computed weights in it
   WeightMemo memo;
   int memo_mode;
+  // the stage start of the mixed form (ibm_memo_f_tasks): miss[0] counts the tasks the
+  // memo did not serve, miss[1 ..] lists them; with `only` set, ibm_work_f_tasks
+  // evaluates just the tasks listed there (same layout)
+  int *miss;
+  const int *only;
   Bounds bd;
 };
 
@@ -653,11 +658,28 @@ __device__ __forceinline__ float indicator_f(const EllF &e, float x_, float y_, 
   return f0 > 0.f ? th : -th;
 }
 
+// One cell's contributions to the inertia integrals (inertia.c:9-70) in single precision,
+// with every rounding explicit: the bodies that form these sums (the full evaluation, the
+// memo-served stage start, the cached-weight sums) then give the same bits in whatever
+// kernel they are compiled, whichever products the compiler would fuse there.
+__device__ __forceinline__ void inertia_cell_f(float th, float X, float Y, float uxs, float uys, float dxdy,
+                                               float rpm, float rpim, float &s0, float &s1, float &s2) {
+  const float w = __fmul_rn(0.5f, __fadd_rn(1.f, th));
+  const float valx = __fmul_rn(__fmul_rn(__fmul_rn(w, 0.5f), uxs), dxdy);
+  const float valy = __fmul_rn(__fmul_rn(__fmul_rn(w, 0.5f), uys), dxdy);
+  s0 = __fmaf_rn(valx, rpm, s0);
+  s1 = __fmaf_rn(valy, rpm, s1);
+  s2 = __fmaf_rn(__fmaf_rn(X, valy, __fmul_rn(-Y, valx)), rpim, s2);
+}
+
 // one warp per row task, single precision (see ibm_work_tasks)
 template <bool NC>
 __device__ __forceinline__ void ibm_work_f_tasks(const WorkArgs &a, int wmode, int first, int stride, float2 *slots) {
   const int lane = threadIdx.x & 31;
-  const int total = EIF_CHK(a.bd.rec, a.np, a.bd.off, 50) ? ldro<NC>(a.off + a.np) : 0;
+  // all tasks, or (with a.only) the listed ones: task number c of list entry k
+  const int total = a.only ? (int)min((long long)ldro<NC>(a.only), (long long)(a.bd.partial / 3))
+                           : (EIF_CHK(a.bd.rec, a.np, a.bd.off, 50) ? ldro<NC>(a.off + a.np) : 0);
+  auto task_no = [&](int k) { return a.only ? ldro<NC>(a.only + 1 + k) : k; };
   const float rh = a.rh_f, dxf = a.dx_f, dyf = a.dy_f, dxdy = a.dxdy_f;
   const float rdtv = a.mode == 1 ? __ldg(a.coef + 9) : 0.f;
   const int ld = a.ld;
@@ -665,10 +687,17 @@ __device__ __forceinline__ void ibm_work_f_tasks(const WorkArgs &a, int wmode, i
   float *wcache = static_cast<float *>(a.wcache);
   // the next task's table entry is loaded while the current task is processed
   int4 nxt = make_int4(-1, 0, 0, 0);
-  if (first < total && EIF_CHK(a.bd.rec, first, a.bd.partial / 3, 51)) nxt = ldro<NC>(a.tdesc + first);
-  for (int c = first; c < total; c += stride) {
+  if (first < total) {
+    const int cf = task_no(first);
+    if (EIF_CHK(a.bd.rec, cf, a.bd.partial / 3, 51)) nxt = ldro<NC>(a.tdesc + cf);
+  }
+  for (int k = first; k < total; k += stride) {
+    const int c = task_no(k);
     const int4 dsc = nxt;
-    if (c + stride < total && EIF_CHK(a.bd.rec, c + stride, a.bd.partial / 3, 51)) nxt = ldro<NC>(a.tdesc + c + stride);
+    if (k + stride < total) {
+      const int cn = task_no(k + stride);
+      if (EIF_CHK(a.bd.rec, cn, a.bd.partial / 3, 51)) nxt = ldro<NC>(a.tdesc + cn);
+    }
     const int n = dsc.x;
     if (!EIF_CHK(a.bd.rec, n, a.np, 52)) continue;
     RowTask t;
@@ -809,12 +838,7 @@ __device__ __forceinline__ void ibm_work_f_tasks(const WorkArgs &a, int wmode, i
         const float uxs = fuw[half] + fue[half];
         const float uys = fvs[half] + fvn[half];
         if (a.mode == 0) {
-          const float w = 0.5f * (1.f + th);
-          const float valx = w * 0.5f * uxs * dxdy;
-          const float valy = w * 0.5f * uys * dxdy;
-          sacc0 += valx * rpm;
-          sacc1 += valy * rpm;
-          sacc2 += (-Y * valx + X * valy) * rpim;
+          inertia_cell_f(th, X, Y, uxs, uys, dxdy, rpm, rpim, sacc0, sacc1, sacc2);
         } else {
           const float w = 1.f - th * th;
           const float uxp = pux - pvz * Y;
@@ -839,6 +863,106 @@ __device__ __forceinline__ void ibm_work_f_tasks(const WorkArgs &a, int wmode, i
     }
     if (lane == 0 && EIF_CHK(a.bd.rec, 3LL * c + 2, a.bd.partial, 58)) {
       // single-precision partial sums, reduced per particle by k_chunk_reduce_f
+      float *pf3 = reinterpret_cast<float *>(a.partial);
+      pf3[3 * (size_t)c + 0] = sacc0;
+      pf3[3 * (size_t)c + 1] = sacc1;
+      pf3[3 * (size_t)c + 2] = sacc2;
+    }
+  }
+}
+
+// The stage start of the mixed form (inertia at X with zero increments, weights stored for
+// the stage: wmode 1, memo_mode 1 of ibm_work_f_tasks) without the geometry code: a task
+// whose particle geometry words and boxes are bitwise those of the memo takes the memo's
+// weights, stores them in wcache and forms its sums exactly as ibm_work_f_tasks does;
+// any other task is appended to a.miss for k_ibm_work_f, which evaluates those in full.
+// It runs with the registers of the sums kernel, so more warps hide its loads.
+template <bool NC>
+__device__ __forceinline__ void ibm_memo_f_tasks(const WorkArgs &a, int first, int stride) {
+  const int lane = threadIdx.x & 31;
+  const int total = EIF_CHK(a.bd.rec, a.np, a.bd.off, 90) ? ldro<NC>(a.off + a.np) : 0;
+  const float dxf = a.dx_f, dyf = a.dy_f, dxdy = a.dxdy_f;
+  const int ld = a.ld;
+  float *wcache = static_cast<float *>(a.wcache);
+  const bool valid = ldro<NC>(a.memo.valid) != 0;
+  for (int c = first; c < total; c += stride) {
+    if (!EIF_CHK(a.bd.rec, c, a.bd.partial / 3, 91)) continue;
+    const int4 dsc = ldro<NC>(a.tdesc + c);
+    const int n = dsc.x;
+    if (!EIF_CHK(a.bd.rec, n, a.np, 92)) continue;
+    bool eq = false;
+    if (valid) {
+      if (lane < 20) {
+        const size_t q = (size_t)PF_WORDS * n + memo_word(lane);
+        eq = __float_as_uint(ldro<NC>(a.pf + q)) == __float_as_uint(ldro<NC>(a.memo.pf + q));
+      } else {
+        const size_t q = 12 * (size_t)n + (lane - 20);
+        eq = ldro<NC>(a.box + q) == ldro<NC>(a.memo.box + q);
+      }
+    }
+    if (!__all_sync(0xffffffffu, eq)) {
+      if (lane == 0) {
+        const int k = atomicAdd(a.miss, 1);
+        if (EIF_CHK(a.bd.rec, k, a.bd.partial / 3, 93)) a.miss[1 + k] = c;
+      }
+      continue;
+    }
+    if (a.count && lane == 0) atomicAdd(a.count + 2, 1ull);
+    const long long src = (long long)c + (ldro<NC>(a.memo.off + n) - ldro<NC>(a.off + n));
+    RowTask t;
+    const bool task = task_of(dsc, a.np, t);
+    const float4 *q4 = reinterpret_cast<const float4 *>(a.pf + (size_t)PF_WORDS * n);
+    const float4 qB = ldro<NC>(q4 + 1), qC = ldro<NC>(q4 + 2), qD = ldro<NC>(q4 + 3), qE = ldro<NC>(q4 + 4);
+    const float rpm = qB.z, rpim = qB.w, gx = qC.w;
+    const int i0 = __float_as_int(qD.x);
+    const int m = task ? t.img + 1 : 1;
+    const int j0i = __float_as_int(m == 0 ? qD.y : (m == 1 ? qD.z : qD.w));
+    const float gyi = m == 0 ? qE.x : (m == 1 ? qE.y : qE.z);
+    const int j = task ? t.j : 1;
+    const float Y = ((float)(j - j0i) - gyi) * dyf;
+    bool cin[2];
+    float cX[2], th2[2], fuw[2], fue[2], fvs[2], fvn[2];
+#pragma unroll
+    for (int half = 0; half < CHUNK / 32; half++) {
+      const int i = (task ? t.ib : 1) + half * 32 + lane;
+      bool in = task && i <= t.ie;
+      if (in) {
+        in = EIF_CHK(a.bd.rec, j * ld + i, a.bd.field, 94) && EIF_CHK(a.bd.rec, (j + 1) * ld + i, a.bd.field, 95) &&
+             EIF_CHK(a.bd.rec, j * ld + (i - 1), a.bd.field, 96);
+      }
+      fuw[half] = fue[half] = fvs[half] = fvn[half] = 0.f;
+      if (in) {
+        fuw[half] = __ldg(a.uxf + j * ld + (i - 1));
+        fue[half] = __ldg(a.uxf + j * ld + i);
+        fvs[half] = __ldg(a.uyf + j * ld + i);
+        fvn[half] = __ldg(a.uyf + (j + 1) * ld + i);
+      }
+      if (in) in = EIF_CHK(a.bd.rec, src * CHUNK + half * 32 + lane, a.bd.wbuf, 97);
+      cin[half] = in;
+      cX[half] = ((float)(i - i0) - gx) * dxf;
+      th2[half] = in ? a.memo.w[(size_t)src * CHUNK + half * 32 + lane] : 0.f;
+    }
+#pragma unroll
+    for (int half = 0; half < CHUNK / 32; half++)
+      if (EIF_CHK(a.bd.rec, (long long)c * CHUNK + half * 32 + lane, 2 * a.bd.wbuf, 98))
+        wcache[(size_t)c * CHUNK + half * 32 + lane] = th2[half];
+    float sacc0 = 0.f, sacc1 = 0.f, sacc2 = 0.f;
+#pragma unroll
+    for (int half = 0; half < CHUNK / 32; half++) {
+      const float th_ = th2[half];
+      if (cin[half] && th_ != -1.f) {
+        const float uxs = fuw[half] + fue[half];
+        const float uys = fvs[half] + fvn[half];
+        inertia_cell_f(th_, cX[half], Y, uxs, uys, dxdy, rpm, rpim, sacc0, sacc1, sacc2);
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      sacc0 += __shfl_xor_sync(0xffffffffu, sacc0, o);
+      sacc1 += __shfl_xor_sync(0xffffffffu, sacc1, o);
+      sacc2 += __shfl_xor_sync(0xffffffffu, sacc2, o);
+    }
+    if (lane == 0 && EIF_CHK(a.bd.rec, 3LL * c + 2, a.bd.partial, 99)) {
       float *pf3 = reinterpret_cast<float *>(a.partial);
       pf3[3 * (size_t)c + 0] = sacc0;
       pf3[3 * (size_t)c + 1] = sacc1;
@@ -931,12 +1055,7 @@ __device__ __forceinline__ void ibm_sum_f_tasks(const WorkArgs &a, int first, in
         const float uxs = uw[half] + ue[half];
         const float uys = vs[half] + vn[half];
         if (a.mode == 0) {
-          const float w = 0.5f * (1.f + th);
-          const float valx = w * 0.5f * uxs * dxdy;
-          const float valy = w * 0.5f * uys * dxdy;
-          sacc0 += valx * rpm;
-          sacc1 += valy * rpm;
-          sacc2 += (-Y * valx + X * valy) * rpim;
+          inertia_cell_f(th, X, Y, uxs, uys, dxdy, rpm, rpim, sacc0, sacc1, sacc2);
         } else {
           const float w = 1.f - th * th;
           const float uxp = pux - pvz * Y;
@@ -1112,6 +1231,8 @@ inline WorkArgs work_args(const eif_ctx *c, int mode, int cn) {
   w.count = nullptr;
   w.memo = memo_of(c);
   w.memo_mode = 0;
+  w.miss = nullptr;
+  w.only = nullptr;
   return w;
 }
 
