@@ -120,15 +120,16 @@ def test_mixed_predictor_matches_fp64(builder, gpu_lib):
     lambda: cases.poiseuille(itot=32, jtot=64, n=1, a=0.2, b=0.1, seed=2),
     lambda: cases.poiseuille(itot=1024, jtot=2048, n=16, a=0.02, b=0.01, seed=5),
     lambda: cases.poiseuille(itot=2048, jtot=4096, n=32, a=0.012, b=0.006, seed=3),
+    lambda: cases.poiseuille(itot=128, jtot=256, n=4, a=0.06, b=0.03, seed=7),
 ], ids=["couette_circle", "poiseuille_384x768", "poiseuille_256x512", "poiseuille_32x64", "poiseuille_1024x2048",
-        "poiseuille_2048x4096"])
+        "poiseuille_2048x4096", "poiseuille_128x256"])
 def test_mixed_poisson_matches_fp64(builder, gpu_lib):
     """The mixed form's Poisson solve agrees with the double-precision form's to 1e-10
     relative in psi and in the projected velocity. The half lengths m = itot/2 cover
-    the refined single-precision solve (register-radix, radix-8, transforms) with a
-    last pass of radix 2 (m = 16, 128, 1024) and 4 (m = 32), and the double-float
-    radix-4/2/3 transform of the other lengths (m = 192); m = 512 (no last pass) runs
-    in the step test."""
+    the refined single-precision solve (register-radix, radix-8, transforms, one
+    instance per m) with a last pass of radix 2 (m = 16, 128, 1024), of radix 4
+    (m = 32) and without one (m = 64, 512), and the double-float radix-4/2/3 transform
+    of the other lengths (m = 192)."""
     from conftest import interior_p
     case = builder()
     d, m = pair(case)
