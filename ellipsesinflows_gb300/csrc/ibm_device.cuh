@@ -441,8 +441,9 @@ struct WorkArgs {
   // normal-foot iteration, added to count[0] and count[1], and the tasks whose weights
   // come from the memo, added to count[2] (null: not counted)
   unsigned long long *count;
-  // mixed form: memo_mode 1 takes the weights of a task from the memo when its
-  // particle's geometry and boxes are the memo's; 2 stores computed weights in it
+  // mixed form: memo_mode 1 (the stage start, ibm_memo_f_tasks) takes the weights of a
+  // task from the memo when its particle's geometry and boxes are the memo's; 2
+  // (ibm_work_f_tasks in the loops) stores computed weights in it
   WeightMemo memo;
   int memo_mode;
   // the stage start of the mixed form (ibm_memo_f_tasks): miss[0] counts the tasks the
@@ -740,34 +741,16 @@ __device__ __forceinline__ void ibm_work_f_tasks(const WorkArgs &a, int wmode, i
         fvn[half] = __ldg(a.uyf + (j + 1) * ld + i);
       }
     }
-    // the memo's weights for this task when the particle's geometry words and boxes are
-    // bitwise those of the stored evaluation (its tasks are then the same rows, shifted
-    // by the difference of the first tasks)
-    bool reuse = false;
-    long long src = c;
-    if (a.memo_mode == 1 && ldro<NC>(a.memo.valid) != 0) {
-      bool eq;
-      if (lane < 20) {
-        const size_t q = (size_t)PF_WORDS * n + memo_word(lane);
-        eq = __float_as_uint(ldro<NC>(a.pf + q)) == __float_as_uint(ldro<NC>(a.memo.pf + q));
-      } else {
-        const size_t q = 12 * (size_t)n + (lane - 20);
-        eq = ldro<NC>(a.box + q) == ldro<NC>(a.memo.box + q);
-      }
-      reuse = __all_sync(0xffffffffu, eq);
-      if (reuse) src = (long long)c + (ldro<NC>(a.memo.off + n) - ldro<NC>(a.off + n));
-      if (reuse && a.count && lane == 0) atomicAdd(a.count + 2, 1ull);
-    }
-    if (wmode == 2 || reuse) {
+    // (the stage start's weights from the memo are taken by ibm_memo_f_tasks, which
+    // leaves this body only the tasks the memo did not serve)
+    if (wmode == 2) {
       // weights of the same geometry from an earlier evaluation
-      const float *wsrc = reuse ? a.memo.w : wcache;
-      const long long bound = reuse ? a.bd.wbuf : 2 * a.bd.wbuf;
 #pragma unroll
       for (int half = 0; half < CHUNK / 32; half++) {
         const int i = (task ? t.ib : 1) + half * 32 + lane;
-        if (cin[half]) cin[half] = EIF_CHK(a.bd.rec, src * CHUNK + half * 32 + lane, bound, 59);
+        if (cin[half]) cin[half] = EIF_CHK(a.bd.rec, (long long)c * CHUNK + half * 32 + lane, 2 * a.bd.wbuf, 59);
         cX[half] = ((float)(i - i0) - gx) * dxf;
-        th2[half] = cin[half] ? wsrc[(size_t)src * CHUNK + half * 32 + lane] : 0.f;
+        th2[half] = cin[half] ? wcache[(size_t)c * CHUNK + half * 32 + lane] : 0.f;
       }
     } else {
     // far cells of this row (PF_AL .. PF_RO2: al, ka, de, so^2, si^2, ro^2)
